@@ -1,0 +1,1154 @@
+// enb_api.cu -- C ABI of the GB300 enblend/enfuse path: context, pyramid
+// handles, primitive entry points and the enfuse/enblend drivers (host C++).
+#include <cuda_runtime.h>
+
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "enb_internal.h"
+#include "enbgpu.h"
+
+using namespace enb;
+
+struct enb_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    uint64_t launches = 0;
+    // cached enfuse weight tables
+    std::string table_key;
+    void* table_mem = nullptr;
+    WeightTables tables{};
+};
+
+struct enb_pyramid {
+    int levels = 0;
+    int C = 0;
+    int dtype = ENB_I32;
+    int w[kMaxLevels + 1] = {};
+    int h[kMaxLevels + 1] = {};
+    int64_t pitch[kMaxLevels + 1] = {};  // elements
+    int64_t offset[kMaxLevels + 1] = {}; // bytes from base
+    void* base = nullptr;
+    size_t bytes = 0;
+};
+
+namespace {
+
+size_t dtype_size(int dt)
+{
+    switch (dt) {
+    case ENB_U8: return 1;
+    case ENB_U16: return 2;
+    case ENB_I16: return 2;
+    case ENB_F32: return 4;
+    case ENB_I32: return 4;
+    default: return 0;
+    }
+}
+
+enb_status fail(enb_ctx* ctx, enb_status st, const std::string& msg)
+{
+    if (ctx) {
+        ctx->err = msg;
+    }
+    return st;
+}
+
+enb_status cuda_fail(enb_ctx* ctx, cudaError_t e, const char* where)
+{
+    return fail(ctx, ENB_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define ENB_LAUNCH(ctx, call)                                  \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        (ctx)->launches++;                                     \
+        if (e_ != cudaSuccess) {                               \
+            return cuda_fail((ctx), e_, #call);                \
+        }                                                      \
+    } while (0)
+
+#define ENB_CUDA(ctx, call)                                    \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess) {                               \
+            return cuda_fail((ctx), e_, #call);                \
+        }                                                      \
+    } while (0)
+
+#define ENB_CHECK(ctx, cond, msg)                              \
+    do {                                                       \
+        if (!(cond)) {                                         \
+            return fail((ctx), ENB_ERR_INVALID, (msg));        \
+        }                                                      \
+    } while (0)
+
+#define ENB_TRY(call)                                          \
+    do {                                                       \
+        enb_status s_ = (call);                                \
+        if (s_ != ENB_OK) {                                    \
+            return s_;                                         \
+        }                                                      \
+    } while (0)
+
+// Stream-ordered device allocation freed on scope exit.
+struct DevBuf {
+    void* p = nullptr;
+    cudaStream_t st = nullptr;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf()
+    {
+        if (p) {
+            cudaFreeAsync(p, st);
+        }
+    }
+    cudaError_t alloc(size_t bytes, cudaStream_t s)
+    {
+        st = s;
+        return cudaMallocAsync(&p, bytes == 0 ? 1 : bytes, s);
+    }
+};
+
+int64_t round_up(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
+
+// ---- descriptor -> view conversions ------------------------------------
+
+bool planar_ok(const enb_image* im)
+{
+    return im && im->data && im->planar && (im->dtype == ENB_I16 || im->dtype == ENB_I32) && im->width > 0 &&
+           im->height > 0 && im->channels >= 1 && im->pitch % (int64_t)dtype_size(im->dtype) == 0 &&
+           im->plane_pitch % (int64_t)dtype_size(im->dtype) == 0 && im->pitch >= im->width * (int64_t)dtype_size(im->dtype);
+}
+
+PlanarView planar_view(const enb_image* im)
+{
+    const int64_t es = (int64_t)dtype_size(im->dtype);
+    return PlanarView{im->data, im->pitch / es, im->plane_pitch / es, im->width, im->height, im->channels, im->dtype};
+}
+
+bool pixels_ok(const enb_image* im)
+{
+    if (!im || !im->data || im->planar || (im->dtype != ENB_U8 && im->dtype != ENB_U16) || im->width <= 0 ||
+        im->height <= 0) {
+        return false;
+    }
+    if (im->channels != 1 && im->channels != 3) {
+        return false;
+    }
+    const int stride = im->pix_stride > 0 ? im->pix_stride : im->channels;
+    return stride >= im->channels && stride <= 4 && im->pitch % (int64_t)dtype_size(im->dtype) == 0 &&
+           im->pitch >= (int64_t)im->width * stride * (int64_t)dtype_size(im->dtype);
+}
+
+PixelView pixel_view(const enb_image* im)
+{
+    const int64_t es = (int64_t)dtype_size(im->dtype);
+    const int stride = im->pix_stride > 0 ? im->pix_stride : im->channels;
+    return PixelView{im->data, im->pitch / es, im->width, im->height, im->channels, stride, im->dtype};
+}
+
+bool bytes_ok(const enb_image* im, int w, int h)
+{
+    return im && im->data && im->dtype == ENB_U8 && im->width == w && im->height == h && im->pitch >= w;
+}
+
+BytePlane byte_plane(const enb_image* im)
+{
+    return BytePlane{(uint8_t*)im->data, im->pitch, im->width, im->height};
+}
+
+bool floats_ok(const enb_image* im, int w, int h)
+{
+    return im && im->data && im->dtype == ENB_F32 && im->width == w && im->height == h && im->pitch % 4 == 0 &&
+           im->pitch >= (int64_t)w * 4;
+}
+
+FloatPlane float_plane(const enb_image* im) { return FloatPlane{(float*)im->data, im->pitch / 4, im->width, im->height}; }
+
+PlanarView level_view(const enb_pyramid* p, int l)
+{
+    return PlanarView{(char*)p->base + p->offset[l], p->pitch[l], p->pitch[l] * p->h[l], p->w[l], p->h[l], p->C,
+                      p->dtype};
+}
+
+// Alpha source of an interleaved image: explicit plane, thresholded 4th
+// component (src/assemble.h:240-253: Threshold(max/2, max) -> 0/255), or opaque.
+AlphaSrc alpha_source(const enb_image* img, const enb_image* alpha)
+{
+    AlphaSrc a{};
+    if (alpha && alpha->data) {
+        a.mode = kAlphaPlane;
+        a.plane = byte_plane(alpha);
+    } else if (img->pix_stride == 4) {
+        a.mode = kAlphaChannel3;
+        a.pix = pixel_view(img);
+        const uint32_t maxv = img->dtype == ENB_U8 ? 255u : 65535u;
+        a.lo = (uint32_t)(maxv / 2.0);  // static_cast of range.second / 2.0
+        a.hi = maxv;
+    } else {
+        a.mode = kAlphaOpaque;
+    }
+    return a;
+}
+
+// ---- pyramids -------------------------------------------------------------
+
+enb_status pyramid_alloc(enb_ctx* ctx, int levels, int w, int h, int C, int dtype, enb_pyramid** out)
+{
+    ENB_CHECK(ctx, levels >= 1 && levels <= kMaxLevels, "pyramid: levels outside 1..29");
+    ENB_CHECK(ctx, w > 0 && h > 0 && (C == 1 || C == 3), "pyramid: bad size or channel count");
+    ENB_CHECK(ctx, dtype == ENB_I16 || dtype == ENB_I32, "pyramid: dtype must be ENB_I16 or ENB_I32");
+    std::unique_ptr<enb_pyramid> p(new enb_pyramid());
+    p->levels = levels;
+    p->C = C;
+    p->dtype = dtype;
+    const int64_t es = (int64_t)dtype_size(dtype);
+    int64_t off = 0;
+    int lw = w, lh = h;
+    for (int l = 0; l < levels; ++l) {
+        p->w[l] = lw;
+        p->h[l] = lh;
+        p->pitch[l] = round_up(lw, 128 / es);  // 128-byte aligned rows
+        p->offset[l] = off;
+        off += round_up(p->pitch[l] * lh * C * es, 256);
+        lw = (lw + 1) >> 1;
+        lh = (lh + 1) >> 1;
+    }
+    p->bytes = (size_t)off;
+    cudaError_t e = cudaMallocAsync(&p->base, p->bytes, ctx->stream);
+    if (e != cudaSuccess) {
+        return fail(ctx, ENB_ERR_NOMEM, std::string("pyramid allocation: ") + cudaGetErrorString(e));
+    }
+    *out = p.release();
+    return ENB_OK;
+}
+
+void pyramid_release(enb_ctx* ctx, enb_pyramid* p)
+{
+    if (p) {
+        if (p->base) {
+            cudaFreeAsync(p->base, ctx->stream);
+        }
+        delete p;
+    }
+}
+
+struct PyrHolder {
+    enb_ctx* ctx;
+    enb_pyramid* p = nullptr;
+    explicit PyrHolder(enb_ctx* c) : ctx(c) {}
+    ~PyrHolder() { pyramid_release(ctx, p); }
+};
+
+// Alpha planes of levels 1..L-1 (level l at offset[l]); level 0 is the source alpha.
+struct AlphaChain {
+    DevBuf mem;
+    int64_t pitch[kMaxLevels + 1] = {};
+    int64_t offset[kMaxLevels + 1] = {};
+    int w[kMaxLevels + 1] = {}, h[kMaxLevels + 1] = {};
+    cudaError_t alloc(int levels, int w0, int h0, cudaStream_t st)
+    {
+        int64_t off = 0;
+        int lw = w0, lh = h0;
+        for (int l = 0; l < levels; ++l) {
+            w[l] = lw;
+            h[l] = lh;
+            pitch[l] = round_up(lw, 128);
+            offset[l] = off;
+            off += round_up(pitch[l] * lh, 256);
+            lw = (lw + 1) >> 1;
+            lh = (lh + 1) >> 1;
+        }
+        return mem.alloc((size_t)off, st);
+    }
+    BytePlane level(int l) { return BytePlane{(uint8_t*)mem.p + offset[l], pitch[l], w[l], h[l]}; }
+};
+
+// Reduce chain of a pyramid whose level 0 is filled (gaussianPyramid,
+// src/pyramid.h:1500-1530 with alpha, :1590-1610 without).
+enb_status gaussian_levels(enb_ctx* ctx, int wrap, enb_pyramid* p, const BytePlane* alpha0)
+{
+    if (p->levels <= 1) {
+        return ENB_OK;
+    }
+    if (!alpha0) {
+        for (int l = 1; l < p->levels; ++l) {
+            ENB_CHECK(ctx, p->w[l - 1] > 1 && p->h[l - 1] > 1, "reduce: src image too small in reduce");
+            ENB_LAUNCH(ctx, launch_reduce(wrap, level_view(p, l - 1), nullptr, level_view(p, l), nullptr, ctx->stream));
+        }
+        return ENB_OK;
+    }
+    AlphaChain ac;
+    ENB_CUDA(ctx, ac.alloc(p->levels, p->w[0], p->h[0], ctx->stream));
+    for (int l = 1; l < p->levels; ++l) {
+        ENB_CHECK(ctx, p->w[l - 1] > 1 && p->h[l - 1] > 1, "reduce: src image too small in reduce");
+        const BytePlane src_a = l == 1 ? *alpha0 : ac.level(l - 1);
+        const BytePlane dst_a = ac.level(l);
+        ENB_LAUNCH(ctx, launch_reduce(wrap, level_view(p, l - 1), &src_a, level_view(p, l), &dst_a, ctx->stream));
+    }
+    return ENB_OK;
+}
+
+enb_status laplacian_levels(enb_ctx* ctx, int wrap, enb_pyramid* p)
+{
+    for (int l = 0; l + 1 < p->levels; ++l) {
+        ENB_LAUNCH(ctx, launch_expand(0, wrap, level_view(p, l + 1), level_view(p, l), ctx->stream));
+    }
+    return ENB_OK;
+}
+
+enb_status collapse_levels(enb_ctx* ctx, int wrap, enb_pyramid* p)
+{
+    for (int l = p->levels - 2; l >= 0; --l) {
+        ENB_LAUNCH(ctx, launch_expand(1, wrap, level_view(p, l + 1), level_view(p, l), ctx->stream));
+    }
+    return ENB_OK;
+}
+
+// ---- enfuse weight tables --------------------------------------------------
+
+constexpr double kFwhmGaussian = 2.3548200450309493820231386529193992755;
+constexpr double kFwhmLorentzian = 2.8284271247461900976033774484193961571;
+constexpr double kFwhmHalfSine = 2.0943951023931954923084289221863352561;
+constexpr double kFwhmFullSine = 3.14159265358979323846;
+constexpr double kFwhmBisquare = 1.6817928305074290860622509524664297901;
+
+// Built-in exposure weight functions of src/exposure_weight.h:44-128, each
+// with its width rescaled to the Gaussian's FWHM.
+double exposure_fn(int fn, double y, double opt, double width)
+{
+    double wd = width;
+    switch (fn) {
+    case ENB_EXP_LORENTZIAN: wd = width * kFwhmGaussian / kFwhmLorentzian; break;
+    case ENB_EXP_HALF_SINE: wd = width * kFwhmGaussian / kFwhmHalfSine; break;
+    case ENB_EXP_FULL_SINE: wd = width * kFwhmGaussian / kFwhmFullSine; break;
+    case ENB_EXP_BISQUARE: wd = width * kFwhmGaussian / kFwhmBisquare; break;
+    default: break;
+    }
+    const double z = (y - opt) / wd;
+    switch (fn) {
+    case ENB_EXP_LORENTZIAN: return 1.0 / (1.0 + 0.5 * z * z);
+    case ENB_EXP_HALF_SINE: return fabs(z) <= 1.57079632679489661923 ? cos(z) : 0.0;
+    case ENB_EXP_FULL_SINE: return fabs(z) <= 3.14159265358979323846 ? 0.5 + cos(z) / 2.0 : 0.0;
+    case ENB_EXP_BISQUARE: {
+        if (fabs(z) <= 1.0) {
+            const double z2 = z * z;
+            return (1.0 - z2) * (1.0 + z2);
+        }
+        return 0.0;
+    }
+    default: return exp(-0.5 * z * z);
+    }
+}
+
+enb_status build_tables(enb_ctx* ctx, const enb_enfuse_params* prm, uint32_t maxv)
+{
+    char key[512];
+    snprintf(key, sizeof key, "%u|%.17g|%.17g|%.17g|%.17g|%.17g|%.17g|%d|%d", maxv, prm->w_exposure,
+             prm->w_contrast, prm->w_entropy, prm->w_saturation, prm->exp_optimum, prm->exp_width, prm->exp_function,
+             prm->entropy_window);
+    if (ctx->table_mem && ctx->table_key == key) {
+        return ENB_OK;
+    }
+    const int n = (int)maxv + 1;
+    const int nmax = prm->entropy_window * prm->entropy_window;
+    const int nt = (nmax + 1) * (nmax + 1);
+    std::vector<float> exposure(n), contrast(n), entropy(n);
+    for (int g = 0; g < n; ++g) {
+        const double y = (double)g / (double)maxv;
+        exposure[g] = (float)(prm->w_exposure * exposure_fn(prm->exp_function, y, prm->exp_optimum, prm->exp_width));
+        contrast[g] = (float)(prm->w_contrast * (double)g / (double)maxv);
+        entropy[g] = (float)(prm->w_entropy * (double)(float)g);
+    }
+    std::vector<double> plogp(nt, 0.0), logb(nmax + 1, 0.0);
+    std::vector<long long> plogp_fx(nt, 0);
+    std::vector<float> scale_logb(nmax + 1, 0.0f);
+    for (int tot = 1; tot <= nmax; ++tot) {
+        for (int c = 1; c <= tot; ++c) {
+            const double p = (double)c / (double)tot;
+            const double v = p * log(p);
+            plogp[(size_t)tot * (nmax + 1) + c] = v;
+            plogp_fx[(size_t)tot * (nmax + 1) + c] = llround(v * 72057594037927936.0);  // 2^56
+        }
+    }
+    for (int b = 1; b <= nmax; ++b) {
+        logb[b] = log((double)b);
+        scale_logb[b] = b >= 2 ? (float)((double)maxv / logb[b]) : 0.0f;
+    }
+    const size_t sz_f = (size_t)n * 4, sz_pl = (size_t)nt * 8, sz_lb = (size_t)(nmax + 1) * 8,
+                 sz_sl = (size_t)(nmax + 1) * 4;
+    const size_t o_exp = 0, o_con = round_up((int64_t)(o_exp + sz_f), 256), o_ent = round_up((int64_t)(o_con + sz_f), 256),
+                 o_pl = round_up((int64_t)(o_ent + sz_f), 256), o_fx = round_up((int64_t)(o_pl + sz_pl), 256),
+                 o_lb = round_up((int64_t)(o_fx + sz_pl), 256), o_sl = round_up((int64_t)(o_lb + sz_lb), 256),
+                 total = round_up((int64_t)(o_sl + sz_sl), 256);
+    if (ctx->table_mem) {
+        cudaFreeAsync(ctx->table_mem, ctx->stream);
+        ctx->table_mem = nullptr;
+    }
+    ENB_CUDA(ctx, cudaMallocAsync(&ctx->table_mem, total, ctx->stream));
+    char* b = (char*)ctx->table_mem;
+    ENB_CUDA(ctx, cudaMemcpyAsync(b + o_exp, exposure.data(), sz_f, cudaMemcpyHostToDevice, ctx->stream));
+    ENB_CUDA(ctx, cudaMemcpyAsync(b + o_con, contrast.data(), sz_f, cudaMemcpyHostToDevice, ctx->stream));
+    ENB_CUDA(ctx, cudaMemcpyAsync(b + o_ent, entropy.data(), sz_f, cudaMemcpyHostToDevice, ctx->stream));
+    ENB_CUDA(ctx, cudaMemcpyAsync(b + o_pl, plogp.data(), sz_pl, cudaMemcpyHostToDevice, ctx->stream));
+    ENB_CUDA(ctx, cudaMemcpyAsync(b + o_fx, plogp_fx.data(), sz_pl, cudaMemcpyHostToDevice, ctx->stream));
+    ENB_CUDA(ctx, cudaMemcpyAsync(b + o_lb, logb.data(), sz_lb, cudaMemcpyHostToDevice, ctx->stream));
+    ENB_CUDA(ctx, cudaMemcpyAsync(b + o_sl, scale_logb.data(), sz_sl, cudaMemcpyHostToDevice, ctx->stream));
+    // pageable sources: make sure the copies consumed them before the vectors go
+    ENB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->tables = WeightTables{(const float*)(b + o_exp), (const float*)(b + o_con), (const float*)(b + o_ent),
+                               (const double*)(b + o_pl), (const long long*)(b + o_fx), (const double*)(b + o_lb),
+                               (const float*)(b + o_sl)};
+    ctx->table_key = key;
+    return ENB_OK;
+}
+
+enb_status check_params(enb_ctx* ctx, const enb_enfuse_params* p, int w, int h)
+{
+    ENB_CHECK(ctx, p, "enfuse params: NULL");
+    ENB_CHECK(ctx, p->exp_optimum >= 0.0 && p->exp_optimum <= 1.0, "exposure optimum outside [0, 1]");
+    ENB_CHECK(ctx, p->exp_width > 0.0, "exposure width must be positive");
+    ENB_CHECK(ctx, p->exp_function >= ENB_EXP_GAUSSIAN && p->exp_function <= ENB_EXP_BISQUARE,
+              "unknown exposure weight function");
+    ENB_CHECK(ctx, p->gray_projector >= ENB_GRAY_AVERAGE && p->gray_projector <= ENB_GRAY_MIXER,
+              "unknown grayscale projector");
+    if (p->w_contrast > 0.0) {
+        ENB_CHECK(ctx, p->contrast_window >= 3 && (p->contrast_window & 1) && p->contrast_window <= kMaxContrastWindow,
+                  "contrast window must be odd, 3..31");
+        ENB_CHECK(ctx, w >= p->contrast_window && h >= p->contrast_window, "localStdDevIf(): window larger than image");
+    }
+    if (p->w_entropy > 0.0) {
+        ENB_CHECK(ctx, p->entropy_window >= 3 && (p->entropy_window & 1) && p->entropy_window <= kMaxEntropyWindow,
+                  "entropy window must be odd, 3..15");
+        ENB_CHECK(ctx, w >= p->entropy_window && h >= p->entropy_window, "localEntropyIf(): window larger than image");
+    }
+    if (p->gray_projector == ENB_GRAY_MIXER) {
+        ENB_CHECK(ctx, p->mixer[0] >= 0 && p->mixer[1] >= 0 && p->mixer[2] >= 0 &&
+                           p->mixer[0] + p->mixer[1] + p->mixer[2] != 0.0,
+                  "channel-mixer weights must be non-negative with a non-zero sum");
+    }
+    return ENB_OK;
+}
+
+enb_status enfuse_mask_impl(enb_ctx* ctx, const enb_enfuse_params* prm, const enb_image* src,
+                            const enb_image* alpha, const FloatPlane& out)
+{
+    const uint32_t maxv = src->dtype == ENB_U8 ? 255u : 65535u;
+    ENB_TRY(build_tables(ctx, prm, maxv));
+    WeightParams wp{};
+    wp.use_exposure = prm->w_exposure > 0.0;
+    wp.use_contrast = prm->w_contrast > 0.0;
+    wp.use_saturation = prm->w_saturation > 0.0;
+    wp.use_entropy = prm->w_entropy > 0.0;
+    wp.contrast_window = prm->contrast_window;
+    wp.entropy_window = prm->entropy_window;
+    wp.gray_projector = prm->gray_projector;
+    if (prm->gray_projector == ENB_GRAY_MIXER) {
+        const double s = prm->mixer[0] + prm->mixer[1] + prm->mixer[2];
+        wp.mixer[0] = prm->mixer[0] / s;
+        wp.mixer[1] = prm->mixer[1] / s;
+        wp.mixer[2] = prm->mixer[2] / s;
+    }
+    wp.w_saturation = prm->w_saturation;
+    wp.w_sat_hi = (float)prm->w_saturation;
+    wp.w_sat_lo = (float)(prm->w_saturation - (double)wp.w_sat_hi);
+    wp.maxv = maxv;
+    ENB_LAUNCH(ctx, launch_enfuse_mask(pixel_view(src), alpha_source(src, alpha), wp, ctx->tables, out, ctx->stream));
+    return ENB_OK;
+}
+
+int fixed_bits_image(int dt) { return dt == ENB_U8 ? ENB_I16 : ENB_I32; }
+int fixed_bits_mask(int dt) { return dt == ENB_U8 ? ENB_I16 : ENB_I32; }
+int mask_frac(int dt) { return dt == ENB_U8 ? 7 : 15; }
+constexpr int kImageFrac = 7;
+
+// Materialise the alpha of an interleaved image as a U8 plane.
+enb_status alpha_plane(enb_ctx* ctx, const enb_image* img, const enb_image* alpha, DevBuf& buf, BytePlane& out)
+{
+    if (alpha && alpha->data) {
+        ENB_CHECK(ctx, bytes_ok(alpha, img->width, img->height), "alpha plane: must be U8 of the image size");
+        out = byte_plane(alpha);
+        return ENB_OK;
+    }
+    const int64_t pitch = round_up(img->width, 128);
+    ENB_CUDA(ctx, buf.alloc((size_t)(pitch * img->height), ctx->stream));
+    out = BytePlane{(uint8_t*)buf.p, pitch, img->width, img->height};
+    ENB_LAUNCH(ctx, launch_alpha_extract(alpha_source(img, nullptr), out, ctx->stream));
+    return ENB_OK;
+}
+
+// ---- host-buffer staging ---------------------------------------------------
+
+struct Staged {
+    DevBuf buf;
+    enb_image dev{};
+};
+
+enb_status stage_in(enb_ctx* ctx, const enb_image* host, Staged& s, bool copy)
+{
+    s.dev = *host;
+    const int stride = host->planar ? 1 : (host->pix_stride > 0 ? host->pix_stride : host->channels);
+    const int64_t row = (int64_t)host->width * stride * (int64_t)dtype_size(host->dtype);
+    const int64_t pitch = round_up(row, 128);
+    ENB_CUDA(ctx, s.buf.alloc((size_t)(pitch * host->height), ctx->stream));
+    s.dev.data = s.buf.p;
+    s.dev.pitch = pitch;
+    if (copy) {
+        ENB_CUDA(ctx, cudaMemcpy2DAsync(s.buf.p, pitch, host->data, host->pitch, row, host->height,
+                                        cudaMemcpyHostToDevice, ctx->stream));
+    }
+    return ENB_OK;
+}
+
+enb_status stage_out(enb_ctx* ctx, const enb_image* host, const Staged& s)
+{
+    const int stride = host->planar ? 1 : (host->pix_stride > 0 ? host->pix_stride : host->channels);
+    const int64_t row = (int64_t)host->width * stride * (int64_t)dtype_size(host->dtype);
+    ENB_CUDA(ctx, cudaMemcpy2DAsync(host->data, host->pitch, s.dev.data, s.dev.pitch, row, host->height,
+                                    cudaMemcpyDeviceToHost, ctx->stream));
+    return ENB_OK;
+}
+
+// ---- drivers ----------------------------------------------------------------
+
+enb_status enblend_device(enb_ctx* ctx, const enb_image* white, const enb_image* white_alpha, const enb_image* black,
+                          const enb_image* black_alpha, const enb_image* mask, const enb_image* out,
+                          const enb_image* out_alpha, const enb_fuse_options& o, int32_t* level0)
+{
+    const int w = black->width, h = black->height, C = black->channels, dt = black->dtype;
+    const int L = enb_num_levels(w, h, 1, o.levels);
+    const int pdt = fixed_bits_image(dt), mdt = fixed_bits_mask(dt), mf = mask_frac(dt);
+    const int wrap = o.wrap != 0;
+
+    // Mask Gaussian pyramid without alpha (src/enblend.h:384-388).
+    PyrHolder mg(ctx), wl(ctx), bl(ctx);
+    ENB_TRY(pyramid_alloc(ctx, L, w, h, 1, mdt, &mg.p));
+    ENB_LAUNCH(ctx, launch_bytes_to_fixed(byte_plane(mask), level_view(mg.p, 0), mf, ctx->stream));
+    ENB_TRY(gaussian_levels(ctx, wrap, mg.p, nullptr));
+
+    // White and black Laplacian pyramids (src/enblend.h:418-446).
+    DevBuf wa_buf, ba_buf;
+    BytePlane wa, ba;
+    ENB_TRY(alpha_plane(ctx, white, white_alpha, wa_buf, wa));
+    ENB_TRY(alpha_plane(ctx, black, black_alpha, ba_buf, ba));
+    ENB_TRY(pyramid_alloc(ctx, L, w, h, C, pdt, &wl.p));
+    ENB_TRY(pyramid_alloc(ctx, L, w, h, C, pdt, &bl.p));
+    ENB_LAUNCH(ctx, launch_to_fixed(pixel_view(white), level_view(wl.p, 0), kImageFrac, ctx->stream));
+    ENB_TRY(gaussian_levels(ctx, wrap, wl.p, &wa));
+    ENB_TRY(laplacian_levels(ctx, wrap, wl.p));
+    ENB_LAUNCH(ctx, launch_to_fixed(pixel_view(black), level_view(bl.p, 0), kImageFrac, ctx->stream));
+    ENB_TRY(gaussian_levels(ctx, wrap, bl.p, &ba));
+    ENB_TRY(laplacian_levels(ctx, wrap, bl.p));
+
+    // Union alpha: black alpha where white is transparent, else opaque
+    // (src/enblend.h:461-464).
+    DevBuf ua_buf;
+    BytePlane ua;
+    if (out_alpha && out_alpha->data) {
+        ENB_CHECK(ctx, bytes_ok(out_alpha, w, h), "out_alpha: must be U8 of the image size");
+        ua = byte_plane(out_alpha);
+    } else {
+        const int64_t pitch = round_up(w, 128);
+        ENB_CUDA(ctx, ua_buf.alloc((size_t)(pitch * h), ctx->stream));
+        ua = BytePlane{(uint8_t*)ua_buf.p, pitch, w, h};
+    }
+    ENB_LAUNCH(ctx, launch_union_alpha(ba, ua, 1, ctx->stream));
+    ENB_LAUNCH(ctx, launch_union_alpha(wa, ua, 0, ctx->stream));
+
+    // Blend, collapse, copy out (src/enblend.h:468-510).
+    for (int l = 0; l < L; ++l) {
+        ENB_LAUNCH(ctx, launch_blend(level_view(mg.p, l), level_view(wl.p, l), level_view(bl.p, l), 255 << mf,
+                                     ctx->stream));
+    }
+    ENB_TRY(collapse_levels(ctx, wrap, bl.p));
+    if (level0) {
+        ENB_LAUNCH(ctx, launch_copy_level0(level_view(bl.p, 0), level0, ctx->stream));
+    }
+    const PixelView ov = pixel_view(out);
+    if (out->data != black->data) {
+        ENB_LAUNCH(ctx, launch_copy_pixels(pixel_view(black), out->data, ov.pitch, ctx->stream));
+    }
+    ENB_LAUNCH(ctx, launch_from_fixed(level_view(bl.p, 0), ua, out->data, ov.pitch, out->dtype, ov.stride, kImageFrac,
+                                      o.dither, o.seed, ctx->stream));
+    return ENB_OK;
+}
+
+enb_status enfuse_device(enb_ctx* ctx, const enb_enfuse_params* prm, int K, const enb_image* images,
+                         const enb_image* alphas, const enb_image* masks_in, const enb_image* out,
+                         const enb_image* out_alpha, const enb_fuse_options& o, int32_t* level0)
+{
+    const int w = images[0].width, h = images[0].height, C = images[0].channels, dt = images[0].dtype;
+    const int L = enb_num_levels(w, h, 1, o.levels);
+    const int pdt = fixed_bits_image(dt), mdt = fixed_bits_mask(dt), mf = mask_frac(dt);
+    const int wrap = o.wrap != 0;
+    const int64_t fpitch = round_up(w, 32);
+
+    // Weight masks (enfuseMask or --load-masks), their sum and the union alpha
+    // (src/enfuse.h:1281-1391).
+    DevBuf mask_mem, norm_mem;
+    ENB_CUDA(ctx, mask_mem.alloc((size_t)(fpitch * h * 4) * K, ctx->stream));
+    ENB_CUDA(ctx, norm_mem.alloc((size_t)(fpitch * h * 4), ctx->stream));
+    std::vector<FloatPlane> masks(K);
+    const FloatPlane norm{(float*)norm_mem.p, fpitch, w, h};
+    std::vector<DevBuf> abufs(K);
+    std::vector<BytePlane> aplanes(K);
+    DevBuf ua_buf;
+    BytePlane ua;
+    if (out_alpha && out_alpha->data) {
+        ENB_CHECK(ctx, bytes_ok(out_alpha, w, h), "out_alpha: must be U8 of the image size");
+        ua = byte_plane(out_alpha);
+    } else {
+        const int64_t pitch = round_up(w, 128);
+        ENB_CUDA(ctx, ua_buf.alloc((size_t)(pitch * h), ctx->stream));
+        ua = BytePlane{(uint8_t*)ua_buf.p, pitch, w, h};
+    }
+    for (int k = 0; k < K; ++k) {
+        masks[k] = FloatPlane{(float*)mask_mem.p + (size_t)k * fpitch * h, fpitch, w, h};
+        ENB_TRY(alpha_plane(ctx, &images[k], alphas ? &alphas[k] : nullptr, abufs[k], aplanes[k]));
+        if (masks_in) {
+            ENB_CHECK(ctx, floats_ok(&masks_in[k], w, h), "masks_in: F32 planes of the image size expected");
+            ENB_CUDA(ctx, cudaMemcpy2DAsync(masks[k].p, fpitch * 4, masks_in[k].data, masks_in[k].pitch, (size_t)w * 4, h,
+                                            cudaMemcpyDeviceToDevice, ctx->stream));
+        } else {
+            enb_image ai{};
+            ai.data = aplanes[k].p;
+            ai.pitch = aplanes[k].pitch;
+            ai.width = w;
+            ai.height = h;
+            ai.channels = 1;
+            ai.pix_stride = 1;
+            ai.dtype = ENB_U8;
+            ENB_TRY(enfuse_mask_impl(ctx, prm, &images[k], &ai, masks[k]));
+        }
+        ENB_LAUNCH(ctx, launch_union_alpha(aplanes[k], ua, k == 0, ctx->stream));
+        ENB_LAUNCH(ctx, launch_norm_accumulate(masks[k], norm, k == 0, ctx->stream));
+    }
+    if (o.hard_mask) {
+        ENB_CHECK(ctx, K <= 64, "hard mask: at most 64 images");
+        ENB_LAUNCH(ctx, launch_hard_mask(masks.data(), K, ctx->stream));
+    }
+
+    // Pyramids, merge and accumulation (src/enfuse.h:1501-1595).
+    PyrHolder result(ctx), lp(ctx), mg(ctx);
+    ENB_TRY(pyramid_alloc(ctx, L, w, h, C, pdt, &result.p));
+    ENB_TRY(pyramid_alloc(ctx, L, w, h, C, pdt, &lp.p));
+    ENB_TRY(pyramid_alloc(ctx, L, w, h, 1, mdt, &mg.p));
+    for (int k = 0; k < K; ++k) {
+        ENB_LAUNCH(ctx, launch_to_fixed(pixel_view(&images[k]), level_view(lp.p, 0), kImageFrac, ctx->stream));
+        ENB_TRY(gaussian_levels(ctx, wrap, lp.p, &aplanes[k]));
+        ENB_TRY(laplacian_levels(ctx, wrap, lp.p));
+        if (o.hard_mask) {
+            ENB_LAUNCH(ctx, launch_float_to_fixed(masks[k], level_view(mg.p, 0), mf, ctx->stream));
+        } else {
+            ENB_LAUNCH(ctx, launch_soft_mask_to_fixed(masks[k], norm, K, level_view(mg.p, 0), mf, ctx->stream));
+        }
+        ENB_TRY(gaussian_levels(ctx, wrap, mg.p, &ua));
+        for (int l = 0; l < L; ++l) {
+            ENB_LAUNCH(ctx, launch_mask_mul_acc(level_view(lp.p, l), level_view(mg.p, l), 255 << mf,
+                                                level_view(result.p, l), k > 0, ctx->stream));
+        }
+    }
+    ENB_TRY(collapse_levels(ctx, wrap, result.p));
+    if (level0) {
+        ENB_LAUNCH(ctx, launch_copy_level0(level_view(result.p, 0), level0, ctx->stream));
+    }
+    const PixelView ov = pixel_view(out);
+    ENB_CUDA(ctx, cudaMemset2DAsync(out->data, out->pitch, 0, (size_t)w * ov.stride * dtype_size(dt), h, ctx->stream));
+    ENB_LAUNCH(ctx, launch_from_fixed(level_view(result.p, 0), ua, out->data, ov.pitch, out->dtype, ov.stride,
+                                      kImageFrac, o.dither, o.seed, ctx->stream));
+    return ENB_OK;
+}
+
+bool same_geometry(const enb_image* a, const enb_image* b)
+{
+    return a->width == b->width && a->height == b->height && a->channels == b->channels && a->dtype == b->dtype;
+}
+
+}  // namespace
+
+// ============================================================================
+// C ABI
+// ============================================================================
+
+extern "C" {
+
+int enb_abi_version(void) { return ENBGPU_ABI_VERSION; }
+
+enb_status enb_create(int device, enb_ctx** out)
+{
+    if (!out) {
+        return ENB_ERR_INVALID;
+    }
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0 || device < 0 || device >= n) {
+        cudaGetLastError();
+        return ENB_ERR_CUDA;
+    }
+    if (cudaSetDevice(device) != cudaSuccess) {
+        return ENB_ERR_CUDA;
+    }
+    enb_ctx* ctx = new enb_ctx();
+    ctx->device = device;
+    *out = ctx;
+    return ENB_OK;
+}
+
+enb_status enb_destroy(enb_ctx* ctx)
+{
+    if (!ctx) {
+        return ENB_ERR_INVALID;
+    }
+    if (ctx->table_mem) {
+        cudaFreeAsync(ctx->table_mem, ctx->stream);
+        cudaStreamSynchronize(ctx->stream);
+    }
+    delete ctx;
+    return ENB_OK;
+}
+
+enb_status enb_set_stream(enb_ctx* ctx, void* stream)
+{
+    if (!ctx) {
+        return ENB_ERR_INVALID;
+    }
+    ctx->stream = (cudaStream_t)stream;
+    return ENB_OK;
+}
+
+enb_status enb_synchronize(enb_ctx* ctx)
+{
+    if (!ctx) {
+        return ENB_ERR_INVALID;
+    }
+    ENB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return ENB_OK;
+}
+
+const char* enb_last_error(const enb_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+uint64_t enb_launch_count(const enb_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+void enb_default_enfuse_params(enb_enfuse_params* p)
+{
+    if (!p) {
+        return;
+    }
+    memset(p, 0, sizeof *p);
+    p->w_exposure = 1.0;
+    p->w_saturation = 0.0;
+    p->w_contrast = 0.0;
+    p->w_entropy = 0.0;
+    p->exp_optimum = 0.5;
+    p->exp_width = 0.2;
+    p->exp_function = ENB_EXP_GAUSSIAN;
+    p->contrast_window = 5;
+    p->entropy_window = 3;
+    p->gray_projector = ENB_GRAY_AVERAGE;
+}
+
+void enb_default_fuse_options(enb_fuse_options* o)
+{
+    if (!o) {
+        return;
+    }
+    memset(o, 0, sizeof *o);
+    o->dither = ENB_DITHER_HASH;
+    o->seed = 0x5eed;
+}
+
+int enb_num_levels(int w, int h, int min_levels, int exact_levels)
+{
+    unsigned int shortdim = (unsigned int)std::min(w, h);
+    int allowable = min_levels;
+    while (allowable <= kMaxLevels) {
+        if (shortdim <= 8u) {
+            break;
+        }
+        shortdim = (shortdim + 1u) >> 1;
+        ++allowable;
+    }
+    if (allowable > min_levels) {
+        if (exact_levels >= 1) {
+            allowable = std::min(allowable, exact_levels);
+        } else if (exact_levels < 0) {
+            allowable = allowable + exact_levels >= min_levels ? allowable + exact_levels : min_levels;
+        }
+    }
+    return allowable;
+}
+
+enb_status enb_pyramid_create(enb_ctx* ctx, int levels, int width, int height, int channels, int dtype,
+                              enb_pyramid** out)
+{
+    if (!ctx || !out) {
+        return ENB_ERR_INVALID;
+    }
+    return pyramid_alloc(ctx, levels, width, height, channels, dtype, out);
+}
+
+enb_status enb_pyramid_free(enb_ctx* ctx, enb_pyramid* pyr)
+{
+    if (!ctx) {
+        return ENB_ERR_INVALID;
+    }
+    pyramid_release(ctx, pyr);
+    return ENB_OK;
+}
+
+int enb_pyramid_levels(const enb_pyramid* pyr) { return pyr ? pyr->levels : 0; }
+
+enb_status enb_pyramid_level(const enb_pyramid* p, int l, enb_image* out)
+{
+    if (!p || !out || l < 0 || l >= p->levels) {
+        return ENB_ERR_INVALID;
+    }
+    const int64_t es = (int64_t)dtype_size(p->dtype);
+    memset(out, 0, sizeof *out);
+    out->data = (char*)p->base + p->offset[l];
+    out->pitch = p->pitch[l] * es;
+    out->plane_pitch = p->pitch[l] * p->h[l] * es;
+    out->width = p->w[l];
+    out->height = p->h[l];
+    out->channels = p->C;
+    out->pix_stride = 1;
+    out->dtype = p->dtype;
+    out->planar = 1;
+    return ENB_OK;
+}
+
+static enb_status level_copy(enb_ctx* ctx, const enb_pyramid* p, int l, void* host, bool to_host)
+{
+    if (!ctx || !p || !host || l < 0 || l >= p->levels) {
+        return fail(ctx, ENB_ERR_INVALID, "pyramid level copy: bad arguments");
+    }
+    const size_t es = dtype_size(p->dtype);
+    const size_t row = (size_t)p->w[l] * es;
+    char* dev = (char*)p->base + p->offset[l];
+    const size_t dpitch = (size_t)p->pitch[l] * es;
+    for (int c = 0; c < p->C; ++c) {
+        char* dplane = dev + (size_t)c * dpitch * p->h[l];
+        char* hplane = (char*)host + (size_t)c * row * p->h[l];
+        if (to_host) {
+            ENB_CUDA(ctx, cudaMemcpy2DAsync(hplane, row, dplane, dpitch, row, p->h[l], cudaMemcpyDeviceToHost, ctx->stream));
+        } else {
+            ENB_CUDA(ctx, cudaMemcpy2DAsync(dplane, dpitch, hplane, row, row, p->h[l], cudaMemcpyHostToDevice, ctx->stream));
+        }
+    }
+    ENB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return ENB_OK;
+}
+
+enb_status enb_pyramid_read_level(enb_ctx* ctx, const enb_pyramid* p, int l, void* host_dst)
+{
+    return level_copy(ctx, p, l, host_dst, true);
+}
+
+enb_status enb_pyramid_write_level(enb_ctx* ctx, enb_pyramid* p, int l, const void* host_src)
+{
+    return level_copy(ctx, p, l, const_cast<void*>(host_src), false);
+}
+
+enb_status enb_to_pyramid(enb_ctx* ctx, const enb_image* src, const enb_image* dst, int frac)
+{
+    if (!ctx) {
+        return ENB_ERR_INVALID;
+    }
+    ENB_CHECK(ctx, planar_ok(dst), "to_pyramid: dst must be a planar I16/I32 level");
+    ENB_CHECK(ctx, frac >= 0 && frac <= 24, "to_pyramid: frac_bits outside 0..24");
+    ENB_CHECK(ctx, src && src->width == dst->width && src->height == dst->height, "to_pyramid: size mismatch");
+    if (src->dtype == ENB_F32) {
+        ENB_CHECK(ctx, src->channels == 1 && dst->channels == 1 && floats_ok(src, src->width, src->height),
+                  "to_pyramid: F32 sources are single-channel planes");
+        ENB_LAUNCH(ctx, launch_float_to_fixed(float_plane(src), planar_view(dst), frac, ctx->stream));
+        return ENB_OK;
+    }
+    ENB_CHECK(ctx, pixels_ok(src), "to_pyramid: src must be interleaved U8/U16");
+    ENB_CHECK(ctx, src->channels == dst->channels, "to_pyramid: channel mismatch");
+    ENB_LAUNCH(ctx, launch_to_fixed(pixel_view(src), planar_view(dst), frac, ctx->stream));
+    return ENB_OK;
+}
+
+enb_status enb_reduce(enb_ctx* ctx, int wrap, const enb_image* src, const enb_image* src_alpha, const enb_image* dst,
+                      const enb_image* dst_alpha)
+{
+    if (!ctx) {
+        return ENB_ERR_INVALID;
+    }
+    ENB_CHECK(ctx, planar_ok(src) && planar_ok(dst), "reduce: planar I16/I32 levels expected");
+    ENB_CHECK(ctx, src->dtype == dst->dtype && src->channels == dst->channels && (src->channels == 1 || src->channels == 3),
+              "reduce: dtype/channel mismatch");
+    ENB_CHECK(ctx, src->width > 1 && src->height > 1, "reduce: src image too small in reduce");
+    ENB_CHECK(ctx, dst->width == (src->width + 1) >> 1 && dst->height == (src->height + 1) >> 1,
+              "reduce: dst must be ((w+1)>>1, (h+1)>>1)");
+    if (src_alpha) {
+        ENB_CHECK(ctx, bytes_ok(src_alpha, src->width, src->height) && bytes_ok(dst_alpha, dst->width, dst->height),
+                  "reduce: alpha planes must be U8 of the level sizes");
+        const BytePlane sa = byte_plane(src_alpha), da = byte_plane(dst_alpha);
+        ENB_LAUNCH(ctx, launch_reduce(wrap != 0, planar_view(src), &sa, planar_view(dst), &da, ctx->stream));
+    } else {
+        ENB_LAUNCH(ctx, launch_reduce(wrap != 0, planar_view(src), nullptr, planar_view(dst), nullptr, ctx->stream));
+    }
+    return ENB_OK;
+}
+
+enb_status enb_expand(enb_ctx* ctx, int add, int wrap, const enb_image* src, const enb_image* dst)
+{
+    if (!ctx) {
+        return ENB_ERR_INVALID;
+    }
+    ENB_CHECK(ctx, planar_ok(src) && planar_ok(dst), "expand: planar I16/I32 levels expected");
+    ENB_CHECK(ctx, src->dtype == dst->dtype && src->channels == dst->channels && (src->channels == 1 || src->channels == 3),
+              "expand: dtype/channel mismatch");
+    ENB_CHECK(ctx, src->width == (dst->width + 1) >> 1 && src->height == (dst->height + 1) >> 1,
+              "expand: src must be ((w+1)>>1, (h+1)>>1) of dst");
+    ENB_LAUNCH(ctx, launch_expand(add != 0, wrap != 0, planar_view(src), planar_view(dst), ctx->stream));
+    return ENB_OK;
+}
+
+enb_status enb_blend(enb_ctx* ctx, const enb_image* mask, const enb_image* white, const enb_image* black,
+                     int32_t white_value)
+{
+    if (!ctx) {
+        return ENB_ERR_INVALID;
+    }
+    ENB_CHECK(ctx, planar_ok(mask) && planar_ok(white) && planar_ok(black), "blend: planar levels expected");
+    ENB_CHECK(ctx, mask->channels == 1 && same_geometry(white, black) && mask->width == black->width &&
+                       mask->height == black->height && (black->channels == 1 || black->channels == 3),
+              "blend: size/channel mismatch");
+    ENB_CHECK(ctx, white_value > 0, "blend: white value must be positive");
+    ENB_LAUNCH(ctx, launch_blend(planar_view(mask), planar_view(white), planar_view(black), white_value, ctx->stream));
+    return ENB_OK;
+}
+
+enb_status enb_mask_multiply_accumulate(enb_ctx* ctx, const enb_image* lp, const enb_image* mask, int32_t divisor,
+                                        const enb_image* result, int accumulate)
+{
+    if (!ctx) {
+        return ENB_ERR_INVALID;
+    }
+    ENB_CHECK(ctx, planar_ok(lp) && planar_ok(mask) && planar_ok(result), "mask_multiply: planar levels expected");
+    ENB_CHECK(ctx, mask->channels == 1 && same_geometry(lp, result) && mask->width == lp->width &&
+                       mask->height == lp->height && (lp->channels == 1 || lp->channels == 3),
+              "mask_multiply: size/channel mismatch");
+    ENB_CHECK(ctx, divisor > 0, "mask_multiply: divisor must be positive");
+    ENB_LAUNCH(ctx, launch_mask_mul_acc(planar_view(lp), planar_view(mask), divisor, planar_view(result),
+                                        accumulate != 0, ctx->stream));
+    return ENB_OK;
+}
+
+enb_status enb_from_pyramid(enb_ctx* ctx, const enb_image* src, const enb_image* alpha, const enb_image* dst,
+                            int frac, int dither, uint64_t seed)
+{
+    if (!ctx) {
+        return ENB_ERR_INVALID;
+    }
+    ENB_CHECK(ctx, planar_ok(src), "from_pyramid: planar source level expected");
+    ENB_CHECK(ctx, pixels_ok(dst) && dst->width == src->width && dst->height == src->height &&
+                       dst->channels == src->channels,
+              "from_pyramid: dst must be an interleaved U8/U16 image of the level size");
+    ENB_CHECK(ctx, bytes_ok(alpha, src->width, src->height), "from_pyramid: alpha must be U8 of the level size");
+    ENB_CHECK(ctx, frac >= 2 && frac <= 24, "from_pyramid: frac_bits must be 2..24");
+    ENB_CHECK(ctx, dither == ENB_DITHER_HASH || dither == ENB_DITHER_NEAREST, "from_pyramid: unknown dither mode");
+    const PixelView dv = pixel_view(dst);
+    ENB_LAUNCH(ctx, launch_from_fixed(planar_view(src), byte_plane(alpha), dst->data, dv.pitch, dst->dtype, dv.stride,
+                                      frac, dither, seed, ctx->stream));
+    return ENB_OK;
+}
+
+enb_status enb_gaussian_pyramid(enb_ctx* ctx, int wrap, const enb_image* src, const enb_image* alpha, int frac,
+                                enb_pyramid* pyr)
+{
+    if (!ctx || !pyr) {
+        return ENB_ERR_INVALID;
+    }
+    enb_image l0;
+    enb_pyramid_level(pyr, 0, &l0);
+    ENB_TRY(enb_to_pyramid(ctx, src, &l0, frac));
+    if (alpha) {
+        ENB_CHECK(ctx, bytes_ok(alpha, src->width, src->height), "gaussian_pyramid: alpha must be U8 of the image size");
+        const BytePlane a = byte_plane(alpha);
+        return gaussian_levels(ctx, wrap != 0, pyr, &a);
+    }
+    return gaussian_levels(ctx, wrap != 0, pyr, nullptr);
+}
+
+enb_status enb_laplacian_pyramid(enb_ctx* ctx, int wrap, const enb_image* src, const enb_image* alpha, int frac,
+                                 enb_pyramid* pyr)
+{
+    ENB_TRY(enb_gaussian_pyramid(ctx, wrap, src, alpha, frac, pyr));
+    return laplacian_levels(ctx, wrap != 0, pyr);
+}
+
+enb_status enb_collapse_pyramid(enb_ctx* ctx, int wrap, enb_pyramid* pyr)
+{
+    if (!ctx || !pyr) {
+        return ENB_ERR_INVALID;
+    }
+    return collapse_levels(ctx, wrap != 0, pyr);
+}
+
+enb_status enb_blend_pyramids(enb_ctx* ctx, const enb_pyramid* mask_gp, const enb_pyramid* white_lp,
+                              enb_pyramid* black_lp, int32_t white_value)
+{
+    if (!ctx || !mask_gp || !white_lp || !black_lp) {
+        return ENB_ERR_INVALID;
+    }
+    ENB_CHECK(ctx, mask_gp->levels == black_lp->levels && white_lp->levels == black_lp->levels,
+              "blend_pyramids: level count mismatch");
+    for (int l = 0; l < black_lp->levels; ++l) {
+        ENB_CHECK(ctx, mask_gp->w[l] == black_lp->w[l] && mask_gp->h[l] == black_lp->h[l], "blend_pyramids: size mismatch");
+        ENB_LAUNCH(ctx, launch_blend(level_view(mask_gp, l), level_view(white_lp, l), level_view(black_lp, l),
+                                     white_value, ctx->stream));
+    }
+    return ENB_OK;
+}
+
+enb_status enb_enfuse_mask(enb_ctx* ctx, const enb_enfuse_params* prm, const enb_image* src, const enb_image* alpha,
+                           const enb_image* mask_out)
+{
+    if (!ctx) {
+        return ENB_ERR_INVALID;
+    }
+    ENB_CHECK(ctx, pixels_ok(src), "enfuse_mask: src must be interleaved U8/U16 (1 or 3 channels)");
+    ENB_TRY(check_params(ctx, prm, src->width, src->height));
+    ENB_CHECK(ctx, floats_ok(mask_out, src->width, src->height), "enfuse_mask: mask_out must be F32 of the image size");
+    if (alpha && alpha->data) {
+        ENB_CHECK(ctx, bytes_ok(alpha, src->width, src->height), "enfuse_mask: alpha must be U8 of the image size");
+    }
+    return enfuse_mask_impl(ctx, prm, src, alpha, float_plane(mask_out));
+}
+
+enb_status enb_enfuse(enb_ctx* ctx, const enb_enfuse_params* prm, int K, const enb_image* images,
+                      const enb_image* alphas, const enb_image* masks_in, const enb_image* out,
+                      const enb_image* out_alpha, const enb_fuse_options* opt)
+{
+    if (!ctx) {
+        return ENB_ERR_INVALID;
+    }
+    enb_fuse_options o;
+    enb_default_fuse_options(&o);
+    if (opt) {
+        o = *opt;
+    }
+    ENB_CHECK(ctx, K >= 1 && images, "enfuse: need at least one image");
+    for (int k = 0; k < K; ++k) {
+        ENB_CHECK(ctx, pixels_ok(&images[k]), "enfuse: images must be interleaved U8/U16 with 1 or 3 channels");
+        ENB_CHECK(ctx, same_geometry(&images[k], &images[0]), "enfuse: images differ in size, channels or type");
+    }
+    ENB_CHECK(ctx, out && pixels_ok(out) && same_geometry(out, &images[0]), "enfuse: out must match the inputs");
+    ENB_CHECK(ctx, o.dither == ENB_DITHER_HASH || o.dither == ENB_DITHER_NEAREST, "enfuse: unknown dither mode");
+    if (!masks_in) {
+        ENB_TRY(check_params(ctx, prm, images[0].width, images[0].height));
+    }
+    const int w = images[0].width, h = images[0].height, C = images[0].channels;
+    if (!o.host_buffers) {
+        return enfuse_device(ctx, prm, K, images, alphas, masks_in, out, out_alpha, o, (int32_t*)o.level0_out);
+    }
+    // Host buffers: stage in, run, stage out (copies on the context stream).
+    std::vector<Staged> si(K), sa(alphas ? K : 0), sm(masks_in ? K : 0);
+    std::vector<enb_image> di(K), da(alphas ? K : 0), dm(masks_in ? K : 0);
+    for (int k = 0; k < K; ++k) {
+        ENB_TRY(stage_in(ctx, &images[k], si[k], true));
+        di[k] = si[k].dev;
+        if (alphas) {
+            ENB_TRY(stage_in(ctx, &alphas[k], sa[k], alphas[k].data != nullptr));
+            da[k] = sa[k].dev;
+            if (!alphas[k].data) {
+                da[k].data = nullptr;
+            }
+        }
+        if (masks_in) {
+            ENB_TRY(stage_in(ctx, &masks_in[k], sm[k], true));
+            dm[k] = sm[k].dev;
+        }
+    }
+    Staged so, soa;
+    ENB_TRY(stage_in(ctx, out, so, false));
+    const bool want_alpha = out_alpha && out_alpha->data;
+    if (want_alpha) {
+        ENB_TRY(stage_in(ctx, out_alpha, soa, false));
+    }
+    DevBuf l0;
+    if (o.level0_out) {
+        ENB_CUDA(ctx, l0.alloc((size_t)w * h * C * 4, ctx->stream));
+    }
+    ENB_TRY(enfuse_device(ctx, prm, K, di.data(), alphas ? da.data() : nullptr, masks_in ? dm.data() : nullptr,
+                          &so.dev, want_alpha ? &soa.dev : nullptr, o, (int32_t*)l0.p));
+    ENB_TRY(stage_out(ctx, out, so));
+    if (want_alpha) {
+        ENB_TRY(stage_out(ctx, out_alpha, soa));
+    }
+    if (o.level0_out) {
+        ENB_CUDA(ctx, cudaMemcpyAsync(o.level0_out, l0.p, (size_t)w * h * C * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    ENB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return ENB_OK;
+}
+
+enb_status enb_enblend(enb_ctx* ctx, const enb_image* white, const enb_image* white_alpha, const enb_image* black,
+                       const enb_image* black_alpha, const enb_image* mask, const enb_image* out,
+                       const enb_image* out_alpha, const enb_fuse_options* opt)
+{
+    if (!ctx) {
+        return ENB_ERR_INVALID;
+    }
+    enb_fuse_options o;
+    enb_default_fuse_options(&o);
+    if (opt) {
+        o = *opt;
+    }
+    ENB_CHECK(ctx, pixels_ok(white) && pixels_ok(black) && same_geometry(white, black),
+              "enblend: white/black must be interleaved U8/U16 images of one geometry");
+    ENB_CHECK(ctx, out && pixels_ok(out) && same_geometry(out, black), "enblend: out must match the inputs");
+    ENB_CHECK(ctx, mask && bytes_ok(mask, black->width, black->height), "enblend: mask must be U8 of the image size");
+    ENB_CHECK(ctx, black->width > 1 && black->height > 1, "enblend: image too small");
+    ENB_CHECK(ctx, o.dither == ENB_DITHER_HASH || o.dither == ENB_DITHER_NEAREST, "enblend: unknown dither mode");
+    const int w = black->width, h = black->height, C = black->channels;
+    if (!o.host_buffers) {
+        return enblend_device(ctx, white, white_alpha, black, black_alpha, mask, out, out_alpha, o,
+                              (int32_t*)o.level0_out);
+    }
+    Staged sw, sb, swa, sba, sm, so, soa;
+    ENB_TRY(stage_in(ctx, white, sw, true));
+    ENB_TRY(stage_in(ctx, black, sb, true));
+    ENB_TRY(stage_in(ctx, mask, sm, true));
+    const bool has_wa = white_alpha && white_alpha->data, has_ba = black_alpha && black_alpha->data;
+    if (has_wa) {
+        ENB_TRY(stage_in(ctx, white_alpha, swa, true));
+    }
+    if (has_ba) {
+        ENB_TRY(stage_in(ctx, black_alpha, sba, true));
+    }
+    ENB_TRY(stage_in(ctx, out, so, false));
+    const bool want_alpha = out_alpha && out_alpha->data;
+    if (want_alpha) {
+        ENB_TRY(stage_in(ctx, out_alpha, soa, false));
+    }
+    DevBuf l0;
+    if (o.level0_out) {
+        ENB_CUDA(ctx, l0.alloc((size_t)w * h * C * 4, ctx->stream));
+    }
+    ENB_TRY(enblend_device(ctx, &sw.dev, has_wa ? &swa.dev : nullptr, &sb.dev, has_ba ? &sba.dev : nullptr, &sm.dev,
+                           &so.dev, want_alpha ? &soa.dev : nullptr, o, (int32_t*)l0.p));
+    ENB_TRY(stage_out(ctx, out, so));
+    if (want_alpha) {
+        ENB_TRY(stage_out(ctx, out_alpha, soa));
+    }
+    if (o.level0_out) {
+        ENB_CUDA(ctx, cudaMemcpyAsync(o.level0_out, l0.p, (size_t)w * h * C * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    ENB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return ENB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,115 @@
+// enb_internal.h -- shared declarations of the CUDA kernels and the C ABI layer.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "enbgpu.h"
+
+namespace enb {
+
+constexpr int kMaxLevels = 29;  // MAX_PYRAMID_LEVELS, src/common.h:55
+constexpr int kMaxEntropyWindow = 15;
+constexpr int kMaxContrastWindow = 31;
+
+// A planar level: `C` planes of h rows; pitch and plane strides in elements.
+struct PlanarView {
+    void* p;
+    int64_t pitch;
+    int64_t plane;
+    int w, h, C;
+    int dtype;  // ENB_I16 / ENB_I32
+};
+
+// An interleaved pixel image; pitch in elements of the sample type.
+struct PixelView {
+    const void* p;
+    int64_t pitch;
+    int w, h, C, stride;
+    int dtype;  // ENB_U8 / ENB_U16
+};
+
+// An 8-bit plane (alpha, seam mask).
+struct BytePlane {
+    uint8_t* p;
+    int64_t pitch;
+    int w, h;
+};
+
+// A float plane (weights).
+struct FloatPlane {
+    float* p;
+    int64_t pitch;
+    int w, h;
+};
+
+// Where the alpha of a pixel comes from.
+enum AlphaMode { kAlphaPlane = 0, kAlphaOpaque = 1, kAlphaChannel3 = 2 };
+
+struct AlphaSrc {
+    int mode;
+    BytePlane plane;  // kAlphaPlane
+    PixelView pix;    // kAlphaChannel3: 4th component thresholded at [lo, hi]
+    uint32_t lo, hi;
+};
+
+// Device-side constant tables of the enfuse weights.
+struct WeightTables {
+    const float* exposure;    // [max+1]: (float)(W_exp * f(g / max))
+    const float* contrast;    // [max+1]: (float)(W_con * g / max)
+    const float* entropy;     // [max+1]: (float)(W_ent * (double)(float)m)
+    const double* plogp;      // [(n_max+1)*(n_max+1)]: p log p, p = c / n
+    const long long* plogp_fx;// same in 2^-56 fixed point
+    const double* logb;       // [n_max+1]: log(b)
+    const float* scale_logb;  // [n_max+1]: max / log(b) as float
+};
+
+struct WeightParams {
+    int use_exposure, use_contrast, use_saturation, use_entropy;
+    int contrast_window, entropy_window;
+    int gray_projector;
+    double mixer[3];          // normalised channel-mixer weights
+    double w_saturation;
+    float w_sat_hi, w_sat_lo; // w_saturation split into two floats
+    uint32_t maxv;
+};
+
+// Name and algorithmic bytes of the most recent launch on this host thread;
+// each launcher sets it (read by the profiler of the C ABI layer).
+struct LaunchInfo {
+    const char* name;
+    double bytes;
+};
+LaunchInfo& last_launch();
+
+// ---- launchers (all queue on `st` and return the CUDA launch status) ------
+cudaError_t launch_to_fixed(const PixelView& src, const PlanarView& dst, int frac, cudaStream_t st);
+cudaError_t launch_bytes_to_fixed(const BytePlane& src, const PlanarView& dst, int frac, cudaStream_t st);
+cudaError_t launch_float_to_fixed(const FloatPlane& src, const PlanarView& dst, int frac,
+                                  cudaStream_t st);
+cudaError_t launch_alpha_extract(const AlphaSrc& a, const BytePlane& dst, cudaStream_t st);
+cudaError_t launch_reduce(int wrap, const PlanarView& src, const BytePlane* src_alpha,
+                          const PlanarView& dst, const BytePlane* dst_alpha, cudaStream_t st);
+cudaError_t launch_expand(int add, int wrap, const PlanarView& src, const PlanarView& dst,
+                          cudaStream_t st);
+cudaError_t launch_blend(const PlanarView& mask, const PlanarView& white, const PlanarView& black,
+                         int32_t white_value, cudaStream_t st);
+cudaError_t launch_mask_mul_acc(const PlanarView& lp, const PlanarView& mask, int32_t divisor,
+                                const PlanarView& result, int accumulate, cudaStream_t st);
+cudaError_t launch_from_fixed(const PlanarView& src, const BytePlane& alpha, void* dst,
+                              int64_t dst_pitch, int dst_dtype, int dst_stride, int frac,
+                              int dither, uint64_t seed, cudaStream_t st);
+cudaError_t launch_copy_pixels(const PixelView& src, void* dst, int64_t dst_pitch, cudaStream_t st);
+cudaError_t launch_enfuse_mask(const PixelView& img, const AlphaSrc& alpha, const WeightParams& wp,
+                               const WeightTables& tab, const FloatPlane& out, cudaStream_t st);
+cudaError_t launch_norm_accumulate(const FloatPlane& mask, const FloatPlane& norm, int first,
+                                   cudaStream_t st);
+cudaError_t launch_union_alpha(const BytePlane& a, const BytePlane& uni, int first, cudaStream_t st);
+cudaError_t launch_hard_mask(const FloatPlane* masks, int K, cudaStream_t st);
+cudaError_t launch_soft_mask_to_fixed(const FloatPlane& mask, const FloatPlane& norm, int K,
+                                      const PlanarView& dst, int frac, cudaStream_t st);
+cudaError_t launch_copy_level0(const PlanarView& src, int32_t* dst, cudaStream_t st);
+
+}  // namespace enb

@@ -1,0 +1,1360 @@
+// enb_kernels.cu -- sm_103a kernels of the enblend/enfuse multiresolution path.
+//
+// Integer stages reproduce the reference's fixed-point arithmetic exactly
+// (src/pyramid.h, src/fixmath.h, src/blend.h, src/enfuse.h:601-620).  Where the
+// reference rounds an IEEE double expression, the kernels either evaluate it
+// with the same round-to-nearest double operations (__dmul_rn/__dadd_rn/
+// __ddiv_rn, never contracted into FMAs) or with an exact integer/float
+// formulation that provably yields the same result, falling back to the double
+// expression in the rare cases the fast path cannot decide.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "enb_internal.h"
+
+namespace enb {
+
+// ---------------------------------------------------------------------------
+// Helpers
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__device__ __forceinline__ T cast_store(int64_t v);  // static_cast into the pyramid type
+
+template <>
+__device__ __forceinline__ int16_t cast_store<int16_t>(int64_t v) { return (int16_t)(uint16_t)(v & 0xffff); }
+
+template <>
+__device__ __forceinline__ int32_t cast_store<int32_t>(int64_t v) { return (int32_t)(uint32_t)(v & 0xffffffffu); }
+
+// NumericTraits<T>::fromPromote: saturate Int16, identity for Int32.
+template <typename T>
+__device__ __forceinline__ T sat_store(int32_t v);
+
+template <>
+__device__ __forceinline__ int16_t sat_store<int16_t>(int32_t v) { return (int16_t)min(max(v, -32768), 32767); }
+
+template <>
+__device__ __forceinline__ int32_t sat_store<int32_t>(int32_t v) { return v; }
+
+// NumericTraits<T>::fromRealPromote of a double (round half away from zero
+// through +-0.5 and a truncating cast, saturating).
+template <typename T>
+__device__ __forceinline__ T frp_store(double v);
+
+template <>
+__device__ __forceinline__ int32_t frp_store<int32_t>(double v)
+{
+    if (v < 0.0) {
+        return v < -2147483648.0 ? INT32_MIN : __double2int_rz(__dadd_rn(v, -0.5));
+    }
+    return v > 2147483647.0 ? INT32_MAX : __double2int_rz(__dadd_rn(v, 0.5));
+}
+
+template <>
+__device__ __forceinline__ int16_t frp_store<int16_t>(double v)
+{
+    if (v < 0.0) {
+        return v < -32768.0 ? (int16_t)-32768 : (int16_t)__double2int_rz(__dadd_rn(v, -0.5));
+    }
+    return v > 32767.0 ? (int16_t)32767 : (int16_t)__double2int_rz(__dadd_rn(v, 0.5));
+}
+
+__device__ __forceinline__ uint32_t frp_unsigned(double v, uint32_t maxv)
+{
+    if (v < 0.0) {
+        return 0u;
+    }
+    return v > (double)maxv ? maxv : (uint32_t)__double2uint_rz(__dadd_rn(v, 0.5));
+}
+
+__host__ __device__ __forceinline__ int imod(int a, int m)
+{
+    int r = a % m;
+    return r < 0 ? r + m : r;
+}
+
+template <typename T>
+__device__ __forceinline__ T* plane_ptr(const PlanarView& v, int c, int y)
+{
+    return reinterpret_cast<T*>(v.p) + (int64_t)c * v.plane + (int64_t)y * v.pitch;
+}
+
+__device__ __forceinline__ uint32_t load_sample(const void* p, int dtype, int64_t i)
+{
+    return dtype == ENB_U8 ? (uint32_t)reinterpret_cast<const uint8_t*>(p)[i]
+                           : (uint32_t)reinterpret_cast<const uint16_t*>(p)[i];
+}
+
+__device__ __forceinline__ int alpha_at(const AlphaSrc& a, int x, int y)
+{
+    if (a.mode == kAlphaOpaque) {
+        return 1;
+    }
+    if (a.mode == kAlphaPlane) {
+        return a.plane.p[(int64_t)y * a.plane.pitch + x] != 0;
+    }
+    const uint32_t v = load_sample(a.pix.p, a.pix.dtype, (int64_t)y * a.pix.pitch + (int64_t)x * a.pix.stride + 3);
+    return v >= a.lo && v <= a.hi;
+}
+
+static inline dim3 grid2d(int w, int h, int tw, int th)
+{
+    return dim3((unsigned)((w + tw - 1) / tw), (unsigned)((h + th - 1) / th));
+}
+
+// ---------------------------------------------------------------------------
+// Conversions to fixed point (src/fixmath.h:116-206)
+// ---------------------------------------------------------------------------
+
+template <typename TS, typename TD>
+__global__ void __launch_bounds__(256) k_to_fixed(const TS* __restrict__ src, int64_t spitch, int stride, int C,
+                                                  TD* __restrict__ dst, int64_t dpitch, int64_t dplane,
+                                                  int w, int h, int frac)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= w) {
+        return;
+    }
+    const TS* s = src + (int64_t)y * spitch + (int64_t)x * stride;
+    for (int c = 0; c < C; ++c) {
+        dst[(int64_t)c * dplane + (int64_t)y * dpitch + x] = (TD)((int32_t)s[c] << frac);
+    }
+}
+
+template <typename TD>
+__global__ void __launch_bounds__(256) k_float_to_fixed(const float* __restrict__ src, int64_t spitch,
+                                                        TD* __restrict__ dst, int64_t dpitch, int w, int h,
+                                                        int frac)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= w) {
+        return;
+    }
+    const double v = __dmul_rn((double)src[(int64_t)y * spitch + x], (double)(1u << frac));
+    dst[(int64_t)y * dpitch + x] = frp_store<TD>(v);
+}
+
+// Exact fromRealPromote(m * 2^frac) for 0 <= m * 2^frac < 2^23 in float
+// arithmetic: the product is exact, floor and the fractional part are exact.
+template <typename TD>
+__device__ __forceinline__ TD mask_to_fixed(float m, int frac)
+{
+    const float v = m * (float)(1u << frac);
+    if (v >= 0.0f && v < 8388608.0f) {
+        const float fl = floorf(v);
+        const int r = (int)fl + ((v - fl) >= 0.5f ? 1 : 0);
+        return (TD)r;
+    }
+    return frp_store<TD>(__dmul_rn((double)m, (double)(1u << frac)));
+}
+
+// Soft-mask normalisation fused with the conversion of the mask to fixed
+// point (src/enfuse.h:1526-1535 then fixmath.h:189-195).
+template <typename TD>
+__global__ void __launch_bounds__(256) k_soft_mask_to_fixed(const float* __restrict__ mask, int64_t mpitch,
+                                                            const float* __restrict__ norm, int64_t npitch,
+                                                            float fallback, TD* __restrict__ dst,
+                                                            int64_t dpitch, int w, int h, int frac)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= w) {
+        return;
+    }
+    const float n = norm[(int64_t)y * npitch + x];
+    const float m = n > 0.0f ? __fdiv_rn(__fmul_rn(255.0f, mask[(int64_t)y * mpitch + x]), n) : fallback;
+    dst[(int64_t)y * dpitch + x] = mask_to_fixed<TD>(m, frac);
+}
+
+template <typename TD>
+__global__ void __launch_bounds__(256) k_bytes_to_fixed(const uint8_t* __restrict__ src, int64_t spitch,
+                                                        TD* __restrict__ dst, int64_t dpitch, int w, int h,
+                                                        int frac)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= w) {
+        return;
+    }
+    dst[(int64_t)y * dpitch + x] = (TD)((int32_t)src[(int64_t)y * spitch + x] << frac);
+}
+
+__global__ void __launch_bounds__(256) k_alpha_extract(AlphaSrc a, uint8_t* __restrict__ dst, int64_t dpitch,
+                                                       int w, int h)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= w) {
+        return;
+    }
+    dst[(int64_t)y * dpitch + x] = alpha_at(a, x, y) ? 255 : 0;
+}
+
+// ---------------------------------------------------------------------------
+// Reduce (src/pyramid.h:166-848)
+// ---------------------------------------------------------------------------
+//
+// One CTA computes a 32x8 tile of destination pixels.  The 67x19 source
+// window (2 pixels of halo) is staged in shared memory, then filtered with
+// the separable [1 4 6 4 1] kernel: first along x at the even source
+// columns, then along y.  Integer sums are exact, so the order of the taps
+// does not matter.
+
+constexpr int RTW = 32, RTH = 8;
+constexpr int RIW = 2 * RTW + 3, RIH = 2 * RTH + 3;
+
+// With alpha: normalised convolution over the opaque taps, taps outside the
+// image dropped, x periodic when wrap.
+template <typename TS, typename TD, int C>
+__global__ void __launch_bounds__(256) k_reduce_alpha(const TS* __restrict__ src, int64_t spitch, int64_t splane,
+                                                      int sw, int sh, const uint8_t* __restrict__ sa,
+                                                      int64_t sapitch, TD* __restrict__ dst, int64_t dpitch,
+                                                      int64_t dplane, int dw, int dh, uint8_t* __restrict__ da,
+                                                      int64_t dapitch, int wrap)
+{
+    __shared__ int32_t sv[C][RIH][RIW];
+    __shared__ int32_t sm[RIH][RIW];
+    __shared__ int32_t hv[C][RIH][RTW];
+    __shared__ int32_t hm[RIH][RTW];
+
+    const int X0 = blockIdx.x * RTW, Y0 = blockIdx.y * RTH;
+    const int gx0 = 2 * X0 - 2, gy0 = 2 * Y0 - 2;
+    const int tid = threadIdx.x;
+
+    for (int i = tid; i < RIH * RIW; i += 256) {
+        const int r = i / RIW, c = i - r * RIW;
+        const int gy = gy0 + r;
+        int gx = gx0 + c;
+        int a = 0;
+        int32_t v[C];
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) {
+            v[ch] = 0;
+        }
+        if (gy >= 0 && gy < sh) {
+            if (wrap) {
+                gx = imod(gx, sw);
+            }
+            if (gx >= 0 && gx < sw) {
+                a = sa[(int64_t)gy * sapitch + gx] != 0;
+                if (a) {
+#pragma unroll
+                    for (int ch = 0; ch < C; ++ch) {
+                        v[ch] = (int32_t)src[(int64_t)ch * splane + (int64_t)gy * spitch + gx];
+                    }
+                }
+            }
+        }
+        sm[r][c] = a;
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) {
+            sv[ch][r][c] = v[ch];
+        }
+    }
+    __syncthreads();
+
+    for (int i = tid; i < RIH * RTW; i += 256) {
+        const int r = i / RTW, j = i - r * RTW;
+        const int c0 = 2 * j;
+        hm[r][j] = sm[r][c0] + 4 * sm[r][c0 + 1] + 6 * sm[r][c0 + 2] + 4 * sm[r][c0 + 3] + sm[r][c0 + 4];
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) {
+            hv[ch][r][j] = sv[ch][r][c0] + 4 * sv[ch][r][c0 + 1] + 6 * sv[ch][r][c0 + 2] +
+                           4 * sv[ch][r][c0 + 3] + sv[ch][r][c0 + 4];
+        }
+    }
+    __syncthreads();
+
+    const int tx = tid % RTW, ty = tid / RTW;
+    const int X = X0 + tx, Y = Y0 + ty;
+    if (X >= dw || Y >= dh) {
+        return;
+    }
+    const int r0 = 2 * ty;
+    const int den = hm[r0][tx] + 4 * hm[r0 + 1][tx] + 6 * hm[r0 + 2][tx] + 4 * hm[r0 + 3][tx] + hm[r0 + 4][tx];
+    if (den > 0) {
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) {
+            const int32_t num = hv[ch][r0][tx] + 4 * hv[ch][r0 + 1][tx] + 6 * hv[ch][r0 + 2][tx] +
+                                4 * hv[ch][r0 + 3][tx] + hv[ch][r0 + 4][tx];
+            const int32_t q = den == 256 ? num / 256 : num / den;
+            dst[(int64_t)ch * dplane + (int64_t)Y * dpitch + X] = cast_store<TD>(q);
+        }
+        da[(int64_t)Y * dapitch + X] = 255;
+    } else {
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) {
+            dst[(int64_t)ch * dplane + (int64_t)Y * dpitch + X] = (TD)0;
+        }
+        da[(int64_t)Y * dapitch + X] = 0;
+    }
+}
+
+// Without alpha: clamp-to-edge in y (and x unless wrap), divide by 256.
+template <typename TS, typename TD, int C>
+__global__ void __launch_bounds__(256) k_reduce_noalpha(const TS* __restrict__ src, int64_t spitch, int64_t splane,
+                                                        int sw, int sh, TD* __restrict__ dst, int64_t dpitch,
+                                                        int64_t dplane, int dw, int dh, int wrap)
+{
+    __shared__ int32_t sv[C][RIH][RIW];
+    __shared__ int32_t hv[C][RIH][RTW];
+
+    const int X0 = blockIdx.x * RTW, Y0 = blockIdx.y * RTH;
+    const int gx0 = 2 * X0 - 2, gy0 = 2 * Y0 - 2;
+    const int tid = threadIdx.x;
+
+    for (int i = tid; i < RIH * RIW; i += 256) {
+        const int r = i / RIW, c = i - r * RIW;
+        const int gy = min(max(gy0 + r, 0), sh - 1);
+        int gx = gx0 + c;
+        gx = wrap ? imod(gx, sw) : min(max(gx, 0), sw - 1);
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) {
+            sv[ch][r][c] = (int32_t)src[(int64_t)ch * splane + (int64_t)gy * spitch + gx];
+        }
+    }
+    __syncthreads();
+
+    for (int i = tid; i < RIH * RTW; i += 256) {
+        const int r = i / RTW, j = i - r * RTW;
+        const int c0 = 2 * j;
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) {
+            hv[ch][r][j] = sv[ch][r][c0] + 4 * sv[ch][r][c0 + 1] + 6 * sv[ch][r][c0 + 2] +
+                           4 * sv[ch][r][c0 + 3] + sv[ch][r][c0 + 4];
+        }
+    }
+    __syncthreads();
+
+    const int tx = tid % RTW, ty = tid / RTW;
+    const int X = X0 + tx, Y = Y0 + ty;
+    if (X >= dw || Y >= dh) {
+        return;
+    }
+    const int r0 = 2 * ty;
+#pragma unroll
+    for (int ch = 0; ch < C; ++ch) {
+        const int32_t num = hv[ch][r0][tx] + 4 * hv[ch][r0 + 1][tx] + 6 * hv[ch][r0 + 2][tx] +
+                            4 * hv[ch][r0 + 3][tx] + hv[ch][r0 + 4][tx];
+        dst[(int64_t)ch * dplane + (int64_t)Y * dpitch + X] = cast_store<TD>(num / 256);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Expand (src/pyramid.h:875-1457)
+// ---------------------------------------------------------------------------
+//
+// Destination pixel (X, Y) is a separable interpolation of the source:
+// horizontally (1,6,1) at even X and (4,4) at odd X, vertically (1,6,1) at
+// even Y and (1,1) at odd Y, divided by the product of the in-image weight
+// sums (64 or 16 inside the image; 56, 49, 14, 8, ... at the borders).  One
+// thread handles the 2x2 destination quad of one source pixel.
+
+constexpr int ETW = 64, ETH = 16;
+constexpr int ESW = ETW / 2 + 2, ESH = ETH / 2 + 2;
+
+// Horizontal weights on source offsets (-1, 0, +1) of destination column X
+// and their divisor; see the SKIPSM scale tables at src/pyramid.h:1227-1411.
+__device__ __forceinline__ void expand_hweights(int X, int sw, int dw, int wrap, int w[3], int& den)
+{
+    const int i = X >> 1;
+    if ((X & 1) == 0) {
+        if (wrap && sw == 1) {
+            // single source column: the wrapped left state joins the
+            // numerator over the plain divisor (src/pyramid.h:1233-1236,1304-1307)
+            w[0] = 0;
+            w[1] = (dw & 1) ? 10 : 7;
+            w[2] = 0;
+            den = 6;
+            return;
+        }
+        w[0] = 1;
+        w[1] = 6;
+        w[2] = 1;
+        if (wrap) {
+            if (dw & 1) {
+                if (i == 0) {
+                    w[0] = 4;
+                }
+                if (i == sw - 1) {
+                    w[2] = 4;
+                }
+            }
+        } else {
+            if (i == 0) {
+                w[0] = 0;
+            }
+            if (i + 1 >= sw) {
+                w[2] = 0;
+            }
+        }
+    } else {
+        w[0] = 0;
+        w[1] = 4;
+        w[2] = (i + 1 < sw || (wrap && sw > 1)) ? 4 : 0;
+    }
+    den = w[0] + w[1] + w[2];
+}
+
+__device__ __forceinline__ void expand_vweights(int Y, int sh, int w[3], int& den)
+{
+    const int j = Y >> 1;
+    if ((Y & 1) == 0) {
+        w[0] = j > 0 ? 1 : 0;
+        w[1] = 6;
+        w[2] = j + 1 < sh ? 1 : 0;
+    } else {
+        w[0] = 0;
+        w[1] = 1;
+        w[2] = j + 1 < sh ? 1 : 0;
+    }
+    den = w[0] + w[1] + w[2];
+}
+
+template <typename T, bool ADD>
+__device__ __forceinline__ void expand_combine(T* d, int32_t e)
+{
+    if (ADD) {
+        *d = sat_store<T>((int32_t)*d + e);
+    } else {
+        *d = cast_store<T>((int64_t)*d - e);
+    }
+}
+
+__device__ __forceinline__ int32_t div_den(int32_t num, int den)
+{
+    if (den == 64) {
+        return num / 64;
+    }
+    if (den == 16) {
+        return num / 16;
+    }
+    return num / den;
+}
+
+template <typename T, int C, bool ADD>
+__global__ void __launch_bounds__(256) k_expand(const T* __restrict__ src, int64_t spitch, int64_t splane, int sw,
+                                                int sh, T* __restrict__ dst, int64_t dpitch, int64_t dplane, int dw,
+                                                int dh, int wrap)
+{
+    __shared__ int32_t ss[C][ESH][ESW];
+    const int X0 = blockIdx.x * ETW, Y0 = blockIdx.y * ETH;
+    const int I0 = X0 >> 1, J0 = Y0 >> 1;
+    const int tid = threadIdx.x;
+
+    for (int k = tid; k < ESH * ESW; k += 256) {
+        const int r = k / ESW, c = k - r * ESW;
+        const int j = J0 - 1 + r;
+        int i = I0 - 1 + c;
+        if (wrap) {
+            i = imod(i, sw);
+        }
+        const bool in = j >= 0 && j < sh && i >= 0 && i < sw;
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) {
+            ss[ch][r][c] = in ? (int32_t)src[(int64_t)ch * splane + (int64_t)j * spitch + i] : 0;
+        }
+    }
+    __syncthreads();
+
+    const int qx = tid % 32, qy = tid / 32;
+    const int i = I0 + qx, j = J0 + qy;
+    const int X = 2 * i, Y = 2 * j;
+    if (X >= dw || Y >= dh) {
+        return;
+    }
+    const bool has_x1 = X + 1 < dw, has_y1 = Y + 1 < dh;
+    const bool interior = i >= 1 && i + 1 < sw && j >= 1 && j + 1 < sh;
+
+    if (interior) {
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) {
+            const int32_t* a = &ss[ch][qy][qx];
+            const int32_t* b = &ss[ch][qy + 1][qx];
+            const int32_t* c = &ss[ch][qy + 2][qx];
+            const int32_t hea = a[0] + 6 * a[1] + a[2], heb = b[0] + 6 * b[1] + b[2], hec = c[0] + 6 * c[1] + c[2];
+            const int32_t hoa = 4 * (a[1] + a[2]), hob = 4 * (b[1] + b[2]), hoc = 4 * (c[1] + c[2]);
+            T* d0 = reinterpret_cast<T*>(dst) + (int64_t)ch * dplane + (int64_t)Y * dpitch + X;
+            expand_combine<T, ADD>(d0, (hea + 6 * heb + hec) / 64);
+            if (has_x1) {
+                expand_combine<T, ADD>(d0 + 1, (hoa + 6 * hob + hoc) / 64);
+            }
+            if (has_y1) {
+                T* d1 = d0 + dpitch;
+                expand_combine<T, ADD>(d1, (heb + hec) / 16);
+                if (has_x1) {
+                    expand_combine<T, ADD>(d1 + 1, (hob + hoc) / 16);
+                }
+            }
+        }
+        return;
+    }
+
+    // Border quads: per-position weights and divisors.
+#pragma unroll
+    for (int oy = 0; oy < 2; ++oy) {
+        const int YY = Y + oy;
+        if (YY >= dh) {
+            continue;
+        }
+        int vw[3], vden;
+        expand_vweights(YY, sh, vw, vden);
+#pragma unroll
+        for (int ox = 0; ox < 2; ++ox) {
+            const int XX = X + ox;
+            if (XX >= dw) {
+                continue;
+            }
+            int hw[3], hden;
+            expand_hweights(XX, sw, dw, wrap, hw, hden);
+            const int den = hden * vden;
+#pragma unroll
+            for (int ch = 0; ch < C; ++ch) {
+                int32_t num = 0;
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    const int32_t* row = &ss[ch][qy + a][qx];
+                    num += vw[a] * (hw[0] * row[0] + hw[1] * row[1] + hw[2] * row[2]);
+                }
+                T* d = reinterpret_cast<T*>(dst) + (int64_t)ch * dplane + (int64_t)YY * dpitch + XX;
+                expand_combine<T, ADD>(d, div_den(num, den));
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Merge operators
+// ---------------------------------------------------------------------------
+
+// CartesianBlendFunctor (src/blend.h:41-76).  mask >= white_value and
+// mask <= 0 are the coefficient tests 1.0 / 0.0 decided exactly on integers;
+// the mixed case is the reference's double expression.
+template <typename T, typename TM, int C>
+__global__ void __launch_bounds__(256) k_blend(const TM* __restrict__ mask, int64_t mpitch,
+                                               const T* __restrict__ white, int64_t wpitch, int64_t wplane,
+                                               T* __restrict__ black, int64_t bpitch, int64_t bplane, int w,
+                                               int h, int32_t white_value)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= w) {
+        return;
+    }
+    const int32_t m = (int32_t)mask[(int64_t)y * mpitch + x];
+    if (m <= 0) {
+        return;
+    }
+    if (m >= white_value) {
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            black[(int64_t)c * bplane + (int64_t)y * bpitch + x] = white[(int64_t)c * wplane + (int64_t)y * wpitch + x];
+        }
+        return;
+    }
+    const double wc = __ddiv_rn((double)m, (double)white_value);
+    const double bc = __dadd_rn(1.0, -wc);
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        T* b = &black[(int64_t)c * bplane + (int64_t)y * bpitch + x];
+        const double v = __dadd_rn(__dmul_rn(wc, (double)white[(int64_t)c * wplane + (int64_t)y * wpitch + x]),
+                                   __dmul_rn(bc, (double)*b));
+        *b = frp_store<T>(v);
+    }
+}
+
+// fromRealPromote(lp * fl(m / D)) with D = 255 * 2^F (src/enfuse.h:601-620).
+//
+// For 0 < m < D the exact value t = lp*m/D has denominator 2D after adding
+// 1/2, so its distance to the rounding boundary is either 0 or >= 1/(2D);
+// the double expression differs from t by < 2^-26, which is smaller.  Hence
+// round-half-away(t) is the reference's result unless t is exactly a
+// half-integer, in which case the double expression is evaluated as is.
+template <typename T, int F>
+__device__ __forceinline__ T mask_multiply(int32_t lp, int32_t m)
+{
+    constexpr int32_t D = 255 << F;
+    if (m == 0) {
+        return (T)0;  // lp * 0.0 rounds to 0
+    }
+    if (m == D) {
+        return (T)lp;  // coefficient exactly 1.0
+    }
+    const uint32_t a = lp < 0 ? (uint32_t)(-(int64_t)lp) : (uint32_t)lp;
+    if (m > 0 && m < D && a < (1u << 24)) {
+        const uint64_t N = 2ull * (uint64_t)a * (uint64_t)m + (uint64_t)D;
+        const uint32_t hi = (uint32_t)(N >> (F + 1));
+        const uint32_t lo = (uint32_t)(N & ((1ull << (F + 1)) - 1));
+        const uint32_t q = hi / 255u;
+        const bool tie = lo == 0 && hi == q * 255u;
+        if (!tie) {
+            const int32_t r = lp < 0 ? -(int32_t)q : (int32_t)q;
+            return sizeof(T) == 2 ? (T)min(max(r, -32768), 32767) : (T)r;
+        }
+    }
+    const double coeff = __ddiv_rn((double)m, (double)D);
+    return frp_store<T>(__dmul_rn((double)lp, coeff));
+}
+
+template <typename T, typename TM, int C, int F>
+__global__ void __launch_bounds__(256) k_mask_mul_acc(const T* __restrict__ lp, int64_t lpitch, int64_t lplane,
+                                                      const TM* __restrict__ mask, int64_t mpitch,
+                                                      T* __restrict__ res, int64_t rpitch, int64_t rplane, int w,
+                                                      int h, int accumulate)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= w) {
+        return;
+    }
+    const int32_t m = (int32_t)mask[(int64_t)y * mpitch + x];
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        const T v = mask_multiply<T, F>((int32_t)lp[(int64_t)c * lplane + (int64_t)y * lpitch + x], m);
+        T* r = &res[(int64_t)c * rplane + (int64_t)y * rpitch + x];
+        *r = accumulate ? cast_store<T>((int64_t)*r + v) : v;
+    }
+}
+
+// Generic (non-constant divisor) variant for the primitive entry point.
+template <typename T, typename TM, int C>
+__global__ void __launch_bounds__(256) k_mask_mul_acc_generic(const T* __restrict__ lp, int64_t lpitch,
+                                                              int64_t lplane, const TM* __restrict__ mask,
+                                                              int64_t mpitch, int32_t divisor,
+                                                              T* __restrict__ res, int64_t rpitch, int64_t rplane,
+                                                              int w, int h, int accumulate)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= w) {
+        return;
+    }
+    const double coeff = __ddiv_rn((double)mask[(int64_t)y * mpitch + x], (double)divisor);
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        const T v = frp_store<T>(__dmul_rn((double)lp[(int64_t)c * lplane + (int64_t)y * lpitch + x], coeff));
+        T* r = &res[(int64_t)c * rplane + (int64_t)y * rpitch + x];
+        *r = accumulate ? cast_store<T>((int64_t)*r + v) : v;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Conversion from fixed point (src/fixmath.h:241-277)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t mix32(uint32_t x)
+{
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+// Counter-based random bits of sample `index` (same rule as the oracle).
+__device__ __forceinline__ uint32_t dither_bits(uint64_t seed, uint64_t index)
+{
+    const uint32_t hi = mix32((uint32_t)(index >> 32) ^ (uint32_t)(seed >> 32) ^ 0x9e3779b9u);
+    return mix32((uint32_t)index ^ (uint32_t)seed ^ hi);
+}
+
+template <typename TS, typename TD>
+__global__ void __launch_bounds__(256) k_from_fixed(const TS* __restrict__ src, int64_t spitch, int64_t splane, int C,
+                                                    const uint8_t* __restrict__ alpha, int64_t apitch,
+                                                    TD* __restrict__ dst, int64_t dpitch, int dstride, int w, int h,
+                                                    int frac, int dither, uint64_t seed, int32_t maxv)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= w || !alpha[(int64_t)y * apitch + x]) {
+        return;
+    }
+    const int32_t half_m1 = (1 << (frac - 1)) - 1;
+    const int32_t quarter = 1 << (frac - 2);
+    const int32_t three_quarter = 3 << (frac - 2);
+    const int32_t half = 1 << (frac - 1);
+    const uint64_t pix = (uint64_t)y * (uint64_t)w + (uint64_t)x;
+    for (int c = 0; c < C; ++c) {
+        const int32_t v = (int32_t)src[(int64_t)c * splane + (int64_t)y * spitch + x];
+        const int32_t q = v >> frac;
+        const int32_t f = v & ((1 << frac) - 1);
+        int32_t r;
+        if (dither == ENB_DITHER_NEAREST) {
+            r = f >= half ? q + 1 : q;
+        } else if (f >= quarter && f < three_quarter) {
+            const int32_t rnd = (int32_t)(dither_bits(seed, pix * (uint64_t)C + (uint64_t)c) & (uint32_t)half_m1) + quarter;
+            r = rnd <= f ? q + 1 : q;
+        } else {
+            r = f >= quarter ? q + 1 : q;
+        }
+        r = min(max(r, 0), maxv);
+        dst[(int64_t)y * dpitch + (int64_t)x * dstride + c] = (TD)r;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_copy_pixels(const T* __restrict__ src, int64_t spitch,
+                                                     T* __restrict__ dst, int64_t dpitch, int rowlen, int h)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x < rowlen) {
+        dst[(int64_t)y * dpitch + x] = src[(int64_t)y * spitch + x];
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_copy_level0(const T* __restrict__ src, int64_t spitch, int64_t splane,
+                                                     int C, int32_t* __restrict__ dst, int w, int h)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= w) {
+        return;
+    }
+    for (int c = 0; c < C; ++c) {
+        dst[((int64_t)y * w + x) * C + c] = (int32_t)src[(int64_t)c * splane + (int64_t)y * spitch + x];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// enfuse weights (src/enfuse.h:962-1212)
+// ---------------------------------------------------------------------------
+
+constexpr int WT = 16;  // 16x16 weight pixels per CTA
+
+// MultiGrayscaleAccessor::project for integer RGB (src/mga.h:185-222):
+// average = fromRealPromote((r+g+b)/3.0) = (r+g+b+1)/3 and lightness =
+// fromRealPromote((min+max)/2.0) = (min+max+1)/2 exactly for non-negative
+// integers; luminance and the mixer evaluate the reference's double sums.
+__device__ __forceinline__ int32_t gray_of(const WeightParams& wp, uint32_t r, uint32_t g, uint32_t b)
+{
+    switch (wp.gray_projector) {
+    case ENB_GRAY_VALUE: return (int32_t)max(r, max(g, b));
+    case ENB_GRAY_ANTI_VALUE: return (int32_t)min(r, min(g, b));
+    case ENB_GRAY_LIGHTNESS: return (int32_t)((min(r, min(g, b)) + max(r, max(g, b)) + 1) >> 1);
+    case ENB_GRAY_LUMINANCE: {
+        const double s = __dadd_rn(__dadd_rn(__dmul_rn(0.3, (double)r), __dmul_rn(0.59, (double)g)),
+                                   __dmul_rn(0.11, (double)b));
+        return (int32_t)frp_unsigned(s, wp.maxv);
+    }
+    case ENB_GRAY_MIXER: {
+        const double s = __dadd_rn(__dadd_rn(__dmul_rn(wp.mixer[0], (double)r), __dmul_rn(wp.mixer[1], (double)g)),
+                                   __dmul_rn(wp.mixer[2], (double)b));
+        return (int32_t)frp_unsigned(s, wp.maxv);
+    }
+    default: return (int32_t)((r + g + b + 1u) / 3u);
+    }
+}
+
+// fromRealPromote(sqrt((Q - S*S/n) / (n-1))) of the window sums
+// (src/enfuse.h:154-160).  The exact value sqrt((nQ - S^2)/(n(n-1))) is
+// approximated in float (error < 0.01); unless it lies within 0.03 of a
+// rounding boundary that decides the integer, otherwise the reference's
+// double expression is evaluated.
+__device__ __forceinline__ int32_t stddev_round(int64_t S, int64_t Q, int n)
+{
+    if (n <= 1) {
+        return 0;
+    }
+    const int64_t num = (int64_t)n * Q - S * S;
+    const float r = sqrtf(__fdiv_rn((float)num, (float)(n * (n - 1))));
+    const float x = r + 0.5f;
+    const float fl = floorf(x);
+    const float d = x - fl;
+    if (d > 0.03f && d < 0.97f) {
+        return (int32_t)fl;
+    }
+    const double sum = (double)S;
+    const double var = __ddiv_rn(__dadd_rn((double)Q, -__ddiv_rn(__dmul_rn(sum, sum), (double)n)), (double)(n - 1));
+    const double sd = __dsqrt_rn(var);
+    return __double2int_rz(__dadd_rn(sd, 0.5));
+}
+
+// Histogram::entropyOfChannel of n sorted samples (src/enfuse.h:346-375),
+// scaled by the channel maximum and rounded (Histogram::entropyFun).  The
+// sum of p log p is accumulated exactly in 2^-56 fixed point for a float
+// estimate; near a rounding boundary the reference's double sum (bins in
+// ascending key order) is evaluated.
+__device__ int32_t entropy_round(const uint16_t* v, int n, const WeightTables& tab, int nmax, uint32_t maxv)
+{
+    if (n == 0) {
+        return 0;
+    }
+    int bins = 0;
+    long long acc = 0;
+    const long long* fx = tab.plogp_fx + (int64_t)n * (nmax + 1);
+    int i = 0;
+    while (i < n) {
+        int j = i + 1;
+        while (j < n && v[j] == v[i]) {
+            ++j;
+        }
+        acc += fx[j - i];
+        ++bins;
+        i = j;
+    }
+    if (bins <= 1) {
+        return 0;
+    }
+    const float e = -(float)acc * 1.3877787807814457e-17f;  // 2^-56
+    const float val = __fmul_rn(e, tab.scale_logb[bins]);
+    const float x = val + 0.5f;
+    const float fl = floorf(x);
+    const float d = x - fl;
+    if (d > 0.03f && d < 0.97f) {
+        return (int32_t)min((uint32_t)max(fl, 0.0f), maxv);
+    }
+    const double* pl = tab.plogp + (int64_t)n * (nmax + 1);
+    double es = 0.0;
+    i = 0;
+    while (i < n) {
+        int j = i + 1;
+        while (j < n && v[j] == v[i]) {
+            ++j;
+        }
+        es = __dadd_rn(es, pl[j - i]);
+        i = j;
+    }
+    const double H = __ddiv_rn(-es, tab.logb[bins]);
+    return (int32_t)frp_unsigned(__dmul_rn(H, (double)maxv), maxv);
+}
+
+// (float)(w * s) with s = fl(d / S) in double, d < S integers
+// (SaturationFunctor, src/enfuse.h:755-776), via a float-float product;
+// near a float rounding midpoint the double expression is evaluated.
+__device__ __forceinline__ float saturation_weight(const WeightParams& wp, uint32_t d, uint32_t S)
+{
+    const float fd = (float)d, fS = (float)S;
+    const float q1 = __fdiv_rn(fd, fS);
+    const float rem = __fmaf_rn(-q1, fS, fd);       // exact remainder
+    const float q2 = __fdiv_rn(rem, fS);
+    const float p_hi = __fmul_rn(wp.w_sat_hi, q1);
+    const float e1 = __fmaf_rn(wp.w_sat_hi, q1, -p_hi);
+    const float p_lo = __fadd_rn(e1, __fadd_rn(__fmul_rn(wp.w_sat_hi, q2), __fmul_rn(wp.w_sat_lo, q1)));
+    const float s = __fadd_rn(p_hi, p_lo);
+    // residual of the float-float value against its rounding s
+    const float t = __fadd_rn(__fadd_rn(p_hi, -s), p_lo);
+    const float ulp = __int_as_float(__float_as_int(s) + 1) - s;
+    const float dist = fabsf(fabsf(t) - 0.5f * ulp);
+    const bool pow2 = (__float_as_int(s) & 0x7fffff) == 0;  // ulp below s is half as large
+    if (dist > 1.0e-5f * ulp && s > 1.0e-30f && !pow2) {
+        return s;
+    }
+    const double sd = __ddiv_rn((double)d, (double)S);
+    return (float)__dmul_rn(wp.w_saturation, sd);
+}
+
+__global__ void __launch_bounds__(256) k_enfuse_mask(PixelView img, AlphaSrc alpha, WeightParams wp,
+                                                     WeightTables tab, float* __restrict__ out, int64_t opitch)
+{
+    extern __shared__ unsigned char smem[];
+    const int halo = max(wp.use_contrast ? wp.contrast_window / 2 : 0, wp.use_entropy ? wp.entropy_window / 2 : 0);
+    const int TW = WT + 2 * halo;
+    int32_t* s_gray = reinterpret_cast<int32_t*>(smem);
+    uint16_t* s_raw = reinterpret_cast<uint16_t*>(s_gray + TW * TW);   // [C][TW*TW]
+    uint8_t* s_a = reinterpret_cast<uint8_t*>(s_raw + 3 * TW * TW);
+
+    const int x0 = blockIdx.x * WT - halo, y0 = blockIdx.y * WT - halo;
+    const int w = img.w, h = img.h, C = img.C;
+    for (int k = threadIdx.x; k < TW * TW; k += blockDim.x) {
+        const int r = k / TW, c = k - r * TW;
+        const int gx = x0 + c, gy = y0 + r;
+        int32_t g = 0;
+        uint8_t a = 0;
+        uint32_t rgb[3] = {0, 0, 0};
+        if (gx >= 0 && gx < w && gy >= 0 && gy < h) {
+            const int64_t base = (int64_t)gy * img.pitch + (int64_t)gx * img.stride;
+            for (int ch = 0; ch < C; ++ch) {
+                rgb[ch] = load_sample(img.p, img.dtype, base + ch);
+            }
+            g = C == 1 ? (int32_t)rgb[0] : gray_of(wp, rgb[0], rgb[1], rgb[2]);
+            a = (uint8_t)alpha_at(alpha, gx, gy);
+        }
+        s_gray[k] = g;
+        s_a[k] = a;
+        for (int ch = 0; ch < 3; ++ch) {
+            s_raw[ch * TW * TW + k] = (uint16_t)rgb[ch];
+        }
+    }
+    __syncthreads();
+
+    const int lx = threadIdx.x % WT, ly = threadIdx.x / WT;
+    const int x = blockIdx.x * WT + lx, y = blockIdx.y * WT + ly;
+    if (x >= w || y >= h) {
+        return;
+    }
+    const int ci = (ly + halo) * TW + (lx + halo);
+    float result = 0.0f;
+    if (s_a[ci]) {
+        const int32_t g = s_gray[ci];
+        if (wp.use_exposure) {
+            result = tab.exposure[g];
+        }
+        if (wp.use_contrast) {
+            const int b = wp.contrast_window / 2;
+            uint32_t gc = 0;
+            if (x >= b && x < w - b && y >= b && y < h - b) {
+                int64_t S = 0, Q = 0;
+                int n = 0;
+                for (int dy = -b; dy <= b; ++dy) {
+                    const int row = (ly + halo + dy) * TW + lx + halo;
+                    for (int dx = -b; dx <= b; ++dx) {
+                        if (s_a[row + dx]) {
+                            const int64_t v = s_gray[row + dx];
+                            S += v;
+                            Q += v * v;
+                            ++n;
+                        }
+                    }
+                }
+                // the combine lambda receives the gradient as the pixel's scalar type
+                gc = (uint32_t)stddev_round(S, Q, n) & wp.maxv;
+            }
+            result = __fadd_rn(tab.contrast[gc], result);
+        }
+        if (wp.use_saturation && C == 3) {
+            const uint32_t r = s_raw[ci], gg = s_raw[TW * TW + ci], bb = s_raw[2 * TW * TW + ci];
+            const uint32_t mx = max(r, max(gg, bb)), mn = min(r, min(gg, bb));
+            float sw = 0.0f;
+            if (mx != mn) {
+                const uint32_t sum = mx + mn;
+                const uint32_t S = sum <= wp.maxv ? sum : 2u * wp.maxv - sum;
+                sw = saturation_weight(wp, mx - mn, S);
+            }
+            result = __fadd_rn(sw, result);
+        }
+        if (wp.use_entropy) {
+            const int b = wp.entropy_window / 2;
+            uint32_t emin = 0;
+            if (x >= b && x < w - b && y >= b && y < h - b) {
+                uint16_t vals[kMaxEntropyWindow * kMaxEntropyWindow];
+                const int nmax = wp.entropy_window * wp.entropy_window;
+                emin = wp.maxv;
+                for (int ch = 0; ch < C; ++ch) {
+                    int n = 0;
+                    for (int dy = -b; dy <= b; ++dy) {
+                        const int row = (ly + halo + dy) * TW + lx + halo;
+                        for (int dx = -b; dx <= b; ++dx) {
+                            if (s_a[row + dx]) {
+                                // insertion into the sorted prefix
+                                const uint16_t v = s_raw[ch * TW * TW + row + dx];
+                                int p = n++;
+                                while (p > 0 && vals[p - 1] > v) {
+                                    vals[p] = vals[p - 1];
+                                    --p;
+                                }
+                                vals[p] = v;
+                            }
+                        }
+                    }
+                    const uint32_t e = (uint32_t)entropy_round(vals, n, tab, nmax, wp.maxv);
+                    emin = min(emin, e);
+                }
+            }
+            result = __fadd_rn(tab.entropy[emin], result);
+        }
+    }
+    out[(int64_t)y * opitch + x] = result;
+}
+
+__global__ void __launch_bounds__(256) k_norm_accumulate(const float* __restrict__ m, int64_t mpitch,
+                                                         float* __restrict__ norm, int64_t npitch, int w, int h,
+                                                         int first)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= w) {
+        return;
+    }
+    const float v = m[(int64_t)y * mpitch + x];
+    float* n = &norm[(int64_t)y * npitch + x];
+    *n = first ? __fadd_rn(v, 0.0f) : __fadd_rn(v, *n);
+}
+
+__global__ void __launch_bounds__(256) k_union_alpha(const uint8_t* __restrict__ a, int64_t apitch,
+                                                     uint8_t* __restrict__ u, int64_t upitch, int w, int h,
+                                                     int first)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= w) {
+        return;
+    }
+    const uint8_t v = a[(int64_t)y * apitch + x];
+    uint8_t* d = &u[(int64_t)y * upitch + x];
+    if (first) {
+        *d = v;
+    } else if (v) {
+        *d = v;
+    }
+}
+
+constexpr int kMaxHardMasks = 64;
+struct HardMaskArgs {
+    float* p[kMaxHardMasks];
+    int64_t pitch[kMaxHardMasks];
+};
+
+// Hard mask: argmax (first maximum) -> 255, others 0; all-zero -> 255/K
+// (src/enfuse.h:1402-1442).
+__global__ void __launch_bounds__(256) k_hard_mask(HardMaskArgs m, int K, int w, int h)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= w) {
+        return;
+    }
+    float mx = 0.0f;
+    int mi = 0;
+    for (int k = 0; k < K; ++k) {
+        const float v = m.p[k][(int64_t)y * m.pitch[k] + x];
+        if (v > mx) {
+            mx = v;
+            mi = k;
+        }
+    }
+    const float fallback = __fdiv_rn(255.0f, (float)K);
+    for (int k = 0; k < K; ++k) {
+        m.p[k][(int64_t)y * m.pitch[k] + x] = mx == 0.0f ? fallback : (k == mi ? 255.0f : 0.0f);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+
+static inline dim3 row_grid(int w, int h) { return dim3((unsigned)((w + 255) / 256), (unsigned)h); }
+
+LaunchInfo& last_launch()
+{
+    static thread_local LaunchInfo li{"", 0.0};
+    return li;
+}
+
+static inline double esz(int dt) { return dt == ENB_U8 ? 1.0 : ((dt == ENB_U16 || dt == ENB_I16) ? 2.0 : 4.0); }
+static inline double npix(int w, int h) { return (double)w * (double)h; }
+static inline double planar_bytes(const PlanarView& v) { return npix(v.w, v.h) * v.C * esz(v.dtype); }
+static inline void note(const char* name, double bytes) { last_launch() = LaunchInfo{name, bytes}; }
+
+cudaError_t launch_to_fixed(const PixelView& s, const PlanarView& d, int frac, cudaStream_t st)
+{
+    note("to_fixed", npix(s.w, s.h) * s.C * esz(s.dtype) + planar_bytes(d));
+    const dim3 g = row_grid(s.w, s.h);
+    if (s.dtype == ENB_U8 && d.dtype == ENB_I16) {
+        k_to_fixed<uint8_t, int16_t><<<g, 256, 0, st>>>((const uint8_t*)s.p, s.pitch, s.stride, s.C, (int16_t*)d.p,
+                                                        d.pitch, d.plane, s.w, s.h, frac);
+    } else if (s.dtype == ENB_U8 && d.dtype == ENB_I32) {
+        k_to_fixed<uint8_t, int32_t><<<g, 256, 0, st>>>((const uint8_t*)s.p, s.pitch, s.stride, s.C, (int32_t*)d.p,
+                                                        d.pitch, d.plane, s.w, s.h, frac);
+    } else if (s.dtype == ENB_U16 && d.dtype == ENB_I32) {
+        k_to_fixed<uint16_t, int32_t><<<g, 256, 0, st>>>((const uint16_t*)s.p, s.pitch, s.stride, s.C,
+                                                         (int32_t*)d.p, d.pitch, d.plane, s.w, s.h, frac);
+    } else if (s.dtype == ENB_U16 && d.dtype == ENB_I16) {
+        k_to_fixed<uint16_t, int16_t><<<g, 256, 0, st>>>((const uint16_t*)s.p, s.pitch, s.stride, s.C,
+                                                         (int16_t*)d.p, d.pitch, d.plane, s.w, s.h, frac);
+    } else {
+        return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bytes_to_fixed(const BytePlane& s, const PlanarView& d, int frac, cudaStream_t st)
+{
+    note("bytes_to_fixed", npix(s.w, s.h) + planar_bytes(d));
+    const dim3 g = row_grid(s.w, s.h);
+    if (d.dtype == ENB_I16) {
+        k_bytes_to_fixed<int16_t><<<g, 256, 0, st>>>(s.p, s.pitch, (int16_t*)d.p, d.pitch, s.w, s.h, frac);
+    } else {
+        k_bytes_to_fixed<int32_t><<<g, 256, 0, st>>>(s.p, s.pitch, (int32_t*)d.p, d.pitch, s.w, s.h, frac);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_float_to_fixed(const FloatPlane& s, const PlanarView& d, int frac, cudaStream_t st)
+{
+    note("float_to_fixed", 4.0 * npix(s.w, s.h) + planar_bytes(d));
+    const dim3 g = row_grid(s.w, s.h);
+    if (d.dtype == ENB_I16) {
+        k_float_to_fixed<int16_t><<<g, 256, 0, st>>>(s.p, s.pitch, (int16_t*)d.p, d.pitch, s.w, s.h, frac);
+    } else {
+        k_float_to_fixed<int32_t><<<g, 256, 0, st>>>(s.p, s.pitch, (int32_t*)d.p, d.pitch, s.w, s.h, frac);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_soft_mask_to_fixed(const FloatPlane& m, const FloatPlane& n, int K, const PlanarView& d,
+                                      int frac, cudaStream_t st)
+{
+    note("soft_mask_to_fixed", 8.0 * npix(m.w, m.h) + planar_bytes(d));
+    const dim3 g = row_grid(m.w, m.h);
+    const float fallback = (float)(255 / K);  // integer division, src/enfuse.h:1534
+    if (d.dtype == ENB_I16) {
+        k_soft_mask_to_fixed<int16_t><<<g, 256, 0, st>>>(m.p, m.pitch, n.p, n.pitch, fallback, (int16_t*)d.p, d.pitch,
+                                                         m.w, m.h, frac);
+    } else {
+        k_soft_mask_to_fixed<int32_t><<<g, 256, 0, st>>>(m.p, m.pitch, n.p, n.pitch, fallback, (int32_t*)d.p, d.pitch,
+                                                         m.w, m.h, frac);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_alpha_extract(const AlphaSrc& a, const BytePlane& d, cudaStream_t st)
+{
+    note("alpha_extract", npix(d.w, d.h) * (a.mode == kAlphaChannel3 ? 1.0 + esz(a.pix.dtype) : 1.0));
+    k_alpha_extract<<<row_grid(d.w, d.h), 256, 0, st>>>(a, d.p, d.pitch, d.w, d.h);
+    return cudaGetLastError();
+}
+
+template <typename TS, typename TD, int C>
+static void reduce_dispatch(int wrap, const PlanarView& s, const BytePlane* sa, const PlanarView& d,
+                            const BytePlane* da, cudaStream_t st)
+{
+    const dim3 g = grid2d(d.w, d.h, RTW, RTH);
+    if (sa) {
+        k_reduce_alpha<TS, TD, C><<<g, 256, 0, st>>>((const TS*)s.p, s.pitch, s.plane, s.w, s.h, sa->p, sa->pitch,
+                                                     (TD*)d.p, d.pitch, d.plane, d.w, d.h, da->p, da->pitch, wrap);
+    } else {
+        k_reduce_noalpha<TS, TD, C><<<g, 256, 0, st>>>((const TS*)s.p, s.pitch, s.plane, s.w, s.h, (TD*)d.p, d.pitch,
+                                                       d.plane, d.w, d.h, wrap);
+    }
+}
+
+cudaError_t launch_reduce(int wrap, const PlanarView& s, const BytePlane* sa, const PlanarView& d,
+                          const BytePlane* da, cudaStream_t st)
+{
+    if (s.dtype != d.dtype || s.C != d.C) {
+        return cudaErrorInvalidValue;
+    }
+    if (sa) {
+        note("reduce_alpha", planar_bytes(s) + npix(s.w, s.h) + planar_bytes(d) + npix(d.w, d.h));
+    } else {
+        note("reduce", planar_bytes(s) + planar_bytes(d));
+    }
+    if (s.dtype == ENB_I16) {
+        if (s.C == 1) {
+            reduce_dispatch<int16_t, int16_t, 1>(wrap, s, sa, d, da, st);
+        } else {
+            reduce_dispatch<int16_t, int16_t, 3>(wrap, s, sa, d, da, st);
+        }
+    } else {
+        if (s.C == 1) {
+            reduce_dispatch<int32_t, int32_t, 1>(wrap, s, sa, d, da, st);
+        } else {
+            reduce_dispatch<int32_t, int32_t, 3>(wrap, s, sa, d, da, st);
+        }
+    }
+    return cudaGetLastError();
+}
+
+template <typename T, int C>
+static void expand_dispatch(int add, int wrap, const PlanarView& s, const PlanarView& d, cudaStream_t st)
+{
+    const dim3 g = grid2d(d.w, d.h, ETW, ETH);
+    if (add) {
+        k_expand<T, C, true><<<g, 256, 0, st>>>((const T*)s.p, s.pitch, s.plane, s.w, s.h, (T*)d.p, d.pitch, d.plane,
+                                                d.w, d.h, wrap);
+    } else {
+        k_expand<T, C, false><<<g, 256, 0, st>>>((const T*)s.p, s.pitch, s.plane, s.w, s.h, (T*)d.p, d.pitch, d.plane,
+                                                 d.w, d.h, wrap);
+    }
+}
+
+cudaError_t launch_expand(int add, int wrap, const PlanarView& s, const PlanarView& d, cudaStream_t st)
+{
+    if (s.dtype != d.dtype || s.C != d.C) {
+        return cudaErrorInvalidValue;
+    }
+    note(add ? "expand_add" : "expand_sub", planar_bytes(s) + 2.0 * planar_bytes(d));
+    if (s.dtype == ENB_I16) {
+        if (s.C == 1) {
+            expand_dispatch<int16_t, 1>(add, wrap, s, d, st);
+        } else {
+            expand_dispatch<int16_t, 3>(add, wrap, s, d, st);
+        }
+    } else {
+        if (s.C == 1) {
+            expand_dispatch<int32_t, 1>(add, wrap, s, d, st);
+        } else {
+            expand_dispatch<int32_t, 3>(add, wrap, s, d, st);
+        }
+    }
+    return cudaGetLastError();
+}
+
+template <typename T, typename TM, int C>
+static void blend_dispatch(const PlanarView& m, const PlanarView& wt, const PlanarView& b, int32_t wv,
+                           cudaStream_t st)
+{
+    k_blend<T, TM, C><<<row_grid(b.w, b.h), 256, 0, st>>>((const TM*)m.p, m.pitch, (const T*)wt.p, wt.pitch, wt.plane,
+                                                          (T*)b.p, b.pitch, b.plane, b.w, b.h, wv);
+}
+
+cudaError_t launch_blend(const PlanarView& m, const PlanarView& wt, const PlanarView& b, int32_t wv,
+                         cudaStream_t st)
+{
+    if (wt.dtype != b.dtype || wt.C != b.C) {
+        return cudaErrorInvalidValue;
+    }
+    note("blend", planar_bytes(m) + planar_bytes(wt) + 2.0 * planar_bytes(b));
+    const bool m16 = m.dtype == ENB_I16;
+    if (b.dtype == ENB_I16) {
+        if (b.C == 1) {
+            m16 ? blend_dispatch<int16_t, int16_t, 1>(m, wt, b, wv, st) : blend_dispatch<int16_t, int32_t, 1>(m, wt, b, wv, st);
+        } else {
+            m16 ? blend_dispatch<int16_t, int16_t, 3>(m, wt, b, wv, st) : blend_dispatch<int16_t, int32_t, 3>(m, wt, b, wv, st);
+        }
+    } else {
+        if (b.C == 1) {
+            m16 ? blend_dispatch<int32_t, int16_t, 1>(m, wt, b, wv, st) : blend_dispatch<int32_t, int32_t, 1>(m, wt, b, wv, st);
+        } else {
+            m16 ? blend_dispatch<int32_t, int16_t, 3>(m, wt, b, wv, st) : blend_dispatch<int32_t, int32_t, 3>(m, wt, b, wv, st);
+        }
+    }
+    return cudaGetLastError();
+}
+
+template <typename T, typename TM, int C>
+static void mma_dispatch(const PlanarView& lp, const PlanarView& m, int32_t divisor, const PlanarView& r, int acc,
+                         cudaStream_t st)
+{
+    const dim3 g = row_grid(lp.w, lp.h);
+    if (divisor == (255 << 15)) {
+        k_mask_mul_acc<T, TM, C, 15><<<g, 256, 0, st>>>((const T*)lp.p, lp.pitch, lp.plane, (const TM*)m.p, m.pitch,
+                                                        (T*)r.p, r.pitch, r.plane, lp.w, lp.h, acc);
+    } else if (divisor == (255 << 7)) {
+        k_mask_mul_acc<T, TM, C, 7><<<g, 256, 0, st>>>((const T*)lp.p, lp.pitch, lp.plane, (const TM*)m.p, m.pitch,
+                                                       (T*)r.p, r.pitch, r.plane, lp.w, lp.h, acc);
+    } else {
+        k_mask_mul_acc_generic<T, TM, C><<<g, 256, 0, st>>>((const T*)lp.p, lp.pitch, lp.plane, (const TM*)m.p,
+                                                            m.pitch, divisor, (T*)r.p, r.pitch, r.plane, lp.w, lp.h,
+                                                            acc);
+    }
+}
+
+cudaError_t launch_mask_mul_acc(const PlanarView& lp, const PlanarView& m, int32_t divisor, const PlanarView& r,
+                                int acc, cudaStream_t st)
+{
+    if (lp.dtype != r.dtype || lp.C != r.C) {
+        return cudaErrorInvalidValue;
+    }
+    note("mask_mul_acc", planar_bytes(lp) + planar_bytes(m) + (acc ? 2.0 : 1.0) * planar_bytes(r));
+    const bool m16 = m.dtype == ENB_I16;
+    if (lp.dtype == ENB_I16) {
+        if (lp.C == 1) {
+            m16 ? mma_dispatch<int16_t, int16_t, 1>(lp, m, divisor, r, acc, st) : mma_dispatch<int16_t, int32_t, 1>(lp, m, divisor, r, acc, st);
+        } else {
+            m16 ? mma_dispatch<int16_t, int16_t, 3>(lp, m, divisor, r, acc, st) : mma_dispatch<int16_t, int32_t, 3>(lp, m, divisor, r, acc, st);
+        }
+    } else {
+        if (lp.C == 1) {
+            m16 ? mma_dispatch<int32_t, int16_t, 1>(lp, m, divisor, r, acc, st) : mma_dispatch<int32_t, int32_t, 1>(lp, m, divisor, r, acc, st);
+        } else {
+            m16 ? mma_dispatch<int32_t, int16_t, 3>(lp, m, divisor, r, acc, st) : mma_dispatch<int32_t, int32_t, 3>(lp, m, divisor, r, acc, st);
+        }
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_from_fixed(const PlanarView& s, const BytePlane& a, void* dst, int64_t dpitch, int ddtype,
+                              int dstride, int frac, int dither, uint64_t seed, cudaStream_t st)
+{
+    note("from_fixed", planar_bytes(s) + npix(s.w, s.h) * (1.0 + s.C * esz(ddtype)));
+    const dim3 g = row_grid(s.w, s.h);
+    if (s.dtype == ENB_I16) {
+        if (ddtype == ENB_U8) {
+            k_from_fixed<int16_t, uint8_t><<<g, 256, 0, st>>>((const int16_t*)s.p, s.pitch, s.plane, s.C, a.p, a.pitch,
+                                                              (uint8_t*)dst, dpitch, dstride, s.w, s.h, frac, dither,
+                                                              seed, 255);
+        } else {
+            k_from_fixed<int16_t, uint16_t><<<g, 256, 0, st>>>((const int16_t*)s.p, s.pitch, s.plane, s.C, a.p, a.pitch,
+                                                               (uint16_t*)dst, dpitch, dstride, s.w, s.h, frac, dither,
+                                                               seed, 65535);
+        }
+    } else {
+        if (ddtype == ENB_U8) {
+            k_from_fixed<int32_t, uint8_t><<<g, 256, 0, st>>>((const int32_t*)s.p, s.pitch, s.plane, s.C, a.p, a.pitch,
+                                                              (uint8_t*)dst, dpitch, dstride, s.w, s.h, frac, dither,
+                                                              seed, 255);
+        } else {
+            k_from_fixed<int32_t, uint16_t><<<g, 256, 0, st>>>((const int32_t*)s.p, s.pitch, s.plane, s.C, a.p, a.pitch,
+                                                               (uint16_t*)dst, dpitch, dstride, s.w, s.h, frac, dither,
+                                                               seed, 65535);
+        }
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_copy_pixels(const PixelView& s, void* dst, int64_t dpitch, cudaStream_t st)
+{
+    const int rowlen = s.w * s.stride;
+    note("copy_pixels", 2.0 * npix(rowlen, s.h) * esz(s.dtype));
+    const dim3 g = row_grid(rowlen, s.h);
+    if (s.dtype == ENB_U8) {
+        k_copy_pixels<uint8_t><<<g, 256, 0, st>>>((const uint8_t*)s.p, s.pitch, (uint8_t*)dst, dpitch, rowlen, s.h);
+    } else {
+        k_copy_pixels<uint16_t><<<g, 256, 0, st>>>((const uint16_t*)s.p, s.pitch, (uint16_t*)dst, dpitch, rowlen, s.h);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_copy_level0(const PlanarView& s, int32_t* dst, cudaStream_t st)
+{
+    note("copy_level0", planar_bytes(s) + 4.0 * npix(s.w, s.h) * s.C);
+    const dim3 g = row_grid(s.w, s.h);
+    if (s.dtype == ENB_I16) {
+        k_copy_level0<int16_t><<<g, 256, 0, st>>>((const int16_t*)s.p, s.pitch, s.plane, s.C, dst, s.w, s.h);
+    } else {
+        k_copy_level0<int32_t><<<g, 256, 0, st>>>((const int32_t*)s.p, s.pitch, s.plane, s.C, dst, s.w, s.h);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_enfuse_mask(const PixelView& img, const AlphaSrc& alpha, const WeightParams& wp,
+                               const WeightTables& tab, const FloatPlane& out, cudaStream_t st)
+{
+    const int halo = max(wp.use_contrast ? wp.contrast_window / 2 : 0, wp.use_entropy ? wp.entropy_window / 2 : 0);
+    const int TW = WT + 2 * halo;
+    const size_t smem = (size_t)TW * TW * (sizeof(int32_t) + 3 * sizeof(uint16_t) + 1);
+    note("enfuse_mask", npix(img.w, img.h) * (img.stride * esz(img.dtype) + (alpha.mode == kAlphaPlane ? 1.0 : 0.0) + 4.0));
+    if (smem > 48 * 1024) {
+        cudaFuncSetAttribute(k_enfuse_mask, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    }
+    k_enfuse_mask<<<grid2d(img.w, img.h, WT, WT), WT * WT, smem, st>>>(img, alpha, wp, tab, out.p, out.pitch);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_norm_accumulate(const FloatPlane& m, const FloatPlane& n, int first, cudaStream_t st)
+{
+    note("norm_accumulate", npix(m.w, m.h) * (first ? 8.0 : 12.0));
+    k_norm_accumulate<<<row_grid(m.w, m.h), 256, 0, st>>>(m.p, m.pitch, n.p, n.pitch, m.w, m.h, first);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_union_alpha(const BytePlane& a, const BytePlane& u, int first, cudaStream_t st)
+{
+    note("union_alpha", npix(a.w, a.h) * (first ? 2.0 : 3.0));
+    k_union_alpha<<<row_grid(a.w, a.h), 256, 0, st>>>(a.p, a.pitch, u.p, u.pitch, a.w, a.h, first);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_hard_mask(const FloatPlane* masks, int K, cudaStream_t st)
+{
+    if (K > kMaxHardMasks) {
+        return cudaErrorInvalidValue;
+    }
+    note("hard_mask", 8.0 * K * npix(masks[0].w, masks[0].h));
+    HardMaskArgs a;
+    for (int k = 0; k < K; ++k) {
+        a.p[k] = masks[k].p;
+        a.pitch[k] = masks[k].pitch;
+    }
+    k_hard_mask<<<row_grid(masks[0].w, masks[0].h), 256, 0, st>>>(a, K, masks[0].w, masks[0].h);
+    return cudaGetLastError();
+}
+
+}  // namespace enb

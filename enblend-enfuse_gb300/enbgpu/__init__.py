@@ -1,0 +1,420 @@
+"""enbgpu -- Python binding of the GB300 enblend/enfuse multiresolution path.
+
+A thin ctypes layer over the C ABI of ``libenbgpu.so`` (``include/enbgpu.h``).
+The names mirror the reference's internal API (``gaussianPyramid``,
+``laplacianPyramid``, ``collapsePyramid``, ``blend``, ``enfuseMask``,
+``enfuseMain``/``enblendMain``) and its command-line weighting options.  Every
+computation runs in the CUDA library; there is no CPU fallback, and importing
+this package fails if the library has not been built.
+
+Arrays: numpy arrays are host buffers (the library copies them on its
+stream); ``torch`` CUDA tensors are used in place.  Pixel images are
+``(H, W, S)`` arrays of uint8/uint16 with S = 3 (RGB) or 4 (RGBA, alpha in
+the 4th component), or ``(H, W)`` for gray; alpha and seam masks are
+``(H, W)`` uint8; weight masks ``(H, W)`` float32.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+from dataclasses import dataclass, field
+from pathlib import Path
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _build
+
+LIB_PATH = _build.LIB_PATH
+HEADER = _build.INCLUDE / "enbgpu.h"
+
+ENB_OK, ENB_ERR_INVALID, ENB_ERR_UNSUPPORTED, ENB_ERR_CUDA, ENB_ERR_NOMEM = range(5)
+ENB_U8, ENB_U16, ENB_F32, ENB_I16, ENB_I32 = range(5)
+DITHER = {"hash": 0, "nearest": 1}
+EXPOSURE_FUNCTIONS = {"gaussian": 0, "lorentzian": 1, "halfsine": 2, "fullsine": 3, "bisquare": 4}
+GRAY_PROJECTORS = {"average": 0, "value": 1, "anti-value": 2, "lightness": 3, "luminance": 4,
+                   "channel-mixer": 5}
+
+
+class EnbError(RuntimeError):
+    """A failed C-ABI call; ``status`` is the enb_status code."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"enbgpu status {status}: {message}")
+        self.status = status
+
+
+class EnbImage(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("pitch", ctypes.c_int64), ("plane_pitch", ctypes.c_int64),
+                ("width", ctypes.c_int32), ("height", ctypes.c_int32), ("channels", ctypes.c_int32),
+                ("pix_stride", ctypes.c_int32), ("dtype", ctypes.c_int32), ("planar", ctypes.c_int32)]
+
+
+class EnbEnfuseParams(ctypes.Structure):
+    _fields_ = [("w_exposure", ctypes.c_double), ("w_saturation", ctypes.c_double),
+                ("w_contrast", ctypes.c_double), ("w_entropy", ctypes.c_double),
+                ("exp_optimum", ctypes.c_double), ("exp_width", ctypes.c_double),
+                ("exp_function", ctypes.c_int32), ("contrast_window", ctypes.c_int32),
+                ("entropy_window", ctypes.c_int32), ("gray_projector", ctypes.c_int32),
+                ("mixer", ctypes.c_double * 3)]
+
+
+class EnbFuseOptions(ctypes.Structure):
+    _fields_ = [("levels", ctypes.c_int32), ("wrap", ctypes.c_int32), ("hard_mask", ctypes.c_int32),
+                ("dither", ctypes.c_int32), ("seed", ctypes.c_uint64), ("host_buffers", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("level0_out", ctypes.c_void_p)]
+
+
+_P = ctypes.POINTER
+_IMG = _P(EnbImage)
+_SIGNATURES = {
+    "enb_abi_version": (ctypes.c_int, []),
+    "enb_create": (ctypes.c_int, [ctypes.c_int, _P(ctypes.c_void_p)]),
+    "enb_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "enb_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "enb_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
+    "enb_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "enb_launch_count": (ctypes.c_uint64, [ctypes.c_void_p]),
+    "enb_default_enfuse_params": (None, [_P(EnbEnfuseParams)]),
+    "enb_default_fuse_options": (None, [_P(EnbFuseOptions)]),
+    "enb_num_levels": (ctypes.c_int, [ctypes.c_int] * 4),
+    "enb_pyramid_create": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.c_int] * 5 + [_P(ctypes.c_void_p)]),
+    "enb_pyramid_free": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "enb_pyramid_levels": (ctypes.c_int, [ctypes.c_void_p]),
+    "enb_pyramid_level": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _IMG]),
+    "enb_pyramid_read_level": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "enb_pyramid_write_level": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "enb_to_pyramid": (ctypes.c_int, [ctypes.c_void_p, _IMG, _IMG, ctypes.c_int]),
+    "enb_reduce": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _IMG, _IMG, _IMG, _IMG]),
+    "enb_expand": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _IMG, _IMG]),
+    "enb_blend": (ctypes.c_int, [ctypes.c_void_p, _IMG, _IMG, _IMG, ctypes.c_int32]),
+    "enb_mask_multiply_accumulate": (ctypes.c_int, [ctypes.c_void_p, _IMG, _IMG, ctypes.c_int32, _IMG, ctypes.c_int]),
+    "enb_from_pyramid": (ctypes.c_int, [ctypes.c_void_p, _IMG, _IMG, _IMG, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_uint64]),
+    "enb_gaussian_pyramid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _IMG, _IMG, ctypes.c_int,
+                                            ctypes.c_void_p]),
+    "enb_laplacian_pyramid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _IMG, _IMG, ctypes.c_int,
+                                             ctypes.c_void_p]),
+    "enb_collapse_pyramid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "enb_blend_pyramids": (ctypes.c_int, [ctypes.c_void_p] * 4 + [ctypes.c_int32]),
+    "enb_enfuse_mask": (ctypes.c_int, [ctypes.c_void_p, _P(EnbEnfuseParams), _IMG, _IMG, _IMG]),
+    "enb_enfuse": (ctypes.c_int, [ctypes.c_void_p, _P(EnbEnfuseParams), ctypes.c_int, _IMG, _IMG, _IMG, _IMG,
+                                  _IMG, _P(EnbFuseOptions)]),
+    "enb_enblend": (ctypes.c_int, [ctypes.c_void_p, _IMG, _IMG, _IMG, _IMG, _IMG, _IMG, _IMG,
+                                   _P(EnbFuseOptions)]),
+}
+
+
+def header_functions() -> list[str]:
+    """Names of the functions declared in include/enbgpu.h."""
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(enb_[a-z0-9_]+)\s*\(", text)))
+
+
+_lib: Optional[ctypes.CDLL] = None
+
+
+def load_library() -> ctypes.CDLL:
+    """Load libenbgpu.so (built by ``_build.build()``); raise if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"{LIB_PATH} is missing: build the CUDA library first (enbgpu._build.build())")
+    lib = ctypes.CDLL(str(LIB_PATH))
+    for name, (res, args) in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+# --------------------------------------------------------------------------
+# descriptors
+# --------------------------------------------------------------------------
+
+_NP_DTYPE = {np.dtype(np.uint8): ENB_U8, np.dtype(np.uint16): ENB_U16, np.dtype(np.float32): ENB_F32,
+             np.dtype(np.int16): ENB_I16, np.dtype(np.int32): ENB_I32}
+
+
+def _is_torch(x) -> bool:
+    return type(x).__module__.startswith("torch")
+
+
+def _dtype_code(x) -> int:
+    if _is_torch(x):
+        import torch
+        m = {torch.uint8: ENB_U8, torch.uint16: ENB_U16, torch.float32: ENB_F32, torch.int16: ENB_I16,
+             torch.int32: ENB_I32}
+        return m[x.dtype]
+    return _NP_DTYPE[np.dtype(x.dtype)]
+
+
+def _ptr_and_strides(x):
+    if _is_torch(x):
+        return x.data_ptr(), [s * x.element_size() for s in x.stride()], x.is_cuda
+    return x.ctypes.data, list(x.strides), False
+
+
+def pixel_image(x, channels: Optional[int] = None) -> EnbImage:
+    """Descriptor of an interleaved (H, W, S) or (H, W) pixel array."""
+    ptr, strides, _ = _ptr_and_strides(x)
+    if x.ndim == 2:
+        h, w = x.shape
+        s = 1
+    else:
+        h, w, s = x.shape
+    es = x.element_size() if _is_torch(x) else x.itemsize
+    if strides[-1] != es or (x.ndim == 3 and strides[1] != s * es):
+        raise ValueError("pixel arrays must be contiguous within a row")
+    c = channels if channels is not None else (3 if s >= 3 else 1)
+    return EnbImage(ptr, strides[0], 0, w, h, c, s, _dtype_code(x), 0)
+
+
+def plane_image(x) -> EnbImage:
+    """Descriptor of an (H, W) plane (alpha, seam mask or weight mask)."""
+    ptr, strides, _ = _ptr_and_strides(x)
+    h, w = x.shape
+    es = x.element_size() if _is_torch(x) else x.itemsize
+    if strides[1] != es:
+        raise ValueError("planes must be contiguous within a row")
+    return EnbImage(ptr, strides[0], 0, w, h, 1, 1, _dtype_code(x), 0)
+
+
+def enfuse_params(exposure_weight: float = 1.0, saturation_weight: float = 0.0, contrast_weight: float = 0.0,
+                  entropy_weight: float = 0.0, exposure_optimum: float = 0.5, exposure_width: float = 0.2,
+                  exposure_weight_function: str = "gaussian", contrast_window_size: int = 5,
+                  entropy_window_size: int = 3, gray_projector: str = "average",
+                  mixer: Sequence[float] = (0.0, 0.0, 0.0)) -> EnbEnfuseParams:
+    """enfuse's weighting options (src/enfuse.cc:117-140, same defaults)."""
+    p = EnbEnfuseParams()
+    p.w_exposure, p.w_saturation = exposure_weight, saturation_weight
+    p.w_contrast, p.w_entropy = contrast_weight, entropy_weight
+    p.exp_optimum, p.exp_width = exposure_optimum, exposure_width
+    p.exp_function = EXPOSURE_FUNCTIONS[exposure_weight_function]
+    p.contrast_window, p.entropy_window = contrast_window_size, entropy_window_size
+    p.gray_projector = GRAY_PROJECTORS[gray_projector]
+    p.mixer[:] = list(mixer)
+    return p
+
+
+# --------------------------------------------------------------------------
+# context
+# --------------------------------------------------------------------------
+
+class Pyramid:
+    """A device-resident pyramid (std::vector<PyramidImageType*> of the reference)."""
+
+    def __init__(self, ctx: "Context", handle: ctypes.c_void_p, dtype: int, channels: int):
+        self.ctx, self.handle, self.dtype, self.channels = ctx, handle, dtype, channels
+
+    @property
+    def levels(self) -> int:
+        return self.ctx.lib.enb_pyramid_levels(self.handle)
+
+    def level_image(self, l: int) -> EnbImage:
+        img = EnbImage()
+        self.ctx._check(self.ctx.lib.enb_pyramid_level(self.handle, l, ctypes.byref(img)))
+        return img
+
+    def read(self, l: int) -> np.ndarray:
+        """Level l as a (C, H, W) int16/int32 array."""
+        img = self.level_image(l)
+        a = np.empty((img.channels, img.height, img.width), np.int16 if self.dtype == ENB_I16 else np.int32)
+        self.ctx._check(self.ctx.lib.enb_pyramid_read_level(self.ctx.handle, self.handle, l, a.ctypes.data))
+        return a
+
+    def write(self, l: int, a: np.ndarray) -> None:
+        img = self.level_image(l)
+        t = np.int16 if self.dtype == ENB_I16 else np.int32
+        a = np.ascontiguousarray(a, dtype=t).reshape(img.channels, img.height, img.width)
+        self.ctx._check(self.ctx.lib.enb_pyramid_write_level(self.ctx.handle, self.handle, l, a.ctypes.data))
+
+    def free(self) -> None:
+        if self.handle:
+            self.ctx.lib.enb_pyramid_free(self.ctx.handle, self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Context:
+    """One CUDA device and stream (enb_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        st = self.lib.enb_create(device, ctypes.byref(h))
+        if st != ENB_OK:
+            raise EnbError(st, "enb_create failed (no usable CUDA device)")
+        self.handle = h
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.enb_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st: int) -> None:
+        if st != ENB_OK:
+            raise EnbError(st, self.lib.enb_last_error(self.handle).decode())
+
+    def set_stream(self, stream_ptr: int) -> None:
+        self._check(self.lib.enb_set_stream(self.handle, ctypes.c_void_p(stream_ptr)))
+
+    def synchronize(self) -> None:
+        self._check(self.lib.enb_synchronize(self.handle))
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.enb_launch_count(self.handle))
+
+    # ---- pyramids ---------------------------------------------------------
+    def pyramid(self, levels: int, width: int, height: int, channels: int, dtype: int) -> Pyramid:
+        h = ctypes.c_void_p()
+        self._check(self.lib.enb_pyramid_create(self.handle, levels, width, height, channels, dtype, ctypes.byref(h)))
+        return Pyramid(self, h, dtype, channels)
+
+    def reduce(self, src: Pyramid, l: int, dst: Pyramid, dl: int, wrap: bool = False,
+               src_alpha=None, dst_alpha=None) -> None:
+        """reduce (src/pyramid.h:166-848) from level l of src into level dl of dst."""
+        si, di = src.level_image(l), dst.level_image(dl)
+        sa = ctypes.byref(plane_image(src_alpha)) if src_alpha is not None else None
+        da = ctypes.byref(plane_image(dst_alpha)) if dst_alpha is not None else None
+        self._check(self.lib.enb_reduce(self.handle, int(wrap), ctypes.byref(si), sa, ctypes.byref(di), da))
+
+    def expand(self, src: Pyramid, l: int, dst: Pyramid, dl: int, add: bool, wrap: bool = False) -> None:
+        """expand (src/pyramid.h:1102-1457) of level l of src into level dl of dst."""
+        si, di = src.level_image(l), dst.level_image(dl)
+        self._check(self.lib.enb_expand(self.handle, int(add), int(wrap), ctypes.byref(si), ctypes.byref(di)))
+
+    def gaussian_pyramid(self, image, levels: int, alpha=None, wrap: bool = False, frac_bits: int = 7,
+                         dtype: Optional[int] = None) -> Pyramid:
+        """gaussianPyramid (src/pyramid.h:1468-1636) of a device image."""
+        img = plane_image(image) if image.ndim == 2 and _dtype_code(image) == ENB_F32 else pixel_image(image)
+        if dtype is None:
+            dtype = ENB_I16 if img.dtype == ENB_U8 else ENB_I32
+        pyr = self.pyramid(levels, img.width, img.height, img.channels, dtype)
+        a = ctypes.byref(plane_image(alpha)) if alpha is not None else None
+        self._check(self.lib.enb_gaussian_pyramid(self.handle, int(wrap), ctypes.byref(img), a, frac_bits,
+                                                  pyr.handle))
+        return pyr
+
+    def laplacian_pyramid(self, image, levels: int, alpha=None, wrap: bool = False, frac_bits: int = 7,
+                          dtype: Optional[int] = None) -> Pyramid:
+        """laplacianPyramid (src/pyramid.h:1647-1747) of a device image."""
+        img = pixel_image(image)
+        if dtype is None:
+            dtype = ENB_I16 if img.dtype == ENB_U8 else ENB_I32
+        pyr = self.pyramid(levels, img.width, img.height, img.channels, dtype)
+        a = ctypes.byref(plane_image(alpha)) if alpha is not None else None
+        self._check(self.lib.enb_laplacian_pyramid(self.handle, int(wrap), ctypes.byref(img), a, frac_bits,
+                                                   pyr.handle))
+        return pyr
+
+    def collapse_pyramid(self, pyr: Pyramid, wrap: bool = False) -> None:
+        self._check(self.lib.enb_collapse_pyramid(self.handle, int(wrap), pyr.handle))
+
+    def blend_pyramids(self, mask_gp: Pyramid, white_lp: Pyramid, black_lp: Pyramid, white_value: int) -> None:
+        self._check(self.lib.enb_blend_pyramids(self.handle, mask_gp.handle, white_lp.handle, black_lp.handle,
+                                                white_value))
+
+    def blend_level(self, mask: Pyramid, white: Pyramid, black: Pyramid, l: int, white_value: int) -> None:
+        m, w, b = mask.level_image(l), white.level_image(l), black.level_image(l)
+        self._check(self.lib.enb_blend(self.handle, ctypes.byref(m), ctypes.byref(w), ctypes.byref(b), white_value))
+
+    def mask_multiply_accumulate(self, lp: Pyramid, mask: Pyramid, result: Pyramid, l: int, divisor: int,
+                                 accumulate: bool) -> None:
+        a, m, r = lp.level_image(l), mask.level_image(l), result.level_image(l)
+        self._check(self.lib.enb_mask_multiply_accumulate(self.handle, ctypes.byref(a), ctypes.byref(m), divisor,
+                                                          ctypes.byref(r), int(accumulate)))
+
+    def from_pyramid(self, pyr: Pyramid, l: int, alpha, dst, frac_bits: int = 7, dither: str = "hash",
+                     seed: int = 0x5eed) -> None:
+        s = pyr.level_image(l)
+        self._check(self.lib.enb_from_pyramid(self.handle, ctypes.byref(s), ctypes.byref(plane_image(alpha)),
+                                              ctypes.byref(pixel_image(dst, channels=s.channels)), frac_bits,
+                                              DITHER[dither], seed))
+
+    # ---- weights and drivers ---------------------------------------------
+    def enfuse_mask(self, image, alpha, out, params: Optional[EnbEnfuseParams] = None) -> None:
+        """enfuseMask (src/enfuse.h:962-1212) into a device float plane."""
+        p = params if params is not None else enfuse_params()
+        a = ctypes.byref(plane_image(alpha)) if alpha is not None else None
+        self._check(self.lib.enb_enfuse_mask(self.handle, ctypes.byref(p), ctypes.byref(pixel_image(image)), a,
+                                             ctypes.byref(plane_image(out))))
+
+    def _options(self, levels, wrap, hard_mask, dither, seed, host, level0) -> EnbFuseOptions:
+        o = EnbFuseOptions()
+        self.lib.enb_default_fuse_options(ctypes.byref(o))
+        o.levels, o.wrap, o.hard_mask = levels, int(wrap), int(hard_mask)
+        o.dither, o.seed, o.host_buffers = DITHER[dither], seed, int(host)
+        o.level0_out = level0
+        return o
+
+    def enfuse(self, images, alphas=None, params: Optional[EnbEnfuseParams] = None, masks=None, out=None,
+               out_alpha=None, levels: int = 0, wrap: bool = False, hard_mask: bool = False,
+               dither: str = "hash", seed: int = 0x5eed, level0=None):
+        """enfuseMain (src/enfuse.h:1217-1617).  Host (numpy) or device (torch) arrays.
+
+        Returns (out, out_alpha)."""
+        K = len(images)
+        host = not _is_torch(images[0])
+        if out is None:
+            out = np.zeros_like(images[0]) if host else images[0].new_zeros(images[0].shape)
+        if out_alpha is None:
+            shp = images[0].shape[:2]
+            out_alpha = np.zeros(shp, np.uint8) if host else images[0].new_zeros(shp, dtype=__import__("torch").uint8)
+        imgs = (EnbImage * K)(*[pixel_image(x) for x in images])
+        al = (EnbImage * K)(*[plane_image(a) for a in alphas]) if alphas is not None else None
+        ms = (EnbImage * K)(*[plane_image(m) for m in masks]) if masks is not None else None
+        p = params if params is not None else enfuse_params()
+        l0 = None
+        if level0 is not None:
+            l0 = _ptr_and_strides(level0)[0]
+        o = self._options(levels, wrap, hard_mask, dither, seed, host, l0)
+        self._check(self.lib.enb_enfuse(self.handle, ctypes.byref(p), K, imgs, al, ms,
+                                        ctypes.byref(pixel_image(out)), ctypes.byref(plane_image(out_alpha)),
+                                        ctypes.byref(o)))
+        return out, out_alpha
+
+    def enblend(self, white, black, mask, white_alpha=None, black_alpha=None, out=None, out_alpha=None,
+                levels: int = 0, wrap: bool = False, dither: str = "hash", seed: int = 0x5eed, level0=None):
+        """enblendMain's pyramid blend (src/enblend.h:330-510).  Returns (out, out_alpha)."""
+        host = not _is_torch(black)
+        if out is None:
+            out = np.zeros_like(black) if host else black.new_zeros(black.shape)
+        if out_alpha is None:
+            shp = black.shape[:2]
+            out_alpha = np.zeros(shp, np.uint8) if host else black.new_zeros(shp, dtype=__import__("torch").uint8)
+        wa = ctypes.byref(plane_image(white_alpha)) if white_alpha is not None else None
+        ba = ctypes.byref(plane_image(black_alpha)) if black_alpha is not None else None
+        l0 = _ptr_and_strides(level0)[0] if level0 is not None else None
+        o = self._options(levels, wrap, False, dither, seed, host, l0)
+        self._check(self.lib.enb_enblend(self.handle, ctypes.byref(pixel_image(white)), wa,
+                                         ctypes.byref(pixel_image(black)), ba, ctypes.byref(plane_image(mask)),
+                                         ctypes.byref(pixel_image(out)), ctypes.byref(plane_image(out_alpha)),
+                                         ctypes.byref(o)))
+        return out, out_alpha
+
+
+def num_levels(width: int, height: int, min_levels: int = 1, exact_levels: int = 0) -> int:
+    """roiBounds level count (src/bounds.h:97-177)."""
+    return load_library().enb_num_levels(width, height, min_levels, exact_levels)
+
+
+__all__ = ["Context", "Pyramid", "EnbError", "EnbImage", "EnbEnfuseParams", "EnbFuseOptions", "enfuse_params",
+           "num_levels", "load_library", "header_functions", "pixel_image", "plane_image",
+           "ENB_U8", "ENB_U16", "ENB_F32", "ENB_I16", "ENB_I32"]

@@ -1,0 +1,240 @@
+/*
+ * enbgpu.h -- C ABI of the GB300 (sm_103a) enblend/enfuse multiresolution path.
+ *
+ * Each entry point replaces one internal call of enblend-enfuse 4.3 on the
+ * pyramid / blend / weight path; the reference interface it stands in for is
+ * cited beside it (file:line in the reference source tree).  The reference's
+ * templates take VIGRA iterator/accessor triples and `new` their pyramids; here
+ * images are plain descriptors of device memory, pyramids are device-resident
+ * handles, errors are status codes (the reference throws from
+ * vigra_precondition or calls exit(1)), and all work is queued on the
+ * context's CUDA stream.  Nothing is synchronous unless a call says so.
+ *
+ * There is no CPU fallback: without a usable CUDA device every compute entry
+ * point fails with ENB_ERR_CUDA.
+ */
+#ifndef ENBGPU_H
+#define ENBGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ENBGPU_ABI_VERSION 1
+
+typedef enum {
+    ENB_OK = 0,
+    ENB_ERR_INVALID = 1,     /* bad argument (the reference's vigra_precondition) */
+    ENB_ERR_UNSUPPORTED = 2, /* valid in the reference but not implemented here */
+    ENB_ERR_CUDA = 3,        /* CUDA runtime error or no device */
+    ENB_ERR_NOMEM = 4        /* device allocation failed */
+} enb_status;
+
+typedef enum {
+    ENB_U8 = 0,   /* 8-bit unsigned samples */
+    ENB_U16 = 1,  /* 16-bit unsigned samples */
+    ENB_F32 = 2,  /* 32-bit float samples (weight masks) */
+    ENB_I16 = 3,  /* 16-bit signed fixed point (pyramids of 8-bit images) */
+    ENB_I32 = 4   /* 32-bit signed fixed point (pyramids of 16-bit images, masks) */
+} enb_dtype;
+
+/* Dither rule of the fixed-point -> pixel conversion. */
+typedef enum {
+    ENB_DITHER_HASH = 0,    /* the reference's rule (src/fixmath.h:251-277), random
+                               bits from a counter hash of (seed, sample index) */
+    ENB_DITHER_NEAREST = 1  /* no dither: round half up */
+} enb_dither;
+
+/* Exposure weight functions, src/exposure_weight.h:44-128. */
+typedef enum {
+    ENB_EXP_GAUSSIAN = 0,
+    ENB_EXP_LORENTZIAN = 1,
+    ENB_EXP_HALF_SINE = 2,
+    ENB_EXP_FULL_SINE = 3,
+    ENB_EXP_BISQUARE = 4
+} enb_exposure_function;
+
+/* Grayscale projectors, src/mga.h:78-87 (l-star and pl-star are not provided). */
+typedef enum {
+    ENB_GRAY_AVERAGE = 0,
+    ENB_GRAY_VALUE = 1,
+    ENB_GRAY_ANTI_VALUE = 2,
+    ENB_GRAY_LIGHTNESS = 3,
+    ENB_GRAY_LUMINANCE = 4,
+    ENB_GRAY_MIXER = 5
+} enb_gray_projector;
+
+/* An image in device memory (host memory for the drivers when
+ * enb_fuse_options.host_buffers is set).
+ *   interleaved pixel images: `channels` colour samples out of `pix_stride`
+ *     components per pixel, rows `pitch` bytes apart (RGB: 3/3, RGBA: 3/4);
+ *   planar pyramid levels: `channels` planes of `height` rows, rows `pitch`
+ *     bytes apart, planes `plane_pitch` bytes apart (pix_stride ignored);
+ *   alpha and mask planes: channels = 1, U8 (0 transparent, else opaque). */
+typedef struct {
+    void* data;
+    int64_t pitch;
+    int64_t plane_pitch;
+    int32_t width;
+    int32_t height;
+    int32_t channels;
+    int32_t pix_stride;
+    int32_t dtype;   /* enb_dtype */
+    int32_t planar;  /* 0 interleaved, 1 planar */
+} enb_image;
+
+/* enfuse weighting parameters; defaults as in src/enfuse.cc:117-140. */
+typedef struct {
+    double w_exposure;      /* --exposure-weight, default 1.0 */
+    double w_saturation;    /* --saturation-weight, default 0.0 */
+    double w_contrast;      /* --contrast-weight, default 0.0 */
+    double w_entropy;       /* --entropy-weight, default 0.0 */
+    double exp_optimum;     /* --exposure-optimum, default 0.5 */
+    double exp_width;       /* --exposure-width, default 0.2 */
+    int32_t exp_function;   /* --exposure-weight-function, enb_exposure_function */
+    int32_t contrast_window;/* --contrast-window-size, odd >= 3, default 5 */
+    int32_t entropy_window; /* --entropy-window-size, odd 3..15, default 3 */
+    int32_t gray_projector; /* --gray-projector, enb_gray_projector */
+    double mixer[3];        /* channel-mixer weights (unnormalised) */
+} enb_enfuse_params;
+
+/* Options of the fuse drivers. */
+typedef struct {
+    int32_t levels;        /* 0: automatic (roiBounds, src/bounds.h:97-177); >0 --levels */
+    int32_t wrap;          /* --wrap horizontal (periodic x) */
+    int32_t hard_mask;     /* enfuse --hard-mask */
+    int32_t dither;        /* enb_dither */
+    uint64_t seed;         /* dither seed */
+    int32_t host_buffers;  /* 1: all image pointers are host memory; copies are
+                              done on the context stream and the call returns
+                              after the result is back in host memory */
+    int32_t reserved;
+    void* level0_out;      /* optional device buffer (host if host_buffers):
+                              collapsed level 0 before conversion, int32,
+                              interleaved width*height*channels */
+} enb_fuse_options;
+
+typedef struct enb_ctx enb_ctx;
+typedef struct enb_pyramid enb_pyramid;
+
+/* ---- context ----------------------------------------------------------- */
+int enb_abi_version(void);
+enb_status enb_create(int device, enb_ctx** ctx);
+enb_status enb_destroy(enb_ctx* ctx);
+/* Queue all later work on `cuda_stream` (a cudaStream_t; NULL = legacy default). */
+enb_status enb_set_stream(enb_ctx* ctx, void* cuda_stream);
+enb_status enb_synchronize(enb_ctx* ctx);
+/* Message of the last failed call on this context (never NULL). */
+const char* enb_last_error(const enb_ctx* ctx);
+/* Kernels launched on this context since creation (a counter, for profiling). */
+uint64_t enb_launch_count(const enb_ctx* ctx);
+void enb_default_enfuse_params(enb_enfuse_params* p);
+void enb_default_fuse_options(enb_fuse_options* o);
+
+/* Per-kernel timing with CUDA events around every launch on the context
+ * stream, with the algorithmic bytes each launch must move (the role of
+ * ShowProfileData for the reference's OpenCL kernels, src/opencl.h:199).
+ * Enabling (or disabling) clears the records.  enb_profile_entry
+ * synchronises the stream and returns kernel i's launch count, summed device
+ * time and summed algorithmic bytes. */
+enb_status enb_profile_enable(enb_ctx* ctx, int enable);
+int enb_profile_count(enb_ctx* ctx);
+enb_status enb_profile_entry(enb_ctx* ctx, int i, const char** name, uint64_t* launches,
+                             double* total_ms, double* bytes);
+
+/* roiBounds level count (src/bounds.h:97-177). */
+int enb_num_levels(int width, int height, int min_levels, int exact_levels);
+
+/* ---- pyramids (std::vector<PyramidImageType*>*, src/pyramid.h:1471) ----- */
+/* Device-resident pyramid: `levels` planar levels of `channels` planes of
+ * dtype ENB_I16 or ENB_I32, level l of size ((w+1)>>1)^l.  Ownership stays
+ * with the caller (the reference's `delete` of each level and the vector,
+ * src/enfuse.h:1568-1570 -> enb_pyramid_free). */
+enb_status enb_pyramid_create(enb_ctx* ctx, int levels, int width, int height, int channels,
+                              int dtype, enb_pyramid** out);
+enb_status enb_pyramid_free(enb_ctx* ctx, enb_pyramid* pyr);
+int enb_pyramid_levels(const enb_pyramid* pyr);
+enb_status enb_pyramid_level(const enb_pyramid* pyr, int level, enb_image* out);
+/* Copy one level to / from dense host memory laid out as channels x height x
+ * width samples of the pyramid dtype; synchronous.  The debugging role of
+ * exportPyramid (src/pyramid.h:1788-1857). */
+enb_status enb_pyramid_read_level(enb_ctx* ctx, const enb_pyramid* pyr, int level, void* host_dst);
+enb_status enb_pyramid_write_level(enb_ctx* ctx, enb_pyramid* pyr, int level, const void* host_src);
+
+/* ---- primitives (device images) ---------------------------------------- */
+/* copyToPyramidImage / ConvertScalarToPyramidFunctor (src/fixmath.h:116-206,
+ * 2019-2147): U8/U16 samples -> `v << frac_bits`; F32 -> fromRealPromote(v *
+ * 2^frac_bits).  dst is a planar I16/I32 level. */
+enb_status enb_to_pyramid(enb_ctx* ctx, const enb_image* src, const enb_image* dst, int frac_bits);
+
+/* reduce (src/pyramid.h:166-573 with alpha, :601-848 without).  src_alpha ==
+ * NULL selects the alpha-free operator (clamp-to-edge, /256); otherwise
+ * dst_alpha receives 255 where any opaque tap contributed. */
+enb_status enb_reduce(enb_ctx* ctx, int wraparound, const enb_image* src, const enb_image* src_alpha,
+                      const enb_image* dst, const enb_image* dst_alpha);
+
+/* expand (src/pyramid.h:1102-1457): add == 0: dst -= E(src) (laplacian build);
+ * add != 0: dst = fromPromote(dst + E(src)) (collapse). */
+enb_status enb_expand(enb_ctx* ctx, int add, int wraparound, const enb_image* src,
+                      const enb_image* dst);
+
+/* CartesianBlendFunctor over one level (src/blend.h:41-76): black := blend of
+ * white and black under mask / white_value. */
+enb_status enb_blend(enb_ctx* ctx, const enb_image* mask, const enb_image* white,
+                     const enb_image* black, int32_t white_value);
+
+/* ImageMaskMultiplyFunctor and accumulation (src/enfuse.h:601-620,
+ * 1554-1588): result = (accumulate ? result : 0) + fromRealPromote(lp * mask / divisor). */
+enb_status enb_mask_multiply_accumulate(enb_ctx* ctx, const enb_image* lp, const enb_image* mask,
+                                        int32_t divisor, const enb_image* result, int accumulate);
+
+/* copyFromPyramidImageIf (src/fixmath.h:2158-2294, rule :251-277): planar
+ * fixed point -> interleaved U8/U16 pixels where alpha != 0. */
+enb_status enb_from_pyramid(enb_ctx* ctx, const enb_image* src, const enb_image* alpha,
+                            const enb_image* dst, int frac_bits, int dither, uint64_t seed);
+
+/* ---- pyramid builders --------------------------------------------------- */
+/* gaussianPyramid (src/pyramid.h:1468-1636); alpha NULL -> alpha-free reduce. */
+enb_status enb_gaussian_pyramid(enb_ctx* ctx, int wraparound, const enb_image* src,
+                                const enb_image* alpha, int frac_bits, enb_pyramid* pyr);
+/* laplacianPyramid (src/pyramid.h:1647-1747). */
+enb_status enb_laplacian_pyramid(enb_ctx* ctx, int wraparound, const enb_image* src,
+                                 const enb_image* alpha, int frac_bits, enb_pyramid* pyr);
+/* collapsePyramid (src/pyramid.h:1758-1784); level 0 receives the result. */
+enb_status enb_collapse_pyramid(enb_ctx* ctx, int wraparound, enb_pyramid* pyr);
+/* blend (src/blend.h:81-121): black_lp := per-level CartesianBlend. */
+enb_status enb_blend_pyramids(enb_ctx* ctx, const enb_pyramid* mask_gp, const enb_pyramid* white_lp,
+                              enb_pyramid* black_lp, int32_t white_value);
+
+/* ---- enfuse weights ----------------------------------------------------- */
+/* enfuseMask (src/enfuse.h:962-1212): F32 weight plane of an U8/U16 image. */
+enb_status enb_enfuse_mask(enb_ctx* ctx, const enb_enfuse_params* params, const enb_image* src,
+                           const enb_image* alpha, const enb_image* mask_out);
+
+/* ---- drivers ------------------------------------------------------------ */
+/* enfuseMain's weighting, normalisation, pyramids, merge, collapse and
+ * output conversion (src/enfuse.h:1217-1617) for K union-sized images.
+ * alphas: K alpha planes or NULL (for RGBA images the alpha is then the
+ * thresholded 4th component as imported by src/assemble.h:240-253, else fully
+ * opaque).  masks_in: K F32 weight planes replacing enfuseMask (--load-masks),
+ * or NULL.  out: interleaved image of the input type (zero where out_alpha is
+ * 0); out_alpha: U8 union alpha, may be NULL. */
+enb_status enb_enfuse(enb_ctx* ctx, const enb_enfuse_params* params, int K, const enb_image* images,
+                      const enb_image* alphas, const enb_image* masks_in, const enb_image* out,
+                      const enb_image* out_alpha, const enb_fuse_options* opt);
+
+/* enblendMain's pyramid section (src/enblend.h:330-510): blend `white` into
+ * `black` under the 0/255 seam mask over the whole canvas.  out receives the
+ * black image with the blended pixels where the union alpha is set. */
+enb_status enb_enblend(enb_ctx* ctx, const enb_image* white, const enb_image* white_alpha,
+                       const enb_image* black, const enb_image* black_alpha, const enb_image* mask,
+                       const enb_image* out, const enb_image* out_alpha, const enb_fuse_options* opt);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ENBGPU_H */

@@ -1,0 +1,1033 @@
+/*
+ * enb_oracle.c -- CPU restatement of the enblend/enfuse multiresolution hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY (parity checker and timed CPU baseline); see
+ * enb_oracle.h.  The reduce/expand operators are written as direct per-pixel
+ * formulas (weights and divisors per output position) rather than the
+ * reference's SKIPSM raster state machines; the divisor tables they produce are
+ * the ones implied by src/pyramid.h:875-1419.  Pyramid passes run serially and
+ * pointwise passes under OpenMP, which is the parallel structure of the
+ * reference (src/pyramid.h has no OpenMP; src/openmp_vigra.h parallelises the
+ * pointwise wrappers).
+ *
+ * Must be compiled with -ffp-contract=off and without -ffast-math: several
+ * steps reproduce the reference's IEEE double expressions exactly.
+ */
+#include "enb_oracle.h"
+
+#include <float.h>
+#include <limits.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------------- */
+/* VIGRA NumericTraits conversions used by the reference.                     */
+/* ------------------------------------------------------------------------- */
+
+/* NumericTraits<int>::fromRealPromote: round half away from zero via +-0.5 and a
+ * truncating cast, saturating at the type limits. */
+static inline int32_t frp_i32(double v)
+{
+    if (v < 0.0) {
+        return v < (double)INT_MIN ? INT_MIN : (int32_t)(v - 0.5);
+    }
+    return v > (double)INT_MAX ? INT_MAX : (int32_t)(v + 0.5);
+}
+
+static inline int32_t frp_i16(double v)
+{
+    if (v < 0.0) {
+        return v < (double)SHRT_MIN ? SHRT_MIN : (int32_t)(short)(v - 0.5);
+    }
+    return v > (double)SHRT_MAX ? SHRT_MAX : (int32_t)(short)(v + 0.5);
+}
+
+static inline int32_t frp_bits(double v, int bits) { return bits == 16 ? frp_i16(v) : frp_i32(v); }
+
+static inline uint32_t frp_unsigned(double v, uint32_t maxv)
+{
+    if (v < 0.0) {
+        return 0u;
+    }
+    return v > (double)maxv ? maxv : (uint32_t)(v + 0.5);
+}
+
+/* Assignment through the pyramid accessor: static_cast to the pyramid type. */
+static inline int32_t cast_bits(int64_t v, int bits)
+{
+    return bits == 16 ? (int32_t)(int16_t)(uint16_t)(v & 0xffff) : (int32_t)(uint32_t)(v & 0xffffffffu);
+}
+
+/* NumericTraits<PyramidType>::fromPromote: saturate for Int16, identity for Int32. */
+static inline int32_t fp_bits(int64_t v, int bits)
+{
+    if (bits == 16) {
+        return v < SHRT_MIN ? SHRT_MIN : (v > SHRT_MAX ? SHRT_MAX : (int32_t)v);
+    }
+    return (int32_t)v;
+}
+
+static inline int imod(int a, int m)
+{
+    int r = a % m;
+    return r < 0 ? r + m : r;
+}
+
+static inline uint32_t sample_int(const void* src, int dtype, int64_t i)
+{
+    return dtype == ORC_U8 ? ((const uint8_t*)src)[i] : ((const uint16_t*)src)[i];
+}
+
+/* ------------------------------------------------------------------------- */
+/* roiBounds level count, src/bounds.h:121-133.                              */
+/* ------------------------------------------------------------------------- */
+
+int orc_num_levels(int w, int h, int min_levels, int exact_levels)
+{
+    const int max_levels = 29; /* MAX_PYRAMID_LEVELS, src/common.h:55 */
+    unsigned int shortdim = (unsigned int)(w < h ? w : h);
+    int allowable = min_levels;
+    while (allowable <= max_levels) {
+        if (shortdim <= 8u) {
+            break;
+        }
+        shortdim = (shortdim + 1u) >> 1;
+        ++allowable;
+    }
+    if (allowable > min_levels) {
+        if (exact_levels >= 1) {
+            if (exact_levels < allowable) {
+                allowable = exact_levels;
+            }
+        } else if (exact_levels < 0) {
+            if (allowable + exact_levels >= min_levels) {
+                allowable += exact_levels;
+            } else {
+                allowable = min_levels;
+            }
+        }
+    }
+    return allowable;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Conversions to fixed point, src/fixmath.h:189-202.                        */
+/* ------------------------------------------------------------------------- */
+
+void orc_fixed_from_int(const void* src, int dtype, int64_t npix, int C, int pix_stride,
+                        int32_t* dst, int frac)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t p = 0; p < npix; ++p) {
+        for (int c = 0; c < C; ++c) {
+            dst[p * C + c] = (int32_t)(sample_int(src, dtype, p * pix_stride + c) << frac);
+        }
+    }
+}
+
+void orc_fixed_from_float(const float* src, int64_t n, int32_t* dst, int frac, int bits)
+{
+    const double scale = (double)(1u << frac);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        dst[i] = frp_bits((double)src[i] * scale, bits);
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Reduce, src/pyramid.h:166-848.                                             */
+/* ------------------------------------------------------------------------- */
+
+static const int W5[5] = {1, 4, 6, 4, 1};
+
+/* Normalised 5x5 binomial over the opaque taps; taps outside the image are
+ * dropped, columns wrap when `wrap` (periodic x, src/pyramid.h:234-244). */
+int orc_reduce_alpha(int wrap, const int32_t* src, const uint8_t* alpha, int sw, int sh, int C,
+                     int32_t* dst, uint8_t* dst_alpha, int bits)
+{
+    if (sw <= 1 || sh <= 1 || C > 4) {
+        return -1; /* vigra_precondition "src image too small in reduce" */
+    }
+    const int dw = (sw + 1) >> 1, dh = (sh + 1) >> 1;
+    for (int Y = 0; Y < dh; ++Y) {
+        for (int X = 0; X < dw; ++X) {
+            int64_t num[4] = {0, 0, 0, 0};
+            int64_t den = 0;
+            for (int j = -2; j <= 2; ++j) {
+                const int y = 2 * Y + j;
+                if (y < 0 || y >= sh) {
+                    continue;
+                }
+                for (int i = -2; i <= 2; ++i) {
+                    int x = 2 * X + i;
+                    if (wrap) {
+                        x = imod(x, sw);
+                    } else if (x < 0 || x >= sw) {
+                        continue;
+                    }
+                    const int64_t p = (int64_t)y * sw + x;
+                    if (alpha[p]) {
+                        const int wgt = W5[j + 2] * W5[i + 2];
+                        den += wgt;
+                        for (int c = 0; c < C; ++c) {
+                            num[c] += (int64_t)wgt * src[p * C + c];
+                        }
+                    }
+                }
+            }
+            const int64_t q = (int64_t)Y * dw + X;
+            if (den > 0) {
+                for (int c = 0; c < C; ++c) {
+                    dst[q * C + c] = cast_bits(num[c] / den, bits);
+                }
+                dst_alpha[q] = 255;
+            } else {
+                for (int c = 0; c < C; ++c) {
+                    dst[q * C + c] = 0;
+                }
+                dst_alpha[q] = 0;
+            }
+        }
+    }
+    return 0;
+}
+
+/* 5x5 binomial / 256 with clamp-to-edge replication in y (and in x unless
+ * `wrap`), src/pyramid.h:646-847. */
+int orc_reduce(int wrap, const int32_t* src, int sw, int sh, int C, int32_t* dst, int bits)
+{
+    if (sw <= 1 || sh <= 1 || C > 4) {
+        return -1;
+    }
+    const int dw = (sw + 1) >> 1, dh = (sh + 1) >> 1;
+    for (int Y = 0; Y < dh; ++Y) {
+        for (int X = 0; X < dw; ++X) {
+            int64_t num[4] = {0, 0, 0, 0};
+            for (int j = -2; j <= 2; ++j) {
+                int y = 2 * Y + j;
+                y = y < 0 ? 0 : (y >= sh ? sh - 1 : y);
+                for (int i = -2; i <= 2; ++i) {
+                    int x = 2 * X + i;
+                    if (wrap) {
+                        x = imod(x, sw);
+                    } else {
+                        x = x < 0 ? 0 : (x >= sw ? sw - 1 : x);
+                    }
+                    const int wgt = W5[j + 2] * W5[i + 2];
+                    for (int c = 0; c < C; ++c) {
+                        num[c] += (int64_t)wgt * src[((int64_t)y * sw + x) * C + c];
+                    }
+                }
+            }
+            for (int c = 0; c < C; ++c) {
+                dst[((int64_t)Y * dw + X) * C + c] = cast_bits(num[c] / 256, bits);
+            }
+        }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Expand, src/pyramid.h:875-1457.                                            */
+/* ------------------------------------------------------------------------- */
+
+/* Horizontal taps of destination column X.  Even columns interpolate with
+ * (1,6,1), odd columns with (4,4); the divisor is the sum of the weights whose
+ * taps lie inside the source.  With wrap-around, an odd destination width puts
+ * weight 4 on the wrapped neighbour of the first and the last even column
+ * (divisor 11, src/pyramid.h:1058-1078, 1153-1161), and a one-column source
+ * keeps the wrapped state as an extra numerator term over the plain divisor 6
+ * (src/pyramid.h:1233-1236, 1304-1307). */
+static void expand_htaps(int X, int sw, int dw, int wrap, int idx[3], int wt[3], int* n, int* den)
+{
+    const int i = X >> 1;
+    int cnt = 0, d = 0;
+    if ((X & 1) == 0) {
+        if (wrap && sw == 1) {
+            idx[0] = 0;
+            wt[0] = (dw & 1) ? 10 : 7;
+            *n = 1;
+            *den = 6;
+            return;
+        }
+        int cand[3] = {i - 1, i, i + 1};
+        int cw[3] = {1, 6, 1};
+        if (wrap && (dw & 1)) {
+            if (i == 0) {
+                cw[0] = 4;
+            }
+            if (i == sw - 1) {
+                cw[2] = 4;
+            }
+        }
+        for (int k = 0; k < 3; ++k) {
+            int t = cand[k];
+            if (wrap) {
+                t = imod(t, sw);
+            } else if (t < 0 || t >= sw) {
+                continue;
+            }
+            idx[cnt] = t;
+            wt[cnt] = cw[k];
+            d += cw[k];
+            ++cnt;
+        }
+    } else {
+        int cand[2] = {i, i + 1};
+        for (int k = 0; k < 2; ++k) {
+            int t = cand[k];
+            if (wrap && sw > 1) {
+                t = imod(t, sw);
+            } else if (t < 0 || t >= sw) {
+                continue;
+            }
+            idx[cnt] = t;
+            wt[cnt] = 4;
+            d += 4;
+            ++cnt;
+        }
+    }
+    *n = cnt;
+    *den = d;
+}
+
+/* Vertical taps of destination row Y: (1,6,1) for even rows, (1,1) for odd
+ * rows, taps outside the source dropped (no wrap-around in y). */
+static void expand_vtaps(int Y, int sh, int idx[3], int wt[3], int* n, int* den)
+{
+    const int j = Y >> 1;
+    int cnt = 0, d = 0;
+    if ((Y & 1) == 0) {
+        const int cand[3] = {j - 1, j, j + 1};
+        const int cw[3] = {1, 6, 1};
+        for (int k = 0; k < 3; ++k) {
+            if (cand[k] >= 0 && cand[k] < sh) {
+                idx[cnt] = cand[k];
+                wt[cnt] = cw[k];
+                d += cw[k];
+                ++cnt;
+            }
+        }
+    } else {
+        const int cand[2] = {j, j + 1};
+        for (int k = 0; k < 2; ++k) {
+            if (cand[k] >= 0 && cand[k] < sh) {
+                idx[cnt] = cand[k];
+                wt[cnt] = 1;
+                d += 1;
+                ++cnt;
+            }
+        }
+    }
+    *n = cnt;
+    *den = d;
+}
+
+int orc_expand(int add, int wrap, const int32_t* src, int sw, int sh,
+               int32_t* dst, int dw, int dh, int C, int bits)
+{
+    if (sw < 1 || sh < 1 || sw != ((dw + 1) >> 1) || sh != ((dh + 1) >> 1) || C > 4) {
+        return -1;
+    }
+    for (int Y = 0; Y < dh; ++Y) {
+        int vi[3], vw[3], vn, vd;
+        expand_vtaps(Y, sh, vi, vw, &vn, &vd);
+        for (int X = 0; X < dw; ++X) {
+            int hi[3], hw[3], hn, hd;
+            expand_htaps(X, sw, dw, wrap, hi, hw, &hn, &hd);
+            const int64_t den = (int64_t)hd * vd;
+            for (int c = 0; c < C; ++c) {
+                int64_t num = 0;
+                for (int a = 0; a < vn; ++a) {
+                    int64_t row = 0;
+                    for (int b = 0; b < hn; ++b) {
+                        row += (int64_t)hw[b] * src[((int64_t)vi[a] * sw + hi[b]) * C + c];
+                    }
+                    num += vw[a] * row;
+                }
+                const int64_t e = num / den;
+                int32_t* d = &dst[((int64_t)Y * dw + X) * C + c];
+                *d = add ? fp_bits((int64_t)*d + e, bits) : cast_bits((int64_t)*d - e, bits);
+            }
+        }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Merge operators.                                                           */
+/* ------------------------------------------------------------------------- */
+
+/* CartesianBlendFunctor, src/blend.h:41-76. */
+void orc_blend(const int32_t* mask, const int32_t* white, int32_t* black, int64_t npix, int C,
+               int32_t white_value, int bits)
+{
+    const double wv = (double)white_value;
+#pragma omp parallel for schedule(guided)
+    for (int64_t p = 0; p < npix; ++p) {
+        const double wc = (double)mask[p] / wv;
+        if (wc >= 1.0) {
+            for (int c = 0; c < C; ++c) {
+                black[p * C + c] = white[p * C + c];
+            }
+        } else if (wc <= 0.0) {
+            /* keep black */
+        } else {
+            const double bc = 1.0 - wc;
+            for (int c = 0; c < C; ++c) {
+                const double a = wc * (double)white[p * C + c];
+                const double b = bc * (double)black[p * C + c];
+                black[p * C + c] = frp_bits(a + b, bits);
+            }
+        }
+    }
+}
+
+/* ImageMaskMultiplyFunctor, src/enfuse.h:601-620. */
+void orc_mask_multiply(int32_t* lp, const int32_t* mask, int64_t npix, int C, int32_t divisor,
+                       int bits)
+{
+    const double dv = (double)divisor;
+#pragma omp parallel for schedule(static)
+    for (int64_t p = 0; p < npix; ++p) {
+        const double coeff = (double)mask[p] / dv;
+        for (int c = 0; c < C; ++c) {
+            lp[p * C + c] = frp_bits((double)lp[p * C + c] * coeff, bits);
+        }
+    }
+}
+
+/* vigra Arg1()+Arg2() into the pyramid type (static_cast), src/enfuse.h:1579-1582. */
+void orc_accumulate(const int32_t* lp, int32_t* res, int64_t n, int bits)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        res[i] = cast_bits((int64_t)lp[i] + res[i], bits);
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Conversion from fixed point, src/fixmath.h:241-277.                        */
+/* ------------------------------------------------------------------------- */
+
+/* 32-bit integer finaliser (public-domain "lowbias32" constants by C. Wellons). */
+static inline uint32_t mix32(uint32_t x)
+{
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+uint32_t orc_dither_bits(uint64_t seed, uint64_t index)
+{
+    const uint32_t hi = mix32((uint32_t)(index >> 32) ^ (uint32_t)(seed >> 32) ^ 0x9e3779b9u);
+    return mix32((uint32_t)index ^ (uint32_t)seed ^ hi);
+}
+
+void orc_from_fixed(const int32_t* src, const uint8_t* alpha, int64_t npix, int C,
+                    void* dst, int dtype, int pix_stride, int frac, int dither_mode, uint64_t seed)
+{
+    const int32_t half_m1 = (1 << (frac - 1)) - 1;
+    const int32_t quarter = 1 << (frac - 2);
+    const int32_t three_quarter = 3 << (frac - 2);
+    const int32_t half = 1 << (frac - 1);
+    const int32_t maxv = dtype == ORC_U8 ? 255 : 65535;
+#pragma omp parallel for schedule(static)
+    for (int64_t p = 0; p < npix; ++p) {
+        if (!alpha[p]) {
+            continue;
+        }
+        for (int c = 0; c < C; ++c) {
+            const int32_t v = src[p * C + c];
+            const int32_t q = v >> frac;            /* arithmetic shift: floor */
+            const int32_t f = v & ((1 << frac) - 1);
+            int32_t r;
+            if (dither_mode == ORC_DITHER_NEAREST) {
+                r = f >= half ? q + 1 : q;
+            } else if (f >= quarter && f < three_quarter) {
+                const int32_t rnd =
+                    (int32_t)(orc_dither_bits(seed, (uint64_t)p * (uint64_t)C + (uint64_t)c) & (uint32_t)half_m1) + quarter;
+                r = rnd <= f ? q + 1 : q;
+            } else if (f >= quarter) {
+                r = q + 1;
+            } else {
+                r = q;
+            }
+            r = r < 0 ? 0 : (r > maxv ? maxv : r); /* fromPromote */
+            if (dtype == ORC_U8) {
+                ((uint8_t*)dst)[p * pix_stride + c] = (uint8_t)r;
+            } else {
+                ((uint16_t*)dst)[p * pix_stride + c] = (uint16_t)r;
+            }
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Pyramid builders, src/pyramid.h:1468-1784.                                */
+/* ------------------------------------------------------------------------- */
+
+typedef struct {
+    int levels;
+    int C;
+    int w[30], h[30];
+    int32_t* lv[30];
+} pyr_t;
+
+static void pyr_alloc(pyr_t* p, int levels, int w, int h, int C)
+{
+    p->levels = levels;
+    p->C = C;
+    for (int l = 0; l < levels; ++l) {
+        p->w[l] = w;
+        p->h[l] = h;
+        p->lv[l] = (int32_t*)calloc((size_t)w * h * C, sizeof(int32_t));
+        w = (w + 1) >> 1;
+        h = (h + 1) >> 1;
+    }
+}
+
+static void pyr_free(pyr_t* p)
+{
+    for (int l = 0; l < p->levels; ++l) {
+        free(p->lv[l]);
+    }
+}
+
+/* gaussianPyramid with alpha: level 0 already in p->lv[0]; the first reduce
+ * uses the given alpha, later ones the reduced binary alpha (pyramid.h:1500-1530). */
+static int gaussian_alpha(pyr_t* p, const uint8_t* alpha0, int wrap, int bits)
+{
+    const uint8_t* a = alpha0;
+    uint8_t* owned = NULL;
+    for (int l = 1; l < p->levels; ++l) {
+        uint8_t* na = (uint8_t*)malloc((size_t)p->w[l] * p->h[l]);
+        const int rc = orc_reduce_alpha(wrap, p->lv[l - 1], a, p->w[l - 1], p->h[l - 1], p->C,
+                                        p->lv[l], na, bits);
+        free(owned);
+        owned = na;
+        a = na;
+        if (rc) {
+            free(owned);
+            return rc;
+        }
+    }
+    free(owned);
+    return 0;
+}
+
+static int gaussian_noalpha(pyr_t* p, int wrap, int bits)
+{
+    for (int l = 1; l < p->levels; ++l) {
+        const int rc = orc_reduce(wrap, p->lv[l - 1], p->w[l - 1], p->h[l - 1], p->C, p->lv[l], bits);
+        if (rc) {
+            return rc;
+        }
+    }
+    return 0;
+}
+
+/* laplacianPyramid: gp[l] -= expand(gp[l+1]) for l = 0..L-2 (pyramid.h:1672-1736). */
+static int laplacian_inplace(pyr_t* p, int wrap, int bits)
+{
+    for (int l = 0; l + 1 < p->levels; ++l) {
+        const int rc = orc_expand(0, wrap, p->lv[l + 1], p->w[l + 1], p->h[l + 1], p->lv[l],
+                                  p->w[l], p->h[l], p->C, bits);
+        if (rc) {
+            return rc;
+        }
+    }
+    return 0;
+}
+
+/* collapsePyramid: p[l] = fromPromote(p[l] + expand(p[l+1])), l = L-2..0 (pyramid.h:1758-1784). */
+static int collapse(pyr_t* p, int wrap, int bits)
+{
+    for (int l = p->levels - 2; l >= 0; --l) {
+        const int rc = orc_expand(1, wrap, p->lv[l + 1], p->w[l + 1], p->h[l + 1], p->lv[l],
+                                  p->w[l], p->h[l], p->C, bits);
+        if (rc) {
+            return rc;
+        }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Enfuse weights, src/enfuse.h:64-1212 and src/mga.h.                       */
+/* ------------------------------------------------------------------------- */
+
+#define FWHM_GAUSSIAN_C 2.3548200450309493820231386529193992755
+#define FWHM_LORENTZIAN_C 2.8284271247461900976033774484193961571
+#define FWHM_HALFSINE_C 2.0943951023931954923084289221863352561
+#define FWHM_FULLSINE_C 3.14159265358979323846
+#define FWHM_BISQUARE_C 1.6817928305074290860622509524664297901
+
+/* Effective width of the built-in exposure weight functions: each rescales the
+ * user width to the Gaussian's FWHM (exposure_weight.h:56-116). */
+static double exposure_effective_width(int fn, double width)
+{
+    switch (fn) {
+    case ORC_EXP_LORENTZIAN: return width * FWHM_GAUSSIAN_C / FWHM_LORENTZIAN_C;
+    case ORC_EXP_HALF_SINE: return width * FWHM_GAUSSIAN_C / FWHM_HALFSINE_C;
+    case ORC_EXP_FULL_SINE: return width * FWHM_GAUSSIAN_C / FWHM_FULLSINE_C;
+    case ORC_EXP_BISQUARE: return width * FWHM_GAUSSIAN_C / FWHM_BISQUARE_C;
+    default: return width;
+    }
+}
+
+/* ExposureWeight::weight of the built-ins (exposure_weight.h:44-128). */
+static double exposure_weight(int fn, double y, double opt, double eff_width)
+{
+    const double z = (y - opt) / eff_width;
+    switch (fn) {
+    case ORC_EXP_LORENTZIAN: return 1.0 / (1.0 + 0.5 * z * z);
+    case ORC_EXP_HALF_SINE: return fabs(z) <= 1.57079632679489661923 ? cos(z) : 0.0;
+    case ORC_EXP_FULL_SINE: return fabs(z) <= 3.14159265358979323846 ? 0.5 + cos(z) / 2.0 : 0.0;
+    case ORC_EXP_BISQUARE:
+        if (fabs(z) <= 1.0) {
+            const double z2 = z * z;
+            return (1.0 - z2) * (1.0 + z2);
+        }
+        return 0.0;
+    default: return exp(-0.5 * z * z);
+    }
+}
+
+/* MultiGrayscaleAccessor::project for integer RGB pixels, result rounded to
+ * an integer by fromRealPromote (mga.h:185-222). */
+static int32_t gray_int(const orc_enfuse_params* prm, int32_t r, int32_t g, int32_t b,
+                        uint32_t maxv, double mw0, double mw1, double mw2)
+{
+    switch (prm->gray_projector) {
+    case ORC_GRAY_VALUE: {
+        int32_t m = r > g ? r : g;
+        return m > b ? m : b;
+    }
+    case ORC_GRAY_ANTI_VALUE: {
+        int32_t m = r < g ? r : g;
+        return m < b ? m : b;
+    }
+    case ORC_GRAY_LIGHTNESS: {
+        int32_t mn = r < g ? r : g;
+        mn = mn < b ? mn : b;
+        int32_t mx = r > g ? r : g;
+        mx = mx > b ? mx : b;
+        return (int32_t)frp_unsigned((double)(mn + mx) / 2.0, maxv);
+    }
+    case ORC_GRAY_LUMINANCE:
+        return (int32_t)frp_unsigned(0.3 * r + 0.59 * g + 0.11 * b, maxv);
+    case ORC_GRAY_MIXER:
+        return (int32_t)frp_unsigned(mw0 * (double)r + mw1 * (double)g + mw2 * (double)b, maxv);
+    default:
+        return (int32_t)frp_unsigned(((double)r + (double)g + (double)b) / 3.0, maxv);
+    }
+}
+
+int orc_local_stddev(const int32_t* gray, const uint8_t* alpha, int w, int h, int window,
+                     int32_t* out)
+{
+    if (window < 2 || w < window || h < window) {
+        return -1;
+    }
+    const int b = window / 2;
+#pragma omp parallel for schedule(static)
+    for (int y = b; y < h - b; ++y) {
+        for (int x = b; x < w - b; ++x) {
+            if (!alpha[(int64_t)y * w + x]) {
+                continue;
+            }
+            double sum = 0.0, sumsq = 0.0;
+            size_t n = 0;
+            for (int yy = y - b; yy <= y + b; ++yy) {
+                for (int xx = x - b; xx <= x + b; ++xx) {
+                    const int64_t p = (int64_t)yy * w + xx;
+                    if (alpha[p]) {
+                        const double v = (double)gray[p];
+                        sum += v;
+                        sumsq += v * v;
+                        ++n;
+                    }
+                }
+            }
+            const double r = n <= 1 ? 0.0 : sqrt((sumsq - sum * sum / (double)n) / (double)(n - 1));
+            out[(int64_t)y * w + x] = frp_i32(r);
+        }
+    }
+    return 0;
+}
+
+static int cmp_u32(const void* a, const void* b)
+{
+    const uint32_t x = *(const uint32_t*)a, y = *(const uint32_t*)b;
+    return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+/* Histogram::entropyOfChannel (enfuse.h:346-375): bins visited in ascending
+ * key order, p = count/total, H = -sum(p log p) / log(#bins). */
+static double entropy_of(uint32_t* vals, int n)
+{
+    if (n == 0) {
+        return 0.0;
+    }
+    qsort(vals, (size_t)n, sizeof(uint32_t), cmp_u32);
+    int bins = 1;
+    for (int i = 1; i < n; ++i) {
+        bins += vals[i] != vals[i - 1];
+    }
+    if (bins <= 1) {
+        return 0.0;
+    }
+    double e = 0.0;
+    int i = 0;
+    while (i < n) {
+        int j = i;
+        while (j < n && vals[j] == vals[i]) {
+            ++j;
+        }
+        const double p = (double)(unsigned)(j - i) / (double)(unsigned)n;
+        e += p * log(p);
+        i = j;
+    }
+    return -e / log((double)bins);
+}
+
+int orc_local_entropy(const void* img, int dtype, int w, int h, int C, int pix_stride,
+                      const uint8_t* alpha, int window, double* out)
+{
+    if (w < window || h < window || dtype == ORC_F32) {
+        return -1;
+    }
+    const int b = window / 2;
+    const double maxv = dtype == ORC_U8 ? 255.0 : 65535.0;
+#pragma omp parallel
+    {
+        uint32_t* vals = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)window * window);
+#pragma omp for schedule(static)
+        for (int y = b; y < h - b; ++y) {
+            for (int x = b; x < w - b; ++x) {
+                if (!alpha[(int64_t)y * w + x]) {
+                    continue;
+                }
+                for (int c = 0; c < C; ++c) {
+                    int n = 0;
+                    for (int yy = y - b; yy <= y + b; ++yy) {
+                        for (int xx = x - b; xx <= x + b; ++xx) {
+                            const int64_t p = (int64_t)yy * w + xx;
+                            if (alpha[p]) {
+                                vals[n++] = sample_int(img, dtype, p * pix_stride + c);
+                            }
+                        }
+                    }
+                    out[((int64_t)y * w + x) * C + c] = entropy_of(vals, n) * maxv;
+                }
+            }
+        }
+        free(vals);
+    }
+    return 0;
+}
+
+int orc_enfuse_mask(const void* img, int dtype, int w, int h, int C, int pix_stride,
+                    const uint8_t* alpha, const orc_enfuse_params* prm, float* out)
+{
+    if (dtype == ORC_F32 || (C != 1 && C != 3)) {
+        return -2; /* float images are handled by the float path */
+    }
+    const int64_t npix = (int64_t)w * h;
+    const uint32_t maxv = dtype == ORC_U8 ? 255u : 65535u;
+    double mw0 = 0, mw1 = 0, mw2 = 0;
+    if (prm->gray_projector == ORC_GRAY_MIXER) {
+        const double s = prm->mixer[0] + prm->mixer[1] + prm->mixer[2];
+        mw0 = prm->mixer[0] / s;
+        mw1 = prm->mixer[1] / s;
+        mw2 = prm->mixer[2] / s;
+    }
+    int32_t* gray = (int32_t*)malloc(sizeof(int32_t) * (size_t)npix);
+#pragma omp parallel for schedule(static)
+    for (int64_t p = 0; p < npix; ++p) {
+        if (C == 1) {
+            gray[p] = (int32_t)sample_int(img, dtype, p * pix_stride);
+        } else {
+            gray[p] = gray_int(prm, (int32_t)sample_int(img, dtype, p * pix_stride),
+                               (int32_t)sample_int(img, dtype, p * pix_stride + 1),
+                               (int32_t)sample_int(img, dtype, p * pix_stride + 2), maxv, mw0, mw1, mw2);
+        }
+    }
+    memset(out, 0, sizeof(float) * (size_t)npix);
+
+    /* Exposure (enfuse.h:974-1010, 623-651). */
+    if (prm->w_exposure > 0.0) {
+        const double ew = exposure_effective_width(prm->exp_function, prm->exp_width);
+#pragma omp parallel for schedule(static)
+        for (int64_t p = 0; p < npix; ++p) {
+            if (alpha[p]) {
+                const double y = (double)gray[p] / (double)maxv;
+                out[p] = (float)(prm->w_exposure * exposure_weight(prm->exp_function, y, prm->exp_optimum, ew));
+            }
+        }
+    }
+
+    /* Contrast (enfuse.h:1013-1122, 783-829). */
+    if (prm->w_contrast > 0.0) {
+        int32_t* grad = (int32_t*)calloc((size_t)npix, sizeof(int32_t));
+        const int rc = orc_local_stddev(gray, alpha, w, h, prm->contrast_window, grad);
+        if (rc) {
+            free(grad);
+            free(gray);
+            return rc;
+        }
+#pragma omp parallel for schedule(static)
+        for (int64_t p = 0; p < npix; ++p) {
+            if (alpha[p]) {
+                /* the combine lambda takes the gradient as the pixel's scalar type */
+                const uint32_t g = dtype == ORC_U8 ? (uint32_t)(uint8_t)grad[p] : (uint32_t)(uint16_t)grad[p];
+                const float cw = (float)(prm->w_contrast * (double)(int32_t)g / (double)maxv);
+                out[p] = cw + out[p];
+            }
+        }
+        free(grad);
+    }
+
+    /* Saturation (enfuse.h:1125-1136, 733-780). */
+    if (prm->w_saturation > 0.0 && C == 3) {
+        const double max_value = (double)maxv;
+#pragma omp parallel for schedule(static)
+        for (int64_t p = 0; p < npix; ++p) {
+            if (!alpha[p]) {
+                continue;
+            }
+            const uint32_t r = sample_int(img, dtype, p * pix_stride);
+            const uint32_t g = sample_int(img, dtype, p * pix_stride + 1);
+            const uint32_t b = sample_int(img, dtype, p * pix_stride + 2);
+            uint32_t mx = r > g ? r : g;
+            mx = mx > b ? mx : b;
+            uint32_t mn = r < g ? r : g;
+            mn = mn < b ? mn : b;
+            float sw = 0.0f;
+            if (mx != mn) {
+                const double sum = (double)mx + (double)mn;
+                const double diff = (double)mx - (double)mn;
+                const double s = sum <= max_value ? diff / sum : diff / (2.0 * max_value - sum);
+                sw = (float)(prm->w_saturation * s);
+            }
+            out[p] = sw + out[p];
+        }
+    }
+
+    /* Entropy (enfuse.h:1139-1211, 832-861). */
+    if (prm->w_entropy > 0.0) {
+        double* ent = (double*)calloc((size_t)npix * C, sizeof(double));
+        const int rc = orc_local_entropy(img, dtype, w, h, C, pix_stride, alpha, prm->entropy_window, ent);
+        if (rc) {
+            free(ent);
+            free(gray);
+            return rc;
+        }
+#pragma omp parallel for schedule(static)
+        for (int64_t p = 0; p < npix; ++p) {
+            if (!alpha[p]) {
+                continue;
+            }
+            uint32_t mn = maxv;
+            for (int c = 0; c < C; ++c) {
+                /* entropy image pixel = fromRealPromote<T>(H * max) */
+                const uint32_t e = frp_unsigned(ent[p * C + c], maxv);
+                mn = e < mn ? e : mn;
+            }
+            const float ew = (float)(prm->w_entropy * (double)(float)mn);
+            out[p] = ew + out[p];
+        }
+        free(ent);
+    }
+    free(gray);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Drivers.                                                                   */
+/* ------------------------------------------------------------------------- */
+
+int orc_enfuse(int K, const void* const* imgs, const uint8_t* const* alphas, int dtype,
+               int w, int h, int C, int pix_stride, const orc_enfuse_params* prm,
+               int levels, int wrap, int hard_mask, const float* const* masks_in,
+               void* out, uint8_t* out_alpha, int dither_mode, uint64_t seed,
+               int32_t* level0_out, float* masks_out)
+{
+    if (K < 1 || dtype == ORC_F32 || (C != 1 && C != 3)) {
+        return -2;
+    }
+    const int64_t npix = (int64_t)w * h;
+    const int bits = dtype == ORC_U8 ? 16 : 32;      /* numerictraits.h:159-163 */
+    const int frac = 7;
+    const int mbits = dtype == ORC_U8 ? 16 : 32;
+    const int mfrac = dtype == ORC_U8 ? 7 : 15;
+    const int32_t max_mask_pyr = 255 << mfrac;       /* enfuse.h:1554-1558 */
+    int rc = 0;
+
+    float** masks = (float**)malloc(sizeof(float*) * (size_t)K);
+    float* norm = (float*)calloc((size_t)npix, sizeof(float));
+    memset(out_alpha, 0, (size_t)npix);
+    for (int k = 0; k < K; ++k) {
+        masks[k] = (float*)malloc(sizeof(float) * (size_t)npix);
+        if (masks_in) {
+            memcpy(masks[k], masks_in[k], sizeof(float) * (size_t)npix);
+        } else {
+            rc = orc_enfuse_mask(imgs[k], dtype, w, h, C, pix_stride, alphas[k], prm, masks[k]);
+            if (rc) {
+                goto done;
+            }
+        }
+        for (int64_t p = 0; p < npix; ++p) {
+            if (alphas[k][p]) {
+                out_alpha[p] = alphas[k][p];            /* copyImageIf, enfuse.h:1377-1379 */
+            }
+            norm[p] = masks[k][p] + norm[p];            /* enfuse.h:1382-1385 */
+        }
+    }
+
+    if (hard_mask) {                                    /* enfuse.h:1399-1442 */
+#pragma omp parallel for schedule(static)
+        for (int64_t p = 0; p < npix; ++p) {
+            float mx = 0.0f;
+            int mi = 0;
+            for (int k = 0; k < K; ++k) {
+                if (masks[k][p] > mx) {
+                    mx = masks[k][p];
+                    mi = k;
+                }
+            }
+            for (int k = 0; k < K; ++k) {
+                masks[k][p] = mx == 0.0f ? 255.0f / (float)K : (k == mi ? 255.0f : 0.0f);
+            }
+        }
+    }
+
+    levels = levels > 0 ? levels : orc_num_levels(w, h, 1, 0);
+    pyr_t result;
+    memset(&result, 0, sizeof(result));
+    for (int k = 0; k < K && rc == 0; ++k) {
+        pyr_t lp, mg;
+        pyr_alloc(&lp, levels, w, h, C);
+        orc_fixed_from_int(imgs[k], dtype, npix, C, pix_stride, lp.lv[0], frac);
+        rc = gaussian_alpha(&lp, alphas[k], wrap, bits);
+        if (!rc) {
+            rc = laplacian_inplace(&lp, wrap, bits);
+        }
+        if (!hard_mask) {                               /* enfuse.h:1526-1535 */
+            const float fallback = (float)(255 / K);
+#pragma omp parallel for schedule(static)
+            for (int64_t p = 0; p < npix; ++p) {
+                masks[k][p] = norm[p] > 0.0f ? (255.0f * masks[k][p]) / norm[p] : fallback;
+            }
+        }
+        if (masks_out) {
+            memcpy(masks_out + (size_t)k * npix, masks[k], sizeof(float) * (size_t)npix);
+        }
+        pyr_alloc(&mg, levels, w, h, 1);
+        orc_fixed_from_float(masks[k], npix, mg.lv[0], mfrac, mbits);
+        if (!rc) {
+            rc = gaussian_alpha(&mg, out_alpha, wrap, mbits);   /* enfuse.h:1539-1546 */
+        }
+        for (int l = 0; l < levels && !rc; ++l) {
+            orc_mask_multiply(lp.lv[l], mg.lv[l], (int64_t)lp.w[l] * lp.h[l], C, max_mask_pyr, bits);
+        }
+        pyr_free(&mg);
+        if (k == 0) {
+            result = lp;
+        } else {
+            for (int l = 0; l < levels; ++l) {
+                orc_accumulate(lp.lv[l], result.lv[l], (int64_t)lp.w[l] * lp.h[l] * C, bits);
+            }
+            pyr_free(&lp);
+        }
+    }
+    if (!rc) {
+        rc = collapse(&result, wrap, bits);
+    }
+    if (!rc) {
+        if (level0_out) {
+            memcpy(level0_out, result.lv[0], sizeof(int32_t) * (size_t)npix * C);
+        }
+        const size_t esz = dtype == ORC_U8 ? 1 : 2;
+        memset(out, 0, esz * (size_t)npix * pix_stride);
+        orc_from_fixed(result.lv[0], out_alpha, npix, C, out, dtype, pix_stride, frac, dither_mode, seed);
+    }
+    pyr_free(&result);
+done:
+    for (int k = 0; k < K; ++k) {
+        if (masks[k]) {
+            free(masks[k]);
+        }
+    }
+    free(masks);
+    free(norm);
+    return rc;
+}
+
+int orc_enblend(const void* white, const uint8_t* white_alpha, const void* black,
+                const uint8_t* black_alpha, const uint8_t* mask, int dtype, int w, int h,
+                int C, int pix_stride, int levels, int wrap, void* out, uint8_t* out_alpha,
+                int dither_mode, uint64_t seed, int32_t* level0_out)
+{
+    if (dtype == ORC_F32 || C > 4) {
+        return -2;
+    }
+    const int64_t npix = (int64_t)w * h;
+    const int bits = dtype == ORC_U8 ? 16 : 32;
+    const int frac = 7;
+    const int mbits = dtype == ORC_U8 ? 16 : 32;
+    const int mfrac = dtype == ORC_U8 ? 7 : 15;
+    int rc;
+    levels = levels > 0 ? levels : orc_num_levels(w, h, 1, 0);
+
+    /* Mask Gaussian pyramid without alpha (enblend.h:384-388). */
+    pyr_t mg, wl, bl;
+    pyr_alloc(&mg, levels, w, h, 1);
+    orc_fixed_from_int(mask, ORC_U8, npix, 1, 1, mg.lv[0], mfrac);
+    rc = gaussian_noalpha(&mg, wrap, mbits);
+
+    /* White and black Laplacian pyramids (enblend.h:418-446). */
+    pyr_alloc(&wl, levels, w, h, C);
+    pyr_alloc(&bl, levels, w, h, C);
+    orc_fixed_from_int(white, dtype, npix, C, pix_stride, wl.lv[0], frac);
+    orc_fixed_from_int(black, dtype, npix, C, pix_stride, bl.lv[0], frac);
+    if (!rc) {
+        rc = gaussian_alpha(&wl, white_alpha, wrap, bits);
+    }
+    if (!rc) {
+        rc = laplacian_inplace(&wl, wrap, bits);
+    }
+    if (!rc) {
+        rc = gaussian_alpha(&bl, black_alpha, wrap, bits);
+    }
+    if (!rc) {
+        rc = laplacian_inplace(&bl, wrap, bits);
+    }
+    /* Black alpha becomes the union (enblend.h:461-464). */
+    for (int64_t p = 0; p < npix; ++p) {
+        out_alpha[p] = white_alpha[p] ? 255 : black_alpha[p];
+    }
+    if (!rc) {
+        for (int l = 0; l < levels; ++l) {             /* blend.h:81-121 */
+            orc_blend(mg.lv[l], wl.lv[l], bl.lv[l], (int64_t)bl.w[l] * bl.h[l], C, 255 << mfrac, bits);
+        }
+        rc = collapse(&bl, wrap, bits);                 /* enblend.h:503 */
+    }
+    if (!rc) {
+        if (level0_out) {
+            memcpy(level0_out, bl.lv[0], sizeof(int32_t) * (size_t)npix * C);
+        }
+        const size_t esz = dtype == ORC_U8 ? 1 : 2;
+        memcpy(out, black, esz * (size_t)npix * pix_stride);
+        orc_from_fixed(bl.lv[0], out_alpha, npix, C, out, dtype, pix_stride, frac, dither_mode, seed);
+    }
+    pyr_free(&mg);
+    pyr_free(&wl);
+    pyr_free(&bl);
+    return rc;
+}

@@ -1,0 +1,277 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+Integer and fixed-point stages must be bit-exact; enfuse weights are
+compared exactly as well (the kernels reproduce the reference's float/double
+rounding), and so are the final pixels for the same dither seed.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+SIZES = [(2, 2), (3, 2), (2, 3), (3, 3), (4, 5), (5, 7), (8, 8), (17, 9), (33, 31), (64, 16),
+         (65, 17), (100, 37), (257, 130)]
+
+
+def _dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _rand_level(rng, h, w, c, dtype, signed=False):
+    if dtype == "i16":
+        lo, hi = (-32640, 32640) if signed else (0, 32640)
+    else:
+        lo, hi = (-(1 << 23), 1 << 23) if signed else (0, 65535 << 7)
+    return rng.integers(lo, hi + 1, size=(h, w, c)).astype(np.int32)
+
+
+def _alpha(rng, h, w, kind):
+    if kind == "opaque":
+        return np.full((h, w), 255, np.uint8)
+    if kind == "holes":
+        return (rng.random((h, w)) < 0.6).astype(np.uint8) * 255
+    a = np.full((h, w), 255, np.uint8)
+    a[: h // 2, : w // 3] = 0
+    return a
+
+
+def _pyr(ctx, enbgpu, w, h, c, dt, levels=2):
+    return ctx.pyramid(levels, w, h, c, enbgpu.ENB_I16 if dt == "i16" else enbgpu.ENB_I32)
+
+
+def _hwc(level_chw):
+    return np.transpose(level_chw, (1, 2, 0)).astype(np.int32)
+
+
+@pytest.mark.parametrize("dt", ["i16", "i32"])
+@pytest.mark.parametrize("wrap", [False, True])
+@pytest.mark.parametrize("akind", ["opaque", "holes", "block"])
+def test_reduce_alpha(ctx, orc, dt, wrap, akind):
+    import enbgpu
+    rng = np.random.default_rng(11)
+    bits = 16 if dt == "i16" else 32
+    for (w, h) in SIZES:
+        for c in (1, 3):
+            src = _rand_level(rng, h, w, c, dt)
+            a = _alpha(rng, h, w, akind)
+            ref, ref_a = orc.reduce(src, a, bits, wrap)
+            p = _pyr(ctx, enbgpu, w, h, c, dt)
+            p.write(0, np.transpose(src, (2, 0, 1)))
+            dh, dw = (h + 1) >> 1, (w + 1) >> 1
+            sa, da = _dev(a), torch.zeros((dh, dw), dtype=torch.uint8, device="cuda")
+            ctx.reduce(p, 0, p, 1, wrap=wrap, src_alpha=sa, dst_alpha=da)
+            got = _hwc(p.read(1))
+            assert np.array_equal(got, ref), (w, h, c)
+            assert np.array_equal(da.cpu().numpy(), ref_a), (w, h, c)
+
+
+@pytest.mark.parametrize("dt", ["i16", "i32"])
+@pytest.mark.parametrize("wrap", [False, True])
+def test_reduce_noalpha(ctx, orc, dt, wrap):
+    import enbgpu
+    rng = np.random.default_rng(12)
+    bits = 16 if dt == "i16" else 32
+    for (w, h) in SIZES:
+        for c in (1, 3):
+            src = _rand_level(rng, h, w, c, dt)
+            ref = orc.reduce(src, None, bits, wrap)
+            p = _pyr(ctx, enbgpu, w, h, c, dt)
+            p.write(0, np.transpose(src, (2, 0, 1)))
+            ctx.reduce(p, 0, p, 1, wrap=wrap)
+            assert np.array_equal(_hwc(p.read(1)), ref), (w, h, c)
+
+
+@pytest.mark.parametrize("dt", ["i16", "i32"])
+@pytest.mark.parametrize("wrap", [False, True])
+@pytest.mark.parametrize("add", [False, True])
+def test_expand(ctx, orc, dt, wrap, add):
+    import enbgpu
+    rng = np.random.default_rng(13)
+    bits = 16 if dt == "i16" else 32
+    sizes = SIZES + [(1, 1), (2, 1), (1, 2), (1, 5), (6, 1)]
+    for (w, h) in sizes:
+        for c in (1, 3):
+            dh, dw = h, w
+            sh, sw = (h + 1) >> 1, (w + 1) >> 1
+            src = _rand_level(rng, sh, sw, c, dt, signed=True)
+            dst = _rand_level(rng, dh, dw, c, dt, signed=True)
+            if dt == "i16":
+                # full int16 range: exercises wrap-around (subtract) and saturation (add)
+                dst = rng.integers(-32768, 32768, size=dst.shape).astype(np.int32)
+            ref = orc.expand(src, dst, add, bits, wrap)
+            p = _pyr(ctx, enbgpu, w, h, c, dt)
+            p.write(0, np.transpose(dst, (2, 0, 1)))
+            p.write(1, np.transpose(src, (2, 0, 1)))
+            ctx.expand(p, 1, p, 0, add=add, wrap=wrap)
+            assert np.array_equal(_hwc(p.read(0)), ref), (w, h, c)
+
+
+@pytest.mark.parametrize("dt", ["i16", "i32"])
+def test_blend_level(ctx, orc, dt):
+    import enbgpu
+    rng = np.random.default_rng(14)
+    bits = 16 if dt == "i16" else 32
+    mfrac = 7 if dt == "i16" else 15
+    white_value = 255 << mfrac
+    for (w, h) in [(64, 16), (100, 37), (257, 130)]:
+        white = _rand_level(rng, h, w, 3, dt, signed=True)
+        black = _rand_level(rng, h, w, 3, dt, signed=True)
+        mask = rng.integers(-3, white_value + 3, size=(h, w, 1)).astype(np.int32)
+        mask[rng.random((h, w)) < 0.3] = 0
+        mask[rng.random((h, w)) < 0.3] = white_value
+        ref = orc.blend(mask, white, black, white_value, bits)
+        pw, pb, pm = (_pyr(ctx, enbgpu, w, h, 3, dt, 1), _pyr(ctx, enbgpu, w, h, 3, dt, 1),
+                      _pyr(ctx, enbgpu, w, h, 1, dt, 1))
+        pw.write(0, np.transpose(white, (2, 0, 1)))
+        pb.write(0, np.transpose(black, (2, 0, 1)))
+        pm.write(0, np.transpose(mask, (2, 0, 1)))
+        ctx.blend_level(pm, pw, pb, 0, white_value)
+        assert np.array_equal(_hwc(pb.read(0)), ref)
+
+
+@pytest.mark.parametrize("dt", ["i16", "i32"])
+@pytest.mark.parametrize("accumulate", [False, True])
+def test_mask_multiply_accumulate(ctx, orc, dt, accumulate):
+    import enbgpu
+    rng = np.random.default_rng(15)
+    bits = 16 if dt == "i16" else 32
+    mfrac = 7 if dt == "i16" else 15
+    D = 255 << mfrac
+    w, h = 257, 130
+    lp = _rand_level(rng, h, w, 3, dt, signed=True)
+    res = _rand_level(rng, h, w, 3, dt, signed=True)
+    mask = rng.integers(0, D + 1, size=(h, w, 1)).astype(np.int32)
+    # exact half-integer products: m = D/2 with odd lp, m = D/4 with lp = 2 mod 4
+    mask[:10] = D // 2
+    mask[10:20] = D // 4
+    mask[20:25] = 0
+    mask[25:30] = D
+    lp[:10] |= 1
+    lp[10:20] = (lp[10:20] & ~3) | 2
+    prod = orc.mask_multiply(lp, mask, D, bits)
+    ref = orc.accumulate(prod, res, bits) if accumulate else prod
+    pl, pm, pr = (_pyr(ctx, enbgpu, w, h, 3, dt, 1), _pyr(ctx, enbgpu, w, h, 1, dt, 1),
+                  _pyr(ctx, enbgpu, w, h, 3, dt, 1))
+    pl.write(0, np.transpose(lp, (2, 0, 1)))
+    pm.write(0, np.transpose(mask, (2, 0, 1)))
+    pr.write(0, np.transpose(res, (2, 0, 1)))
+    ctx.mask_multiply_accumulate(pl, pm, pr, 0, D, accumulate)
+    assert np.array_equal(_hwc(pr.read(0)), ref)
+
+
+@pytest.mark.parametrize("dt,out_dtype", [("i16", np.uint8), ("i32", np.uint16)])
+@pytest.mark.parametrize("dither", ["hash", "nearest"])
+def test_from_pyramid(ctx, orc, dt, out_dtype, dither):
+    import enbgpu
+    rng = np.random.default_rng(16)
+    w, h = 257, 130
+    maxv = np.iinfo(out_dtype).max
+    src = rng.integers(-300, (maxv + 2) << 7, size=(h, w, 3)).astype(np.int32)
+    if dt == "i16":
+        src = np.clip(src, -32768, 32767)
+    alpha = _alpha(rng, h, w, "holes")
+    ref = orc.from_fixed(src, alpha, out_dtype, 7, dither, seed=1234)
+    p = _pyr(ctx, enbgpu, w, h, 3, dt, 1)
+    p.write(0, np.transpose(src, (2, 0, 1)))
+    dst = torch.zeros((h, w, 3), dtype=torch.uint8 if out_dtype == np.uint8 else torch.uint16, device="cuda")
+    ctx.from_pyramid(p, 0, _dev(alpha), dst, 7, dither, seed=1234)
+    assert np.array_equal(dst.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("dt", [np.uint8, np.uint16])
+@pytest.mark.parametrize("proj", ["average", "value", "anti-value", "lightness", "luminance", "channel-mixer"])
+def test_enfuse_mask(ctx, orc, dt, proj):
+    import enbgpu
+    from enbgpu import synthetic
+    rng = np.random.default_rng(17)
+    h, w = 61, 83
+    lr = synthetic.log_radiance(h, w, 10.0, seed=5)
+    for ev in (-2.0, 0.0, 2.5):
+        img = synthetic.expose(lr, ev, dt, noise=2.0 ** -10, seed=3)
+        alpha = _alpha(rng, h, w, "holes" if ev > 0 else "opaque")
+        kw = dict(exposure_weight=1.0, saturation_weight=0.2, contrast_weight=0.5, entropy_weight=0.3,
+                  contrast_window_size=5, entropy_window_size=5, gray_projector=proj, mixer=(0.3, 0.59, 0.11))
+        ref = orc.enfuse_mask(img, alpha, orc.params(**kw))
+        out = torch.zeros((h, w), dtype=torch.float32, device="cuda")
+        ctx.enfuse_mask(_dev(img), _dev(alpha), out, enbgpu.enfuse_params(**kw))
+        got = out.cpu().numpy()
+        assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), np.abs(got - ref).max()
+
+
+@pytest.mark.parametrize("fn", ["gaussian", "lorentzian", "halfsine", "fullsine", "bisquare"])
+@pytest.mark.parametrize("window", [3, 7])
+def test_enfuse_mask_functions(ctx, orc, fn, window):
+    import enbgpu
+    from enbgpu import synthetic
+    h, w = 40, 52
+    img = synthetic.exposure_stack(h, w, [0.5], np.uint16, 8.0, seed=9)[0]
+    alpha = np.full((h, w), 255, np.uint8)
+    kw = dict(exposure_weight=0.7, saturation_weight=0.4, contrast_weight=0.9, entropy_weight=0.6,
+              exposure_optimum=0.4, exposure_width=0.25, exposure_weight_function=fn,
+              contrast_window_size=window, entropy_window_size=window)
+    ref = orc.enfuse_mask(img, alpha, orc.params(**kw))
+    out = torch.zeros((h, w), dtype=torch.float32, device="cuda")
+    ctx.enfuse_mask(_dev(img), _dev(alpha), out, enbgpu.enfuse_params(**kw))
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), ref.view(np.uint32))
+
+
+def _stack(dt, h, w, n, seed):
+    from enbgpu import synthetic
+    evs = np.linspace(-2, 2, n)
+    return synthetic.exposure_stack(h, w, evs, dt, 8.0, seed, noise=2.0 ** -11)
+
+
+@pytest.mark.parametrize("dt", [np.uint8, np.uint16])
+@pytest.mark.parametrize("hard", [False, True])
+@pytest.mark.parametrize("wrap", [False, True])
+def test_enfuse_end_to_end(ctx, orc, dt, hard, wrap):
+    import enbgpu
+    h, w = 75, 97
+    imgs = _stack(dt, h, w, 3, seed=21)
+    rng = np.random.default_rng(3)
+    alphas = [np.full((h, w), 255, np.uint8) for _ in imgs]
+    alphas[1][10:30, 5:40] = 0
+    kw = dict(exposure_weight=1.0, saturation_weight=0.2, contrast_weight=0.5, entropy_weight=0.3,
+              contrast_window_size=5, entropy_window_size=5)
+    ref = orc.enfuse(imgs, alphas, orc.params(**kw), hard_mask=hard, wrap=wrap, seed=77, want_level0=True)
+    l0 = torch.zeros((h, w, 3), dtype=torch.int32, device="cuda")
+    out, oa = ctx.enfuse([_dev(x) for x in imgs], [_dev(a) for a in alphas], enbgpu.enfuse_params(**kw),
+                         hard_mask=hard, wrap=wrap, seed=77, level0=l0)
+    assert np.array_equal(l0.cpu().numpy(), ref["level0"])
+    assert np.array_equal(oa.cpu().numpy(), ref["alpha"])
+    assert np.array_equal(out.cpu().numpy(), ref["out"])
+
+
+@pytest.mark.parametrize("dt", [np.uint8, np.uint16])
+def test_enfuse_host_buffers_and_injected_masks(ctx, orc, dt):
+    import enbgpu
+    h, w = 50, 66
+    imgs = _stack(dt, h, w, 4, seed=22)
+    rng = np.random.default_rng(4)
+    masks = [rng.random((h, w)).astype(np.float32) for _ in imgs]
+    masks[0][:5] = 0.0
+    for m in masks:
+        m[:5, :5] = 0.0  # all-zero weights -> integer 255/K fallback
+    ref = orc.enfuse(imgs, None, masks=masks, seed=5, want_level0=True)
+    l0 = np.zeros((h, w, 3), np.int32)
+    out, oa = ctx.enfuse(imgs, masks=masks, seed=5, level0=l0)
+    assert np.array_equal(l0, ref["level0"])
+    assert np.array_equal(out, ref["out"])
+
+
+@pytest.mark.parametrize("dt", [np.uint8, np.uint16])
+@pytest.mark.parametrize("wrap", [False, True])
+def test_enblend_end_to_end(ctx, orc, dt, wrap):
+    from enbgpu import synthetic
+    white, black, mask = synthetic.panorama_pair(90, 120, 80, dt, seed=31)
+    ref = orc.enblend(white, black, mask, wrap=wrap, seed=9, want_level0=True)
+    l0 = torch.zeros((90, 200, 3), dtype=torch.int32, device="cuda")
+    out, oa = ctx.enblend(_dev(white), _dev(black), _dev(mask), wrap=wrap, seed=9, level0=l0)
+    assert np.array_equal(l0.cpu().numpy(), ref["level0"])
+    assert np.array_equal(oa.cpu().numpy(), ref["alpha"])
+    assert np.array_equal(out.cpu().numpy(), ref["out"])
+    # host-buffer entry point gives the same image
+    out2, _ = ctx.enblend(white, black, mask, wrap=wrap, seed=9)
+    assert np.array_equal(out2, ref["out"])
