@@ -1,0 +1,346 @@
+#!/usr/bin/env python3
+"""Benchmark of the enblend/enfuse multiresolution path on GB300.
+
+Default workload: enblend's two-image pyramid blend of 2 x 4096x3072 RGBA
+uint16 images offset by 2867 px (union canvas 6963x3072, 10 levels) under a
+random-walk seam mask, synthetic and seeded.  Metric: Mpx*exposures/s, the
+input pixels blended per second (2 x 4096 x 3072 = 25.17 Mpx per step).
+
+  value  device-resident inputs, one enb_enblend call per step (CUDA events
+         on the library's stream, which is torch's current stream)
+  e2e    the same call with pinned host buffers: host->device copies of both
+         images and the mask, the blend, device->host copies of the image
+         and its alpha, every step
+  roofline  the dominant kernel from the library's per-launch CUDA-event
+         profile: algorithmic bytes / device time, against the measured HBM
+         copy bandwidth
+  cpu_baseline  the CPU oracle (a port of the reference's algorithm: serial
+         pyramids, OpenMP pointwise steps) on a quarter of the rows
+
+--impl reference times that CPU implementation alone on the same metric.
+Multi-GPU runs are independent replicas (the path does not shard): each rank
+blends its own copy, value = total Mpx / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+REPO = Path(__file__).resolve().parent
+for _p in (REPO, REPO / "enblend-enfuse_gb300"):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+import numpy as np  # noqa: E402
+
+WORKLOAD = "enblend 2x4096x3072 RGBA u16, offset 2867 (union 6963x3072), 10 levels"
+H, W, OFFSET = 3072, 4096, 2867
+UNITS = 2 * W * H / 1e6              # Mpx*exposures per step
+CPU_ROWS = 768                       # bounded CPU sample: a quarter of the rows
+METRIC = "Mpx*exposures/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-only", action="store_true",
+                    help="run warmup + steps on device inputs only (for ncu launch lists)")
+    return ap.parse_args()
+
+
+# --------------------------------------------------------------------------
+# clocks sampled during the timed region
+# --------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu, self.rows, self.proc, self.thread = gpu, [], None, None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "50", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append((time.time(), [x.strip() for x in line.split(",")]))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+
+    def summary(self, t0: float, t1: float) -> dict:
+        inside = [r for t, r in self.rows if t0 <= t <= t1 + 0.05]
+        note = "sampled during the timed region"
+        if not inside:
+            # the region is shorter than the sampling interval: nearest samples
+            inside = [r for t, r in self.rows if t0 - 0.5 <= t <= t1 + 0.5]
+            note = "timed region shorter than the 50 ms sampling interval; samples within 0.5 s of it"
+        if not inside:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "note": "nvidia-smi unavailable"}
+        sm = [float(r[2]) for r in inside if r[2].replace(".", "").isdigit()]
+        mx = [float(r[3]) for r in inside if r[3].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in inside:
+            for n, v in zip(names, r[6:10]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(inside), "note": note}
+
+
+# --------------------------------------------------------------------------
+# helpers
+# --------------------------------------------------------------------------
+
+def measured_peaks() -> dict:
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d.get("hbm_gbs"), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def ncu_traffic() -> dict:
+    """Per-launch DRAM bytes of each kernel from the committed ncu summary, if any."""
+    p = REPO / "profiles" / "traffic_enblend_2x4096x3072_u16.txt"
+    out = {}
+    if p.exists():
+        for line in p.read_text().splitlines():
+            parts = line.split()
+            if len(parts) == 2 and not line.startswith("#"):
+                try:
+                    out[parts[0]] = float(parts[1])
+                except ValueError:
+                    pass
+    return out
+
+
+def make_inputs(seed: int, rows: int = H):
+    from enbgpu import synthetic
+    return synthetic.panorama_pair(rows, W, OFFSET, np.uint16, seed)
+
+
+def cpu_oracle_rate(seed: int, repeats: int = 3) -> dict:
+    """Time the CPU oracle on the bounded sample (rows 0..CPU_ROWS of the scene)."""
+    from oracle import oracle
+    white, black, mask = make_inputs(seed, CPU_ROWS)
+    oracle.enblend(white, black, mask)  # warm (builds, pages in)
+    times = []
+    for _ in range(repeats):
+        t = time.perf_counter()
+        oracle.enblend(white, black, mask)
+        times.append(time.perf_counter() - t)
+    units = 2 * W * CPU_ROWS / 1e6
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": units / statistics.median(times), "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"2 x 4096x{CPU_ROWS} RGBA u16 (quarter of the rows of the workload), median of {repeats}; "
+                      f"serial pyramid passes and OpenMP pointwise passes as in the reference"}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# --------------------------------------------------------------------------
+# arms
+# --------------------------------------------------------------------------
+
+def run_reference(args) -> None:
+    ws, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    from oracle import oracle
+    white, black, mask = make_inputs(args.seed, CPU_ROWS)
+    units = 2 * W * CPU_ROWS / 1e6
+    for _ in range(args.warmup):
+        oracle.enblend(white, black, mask)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.enblend(white, black, mask)
+    dt = time.perf_counter() - t0
+    value = units * args.steps / dt
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample_rows": CPU_ROWS},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
+                         "sample": f"each step: 2 x 4096x{CPU_ROWS} RGBA u16 (a quarter of the rows)"},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args) -> None:
+    import torch
+    import enbgpu
+
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    ctx = enbgpu.Context(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+
+    white, black, mask = make_inputs(args.seed + rank * 0)
+    dw, db, dm = (torch.from_numpy(x).cuda() for x in (white, black, mask))
+    out = torch.empty_like(db)
+    oa = torch.empty(mask.shape, dtype=torch.uint8, device="cuda")
+
+    def step():
+        ctx.enblend(dw, db, dm, out=out, out_alpha=oa)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if args.profile_only:
+        for _ in range(args.steps):
+            step()
+        torch.cuda.synchronize()
+        return
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident timed region ----
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    launches0 = ctx.launches
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.time()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    barrier()
+    t1 = time.time()
+    sampler.stop()
+    launches = ctx.launches - launches0
+    ms = e0.elapsed_time(e1)
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * UNITS * args.steps / (ms / 1e3)
+
+    # ---- end to end through the host-buffer entry point (pinned memory) ----
+    pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
+    hw, hb, hm = pin(white), pin(black), pin(mask)
+    ho = torch.empty(black.shape, dtype=torch.uint16).pin_memory().numpy()
+    hoa = torch.empty(mask.shape, dtype=torch.uint8).pin_memory().numpy()
+    e2e_steps = max(3, min(args.steps, 20))
+    for _ in range(2):
+        ctx.enblend(hw, hb, hm, out=ho, out_alpha=hoa)
+    barrier()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(e2e_steps):
+        ctx.enblend(hw, hb, hm, out=ho, out_alpha=hoa)
+    f1.record(stream)
+    barrier()
+    e2e_ms = f0.elapsed_time(f1)
+    if ws > 1:
+        t = torch.tensor([e2e_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = ws * UNITS * e2e_steps / (e2e_ms / 1e3)
+    h2d = hw.nbytes + hb.nbytes + hm.nbytes
+    d2h = ho.nbytes + hoa.nbytes
+
+    # ---- per-kernel profile (CUDA events per launch) ----
+    ctx.profile(True)
+    prof_steps = max(3, min(args.steps, 20))
+    for _ in range(prof_steps):
+        step()
+    report = ctx.profile_report()
+    ctx.profile(False)
+    total_ms = sum(v["ms"] for v in report.values())
+    dom = max(report, key=lambda k: report[k]["ms"])
+    d = report[dom]
+    peaks = measured_peaks()
+    achieved = d["bytes"] / (d["ms"] / 1e3) / 1e9
+    traffic = ncu_traffic().get(dom)
+    per_launch_bytes = d["bytes"] / d["launches"]
+    roofline = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"] if peaks["hbm_gbs"] else None,
+                "peak_source": peaks["source"], "algorithmic_bytes_per_launch": per_launch_bytes,
+                "traffic": traffic, "share_of_device_time": d["ms"] / total_ms if total_ms else None}
+    kernels = {k: {"launches_per_step": v["launches"] / prof_steps, "ms_per_step": v["ms"] / prof_steps,
+                   "GBps": v["bytes"] / (v["ms"] / 1e3) / 1e9 if v["ms"] > 0 else None}
+               for k, v in sorted(report.items(), key=lambda kv: -kv[1]["ms"])}
+    pipeline_bytes = sum(v["bytes"] for v in report.values()) / prof_steps
+
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "levels": enbgpu.num_levels(W + OFFSET, H), "pixel": "RGBA u16",
+                   "pyramid": "int32 17.7 fixed point, mask int32 9.15", "parallelism": f"replicas x{ws}",
+                   "l2": "inputs larger than L2 (each image 171 MB)"},
+        "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_ms / e2e_steps},
+        "gpu_launches": launches,
+        "roofline": roofline,
+        "kernels": kernels,
+        "pipeline": {"algorithmic_bytes_per_step": pipeline_bytes,
+                     "GBps": pipeline_bytes / (ms / args.steps / 1e3) / 1e9},
+        "clocks": sampler.summary(t0, t1),
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_oracle_rate(args.seed)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -21,6 +21,21 @@ struct enb_ctx {
     cudaStream_t stream = nullptr;
     std::string err;
     uint64_t launches = 0;
+    // kernel profiling (enb_profile_*)
+    struct ProfKernel {
+        std::string name;
+        uint64_t launches = 0;
+        double ms = 0.0;
+        double bytes = 0.0;
+    };
+    struct ProfPending {
+        size_t k;
+        cudaEvent_t a, b;
+    };
+    bool prof = false;
+    std::vector<ProfKernel> kernels;
+    std::vector<ProfPending> pending;
+    std::vector<cudaEvent_t> pool;
     // cached enfuse weight tables
     std::string table_key;
     void* table_mem = nullptr;
@@ -66,9 +81,71 @@ enb_status cuda_fail(enb_ctx* ctx, cudaError_t e, const char* where)
     return fail(ctx, ENB_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
 
+cudaEvent_t prof_event(enb_ctx* ctx)
+{
+    if (!ctx->pool.empty()) {
+        cudaEvent_t e = ctx->pool.back();
+        ctx->pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+cudaEvent_t prof_begin(enb_ctx* ctx)
+{
+    if (!ctx->prof) {
+        return nullptr;
+    }
+    cudaEvent_t a = prof_event(ctx);
+    cudaEventRecord(a, ctx->stream);
+    return a;
+}
+
+void prof_end(enb_ctx* ctx, cudaEvent_t a)
+{
+    if (!a) {
+        return;
+    }
+    cudaEvent_t b = prof_event(ctx);
+    cudaEventRecord(b, ctx->stream);
+    const LaunchInfo& li = last_launch();
+    size_t k = 0;
+    while (k < ctx->kernels.size() && ctx->kernels[k].name != li.name) {
+        ++k;
+    }
+    if (k == ctx->kernels.size()) {
+        ctx->kernels.push_back(enb_ctx::ProfKernel{li.name, 0, 0.0, 0.0});
+    }
+    ctx->kernels[k].launches++;
+    ctx->kernels[k].bytes += li.bytes;
+    ctx->pending.push_back(enb_ctx::ProfPending{k, a, b});
+}
+
+// Sum the elapsed times of finished launches (synchronises the stream).
+void prof_resolve(enb_ctx* ctx)
+{
+    if (ctx->pending.empty()) {
+        return;
+    }
+    cudaStreamSynchronize(ctx->stream);
+    for (auto& p : ctx->pending) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+            ctx->kernels[p.k].ms += ms;
+        }
+        ctx->pool.push_back(p.a);
+        ctx->pool.push_back(p.b);
+    }
+    ctx->pending.clear();
+}
+
 #define ENB_LAUNCH(ctx, call)                                  \
     do {                                                       \
+        cudaEvent_t a_ = prof_begin(ctx);                      \
         cudaError_t e_ = (call);                               \
+        prof_end((ctx), a_);                                   \
         (ctx)->launches++;                                     \
         if (e_ != cudaSuccess) {                               \
             return cuda_fail((ctx), e_, #call);                \
@@ -697,6 +774,13 @@ enb_status enb_create(int device, enb_ctx** out)
     if (cudaSetDevice(device) != cudaSuccess) {
         return ENB_ERR_CUDA;
     }
+    // Keep freed pyramid memory in the stream-ordered pool across
+    // synchronisations instead of returning it to the driver after each call.
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     enb_ctx* ctx = new enb_ctx();
     ctx->device = device;
     *out = ctx;
@@ -712,7 +796,47 @@ enb_status enb_destroy(enb_ctx* ctx)
         cudaFreeAsync(ctx->table_mem, ctx->stream);
         cudaStreamSynchronize(ctx->stream);
     }
+    prof_resolve(ctx);
+    for (cudaEvent_t e : ctx->pool) {
+        cudaEventDestroy(e);
+    }
     delete ctx;
+    return ENB_OK;
+}
+
+enb_status enb_profile_enable(enb_ctx* ctx, int enable)
+{
+    if (!ctx) {
+        return ENB_ERR_INVALID;
+    }
+    prof_resolve(ctx);
+    ctx->kernels.clear();
+    ctx->prof = enable != 0;
+    return ENB_OK;
+}
+
+int enb_profile_count(enb_ctx* ctx) { return ctx ? (int)ctx->kernels.size() : 0; }
+
+enb_status enb_profile_entry(enb_ctx* ctx, int i, const char** name, uint64_t* launches, double* total_ms,
+                             double* bytes)
+{
+    if (!ctx || i < 0 || i >= (int)ctx->kernels.size()) {
+        return ENB_ERR_INVALID;
+    }
+    prof_resolve(ctx);
+    const auto& k = ctx->kernels[(size_t)i];
+    if (name) {
+        *name = k.name.c_str();
+    }
+    if (launches) {
+        *launches = k.launches;
+    }
+    if (total_ms) {
+        *total_ms = k.ms;
+    }
+    if (bytes) {
+        *bytes = k.bytes;
+    }
     return ENB_OK;
 }
 

@@ -76,6 +76,10 @@ _SIGNATURES = {
     "enb_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
     "enb_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "enb_launch_count": (ctypes.c_uint64, [ctypes.c_void_p]),
+    "enb_profile_enable": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "enb_profile_count": (ctypes.c_int, [ctypes.c_void_p]),
+    "enb_profile_entry": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _P(ctypes.c_char_p), _P(ctypes.c_uint64),
+                                         _P(ctypes.c_double), _P(ctypes.c_double)]),
     "enb_default_enfuse_params": (None, [_P(EnbEnfuseParams)]),
     "enb_default_fuse_options": (None, [_P(EnbFuseOptions)]),
     "enb_num_levels": (ctypes.c_int, [ctypes.c_int] * 4),
@@ -280,6 +284,20 @@ class Context:
     @property
     def launches(self) -> int:
         return int(self.lib.enb_launch_count(self.handle))
+
+    def profile(self, enable: bool) -> None:
+        """Start (or stop) per-kernel CUDA-event timing; clears earlier records."""
+        self._check(self.lib.enb_profile_enable(self.handle, int(enable)))
+
+    def profile_report(self) -> dict:
+        """{kernel: {"launches", "ms", "bytes"}} of the launches since profiling started."""
+        out = {}
+        for i in range(self.lib.enb_profile_count(self.handle)):
+            name, n, ms, b = ctypes.c_char_p(), ctypes.c_uint64(), ctypes.c_double(), ctypes.c_double()
+            self._check(self.lib.enb_profile_entry(self.handle, i, ctypes.byref(name), ctypes.byref(n),
+                                                   ctypes.byref(ms), ctypes.byref(b)))
+            out[name.value.decode()] = {"launches": int(n.value), "ms": ms.value, "bytes": b.value}
+        return out
 
     # ---- pyramids ---------------------------------------------------------
     def pyramid(self, levels: int, width: int, height: int, channels: int, dtype: int) -> Pyramid:

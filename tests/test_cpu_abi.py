@@ -1,0 +1,67 @@
+"""CPU-side checks of the C ABI library: it loads, exports every symbol the
+header declares, and its host-only logic matches the oracle (no GPU needed)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from enbgpu import _build
+    _build.build()
+    import enbgpu
+    return enbgpu.load_library()
+
+
+def test_exports_every_header_symbol(lib):
+    import enbgpu
+    names = enbgpu.header_functions()
+    assert len(names) >= 30
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_abi_version(lib):
+    assert lib.enb_abi_version() == 1
+
+
+def test_num_levels_matches_oracle(lib, orc):
+    rng = np.random.default_rng(0)
+    sizes = [(1, 1), (8, 8), (9, 9), (16, 17), (768, 1024), (3072, 6963), (4000, 6000), (2048, 2048)]
+    sizes += [tuple(rng.integers(1, 20000, 2)) for _ in range(200)]
+    for h, w in sizes:
+        for exact in (0, 1, 3, 50, -1, -4, -100):
+            assert lib.enb_num_levels(int(w), int(h), 1, exact) == orc.num_levels(int(w), int(h), 1, exact)
+
+
+def test_level_counts_of_the_workloads(lib):
+    # roiBounds: 768 -> 8, 3072 -> 10, 4000 -> 10, 2048 -> 9 levels
+    assert lib.enb_num_levels(1024, 768, 1, 0) == 8
+    assert lib.enb_num_levels(6963, 3072, 1, 0) == 10
+    assert lib.enb_num_levels(6000, 4000, 1, 0) == 10
+    assert lib.enb_num_levels(2048, 2048, 1, 0) == 9
+
+
+def test_defaults_match_enfuse_cli(lib):
+    import enbgpu
+    p = enbgpu.EnbEnfuseParams()
+    lib.enb_default_enfuse_params(ctypes.byref(p))
+    assert (p.w_exposure, p.w_saturation, p.w_contrast, p.w_entropy) == (1.0, 0.0, 0.0, 0.0)
+    assert (p.exp_optimum, p.exp_width) == (0.5, 0.2)
+    assert (p.contrast_window, p.entropy_window) == (5, 3)
+
+
+def test_create_without_device_fails_cleanly(lib):
+    """No CUDA device in this container: enb_create reports ENB_ERR_CUDA, never falls back."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    h = ctypes.c_void_p()
+    assert lib.enb_create(0, ctypes.byref(h)) == 3
+    assert not h.value
+
+
+def test_null_context_is_rejected(lib):
+    assert lib.enb_synchronize(None) == 1
+    assert lib.enb_destroy(None) == 1
