@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -15,6 +16,11 @@
 #include "enbgpu.h"
 
 using namespace enb;
+
+// Scratch of enb_gaussian_pyramid_noalloc: the alpha planes of pyramid levels
+// 1..L-1.  Host code must not use this name as an address; it looks the
+// device address up with cudaGetSymbolAddress (noalloc_scratch below).
+static __device__ __align__(256) unsigned char g_noalloc_scratch[ENB_NOALLOC_SCRATCH_BYTES];
 
 struct enb_ctx {
     int device = 0;
@@ -750,6 +756,38 @@ bool same_geometry(const enb_image* a, const enb_image* b)
     return a->width == b->width && a->height == b->height && a->channels == b->channels && a->dtype == b->dtype;
 }
 
+// Device address of g_noalloc_scratch on the context's device, looked up on
+// the first call per device with that device current, then cached.
+constexpr int kMaxNoAllocDevices = 128;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kMaxNoAllocDevices] = {};
+
+enb_status noalloc_scratch(enb_ctx* ctx, void** out)
+{
+    if (ctx->device < 0 || ctx->device >= kMaxNoAllocDevices) {
+        return fail(ctx, ENB_ERR_INVALID, "noalloc: device ordinal out of range");
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[ctx->device]) {
+        int cur = -1;
+        ENB_CUDA(ctx, cudaGetDevice(&cur));
+        if (cur != ctx->device) {
+            ENB_CUDA(ctx, cudaSetDevice(ctx->device));
+        }
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (cur != ctx->device) {
+            cudaSetDevice(cur);
+        }
+        if (e != cudaSuccess || !p) {
+            return cuda_fail(ctx, e == cudaSuccess ? cudaErrorInvalidSymbol : e, "cudaGetSymbolAddress(noalloc scratch)");
+        }
+        g_noalloc_ptr[ctx->device] = p;
+    }
+    *out = g_noalloc_ptr[ctx->device];
+    return ENB_OK;
+}
+
 }  // namespace
 
 // ============================================================================
@@ -1104,6 +1142,72 @@ enb_status enb_gaussian_pyramid(enb_ctx* ctx, int wrap, const enb_image* src, co
         return gaussian_levels(ctx, wrap != 0, pyr, &a);
     }
     return gaussian_levels(ctx, wrap != 0, pyr, nullptr);
+}
+
+// Allocation-free variant of enb_gaussian_pyramid: the reduced alpha planes
+// go to g_noalloc_scratch instead of a stream-ordered allocation.  Launches
+// bypass the profiler (which creates CUDA events on demand).
+enb_status enb_gaussian_pyramid_noalloc(enb_ctx* ctx, int wrap, const enb_image* src, const enb_image* alpha,
+                                        int frac, enb_pyramid* p)
+{
+    if (!ctx || !p) {
+        return ENB_ERR_INVALID;
+    }
+    ENB_CHECK(ctx, src && src->width == p->w[0] && src->height == p->h[0], "noalloc: src size differs from level 0");
+    ENB_CHECK(ctx, frac >= 0 && frac <= 24, "noalloc: frac_bits outside 0..24");
+    const PlanarView l0 = level_view(p, 0);
+    if (src->dtype == ENB_F32) {
+        ENB_CHECK(ctx, src->channels == 1 && p->C == 1 && floats_ok(src, src->width, src->height),
+                  "noalloc: F32 sources are single-channel planes");
+    } else {
+        ENB_CHECK(ctx, pixels_ok(src) && src->channels == p->C, "noalloc: src must be interleaved U8/U16 of the pyramid's channels");
+    }
+    if (alpha) {
+        ENB_CHECK(ctx, bytes_ok(alpha, src->width, src->height), "noalloc: alpha must be U8 of the image size");
+    }
+    // Layout of the alpha planes of levels 1..L-1 in the scratch array.
+    int64_t off[kMaxLevels + 1] = {}, pitch[kMaxLevels + 1] = {};
+    int64_t total = 0;
+    for (int l = 1; l < p->levels; ++l) {
+        pitch[l] = round_up(p->w[l], 128);
+        off[l] = total;
+        total += round_up(pitch[l] * p->h[l], 256);
+    }
+    if (alpha && total > (int64_t)ENB_NOALLOC_SCRATCH_BYTES) {
+        return fail(ctx, ENB_ERR_INVALID,
+                    "noalloc: the reduced alpha planes need " + std::to_string(total) + " bytes, more than the " +
+                        std::to_string((unsigned)ENB_NOALLOC_SCRATCH_BYTES) + "-byte scratch (about 48 Mpx at level 0)");
+    }
+    for (int l = 1; l < p->levels; ++l) {
+        ENB_CHECK(ctx, p->w[l - 1] > 1 && p->h[l - 1] > 1, "reduce: src image too small in reduce");
+    }
+    uint8_t* scratch = nullptr;
+    if (alpha) {
+        void* s = nullptr;
+        ENB_TRY(noalloc_scratch(ctx, &s));
+        scratch = (uint8_t*)s;
+    }
+    cudaError_t e = src->dtype == ENB_F32 ? launch_float_to_fixed(float_plane(src), l0, frac, ctx->stream)
+                                          : launch_to_fixed(pixel_view(src), l0, frac, ctx->stream);
+    ctx->launches++;
+    if (e != cudaSuccess) {
+        return cuda_fail(ctx, e, "noalloc: conversion to fixed point");
+    }
+    for (int l = 1; l < p->levels; ++l) {
+        if (alpha) {
+            const BytePlane sa = l == 1 ? byte_plane(alpha)
+                                        : BytePlane{scratch + off[l - 1], pitch[l - 1], p->w[l - 1], p->h[l - 1]};
+            const BytePlane da{scratch + off[l], pitch[l], p->w[l], p->h[l]};
+            e = launch_reduce(wrap != 0, level_view(p, l - 1), &sa, level_view(p, l), &da, ctx->stream);
+        } else {
+            e = launch_reduce(wrap != 0, level_view(p, l - 1), nullptr, level_view(p, l), nullptr, ctx->stream);
+        }
+        ctx->launches++;
+        if (e != cudaSuccess) {
+            return cuda_fail(ctx, e, "noalloc: reduce");
+        }
+    }
+    return ENB_OK;
 }
 
 enb_status enb_laplacian_pyramid(enb_ctx* ctx, int wrap, const enb_image* src, const enb_image* alpha, int frac,

@@ -98,6 +98,8 @@ _SIGNATURES = {
                                         ctypes.c_uint64]),
     "enb_gaussian_pyramid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _IMG, _IMG, ctypes.c_int,
                                             ctypes.c_void_p]),
+    "enb_gaussian_pyramid_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _IMG, _IMG, ctypes.c_int,
+                                                    ctypes.c_void_p]),
     "enb_laplacian_pyramid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _IMG, _IMG, ctypes.c_int,
                                              ctypes.c_void_p]),
     "enb_collapse_pyramid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),

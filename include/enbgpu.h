@@ -200,6 +200,21 @@ enb_status enb_from_pyramid(enb_ctx* ctx, const enb_image* src, const enb_image*
 /* gaussianPyramid (src/pyramid.h:1468-1636); alpha NULL -> alpha-free reduce. */
 enb_status enb_gaussian_pyramid(enb_ctx* ctx, int wraparound, const enb_image* src,
                                 const enb_image* alpha, int frac_bits, enb_pyramid* pyr);
+/* No counterpart in the reference.  Same result as enb_gaussian_pyramid, but
+ * the call allocates nothing: for callers that must not allocate device
+ * memory while they run, such as an application that reserves its whole GPU
+ * budget up front in its own pool and forbids allocations in its processing
+ * callbacks (cudaMalloc can block the device and can fail mid-run), or a
+ * fixed-budget embedded pipeline.  The alpha planes of levels 1..L-1 live in
+ * a file-scope device array of ENB_NOALLOC_SCRATCH_BYTES (16 MiB, about
+ * 48 Mpx at level 0) that every GPU loading the library holds until exit;
+ * larger images are rejected with ENB_ERR_INVALID.  The first call on each
+ * device looks up that array's device address (make that first call before
+ * any stream capture).  All calls share the array: calls that overlap on the
+ * GPU (other streams, other threads) race on it. */
+#define ENB_NOALLOC_SCRATCH_BYTES (16u << 20)
+enb_status enb_gaussian_pyramid_noalloc(enb_ctx* ctx, int wraparound, const enb_image* src,
+                                        const enb_image* alpha, int frac_bits, enb_pyramid* pyr);
 /* laplacianPyramid (src/pyramid.h:1647-1747). */
 enb_status enb_laplacian_pyramid(enb_ctx* ctx, int wraparound, const enb_image* src,
                                  const enb_image* alpha, int frac_bits, enb_pyramid* pyr);
