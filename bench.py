@@ -57,6 +57,10 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-only", action="store_true",
                     help="run warmup + steps on device inputs only (for ncu launch lists)")
+    ap.add_argument("--rows", type=int, default=H,
+                    help="with --profile-only: scene height (a smaller case of the same workload for ncu)")
+    ap.add_argument("--plain", action="store_true",
+                    help="with --profile-only: the reference's pass structure instead of the fused passes")
     return ap.parse_args()
 
 
@@ -217,22 +221,22 @@ def run_ours(args) -> None:
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
 
-    white, black, mask = make_inputs(args.seed + rank * 0)
+    white, black, mask = make_inputs(args.seed, args.rows if args.profile_only else H)
     dw, db, dm = (torch.from_numpy(x).cuda() for x in (white, black, mask))
     out = torch.empty_like(db)
     oa = torch.empty(mask.shape, dtype=torch.uint8, device="cuda")
 
-    def step():
-        ctx.enblend(dw, db, dm, out=out, out_alpha=oa)
+    def step(plain=False):
+        ctx.enblend(dw, db, dm, out=out, out_alpha=oa, plain=plain)
 
+    if args.profile_only:
+        for _ in range(args.warmup + args.steps):
+            step(args.plain)
+        torch.cuda.synchronize()
+        return
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    if args.profile_only:
-        for _ in range(args.steps):
-            step()
-        torch.cuda.synchronize()
-        return
 
     def barrier():
         if ws > 1:
@@ -261,6 +265,18 @@ def run_ours(args) -> None:
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     value = ws * UNITS * args.steps / (ms / 1e3)
+
+    # ---- the reference's pass structure on the same GPU, for comparison ----
+    plain_steps = max(3, min(args.steps, 20))
+    step(plain=True)
+    barrier()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    for _ in range(plain_steps):
+        step(plain=True)
+    p1.record(stream)
+    barrier()
+    plain_ms = p0.elapsed_time(p1) / plain_steps
 
     # ---- end to end through the host-buffer entry point (pinned memory) ----
     pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
@@ -318,6 +334,8 @@ def run_ours(args) -> None:
                    "l2": "inputs larger than L2 (each image 171 MB)"},
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_ms / e2e_steps},
+        "plain_passes": {"value": UNITS / (plain_ms / 1e3), "unit": METRIC, "ms_per_step": plain_ms,
+                         "what": "same call with one kernel per reference operation (enb_fuse_options.plain)"},
         "gpu_launches": launches,
         "roofline": roofline,
         "kernels": kernels,

@@ -603,9 +603,11 @@ enb_status stage_out(enb_ctx* ctx, const enb_image* host, const Staged& s)
 
 // ---- drivers ----------------------------------------------------------------
 
-enb_status enblend_device(enb_ctx* ctx, const enb_image* white, const enb_image* white_alpha, const enb_image* black,
-                          const enb_image* black_alpha, const enb_image* mask, const enb_image* out,
-                          const enb_image* out_alpha, const enb_fuse_options& o, int32_t* level0)
+// enblend with the reference's pass structure: every level of the mask,
+// white and black pyramids materialised, one kernel per reference operation.
+enb_status enblend_plain(enb_ctx* ctx, const enb_image* white, const enb_image* white_alpha, const enb_image* black,
+                         const enb_image* black_alpha, const enb_image* mask, const enb_image* out,
+                         const enb_image* out_alpha, const enb_fuse_options& o, int32_t* level0)
 {
     const int w = black->width, h = black->height, C = black->channels, dt = black->dtype;
     const int L = enb_num_levels(w, h, 1, o.levels);
@@ -662,6 +664,104 @@ enb_status enblend_device(enb_ctx* ctx, const enb_image* white, const enb_image*
     }
     ENB_LAUNCH(ctx, launch_from_fixed(level_view(bl.p, 0), ua, out->data, ov.pitch, out->dtype, ov.stride, kImageFrac,
                                       o.dither, o.seed, ctx->stream));
+    if (ov.stride == 4) {
+        ENB_LAUNCH(ctx, launch_alpha_component(ua, out->data, ov.pitch, out->dtype, ctx->stream));
+    }
+    return ENB_OK;
+}
+
+// enblend with fused level passes (enb_fused.cu): level 0 is only read (the
+// first reduce converts on the fly, the last pass writes the output pixels);
+// levels 1..L-1 of the white, black and mask Gaussian pyramids are built by
+// the reduce chain, then one pass per level forms the Laplacians, blends and
+// collapses into the result pyramid R.
+enb_status enblend_fused(enb_ctx* ctx, const enb_image* white, const enb_image* white_alpha, const enb_image* black,
+                         const enb_image* black_alpha, const enb_image* mask, const enb_image* out,
+                         const enb_image* out_alpha, const enb_fuse_options& o, int32_t* level0)
+{
+    const int w = black->width, h = black->height, C = black->channels, dt = black->dtype;
+    const int L = enb_num_levels(w, h, 1, o.levels);
+    const int pdt = fixed_bits_image(dt), mdt = fixed_bits_mask(dt), mf = mask_frac(dt);
+    const int wrap = o.wrap != 0;
+    const int32_t white_value = 255 << mf;
+
+    // Both images' alpha must come from the same kind of source; otherwise
+    // materialise both as planes.
+    AlphaSrc wa = alpha_source(white, white_alpha), ba = alpha_source(black, black_alpha);
+    DevBuf wa_buf, ba_buf;
+    if (wa.mode != ba.mode) {
+        BytePlane wp, bp;
+        ENB_TRY(alpha_plane(ctx, white, white_alpha, wa_buf, wp));
+        ENB_TRY(alpha_plane(ctx, black, black_alpha, ba_buf, bp));
+        wa = AlphaSrc{};
+        wa.mode = kAlphaPlane;
+        wa.plane = wp;
+        ba = AlphaSrc{};
+        ba.mode = kAlphaPlane;
+        ba.plane = bp;
+    }
+    if (out_alpha && out_alpha->data) {
+        ENB_CHECK(ctx, bytes_ok(out_alpha, w, h), "out_alpha: must be U8 of the image size");
+    }
+
+    PyrHolder gw(ctx), gb(ctx), mg(ctx), rr(ctx);
+    AlphaChain awc, abc;
+    const int NL = L - 1;  // stored levels 1..L-1 as local levels 0..NL-1
+    if (NL >= 1) {
+        const int w1 = (w + 1) >> 1, h1 = (h + 1) >> 1;
+        ENB_TRY(pyramid_alloc(ctx, NL, w1, h1, C, pdt, &gw.p));
+        ENB_TRY(pyramid_alloc(ctx, NL, w1, h1, C, pdt, &gb.p));
+        ENB_TRY(pyramid_alloc(ctx, NL, w1, h1, C, pdt, &rr.p));
+        ENB_TRY(pyramid_alloc(ctx, NL, w1, h1, 1, mdt, &mg.p));
+        ENB_CUDA(ctx, awc.alloc(NL, w1, h1, ctx->stream));
+        ENB_CUDA(ctx, abc.alloc(NL, w1, h1, ctx->stream));
+        // Down sweep (src/enblend.h:384-446: the three Gaussian pyramids).
+        ENB_LAUNCH(ctx, launch_reduce0_alpha(pixel_view(white), wa, kImageFrac, level_view(gw.p, 0), awc.level(0),
+                                             wrap, ctx->stream));
+        ENB_LAUNCH(ctx, launch_reduce0_alpha(pixel_view(black), ba, kImageFrac, level_view(gb.p, 0), abc.level(0),
+                                             wrap, ctx->stream));
+        ENB_LAUNCH(ctx, launch_reduce0_bytes(byte_plane(mask), mf, level_view(mg.p, 0), wrap, ctx->stream));
+        for (int j = 1; j < NL; ++j) {
+            ENB_CHECK(ctx, gw.p->w[j - 1] > 1 && gw.p->h[j - 1] > 1, "reduce: src image too small in reduce");
+            const BytePlane sa = awc.level(j - 1), da = awc.level(j), sb = abc.level(j - 1), db = abc.level(j);
+            ENB_LAUNCH(ctx, launch_reduce(wrap, level_view(gw.p, j - 1), &sa, level_view(gw.p, j), &da, ctx->stream));
+            ENB_LAUNCH(ctx, launch_reduce(wrap, level_view(gb.p, j - 1), &sb, level_view(gb.p, j), &db, ctx->stream));
+            ENB_LAUNCH(ctx, launch_reduce(wrap, level_view(mg.p, j - 1), nullptr, level_view(mg.p, j), nullptr,
+                                          ctx->stream));
+        }
+        // Up sweep: top level blend, then Laplacian + blend + collapse per level
+        // (src/blend.h:81-121, src/pyramid.h:1758-1784).
+        ENB_LAUNCH(ctx, launch_blend_into(level_view(mg.p, NL - 1), level_view(gw.p, NL - 1), level_view(gb.p, NL - 1),
+                                          level_view(rr.p, NL - 1), white_value, ctx->stream));
+        for (int j = NL - 2; j >= 0; --j) {
+            ENB_LAUNCH(ctx, launch_up_level(level_view(gw.p, j + 1), level_view(gb.p, j + 1), level_view(rr.p, j + 1),
+                                            level_view(mg.p, j), level_view(gw.p, j), level_view(gb.p, j),
+                                            level_view(rr.p, j), white_value, wrap, ctx->stream));
+        }
+    }
+    // Level 0 straight to the output pixels (src/enblend.h:468-510).
+    Out0Host h0{};
+    h0.white = pixel_view(white);
+    h0.black = pixel_view(black);
+    h0.white_alpha = wa;
+    h0.black_alpha = ba;
+    h0.mask = byte_plane(mask);
+    h0.mfrac = mf;
+    h0.white_value = white_value;
+    h0.out = out->data;
+    h0.opitch = pixel_view(out).pitch;
+    h0.out_alpha = (out_alpha && out_alpha->data) ? byte_plane(out_alpha) : BytePlane{nullptr, 0, w, h};
+    h0.level0 = level0;
+    h0.frac = kImageFrac;
+    h0.dither = o.dither;
+    h0.wrap = wrap;
+    h0.seed = o.seed;
+    if (NL >= 1) {
+        const PlanarView g0 = level_view(gw.p, 0), b0 = level_view(gb.p, 0), r0 = level_view(rr.p, 0);
+        ENB_LAUNCH(ctx, launch_out0(&g0, &b0, &r0, h0, ctx->stream));
+    } else {
+        ENB_LAUNCH(ctx, launch_out0(nullptr, nullptr, nullptr, h0, ctx->stream));
+    }
     return ENB_OK;
 }
 
@@ -748,6 +848,9 @@ enb_status enfuse_device(enb_ctx* ctx, const enb_enfuse_params* prm, int K, cons
     ENB_CUDA(ctx, cudaMemset2DAsync(out->data, out->pitch, 0, (size_t)w * ov.stride * dtype_size(dt), h, ctx->stream));
     ENB_LAUNCH(ctx, launch_from_fixed(level_view(result.p, 0), ua, out->data, ov.pitch, out->dtype, ov.stride,
                                       kImageFrac, o.dither, o.seed, ctx->stream));
+    if (ov.stride == 4) {
+        ENB_LAUNCH(ctx, launch_alpha_component(ua, out->data, ov.pitch, out->dtype, ctx->stream));
+    }
     return ENB_OK;
 }
 
@@ -1342,11 +1445,17 @@ enb_status enb_enblend(enb_ctx* ctx, const enb_image* white, const enb_image* wh
     ENB_CHECK(ctx, black->width > 1 && black->height > 1, "enblend: image too small");
     ENB_CHECK(ctx, o.dither == ENB_DITHER_HASH || o.dither == ENB_DITHER_NEAREST, "enblend: unknown dither mode");
     const int w = black->width, h = black->height, C = black->channels;
+    auto run = [&](const enb_image* wi, const enb_image* wai, const enb_image* bi, const enb_image* bai,
+                   const enb_image* mi, const enb_image* oi, const enb_image* oai, int32_t* l0) {
+        return o.plain ? enblend_plain(ctx, wi, wai, bi, bai, mi, oi, oai, o, l0)
+                       : enblend_fused(ctx, wi, wai, bi, bai, mi, oi, oai, o, l0);
+    };
     if (!o.host_buffers) {
-        return enblend_device(ctx, white, white_alpha, black, black_alpha, mask, out, out_alpha, o,
-                              (int32_t*)o.level0_out);
+        return run(white, white_alpha, black, black_alpha, mask, out, out_alpha, (int32_t*)o.level0_out);
     }
-    Staged sw, sb, swa, sba, sm, so, soa;
+    // Host buffers: the result is formed in place in the device copy of the
+    // black image and copied back from there.
+    Staged sw, sb, swa, sba, sm, soa;
     ENB_TRY(stage_in(ctx, white, sw, true));
     ENB_TRY(stage_in(ctx, black, sb, true));
     ENB_TRY(stage_in(ctx, mask, sm, true));
@@ -1357,7 +1466,6 @@ enb_status enb_enblend(enb_ctx* ctx, const enb_image* white, const enb_image* wh
     if (has_ba) {
         ENB_TRY(stage_in(ctx, black_alpha, sba, true));
     }
-    ENB_TRY(stage_in(ctx, out, so, false));
     const bool want_alpha = out_alpha && out_alpha->data;
     if (want_alpha) {
         ENB_TRY(stage_in(ctx, out_alpha, soa, false));
@@ -1366,9 +1474,9 @@ enb_status enb_enblend(enb_ctx* ctx, const enb_image* white, const enb_image* wh
     if (o.level0_out) {
         ENB_CUDA(ctx, l0.alloc((size_t)w * h * C * 4, ctx->stream));
     }
-    ENB_TRY(enblend_device(ctx, &sw.dev, has_wa ? &swa.dev : nullptr, &sb.dev, has_ba ? &sba.dev : nullptr, &sm.dev,
-                           &so.dev, want_alpha ? &soa.dev : nullptr, o, (int32_t*)l0.p));
-    ENB_TRY(stage_out(ctx, out, so));
+    ENB_TRY(run(&sw.dev, has_wa ? &swa.dev : nullptr, &sb.dev, has_ba ? &sba.dev : nullptr, &sm.dev, &sb.dev,
+                want_alpha ? &soa.dev : nullptr, (int32_t*)l0.p));
+    ENB_TRY(stage_out(ctx, out, sb));
     if (want_alpha) {
         ENB_TRY(stage_out(ctx, out_alpha, soa));
     }

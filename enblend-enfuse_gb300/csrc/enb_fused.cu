@@ -1,0 +1,836 @@
+// enb_fused.cu -- fused level kernels of the enblend pyramid blend.
+//
+// The reference builds the white and black Laplacian pyramids and the mask
+// Gaussian pyramid in full, blends level by level and collapses
+// (src/enblend.h:384-510): every level crosses memory several times.  Here
+//   * level 0 is never materialised: the first reduce reads the interleaved
+//     RGBA pixels and converts them to fixed point on the fly;
+//   * each coarser level l is one pass that forms both Laplacians
+//     G_l - E(G_{l+1}), blends them under the mask pyramid and adds the
+//     expansion of the collapsed level l+1 (the collapse recursion
+//     R_l = fromPromote(B_l + E(R_{l+1})), src/pyramid.h:1758-1784);
+//   * level 0 is one pass from the two images, the seam mask and the three
+//     level-1 pyramids straight to the dithered output pixels.
+// The integer results are the reference's: each step is the same operation on
+// the same integers, only the order of the passes over memory changes.
+//
+// Kernel structure: a CTA covers a 64x16 destination tile as 2x2 quads (one
+// per thread).  Each thread first issues its global loads (fine-level values
+// or image pixels), then the CTA stages the 34x10 coarse neighbourhoods of the
+// three level-(l+1) pyramids in shared memory.  Tiles inside the image take a
+// path without bounds or border weights, expand only the planes the quad's
+// seam mask selects, and use paired/vector loads and stores.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "enb_device.cuh"
+#include "enb_internal.h"
+#include "enb_reduce.cuh"
+
+namespace enb {
+
+// ---------------------------------------------------------------------------
+// Pixel I/O
+// ---------------------------------------------------------------------------
+
+// Interleaved pixel load/store; VEC packs the 4 samples of an RGBA pixel in
+// one 4- or 8-byte access (the caller checks the alignment).
+template <typename TIn, int S, bool VEC>
+__device__ __forceinline__ void ld_px(const TIn* p, TIn (&o)[S])
+{
+    if (VEC && S == 4 && sizeof(TIn) == 2) {
+        const uint2 v = *reinterpret_cast<const uint2*>(p);
+        o[0] = (TIn)(v.x & 0xffffu);
+        o[1] = (TIn)(v.x >> 16);
+        o[2] = (TIn)(v.y & 0xffffu);
+        o[S - 1] = (TIn)(v.y >> 16);
+    } else if (VEC && S == 4 && sizeof(TIn) == 1) {
+        const uint32_t v = *reinterpret_cast<const uint32_t*>(p);
+        o[0] = (TIn)(v & 0xffu);
+        o[1] = (TIn)((v >> 8) & 0xffu);
+        o[2] = (TIn)((v >> 16) & 0xffu);
+        o[S - 1] = (TIn)(v >> 24);
+    } else {
+#pragma unroll
+        for (int c = 0; c < S; ++c) {
+            o[c] = p[c];
+        }
+    }
+}
+
+template <typename TIn, int S, bool VEC>
+__device__ __forceinline__ void st_px(TIn* p, const TIn (&o)[S])
+{
+    if (VEC && S == 4 && sizeof(TIn) == 2) {
+        uint2 v;
+        v.x = (uint32_t)o[0] | ((uint32_t)o[1] << 16);
+        v.y = (uint32_t)o[2] | ((uint32_t)o[S - 1] << 16);
+        *reinterpret_cast<uint2*>(p) = v;
+    } else if (VEC && S == 4 && sizeof(TIn) == 1) {
+        *reinterpret_cast<uint32_t*>(p) =
+            (uint32_t)o[0] | ((uint32_t)o[1] << 8) | ((uint32_t)o[2] << 16) | ((uint32_t)o[S - 1] << 24);
+    } else {
+#pragma unroll
+        for (int c = 0; c < S; ++c) {
+            p[c] = o[c];
+        }
+    }
+}
+
+// Alpha of an interleaved pixel: 8-bit plane (AM 0), opaque (AM 1) or the
+// thresholded 4th component (AM 2, src/assemble.h:240-253).
+template <int AM, typename TIn, int S>
+__device__ __forceinline__ int pixel_alpha(const TIn (&px)[S], const uint8_t* ap, int64_t apitch, int x, int y,
+                                           uint32_t alo, uint32_t ahi)
+{
+    if (AM == 0) {
+        return ap[(int64_t)y * apitch + x] != 0;
+    }
+    if (AM == 1) {
+        return 1;
+    }
+    const uint32_t v = px[S - 1];
+    return v >= alo && v <= ahi;
+}
+
+// Source of the tiled reduce: interleaved pixels converted to fixed point
+// on the fly (copyToPyramidImage, src/fixmath.h:197-202).
+template <typename TIn, int C, int S, int AM, bool VEC>
+struct PixelSourceV {
+    const TIn* p;
+    int64_t pitch;
+    const uint8_t* a;
+    int64_t apitch;
+    uint32_t lo, hi;
+    int frac;
+    __device__ __forceinline__ void load(int gy, int gx, int32_t (&v)[C], int& al) const
+    {
+        TIn px[S];
+        ld_px<TIn, S, VEC>(p + (int64_t)gy * pitch + (int64_t)gx * S, px);
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            v[c] = (int32_t)px[c] << frac;
+        }
+        al = pixel_alpha<AM, TIn, S>(px, a, apitch, gx, gy, lo, hi);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Merge helpers
+// ---------------------------------------------------------------------------
+
+// CartesianBlendFunctor of one sample (src/blend.h:41-76): integer tests for
+// the coefficients 1 and 0, the reference's double expression otherwise.
+template <typename T>
+__device__ __forceinline__ int32_t blend1(int32_t m, int32_t white_value, int32_t lw, int32_t lb)
+{
+    if (m >= white_value) {
+        return lw;
+    }
+    if (m <= 0) {
+        return lb;
+    }
+    const double wc = __ddiv_rn((double)m, (double)white_value);
+    const double bc = __dadd_rn(1.0, -wc);
+    return (int32_t)frp_store<T>(__dadd_rn(__dmul_rn(wc, (double)lw), __dmul_rn(bc, (double)lb)));
+}
+
+// Top level: R = blend(M, Gw, Gb) (the top Laplacian level is the Gaussian).
+template <typename T, typename TM, int C>
+__global__ void __launch_bounds__(256) k_blend_into(const TM* __restrict__ mask, int64_t mpitch,
+                                                    const T* __restrict__ gw, const T* __restrict__ gb,
+                                                    T* __restrict__ r, int64_t pitch, int64_t plane, int w, int h,
+                                                    int32_t white_value)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x >= w) {
+        return;
+    }
+    const int64_t o = (int64_t)y * pitch + x;
+    const int32_t m = (int32_t)mask[(int64_t)y * mpitch + x];
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        r[c * plane + o] = (T)blend1<T>(m, white_value, gw[c * plane + o], gb[c * plane + o]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Tiled expansion of coarse planes
+// ---------------------------------------------------------------------------
+
+struct CoarseLevels {
+    // plane pointers of Gw_{l+1}, Gb_{l+1}, R_{l+1}, channel-major: [which*C + c]
+    const void* p[9];
+    int64_t pitch;  // elements
+    int w, h;
+};
+
+// Stage the 34x10 coarse neighbourhoods of a 64x16 destination tile for NP
+// planes; loads unrolled and independent of each other.
+template <int NP, typename T>
+__device__ __forceinline__ void stage_coarse(int32_t (*ss)[ESH][ESW], const CoarseLevels& cl, int I0, int J0,
+                                             int wrap)
+{
+    constexpr int N = ESH * ESW;
+    constexpr int IT = (N + 255) / 256;
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+        const int k = threadIdx.x + it * 256;
+        if (k < N) {
+            const int r = k / ESW, c = k - r * ESW;
+            const int j = J0 - 1 + r;
+            int i = I0 - 1 + c;
+            if (wrap) {
+                i = imod(i, cl.w);
+            }
+            const bool in = j >= 0 && j < cl.h && i >= 0 && i < cl.w;
+            const int64_t o = (int64_t)j * cl.pitch + i;
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                ss[p][r][c] = in ? (int32_t) reinterpret_cast<const T*>(cl.p[p])[o] : 0;
+            }
+        }
+    }
+}
+
+// Staging when the whole 34x10 neighbourhood lies inside the coarse level.
+template <int NP, typename T>
+__device__ __forceinline__ void stage_coarse_interior(int32_t (*ss)[ESH][ESW], const CoarseLevels& cl, int I0, int J0)
+{
+    constexpr int N = ESH * ESW;
+    constexpr int IT = (N + 255) / 256;
+    const T* base[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        base[p] = reinterpret_cast<const T*>(cl.p[p]) + (int64_t)(J0 - 1) * cl.pitch + (I0 - 1);
+    }
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+        const int k = threadIdx.x + it * 256;
+        if (k < N) {
+            const int r = k / ESW, c = k - r * ESW;
+            const int o = r * (int)cl.pitch + c;
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                ss[p][r][c] = (int32_t)base[p][o];
+            }
+        }
+    }
+}
+
+// Expansion of the four destination pixels of the quad at tile position
+// (qx, qy) from one staged coarse plane (the 3x3 source neighbourhood), with
+// the border weights and divisors of expand_hweights / expand_vweights.
+__device__ __forceinline__ void expand_quad(const int32_t (*s)[ESW], int qx, int qy, int X, int Y, int sw, int sh,
+                                            int dw, int dh, int wrap, int32_t e[4])
+{
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int XX = X + (q & 1), YY = Y + (q >> 1);
+        e[q] = 0;
+        if (XX >= dw || YY >= dh) {
+            continue;
+        }
+        int vw[3], vden, hw[3], hden;
+        expand_vweights(YY, sh, vw, vden);
+        expand_hweights(XX, sw, dw, wrap, hw, hden);
+        int32_t num = 0;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const int32_t* row = &s[qy + a][qx];
+            num += vw[a] * (hw[0] * row[0] + hw[1] * row[1] + hw[2] * row[2]);
+        }
+        e[q] = div_den(num, hden * vden);
+    }
+}
+
+// Expansion of an interior quad (all taps inside the level).  The (4,4) taps
+// enter without their common factor 4, which is folded into the divisors:
+// trunc(4n/64) = trunc(n/16) and trunc(4n/16) = trunc(n/4).  NONNEG: the
+// source is a Gaussian level of an unsigned image (all values >= 0), so the
+// truncating divisions are shifts.
+template <bool NONNEG>
+__device__ __forceinline__ void expand_quad_interior(const int32_t (*s)[ESW], int qx, int qy, int32_t e[4])
+{
+    const int32_t* a = &s[qy][qx];
+    const int32_t* b = &s[qy + 1][qx];
+    const int32_t* c = &s[qy + 2][qx];
+    const int32_t hea = a[0] + 6 * a[1] + a[2], heb = b[0] + 6 * b[1] + b[2], hec = c[0] + 6 * c[1] + c[2];
+    const int32_t hoa = a[1] + a[2], hob = b[1] + b[2], hoc = c[1] + c[2];
+    const int32_t n0 = hea + 6 * heb + hec, n1 = hoa + 6 * hob + hoc, n2 = heb + hec, n3 = hob + hoc;
+    if (NONNEG) {
+        e[0] = (int32_t)((uint32_t)n0 >> 6);
+        e[1] = (int32_t)((uint32_t)n1 >> 4);
+        e[2] = (int32_t)((uint32_t)n2 >> 4);
+        e[3] = (int32_t)((uint32_t)n3 >> 2);
+    } else {
+        e[0] = n0 / 64;
+        e[1] = n1 / 16;
+        e[2] = n2 / 16;
+        e[3] = n3 / 4;
+    }
+}
+
+// Two horizontally adjacent samples of a planar level (even x: 4- or 8-byte aligned).
+template <typename T>
+__device__ __forceinline__ void ld2(const T* p, int32_t& a, int32_t& b)
+{
+    if (sizeof(T) == 4) {
+        const int2 v = *reinterpret_cast<const int2*>(p);
+        a = v.x;
+        b = v.y;
+    } else {
+        const int v = *reinterpret_cast<const int*>(p);
+        a = (int32_t)(int16_t)(v & 0xffff);
+        b = v >> 16;
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void st2(T* p, T a, T b)
+{
+    if (sizeof(T) == 4) {
+        *reinterpret_cast<int2*>(p) = make_int2((int32_t)a, (int32_t)b);
+    } else {
+        *reinterpret_cast<int*>(p) = (int)(((uint32_t)(uint16_t)a) | ((uint32_t)(uint16_t)b << 16));
+    }
+}
+
+// CTA-uniform test: the 64x16 destination tile lies inside the level and
+// every quad's 3x3 coarse neighbourhood lies inside the coarse level.
+__device__ __forceinline__ bool interior_tile(int X0, int Y0, int w, int h, int I0, int J0, int cw, int ch)
+{
+    return X0 + ETW <= w && Y0 + ETH <= h && I0 >= 1 && I0 + ETW / 2 < cw && J0 >= 1 && J0 + ETH / 2 < ch;
+}
+
+// ---------------------------------------------------------------------------
+// Coarse level l (1 <= l <= L-2): Laplacians, blend, collapse in one pass
+// ---------------------------------------------------------------------------
+
+template <typename T, typename TM, int C>
+__global__ void __launch_bounds__(256) k_up_level(CoarseLevels cl, const TM* __restrict__ mask, int64_t mpitch,
+                                                  const T* __restrict__ gw, const T* __restrict__ gb,
+                                                  T* __restrict__ r, int64_t pitch, int64_t plane, int w, int h,
+                                                  int32_t white_value, int wrap)
+{
+    __shared__ int32_t ss[3 * C][ESH][ESW];
+    const int X0 = blockIdx.x * ETW, Y0 = blockIdx.y * ETH;
+    const int I0 = X0 >> 1, J0 = Y0 >> 1;
+    const int qx = threadIdx.x % 32, qy = threadIdx.x / 32;
+    const int i = I0 + qx, j = J0 + qy;
+    const int X = 2 * i, Y = 2 * j;
+
+    if (interior_tile(X0, Y0, w, h, I0, J0, cl.w, cl.h)) {
+        // interior tile: no bounds, paired loads and stores, interior
+        // expansions, only the expansions the quad's mask values select
+        const int64_t o0 = (int64_t)Y * pitch + X;
+        int32_t fw[C][4], fb[C][4], fm[4];
+        ld2<TM>(mask + (int64_t)Y * mpitch + X, fm[0], fm[1]);
+        ld2<TM>(mask + (int64_t)(Y + 1) * mpitch + X, fm[2], fm[3]);
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            ld2<T>(gw + c * plane + o0, fw[c][0], fw[c][1]);
+            ld2<T>(gw + c * plane + o0 + pitch, fw[c][2], fw[c][3]);
+            ld2<T>(gb + c * plane + o0, fb[c][0], fb[c][1]);
+            ld2<T>(gb + c * plane + o0 + pitch, fb[c][2], fb[c][3]);
+        }
+        stage_coarse_interior<3 * C, T>(ss, cl, I0, J0);
+        __syncthreads();
+        const bool need_w = fm[0] > 0 || fm[1] > 0 || fm[2] > 0 || fm[3] > 0;
+        const bool need_b = fm[0] < white_value || fm[1] < white_value || fm[2] < white_value || fm[3] < white_value;
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            int32_t ew[4] = {0, 0, 0, 0}, eb[4] = {0, 0, 0, 0}, er[4];
+            if (need_w) {
+                expand_quad_interior<true>(ss[c], qx, qy, ew);
+            }
+            if (need_b) {
+                expand_quad_interior<true>(ss[C + c], qx, qy, eb);
+            }
+            expand_quad_interior<false>(ss[2 * C + c], qx, qy, er);
+            T res[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int32_t lw = (int32_t)cast_store<T>((int64_t)fw[c][q] - ew[q]);
+                const int32_t lb = (int32_t)cast_store<T>((int64_t)fb[c][q] - eb[q]);
+                res[q] = sat_store<T>(blend1<T>(fm[q], white_value, lw, lb) + er[q]);
+            }
+            st2<T>(r + c * plane + o0, res[0], res[1]);
+            st2<T>(r + c * plane + o0 + pitch, res[2], res[3]);
+        }
+        return;
+    }
+
+    // border tile: fine-level values of the quad, loaded before the barrier
+    int32_t fw[C][4], fb[C][4], fm[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int XX = X + (q & 1), YY = Y + (q >> 1);
+        const bool v = XX < w && YY < h;
+        const int64_t o = (int64_t)YY * pitch + XX;
+        fm[q] = v ? (int32_t)mask[(int64_t)YY * mpitch + XX] : 0;
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            fw[c][q] = v ? (int32_t)gw[c * plane + o] : 0;
+            fb[c][q] = v ? (int32_t)gb[c * plane + o] : 0;
+        }
+    }
+    stage_coarse<3 * C, T>(ss, cl, I0, J0, wrap);
+    __syncthreads();
+    if (X >= w || Y >= h) {
+        return;
+    }
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        int32_t ew[4], eb[4], er[4];
+        expand_quad(ss[c], qx, qy, X, Y, cl.w, cl.h, w, h, wrap, ew);
+        expand_quad(ss[C + c], qx, qy, X, Y, cl.w, cl.h, w, h, wrap, eb);
+        expand_quad(ss[2 * C + c], qx, qy, X, Y, cl.w, cl.h, w, h, wrap, er);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int XX = X + (q & 1), YY = Y + (q >> 1);
+            if (XX >= w || YY >= h) {
+                continue;
+            }
+            const int32_t lw = (int32_t)cast_store<T>((int64_t)fw[c][q] - ew[q]);
+            const int32_t lb = (int32_t)cast_store<T>((int64_t)fb[c][q] - eb[q]);
+            const int32_t bl = blend1<T>(fm[q], white_value, lw, lb);
+            r[c * plane + (int64_t)YY * pitch + XX] = sat_store<T>(bl + er[q]);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Level 0: images, seam mask and level-1 pyramids -> dithered output pixels
+// ---------------------------------------------------------------------------
+
+struct Out0Args {
+    const void* white;
+    const void* black;
+    int64_t wpitch, bpitch;      // elements
+    const uint8_t* wa;           // alpha planes (AM 0) or null
+    const uint8_t* ba;
+    int64_t wapitch, bapitch;
+    uint32_t alo, ahi;           // channel-3 threshold (AM 2)
+    const uint8_t* mask;
+    int64_t mpitch;
+    int mfrac;
+    int32_t white_value;
+    void* out;
+    int64_t opitch;              // elements
+    uint8_t* out_alpha;          // union alpha plane or null
+    int64_t oapitch;
+    int32_t* level0;             // collapsed level 0 (interleaved int32) or null
+    int w, h, frac, dither, has_coarse, wrap;
+    uint64_t seed;
+    uint32_t key;                // dither_key(seed)
+    int32_t maxv;
+};
+
+template <typename TIn, typename T, int C, int S, int AM, bool VEC>
+__global__ void __launch_bounds__(256) k_out0(CoarseLevels cl, Out0Args a)
+{
+    __shared__ int32_t ss[3 * C][ESH][ESW];
+    const int X0 = blockIdx.x * ETW, Y0 = blockIdx.y * ETH;
+    const int I0 = X0 >> 1, J0 = Y0 >> 1;
+    const int qx = threadIdx.x % 32, qy = threadIdx.x / 32;
+    const int i = I0 + qx, j = J0 + qy;
+    const int X = 2 * i, Y = 2 * j;
+    const bool nearest = a.dither == ENB_DITHER_NEAREST;
+
+    if (a.has_coarse && interior_tile(X0, Y0, a.w, a.h, I0, J0, cl.w, cl.h)) {
+        // interior tile: no bounds, interior expansions, only the expansions
+        // the seam mask of the quad selects
+        TIn wp[4][S], bp[4][S];
+        const TIn* w0 = reinterpret_cast<const TIn*>(a.white) + (int64_t)Y * a.wpitch + (int64_t)X * S;
+        const TIn* b0 = reinterpret_cast<const TIn*>(a.black) + (int64_t)Y * a.bpitch + (int64_t)X * S;
+        ld_px<TIn, S, VEC>(w0, wp[0]);
+        ld_px<TIn, S, VEC>(w0 + S, wp[1]);
+        ld_px<TIn, S, VEC>(w0 + a.wpitch, wp[2]);
+        ld_px<TIn, S, VEC>(w0 + a.wpitch + S, wp[3]);
+        ld_px<TIn, S, VEC>(b0, bp[0]);
+        ld_px<TIn, S, VEC>(b0 + S, bp[1]);
+        ld_px<TIn, S, VEC>(b0 + a.bpitch, bp[2]);
+        ld_px<TIn, S, VEC>(b0 + a.bpitch + S, bp[3]);
+        const uint8_t* m0 = a.mask + (int64_t)Y * a.mpitch + X;
+        const int32_t mk[4] = {(int32_t)m0[0] << a.mfrac, (int32_t)m0[1] << a.mfrac, (int32_t)m0[a.mpitch] << a.mfrac,
+                               (int32_t)m0[a.mpitch + 1] << a.mfrac};
+        stage_coarse_interior<3 * C, T>(ss, cl, I0, J0);
+        __syncthreads();
+        bool uni[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int XX = X + (q & 1), YY = Y + (q >> 1);
+            uni[q] = pixel_alpha<AM, TIn, S>(wp[q], a.wa, a.wapitch, XX, YY, a.alo, a.ahi) ||
+                     pixel_alpha<AM, TIn, S>(bp[q], a.ba, a.bapitch, XX, YY, a.alo, a.ahi);
+        }
+        const bool need_w = mk[0] > 0 || mk[1] > 0 || mk[2] > 0 || mk[3] > 0;
+        const bool need_b = mk[0] < a.white_value || mk[1] < a.white_value || mk[2] < a.white_value ||
+                            mk[3] < a.white_value;
+        const uint32_t pix0 = (uint32_t)Y * (uint32_t)a.w + (uint32_t)X;
+        const uint32_t pixq[4] = {pix0, pix0 + 1, pix0 + (uint32_t)a.w, pix0 + (uint32_t)a.w + 1};
+        uint32_t pb[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            pb[q] = mix32(pixq[q] ^ a.key);
+        }
+        TIn o[4][S];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+#pragma unroll
+            for (int c = 0; c < S; ++c) {
+                o[q][c] = bp[q][c];
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            int32_t ew[4] = {0, 0, 0, 0}, eb[4] = {0, 0, 0, 0}, er[4];
+            if (need_w) {
+                expand_quad_interior<true>(ss[c], qx, qy, ew);
+            }
+            if (need_b) {
+                expand_quad_interior<true>(ss[C + c], qx, qy, eb);
+            }
+            expand_quad_interior<false>(ss[2 * C + c], qx, qy, er);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int32_t lw = (int32_t)cast_store<T>((int64_t)((int32_t)wp[q][c] << a.frac) - ew[q]);
+                const int32_t lb = (int32_t)cast_store<T>((int64_t)((int32_t)bp[q][c] << a.frac) - eb[q]);
+                const int32_t res = (int32_t)sat_store<T>(blend1<T>(mk[q], a.white_value, lw, lb) + er[q]);
+                if (a.level0) {
+                    a.level0[(uint64_t)pixq[q] * C + c] = res;
+                }
+                if (uni[q]) {
+                    const uint32_t bits = dither_sample_bits(a.key, pb[q], pixq[q], C, c, a.frac);
+                    o[q][c] = (TIn)dither_rule(res, a.frac, nearest, bits, a.maxv);
+                }
+            }
+        }
+        TIn* out0 = reinterpret_cast<TIn*>(a.out) + (int64_t)Y * a.opitch + (int64_t)X * S;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (S == 4) {
+                o[q][S - 1] = uni[q] ? (TIn)a.maxv : (TIn)0;
+            }
+            st_px<TIn, S, VEC>(out0 + (q >> 1) * a.opitch + (q & 1) * S, o[q]);
+        }
+        if (a.out_alpha) {
+            uint8_t* oa = a.out_alpha + (int64_t)Y * a.oapitch + X;
+            oa[0] = uni[0] ? 255 : 0;
+            oa[1] = uni[1] ? 255 : 0;
+            oa[a.oapitch] = uni[2] ? 255 : 0;
+            oa[a.oapitch + 1] = uni[3] ? 255 : 0;
+        }
+        return;
+    }
+
+    // border tile (or a single level): the quad's pixels, loaded before the barrier
+    TIn wp[4][S], bp[4][S];
+    int32_t mk[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int XX = X + (q & 1), YY = Y + (q >> 1);
+        if (XX < a.w && YY < a.h) {
+            ld_px<TIn, S, VEC>(reinterpret_cast<const TIn*>(a.white) + (int64_t)YY * a.wpitch + (int64_t)XX * S, wp[q]);
+            ld_px<TIn, S, VEC>(reinterpret_cast<const TIn*>(a.black) + (int64_t)YY * a.bpitch + (int64_t)XX * S, bp[q]);
+            mk[q] = (int32_t)a.mask[(int64_t)YY * a.mpitch + XX] << a.mfrac;
+        } else {
+#pragma unroll
+            for (int c = 0; c < S; ++c) {
+                wp[q][c] = bp[q][c] = 0;
+            }
+            mk[q] = 0;
+        }
+    }
+    if (a.has_coarse) {
+        stage_coarse<3 * C, T>(ss, cl, I0, J0, a.wrap);
+        __syncthreads();
+    }
+    if (X >= a.w || Y >= a.h) {
+        return;
+    }
+    bool uni[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int XX = X + (q & 1), YY = Y + (q >> 1);
+        uni[q] = pixel_alpha<AM, TIn, S>(wp[q], a.wa, a.wapitch, XX, YY, a.alo, a.ahi) ||
+                 pixel_alpha<AM, TIn, S>(bp[q], a.ba, a.bapitch, XX, YY, a.alo, a.ahi);
+    }
+    TIn o[4][S];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+#pragma unroll
+        for (int c = 0; c < S; ++c) {
+            o[q][c] = bp[q][c];
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        int32_t ew[4] = {0, 0, 0, 0}, eb[4] = {0, 0, 0, 0}, er[4] = {0, 0, 0, 0};
+        if (a.has_coarse) {
+            expand_quad(ss[c], qx, qy, X, Y, cl.w, cl.h, a.w, a.h, a.wrap, ew);
+            expand_quad(ss[C + c], qx, qy, X, Y, cl.w, cl.h, a.w, a.h, a.wrap, eb);
+            expand_quad(ss[2 * C + c], qx, qy, X, Y, cl.w, cl.h, a.w, a.h, a.wrap, er);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int XX = X + (q & 1), YY = Y + (q >> 1);
+            if (XX >= a.w || YY >= a.h) {
+                continue;
+            }
+            const int32_t lw = (int32_t)cast_store<T>((int64_t)((int32_t)wp[q][c] << a.frac) - ew[q]);
+            const int32_t lb = (int32_t)cast_store<T>((int64_t)((int32_t)bp[q][c] << a.frac) - eb[q]);
+            const int32_t res = (int32_t)sat_store<T>(blend1<T>(mk[q], a.white_value, lw, lb) + er[q]);
+            const uint64_t pix = (uint64_t)YY * (uint64_t)a.w + (uint64_t)XX;
+            if (a.level0) {
+                a.level0[pix * C + c] = res;
+            }
+            if (uni[q]) {
+                const uint32_t bits = dither_sample_bits(a.key, mix32((uint32_t)pix ^ a.key), pix, C, c, a.frac);
+                o[q][c] = (TIn)dither_rule(res, a.frac, nearest, bits, a.maxv);
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int XX = X + (q & 1), YY = Y + (q >> 1);
+        if (XX >= a.w || YY >= a.h) {
+            continue;
+        }
+        if (S == 4) {
+            o[q][S - 1] = uni[q] ? (TIn)a.maxv : (TIn)0;
+        }
+        st_px<TIn, S, VEC>(reinterpret_cast<TIn*>(a.out) + (int64_t)YY * a.opitch + (int64_t)XX * S, o[q]);
+        if (a.out_alpha) {
+            a.out_alpha[(int64_t)YY * a.oapitch + XX] = uni[q] ? 255 : 0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+
+static inline double esz_f(int dt) { return dt == ENB_U8 ? 1.0 : ((dt == ENB_U16 || dt == ENB_I16) ? 2.0 : 4.0); }
+static inline double npix_f(int w, int h) { return (double)w * (double)h; }
+static inline double pbytes(const PlanarView& v) { return npix_f(v.w, v.h) * v.C * esz_f(v.dtype); }
+
+struct Reduce0Launch {
+    const PixelView& s;
+    const uint8_t* ap;
+    int64_t apitch;
+    uint32_t lo, hi;
+    int frac;
+    const PlanarView& d;
+    const BytePlane& da;
+    int wrap;
+    cudaStream_t st;
+    template <typename TIn, typename T, int C, int S, int AM, bool VEC>
+    void operator()() const
+    {
+        PixelSourceV<TIn, C, S, AM, VEC> src{(const TIn*)s.p, s.pitch, ap, apitch, lo, hi, frac};
+        launch_reduce_tiles<PixelSourceV<TIn, C, S, AM, VEC>, T, C, true>(src, s.w, s.h, (T*)d.p, d.pitch, d.plane, d.w,
+                                                                         d.h, da.p, da.pitch, wrap, st);
+    }
+};
+
+struct Out0Launch {
+    const CoarseLevels& cl;
+    const Out0Args& a;
+    dim3 g;
+    cudaStream_t st;
+    template <typename TIn, typename T, int C, int S, int AM, bool VEC>
+    void operator()() const
+    {
+        k_out0<TIn, T, C, S, AM, VEC><<<g, 256, 0, st>>>(cl, a);
+    }
+};
+
+// Calls f.operator()<TIn, T, C, S, AM, VEC>() for the runtime combination
+// (the pyramid type follows the sample type: U8 -> Int16, U16 -> Int32).
+template <typename F>
+static cudaError_t dispatch_pixels(int dtype, int C, int S, int AM, bool vec, F&& f)
+{
+#define ENB_PX_CASE(TIN, TP, CC, SS, AMM, VV)                      \
+    if (C == CC && S == SS && AM == AMM && vec == VV) {            \
+        f.template operator()<TIN, TP, CC, SS, AMM, VV>();         \
+        return cudaGetLastError();                                 \
+    }
+#define ENB_PX_TYPE(TIN, TP)                                       \
+    ENB_PX_CASE(TIN, TP, 1, 1, 0, false)                           \
+    ENB_PX_CASE(TIN, TP, 1, 1, 1, false)                           \
+    ENB_PX_CASE(TIN, TP, 3, 3, 0, false)                           \
+    ENB_PX_CASE(TIN, TP, 3, 3, 1, false)                           \
+    ENB_PX_CASE(TIN, TP, 3, 4, 0, false)                           \
+    ENB_PX_CASE(TIN, TP, 3, 4, 1, false)                           \
+    ENB_PX_CASE(TIN, TP, 3, 4, 2, false)                           \
+    ENB_PX_CASE(TIN, TP, 3, 4, 0, true)                            \
+    ENB_PX_CASE(TIN, TP, 3, 4, 1, true)                            \
+    ENB_PX_CASE(TIN, TP, 3, 4, 2, true)
+    if (dtype == ENB_U8) {
+        ENB_PX_TYPE(uint8_t, int16_t)
+    } else {
+        ENB_PX_TYPE(uint16_t, int32_t)
+    }
+#undef ENB_PX_TYPE
+#undef ENB_PX_CASE
+    return cudaErrorInvalidValue;
+}
+
+static bool vec_ok(const void* p, int64_t pitch_elems, int dtype, int S)
+{
+    const size_t bytes = (size_t)S * (dtype == ENB_U8 ? 1 : 2);
+    return S == 4 && ((uintptr_t)p % bytes) == 0 && ((size_t)pitch_elems * (dtype == ENB_U8 ? 1 : 2)) % bytes == 0;
+}
+
+static int alpha_mode_code(const AlphaSrc& a)
+{
+    return a.mode == kAlphaPlane ? 0 : (a.mode == kAlphaOpaque ? 1 : 2);
+}
+
+cudaError_t launch_reduce0_alpha(const PixelView& s, const AlphaSrc& a, int frac, const PlanarView& d,
+                                 const BytePlane& da, int wrap, cudaStream_t st)
+{
+    note_launch("reduce0_alpha", npix_f(s.w, s.h) * s.stride * esz_f(s.dtype) +
+                                     (a.mode == kAlphaPlane ? npix_f(s.w, s.h) : 0.0) + pbytes(d) + npix_f(d.w, d.h));
+    const uint8_t* ap = a.mode == kAlphaPlane ? a.plane.p : nullptr;
+    const int64_t apitch = a.mode == kAlphaPlane ? a.plane.pitch : 0;
+    Reduce0Launch l{s, ap, apitch, a.lo, a.hi, frac, d, da, wrap, st};
+    return dispatch_pixels(s.dtype, s.C, s.stride, alpha_mode_code(a), vec_ok(s.p, s.pitch, s.dtype, s.stride), l);
+}
+
+cudaError_t launch_reduce0_bytes(const BytePlane& s, int frac, const PlanarView& d, int wrap, cudaStream_t st)
+{
+    note_launch("reduce0_mask", npix_f(s.w, s.h) + pbytes(d));
+    ByteSource src{s.p, s.pitch, frac};
+    if (d.dtype == ENB_I16) {
+        launch_reduce_tiles<ByteSource, int16_t, 1, false>(src, s.w, s.h, (int16_t*)d.p, d.pitch, 0, d.w, d.h, nullptr,
+                                                           0, wrap, st);
+    } else {
+        launch_reduce_tiles<ByteSource, int32_t, 1, false>(src, s.w, s.h, (int32_t*)d.p, d.pitch, 0, d.w, d.h, nullptr,
+                                                           0, wrap, st);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_blend_into(const PlanarView& m, const PlanarView& gw, const PlanarView& gb, const PlanarView& r,
+                              int32_t wv, cudaStream_t st)
+{
+    note_launch("blend_top", pbytes(m) + pbytes(gw) + pbytes(gb) + pbytes(r));
+    const dim3 g((unsigned)((r.w + 255) / 256), (unsigned)r.h);
+    const bool m16 = m.dtype == ENB_I16;
+#define ENB_BI(T, TM, CC)                                                                                         \
+    k_blend_into<T, TM, CC><<<g, 256, 0, st>>>((const TM*)m.p, m.pitch, (const T*)gw.p, (const T*)gb.p, (T*)r.p, \
+                                               r.pitch, r.plane, r.w, r.h, wv)
+    if (r.dtype == ENB_I16) {
+        if (r.C == 1) {
+            if (m16) ENB_BI(int16_t, int16_t, 1); else ENB_BI(int16_t, int32_t, 1);
+        } else {
+            if (m16) ENB_BI(int16_t, int16_t, 3); else ENB_BI(int16_t, int32_t, 3);
+        }
+    } else {
+        if (r.C == 1) {
+            if (m16) ENB_BI(int32_t, int16_t, 1); else ENB_BI(int32_t, int32_t, 1);
+        } else {
+            if (m16) ENB_BI(int32_t, int16_t, 3); else ENB_BI(int32_t, int32_t, 3);
+        }
+    }
+#undef ENB_BI
+    return cudaGetLastError();
+}
+
+static CoarseLevels coarse_of(const PlanarView& gw, const PlanarView& gb, const PlanarView& r)
+{
+    CoarseLevels cl{};
+    const size_t es = gw.dtype == ENB_I16 ? 2 : 4;
+    for (int c = 0; c < gw.C; ++c) {
+        cl.p[c] = (const char*)gw.p + (size_t)c * gw.plane * es;
+        cl.p[gw.C + c] = (const char*)gb.p + (size_t)c * gb.plane * es;
+        cl.p[2 * gw.C + c] = (const char*)r.p + (size_t)c * r.plane * es;
+    }
+    cl.pitch = gw.pitch;
+    cl.w = gw.w;
+    cl.h = gw.h;
+    return cl;
+}
+
+cudaError_t launch_up_level(const PlanarView& gw1, const PlanarView& gb1, const PlanarView& r1, const PlanarView& m,
+                            const PlanarView& gw, const PlanarView& gb, const PlanarView& r, int32_t wv, int wrap,
+                            cudaStream_t st)
+{
+    if (gw1.pitch != gb1.pitch || gw1.pitch != r1.pitch || gw.pitch != gb.pitch || gw.pitch != r.pitch ||
+        gw.plane != gb.plane || gw.plane != r.plane) {
+        return cudaErrorInvalidValue;
+    }
+    note_launch("up_level", 3.0 * pbytes(gw1) + pbytes(m) + 3.0 * pbytes(gw));
+    const CoarseLevels cl = coarse_of(gw1, gb1, r1);
+    const dim3 g = grid2d(r.w, r.h, ETW, ETH);
+    const bool m16 = m.dtype == ENB_I16;
+#define ENB_UL(T, TM, CC)                                                                                       \
+    k_up_level<T, TM, CC><<<g, 256, 0, st>>>(cl, (const TM*)m.p, m.pitch, (const T*)gw.p, (const T*)gb.p, (T*)r.p, \
+                                             r.pitch, r.plane, r.w, r.h, wv, wrap)
+    if (r.dtype == ENB_I16) {
+        if (r.C == 1) {
+            if (m16) ENB_UL(int16_t, int16_t, 1); else ENB_UL(int16_t, int32_t, 1);
+        } else {
+            if (m16) ENB_UL(int16_t, int16_t, 3); else ENB_UL(int16_t, int32_t, 3);
+        }
+    } else {
+        if (r.C == 1) {
+            if (m16) ENB_UL(int32_t, int16_t, 1); else ENB_UL(int32_t, int32_t, 1);
+        } else {
+            if (m16) ENB_UL(int32_t, int16_t, 3); else ENB_UL(int32_t, int32_t, 3);
+        }
+    }
+#undef ENB_UL
+    return cudaGetLastError();
+}
+
+cudaError_t launch_out0(const PlanarView* gw1, const PlanarView* gb1, const PlanarView* r1, const Out0Host& h,
+                        cudaStream_t st)
+{
+    const PixelView& wv = h.white;
+    Out0Args a{};
+    a.white = wv.p;
+    a.black = h.black.p;
+    a.wpitch = wv.pitch;
+    a.bpitch = h.black.pitch;
+    a.wa = h.white_alpha.mode == kAlphaPlane ? h.white_alpha.plane.p : nullptr;
+    a.ba = h.black_alpha.mode == kAlphaPlane ? h.black_alpha.plane.p : nullptr;
+    a.wapitch = h.white_alpha.mode == kAlphaPlane ? h.white_alpha.plane.pitch : 0;
+    a.bapitch = h.black_alpha.mode == kAlphaPlane ? h.black_alpha.plane.pitch : 0;
+    a.alo = h.white_alpha.lo;
+    a.ahi = h.white_alpha.hi;
+    a.mask = h.mask.p;
+    a.mpitch = h.mask.pitch;
+    a.mfrac = h.mfrac;
+    a.white_value = h.white_value;
+    a.out = h.out;
+    a.opitch = h.opitch;
+    a.out_alpha = h.out_alpha.p;
+    a.oapitch = h.out_alpha.pitch;
+    a.level0 = h.level0;
+    a.w = wv.w;
+    a.h = wv.h;
+    a.frac = h.frac;
+    a.dither = h.dither;
+    a.has_coarse = gw1 != nullptr;
+    a.wrap = h.wrap;
+    a.seed = h.seed;
+    a.key = dither_key(h.seed);
+    a.maxv = wv.dtype == ENB_U8 ? 255 : 65535;
+    CoarseLevels cl{};
+    if (gw1) {
+        cl = coarse_of(*gw1, *gb1, *r1);
+    }
+    const double px = npix_f(wv.w, wv.h);
+    note_launch("out0", px * (3.0 * wv.stride * esz_f(wv.dtype) + 1.0 + (h.out_alpha.p ? 1.0 : 0.0)) +
+                            (gw1 ? 3.0 * pbytes(*gw1) : 0.0));
+    Out0Launch l{cl, a, grid2d(wv.w, wv.h, ETW, ETH), st};
+    const bool vec = vec_ok(wv.p, wv.pitch, wv.dtype, wv.stride) &&
+                     vec_ok(h.black.p, h.black.pitch, wv.dtype, wv.stride) && vec_ok(h.out, h.opitch, wv.dtype, wv.stride);
+    return dispatch_pixels(wv.dtype, wv.C, wv.stride, alpha_mode_code(h.white_alpha), vec, l);
+}
+
+}  // namespace enb

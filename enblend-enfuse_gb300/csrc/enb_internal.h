@@ -83,6 +83,22 @@ struct LaunchInfo {
     double bytes;
 };
 LaunchInfo& last_launch();
+inline void note_launch(const char* name, double bytes) { last_launch() = LaunchInfo{name, bytes}; }
+
+// Level-0 pass of the fused enblend (enb_fused.cu).
+struct Out0Host {
+    PixelView white, black;
+    AlphaSrc white_alpha, black_alpha;  // same mode for both
+    BytePlane mask;
+    int mfrac;
+    int32_t white_value;
+    void* out;
+    int64_t opitch;       // elements
+    BytePlane out_alpha;  // p == nullptr: not written
+    int32_t* level0;      // collapsed level 0 (interleaved int32) or nullptr
+    int frac, dither, wrap;
+    uint64_t seed;
+};
 
 // ---- launchers (all queue on `st` and return the CUDA launch status) ------
 cudaError_t launch_to_fixed(const PixelView& src, const PlanarView& dst, int frac, cudaStream_t st);
@@ -111,5 +127,19 @@ cudaError_t launch_hard_mask(const FloatPlane* masks, int K, cudaStream_t st);
 cudaError_t launch_soft_mask_to_fixed(const FloatPlane& mask, const FloatPlane& norm, int K,
                                       const PlanarView& dst, int frac, cudaStream_t st);
 cudaError_t launch_copy_level0(const PlanarView& src, int32_t* dst, cudaStream_t st);
+cudaError_t launch_alpha_component(const BytePlane& alpha, void* dst, int64_t dst_pitch, int dst_dtype,
+                                   cudaStream_t st);
+
+// fused enblend passes (enb_fused.cu)
+cudaError_t launch_reduce0_alpha(const PixelView& src, const AlphaSrc& a, int frac, const PlanarView& dst,
+                                 const BytePlane& dst_alpha, int wrap, cudaStream_t st);
+cudaError_t launch_reduce0_bytes(const BytePlane& src, int frac, const PlanarView& dst, int wrap, cudaStream_t st);
+cudaError_t launch_blend_into(const PlanarView& mask, const PlanarView& gw, const PlanarView& gb,
+                              const PlanarView& r, int32_t white_value, cudaStream_t st);
+cudaError_t launch_up_level(const PlanarView& gw1, const PlanarView& gb1, const PlanarView& r1,
+                            const PlanarView& mask, const PlanarView& gw, const PlanarView& gb,
+                            const PlanarView& r, int32_t white_value, int wrap, cudaStream_t st);
+cudaError_t launch_out0(const PlanarView* gw1, const PlanarView* gb1, const PlanarView* r1, const Out0Host& h,
+                        cudaStream_t st);
 
 }  // namespace enb

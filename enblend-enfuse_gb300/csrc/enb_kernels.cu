@@ -10,81 +10,11 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "enb_device.cuh"
 #include "enb_internal.h"
+#include "enb_reduce.cuh"
 
 namespace enb {
-
-// ---------------------------------------------------------------------------
-// Helpers
-// ---------------------------------------------------------------------------
-
-template <typename T>
-__device__ __forceinline__ T cast_store(int64_t v);  // static_cast into the pyramid type
-
-template <>
-__device__ __forceinline__ int16_t cast_store<int16_t>(int64_t v) { return (int16_t)(uint16_t)(v & 0xffff); }
-
-template <>
-__device__ __forceinline__ int32_t cast_store<int32_t>(int64_t v) { return (int32_t)(uint32_t)(v & 0xffffffffu); }
-
-// NumericTraits<T>::fromPromote: saturate Int16, identity for Int32.
-template <typename T>
-__device__ __forceinline__ T sat_store(int32_t v);
-
-template <>
-__device__ __forceinline__ int16_t sat_store<int16_t>(int32_t v) { return (int16_t)min(max(v, -32768), 32767); }
-
-template <>
-__device__ __forceinline__ int32_t sat_store<int32_t>(int32_t v) { return v; }
-
-// NumericTraits<T>::fromRealPromote of a double (round half away from zero
-// through +-0.5 and a truncating cast, saturating).
-template <typename T>
-__device__ __forceinline__ T frp_store(double v);
-
-template <>
-__device__ __forceinline__ int32_t frp_store<int32_t>(double v)
-{
-    if (v < 0.0) {
-        return v < -2147483648.0 ? INT32_MIN : __double2int_rz(__dadd_rn(v, -0.5));
-    }
-    return v > 2147483647.0 ? INT32_MAX : __double2int_rz(__dadd_rn(v, 0.5));
-}
-
-template <>
-__device__ __forceinline__ int16_t frp_store<int16_t>(double v)
-{
-    if (v < 0.0) {
-        return v < -32768.0 ? (int16_t)-32768 : (int16_t)__double2int_rz(__dadd_rn(v, -0.5));
-    }
-    return v > 32767.0 ? (int16_t)32767 : (int16_t)__double2int_rz(__dadd_rn(v, 0.5));
-}
-
-__device__ __forceinline__ uint32_t frp_unsigned(double v, uint32_t maxv)
-{
-    if (v < 0.0) {
-        return 0u;
-    }
-    return v > (double)maxv ? maxv : (uint32_t)__double2uint_rz(__dadd_rn(v, 0.5));
-}
-
-__host__ __device__ __forceinline__ int imod(int a, int m)
-{
-    int r = a % m;
-    return r < 0 ? r + m : r;
-}
-
-template <typename T>
-__device__ __forceinline__ T* plane_ptr(const PlanarView& v, int c, int y)
-{
-    return reinterpret_cast<T*>(v.p) + (int64_t)c * v.plane + (int64_t)y * v.pitch;
-}
-
-__device__ __forceinline__ uint32_t load_sample(const void* p, int dtype, int64_t i)
-{
-    return dtype == ENB_U8 ? (uint32_t)reinterpret_cast<const uint8_t*>(p)[i]
-                           : (uint32_t)reinterpret_cast<const uint16_t*>(p)[i];
-}
 
 __device__ __forceinline__ int alpha_at(const AlphaSrc& a, int x, int y)
 {
@@ -96,11 +26,6 @@ __device__ __forceinline__ int alpha_at(const AlphaSrc& a, int x, int y)
     }
     const uint32_t v = load_sample(a.pix.p, a.pix.dtype, (int64_t)y * a.pix.pitch + (int64_t)x * a.pix.stride + 3);
     return v >= a.lo && v <= a.hi;
-}
-
-static inline dim3 grid2d(int w, int h, int tw, int th)
-{
-    return dim3((unsigned)((w + tw - 1) / tw), (unsigned)((h + th - 1) / th));
 }
 
 // ---------------------------------------------------------------------------
@@ -193,155 +118,7 @@ __global__ void __launch_bounds__(256) k_alpha_extract(AlphaSrc a, uint8_t* __re
     dst[(int64_t)y * dpitch + x] = alpha_at(a, x, y) ? 255 : 0;
 }
 
-// ---------------------------------------------------------------------------
-// Reduce (src/pyramid.h:166-848)
-// ---------------------------------------------------------------------------
-//
-// One CTA computes a 32x8 tile of destination pixels.  The 67x19 source
-// window (2 pixels of halo) is staged in shared memory, then filtered with
-// the separable [1 4 6 4 1] kernel: first along x at the even source
-// columns, then along y.  Integer sums are exact, so the order of the taps
-// does not matter.
-
-constexpr int RTW = 32, RTH = 8;
-constexpr int RIW = 2 * RTW + 3, RIH = 2 * RTH + 3;
-
-// With alpha: normalised convolution over the opaque taps, taps outside the
-// image dropped, x periodic when wrap.
-template <typename TS, typename TD, int C>
-__global__ void __launch_bounds__(256) k_reduce_alpha(const TS* __restrict__ src, int64_t spitch, int64_t splane,
-                                                      int sw, int sh, const uint8_t* __restrict__ sa,
-                                                      int64_t sapitch, TD* __restrict__ dst, int64_t dpitch,
-                                                      int64_t dplane, int dw, int dh, uint8_t* __restrict__ da,
-                                                      int64_t dapitch, int wrap)
-{
-    __shared__ int32_t sv[C][RIH][RIW];
-    __shared__ int32_t sm[RIH][RIW];
-    __shared__ int32_t hv[C][RIH][RTW];
-    __shared__ int32_t hm[RIH][RTW];
-
-    const int X0 = blockIdx.x * RTW, Y0 = blockIdx.y * RTH;
-    const int gx0 = 2 * X0 - 2, gy0 = 2 * Y0 - 2;
-    const int tid = threadIdx.x;
-
-    for (int i = tid; i < RIH * RIW; i += 256) {
-        const int r = i / RIW, c = i - r * RIW;
-        const int gy = gy0 + r;
-        int gx = gx0 + c;
-        int a = 0;
-        int32_t v[C];
-#pragma unroll
-        for (int ch = 0; ch < C; ++ch) {
-            v[ch] = 0;
-        }
-        if (gy >= 0 && gy < sh) {
-            if (wrap) {
-                gx = imod(gx, sw);
-            }
-            if (gx >= 0 && gx < sw) {
-                a = sa[(int64_t)gy * sapitch + gx] != 0;
-                if (a) {
-#pragma unroll
-                    for (int ch = 0; ch < C; ++ch) {
-                        v[ch] = (int32_t)src[(int64_t)ch * splane + (int64_t)gy * spitch + gx];
-                    }
-                }
-            }
-        }
-        sm[r][c] = a;
-#pragma unroll
-        for (int ch = 0; ch < C; ++ch) {
-            sv[ch][r][c] = v[ch];
-        }
-    }
-    __syncthreads();
-
-    for (int i = tid; i < RIH * RTW; i += 256) {
-        const int r = i / RTW, j = i - r * RTW;
-        const int c0 = 2 * j;
-        hm[r][j] = sm[r][c0] + 4 * sm[r][c0 + 1] + 6 * sm[r][c0 + 2] + 4 * sm[r][c0 + 3] + sm[r][c0 + 4];
-#pragma unroll
-        for (int ch = 0; ch < C; ++ch) {
-            hv[ch][r][j] = sv[ch][r][c0] + 4 * sv[ch][r][c0 + 1] + 6 * sv[ch][r][c0 + 2] +
-                           4 * sv[ch][r][c0 + 3] + sv[ch][r][c0 + 4];
-        }
-    }
-    __syncthreads();
-
-    const int tx = tid % RTW, ty = tid / RTW;
-    const int X = X0 + tx, Y = Y0 + ty;
-    if (X >= dw || Y >= dh) {
-        return;
-    }
-    const int r0 = 2 * ty;
-    const int den = hm[r0][tx] + 4 * hm[r0 + 1][tx] + 6 * hm[r0 + 2][tx] + 4 * hm[r0 + 3][tx] + hm[r0 + 4][tx];
-    if (den > 0) {
-#pragma unroll
-        for (int ch = 0; ch < C; ++ch) {
-            const int32_t num = hv[ch][r0][tx] + 4 * hv[ch][r0 + 1][tx] + 6 * hv[ch][r0 + 2][tx] +
-                                4 * hv[ch][r0 + 3][tx] + hv[ch][r0 + 4][tx];
-            const int32_t q = den == 256 ? num / 256 : num / den;
-            dst[(int64_t)ch * dplane + (int64_t)Y * dpitch + X] = cast_store<TD>(q);
-        }
-        da[(int64_t)Y * dapitch + X] = 255;
-    } else {
-#pragma unroll
-        for (int ch = 0; ch < C; ++ch) {
-            dst[(int64_t)ch * dplane + (int64_t)Y * dpitch + X] = (TD)0;
-        }
-        da[(int64_t)Y * dapitch + X] = 0;
-    }
-}
-
-// Without alpha: clamp-to-edge in y (and x unless wrap), divide by 256.
-template <typename TS, typename TD, int C>
-__global__ void __launch_bounds__(256) k_reduce_noalpha(const TS* __restrict__ src, int64_t spitch, int64_t splane,
-                                                        int sw, int sh, TD* __restrict__ dst, int64_t dpitch,
-                                                        int64_t dplane, int dw, int dh, int wrap)
-{
-    __shared__ int32_t sv[C][RIH][RIW];
-    __shared__ int32_t hv[C][RIH][RTW];
-
-    const int X0 = blockIdx.x * RTW, Y0 = blockIdx.y * RTH;
-    const int gx0 = 2 * X0 - 2, gy0 = 2 * Y0 - 2;
-    const int tid = threadIdx.x;
-
-    for (int i = tid; i < RIH * RIW; i += 256) {
-        const int r = i / RIW, c = i - r * RIW;
-        const int gy = min(max(gy0 + r, 0), sh - 1);
-        int gx = gx0 + c;
-        gx = wrap ? imod(gx, sw) : min(max(gx, 0), sw - 1);
-#pragma unroll
-        for (int ch = 0; ch < C; ++ch) {
-            sv[ch][r][c] = (int32_t)src[(int64_t)ch * splane + (int64_t)gy * spitch + gx];
-        }
-    }
-    __syncthreads();
-
-    for (int i = tid; i < RIH * RTW; i += 256) {
-        const int r = i / RTW, j = i - r * RTW;
-        const int c0 = 2 * j;
-#pragma unroll
-        for (int ch = 0; ch < C; ++ch) {
-            hv[ch][r][j] = sv[ch][r][c0] + 4 * sv[ch][r][c0 + 1] + 6 * sv[ch][r][c0 + 2] +
-                           4 * sv[ch][r][c0 + 3] + sv[ch][r][c0 + 4];
-        }
-    }
-    __syncthreads();
-
-    const int tx = tid % RTW, ty = tid / RTW;
-    const int X = X0 + tx, Y = Y0 + ty;
-    if (X >= dw || Y >= dh) {
-        return;
-    }
-    const int r0 = 2 * ty;
-#pragma unroll
-    for (int ch = 0; ch < C; ++ch) {
-        const int32_t num = hv[ch][r0][tx] + 4 * hv[ch][r0 + 1][tx] + 6 * hv[ch][r0 + 2][tx] +
-                            4 * hv[ch][r0 + 3][tx] + hv[ch][r0 + 4][tx];
-        dst[(int64_t)ch * dplane + (int64_t)Y * dpitch + X] = cast_store<TD>(num / 256);
-    }
-}
+// Reduce (src/pyramid.h:166-848): k_reduce_tiles in enb_reduce.cuh.
 
 // ---------------------------------------------------------------------------
 // Expand (src/pyramid.h:875-1457)
@@ -353,67 +130,6 @@ __global__ void __launch_bounds__(256) k_reduce_noalpha(const TS* __restrict__ s
 // sums (64 or 16 inside the image; 56, 49, 14, 8, ... at the borders).  One
 // thread handles the 2x2 destination quad of one source pixel.
 
-constexpr int ETW = 64, ETH = 16;
-constexpr int ESW = ETW / 2 + 2, ESH = ETH / 2 + 2;
-
-// Horizontal weights on source offsets (-1, 0, +1) of destination column X
-// and their divisor; see the SKIPSM scale tables at src/pyramid.h:1227-1411.
-__device__ __forceinline__ void expand_hweights(int X, int sw, int dw, int wrap, int w[3], int& den)
-{
-    const int i = X >> 1;
-    if ((X & 1) == 0) {
-        if (wrap && sw == 1) {
-            // single source column: the wrapped left state joins the
-            // numerator over the plain divisor (src/pyramid.h:1233-1236,1304-1307)
-            w[0] = 0;
-            w[1] = (dw & 1) ? 10 : 7;
-            w[2] = 0;
-            den = 6;
-            return;
-        }
-        w[0] = 1;
-        w[1] = 6;
-        w[2] = 1;
-        if (wrap) {
-            if (dw & 1) {
-                if (i == 0) {
-                    w[0] = 4;
-                }
-                if (i == sw - 1) {
-                    w[2] = 4;
-                }
-            }
-        } else {
-            if (i == 0) {
-                w[0] = 0;
-            }
-            if (i + 1 >= sw) {
-                w[2] = 0;
-            }
-        }
-    } else {
-        w[0] = 0;
-        w[1] = 4;
-        w[2] = (i + 1 < sw || (wrap && sw > 1)) ? 4 : 0;
-    }
-    den = w[0] + w[1] + w[2];
-}
-
-__device__ __forceinline__ void expand_vweights(int Y, int sh, int w[3], int& den)
-{
-    const int j = Y >> 1;
-    if ((Y & 1) == 0) {
-        w[0] = j > 0 ? 1 : 0;
-        w[1] = 6;
-        w[2] = j + 1 < sh ? 1 : 0;
-    } else {
-        w[0] = 0;
-        w[1] = 1;
-        w[2] = j + 1 < sh ? 1 : 0;
-    }
-    den = w[0] + w[1] + w[2];
-}
-
 template <typename T, bool ADD>
 __device__ __forceinline__ void expand_combine(T* d, int32_t e)
 {
@@ -422,17 +138,6 @@ __device__ __forceinline__ void expand_combine(T* d, int32_t e)
     } else {
         *d = cast_store<T>((int64_t)*d - e);
     }
-}
-
-__device__ __forceinline__ int32_t div_den(int32_t num, int den)
-{
-    if (den == 64) {
-        return num / 64;
-    }
-    if (den == 16) {
-        return num / 16;
-    }
-    return num / den;
 }
 
 template <typename T, int C, bool ADD>
@@ -645,23 +350,6 @@ __global__ void __launch_bounds__(256) k_mask_mul_acc_generic(const T* __restric
 // Conversion from fixed point (src/fixmath.h:241-277)
 // ---------------------------------------------------------------------------
 
-__device__ __forceinline__ uint32_t mix32(uint32_t x)
-{
-    x ^= x >> 16;
-    x *= 0x7feb352du;
-    x ^= x >> 15;
-    x *= 0x846ca68bu;
-    x ^= x >> 16;
-    return x;
-}
-
-// Counter-based random bits of sample `index` (same rule as the oracle).
-__device__ __forceinline__ uint32_t dither_bits(uint64_t seed, uint64_t index)
-{
-    const uint32_t hi = mix32((uint32_t)(index >> 32) ^ (uint32_t)(seed >> 32) ^ 0x9e3779b9u);
-    return mix32((uint32_t)index ^ (uint32_t)seed ^ hi);
-}
-
 template <typename TS, typename TD>
 __global__ void __launch_bounds__(256) k_from_fixed(const TS* __restrict__ src, int64_t spitch, int64_t splane, int C,
                                                     const uint8_t* __restrict__ alpha, int64_t apitch,
@@ -673,26 +361,14 @@ __global__ void __launch_bounds__(256) k_from_fixed(const TS* __restrict__ src, 
     if (x >= w || !alpha[(int64_t)y * apitch + x]) {
         return;
     }
-    const int32_t half_m1 = (1 << (frac - 1)) - 1;
-    const int32_t quarter = 1 << (frac - 2);
-    const int32_t three_quarter = 3 << (frac - 2);
-    const int32_t half = 1 << (frac - 1);
+    const uint32_t key = dither_key(seed);
     const uint64_t pix = (uint64_t)y * (uint64_t)w + (uint64_t)x;
+    const uint32_t pixbits = mix32((uint32_t)pix ^ key);
     for (int c = 0; c < C; ++c) {
         const int32_t v = (int32_t)src[(int64_t)c * splane + (int64_t)y * spitch + x];
-        const int32_t q = v >> frac;
-        const int32_t f = v & ((1 << frac) - 1);
-        int32_t r;
-        if (dither == ENB_DITHER_NEAREST) {
-            r = f >= half ? q + 1 : q;
-        } else if (f >= quarter && f < three_quarter) {
-            const int32_t rnd = (int32_t)(dither_bits(seed, pix * (uint64_t)C + (uint64_t)c) & (uint32_t)half_m1) + quarter;
-            r = rnd <= f ? q + 1 : q;
-        } else {
-            r = f >= quarter ? q + 1 : q;
-        }
-        r = min(max(r, 0), maxv);
-        dst[(int64_t)y * dpitch + (int64_t)x * dstride + c] = (TD)r;
+        const uint32_t bits = dither_sample_bits(key, pixbits, pix, C, c, frac);
+        dst[(int64_t)y * dpitch + (int64_t)x * dstride + c] =
+            (TD)dither_rule(v, frac, dither == ENB_DITHER_NEAREST, bits, maxv);
     }
 }
 
@@ -704,6 +380,19 @@ __global__ void __launch_bounds__(256) k_copy_pixels(const T* __restrict__ src, 
     const int y = blockIdx.y;
     if (x < rowlen) {
         dst[(int64_t)y * dpitch + x] = src[(int64_t)y * spitch + x];
+    }
+}
+
+// 4th component of an RGBA result: the union alpha scaled to the sample type,
+// as the output writer stores the alpha image (src/assemble.h:133-225).
+template <typename T>
+__global__ void __launch_bounds__(256) k_alpha_component(const uint8_t* __restrict__ a, int64_t apitch,
+                                                         T* __restrict__ dst, int64_t dpitch, int w, int h, T maxv)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (x < w) {
+        dst[(int64_t)y * dpitch + (int64_t)x * 4 + 3] = a[(int64_t)y * apitch + x] ? maxv : (T)0;
     }
 }
 
@@ -1114,13 +803,13 @@ template <typename TS, typename TD, int C>
 static void reduce_dispatch(int wrap, const PlanarView& s, const BytePlane* sa, const PlanarView& d,
                             const BytePlane* da, cudaStream_t st)
 {
-    const dim3 g = grid2d(d.w, d.h, RTW, RTH);
+    const PlanarSource<TS, C> src{(const TS*)s.p, s.pitch, s.plane, sa ? sa->p : nullptr, sa ? sa->pitch : 0};
     if (sa) {
-        k_reduce_alpha<TS, TD, C><<<g, 256, 0, st>>>((const TS*)s.p, s.pitch, s.plane, s.w, s.h, sa->p, sa->pitch,
-                                                     (TD*)d.p, d.pitch, d.plane, d.w, d.h, da->p, da->pitch, wrap);
+        launch_reduce_tiles<PlanarSource<TS, C>, TD, C, true>(src, s.w, s.h, (TD*)d.p, d.pitch, d.plane, d.w, d.h, da->p,
+                                                             da->pitch, wrap, st);
     } else {
-        k_reduce_noalpha<TS, TD, C><<<g, 256, 0, st>>>((const TS*)s.p, s.pitch, s.plane, s.w, s.h, (TD*)d.p, d.pitch,
-                                                       d.plane, d.w, d.h, wrap);
+        launch_reduce_tiles<PlanarSource<TS, C>, TD, C, false>(src, s.w, s.h, (TD*)d.p, d.pitch, d.plane, d.w, d.h,
+                                                              nullptr, 0, wrap, st);
     }
 }
 
@@ -1298,6 +987,18 @@ cudaError_t launch_copy_pixels(const PixelView& s, void* dst, int64_t dpitch, cu
         k_copy_pixels<uint8_t><<<g, 256, 0, st>>>((const uint8_t*)s.p, s.pitch, (uint8_t*)dst, dpitch, rowlen, s.h);
     } else {
         k_copy_pixels<uint16_t><<<g, 256, 0, st>>>((const uint16_t*)s.p, s.pitch, (uint16_t*)dst, dpitch, rowlen, s.h);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_alpha_component(const BytePlane& a, void* dst, int64_t dpitch, int ddtype, cudaStream_t st)
+{
+    note("alpha_component", npix(a.w, a.h) * (1.0 + esz(ddtype)));
+    const dim3 g = row_grid(a.w, a.h);
+    if (ddtype == ENB_U8) {
+        k_alpha_component<uint8_t><<<g, 256, 0, st>>>(a.p, a.pitch, (uint8_t*)dst, dpitch, a.w, a.h, (uint8_t)255);
+    } else {
+        k_alpha_component<uint16_t><<<g, 256, 0, st>>>(a.p, a.pitch, (uint16_t*)dst, dpitch, a.w, a.h, (uint16_t)65535);
     }
     return cudaGetLastError();
 }

@@ -20,7 +20,7 @@ INCLUDE = REPO / "include"
 BUILD_DIR = ROOT / "_build"
 LIB_PATH = PKG_DIR / "libenbgpu.so"
 
-SOURCES = ["enb_kernels.cu", "enb_api.cu"]
+SOURCES = ["enb_kernels.cu", "enb_fused.cu", "enb_api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -35,7 +35,7 @@ def _stale() -> bool:
     if not LIB_PATH.exists():
         return True
     t = LIB_PATH.stat().st_mtime
-    deps = [CSRC / s for s in SOURCES] + list(CSRC.glob("*.h")) + [INCLUDE / "enbgpu.h"]
+    deps = [CSRC / s for s in SOURCES] + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [INCLUDE / "enbgpu.h"]
     return any(d.stat().st_mtime > t for d in deps)
 
 

@@ -111,7 +111,10 @@ typedef struct {
     int32_t host_buffers;  /* 1: all image pointers are host memory; copies are
                               done on the context stream and the call returns
                               after the result is back in host memory */
-    int32_t reserved;
+    int32_t plain;         /* 1: run the reference's pass structure (one kernel
+                              per reference operation, every level materialised)
+                              instead of the fused level passes; same result,
+                              for comparisons */
     void* level0_out;      /* optional device buffer (host if host_buffers):
                               collapsed level 0 before conversion, int32,
                               interleaved width*height*channels */
@@ -243,7 +246,9 @@ enb_status enb_enfuse(enb_ctx* ctx, const enb_enfuse_params* params, int K, cons
 
 /* enblendMain's pyramid section (src/enblend.h:330-510): blend `white` into
  * `black` under the 0/255 seam mask over the whole canvas.  out receives the
- * black image with the blended pixels where the union alpha is set. */
+ * black image with the blended pixels where the union alpha is set (for RGBA
+ * images the 4th component becomes the union alpha, 0 or the type maximum);
+ * out may be the black image itself. */
 enb_status enb_enblend(enb_ctx* ctx, const enb_image* white, const enb_image* white_alpha,
                        const enb_image* black, const enb_image* black_alpha, const enb_image* mask,
                        const enb_image* out, const enb_image* out_alpha, const enb_fuse_options* opt);

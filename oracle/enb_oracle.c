@@ -422,10 +422,21 @@ static inline uint32_t mix32(uint32_t x)
     return x;
 }
 
-uint32_t orc_dither_bits(uint64_t seed, uint64_t index)
+/* Random bits of the dither: one hash per pixel, 8 bits per channel when
+ * the rule needs at most 8 bits per sample and the pixel has at most four
+ * samples, otherwise one hash per sample.  The pixel index wraps at 2^32. */
+static inline uint32_t dither_key(uint64_t seed)
 {
-    const uint32_t hi = mix32((uint32_t)(index >> 32) ^ (uint32_t)(seed >> 32) ^ 0x9e3779b9u);
-    return mix32((uint32_t)index ^ (uint32_t)seed ^ hi);
+    return mix32((uint32_t)(seed >> 32) ^ 0x9e3779b9u) ^ (uint32_t)seed;
+}
+
+uint32_t orc_dither_bits(uint64_t seed, uint64_t pixel, int C, int c, int frac)
+{
+    const uint32_t key = dither_key(seed);
+    if (frac - 1 <= 8 && C <= 4) {
+        return mix32((uint32_t)pixel ^ key) >> (8 * c);
+    }
+    return mix32((uint32_t)(pixel * (uint64_t)C + (uint64_t)c) ^ key);
 }
 
 void orc_from_fixed(const int32_t* src, const uint8_t* alpha, int64_t npix, int C,
@@ -450,7 +461,7 @@ void orc_from_fixed(const int32_t* src, const uint8_t* alpha, int64_t npix, int 
                 r = f >= half ? q + 1 : q;
             } else if (f >= quarter && f < three_quarter) {
                 const int32_t rnd =
-                    (int32_t)(orc_dither_bits(seed, (uint64_t)p * (uint64_t)C + (uint64_t)c) & (uint32_t)half_m1) + quarter;
+                    (int32_t)(orc_dither_bits(seed, (uint64_t)p, C, c, frac) & (uint32_t)half_m1) + quarter;
                 r = rnd <= f ? q + 1 : q;
             } else if (f >= quarter) {
                 r = q + 1;
@@ -463,6 +474,22 @@ void orc_from_fixed(const int32_t* src, const uint8_t* alpha, int64_t npix, int 
             } else {
                 ((uint16_t*)dst)[p * pix_stride + c] = (uint16_t)r;
             }
+        }
+    }
+}
+
+/* The alpha component of an RGBA result: the union alpha scaled to the
+ * sample type, as the output writer stores the alpha image
+ * (src/assemble.h:133-225). */
+static void write_alpha_component(void* dst, int dtype, int64_t npix, const uint8_t* alpha)
+{
+    if (dtype == ORC_U8) {
+        for (int64_t p = 0; p < npix; ++p) {
+            ((uint8_t*)dst)[p * 4 + 3] = alpha[p] ? 255 : 0;
+        }
+    } else {
+        for (int64_t p = 0; p < npix; ++p) {
+            ((uint16_t*)dst)[p * 4 + 3] = alpha[p] ? 65535 : 0;
         }
     }
 }
@@ -956,6 +983,9 @@ int orc_enfuse(int K, const void* const* imgs, const uint8_t* const* alphas, int
         const size_t esz = dtype == ORC_U8 ? 1 : 2;
         memset(out, 0, esz * (size_t)npix * pix_stride);
         orc_from_fixed(result.lv[0], out_alpha, npix, C, out, dtype, pix_stride, frac, dither_mode, seed);
+        if (pix_stride == 4) {
+            write_alpha_component(out, dtype, npix, out_alpha);
+        }
     }
     pyr_free(&result);
 done:
@@ -1025,6 +1055,9 @@ int orc_enblend(const void* white, const uint8_t* white_alpha, const void* black
         const size_t esz = dtype == ORC_U8 ? 1 : 2;
         memcpy(out, black, esz * (size_t)npix * pix_stride);
         orc_from_fixed(bl.lv[0], out_alpha, npix, C, out, dtype, pix_stride, frac, dither_mode, seed);
+        if (pix_stride == 4) {
+            write_alpha_component(out, dtype, npix, out_alpha);
+        }
     }
     pyr_free(&mg);
     pyr_free(&wl);

@@ -104,8 +104,9 @@ void orc_accumulate(const int32_t* lp, int32_t* res, int64_t n, int bits);
 void orc_from_fixed(const int32_t* src, const uint8_t* alpha, int64_t npix, int C,
                     void* dst, int dtype, int pix_stride, int frac, int dither_mode, uint64_t seed);
 
-/* Dither random bits of one sample (shared rule with the CUDA path). */
-uint32_t orc_dither_bits(uint64_t seed, uint64_t index);
+/* Dither random bits of sample c of pixel `pixel` (shared rule with the CUDA
+ * path; only the low frac-1 bits are used). */
+uint32_t orc_dither_bits(uint64_t seed, uint64_t pixel, int C, int c, int frac);
 
 /* enfuseMask: exposure, contrast, saturation and entropy weights (src/enfuse.h:962-1212). */
 int orc_enfuse_mask(const void* img, int dtype, int w, int h, int C, int pix_stride,

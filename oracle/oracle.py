@@ -69,7 +69,7 @@ def lib() -> ctypes.CDLL:
         L.orc_mask_multiply.argtypes = [vp, vp, i64, i, ctypes.c_int32, i]
         L.orc_accumulate.argtypes = [vp, vp, i64, i]
         L.orc_from_fixed.argtypes = [vp, vp, i64, i, vp, i, i, i, i, u64]
-        L.orc_dither_bits.argtypes = [u64, u64]
+        L.orc_dither_bits.argtypes = [u64, u64, i, i, i]
         L.orc_dither_bits.restype = ctypes.c_uint32
         L.orc_enfuse_mask.argtypes = [vp, i, i, i, i, i, vp, ctypes.POINTER(OrcParams), vp]
         L.orc_local_stddev.argtypes = [vp, vp, i, i, i, vp]
@@ -206,8 +206,8 @@ def from_fixed(src: np.ndarray, alpha: np.ndarray, dtype, frac: int = 7, dither:
     return out
 
 
-def dither_bits(seed: int, index: int) -> int:
-    return int(lib().orc_dither_bits(seed, index))
+def dither_bits(seed: int, pixel: int, C: int = 3, c: int = 0, frac: int = 7) -> int:
+    return int(lib().orc_dither_bits(seed, pixel, C, c, frac))
 
 
 def enfuse_mask(img: np.ndarray, alpha: Optional[np.ndarray], prm: OrcParams) -> np.ndarray:

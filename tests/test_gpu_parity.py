@@ -263,15 +263,54 @@ def test_enfuse_host_buffers_and_injected_masks(ctx, orc, dt):
 
 @pytest.mark.parametrize("dt", [np.uint8, np.uint16])
 @pytest.mark.parametrize("wrap", [False, True])
-def test_enblend_end_to_end(ctx, orc, dt, wrap):
+@pytest.mark.parametrize("plain", [False, True])
+@pytest.mark.parametrize("geom", [(90, 120, 80), (7, 9, 5), (21, 30, 17), (40, 64, 40)])
+def test_enblend_end_to_end(ctx, orc, dt, wrap, plain, geom):
+    """Fused level passes and the reference pass structure, against the oracle.
+
+    Geometries give 8, 1, 2 and 4 pyramid levels (union canvases 200x90,
+    14x7, 47x21, 104x40)."""
     from enbgpu import synthetic
-    white, black, mask = synthetic.panorama_pair(90, 120, 80, dt, seed=31)
+    h, w, off = geom
+    white, black, mask = synthetic.panorama_pair(h, w, off, dt, seed=31)
+    if w > 20:
+        mask[: h // 3, off + 2: off + 9] = 128   # intermediate seam weights at level 0 too
     ref = orc.enblend(white, black, mask, wrap=wrap, seed=9, want_level0=True)
-    l0 = torch.zeros((90, 200, 3), dtype=torch.int32, device="cuda")
-    out, oa = ctx.enblend(_dev(white), _dev(black), _dev(mask), wrap=wrap, seed=9, level0=l0)
+    l0 = torch.zeros((h, w + off, 3), dtype=torch.int32, device="cuda")
+    out, oa = ctx.enblend(_dev(white), _dev(black), _dev(mask), wrap=wrap, seed=9, level0=l0, plain=plain)
     assert np.array_equal(l0.cpu().numpy(), ref["level0"])
     assert np.array_equal(oa.cpu().numpy(), ref["alpha"])
     assert np.array_equal(out.cpu().numpy(), ref["out"])
     # host-buffer entry point gives the same image
-    out2, _ = ctx.enblend(white, black, mask, wrap=wrap, seed=9)
+    out2, _ = ctx.enblend(white, black, mask, wrap=wrap, seed=9, plain=plain)
     assert np.array_equal(out2, ref["out"])
+
+
+@pytest.mark.parametrize("plain", [False, True])
+def test_enblend_alpha_sources(ctx, orc, plain):
+    """Alpha from planes, from the 4th component, mixed, and RGB images without alpha."""
+    from enbgpu import synthetic
+    white, black, mask = synthetic.panorama_pair(64, 96, 50, np.uint16, seed=33)
+    wa, ba = orc.alpha_of(white), orc.alpha_of(black)
+    wa[5:20, 60:80] = 0          # a hole in the white image's alpha plane
+    ref = orc.enblend(white, black, mask, white_alpha=wa, black_alpha=ba, seed=1)
+    for wa_arg, ba_arg in [(wa, ba), (wa, None)]:
+        out, oa = ctx.enblend(_dev(white), _dev(black), _dev(mask),
+                              white_alpha=_dev(wa) if wa_arg is not None else None,
+                              black_alpha=_dev(ba) if ba_arg is not None else None, seed=1, plain=plain)
+        assert np.array_equal(out.cpu().numpy(), ref["out"])
+        assert np.array_equal(oa.cpu().numpy(), ref["alpha"])
+    rgb_w, rgb_b = np.ascontiguousarray(white[..., :3]), np.ascontiguousarray(black[..., :3])
+    ref = orc.enblend(rgb_w, rgb_b, mask, seed=2)
+    out, oa = ctx.enblend(_dev(rgb_w), _dev(rgb_b), _dev(mask), seed=2, plain=plain)
+    assert np.array_equal(out.cpu().numpy(), ref["out"])
+
+
+def test_enblend_in_place(ctx, orc):
+    """out may alias the black image (the reference writes into it)."""
+    from enbgpu import synthetic
+    white, black, mask = synthetic.panorama_pair(50, 70, 40, np.uint16, seed=35)
+    ref = orc.enblend(white, black, mask, seed=3)
+    dw, db, dm = _dev(white), _dev(black), _dev(mask)
+    out, _ = ctx.enblend(dw, db, dm, out=db, seed=3)
+    assert np.array_equal(db.cpu().numpy(), ref["out"])
