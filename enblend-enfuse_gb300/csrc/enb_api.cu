@@ -716,16 +716,15 @@ enb_status enblend_fused(enb_ctx* ctx, const enb_image* white, const enb_image* 
         ENB_CUDA(ctx, awc.alloc(NL, w1, h1, ctx->stream));
         ENB_CUDA(ctx, abc.alloc(NL, w1, h1, ctx->stream));
         // Down sweep (src/enblend.h:384-446: the three Gaussian pyramids).
-        ENB_LAUNCH(ctx, launch_reduce0_alpha(pixel_view(white), wa, kImageFrac, level_view(gw.p, 0), awc.level(0),
-                                             wrap, ctx->stream));
-        ENB_LAUNCH(ctx, launch_reduce0_alpha(pixel_view(black), ba, kImageFrac, level_view(gb.p, 0), abc.level(0),
-                                             wrap, ctx->stream));
+        ENB_LAUNCH(ctx, launch_reduce0_alpha2(pixel_view(white), wa, level_view(gw.p, 0), awc.level(0),
+                                              pixel_view(black), ba, level_view(gb.p, 0), abc.level(0), kImageFrac,
+                                              wrap, ctx->stream));
         ENB_LAUNCH(ctx, launch_reduce0_bytes(byte_plane(mask), mf, level_view(mg.p, 0), wrap, ctx->stream));
         for (int j = 1; j < NL; ++j) {
             ENB_CHECK(ctx, gw.p->w[j - 1] > 1 && gw.p->h[j - 1] > 1, "reduce: src image too small in reduce");
             const BytePlane sa = awc.level(j - 1), da = awc.level(j), sb = abc.level(j - 1), db = abc.level(j);
-            ENB_LAUNCH(ctx, launch_reduce(wrap, level_view(gw.p, j - 1), &sa, level_view(gw.p, j), &da, ctx->stream));
-            ENB_LAUNCH(ctx, launch_reduce(wrap, level_view(gb.p, j - 1), &sb, level_view(gb.p, j), &db, ctx->stream));
+            ENB_LAUNCH(ctx, launch_reduce2(wrap, level_view(gw.p, j - 1), &sa, level_view(gw.p, j), &da,
+                                           level_view(gb.p, j - 1), &sb, level_view(gb.p, j), &db, ctx->stream));
             ENB_LAUNCH(ctx, launch_reduce(wrap, level_view(mg.p, j - 1), nullptr, level_view(mg.p, j), nullptr,
                                           ctx->stream));
         }

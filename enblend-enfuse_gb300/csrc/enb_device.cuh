@@ -10,9 +10,6 @@
 
 namespace enb {
 
-// Reduce tiles: 32x8 destination pixels from a 67x19 source window.
-constexpr int RTW = 32, RTH = 8;
-constexpr int RIW = 2 * RTW + 3, RIH = 2 * RTH + 3;
 // Expand tiles: 64x16 destination pixels (2x2 quads of 32x8 source pixels)
 // from a 34x10 source window.
 constexpr int ETW = 64, ETH = 16;
@@ -228,81 +225,42 @@ __device__ __forceinline__ int32_t dither_rule(int32_t v, int frac, int nearest,
     return min(max(r, 0), maxv);
 }
 
-// Second half of the reduce with alpha: separable [1 4 6 4 1] sums over the
-// staged window (values already zero where transparent), normalisation by the
-// opaque weight sum with a truncating division, destination alpha 255/0.
-template <typename TD, int C>
-__device__ __forceinline__ void reduce_alpha_finish(int32_t (*sv)[RIH][RIW], int32_t (*sm)[RIW],
-                                                    int32_t (*hv)[RIH][RTW], int32_t (*hm)[RTW], int X0, int Y0,
-                                                    TD* __restrict__ dst, int64_t dpitch, int64_t dplane, int dw,
-                                                    int dh, uint8_t* __restrict__ da, int64_t dapitch)
+// CartesianBlendFunctor of one sample (src/blend.h:41-76) in integers.
+//
+// The reference evaluates fromRealPromote(wc*lw + (1-wc)*lb) in double with
+// wc = fl(m/W).  For 0 < m < W the exact value v = N/W, N = m*lw + (W-m)*lb,
+// is either a half-integer or at least 1/(2W) away from one.  The double
+// evaluation, including the +-0.5 of the conversion, stays within
+// 7.2 * M * 2^-53 of v (M = max(|lw|, |lb|)): below 1/(2W) whenever
+// M*W < 2^48.  Then rounding v half away from zero is the reference's result;
+// exact half-integers and larger operands take the reference's double
+// expression.  floor(t / (255*2^k)) = floor(floor(t / 2^k) / 255), and
+// floor(x / 255) = mulhi(x, 0x8080808080808081) >> 7 for all 64-bit x.
+template <typename T>
+__device__ __forceinline__ int32_t blend_sample(int32_t m, int32_t W, int32_t lw, int32_t lb)
 {
-    const int tid = threadIdx.x;
-    for (int i = tid; i < RIH * RTW; i += 256) {
-        const int r = i / RTW, j = i - r * RTW;
-        const int c0 = 2 * j;
-        hm[r][j] = sm[r][c0] + 4 * sm[r][c0 + 1] + 6 * sm[r][c0 + 2] + 4 * sm[r][c0 + 3] + sm[r][c0 + 4];
-#pragma unroll
-        for (int ch = 0; ch < C; ++ch) {
-            hv[ch][r][j] = sv[ch][r][c0] + 4 * sv[ch][r][c0 + 1] + 6 * sv[ch][r][c0 + 2] +
-                           4 * sv[ch][r][c0 + 3] + sv[ch][r][c0 + 4];
+    if (m >= W) {
+        return lw;
+    }
+    if (m <= 0) {
+        return lb;
+    }
+    const uint32_t aw = lw < 0 ? 0u - (uint32_t)lw : (uint32_t)lw;
+    const uint32_t ab = lb < 0 ? 0u - (uint32_t)lb : (uint32_t)lb;
+    if ((uint64_t)max(aw, ab) * (uint64_t)W < (1ull << 48)) {
+        const int64_t n = (int64_t)m * lw + (int64_t)(W - m) * lb;
+        const uint64_t t = 2ull * (uint64_t)(n < 0 ? -n : n) + (uint64_t)W;
+        const uint64_t d = 2ull * (uint64_t)W;
+        const int wf = __ffs(W) - 1;
+        const uint64_t q =
+            (W >> wf) == 255 ? __umul64hi(t >> (wf + 1), 0x8080808080808081ull) >> 7 : t / d;
+        if (t != q * d) {
+            return n < 0 ? -(int32_t)q : (int32_t)q;
         }
     }
-    __syncthreads();
-    const int tx = tid % RTW, ty = tid / RTW;
-    const int X = X0 + tx, Y = Y0 + ty;
-    if (X >= dw || Y >= dh) {
-        return;
-    }
-    const int r0 = 2 * ty;
-    const int den = hm[r0][tx] + 4 * hm[r0 + 1][tx] + 6 * hm[r0 + 2][tx] + 4 * hm[r0 + 3][tx] + hm[r0 + 4][tx];
-    if (den > 0) {
-#pragma unroll
-        for (int ch = 0; ch < C; ++ch) {
-            const int32_t num = hv[ch][r0][tx] + 4 * hv[ch][r0 + 1][tx] + 6 * hv[ch][r0 + 2][tx] +
-                                4 * hv[ch][r0 + 3][tx] + hv[ch][r0 + 4][tx];
-            const int32_t q = den == 256 ? num / 256 : num / den;
-            dst[(int64_t)ch * dplane + (int64_t)Y * dpitch + X] = cast_store<TD>(q);
-        }
-        da[(int64_t)Y * dapitch + X] = 255;
-    } else {
-#pragma unroll
-        for (int ch = 0; ch < C; ++ch) {
-            dst[(int64_t)ch * dplane + (int64_t)Y * dpitch + X] = (TD)0;
-        }
-        da[(int64_t)Y * dapitch + X] = 0;
-    }
-}
-
-// Second half of the alpha-free reduce: separable sums, /256.
-template <typename TD, int C>
-__device__ __forceinline__ void reduce_noalpha_finish(int32_t (*sv)[RIH][RIW], int32_t (*hv)[RIH][RTW], int X0,
-                                                      int Y0, TD* __restrict__ dst, int64_t dpitch, int64_t dplane,
-                                                      int dw, int dh)
-{
-    const int tid = threadIdx.x;
-    for (int i = tid; i < RIH * RTW; i += 256) {
-        const int r = i / RTW, j = i - r * RTW;
-        const int c0 = 2 * j;
-#pragma unroll
-        for (int ch = 0; ch < C; ++ch) {
-            hv[ch][r][j] = sv[ch][r][c0] + 4 * sv[ch][r][c0 + 1] + 6 * sv[ch][r][c0 + 2] +
-                           4 * sv[ch][r][c0 + 3] + sv[ch][r][c0 + 4];
-        }
-    }
-    __syncthreads();
-    const int tx = tid % RTW, ty = tid / RTW;
-    const int X = X0 + tx, Y = Y0 + ty;
-    if (X >= dw || Y >= dh) {
-        return;
-    }
-    const int r0 = 2 * ty;
-#pragma unroll
-    for (int ch = 0; ch < C; ++ch) {
-        const int32_t num = hv[ch][r0][tx] + 4 * hv[ch][r0 + 1][tx] + 6 * hv[ch][r0 + 2][tx] +
-                            4 * hv[ch][r0 + 3][tx] + hv[ch][r0 + 4][tx];
-        dst[(int64_t)ch * dplane + (int64_t)Y * dpitch + X] = cast_store<TD>(num / 256);
-    }
+    const double wc = __ddiv_rn((double)m, (double)W);
+    const double bc = __dadd_rn(1.0, -wc);
+    return (int32_t)frp_store<T>(__dadd_rn(__dmul_rn(wc, (double)lw), __dmul_rn(bc, (double)lb)));
 }
 
 }  // namespace enb

@@ -39,13 +39,13 @@ template <typename TIn, int S, bool VEC>
 __device__ __forceinline__ void ld_px(const TIn* p, TIn (&o)[S])
 {
     if (VEC && S == 4 && sizeof(TIn) == 2) {
-        const uint2 v = *reinterpret_cast<const uint2*>(p);
+        const uint2 v = __ldg(reinterpret_cast<const uint2*>(p));
         o[0] = (TIn)(v.x & 0xffffu);
         o[1] = (TIn)(v.x >> 16);
         o[2] = (TIn)(v.y & 0xffffu);
         o[S - 1] = (TIn)(v.y >> 16);
     } else if (VEC && S == 4 && sizeof(TIn) == 1) {
-        const uint32_t v = *reinterpret_cast<const uint32_t*>(p);
+        const uint32_t v = __ldg(reinterpret_cast<const uint32_t*>(p));
         o[0] = (TIn)(v & 0xffu);
         o[1] = (TIn)((v >> 8) & 0xffu);
         o[2] = (TIn)((v >> 16) & 0xffu);
@@ -53,7 +53,7 @@ __device__ __forceinline__ void ld_px(const TIn* p, TIn (&o)[S])
     } else {
 #pragma unroll
         for (int c = 0; c < S; ++c) {
-            o[c] = p[c];
+            o[c] = __ldg(&p[c]);
         }
     }
 }
@@ -84,7 +84,7 @@ __device__ __forceinline__ int pixel_alpha(const TIn (&px)[S], const uint8_t* ap
                                            uint32_t alo, uint32_t ahi)
 {
     if (AM == 0) {
-        return ap[(int64_t)y * apitch + x] != 0;
+        return __ldg(&ap[(int64_t)y * apitch + x]) != 0;
     }
     if (AM == 1) {
         return 1;
@@ -119,20 +119,11 @@ struct PixelSourceV {
 // Merge helpers
 // ---------------------------------------------------------------------------
 
-// CartesianBlendFunctor of one sample (src/blend.h:41-76): integer tests for
-// the coefficients 1 and 0, the reference's double expression otherwise.
+// CartesianBlendFunctor of one sample (src/blend.h:41-76).
 template <typename T>
 __device__ __forceinline__ int32_t blend1(int32_t m, int32_t white_value, int32_t lw, int32_t lb)
 {
-    if (m >= white_value) {
-        return lw;
-    }
-    if (m <= 0) {
-        return lb;
-    }
-    const double wc = __ddiv_rn((double)m, (double)white_value);
-    const double bc = __dadd_rn(1.0, -wc);
-    return (int32_t)frp_store<T>(__dadd_rn(__dmul_rn(wc, (double)lw), __dmul_rn(bc, (double)lb)));
+    return blend_sample<T>(m, white_value, lw, lb);
 }
 
 // Top level: R = blend(M, Gw, Gb) (the top Laplacian level is the Gaussian).
@@ -617,21 +608,27 @@ static inline double npix_f(int w, int h) { return (double)w * (double)h; }
 static inline double pbytes(const PlanarView& v) { return npix_f(v.w, v.h) * v.C * esz_f(v.dtype); }
 
 struct Reduce0Launch {
-    const PixelView& s;
-    const uint8_t* ap;
-    int64_t apitch;
-    uint32_t lo, hi;
+    const PixelView* s[2];
+    const uint8_t* ap[2];
+    int64_t apitch[2];
+    uint32_t lo[2], hi[2];
+    const PlanarView* d[2];
+    const BytePlane* da[2];
+    int n;
     int frac;
-    const PlanarView& d;
-    const BytePlane& da;
     int wrap;
     cudaStream_t st;
     template <typename TIn, typename T, int C, int S, int AM, bool VEC>
     void operator()() const
     {
-        PixelSourceV<TIn, C, S, AM, VEC> src{(const TIn*)s.p, s.pitch, ap, apitch, lo, hi, frac};
-        launch_reduce_tiles<PixelSourceV<TIn, C, S, AM, VEC>, T, C, true>(src, s.w, s.h, (T*)d.p, d.pitch, d.plane, d.w,
-                                                                         d.h, da.p, da.pitch, wrap, st);
+        using Src = PixelSourceV<TIn, C, S, AM, VEC>;
+        ReduceJobs<Src, T> jobs{};
+        for (int i = 0; i < 2; ++i) {
+            const int k = i < n ? i : 0;
+            jobs.j[i] = ReduceJob<Src, T>{Src{(const TIn*)s[k]->p, s[k]->pitch, ap[k], apitch[k], lo[k], hi[k], frac},
+                                          (T*)d[k]->p, d[k]->pitch, d[k]->plane, da[k]->p, da[k]->pitch};
+        }
+        launch_reduce_jobs<Src, T, C, true>(jobs, n, s[0]->w, s[0]->h, d[0]->w, d[0]->h, wrap, st);
     }
 };
 
@@ -689,15 +686,63 @@ static int alpha_mode_code(const AlphaSrc& a)
     return a.mode == kAlphaPlane ? 0 : (a.mode == kAlphaOpaque ? 1 : 2);
 }
 
+static double reduce0_bytes(const PixelView& s, const AlphaSrc& a, const PlanarView& d)
+{
+    return npix_f(s.w, s.h) * s.stride * esz_f(s.dtype) + (a.mode == kAlphaPlane ? npix_f(s.w, s.h) : 0.0) +
+           pbytes(d) + npix_f(d.w, d.h);
+}
+
+static cudaError_t reduce0_launch(int n, const PixelView* const* s, const AlphaSrc* const* a, const PlanarView* const* d,
+                                  const BytePlane* const* da, int frac, int wrap, cudaStream_t st)
+{
+    Reduce0Launch l{};
+    double bytes = 0.0;
+    bool vec = true;
+    for (int i = 0; i < n; ++i) {
+        l.s[i] = s[i];
+        l.ap[i] = a[i]->mode == kAlphaPlane ? a[i]->plane.p : nullptr;
+        l.apitch[i] = a[i]->mode == kAlphaPlane ? a[i]->plane.pitch : 0;
+        l.lo[i] = a[i]->lo;
+        l.hi[i] = a[i]->hi;
+        l.d[i] = d[i];
+        l.da[i] = da[i];
+        bytes += reduce0_bytes(*s[i], *a[i], *d[i]);
+        vec = vec && vec_ok(s[i]->p, s[i]->pitch, s[i]->dtype, s[i]->stride);
+    }
+    l.n = n;
+    l.frac = frac;
+    l.wrap = wrap;
+    l.st = st;
+    note_launch("reduce0_alpha", bytes);
+    return dispatch_pixels(s[0]->dtype, s[0]->C, s[0]->stride, alpha_mode_code(*a[0]), vec, l);
+}
+
 cudaError_t launch_reduce0_alpha(const PixelView& s, const AlphaSrc& a, int frac, const PlanarView& d,
                                  const BytePlane& da, int wrap, cudaStream_t st)
 {
-    note_launch("reduce0_alpha", npix_f(s.w, s.h) * s.stride * esz_f(s.dtype) +
-                                     (a.mode == kAlphaPlane ? npix_f(s.w, s.h) : 0.0) + pbytes(d) + npix_f(d.w, d.h));
-    const uint8_t* ap = a.mode == kAlphaPlane ? a.plane.p : nullptr;
-    const int64_t apitch = a.mode == kAlphaPlane ? a.plane.pitch : 0;
-    Reduce0Launch l{s, ap, apitch, a.lo, a.hi, frac, d, da, wrap, st};
-    return dispatch_pixels(s.dtype, s.C, s.stride, alpha_mode_code(a), vec_ok(s.p, s.pitch, s.dtype, s.stride), l);
+    const PixelView* sv[1] = {&s};
+    const AlphaSrc* av[1] = {&a};
+    const PlanarView* dv[1] = {&d};
+    const BytePlane* dav[1] = {&da};
+    return reduce0_launch(1, sv, av, dv, dav, frac, wrap, st);
+}
+
+cudaError_t launch_reduce0_alpha2(const PixelView& s0, const AlphaSrc& a0, const PlanarView& d0, const BytePlane& da0,
+                                  const PixelView& s1, const AlphaSrc& a1, const PlanarView& d1, const BytePlane& da1,
+                                  int frac, int wrap, cudaStream_t st)
+{
+    const bool same = s0.w == s1.w && s0.h == s1.h && s0.dtype == s1.dtype && s0.C == s1.C &&
+                      s0.stride == s1.stride && a0.mode == a1.mode && a0.lo == a1.lo && a0.hi == a1.hi &&
+                      d0.w == d1.w && d0.h == d1.h && d0.dtype == d1.dtype && d0.C == d1.C;
+    if (!same) {
+        const cudaError_t e = launch_reduce0_alpha(s0, a0, frac, d0, da0, wrap, st);
+        return e != cudaSuccess ? e : launch_reduce0_alpha(s1, a1, frac, d1, da1, wrap, st);
+    }
+    const PixelView* sv[2] = {&s0, &s1};
+    const AlphaSrc* av[2] = {&a0, &a1};
+    const PlanarView* dv[2] = {&d0, &d1};
+    const BytePlane* dav[2] = {&da0, &da1};
+    return reduce0_launch(2, sv, av, dv, dav, frac, wrap, st);
 }
 
 cudaError_t launch_reduce0_bytes(const BytePlane& s, int frac, const PlanarView& d, int wrap, cudaStream_t st)

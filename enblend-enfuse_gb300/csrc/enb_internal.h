@@ -108,6 +108,12 @@ cudaError_t launch_float_to_fixed(const FloatPlane& src, const PlanarView& dst, 
 cudaError_t launch_alpha_extract(const AlphaSrc& a, const BytePlane& dst, cudaStream_t st);
 cudaError_t launch_reduce(int wrap, const PlanarView& src, const BytePlane* src_alpha,
                           const PlanarView& dst, const BytePlane* dst_alpha, cudaStream_t st);
+// The same reduce of two levels of equal geometry and type (the white and
+// black pyramids of one level) as one launch; falls back to two launches when
+// the geometries differ.
+cudaError_t launch_reduce2(int wrap, const PlanarView& s0, const BytePlane* sa0, const PlanarView& d0,
+                           const BytePlane* da0, const PlanarView& s1, const BytePlane* sa1, const PlanarView& d1,
+                           const BytePlane* da1, cudaStream_t st);
 cudaError_t launch_expand(int add, int wrap, const PlanarView& src, const PlanarView& dst,
                           cudaStream_t st);
 cudaError_t launch_blend(const PlanarView& mask, const PlanarView& white, const PlanarView& black,
@@ -133,6 +139,11 @@ cudaError_t launch_alpha_component(const BytePlane& alpha, void* dst, int64_t ds
 // fused enblend passes (enb_fused.cu)
 cudaError_t launch_reduce0_alpha(const PixelView& src, const AlphaSrc& a, int frac, const PlanarView& dst,
                                  const BytePlane& dst_alpha, int wrap, cudaStream_t st);
+// Level-0 reduce of the white and black images in one launch (two launches
+// when their formats, alpha sources or geometries differ).
+cudaError_t launch_reduce0_alpha2(const PixelView& s0, const AlphaSrc& a0, const PlanarView& d0, const BytePlane& da0,
+                                  const PixelView& s1, const AlphaSrc& a1, const PlanarView& d1, const BytePlane& da1,
+                                  int frac, int wrap, cudaStream_t st);
 cudaError_t launch_reduce0_bytes(const BytePlane& src, int frac, const PlanarView& dst, int wrap, cudaStream_t st);
 cudaError_t launch_blend_into(const PlanarView& mask, const PlanarView& gw, const PlanarView& gb,
                               const PlanarView& r, int32_t white_value, cudaStream_t st);

@@ -235,9 +235,8 @@ __global__ void __launch_bounds__(256) k_expand(const T* __restrict__ src, int64
 // Merge operators
 // ---------------------------------------------------------------------------
 
-// CartesianBlendFunctor (src/blend.h:41-76).  mask >= white_value and
-// mask <= 0 are the coefficient tests 1.0 / 0.0 decided exactly on integers;
-// the mixed case is the reference's double expression.
+// CartesianBlendFunctor (src/blend.h:41-76) in place on the black level,
+// evaluated by blend_sample (exact integer rounding, double only at ties).
 template <typename T, typename TM, int C>
 __global__ void __launch_bounds__(256) k_blend(const TM* __restrict__ mask, int64_t mpitch,
                                                const T* __restrict__ white, int64_t wpitch, int64_t wplane,
@@ -260,14 +259,11 @@ __global__ void __launch_bounds__(256) k_blend(const TM* __restrict__ mask, int6
         }
         return;
     }
-    const double wc = __ddiv_rn((double)m, (double)white_value);
-    const double bc = __dadd_rn(1.0, -wc);
 #pragma unroll
     for (int c = 0; c < C; ++c) {
         T* b = &black[(int64_t)c * bplane + (int64_t)y * bpitch + x];
-        const double v = __dadd_rn(__dmul_rn(wc, (double)white[(int64_t)c * wplane + (int64_t)y * wpitch + x]),
-                                   __dmul_rn(bc, (double)*b));
-        *b = frp_store<T>(v);
+        *b = (T)blend_sample<T>(m, white_value, (int32_t)white[(int64_t)c * wplane + (int64_t)y * wpitch + x],
+                                (int32_t)*b);
     }
 }
 
@@ -800,44 +796,79 @@ cudaError_t launch_alpha_extract(const AlphaSrc& a, const BytePlane& d, cudaStre
 }
 
 template <typename TS, typename TD, int C>
-static void reduce_dispatch(int wrap, const PlanarView& s, const BytePlane* sa, const PlanarView& d,
-                            const BytePlane* da, cudaStream_t st)
+static void reduce_dispatch(int wrap, int n, const PlanarView* const* s, const BytePlane* const* sa,
+                            const PlanarView* const* d, const BytePlane* const* da, cudaStream_t st)
 {
-    const PlanarSource<TS, C> src{(const TS*)s.p, s.pitch, s.plane, sa ? sa->p : nullptr, sa ? sa->pitch : 0};
-    if (sa) {
-        launch_reduce_tiles<PlanarSource<TS, C>, TD, C, true>(src, s.w, s.h, (TD*)d.p, d.pitch, d.plane, d.w, d.h, da->p,
-                                                             da->pitch, wrap, st);
-    } else {
-        launch_reduce_tiles<PlanarSource<TS, C>, TD, C, false>(src, s.w, s.h, (TD*)d.p, d.pitch, d.plane, d.w, d.h,
-                                                              nullptr, 0, wrap, st);
+    using Src = PlanarSource<TS, C>;
+    ReduceJobs<Src, TD> jobs{};
+    for (int i = 0; i < 2; ++i) {
+        const int k = i < n ? i : 0;
+        jobs.j[i] = ReduceJob<Src, TD>{Src{(const TS*)s[k]->p, s[k]->pitch, s[k]->plane, sa[k] ? sa[k]->p : nullptr,
+                                           sa[k] ? sa[k]->pitch : 0},
+                                       (TD*)d[k]->p, d[k]->pitch, d[k]->plane, da[k] ? da[k]->p : nullptr,
+                                       da[k] ? da[k]->pitch : 0};
     }
+    if (sa[0]) {
+        launch_reduce_jobs<Src, TD, C, true>(jobs, n, s[0]->w, s[0]->h, d[0]->w, d[0]->h, wrap, st);
+    } else {
+        launch_reduce_jobs<Src, TD, C, false>(jobs, n, s[0]->w, s[0]->h, d[0]->w, d[0]->h, wrap, st);
+    }
+}
+
+static cudaError_t reduce_jobs(int wrap, int n, const PlanarView* const* s, const BytePlane* const* sa,
+                               const PlanarView* const* d, const BytePlane* const* da, cudaStream_t st)
+{
+    double bytes = 0.0;
+    for (int i = 0; i < n; ++i) {
+        if (s[i]->dtype != d[i]->dtype || s[i]->C != d[i]->C || (sa[i] == nullptr) != (da[i] == nullptr)) {
+            return cudaErrorInvalidValue;
+        }
+        bytes += planar_bytes(*s[i]) + planar_bytes(*d[i]) +
+                 (sa[i] ? npix(s[i]->w, s[i]->h) + npix(d[i]->w, d[i]->h) : 0.0);
+    }
+    note(sa[0] ? "reduce_alpha" : "reduce", bytes);
+    if (s[0]->dtype == ENB_I16) {
+        if (s[0]->C == 1) {
+            reduce_dispatch<int16_t, int16_t, 1>(wrap, n, s, sa, d, da, st);
+        } else {
+            reduce_dispatch<int16_t, int16_t, 3>(wrap, n, s, sa, d, da, st);
+        }
+    } else {
+        if (s[0]->C == 1) {
+            reduce_dispatch<int32_t, int32_t, 1>(wrap, n, s, sa, d, da, st);
+        } else {
+            reduce_dispatch<int32_t, int32_t, 3>(wrap, n, s, sa, d, da, st);
+        }
+    }
+    return cudaGetLastError();
 }
 
 cudaError_t launch_reduce(int wrap, const PlanarView& s, const BytePlane* sa, const PlanarView& d,
                           const BytePlane* da, cudaStream_t st)
 {
-    if (s.dtype != d.dtype || s.C != d.C) {
-        return cudaErrorInvalidValue;
+    const PlanarView* sv[1] = {&s};
+    const PlanarView* dv[1] = {&d};
+    const BytePlane* sav[1] = {sa};
+    const BytePlane* dav[1] = {da};
+    return reduce_jobs(wrap, 1, sv, sav, dv, dav, st);
+}
+
+cudaError_t launch_reduce2(int wrap, const PlanarView& s0, const BytePlane* sa0, const PlanarView& d0,
+                           const BytePlane* da0, const PlanarView& s1, const BytePlane* sa1, const PlanarView& d1,
+                           const BytePlane* da1, cudaStream_t st)
+{
+    const bool same = s0.w == s1.w && s0.h == s1.h && d0.w == d1.w && d0.h == d1.h && s0.dtype == s1.dtype &&
+                      s0.C == s1.C && d0.dtype == d1.dtype && d0.C == d1.C && (sa0 == nullptr) == (sa1 == nullptr) &&
+                      (da0 == nullptr) == (da1 == nullptr);
+    if (!same) {
+        const cudaError_t e = launch_reduce(wrap, s0, sa0, d0, da0, st);
+        return e != cudaSuccess ? e : launch_reduce(wrap, s1, sa1, d1, da1, st);
     }
-    if (sa) {
-        note("reduce_alpha", planar_bytes(s) + npix(s.w, s.h) + planar_bytes(d) + npix(d.w, d.h));
-    } else {
-        note("reduce", planar_bytes(s) + planar_bytes(d));
-    }
-    if (s.dtype == ENB_I16) {
-        if (s.C == 1) {
-            reduce_dispatch<int16_t, int16_t, 1>(wrap, s, sa, d, da, st);
-        } else {
-            reduce_dispatch<int16_t, int16_t, 3>(wrap, s, sa, d, da, st);
-        }
-    } else {
-        if (s.C == 1) {
-            reduce_dispatch<int32_t, int32_t, 1>(wrap, s, sa, d, da, st);
-        } else {
-            reduce_dispatch<int32_t, int32_t, 3>(wrap, s, sa, d, da, st);
-        }
-    }
-    return cudaGetLastError();
+    const PlanarView* sv[2] = {&s0, &s1};
+    const PlanarView* dv[2] = {&d0, &d1};
+    const BytePlane* sav[2] = {sa0, sa1};
+    const BytePlane* dav[2] = {da0, da1};
+    return reduce_jobs(wrap, 2, sv, sav, dv, dav, st);
 }
 
 template <typename T, int C>

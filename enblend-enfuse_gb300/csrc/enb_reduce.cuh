@@ -1,31 +1,41 @@
 // enb_reduce.cuh -- the Burt-Adelson reduce (src/pyramid.h:166-848) as one
 // tiled kernel over pluggable sources.
 //
-// One CTA of 256 threads computes a 32x16 tile of destination pixels from the
-// 67x35 source window around it (2 pixels of halo).  All global loads of the
-// window are issued up front (unrolled, independent of the alpha test) so
-// that each thread keeps ~10 loads in flight.  Tiles whose window lies inside
-// the image (almost all) take a path without bounds, clamp or wrap logic.  The
-// window is then filtered with the separable [1 4 6 4 1] kernel in shared
-// memory, first along x at the even source columns (consecutive threads take
-// consecutive rows, so the odd 67-word row stride spreads them over all
-// banks), then along y.  Integer sums are exact, so the order of the taps does
-// not matter.
+// A CTA computes a 64x16 tile of destination pixels from the 131x35 source
+// window around it (2 pixels of halo), in two phases:
+//   1. column sums: 262 threads each take one source column and 8
+//      destination rows, load the column's 19 source rows into registers (all
+//      loads issued before any arithmetic, so that a thread keeps ~19 loads in
+//      flight) and form the vertical [1 4 6 4 1] sums at the even rows;
+//   2. row sums: 256 threads each take 4 adjacent destination pixels of one
+//      row, read the 11 column sums they need with three 16-byte shared loads
+//      per channel and form the horizontal [1 4 6 4 1] sums.
+// The weights are separable and the sums exact integers, so the order of the
+// taps does not change the result.
 //   with alpha: normalised convolution over the opaque taps, taps outside the
 //               image dropped, x periodic when wrap (pyramid.h:166-573);
 //   no alpha:   clamp-to-edge replication in y (and x unless wrap), /256
 //               (pyramid.h:601-848).
+// blockIdx.z selects one of up to two jobs of the same geometry (the white and
+// black pyramids of a level), so a level of both images is one launch.
 #pragma once
 
 #include "enb_device.cuh"
 
 namespace enb {
 
-constexpr int R2W = 32, R2H = 16;                      // destination tile
-constexpr int R2IW = 2 * R2W + 3, R2IH = 2 * R2H + 3;  // 67 x 35 source window
-constexpr int R2N = R2IW * R2IH;
-constexpr int R2ITER = (R2N + 255) / 256;
-constexpr int R2HP = R2W + 1;                          // padded row of the x-filtered window
+constexpr int RDW = 64, RDH = 16;        // destination tile
+constexpr int RSW = 2 * RDW + 3;         // 131 source columns
+constexpr int RSH = 2 * RDH + 3;         // 35 source rows
+constexpr int RGR = 8;                   // destination rows of a column item
+constexpr int RGN = 2 * RGR + 3;         // 19 source rows of a column item
+constexpr int RITEMS = RSW * (RDH / RGR);  // 262 column items
+constexpr int RTHREADS = 288;
+constexpr int RVP = 148;                 // padded row of column sums
+
+// Column c of a row of column sums sits at c + 4*(c/32): the 16-byte reads of
+// phase 2 (8 threads at a stride of 8 words) then hit 32 distinct banks.
+__device__ __forceinline__ int rphys(int c) { return c + ((c >> 5) << 2); }
 
 // Planar pyramid level (+ optional 8-bit alpha plane).
 template <typename TS, int C>
@@ -39,9 +49,9 @@ struct PlanarSource {
         const int64_t o = (int64_t)gy * pitch + gx;
 #pragma unroll
         for (int c = 0; c < C; ++c) {
-            v[c] = (int32_t)p[c * plane + o];
+            v[c] = (int32_t)__ldg(&p[c * plane + o]);
         }
-        al = a ? (a[(int64_t)gy * apitch + gx] != 0) : 1;
+        al = a ? (__ldg(&a[(int64_t)gy * apitch + gx]) != 0) : 1;
     }
 };
 
@@ -52,144 +62,206 @@ struct ByteSource {
     int frac;
     __device__ __forceinline__ void load(int gy, int gx, int32_t (&v)[1], int& al) const
     {
-        v[0] = (int32_t)p[(int64_t)gy * pitch + gx] << frac;
+        v[0] = (int32_t)__ldg(&p[(int64_t)gy * pitch + gx]) << frac;
         al = 1;
     }
 };
 
-template <class Src, int C, bool ALPHA>
-__device__ __forceinline__ void reduce_stage(const Src& src, int gy, int gx, int r, int c, int32_t (*sv)[R2IH][R2IW],
-                                             uint8_t (*sa)[R2IW + 1])
+template <class Src, typename TD>
+struct ReduceJob {
+    Src src;
+    TD* dst;
+    int64_t dpitch, dplane;  // elements
+    uint8_t* da;             // destination alpha (with alpha) or null
+    int64_t dapitch;
+};
+
+template <class Src, typename TD>
+struct ReduceJobs {
+    ReduceJob<Src, TD> j[2];
+};
+
+// Phase 1 for one column item: vertical sums of destination rows r0..r0+7.
+template <class Src, int C, bool ALPHA, bool INTERIOR>
+__device__ __forceinline__ void reduce_column(const Src& src, int gx, int gyb, int sw, int sh, int wrap,
+                                              int32_t (*V)[RDH][RVP], int col, int r0)
 {
-    int32_t v[C];
-    int al = 1;
-    src.load(gy, gx, v, al);
-#pragma unroll
-    for (int ch = 0; ch < C; ++ch) {
-        sv[ch][r][c] = (ALPHA && !al) ? 0 : v[ch];
+    constexpr int NV = C + (ALPHA ? 1 : 0);
+    bool colok = true;
+    if (!INTERIOR) {
+        if (wrap) {
+            gx = imod(gx, sw);
+        } else if (ALPHA) {
+            colok = gx >= 0 && gx < sw;
+        } else {
+            gx = min(max(gx, 0), sw - 1);
+        }
     }
-    if (ALPHA) {
-        sa[r][c] = (uint8_t)al;
+    int32_t x[RGN][NV];
+#pragma unroll
+    for (int k = 0; k < RGN; ++k) {
+        int gy = gyb + k;
+        bool ok = true;
+        if (!INTERIOR) {
+            if (ALPHA) {
+                ok = colok && gy >= 0 && gy < sh;
+            } else {
+                gy = min(max(gy, 0), sh - 1);
+            }
+        }
+        int32_t v[C];
+        int al = 0;
+        if (ok) {
+            src.load(gy, gx, v, al);
+        } else {
+#pragma unroll
+            for (int ch = 0; ch < C; ++ch) {
+                v[ch] = 0;
+            }
+        }
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) {
+            x[k][ch] = (ALPHA && !al) ? 0 : v[ch];
+        }
+        if (ALPHA) {
+            x[k][NV - 1] = al;
+        }
+    }
+    const int pc = rphys(col);
+#pragma unroll
+    for (int r = 0; r < RGR; ++r) {
+#pragma unroll
+        for (int ch = 0; ch < NV; ++ch) {
+            V[ch][r0 + r][pc] =
+                x[2 * r][ch] + 4 * x[2 * r + 1][ch] + 6 * x[2 * r + 2][ch] + 4 * x[2 * r + 3][ch] + x[2 * r + 4][ch];
+        }
+    }
+}
+
+template <typename TD>
+__device__ __forceinline__ void store4(TD* p, const int32_t (&v)[4], int n)
+{
+    if (n == 4 && ((uintptr_t)p & (4 * sizeof(TD) - 1)) == 0) {
+        if (sizeof(TD) == 4) {
+            *reinterpret_cast<int4*>(p) = make_int4(v[0], v[1], v[2], v[3]);
+        } else {
+            *reinterpret_cast<uint2*>(p) = make_uint2((uint32_t)(uint16_t)v[0] | ((uint32_t)(uint16_t)v[1] << 16),
+                                                      (uint32_t)(uint16_t)v[2] | ((uint32_t)(uint16_t)v[3] << 16));
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (q < n) {
+                p[q] = cast_store<TD>(v[q]);
+            }
+        }
     }
 }
 
 template <class Src, typename TD, int C, bool ALPHA>
-__global__ void __launch_bounds__(256) k_reduce_tiles(Src src, int sw, int sh, TD* __restrict__ dst, int64_t dpitch,
-                                                      int64_t dplane, int dw, int dh, uint8_t* __restrict__ da,
-                                                      int64_t dapitch, int wrap)
+__global__ void __launch_bounds__(RTHREADS, 2) k_reduce(ReduceJobs<Src, TD> jobs, int sw, int sh, int dw, int dh,
+                                                        int wrap)
 {
-    __shared__ int32_t sv[C][R2IH][R2IW];
-    __shared__ uint8_t sa[ALPHA ? R2IH : 1][R2IW + 1];
-    __shared__ int32_t hv[C][R2IH][R2HP];
-    __shared__ uint8_t ha[ALPHA ? R2IH : 1][R2HP];
+    constexpr int NV = C + (ALPHA ? 1 : 0);
+    __shared__ __align__(16) int32_t V[NV][RDH][RVP];
 
-    const int X0 = blockIdx.x * R2W, Y0 = blockIdx.y * R2H;
+    const ReduceJob<Src, TD> job = blockIdx.z == 0 ? jobs.j[0] : jobs.j[1];
+    const int X0 = blockIdx.x * RDW, Y0 = blockIdx.y * RDH;
     const int gx0 = 2 * X0 - 2, gy0 = 2 * Y0 - 2;
     const int tid = threadIdx.x;
 
-    if (gx0 >= 0 && gy0 >= 0 && gx0 + R2IW <= sw && gy0 + R2IH <= sh) {
-        // interior window: thread -> column tid%64 (+64 for the last 3), rows tid/64 + 4k
-        const int c = tid & 63, rg = tid >> 6;
+    if (tid < RITEMS) {
+        const int g = tid >= RSW ? 1 : 0;
+        const int col = tid - g * RSW;
+        const int gyb = gy0 + 2 * RGR * g;
+        if (gx0 >= 0 && gy0 >= 0 && gx0 + RSW <= sw && gy0 + RSH <= sh) {
+            reduce_column<Src, C, ALPHA, true>(job.src, gx0 + col, gyb, sw, sh, wrap, V, col, RGR * g);
+        } else {
+            reduce_column<Src, C, ALPHA, false>(job.src, gx0 + col, gyb, sw, sh, wrap, V, col, RGR * g);
+        }
+    }
+    __syncthreads();
+    if (tid >= RDH * (RDW / 4)) {
+        return;
+    }
+
+    const int r = tid >> 4, k = tid & 15;
+    const int Y = Y0 + r, Xb = X0 + 4 * k;
+    if (Y >= dh || Xb >= dw) {
+        return;
+    }
+    const int n = min(4, dw - Xb);
+    int32_t s[NV][4];
 #pragma unroll
-        for (int k = 0; k < (R2IH + 3) / 4; ++k) {
-            const int r = rg + 4 * k;
-            if (r < R2IH) {
-                reduce_stage<Src, C, ALPHA>(src, gy0 + r, gx0 + c, r, c, sv, sa);
-                if (c < R2IW - 64) {
-                    reduce_stage<Src, C, ALPHA>(src, gy0 + r, gx0 + 64 + c, r, 64 + c, sv, sa);
+    for (int ch = 0; ch < NV; ++ch) {
+        const int32_t* row = &V[ch][r][0];
+        const int4 a = *reinterpret_cast<const int4*>(row + rphys(8 * k));
+        const int4 b = *reinterpret_cast<const int4*>(row + rphys(8 * k + 4));
+        const int4 c = *reinterpret_cast<const int4*>(row + rphys(8 * k + 8));
+        const int32_t v[11] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            s[ch][q] = v[2 * q] + 4 * v[2 * q + 1] + 6 * v[2 * q + 2] + 4 * v[2 * q + 3] + v[2 * q + 4];
+        }
+    }
+    const int64_t o = (int64_t)Y * job.dpitch + Xb;
+    if (ALPHA) {
+        int32_t out[C][4];
+        uint32_t abits = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int32_t den = s[NV - 1][q];
+#pragma unroll
+            for (int ch = 0; ch < C; ++ch) {
+                out[ch][q] = den <= 0 ? 0 : (den == 256 ? s[ch][q] / 256 : div_any(s[ch][q], den));
+            }
+            abits |= (den > 0 ? 255u : 0u) << (8 * q);
+        }
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) {
+            store4<TD>(job.dst + ch * job.dplane + o, out[ch], n);
+        }
+        uint8_t* ap = job.da + (int64_t)Y * job.dapitch + Xb;
+        if (n == 4 && ((uintptr_t)ap & 3) == 0) {
+            *reinterpret_cast<uint32_t*>(ap) = abits;
+        } else {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (q < n) {
+                    ap[q] = (uint8_t)(abits >> (8 * q));
                 }
             }
         }
     } else {
 #pragma unroll
-        for (int it = 0; it < R2ITER; ++it) {
-            const int i = tid + it * 256;
-            if (i < R2N) {
-                const int r = i / R2IW, c = i - r * R2IW;
-                int gy = gy0 + r, gx = gx0 + c;
-                if (ALPHA) {
-                    if (wrap) {
-                        gx = imod(gx, sw);
-                    }
-                    if (gy >= 0 && gy < sh && gx >= 0 && gx < sw) {
-                        reduce_stage<Src, C, ALPHA>(src, gy, gx, r, c, sv, sa);
-                    } else {
-#pragma unroll
-                        for (int ch = 0; ch < C; ++ch) {
-                            sv[ch][r][c] = 0;
-                        }
-                        sa[r][c] = 0;
-                    }
-                } else {
-                    gy = min(max(gy, 0), sh - 1);
-                    gx = wrap ? imod(gx, sw) : min(max(gx, 0), sw - 1);
-                    reduce_stage<Src, C, ALPHA>(src, gy, gx, r, c, sv, sa);
-                }
-            }
-        }
-    }
-    __syncthreads();
-
-    // x pass at the even source columns; consecutive threads take consecutive rows
-    for (int i = tid; i < R2IH * R2W; i += 256) {
-        const int j = i / R2IH, r = i - j * R2IH;
-        const int c0 = 2 * j;
-        if (ALPHA) {
-            ha[r][j] = (uint8_t)(sa[r][c0] + 4 * sa[r][c0 + 1] + 6 * sa[r][c0 + 2] + 4 * sa[r][c0 + 3] + sa[r][c0 + 4]);
-        }
-#pragma unroll
         for (int ch = 0; ch < C; ++ch) {
-            const int32_t* s = &sv[ch][r][c0];
-            hv[ch][r][j] = s[0] + 4 * s[1] + 6 * s[2] + 4 * s[3] + s[4];
+            int32_t out[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                out[q] = s[ch][q] / 256;
+            }
+            store4<TD>(job.dst + ch * job.dplane + o, out, n);
         }
     }
-    __syncthreads();
+}
 
-    // y pass: two destination rows per thread
-    const int tx = tid % R2W;
-#pragma unroll
-    for (int half = 0; half < 2; ++half) {
-        const int ty = tid / R2W + 8 * half;
-        const int X = X0 + tx, Y = Y0 + ty;
-        if (X >= dw || Y >= dh) {
-            continue;
-        }
-        const int r0 = 2 * ty;
-        const int64_t o = (int64_t)Y * dpitch + X;
-        if (ALPHA) {
-            const int den = ha[r0][tx] + 4 * ha[r0 + 1][tx] + 6 * ha[r0 + 2][tx] + 4 * ha[r0 + 3][tx] + ha[r0 + 4][tx];
-            if (den > 0) {
-#pragma unroll
-                for (int ch = 0; ch < C; ++ch) {
-                    const int32_t num = hv[ch][r0][tx] + 4 * hv[ch][r0 + 1][tx] + 6 * hv[ch][r0 + 2][tx] +
-                                        4 * hv[ch][r0 + 3][tx] + hv[ch][r0 + 4][tx];
-                    dst[ch * dplane + o] = cast_store<TD>(den == 256 ? num / 256 : div_any(num, den));
-                }
-                da[(int64_t)Y * dapitch + X] = 255;
-            } else {
-#pragma unroll
-                for (int ch = 0; ch < C; ++ch) {
-                    dst[ch * dplane + o] = (TD)0;
-                }
-                da[(int64_t)Y * dapitch + X] = 0;
-            }
-        } else {
-#pragma unroll
-            for (int ch = 0; ch < C; ++ch) {
-                const int32_t num = hv[ch][r0][tx] + 4 * hv[ch][r0 + 1][tx] + 6 * hv[ch][r0 + 2][tx] +
-                                    4 * hv[ch][r0 + 3][tx] + hv[ch][r0 + 4][tx];
-                dst[ch * dplane + o] = cast_store<TD>(num / 256);
-            }
-        }
-    }
+// One launch over njobs (1 or 2) jobs of the same geometry.
+template <class Src, typename TD, int C, bool ALPHA>
+inline void launch_reduce_jobs(const ReduceJobs<Src, TD>& jobs, int njobs, int sw, int sh, int dw, int dh, int wrap,
+                               cudaStream_t st)
+{
+    const dim3 g((unsigned)((dw + RDW - 1) / RDW), (unsigned)((dh + RDH - 1) / RDH), (unsigned)njobs);
+    k_reduce<Src, TD, C, ALPHA><<<g, RTHREADS, 0, st>>>(jobs, sw, sh, dw, dh, wrap);
 }
 
 template <class Src, typename TD, int C, bool ALPHA>
 inline void launch_reduce_tiles(const Src& src, int sw, int sh, TD* dst, int64_t dpitch, int64_t dplane, int dw,
                                 int dh, uint8_t* da, int64_t dapitch, int wrap, cudaStream_t st)
 {
-    const dim3 g((unsigned)((dw + R2W - 1) / R2W), (unsigned)((dh + R2H - 1) / R2H));
-    k_reduce_tiles<Src, TD, C, ALPHA><<<g, 256, 0, st>>>(src, sw, sh, dst, dpitch, dplane, dw, dh, da, dapitch, wrap);
+    ReduceJobs<Src, TD> jobs{};
+    jobs.j[0] = ReduceJob<Src, TD>{src, dst, dpitch, dplane, da, dapitch};
+    jobs.j[1] = jobs.j[0];
+    launch_reduce_jobs<Src, TD, C, ALPHA>(jobs, 1, sw, sh, dw, dh, wrap, st);
 }
 
 }  // namespace enb
