@@ -722,17 +722,51 @@ enb_status enblend_fused(enb_ctx* ctx, const enb_image* white, const enb_image* 
         ENB_LAUNCH(ctx, launch_reduce0_bytes(byte_plane(mask), mf, level_view(mg.p, 0), wrap, ctx->stream));
         for (int j = 1; j < NL; ++j) {
             ENB_CHECK(ctx, gw.p->w[j - 1] > 1 && gw.p->h[j - 1] > 1, "reduce: src image too small in reduce");
+        }
+        // Levels first..NL-1 (all at most coarse_pixels pixels) go to the one
+        // coarse launch, which also blends the top and collapses down to first.
+        const int64_t cpx = o.coarse_pixels == 0 ? kCoarsePixels : (int64_t)o.coarse_pixels;
+        int first = NL;
+        if (cpx > 0) {
+            for (int j = 1; j < NL; ++j) {
+                if ((int64_t)gw.p->w[j] * gw.p->h[j] <= cpx) {
+                    first = j;
+                    break;
+                }
+            }
+        }
+        for (int j = 1; j < first; ++j) {
             const BytePlane sa = awc.level(j - 1), da = awc.level(j), sb = abc.level(j - 1), db = abc.level(j);
             ENB_LAUNCH(ctx, launch_reduce2(wrap, level_view(gw.p, j - 1), &sa, level_view(gw.p, j), &da,
                                            level_view(gb.p, j - 1), &sb, level_view(gb.p, j), &db, ctx->stream));
             ENB_LAUNCH(ctx, launch_reduce(wrap, level_view(mg.p, j - 1), nullptr, level_view(mg.p, j), nullptr,
                                           ctx->stream));
         }
-        // Up sweep: top level blend, then Laplacian + blend + collapse per level
-        // (src/blend.h:81-121, src/pyramid.h:1758-1784).
-        ENB_LAUNCH(ctx, launch_blend_into(level_view(mg.p, NL - 1), level_view(gw.p, NL - 1), level_view(gb.p, NL - 1),
-                                          level_view(rr.p, NL - 1), white_value, ctx->stream));
-        for (int j = NL - 2; j >= 0; --j) {
+        int up_from = NL - 2;
+        if (first < NL) {
+            CoarseHost ch{};
+            ch.n = NL - first + 1;
+            for (int s = 0; s < ch.n; ++s) {
+                const int j = first - 1 + s;
+                ch.gw[s] = level_view(gw.p, j);
+                ch.gb[s] = level_view(gb.p, j);
+                ch.rr[s] = level_view(rr.p, j);
+                ch.mg[s] = level_view(mg.p, j);
+                ch.aw[s] = awc.level(j);
+                ch.ab[s] = abc.level(j);
+            }
+            ch.white_value = white_value;
+            ch.wrap = wrap;
+            ENB_LAUNCH(ctx, launch_coarse(ch, ctx->stream));
+            up_from = first - 1;
+        } else {
+            // Up sweep: top level blend, then Laplacian + blend + collapse per
+            // level (src/blend.h:81-121, src/pyramid.h:1758-1784).
+            ENB_LAUNCH(ctx, launch_blend_into(level_view(mg.p, NL - 1), level_view(gw.p, NL - 1),
+                                              level_view(gb.p, NL - 1), level_view(rr.p, NL - 1), white_value,
+                                              ctx->stream));
+        }
+        for (int j = up_from; j >= 0; --j) {
             ENB_LAUNCH(ctx, launch_up_level(level_view(gw.p, j + 1), level_view(gb.p, j + 1), level_view(rr.p, j + 1),
                                             level_view(mg.p, j), level_view(gw.p, j), level_view(gb.p, j),
                                             level_view(rr.p, j), white_value, wrap, ctx->stream));

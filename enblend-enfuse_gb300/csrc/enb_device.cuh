@@ -205,24 +205,18 @@ __device__ __forceinline__ uint32_t dither_sample_bits(uint32_t key, uint32_t pi
 }
 
 // The conversion rule of SpecializedConvertPyramidToScalarFunctor
-// (src/fixmath.h:251-277): q = v >> F, fraction f; f < 1/4 -> q,
-// f >= 3/4 -> q+1, in between q+1 iff (random & (2^(F-1)-1)) + 1/4 <= f;
-// then fromPromote into [0, maxv].  `bits` is consumed only in the band.
+// (src/fixmath.h:251-277): q = v >> F, fraction f, Q = 2^(F-2); f < Q -> q,
+// f >= 3Q -> q+1, in between q+1 iff (random & (2Q-1)) + Q <= f; then
+// fromPromote into [0, maxv].  With t = (random & (2Q-1)) + Q, which lies in
+// [Q, 3Q-1], all three cases are "q+1 iff f >= t", i.e. (v + 4Q - t) >> F;
+// round-to-nearest is t = 2Q.  v is capped below 2^31 - 4Q first (F <= 15 and
+// maxv <= 65535 keep the result at maxv there).
 __device__ __forceinline__ int32_t dither_rule(int32_t v, int frac, int nearest, uint32_t bits, int32_t maxv)
 {
-    const int32_t q = v >> frac;
-    const int32_t f = v & ((1 << frac) - 1);
-    const int32_t quarter = 1 << (frac - 2);
-    int32_t r;
-    if (nearest) {
-        r = f >= (1 << (frac - 1)) ? q + 1 : q;
-    } else if (f >= quarter && f < 3 * quarter) {
-        const int32_t rnd = (int32_t)(bits & (uint32_t)((1 << (frac - 1)) - 1)) + quarter;
-        r = rnd <= f ? q + 1 : q;
-    } else {
-        r = f >= quarter ? q + 1 : q;
-    }
-    return min(max(r, 0), maxv);
+    const int32_t Q = 1 << (frac - 2);
+    const int32_t t = nearest ? 2 * Q : (int32_t)(bits & (uint32_t)(2 * Q - 1)) + Q;
+    const int32_t vc = min(v, INT32_MAX - 4 * Q);
+    return min(max((vc + 4 * Q - t) >> frac, 0), maxv);
 }
 
 // CartesianBlendFunctor of one sample (src/blend.h:41-76) in integers.

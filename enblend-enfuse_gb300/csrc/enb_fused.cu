@@ -176,35 +176,13 @@ __device__ __forceinline__ void stage_coarse(int32_t (*ss)[ESH][ESW], const Coar
                 i = imod(i, cl.w);
             }
             const bool in = j >= 0 && j < cl.h && i >= 0 && i < cl.w;
-            const int64_t o = (int64_t)j * cl.pitch + i;
+            // clamped position: the loads are unconditional, the taps outside
+            // the level are zeroed afterwards
+            const int64_t o = (int64_t)min(max(j, 0), cl.h - 1) * cl.pitch + min(max(i, 0), cl.w - 1);
 #pragma unroll
             for (int p = 0; p < NP; ++p) {
-                ss[p][r][c] = in ? (int32_t) reinterpret_cast<const T*>(cl.p[p])[o] : 0;
-            }
-        }
-    }
-}
-
-// Staging when the whole 34x10 neighbourhood lies inside the coarse level.
-template <int NP, typename T>
-__device__ __forceinline__ void stage_coarse_interior(int32_t (*ss)[ESH][ESW], const CoarseLevels& cl, int I0, int J0)
-{
-    constexpr int N = ESH * ESW;
-    constexpr int IT = (N + 255) / 256;
-    const T* base[NP];
-#pragma unroll
-    for (int p = 0; p < NP; ++p) {
-        base[p] = reinterpret_cast<const T*>(cl.p[p]) + (int64_t)(J0 - 1) * cl.pitch + (I0 - 1);
-    }
-#pragma unroll
-    for (int it = 0; it < IT; ++it) {
-        const int k = threadIdx.x + it * 256;
-        if (k < N) {
-            const int r = k / ESW, c = k - r * ESW;
-            const int o = r * (int)cl.pitch + c;
-#pragma unroll
-            for (int p = 0; p < NP; ++p) {
-                ss[p][r][c] = (int32_t)base[p][o];
+                const int32_t v = (int32_t)__ldg(&reinterpret_cast<const T*>(cl.p[p])[o]);
+                ss[p][r][c] = in ? v : 0;
             }
         }
     }
@@ -236,19 +214,46 @@ __device__ __forceinline__ void expand_quad(const int32_t (*s)[ESW], int qx, int
     }
 }
 
-// Expansion of an interior quad (all taps inside the level).  The (4,4) taps
-// enter without their common factor 4, which is folded into the divisors:
-// trunc(4n/64) = trunc(n/16) and trunc(4n/16) = trunc(n/4).  NONNEG: the
-// source is a Gaussian level of an unsigned image (all values >= 0), so the
-// truncating divisions are shifts.
-template <bool NONNEG>
-__device__ __forceinline__ void expand_quad_interior(const int32_t (*s)[ESW], int qx, int qy, int32_t e[4])
+// Staging of an interior tile with the three planes of a channel packed into
+// one int4 per tap ({Gw, Gb, R, 0}): a quad's nine taps of all three planes
+// are then nine 16-byte shared loads (a warp's loads are 512 contiguous
+// bytes, four wavefronts, no bank conflicts).
+template <int C, typename T>
+__device__ __forceinline__ void stage_coarse4_interior(int4 (*s4)[ESH][ESW], const CoarseLevels& cl, int I0, int J0)
 {
-    const int32_t* a = &s[qy][qx];
-    const int32_t* b = &s[qy + 1][qx];
-    const int32_t* c = &s[qy + 2][qx];
-    const int32_t hea = a[0] + 6 * a[1] + a[2], heb = b[0] + 6 * b[1] + b[2], hec = c[0] + 6 * c[1] + c[2];
-    const int32_t hoa = a[1] + a[2], hob = b[1] + b[2], hoc = c[1] + c[2];
+    constexpr int N = ESH * ESW;
+    constexpr int IT = (N + 255) / 256;
+    const T* base[3 * C];
+#pragma unroll
+    for (int p = 0; p < 3 * C; ++p) {
+        base[p] = reinterpret_cast<const T*>(cl.p[p]) + (int64_t)(J0 - 1) * cl.pitch + (I0 - 1);
+    }
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+        const int k = threadIdx.x + it * 256;
+        if (k < N) {
+            const int r = k / ESW, c = k - r * ESW;
+            const int o = r * (int)cl.pitch + c;
+#pragma unroll
+            for (int ch = 0; ch < C; ++ch) {
+                s4[ch][r][c] = make_int4((int32_t)__ldg(&base[ch][o]), (int32_t)__ldg(&base[C + ch][o]),
+                                         (int32_t)__ldg(&base[2 * C + ch][o]), 0);
+            }
+        }
+    }
+}
+
+// Expansion of an interior quad (all taps inside the level) from its 3x3
+// source neighbourhood v.  The (4,4) taps enter without their common factor
+// 4, which is folded into the divisors: trunc(4n/64) = trunc(n/16) and
+// trunc(4n/16) = trunc(n/4).  NONNEG: the source is a Gaussian level of an
+// unsigned image (all values >= 0), so the truncating divisions are shifts.
+template <bool NONNEG>
+__device__ __forceinline__ void expand9(const int32_t (&v)[3][3], int32_t e[4])
+{
+    const int32_t hea = v[0][0] + 6 * v[0][1] + v[0][2], heb = v[1][0] + 6 * v[1][1] + v[1][2],
+                  hec = v[2][0] + 6 * v[2][1] + v[2][2];
+    const int32_t hoa = v[0][1] + v[0][2], hob = v[1][1] + v[1][2], hoc = v[2][1] + v[2][2];
     const int32_t n0 = hea + 6 * heb + hec, n1 = hoa + 6 * hob + hoc, n2 = heb + hec, n3 = hob + hoc;
     if (NONNEG) {
         e[0] = (int32_t)((uint32_t)n0 >> 6);
@@ -261,6 +266,92 @@ __device__ __forceinline__ void expand_quad_interior(const int32_t (*s)[ESW], in
         e[2] = n2 / 16;
         e[3] = n3 / 4;
     }
+}
+
+// One 16-byte shared load (all four words, so that it stays one access).
+__device__ __forceinline__ int4 lds128(const int4* p)
+{
+    int4 v;
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    asm volatile("ld.shared.v4.s32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "r"(a)
+                 : "memory");
+    return v;
+}
+
+// Expansions of one channel's planes at an interior quad from the packed
+// taps: er always, ew / eb where the quad's seam mask needs them
+// (kind 1: all white, 2: all black, 0: mixed).
+__device__ __forceinline__ void expand_packed(const int4 (*s)[ESW], int qx, int qy, int kind, int32_t ew[4],
+                                              int32_t eb[4], int32_t er[4])
+{
+    int4 t[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            t[a][b] = lds128(&s[qy + a][qx + b]);
+        }
+    }
+    int32_t v[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            v[a][b] = t[a][b].z;
+        }
+    }
+    expand9<false>(v, er);
+    if (kind != 2) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                v[a][b] = t[a][b].x;
+            }
+        }
+        expand9<true>(v, ew);
+    }
+    if (kind != 1) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                v[a][b] = t[a][b].y;
+            }
+        }
+        expand9<true>(v, eb);
+    }
+}
+
+// Collapsed value of one sample: fromPromote(blend(m, Lw, Lb) + E(R)), with
+// the blend resolved without the mask test when the whole quad is white (1)
+// or black (2).
+template <typename T>
+__device__ __forceinline__ int32_t merge_sample(int kind, int32_t m, int32_t W, int32_t fw, int32_t ew, int32_t fb,
+                                                int32_t eb, int32_t er)
+{
+    if (kind == 1) {
+        return (int32_t)sat_store<T>((int32_t)cast_store<T>((int64_t)fw - ew) + er);
+    }
+    if (kind == 2) {
+        return (int32_t)sat_store<T>((int32_t)cast_store<T>((int64_t)fb - eb) + er);
+    }
+    const int32_t lw = (int32_t)cast_store<T>((int64_t)fw - ew);
+    const int32_t lb = (int32_t)cast_store<T>((int64_t)fb - eb);
+    return (int32_t)sat_store<T>(blend_sample<T>(m, W, lw, lb) + er);
+}
+
+__device__ __forceinline__ int quad_kind(const int32_t (&m)[4], int32_t W)
+{
+    if (m[0] >= W && m[1] >= W && m[2] >= W && m[3] >= W) {
+        return 1;
+    }
+    if (m[0] <= 0 && m[1] <= 0 && m[2] <= 0 && m[3] <= 0) {
+        return 2;
+    }
+    return 0;
 }
 
 // Two horizontally adjacent samples of a planar level (even x: 4- or 8-byte aligned).
@@ -305,7 +396,9 @@ __global__ void __launch_bounds__(256) k_up_level(CoarseLevels cl, const TM* __r
                                                   T* __restrict__ r, int64_t pitch, int64_t plane, int w, int h,
                                                   int32_t white_value, int wrap)
 {
-    __shared__ int32_t ss[3 * C][ESH][ESW];
+    // packed int4 taps for interior tiles, 3C int32 planes for border tiles
+    __shared__ int4 sbuf[C][ESH][ESW];
+    int32_t (*ss)[ESH][ESW] = reinterpret_cast<int32_t (*)[ESH][ESW]>(&sbuf[0][0][0]);
     const int X0 = blockIdx.x * ETW, Y0 = blockIdx.y * ETH;
     const int I0 = X0 >> 1, J0 = Y0 >> 1;
     const int qx = threadIdx.x % 32, qy = threadIdx.x / 32;
@@ -313,8 +406,8 @@ __global__ void __launch_bounds__(256) k_up_level(CoarseLevels cl, const TM* __r
     const int X = 2 * i, Y = 2 * j;
 
     if (interior_tile(X0, Y0, w, h, I0, J0, cl.w, cl.h)) {
-        // interior tile: no bounds, paired loads and stores, interior
-        // expansions, only the expansions the quad's mask values select
+        // interior tile: no bounds, paired loads and stores, packed taps,
+        // only the expansions the quad's mask values select
         const int64_t o0 = (int64_t)Y * pitch + X;
         int32_t fw[C][4], fb[C][4], fm[4];
         ld2<TM>(mask + (int64_t)Y * mpitch + X, fm[0], fm[1]);
@@ -326,26 +419,17 @@ __global__ void __launch_bounds__(256) k_up_level(CoarseLevels cl, const TM* __r
             ld2<T>(gb + c * plane + o0, fb[c][0], fb[c][1]);
             ld2<T>(gb + c * plane + o0 + pitch, fb[c][2], fb[c][3]);
         }
-        stage_coarse_interior<3 * C, T>(ss, cl, I0, J0);
+        stage_coarse4_interior<C, T>(sbuf, cl, I0, J0);
         __syncthreads();
-        const bool need_w = fm[0] > 0 || fm[1] > 0 || fm[2] > 0 || fm[3] > 0;
-        const bool need_b = fm[0] < white_value || fm[1] < white_value || fm[2] < white_value || fm[3] < white_value;
+        const int kind = quad_kind(fm, white_value);
 #pragma unroll
         for (int c = 0; c < C; ++c) {
-            int32_t ew[4] = {0, 0, 0, 0}, eb[4] = {0, 0, 0, 0}, er[4];
-            if (need_w) {
-                expand_quad_interior<true>(ss[c], qx, qy, ew);
-            }
-            if (need_b) {
-                expand_quad_interior<true>(ss[C + c], qx, qy, eb);
-            }
-            expand_quad_interior<false>(ss[2 * C + c], qx, qy, er);
+            int32_t ew[4], eb[4], er[4];
+            expand_packed(sbuf[c], qx, qy, kind, ew, eb, er);
             T res[4];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                const int32_t lw = (int32_t)cast_store<T>((int64_t)fw[c][q] - ew[q]);
-                const int32_t lb = (int32_t)cast_store<T>((int64_t)fb[c][q] - eb[q]);
-                res[q] = sat_store<T>(blend1<T>(fm[q], white_value, lw, lb) + er[q]);
+                res[q] = (T)merge_sample<T>(kind, fm[q], white_value, fw[c][q], ew[q], fb[c][q], eb[q], er[q]);
             }
             st2<T>(r + c * plane + o0, res[0], res[1]);
             st2<T>(r + c * plane + o0 + pitch, res[2], res[3]);
@@ -353,18 +437,18 @@ __global__ void __launch_bounds__(256) k_up_level(CoarseLevels cl, const TM* __r
         return;
     }
 
-    // border tile: fine-level values of the quad, loaded before the barrier
+    // border tile: fine-level values of the quad, loaded (from clamped
+    // positions, unconditionally) before the barrier
     int32_t fw[C][4], fb[C][4], fm[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-        const int XX = X + (q & 1), YY = Y + (q >> 1);
-        const bool v = XX < w && YY < h;
+        const int XX = min(X + (q & 1), w - 1), YY = min(Y + (q >> 1), h - 1);
         const int64_t o = (int64_t)YY * pitch + XX;
-        fm[q] = v ? (int32_t)mask[(int64_t)YY * mpitch + XX] : 0;
+        fm[q] = (int32_t)__ldg(&mask[(int64_t)YY * mpitch + XX]);
 #pragma unroll
         for (int c = 0; c < C; ++c) {
-            fw[c][q] = v ? (int32_t)gw[c * plane + o] : 0;
-            fb[c][q] = v ? (int32_t)gb[c * plane + o] : 0;
+            fw[c][q] = (int32_t)__ldg(&gw[c * plane + o]);
+            fb[c][q] = (int32_t)__ldg(&gb[c * plane + o]);
         }
     }
     stage_coarse<3 * C, T>(ss, cl, I0, J0, wrap);
@@ -420,9 +504,20 @@ struct Out0Args {
 };
 
 template <typename TIn, typename T, int C, int S, int AM, bool VEC>
-__global__ void __launch_bounds__(256) k_out0(CoarseLevels cl, Out0Args a)
+__global__ void __launch_bounds__(256, 3) k_out0(CoarseLevels cl, Out0Args a)
 {
-    __shared__ int32_t ss[3 * C][ESH][ESW];
+    // fixed-point formats of the enblend pyramids (the host checks a.frac,
+    // a.mfrac, a.white_value and a.maxv against these): image 9.7 / 17.7,
+    // mask 9.7 (8-bit) / 9.15 (16-bit); one hash per pixel covers the dither
+    // bits of all its samples (F - 1 <= 8, C <= 4)
+    constexpr int F = 7;
+    constexpr int MF = sizeof(TIn) == 1 ? 7 : 15;
+    constexpr int32_t WV = 255 << MF;
+    constexpr int32_t MAXV = sizeof(TIn) == 1 ? 255 : 65535;
+    static_assert(C <= 4, "per-pixel dither bits");
+    // packed int4 taps for interior tiles, 3C int32 planes for border tiles
+    __shared__ int4 sbuf[C][ESH][ESW];
+    int32_t (*ss)[ESH][ESW] = reinterpret_cast<int32_t (*)[ESH][ESW]>(&sbuf[0][0][0]);
     const int X0 = blockIdx.x * ETW, Y0 = blockIdx.y * ETH;
     const int I0 = X0 >> 1, J0 = Y0 >> 1;
     const int qx = threadIdx.x % 32, qy = threadIdx.x / 32;
@@ -431,8 +526,8 @@ __global__ void __launch_bounds__(256) k_out0(CoarseLevels cl, Out0Args a)
     const bool nearest = a.dither == ENB_DITHER_NEAREST;
 
     if (a.has_coarse && interior_tile(X0, Y0, a.w, a.h, I0, J0, cl.w, cl.h)) {
-        // interior tile: no bounds, interior expansions, only the expansions
-        // the seam mask of the quad selects
+        // interior tile: no bounds, packed taps, only the expansions the seam
+        // mask of the quad selects
         TIn wp[4][S], bp[4][S];
         const TIn* w0 = reinterpret_cast<const TIn*>(a.white) + (int64_t)Y * a.wpitch + (int64_t)X * S;
         const TIn* b0 = reinterpret_cast<const TIn*>(a.black) + (int64_t)Y * a.bpitch + (int64_t)X * S;
@@ -445,9 +540,9 @@ __global__ void __launch_bounds__(256) k_out0(CoarseLevels cl, Out0Args a)
         ld_px<TIn, S, VEC>(b0 + a.bpitch, bp[2]);
         ld_px<TIn, S, VEC>(b0 + a.bpitch + S, bp[3]);
         const uint8_t* m0 = a.mask + (int64_t)Y * a.mpitch + X;
-        const int32_t mk[4] = {(int32_t)m0[0] << a.mfrac, (int32_t)m0[1] << a.mfrac, (int32_t)m0[a.mpitch] << a.mfrac,
-                               (int32_t)m0[a.mpitch + 1] << a.mfrac};
-        stage_coarse_interior<3 * C, T>(ss, cl, I0, J0);
+        const int32_t mk[4] = {(int32_t)__ldg(m0) << MF, (int32_t)__ldg(m0 + 1) << MF,
+                               (int32_t)__ldg(m0 + a.mpitch) << MF, (int32_t)__ldg(m0 + a.mpitch + 1) << MF};
+        stage_coarse4_interior<C, T>(sbuf, cl, I0, J0);
         __syncthreads();
         bool uni[4];
 #pragma unroll
@@ -456,55 +551,43 @@ __global__ void __launch_bounds__(256) k_out0(CoarseLevels cl, Out0Args a)
             uni[q] = pixel_alpha<AM, TIn, S>(wp[q], a.wa, a.wapitch, XX, YY, a.alo, a.ahi) ||
                      pixel_alpha<AM, TIn, S>(bp[q], a.ba, a.bapitch, XX, YY, a.alo, a.ahi);
         }
-        const bool need_w = mk[0] > 0 || mk[1] > 0 || mk[2] > 0 || mk[3] > 0;
-        const bool need_b = mk[0] < a.white_value || mk[1] < a.white_value || mk[2] < a.white_value ||
-                            mk[3] < a.white_value;
+        const int kind = quad_kind(mk, WV);
         const uint32_t pix0 = (uint32_t)Y * (uint32_t)a.w + (uint32_t)X;
         const uint32_t pixq[4] = {pix0, pix0 + 1, pix0 + (uint32_t)a.w, pix0 + (uint32_t)a.w + 1};
-        uint32_t pb[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            pb[q] = mix32(pixq[q] ^ a.key);
-        }
-        TIn o[4][S];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-#pragma unroll
-            for (int c = 0; c < S; ++c) {
-                o[q][c] = bp[q][c];
-            }
-        }
+        int32_t res[C][4];
 #pragma unroll
         for (int c = 0; c < C; ++c) {
-            int32_t ew[4] = {0, 0, 0, 0}, eb[4] = {0, 0, 0, 0}, er[4];
-            if (need_w) {
-                expand_quad_interior<true>(ss[c], qx, qy, ew);
-            }
-            if (need_b) {
-                expand_quad_interior<true>(ss[C + c], qx, qy, eb);
-            }
-            expand_quad_interior<false>(ss[2 * C + c], qx, qy, er);
+            int32_t ew[4], eb[4], er[4];
+            expand_packed(sbuf[c], qx, qy, kind, ew, eb, er);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                const int32_t lw = (int32_t)cast_store<T>((int64_t)((int32_t)wp[q][c] << a.frac) - ew[q]);
-                const int32_t lb = (int32_t)cast_store<T>((int64_t)((int32_t)bp[q][c] << a.frac) - eb[q]);
-                const int32_t res = (int32_t)sat_store<T>(blend1<T>(mk[q], a.white_value, lw, lb) + er[q]);
-                if (a.level0) {
-                    a.level0[(uint64_t)pixq[q] * C + c] = res;
-                }
-                if (uni[q]) {
-                    const uint32_t bits = dither_sample_bits(a.key, pb[q], pixq[q], C, c, a.frac);
-                    o[q][c] = (TIn)dither_rule(res, a.frac, nearest, bits, a.maxv);
+                res[c][q] = merge_sample<T>(kind, mk[q], WV, (int32_t)wp[q][c] << F, ew[q], (int32_t)bp[q][c] << F,
+                                            eb[q], er[q]);
+            }
+        }
+        if (a.level0) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+#pragma unroll
+                for (int c = 0; c < C; ++c) {
+                    a.level0[(uint64_t)pixq[q] * C + c] = res[c][q];
                 }
             }
         }
         TIn* out0 = reinterpret_cast<TIn*>(a.out) + (int64_t)Y * a.opitch + (int64_t)X * S;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            if (S == 4) {
-                o[q][S - 1] = uni[q] ? (TIn)a.maxv : (TIn)0;
+            const uint32_t pb = mix32(pixq[q] ^ a.key);
+            TIn o[S];
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                const int32_t d = dither_rule(res[c][q], F, nearest, pb >> (8 * c), MAXV);
+                o[c] = uni[q] ? (TIn)d : bp[q][c];
             }
-            st_px<TIn, S, VEC>(out0 + (q >> 1) * a.opitch + (q & 1) * S, o[q]);
+            if (S == 4) {
+                o[S - 1] = uni[q] ? (TIn)MAXV : (TIn)0;
+            }
+            st_px<TIn, S, VEC>(out0 + (q >> 1) * a.opitch + (q & 1) * S, o);
         }
         if (a.out_alpha) {
             uint8_t* oa = a.out_alpha + (int64_t)Y * a.oapitch + X;
@@ -516,23 +599,16 @@ __global__ void __launch_bounds__(256) k_out0(CoarseLevels cl, Out0Args a)
         return;
     }
 
-    // border tile (or a single level): the quad's pixels, loaded before the barrier
+    // border tile (or a single level): the quad's pixels, loaded (from
+    // clamped positions, unconditionally) before the barrier
     TIn wp[4][S], bp[4][S];
     int32_t mk[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-        const int XX = X + (q & 1), YY = Y + (q >> 1);
-        if (XX < a.w && YY < a.h) {
-            ld_px<TIn, S, VEC>(reinterpret_cast<const TIn*>(a.white) + (int64_t)YY * a.wpitch + (int64_t)XX * S, wp[q]);
-            ld_px<TIn, S, VEC>(reinterpret_cast<const TIn*>(a.black) + (int64_t)YY * a.bpitch + (int64_t)XX * S, bp[q]);
-            mk[q] = (int32_t)a.mask[(int64_t)YY * a.mpitch + XX] << a.mfrac;
-        } else {
-#pragma unroll
-            for (int c = 0; c < S; ++c) {
-                wp[q][c] = bp[q][c] = 0;
-            }
-            mk[q] = 0;
-        }
+        const int XX = min(X + (q & 1), a.w - 1), YY = min(Y + (q >> 1), a.h - 1);
+        ld_px<TIn, S, VEC>(reinterpret_cast<const TIn*>(a.white) + (int64_t)YY * a.wpitch + (int64_t)XX * S, wp[q]);
+        ld_px<TIn, S, VEC>(reinterpret_cast<const TIn*>(a.black) + (int64_t)YY * a.bpitch + (int64_t)XX * S, bp[q]);
+        mk[q] = (int32_t)__ldg(&a.mask[(int64_t)YY * a.mpitch + XX]) << MF;
     }
     if (a.has_coarse) {
         stage_coarse<3 * C, T>(ss, cl, I0, J0, a.wrap);
@@ -544,7 +620,8 @@ __global__ void __launch_bounds__(256) k_out0(CoarseLevels cl, Out0Args a)
     bool uni[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-        const int XX = X + (q & 1), YY = Y + (q >> 1);
+        // clamped like the loads above; pixels outside the image are not stored
+        const int XX = min(X + (q & 1), a.w - 1), YY = min(Y + (q >> 1), a.h - 1);
         uni[q] = pixel_alpha<AM, TIn, S>(wp[q], a.wa, a.wapitch, XX, YY, a.alo, a.ahi) ||
                  pixel_alpha<AM, TIn, S>(bp[q], a.ba, a.bapitch, XX, YY, a.alo, a.ahi);
     }
@@ -570,16 +647,16 @@ __global__ void __launch_bounds__(256) k_out0(CoarseLevels cl, Out0Args a)
             if (XX >= a.w || YY >= a.h) {
                 continue;
             }
-            const int32_t lw = (int32_t)cast_store<T>((int64_t)((int32_t)wp[q][c] << a.frac) - ew[q]);
-            const int32_t lb = (int32_t)cast_store<T>((int64_t)((int32_t)bp[q][c] << a.frac) - eb[q]);
-            const int32_t res = (int32_t)sat_store<T>(blend1<T>(mk[q], a.white_value, lw, lb) + er[q]);
+            const int32_t lw = (int32_t)cast_store<T>((int64_t)((int32_t)wp[q][c] << F) - ew[q]);
+            const int32_t lb = (int32_t)cast_store<T>((int64_t)((int32_t)bp[q][c] << F) - eb[q]);
+            const int32_t res = (int32_t)sat_store<T>(blend1<T>(mk[q], WV, lw, lb) + er[q]);
             const uint64_t pix = (uint64_t)YY * (uint64_t)a.w + (uint64_t)XX;
             if (a.level0) {
                 a.level0[pix * C + c] = res;
             }
             if (uni[q]) {
-                const uint32_t bits = dither_sample_bits(a.key, mix32((uint32_t)pix ^ a.key), pix, C, c, a.frac);
-                o[q][c] = (TIn)dither_rule(res, a.frac, nearest, bits, a.maxv);
+                const uint32_t bits = mix32((uint32_t)pix ^ a.key) >> (8 * c);
+                o[q][c] = (TIn)dither_rule(res, F, nearest, bits, MAXV);
             }
         }
     }
@@ -590,7 +667,7 @@ __global__ void __launch_bounds__(256) k_out0(CoarseLevels cl, Out0Args a)
             continue;
         }
         if (S == 4) {
-            o[q][S - 1] = uni[q] ? (TIn)a.maxv : (TIn)0;
+            o[q][S - 1] = uni[q] ? (TIn)MAXV : (TIn)0;
         }
         st_px<TIn, S, VEC>(reinterpret_cast<TIn*>(a.out) + (int64_t)YY * a.opitch + (int64_t)XX * S, o[q]);
         if (a.out_alpha) {
@@ -865,6 +942,11 @@ cudaError_t launch_out0(const PlanarView* gw1, const PlanarView* gb1, const Plan
     a.seed = h.seed;
     a.key = dither_key(h.seed);
     a.maxv = wv.dtype == ENB_U8 ? 255 : 65535;
+    // k_out0 compiles these formats in
+    const int mf_expect = wv.dtype == ENB_U8 ? 7 : 15;
+    if (a.frac != 7 || a.mfrac != mf_expect || a.white_value != (255 << mf_expect) || wv.C > 4) {
+        return cudaErrorInvalidValue;
+    }
     CoarseLevels cl{};
     if (gw1) {
         cl = coarse_of(*gw1, *gb1, *r1);

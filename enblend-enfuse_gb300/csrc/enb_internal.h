@@ -100,6 +100,20 @@ struct Out0Host {
     uint64_t seed;
 };
 
+// Coarse end of the fused enblend blend (one launch): slot 0 is the finest
+// level handed over by the tiled kernels, slots 1..n-1 are reduced, blended
+// and collapsed here; R of slots 1..n-1 is produced.
+struct CoarseHost {
+    int n;
+    PlanarView gw[kMaxLevels], gb[kMaxLevels], rr[kMaxLevels], mg[kMaxLevels];
+    BytePlane aw[kMaxLevels], ab[kMaxLevels];
+    int32_t white_value;
+    int wrap;
+};
+
+// Levels of at most this many pixels are left to the coarse launch.
+constexpr int64_t kCoarsePixels = 32768;
+
 // ---- launchers (all queue on `st` and return the CUDA launch status) ------
 cudaError_t launch_to_fixed(const PixelView& src, const PlanarView& dst, int frac, cudaStream_t st);
 cudaError_t launch_bytes_to_fixed(const BytePlane& src, const PlanarView& dst, int frac, cudaStream_t st);
@@ -152,5 +166,6 @@ cudaError_t launch_up_level(const PlanarView& gw1, const PlanarView& gb1, const 
                             const PlanarView& r, int32_t white_value, int wrap, cudaStream_t st);
 cudaError_t launch_out0(const PlanarView* gw1, const PlanarView* gb1, const PlanarView* r1, const Out0Host& h,
                         cudaStream_t st);
+cudaError_t launch_coarse(const CoarseHost& h, cudaStream_t st);
 
 }  // namespace enb

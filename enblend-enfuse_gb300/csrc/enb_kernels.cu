@@ -799,18 +799,23 @@ template <typename TS, typename TD, int C>
 static void reduce_dispatch(int wrap, int n, const PlanarView* const* s, const BytePlane* const* sa,
                             const PlanarView* const* d, const BytePlane* const* da, cudaStream_t st)
 {
-    using Src = PlanarSource<TS, C>;
-    ReduceJobs<Src, TD> jobs{};
-    for (int i = 0; i < 2; ++i) {
-        const int k = i < n ? i : 0;
-        jobs.j[i] = ReduceJob<Src, TD>{Src{(const TS*)s[k]->p, s[k]->pitch, s[k]->plane, sa[k] ? sa[k]->p : nullptr,
-                                           sa[k] ? sa[k]->pitch : 0},
-                                       (TD*)d[k]->p, d[k]->pitch, d[k]->plane, da[k] ? da[k]->p : nullptr,
-                                       da[k] ? da[k]->pitch : 0};
-    }
     if (sa[0]) {
+        using Src = PlanarSource<TS, C, true>;
+        ReduceJobs<Src, TD> jobs{};
+        for (int i = 0; i < 2; ++i) {
+            const int k = i < n ? i : 0;
+            jobs.j[i] = ReduceJob<Src, TD>{Src{(const TS*)s[k]->p, s[k]->pitch, s[k]->plane, sa[k]->p, sa[k]->pitch},
+                                           (TD*)d[k]->p, d[k]->pitch, d[k]->plane, da[k]->p, da[k]->pitch};
+        }
         launch_reduce_jobs<Src, TD, C, true>(jobs, n, s[0]->w, s[0]->h, d[0]->w, d[0]->h, wrap, st);
     } else {
+        using Src = PlanarSource<TS, C, false>;
+        ReduceJobs<Src, TD> jobs{};
+        for (int i = 0; i < 2; ++i) {
+            const int k = i < n ? i : 0;
+            jobs.j[i] = ReduceJob<Src, TD>{Src{(const TS*)s[k]->p, s[k]->pitch, s[k]->plane, nullptr, 0},
+                                           (TD*)d[k]->p, d[k]->pitch, d[k]->plane, nullptr, 0};
+        }
         launch_reduce_jobs<Src, TD, C, false>(jobs, n, s[0]->w, s[0]->h, d[0]->w, d[0]->h, wrap, st);
     }
 }

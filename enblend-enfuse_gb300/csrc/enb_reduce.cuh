@@ -37,8 +37,8 @@ constexpr int RVP = 148;                 // padded row of column sums
 // phase 2 (8 threads at a stride of 8 words) then hit 32 distinct banks.
 __device__ __forceinline__ int rphys(int c) { return c + ((c >> 5) << 2); }
 
-// Planar pyramid level (+ optional 8-bit alpha plane).
-template <typename TS, int C>
+// Planar pyramid level (+ an 8-bit alpha plane when A).
+template <typename TS, int C, bool A>
 struct PlanarSource {
     const TS* p;
     int64_t pitch, plane;   // elements
@@ -51,7 +51,7 @@ struct PlanarSource {
         for (int c = 0; c < C; ++c) {
             v[c] = (int32_t)__ldg(&p[c * plane + o]);
         }
-        al = a ? (__ldg(&a[(int64_t)gy * apitch + gx]) != 0) : 1;
+        al = A ? (__ldg(&a[(int64_t)gy * apitch + gx]) != 0) : 1;
     }
 };
 
@@ -82,6 +82,9 @@ struct ReduceJobs {
 };
 
 // Phase 1 for one column item: vertical sums of destination rows r0..r0+7.
+// Border items load from clamped (always valid) positions and zero the taps
+// outside the image afterwards, so that no load waits behind a branch and
+// all 19 rows are in flight at once.
 template <class Src, int C, bool ALPHA, bool INTERIOR>
 __device__ __forceinline__ void reduce_column(const Src& src, int gx, int gyb, int sw, int sh, int wrap,
                                               int32_t (*V)[RDH][RVP], int col, int r0)
@@ -91,9 +94,8 @@ __device__ __forceinline__ void reduce_column(const Src& src, int gx, int gyb, i
     if (!INTERIOR) {
         if (wrap) {
             gx = imod(gx, sw);
-        } else if (ALPHA) {
-            colok = gx >= 0 && gx < sw;
         } else {
+            colok = gx >= 0 && gx < sw;
             gx = min(max(gx, 0), sw - 1);
         }
     }
@@ -103,25 +105,18 @@ __device__ __forceinline__ void reduce_column(const Src& src, int gx, int gyb, i
         int gy = gyb + k;
         bool ok = true;
         if (!INTERIOR) {
-            if (ALPHA) {
-                ok = colok && gy >= 0 && gy < sh;
-            } else {
-                gy = min(max(gy, 0), sh - 1);
-            }
+            ok = colok && gy >= 0 && gy < sh;
+            gy = min(max(gy, 0), sh - 1);
         }
         int32_t v[C];
-        int al = 0;
-        if (ok) {
-            src.load(gy, gx, v, al);
-        } else {
-#pragma unroll
-            for (int ch = 0; ch < C; ++ch) {
-                v[ch] = 0;
-            }
+        int al = 1;
+        src.load(gy, gx, v, al);
+        if (ALPHA) {
+            al = ok ? al : 0;   // taps outside the image are dropped
         }
 #pragma unroll
         for (int ch = 0; ch < C; ++ch) {
-            x[k][ch] = (ALPHA && !al) ? 0 : v[ch];
+            x[k][ch] = (ALPHA && !al) ? 0 : v[ch];   // without alpha: clamp-to-edge
         }
         if (ALPHA) {
             x[k][NV - 1] = al;

@@ -63,7 +63,7 @@ class EnbEnfuseParams(ctypes.Structure):
 class EnbFuseOptions(ctypes.Structure):
     _fields_ = [("levels", ctypes.c_int32), ("wrap", ctypes.c_int32), ("hard_mask", ctypes.c_int32),
                 ("dither", ctypes.c_int32), ("seed", ctypes.c_uint64), ("host_buffers", ctypes.c_int32),
-                ("plain", ctypes.c_int32), ("level0_out", ctypes.c_void_p)]
+                ("plain", ctypes.c_int32), ("level0_out", ctypes.c_void_p), ("coarse_pixels", ctypes.c_int32)]
 
 
 _P = ctypes.POINTER
@@ -376,13 +376,15 @@ class Context:
         self._check(self.lib.enb_enfuse_mask(self.handle, ctypes.byref(p), ctypes.byref(pixel_image(image)), a,
                                              ctypes.byref(plane_image(out))))
 
-    def _options(self, levels, wrap, hard_mask, dither, seed, host, level0, plain=False) -> EnbFuseOptions:
+    def _options(self, levels, wrap, hard_mask, dither, seed, host, level0, plain=False,
+                 coarse_pixels: int = 0) -> EnbFuseOptions:
         o = EnbFuseOptions()
         self.lib.enb_default_fuse_options(ctypes.byref(o))
         o.levels, o.wrap, o.hard_mask = levels, int(wrap), int(hard_mask)
         o.dither, o.seed, o.host_buffers = DITHER[dither], seed, int(host)
         o.plain = int(plain)
         o.level0_out = level0
+        o.coarse_pixels = coarse_pixels
         return o
 
     def enfuse(self, images, alphas=None, params: Optional[EnbEnfuseParams] = None, masks=None, out=None,
@@ -413,11 +415,12 @@ class Context:
 
     def enblend(self, white, black, mask, white_alpha=None, black_alpha=None, out=None, out_alpha=None,
                 levels: int = 0, wrap: bool = False, dither: str = "hash", seed: int = 0x5eed, level0=None,
-                plain: bool = False):
+                plain: bool = False, coarse_pixels: int = 0):
         """enblendMain's pyramid blend (src/enblend.h:330-510).  Returns (out, out_alpha).
 
         plain=True runs the reference's pass structure (one kernel per reference operation) instead of the
-        fused level passes; the result is the same."""
+        fused level passes; coarse_pixels sets which levels run in the single coarse launch (0 default,
+        negative never).  The result is the same either way."""
         host = not _is_torch(black)
         if out is None:
             out = np.zeros_like(black) if host else black.new_zeros(black.shape)
@@ -427,7 +430,7 @@ class Context:
         wa = ctypes.byref(plane_image(white_alpha)) if white_alpha is not None else None
         ba = ctypes.byref(plane_image(black_alpha)) if black_alpha is not None else None
         l0 = _ptr_and_strides(level0)[0] if level0 is not None else None
-        o = self._options(levels, wrap, False, dither, seed, host, l0, plain)
+        o = self._options(levels, wrap, False, dither, seed, host, l0, plain, coarse_pixels)
         self._check(self.lib.enb_enblend(self.handle, ctypes.byref(pixel_image(white)), wa,
                                          ctypes.byref(pixel_image(black)), ba, ctypes.byref(plane_image(mask)),
                                          ctypes.byref(pixel_image(out)), ctypes.byref(plane_image(out_alpha)),

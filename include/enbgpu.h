@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define ENBGPU_ABI_VERSION 1
+#define ENBGPU_ABI_VERSION 2
 
 typedef enum {
     ENB_OK = 0,
@@ -118,6 +118,9 @@ typedef struct {
     void* level0_out;      /* optional device buffer (host if host_buffers):
                               collapsed level 0 before conversion, int32,
                               interleaved width*height*channels */
+    int32_t coarse_pixels; /* enblend: pyramid levels of at most this many
+                              pixels run in one cluster launch; 0: default
+                              (32768), < 0: every level in its own launches */
 } enb_fuse_options;
 
 typedef struct enb_ctx enb_ctx;

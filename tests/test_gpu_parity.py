@@ -261,12 +261,18 @@ def test_enfuse_host_buffers_and_injected_masks(ctx, orc, dt):
     assert np.array_equal(out, ref["out"])
 
 
+# pass structures of the enblend driver: fused level passes with the coarse
+# levels in one cluster launch (default), fused passes with every level in
+# its own launches, and one kernel per reference operation
+MODES = {"fused": {}, "tiled": {"coarse_pixels": -1}, "plain": {"plain": True}}
+
+
 @pytest.mark.parametrize("dt", [np.uint8, np.uint16])
 @pytest.mark.parametrize("wrap", [False, True])
-@pytest.mark.parametrize("plain", [False, True])
+@pytest.mark.parametrize("mode", list(MODES))
 @pytest.mark.parametrize("geom", [(90, 120, 80), (7, 9, 5), (21, 30, 17), (40, 64, 40)])
-def test_enblend_end_to_end(ctx, orc, dt, wrap, plain, geom):
-    """Fused level passes and the reference pass structure, against the oracle.
+def test_enblend_end_to_end(ctx, orc, dt, wrap, mode, geom):
+    """Every pass structure against the oracle.
 
     Geometries give 8, 1, 2 and 4 pyramid levels (union canvases 200x90,
     14x7, 47x21, 104x40)."""
@@ -277,13 +283,30 @@ def test_enblend_end_to_end(ctx, orc, dt, wrap, plain, geom):
         mask[: h // 3, off + 2: off + 9] = 128   # intermediate seam weights at level 0 too
     ref = orc.enblend(white, black, mask, wrap=wrap, seed=9, want_level0=True)
     l0 = torch.zeros((h, w + off, 3), dtype=torch.int32, device="cuda")
-    out, oa = ctx.enblend(_dev(white), _dev(black), _dev(mask), wrap=wrap, seed=9, level0=l0, plain=plain)
+    out, oa = ctx.enblend(_dev(white), _dev(black), _dev(mask), wrap=wrap, seed=9, level0=l0, **MODES[mode])
     assert np.array_equal(l0.cpu().numpy(), ref["level0"])
     assert np.array_equal(oa.cpu().numpy(), ref["alpha"])
     assert np.array_equal(out.cpu().numpy(), ref["out"])
     # host-buffer entry point gives the same image
-    out2, _ = ctx.enblend(white, black, mask, wrap=wrap, seed=9, plain=plain)
+    out2, _ = ctx.enblend(white, black, mask, wrap=wrap, seed=9, **MODES[mode])
     assert np.array_equal(out2, ref["out"])
+
+
+@pytest.mark.parametrize("wrap", [False, True])
+@pytest.mark.parametrize("coarse", [0, 4000, 1 << 30])
+def test_enblend_coarse_split(ctx, orc, wrap, coarse):
+    """Tiled levels above, the coarse launch below: the default split of a
+    700x300 canvas (coarse from 175x75 down), a split further down (4000
+    pixels) and everything but level 1 in the coarse launch."""
+    from enbgpu import synthetic
+    white, black, mask = synthetic.panorama_pair(300, 400, 300, np.uint16, seed=37)
+    mask[40:90, 310:330] = 77
+    ref = orc.enblend(white, black, mask, wrap=wrap, seed=4, want_level0=True)
+    l0 = torch.zeros((300, 700, 3), dtype=torch.int32, device="cuda")
+    out, oa = ctx.enblend(_dev(white), _dev(black), _dev(mask), wrap=wrap, seed=4, level0=l0, coarse_pixels=coarse)
+    assert np.array_equal(l0.cpu().numpy(), ref["level0"])
+    assert np.array_equal(out.cpu().numpy(), ref["out"])
+    assert np.array_equal(oa.cpu().numpy(), ref["alpha"])
 
 
 @pytest.mark.parametrize("plain", [False, True])
