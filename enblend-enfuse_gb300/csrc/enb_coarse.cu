@@ -14,13 +14,11 @@
 //      R_l = fromPromote(blend(M_l, Gw_l - E(Gw_{l+1}), Gb_l - E(Gb_{l+1}))
 //                        + E(R_{l+1}))
 //      (Laplacians, blend and collapse, src/pyramid.h:1758-1784).
-// The finer levels stay with the tiled kernels.  Each thread computes whole
-// destination pixels with the reference's integer arithmetic (the same
-// operations as the tiled kernels): normalised 5x5 reduce over opaque taps,
-// clamp-to-edge reduce of the mask, expansion with the border weights of
-// expand_hweights / expand_vweights.  Every level is read only after the
-// barrier that follows its last write, and no SM touches a level before it is
-// written, so plain (L1-cached) loads see the written values; the read-only
+// The CTAs of the cluster share out the 64x16 tiles of each step and run the
+// same tile code as the per-level kernels (reduce_tile, up_tile), so the
+// integer results are theirs.  Every level is read only after the barrier that
+// follows its last write, and no SM touches a level before it is written, so
+// plain (L1-cached) loads see the written values; the read-only
 // (non-coherent) load path is never used for them.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
@@ -31,12 +29,13 @@
 
 #include "enb_device.cuh"
 #include "enb_internal.h"
+#include "enb_reduce.cuh"
+#include "enb_tiles.cuh"
 
 namespace enb {
 
 namespace cg = cooperative_groups;
 
-constexpr int kCoarseThreads = 1024;
 
 struct CoarseArgs {
     // slot 0: the finest level (input); slots 1..n-1: produced here
@@ -55,157 +54,59 @@ struct CoarseArgs {
     int wrap;
 };
 
-template <typename T>
-__device__ __forceinline__ T ld_level(const T* p)
-{
-    return *p;
-}
-
-__device__ __forceinline__ int tap5(int k) { return k == 2 ? 6 : ((k & 1) ? 4 : 1); }
-
-// Reduce with alpha of one destination pixel (X, Y).
-template <typename T, int C>
-__device__ __forceinline__ void coarse_reduce_alpha(const T* s, int64_t sp, int64_t spl, const uint8_t* sa,
-                                                    int64_t sap, int sw, int sh, T* d, int64_t dp, int64_t dpl,
-                                                    uint8_t* da, int64_t dap, int X, int Y, int wrap)
-{
-    int32_t num[C];
-#pragma unroll
-    for (int c = 0; c < C; ++c) {
-        num[c] = 0;
-    }
-    int32_t den = 0;
-#pragma unroll
-    for (int a = 0; a < 5; ++a) {
-        const int gy = 2 * Y - 2 + a;
-        const bool rok = gy >= 0 && gy < sh;
-        const int gyc = min(max(gy, 0), sh - 1);
-#pragma unroll
-        for (int b = 0; b < 5; ++b) {
-            int gx = 2 * X - 2 + b;
-            bool ok = rok;
-            if (wrap) {
-                gx = imod(gx, sw);
-            } else {
-                ok = ok && gx >= 0 && gx < sw;
-                gx = min(max(gx, 0), sw - 1);
-            }
-            const int64_t o = (int64_t)gyc * sp + gx;
-            // unconditional load from the clamped position, dropped afterwards
-            const uint8_t al = ld_level(&sa[(int64_t)gyc * sap + gx]);
-            const int32_t wt = (ok && al != 0) ? tap5(a) * tap5(b) : 0;
-            den += wt;
-#pragma unroll
-            for (int c = 0; c < C; ++c) {
-                num[c] += wt * (int32_t)ld_level(&s[c * spl + o]);
-            }
-        }
-    }
-    const int64_t o = (int64_t)Y * dp + X;
-#pragma unroll
-    for (int c = 0; c < C; ++c) {
-        d[c * dpl + o] = den <= 0 ? (T)0 : cast_store<T>(den == 256 ? num[c] / 256 : div_any(num[c], den));
-    }
-    da[(int64_t)Y * dap + X] = den > 0 ? 255 : 0;
-}
-
-// Alpha-free (clamp-to-edge) reduce of one mask pixel.
-template <typename TM>
-__device__ __forceinline__ void coarse_reduce_mask(const TM* s, int64_t sp, int sw, int sh, TM* d, int64_t dp, int X,
-                                                   int Y, int wrap)
-{
-    int32_t num = 0;
-#pragma unroll
-    for (int a = 0; a < 5; ++a) {
-        const int gy = min(max(2 * Y - 2 + a, 0), sh - 1);
-        const TM* row = s + (int64_t)gy * sp;
-        int32_t hs = 0;
-#pragma unroll
-        for (int b = 0; b < 5; ++b) {
-            const int t = 2 * X - 2 + b;
-            const int gx = wrap ? imod(t, sw) : min(max(t, 0), sw - 1);
-            hs += tap5(b) * (int32_t)ld_level(&row[gx]);
-        }
-        num += tap5(a) * hs;
-    }
-    d[(int64_t)Y * dp + X] = cast_store<TM>(num / 256);
-}
-
-// Source taps and weights of the expansion at destination pixel (X, Y); taps
-// of weight 0 point at a valid sample so that every load is unconditional.
-struct ExpandTaps {
-    int jj[3], ii[3], vw[3], hw[3], den;
-};
-
-__device__ __forceinline__ ExpandTaps expand_taps(int X, int Y, int sw, int sh, int dw, int wrap)
-{
-    ExpandTaps t;
-    int vden, hden;
-    expand_vweights(Y, sh, t.vw, vden);
-    expand_hweights(X, sw, dw, wrap, t.hw, hden);
-    t.den = vden * hden;
-    const int i = X >> 1, j = Y >> 1;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        t.jj[k] = min(max(j - 1 + k, 0), sh - 1);
-        const int c = i - 1 + k;
-        t.ii[k] = wrap ? imod(c, sw) : min(max(c, 0), sw - 1);
-    }
-    return t;
-}
-
-template <typename T>
-__device__ __forceinline__ int32_t expand_at(const T* s, int64_t pitch, const ExpandTaps& t)
-{
-    int32_t num = 0;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        const T* row = s + (int64_t)t.jj[a] * pitch;
-        num += t.vw[a] * (t.hw[0] * (int32_t)ld_level(&row[t.ii[0]]) + t.hw[1] * (int32_t)ld_level(&row[t.ii[1]]) +
-                          t.hw[2] * (int32_t)ld_level(&row[t.ii[2]]));
-    }
-    return div_den(num, t.den);
-}
-
 __device__ __forceinline__ void coarse_sync(cg::cluster_group& cluster)
 {
     __threadfence();
     cluster.sync();
 }
 
+constexpr int kCoarseThreads = RTHREADS;
+constexpr int kCoarseWords = ReduceSmem<3, true>::WORDS;   // the largest tile buffer
+static_assert(kCoarseWords * 4 >= 3 * ESH * ESW * 16, "up_tile staging fits the reduce buffer");
+
 // Launched as one cluster (16 CTAs where the GPU allows that cluster size,
 // else the portable 8) of kCoarseThreads threads.
 template <typename T, typename TM, int C>
 __global__ void __launch_bounds__(kCoarseThreads, 1) k_coarse(CoarseArgs a)
 {
+    __shared__ __align__(16) int32_t sm[kCoarseWords];
+    int32_t (*V)[RDH][RVP] = reinterpret_cast<int32_t (*)[RDH][RVP]>(sm);
+    int4 (*S4)[ESH][ESW] = reinterpret_cast<int4 (*)[ESH][ESW]>(sm);
+    griddep_wait();
+    griddep_launch();
     cg::cluster_group cluster = cg::this_cluster();
-    const int nt = (int)cluster.num_blocks() * kCoarseThreads;
-    const int gt = (int)cluster.block_rank() * kCoarseThreads + (int)threadIdx.x;
+    const int nb = (int)cluster.num_blocks();
+    const int rank = (int)cluster.block_rank();
     const int32_t W = a.white_value;
+    using SrcI = PlanarSource<T, C, true, false>;
+    using SrcM = PlanarSource<TM, 1, false, false>;
 
-    // 1. Gaussian levels 1..n-1 of the white, black and mask pyramids
+    // 1. Gaussian levels 1..n-1: white and black (with alpha), mask
     for (int l = 1; l < a.n; ++l) {
         const int dw = a.w[l], dh = a.h[l], sw = a.w[l - 1], sh = a.h[l - 1];
-        const int np = dw * dh;
-        for (int k = gt; k < 3 * np; k += nt) {
-            const int job = k / np;
-            const int p = k - job * np;
-            const int Y = p / dw, X = p - Y * dw;
+        const int tx = (dw + RDW - 1) / RDW, nt = tx * ((dh + RDH - 1) / RDH);
+        for (int t = rank; t < 3 * nt; t += nb) {
+            const int job = t / nt, tile = t - job * nt;
+            const int X0 = (tile % tx) * RDW, Y0 = (tile / tx) * RDH;
+            __syncthreads();  // the previous tile's readers of sm are done
             if (job < 2) {
-                const T* s = reinterpret_cast<const T*>(job == 0 ? a.gw[l - 1] : a.gb[l - 1]);
-                T* d = reinterpret_cast<T*>(job == 0 ? a.gw[l] : a.gb[l]);
-                coarse_reduce_alpha<T, C>(s, a.pitch[l - 1], a.plane[l - 1], job == 0 ? a.aw[l - 1] : a.ab[l - 1],
-                                          a.apitch[l - 1], sw, sh, d, a.pitch[l], a.plane[l],
-                                          job == 0 ? a.aw[l] : a.ab[l], a.apitch[l], X, Y, a.wrap);
+                const ReduceJob<SrcI, T> rj{
+                    SrcI{reinterpret_cast<const T*>(job == 0 ? a.gw[l - 1] : a.gb[l - 1]), a.pitch[l - 1],
+                         a.plane[l - 1], job == 0 ? a.aw[l - 1] : a.ab[l - 1], a.apitch[l - 1]},
+                    reinterpret_cast<T*>(job == 0 ? a.gw[l] : a.gb[l]), a.pitch[l], a.plane[l],
+                    job == 0 ? a.aw[l] : a.ab[l], a.apitch[l]};
+                reduce_tile<SrcI, T, C, true>(rj, X0, Y0, sw, sh, dw, dh, a.wrap, V);
             } else {
-                coarse_reduce_mask<TM>(reinterpret_cast<const TM*>(a.mg[l - 1]), a.mpitch[l - 1], sw, sh,
-                                       reinterpret_cast<TM*>(a.mg[l]), a.mpitch[l], X, Y, a.wrap);
+                const ReduceJob<SrcM, TM> rj{
+                    SrcM{reinterpret_cast<const TM*>(a.mg[l - 1]), a.mpitch[l - 1], 0, nullptr, 0},
+                    reinterpret_cast<TM*>(a.mg[l]), a.mpitch[l], 0, nullptr, 0};
+                reduce_tile<SrcM, TM, 1, false>(rj, X0, Y0, sw, sh, dw, dh, a.wrap, V);
             }
         }
         coarse_sync(cluster);
     }
 
-    // 2. top level: R = blend(M, Gw, Gb)
+    // 2. top level: R = blend(M, Gw, Gb), one pixel per thread
     {
         const int l = a.n - 1;
         const int dw = a.w[l], np = dw * a.h[l];
@@ -213,14 +114,14 @@ __global__ void __launch_bounds__(kCoarseThreads, 1) k_coarse(CoarseArgs a)
         const T* gb = reinterpret_cast<const T*>(a.gb[l]);
         T* rr = reinterpret_cast<T*>(a.rr[l]);
         const TM* mg = reinterpret_cast<const TM*>(a.mg[l]);
-        for (int p = gt; p < np; p += nt) {
+        for (int p = rank * kCoarseThreads + (int)threadIdx.x; p < np; p += nb * kCoarseThreads) {
             const int Y = p / dw, X = p - Y * dw;
-            const int32_t m = (int32_t)ld_level(&mg[(int64_t)Y * a.mpitch[l] + X]);
+            const int32_t m = (int32_t)mg[(int64_t)Y * a.mpitch[l] + X];
             const int64_t o = (int64_t)Y * a.pitch[l] + X;
 #pragma unroll
             for (int c = 0; c < C; ++c) {
-                rr[c * a.plane[l] + o] = (T)blend_sample<T>(m, W, (int32_t)ld_level(&gw[c * a.plane[l] + o]),
-                                                            (int32_t)ld_level(&gb[c * a.plane[l] + o]));
+                rr[c * a.plane[l] + o] =
+                    (T)blend_sample<T>(m, W, (int32_t)gw[c * a.plane[l] + o], (int32_t)gb[c * a.plane[l] + o]);
             }
         }
     }
@@ -228,30 +129,24 @@ __global__ void __launch_bounds__(kCoarseThreads, 1) k_coarse(CoarseArgs a)
     // 3. Laplacians + blend + collapse, levels n-2 .. 1
     for (int l = a.n - 2; l >= 1; --l) {
         coarse_sync(cluster);
-        const int dw = a.w[l], np = dw * a.h[l];
-        const int sw = a.w[l + 1], sh = a.h[l + 1];
-        const T* gw = reinterpret_cast<const T*>(a.gw[l]);
-        const T* gb = reinterpret_cast<const T*>(a.gb[l]);
-        T* rr = reinterpret_cast<T*>(a.rr[l]);
-        const TM* mg = reinterpret_cast<const TM*>(a.mg[l]);
-        const T* cw = reinterpret_cast<const T*>(a.gw[l + 1]);
-        const T* cb = reinterpret_cast<const T*>(a.gb[l + 1]);
-        const T* cr = reinterpret_cast<const T*>(a.rr[l + 1]);
-        for (int p = gt; p < np; p += nt) {
-            const int Y = p / dw, X = p - Y * dw;
-            const ExpandTaps t = expand_taps(X, Y, sw, sh, dw, a.wrap);
-            const int32_t m = (int32_t)ld_level(&mg[(int64_t)Y * a.mpitch[l] + X]);
-            const int64_t o = (int64_t)Y * a.pitch[l] + X;
+        CoarseLevels cl{};
 #pragma unroll
-            for (int c = 0; c < C; ++c) {
-                const int64_t cpl = c * a.plane[l + 1];
-                const int32_t ew = expand_at<T>(cw + cpl, a.pitch[l + 1], t);
-                const int32_t eb = expand_at<T>(cb + cpl, a.pitch[l + 1], t);
-                const int32_t er = expand_at<T>(cr + cpl, a.pitch[l + 1], t);
-                const int32_t lw = (int32_t)cast_store<T>((int64_t)ld_level(&gw[c * a.plane[l] + o]) - ew);
-                const int32_t lb = (int32_t)cast_store<T>((int64_t)ld_level(&gb[c * a.plane[l] + o]) - eb);
-                rr[c * a.plane[l] + o] = sat_store<T>(blend_sample<T>(m, W, lw, lb) + er);
-            }
+        for (int c = 0; c < C; ++c) {
+            cl.p[c] = reinterpret_cast<const T*>(a.gw[l + 1]) + c * a.plane[l + 1];
+            cl.p[C + c] = reinterpret_cast<const T*>(a.gb[l + 1]) + c * a.plane[l + 1];
+            cl.p[2 * C + c] = reinterpret_cast<const T*>(a.rr[l + 1]) + c * a.plane[l + 1];
+        }
+        cl.pitch = a.pitch[l + 1];
+        cl.w = a.w[l + 1];
+        cl.h = a.h[l + 1];
+        const int dw = a.w[l], dh = a.h[l];
+        const int tx = (dw + ETW - 1) / ETW, nt = tx * ((dh + ETH - 1) / ETH);
+        for (int t = rank; t < nt; t += nb) {
+            __syncthreads();  // the previous tile's readers of sm are done
+            up_tile<T, TM, C, false, kCoarseThreads>(
+                cl, reinterpret_cast<const TM*>(a.mg[l]), a.mpitch[l], reinterpret_cast<const T*>(a.gw[l]),
+                reinterpret_cast<const T*>(a.gb[l]), reinterpret_cast<T*>(a.rr[l]), a.pitch[l], a.plane[l], dw, dh, W,
+                a.wrap, (t % tx) * ETW, (t / tx) * ETH, S4);
         }
     }
 }
@@ -289,16 +184,18 @@ static cudaError_t coarse_launch(void (*kernel)(CoarseArgs), const CoarseArgs& a
         }
     }
     cudaLaunchConfig_t cfg{};
-    cudaLaunchAttribute attr{};
+    cudaLaunchAttribute attr[2];
     cfg.gridDim = dim3((unsigned)cs);
     cfg.blockDim = dim3(kCoarseThreads);
     cfg.stream = st;
-    attr.id = cudaLaunchAttributeClusterDimension;
-    attr.val.clusterDim.x = (unsigned)cs;
-    attr.val.clusterDim.y = 1;
-    attr.val.clusterDim.z = 1;
-    cfg.attrs = &attr;
-    cfg.numAttrs = 1;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[1].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 2;
     return cudaLaunchKernelEx(&cfg, kernel, a);
 }
 

@@ -100,6 +100,18 @@ static inline dim3 grid2d(int w, int h, int tw, int th)
     return dim3((unsigned)((w + tw - 1) / tw), (unsigned)((h + th - 1) / th));
 }
 
+// Global load through the read-only path (NC: no thread of the launch writes
+// the data) or a plain, L1-cached load (the data was written earlier in the
+// same launch and is read only after the barrier that follows the write).
+template <bool NC, typename T>
+__device__ __forceinline__ T ld_src(const T* p)
+{
+    if (NC) {
+        return __ldg(p);
+    }
+    return *p;
+}
+
 // Horizontal expand weights on source offsets (-1, 0, +1) of destination
 // column X and their divisor; the SKIPSM scale tables of
 // src/pyramid.h:1227-1411 factor into these per-axis divisors.
@@ -159,10 +171,42 @@ __device__ __forceinline__ void expand_vweights(int Y, int sh, int w[3], int& de
     den = w[0] + w[1] + w[2];
 }
 
-// Truncating division by a divisor known only at run time, kept out of line so
-// that the compiler branches around it instead of predicating it into the
-// common path (the divisor is a power-of-two constant there).
-static __device__ __noinline__ int32_t div_any(int32_t num, int32_t den) { return num / den; }
+// Truncating division by a divisor d in [1, 256] known only at run time, as a
+// multiplication (division by invariant integers, Granlund & Montgomery
+// 1994): with l = ceil(log2 d) and m = floor(2^(31+l) / d) + 1 < 2^32,
+// floor(x / d) = (x * m) >> (31 + l) for every 0 <= x < 2^31.  The table
+// holds m | (31 + l) << 32 per divisor; it is read through the read-only
+// cache, so lanes with different divisors do not serialise.
+struct DivTable {
+    uint64_t e[257];
+};
+
+constexpr DivTable make_div_table()
+{
+    DivTable t{};
+    for (int d = 1; d <= 256; ++d) {
+        int l = 0;
+        while ((1 << l) < d) {
+            ++l;
+        }
+        const uint64_t m = ((uint64_t)1 << (31 + l)) / (uint64_t)d + 1;
+        t.e[d] = m | ((uint64_t)(31 + l) << 32);
+    }
+    return t;
+}
+
+static __device__ const DivTable g_div_table = make_div_table();
+
+__device__ __forceinline__ int32_t div_any(int32_t num, int32_t den)
+{
+    const uint32_t a = num < 0 ? 0u - (uint32_t)num : (uint32_t)num;
+    if (den < 1 || den > 256 || a >= 0x80000000u) {
+        return num / den;
+    }
+    const uint64_t e = __ldg(&g_div_table.e[den]);
+    const uint32_t q = (uint32_t)(((uint64_t)a * (uint32_t)e) >> (uint32_t)(e >> 32));
+    return num < 0 ? -(int32_t)q : (int32_t)q;
+}
 
 __device__ __forceinline__ int32_t div_den(int32_t num, int den)
 {
@@ -174,6 +218,16 @@ __device__ __forceinline__ int32_t div_den(int32_t num, int den)
     }
     return div_any(num, den);
 }
+
+// Programmatic dependent launch: a kernel launched with the programmatic
+// stream serialization attribute may start while its predecessor on the
+// stream drains; griddep_wait() blocks (in hardware) until the predecessor
+// has completed and its writes are visible, and must precede every access to
+// data the predecessor wrote.  griddep_launch() lets the successor be
+// scheduled.  Both are no-ops for kernels launched without the attribute.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+__device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 // 32-bit integer finaliser (public-domain "lowbias32" constants by C. Wellons).
 __host__ __device__ __forceinline__ uint32_t mix32(uint32_t x)

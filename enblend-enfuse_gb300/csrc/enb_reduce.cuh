@@ -21,6 +21,7 @@
 #pragma once
 
 #include "enb_device.cuh"
+#include "enb_internal.h"
 
 namespace enb {
 
@@ -37,8 +38,9 @@ constexpr int RVP = 148;                 // padded row of column sums
 // phase 2 (8 threads at a stride of 8 words) then hit 32 distinct banks.
 __device__ __forceinline__ int rphys(int c) { return c + ((c >> 5) << 2); }
 
-// Planar pyramid level (+ an 8-bit alpha plane when A).
-template <typename TS, int C, bool A>
+// Planar pyramid level (+ an 8-bit alpha plane when A); NC: read-only load
+// path (the level is not written by the launch).
+template <typename TS, int C, bool A, bool NC = true>
 struct PlanarSource {
     const TS* p;
     int64_t pitch, plane;   // elements
@@ -49,9 +51,9 @@ struct PlanarSource {
         const int64_t o = (int64_t)gy * pitch + gx;
 #pragma unroll
         for (int c = 0; c < C; ++c) {
-            v[c] = (int32_t)__ldg(&p[c * plane + o]);
+            v[c] = (int32_t)ld_src<NC>(&p[c * plane + o]);
         }
-        al = A ? (__ldg(&a[(int64_t)gy * apitch + gx]) != 0) : 1;
+        al = A ? (ld_src<NC>(&a[(int64_t)gy * apitch + gx]) != 0) : 1;
     }
 };
 
@@ -153,15 +155,20 @@ __device__ __forceinline__ void store4(TD* p, const int32_t (&v)[4], int n)
     }
 }
 
+// Shared memory of one reduce tile: NV planes of 16 rows of column sums.
+template <int C, bool ALPHA>
+struct ReduceSmem {
+    static constexpr int NV = C + (ALPHA ? 1 : 0);
+    static constexpr int WORDS = NV * RDH * RVP;
+};
+
+// One 64x16 destination tile at (X0, Y0) of a reduce job (RTHREADS threads;
+// V holds ReduceSmem<C, ALPHA>::WORDS 16-byte aligned words).
 template <class Src, typename TD, int C, bool ALPHA>
-__global__ void __launch_bounds__(RTHREADS, 2) k_reduce(ReduceJobs<Src, TD> jobs, int sw, int sh, int dw, int dh,
-                                                        int wrap)
+__device__ __forceinline__ void reduce_tile(const ReduceJob<Src, TD>& job, int X0, int Y0, int sw, int sh, int dw,
+                                            int dh, int wrap, int32_t (*V)[RDH][RVP])
 {
     constexpr int NV = C + (ALPHA ? 1 : 0);
-    __shared__ __align__(16) int32_t V[NV][RDH][RVP];
-
-    const ReduceJob<Src, TD> job = blockIdx.z == 0 ? jobs.j[0] : jobs.j[1];
-    const int X0 = blockIdx.x * RDW, Y0 = blockIdx.y * RDH;
     const int gx0 = 2 * X0 - 2, gy0 = 2 * Y0 - 2;
     const int tid = threadIdx.x;
 
@@ -176,13 +183,10 @@ __global__ void __launch_bounds__(RTHREADS, 2) k_reduce(ReduceJobs<Src, TD> jobs
         }
     }
     __syncthreads();
-    if (tid >= RDH * (RDW / 4)) {
-        return;
-    }
 
     const int r = tid >> 4, k = tid & 15;
     const int Y = Y0 + r, Xb = X0 + 4 * k;
-    if (Y >= dh || Xb >= dw) {
+    if (tid >= RDH * (RDW / 4) || Y >= dh || Xb >= dw) {
         return;
     }
     const int n = min(4, dw - Xb);
@@ -240,13 +244,24 @@ __global__ void __launch_bounds__(RTHREADS, 2) k_reduce(ReduceJobs<Src, TD> jobs
     }
 }
 
+template <class Src, typename TD, int C, bool ALPHA>
+__global__ void __launch_bounds__(RTHREADS, 2) k_reduce(ReduceJobs<Src, TD> jobs, int sw, int sh, int dw, int dh,
+                                                        int wrap)
+{
+    __shared__ __align__(16) int32_t V[ReduceSmem<C, ALPHA>::NV][RDH][RVP];
+    griddep_wait();
+    griddep_launch();
+    const ReduceJob<Src, TD> job = blockIdx.z == 0 ? jobs.j[0] : jobs.j[1];
+    reduce_tile<Src, TD, C, ALPHA>(job, blockIdx.x * RDW, blockIdx.y * RDH, sw, sh, dw, dh, wrap, V);
+}
+
 // One launch over njobs (1 or 2) jobs of the same geometry.
 template <class Src, typename TD, int C, bool ALPHA>
 inline void launch_reduce_jobs(const ReduceJobs<Src, TD>& jobs, int njobs, int sw, int sh, int dw, int dh, int wrap,
                                cudaStream_t st)
 {
     const dim3 g((unsigned)((dw + RDW - 1) / RDW), (unsigned)((dh + RDH - 1) / RDH), (unsigned)njobs);
-    k_reduce<Src, TD, C, ALPHA><<<g, RTHREADS, 0, st>>>(jobs, sw, sh, dw, dh, wrap);
+    (void)launch_pdl(k_reduce<Src, TD, C, ALPHA>, g, dim3(RTHREADS), st, jobs, sw, sh, dw, dh, wrap);
 }
 
 template <class Src, typename TD, int C, bool ALPHA>

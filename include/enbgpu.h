@@ -120,7 +120,7 @@ typedef struct {
                               interleaved width*height*channels */
     int32_t coarse_pixels; /* enblend: pyramid levels of at most this many
                               pixels run in one cluster launch; 0: default
-                              (32768), < 0: every level in its own launches */
+                              (none), < 0: every level in its own launches */
 } enb_fuse_options;
 
 typedef struct enb_ctx enb_ctx;

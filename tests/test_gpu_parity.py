@@ -261,10 +261,10 @@ def test_enfuse_host_buffers_and_injected_masks(ctx, orc, dt):
     assert np.array_equal(out, ref["out"])
 
 
-# pass structures of the enblend driver: fused level passes with the coarse
-# levels in one cluster launch (default), fused passes with every level in
-# its own launches, and one kernel per reference operation
-MODES = {"fused": {}, "tiled": {"coarse_pixels": -1}, "plain": {"plain": True}}
+# pass structures of the enblend driver: fused level passes with every level
+# in its own launches (default), fused passes with all levels below level 1 in
+# one cluster launch, and one kernel per reference operation
+MODES = {"fused": {}, "cluster": {"coarse_pixels": 1 << 30}, "plain": {"plain": True}}
 
 
 @pytest.mark.parametrize("dt", [np.uint8, np.uint16])
@@ -293,11 +293,11 @@ def test_enblend_end_to_end(ctx, orc, dt, wrap, mode, geom):
 
 
 @pytest.mark.parametrize("wrap", [False, True])
-@pytest.mark.parametrize("coarse", [0, 4000, 1 << 30])
+@pytest.mark.parametrize("coarse", [32768, 4000, 1 << 30])
 def test_enblend_coarse_split(ctx, orc, wrap, coarse):
-    """Tiled levels above, the coarse launch below: the default split of a
-    700x300 canvas (coarse from 175x75 down), a split further down (4000
-    pixels) and everything but level 1 in the coarse launch."""
+    """Per-level launches above, the cluster launch below, on a 700x300
+    canvas: coarse from 175x75 down (32768 pixels), a split further down
+    (4000 pixels) and everything but level 1 in the cluster launch."""
     from enbgpu import synthetic
     white, black, mask = synthetic.panorama_pair(300, 400, 300, np.uint16, seed=37)
     mask[40:90, 310:330] = 77
