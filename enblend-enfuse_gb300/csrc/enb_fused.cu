@@ -23,6 +23,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "enb_device.cuh"
 #include "enb_internal.h"
 #include "enb_reduce.cuh"
@@ -186,6 +188,71 @@ struct Out0Args {
     int32_t maxv;
 };
 
+// Level-0 output of the interior quad (X, Y) (tile position qx, qy) from its
+// loaded pixels and seam mask and the packed coarse taps of the tile.
+template <typename TIn, typename T, int C, int S, int AM, bool VEC>
+__device__ __forceinline__ void out0_quad(const Out0Args& a, const int4 (*sbuf)[ESH][ESW], int X, int Y, int qx,
+                                          int qy, const TIn (&wp)[4][S], const TIn (&bp)[4][S], const int32_t (&mk)[4])
+{
+    constexpr int F = 7;
+    constexpr int MF = sizeof(TIn) == 1 ? 7 : 15;
+    constexpr int32_t WV = 255 << MF;
+    constexpr int32_t MAXV = sizeof(TIn) == 1 ? 255 : 65535;
+    const bool nearest = a.dither == ENB_DITHER_NEAREST;
+    bool uni[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int XX = X + (q & 1), YY = Y + (q >> 1);
+        uni[q] = pixel_alpha<AM, TIn, S>(wp[q], a.wa, a.wapitch, XX, YY, a.alo, a.ahi) ||
+                 pixel_alpha<AM, TIn, S>(bp[q], a.ba, a.bapitch, XX, YY, a.alo, a.ahi);
+    }
+    const int kind = quad_kind(mk, WV);
+    const uint32_t pix0 = (uint32_t)Y * (uint32_t)a.w + (uint32_t)X;
+    const uint32_t pixq[4] = {pix0, pix0 + 1, pix0 + (uint32_t)a.w, pix0 + (uint32_t)a.w + 1};
+    int32_t res[C][4];
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        int32_t ew[4], eb[4], er[4];
+        expand_packed(sbuf[c], qx, qy, kind, ew, eb, er);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            res[c][q] = merge_sample<T>(kind, mk[q], WV, (int32_t)wp[q][c] << F, ew[q], (int32_t)bp[q][c] << F,
+                                        eb[q], er[q]);
+        }
+    }
+    if (a.level0) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                a.level0[(uint64_t)pixq[q] * C + c] = res[c][q];
+            }
+        }
+    }
+    TIn* out0 = reinterpret_cast<TIn*>(a.out) + (int64_t)Y * a.opitch + (int64_t)X * S;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const uint32_t pb = mix32(pixq[q] ^ a.key);
+        TIn o[S];
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            const int32_t d = dither_rule(res[c][q], F, nearest, pb >> (8 * c), MAXV);
+            o[c] = uni[q] ? (TIn)d : bp[q][c];
+        }
+        if (S == 4) {
+            o[S - 1] = uni[q] ? (TIn)MAXV : (TIn)0;
+        }
+        st_px<TIn, S, VEC>(out0 + (q >> 1) * a.opitch + (q & 1) * S, o);
+    }
+    if (a.out_alpha) {
+        uint8_t* oa = a.out_alpha + (int64_t)Y * a.oapitch + X;
+        oa[0] = uni[0] ? 255 : 0;
+        oa[1] = uni[1] ? 255 : 0;
+        oa[a.oapitch] = uni[2] ? 255 : 0;
+        oa[a.oapitch + 1] = uni[3] ? 255 : 0;
+    }
+}
+
 template <typename TIn, typename T, int C, int S, int AM, bool VEC>
 __global__ void __launch_bounds__(256, 3) k_out0(CoarseLevels cl, Out0Args a)
 {
@@ -229,58 +296,7 @@ __global__ void __launch_bounds__(256, 3) k_out0(CoarseLevels cl, Out0Args a)
                                (int32_t)__ldg(m0 + a.mpitch) << MF, (int32_t)__ldg(m0 + a.mpitch + 1) << MF};
         stage_coarse4_interior<C, T, true, 256>(sbuf, cl, I0, J0);
         __syncthreads();
-        bool uni[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int XX = X + (q & 1), YY = Y + (q >> 1);
-            uni[q] = pixel_alpha<AM, TIn, S>(wp[q], a.wa, a.wapitch, XX, YY, a.alo, a.ahi) ||
-                     pixel_alpha<AM, TIn, S>(bp[q], a.ba, a.bapitch, XX, YY, a.alo, a.ahi);
-        }
-        const int kind = quad_kind(mk, WV);
-        const uint32_t pix0 = (uint32_t)Y * (uint32_t)a.w + (uint32_t)X;
-        const uint32_t pixq[4] = {pix0, pix0 + 1, pix0 + (uint32_t)a.w, pix0 + (uint32_t)a.w + 1};
-        int32_t res[C][4];
-#pragma unroll
-        for (int c = 0; c < C; ++c) {
-            int32_t ew[4], eb[4], er[4];
-            expand_packed(sbuf[c], qx, qy, kind, ew, eb, er);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                res[c][q] = merge_sample<T>(kind, mk[q], WV, (int32_t)wp[q][c] << F, ew[q], (int32_t)bp[q][c] << F,
-                                            eb[q], er[q]);
-            }
-        }
-        if (a.level0) {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-#pragma unroll
-                for (int c = 0; c < C; ++c) {
-                    a.level0[(uint64_t)pixq[q] * C + c] = res[c][q];
-                }
-            }
-        }
-        TIn* out0 = reinterpret_cast<TIn*>(a.out) + (int64_t)Y * a.opitch + (int64_t)X * S;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const uint32_t pb = mix32(pixq[q] ^ a.key);
-            TIn o[S];
-#pragma unroll
-            for (int c = 0; c < C; ++c) {
-                const int32_t d = dither_rule(res[c][q], F, nearest, pb >> (8 * c), MAXV);
-                o[c] = uni[q] ? (TIn)d : bp[q][c];
-            }
-            if (S == 4) {
-                o[S - 1] = uni[q] ? (TIn)MAXV : (TIn)0;
-            }
-            st_px<TIn, S, VEC>(out0 + (q >> 1) * a.opitch + (q & 1) * S, o);
-        }
-        if (a.out_alpha) {
-            uint8_t* oa = a.out_alpha + (int64_t)Y * a.oapitch + X;
-            oa[0] = uni[0] ? 255 : 0;
-            oa[1] = uni[1] ? 255 : 0;
-            oa[a.oapitch] = uni[2] ? 255 : 0;
-            oa[a.oapitch + 1] = uni[3] ? 255 : 0;
-        }
+        out0_quad<TIn, T, C, S, AM, VEC>(a, sbuf, X, Y, qx, qy, wp, bp, mk);
         return;
     }
 
@@ -639,10 +655,11 @@ cudaError_t launch_out0(const PlanarView* gw1, const PlanarView* gb1, const Plan
     const double px = npix_f(wv.w, wv.h);
     note_launch("out0", px * (3.0 * wv.stride * esz_f(wv.dtype) + 1.0 + (h.out_alpha.p ? 1.0 : 0.0)) +
                             (gw1 ? 3.0 * pbytes(*gw1) : 0.0));
-    Out0Launch l{cl, a, grid2d(wv.w, wv.h, ETW, ETH), st};
     const bool vec = vec_ok(wv.p, wv.pitch, wv.dtype, wv.stride) &&
                      vec_ok(h.black.p, h.black.pitch, wv.dtype, wv.stride) && vec_ok(h.out, h.opitch, wv.dtype, wv.stride);
-    return dispatch_pixels(wv.dtype, wv.C, wv.stride, alpha_mode_code(h.white_alpha), vec, l);
+    const int am = alpha_mode_code(h.white_alpha);
+    Out0Launch l{cl, a, grid2d(wv.w, wv.h, ETW, ETH), st};
+    return dispatch_pixels(wv.dtype, wv.C, wv.stride, am, vec, l);
 }
 
 }  // namespace enb
