@@ -1,0 +1,114 @@
+"""The C oracle against the reference's own code.
+
+tests/golden/reference_pyramid.npz holds outputs of the reference's
+pyramid.h / blend.h / fixmath.h (compiled unmodified against the project's
+VIGRA/GSL/LCMS2 shims by oracle/reference_build.py; regenerate with
+tests/golden/make_golden.py).  The golden tests run everywhere; the live tests
+also compare random cases when the reference tree is present.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import reference_build as ref
+
+GOLDEN = np.load(Path(__file__).resolve().parent / "golden" / "reference_pyramid.npz")
+
+
+def _pbits(bits):
+    return 16 if bits == 8 else 32
+
+
+@pytest.mark.parametrize("k", range(int(GOLDEN["enblend_count"])))
+def test_golden_enblend_level0(orc, k):
+    """mask GP + white/black LP with alpha holes + blend (incl. mask 128) + collapse."""
+    g = {n: GOLDEN[f"enblend{k}_{n}"] for n in ("white", "white_alpha", "black", "black_alpha", "mask", "level0")}
+    levels, wrap = (int(v) for v in GOLDEN[f"enblend{k}_meta"])
+    res = orc.enblend(g["white"], g["black"], g["mask"], white_alpha=g["white_alpha"],
+                      black_alpha=g["black_alpha"], levels=levels, wrap=bool(wrap), want_level0=True)
+    assert np.array_equal(res["level0"], g["level0"])
+
+
+@pytest.mark.parametrize("k", range(int(GOLDEN["step_count"])))
+def test_golden_reduce_expand(orc, k):
+    bits, wrap, alpha_on = (int(v) for v in GOLDEN[f"reduce{k}_meta"])
+    src = GOLDEN[f"reduce{k}_src"]
+    if alpha_on:
+        dst, da = orc.reduce(src, GOLDEN[f"reduce{k}_alpha"], _pbits(bits), bool(wrap))
+        assert np.array_equal(da, GOLDEN[f"reduce{k}_dst_alpha"])
+    else:
+        dst = orc.reduce(src, None, _pbits(bits), bool(wrap))
+    assert np.array_equal(dst, GOLDEN[f"reduce{k}_dst"])
+    coarse, fine = GOLDEN[f"expand{k}_src"], GOLDEN[f"expand{k}_dst"]
+    assert np.array_equal(orc.expand(coarse, fine, False, _pbits(bits), bool(wrap)), GOLDEN[f"expand{k}_sub"])
+    assert np.array_equal(orc.expand(coarse, fine, True, _pbits(bits), bool(wrap)), GOLDEN[f"expand{k}_add"])
+
+
+@pytest.mark.parametrize("bits", [8, 16])
+def test_golden_conversion_rule(orc, bits):
+    """copyFromPyramidImageIf: outside the dither band the result is fixed
+    (q for f < 1/4, q+1 for f >= 3/4, clamped) and must equal the oracle's;
+    inside it the reference's draw picks q or q+1; alpha-0 pixels untouched."""
+    l0, alpha, out = (GOLDEN[f"convert{bits}_{n}"] for n in ("level0", "alpha", "out"))
+    dt = np.uint8 if bits == 8 else np.uint16
+    maxv = 255 if bits == 8 else 65535
+    q, f = l0 >> 7, l0 & 127
+    band = (f >= 32) & (f < 96)
+    lo, hi = np.clip(q, 0, maxv), np.clip(q + 1, 0, maxv)
+    on = np.broadcast_to(alpha[..., None] != 0, l0.shape)
+    assert np.all(out[~on] == 7)
+    ours = orc.from_fixed(l0, alpha, dt, frac=7, dither="hash", seed=11)
+    assert np.array_equal(out[on & ~band], ours[on & ~band])
+    inb = out[on & band].astype(np.int64)
+    assert np.all((inb == lo[on & band]) | (inb == hi[on & band]))
+    ours_b = ours[on & band].astype(np.int64)
+    assert np.all((ours_b == lo[on & band]) | (ours_b == hi[on & band]))
+
+
+live = pytest.mark.skipif(not ref.available(), reason="reference tree not present")
+
+
+@live
+@pytest.mark.parametrize("seed", range(6))
+def test_live_reduce_expand(orc, seed):
+    rng = np.random.default_rng(seed)
+    for _ in range(12):
+        bits = int(rng.choice([8, 16]))
+        C = int(rng.choice([1, 3]))
+        wrap = bool(rng.integers(2))
+        h, w = int(rng.integers(2, 40)), int(rng.integers(4, 40))
+        maxv = 255 if bits == 8 else 65535
+        src = (rng.integers(0, maxv + 1, size=(h, w, C)) << 7).astype(np.int32)
+        alpha = np.where(rng.random((h, w)) < 0.8, 255, 0).astype(np.uint8) if (C == 3 or rng.random() < 0.5) else None
+        r = ref.reduce(src, alpha, bits, wrap)
+        o = orc.reduce(src, alpha, _pbits(bits), wrap)
+        if alpha is None:
+            assert np.array_equal(o, r)
+        else:
+            assert np.array_equal(o[0], r[0]) and np.array_equal(o[1], r[1])
+        # expand from a source at least 2 wide (the reference's expand reads
+        # uninitialised state for one-column sources, which roiBounds never
+        # lets a pyramid reach)
+        lim = 1 << (14 if bits == 8 else 22)
+        coarse = rng.integers(-lim, lim, size=((h + 1) >> 1, (w + 1) >> 1, C)).astype(np.int32)
+        fine = rng.integers(-lim, lim, size=(h, w, C)).astype(np.int32)
+        for add in (False, True):
+            assert np.array_equal(orc.expand(coarse, fine, add, _pbits(bits), wrap),
+                                  ref.expand(coarse, fine, add, bits, wrap))
+
+
+@live
+@pytest.mark.parametrize("dt", [np.uint8, np.uint16])
+@pytest.mark.parametrize("wrap", [False, True])
+def test_live_enblend(orc, dt, wrap):
+    from enbgpu import synthetic
+    for (h, w, off) in [(90, 120, 80), (33, 50, 20)]:
+        white, black, mask = synthetic.panorama_pair(h, w, off, dt, seed=7)
+        mask[: h // 2, off + 1: off + 6] = 200
+        wa, ba = orc.alpha_of(white), orc.alpha_of(black)
+        W, B = np.ascontiguousarray(white[..., :3]), np.ascontiguousarray(black[..., :3])
+        levels = orc.num_levels(W.shape[1], W.shape[0])
+        want = ref.enblend_level0(W, wa, B, ba, mask, levels, wrap)
+        got = orc.enblend(W, B, mask, white_alpha=wa, black_alpha=ba, wrap=wrap, want_level0=True)["level0"]
+        assert np.array_equal(got, want)

@@ -337,3 +337,51 @@ def test_enblend_in_place(ctx, orc):
     dw, db, dm = _dev(white), _dev(black), _dev(mask)
     out, _ = ctx.enblend(dw, db, dm, out=db, seed=3)
     assert np.array_equal(db.cpu().numpy(), ref["out"])
+
+
+# ---- against the reference's own code (tests/golden/make_golden.py) ------------
+
+def _golden():
+    from pathlib import Path
+    return np.load(Path(__file__).resolve().parent / "golden" / "reference_pyramid.npz")
+
+
+@pytest.mark.parametrize("mode", ["fused", "plain"])
+def test_reference_golden_enblend(ctx, mode):
+    """The collapsed level 0 of the CUDA blend equals the reference's
+    pyramid.h/blend.h result on the stored cases (alpha holes, mask 128, wrap)."""
+    g = _golden()
+    for k in range(int(g["enblend_count"])):
+        levels, wrap = (int(v) for v in g[f"enblend{k}_meta"])
+        W, B = g[f"enblend{k}_white"], g[f"enblend{k}_black"]
+        h, w, _ = W.shape
+        l0 = torch.zeros((h, w, 3), dtype=torch.int32, device="cuda")
+        ctx.enblend(_dev(W), _dev(B), _dev(g[f"enblend{k}_mask"]), white_alpha=_dev(g[f"enblend{k}_white_alpha"]),
+                    black_alpha=_dev(g[f"enblend{k}_black_alpha"]), levels=levels, wrap=bool(wrap), level0=l0,
+                    plain=(mode == "plain"))
+        assert np.array_equal(l0.cpu().numpy(), g[f"enblend{k}_level0"]), k
+
+
+def test_reference_golden_reduce_expand(ctx):
+    import enbgpu
+    g = _golden()
+    for k in range(int(g["step_count"])):
+        bits, wrap, alpha_on = (int(v) for v in g[f"reduce{k}_meta"])
+        dt = "i16" if bits == 8 else "i32"
+        src = g[f"reduce{k}_src"]
+        h, w, c = src.shape
+        p = _pyr(ctx, enbgpu, w, h, c, dt)
+        p.write(0, np.transpose(src, (2, 0, 1)))
+        if alpha_on:
+            da = torch.zeros(((h + 1) >> 1, (w + 1) >> 1), dtype=torch.uint8, device="cuda")
+            ctx.reduce(p, 0, p, 1, wrap=bool(wrap), src_alpha=_dev(g[f"reduce{k}_alpha"]), dst_alpha=da)
+            assert np.array_equal(da.cpu().numpy(), g[f"reduce{k}_dst_alpha"]), k
+        else:
+            ctx.reduce(p, 0, p, 1, wrap=bool(wrap))
+        assert np.array_equal(_hwc(p.read(1)), g[f"reduce{k}_dst"]), k
+        for add, key in ((False, "sub"), (True, "add")):
+            q = _pyr(ctx, enbgpu, w, h, c, dt)
+            q.write(0, np.transpose(g[f"expand{k}_dst"], (2, 0, 1)))
+            q.write(1, np.transpose(g[f"expand{k}_src"], (2, 0, 1)))
+            ctx.expand(q, 1, q, 0, add=add, wrap=bool(wrap))
+            assert np.array_equal(_hwc(q.read(0)), g[f"expand{k}_{key}"]), (k, key)
