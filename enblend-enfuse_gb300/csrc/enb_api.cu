@@ -7,6 +7,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <functional>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -46,6 +47,9 @@ struct enb_ctx {
     std::string table_key;
     void* table_mem = nullptr;
     WeightTables tables{};
+    // host-transfer stream and events of the banded host-buffer path
+    cudaStream_t copy_stream = nullptr;
+    std::vector<cudaEvent_t> io_events;
 };
 
 struct enb_pyramid {
@@ -581,7 +585,11 @@ enb_status stage_in(enb_ctx* ctx, const enb_image* host, Staged& s, bool copy)
     s.dev = *host;
     const int stride = host->planar ? 1 : (host->pix_stride > 0 ? host->pix_stride : host->channels);
     const int64_t row = (int64_t)host->width * stride * (int64_t)dtype_size(host->dtype);
-    const int64_t pitch = round_up(row, 128);
+    // a dense host image keeps its pitch on the device (one contiguous copy)
+    // when that pitch keeps whole pixels at their natural alignment
+    const int64_t px = (int64_t)stride * (int64_t)dtype_size(host->dtype);
+    const int64_t align = stride == 4 ? px : (int64_t)dtype_size(host->dtype);
+    const int64_t pitch = (host->pitch == row && row % align == 0) ? row : round_up(row, 128);
     ENB_CUDA(ctx, s.buf.alloc((size_t)(pitch * host->height), ctx->stream));
     s.dev.data = s.buf.p;
     s.dev.pitch = pitch;
@@ -675,9 +683,21 @@ enb_status enblend_plain(enb_ctx* ctx, const enb_image* white, const enb_image* 
 // levels 1..L-1 of the white, black and mask Gaussian pyramids are built by
 // the reduce chain, then one pass per level forms the Laplacians, blends and
 // collapses into the result pyramid R.
+// Host transfers of a host-buffer call overlapped with the level-0 passes:
+// the inputs arrive on the copy stream in row bands, and the level-1 reduces
+// of the rows a band completes run as soon as it lands; the output leaves in
+// row bands as the level-0 pass finishes them.
+struct BandIO {
+    std::vector<int> in_end;           // input rows present after band b
+    std::vector<cudaEvent_t> in_done;  // recorded on the copy stream after band b
+    int out_rows = 0;                  // output rows per band (a multiple of 16)
+    std::function<enb_status(int, int)> out_ready;  // rows [r0, r1) of the output are queued
+};
+
 enb_status enblend_fused(enb_ctx* ctx, const enb_image* white, const enb_image* white_alpha, const enb_image* black,
                          const enb_image* black_alpha, const enb_image* mask, const enb_image* out,
-                         const enb_image* out_alpha, const enb_fuse_options& o, int32_t* level0)
+                         const enb_image* out_alpha, const enb_fuse_options& o, int32_t* level0,
+                         BandIO* io = nullptr)
 {
     const int w = black->width, h = black->height, C = black->channels, dt = black->dtype;
     const int L = enb_num_levels(w, h, 1, o.levels);
@@ -716,10 +736,27 @@ enb_status enblend_fused(enb_ctx* ctx, const enb_image* white, const enb_image* 
         ENB_CUDA(ctx, awc.alloc(NL, w1, h1, ctx->stream));
         ENB_CUDA(ctx, abc.alloc(NL, w1, h1, ctx->stream));
         // Down sweep (src/enblend.h:384-446: the three Gaussian pyramids).
-        ENB_LAUNCH(ctx, launch_reduce0_alpha2(pixel_view(white), wa, level_view(gw.p, 0), awc.level(0),
-                                              pixel_view(black), ba, level_view(gb.p, 0), abc.level(0), kImageFrac,
-                                              wrap, ctx->stream));
-        ENB_LAUNCH(ctx, launch_reduce0_bytes(byte_plane(mask), mf, level_view(mg.p, 0), wrap, ctx->stream));
+        if (io) {
+            // level-1 tile rows as their source rows arrive
+            int done = 0;
+            for (size_t b = 0; b < io->in_end.size(); ++b) {
+                ENB_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, io->in_done[b], 0));
+                const int ready = reduce_tile_rows_ready(h, h1, io->in_end[b]);
+                if (ready > done) {
+                    ENB_LAUNCH(ctx, launch_reduce0_alpha2(pixel_view(white), wa, level_view(gw.p, 0), awc.level(0),
+                                                          pixel_view(black), ba, level_view(gb.p, 0), abc.level(0),
+                                                          kImageFrac, wrap, ctx->stream, done, ready - done));
+                    ENB_LAUNCH(ctx, launch_reduce0_bytes(byte_plane(mask), mf, level_view(mg.p, 0), wrap, ctx->stream,
+                                                         done, ready - done));
+                    done = ready;
+                }
+            }
+        } else {
+            ENB_LAUNCH(ctx, launch_reduce0_alpha2(pixel_view(white), wa, level_view(gw.p, 0), awc.level(0),
+                                                  pixel_view(black), ba, level_view(gb.p, 0), abc.level(0), kImageFrac,
+                                                  wrap, ctx->stream));
+            ENB_LAUNCH(ctx, launch_reduce0_bytes(byte_plane(mask), mf, level_view(mg.p, 0), wrap, ctx->stream));
+        }
         for (int j = 1; j < NL; ++j) {
             ENB_CHECK(ctx, gw.p->w[j - 1] > 1 && gw.p->h[j - 1] > 1, "reduce: src image too small in reduce");
         }
@@ -789,11 +826,28 @@ enb_status enblend_fused(enb_ctx* ctx, const enb_image* white, const enb_image* 
     h0.dither = o.dither;
     h0.wrap = wrap;
     h0.seed = o.seed;
+    PlanarView g0{}, b0{}, r0{};
     if (NL >= 1) {
-        const PlanarView g0 = level_view(gw.p, 0), b0 = level_view(gb.p, 0), r0 = level_view(rr.p, 0);
-        ENB_LAUNCH(ctx, launch_out0(&g0, &b0, &r0, h0, ctx->stream));
+        g0 = level_view(gw.p, 0);
+        b0 = level_view(gb.p, 0);
+        r0 = level_view(rr.p, 0);
+    }
+    const PlanarView* pg = NL >= 1 ? &g0 : nullptr;
+    const PlanarView* pb = NL >= 1 ? &b0 : nullptr;
+    const PlanarView* pr = NL >= 1 ? &r0 : nullptr;
+    if (io) {
+        // every input row is needed here (a single level reads them only now)
+        if (!io->in_done.empty()) {
+            ENB_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, io->in_done.back(), 0));
+        }
+        // output rows in bands, each copied out as soon as it is written
+        for (int y0 = 0; y0 < h; y0 += io->out_rows) {
+            const int y1 = std::min(h, y0 + io->out_rows);
+            ENB_LAUNCH(ctx, launch_out0(pg, pb, pr, h0, ctx->stream, y0 / 16, (y1 - y0 + 15) / 16));
+            ENB_TRY(io->out_ready(y0, y1));
+        }
     } else {
-        ENB_LAUNCH(ctx, launch_out0(nullptr, nullptr, nullptr, h0, ctx->stream));
+        ENB_LAUNCH(ctx, launch_out0(pg, pb, pr, h0, ctx->stream));
     }
     return ENB_OK;
 }
@@ -930,6 +984,128 @@ enb_status noalloc_scratch(enb_ctx* ctx, void** out)
 // C ABI
 // ============================================================================
 
+// Rows of the input bands of the banded host path (a multiple of the 32
+// source rows of a level-1 tile row) and of its output bands.
+constexpr int kInBandRows = 256;
+constexpr int kOutBandRows = 512;
+
+static cudaError_t ensure_io(enb_ctx* ctx, size_t events)
+{
+    if (!ctx->copy_stream) {
+        const cudaError_t e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            return e;
+        }
+    }
+    while (ctx->io_events.size() < events) {
+        cudaEvent_t ev;
+        const cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            return e;
+        }
+        ctx->io_events.push_back(ev);
+    }
+    return cudaSuccess;
+}
+
+static cudaError_t copy_rows(const enb_image* host, const enb_image& dev, int r0, int r1, cudaMemcpyKind kind,
+                             cudaStream_t st)
+{
+    const int stride = host->planar ? 1 : (host->pix_stride > 0 ? host->pix_stride : host->channels);
+    const size_t row = (size_t)host->width * stride * dtype_size(host->dtype);
+    const char* hp = (const char*)host->data + (int64_t)r0 * host->pitch;
+    const char* dp = (const char*)dev.data + (int64_t)r0 * dev.pitch;
+    if (kind == cudaMemcpyHostToDevice) {
+        return cudaMemcpy2DAsync((void*)dp, dev.pitch, hp, host->pitch, row, r1 - r0, kind, st);
+    }
+    return cudaMemcpy2DAsync((void*)hp, host->pitch, dp, dev.pitch, row, r1 - r0, kind, st);
+}
+
+// enblend on host buffers with the transfers overlapped: input row bands go
+// to the device on the copy stream while the level-1 reduces consume the
+// bands that have landed, and output row bands come back while the level-0
+// pass writes the next ones.  The call returns once the output is in host
+// memory, like the unbanded path.
+enb_status enblend_host_banded(enb_ctx* ctx, const enb_image* white, const enb_image* white_alpha,
+                               const enb_image* black, const enb_image* black_alpha, const enb_image* mask,
+                               const enb_image* out, const enb_image* out_alpha, const enb_fuse_options& o)
+{
+    const int w = black->width, h = black->height, C = black->channels;
+    const int nin = (h + kInBandRows - 1) / kInBandRows;
+    const int nout = (h + kOutBandRows - 1) / kOutBandRows;
+    ENB_CUDA(ctx, ensure_io(ctx, (size_t)(nin + nout + 2)));
+    cudaStream_t cs = ctx->copy_stream;
+    cudaEvent_t* ev = ctx->io_events.data();
+
+    Staged sw, sb, swa, sba, sm, soa;
+    ENB_TRY(stage_in(ctx, white, sw, false));
+    ENB_TRY(stage_in(ctx, black, sb, false));
+    ENB_TRY(stage_in(ctx, mask, sm, false));
+    const bool has_wa = white_alpha && white_alpha->data, has_ba = black_alpha && black_alpha->data;
+    if (has_wa) {
+        ENB_TRY(stage_in(ctx, white_alpha, swa, false));
+    }
+    if (has_ba) {
+        ENB_TRY(stage_in(ctx, black_alpha, sba, false));
+    }
+    const bool want_alpha = out_alpha && out_alpha->data;
+    if (want_alpha) {
+        ENB_TRY(stage_in(ctx, out_alpha, soa, false));
+    }
+    DevBuf l0;
+    if (o.level0_out) {
+        ENB_CUDA(ctx, l0.alloc((size_t)w * h * C * 4, ctx->stream));
+    }
+    // the staging buffers come from the stream-ordered pool of the main stream
+    ENB_CUDA(ctx, cudaEventRecord(ev[nin + nout], ctx->stream));
+    ENB_CUDA(ctx, cudaStreamWaitEvent(cs, ev[nin + nout], 0));
+
+    BandIO io;
+    for (int b = 0; b < nin; ++b) {
+        const int r0 = b * kInBandRows, r1 = std::min(h, r0 + kInBandRows);
+        ENB_CUDA(ctx, copy_rows(white, sw.dev, r0, r1, cudaMemcpyHostToDevice, cs));
+        ENB_CUDA(ctx, copy_rows(black, sb.dev, r0, r1, cudaMemcpyHostToDevice, cs));
+        ENB_CUDA(ctx, copy_rows(mask, sm.dev, r0, r1, cudaMemcpyHostToDevice, cs));
+        if (has_wa) {
+            ENB_CUDA(ctx, copy_rows(white_alpha, swa.dev, r0, r1, cudaMemcpyHostToDevice, cs));
+        }
+        if (has_ba) {
+            ENB_CUDA(ctx, copy_rows(black_alpha, sba.dev, r0, r1, cudaMemcpyHostToDevice, cs));
+        }
+        ENB_CUDA(ctx, cudaEventRecord(ev[b], cs));
+        io.in_end.push_back(r1);
+        io.in_done.push_back(ev[b]);
+    }
+    int next_out = 0;
+    io.out_rows = kOutBandRows;
+    io.out_ready = [&](int y0, int y1) -> enb_status {
+        cudaEvent_t e = ev[nin + next_out++];
+        ENB_CUDA(ctx, cudaEventRecord(e, ctx->stream));
+        ENB_CUDA(ctx, cudaStreamWaitEvent(cs, e, 0));
+        ENB_CUDA(ctx, copy_rows(out, sb.dev, y0, y1, cudaMemcpyDeviceToHost, cs));
+        if (want_alpha) {
+            ENB_CUDA(ctx, copy_rows(out_alpha, soa.dev, y0, y1, cudaMemcpyDeviceToHost, cs));
+        }
+        return ENB_OK;
+    };
+    const enb_status st = enblend_fused(ctx, &sw.dev, has_wa ? &swa.dev : nullptr, &sb.dev, has_ba ? &sba.dev : nullptr,
+                                        &sm.dev, &sb.dev, want_alpha ? &soa.dev : nullptr, o, (int32_t*)l0.p, &io);
+    if (st != ENB_OK) {
+        cudaStreamSynchronize(cs);
+        cudaStreamSynchronize(ctx->stream);
+        return st;
+    }
+    if (o.level0_out) {
+        ENB_CUDA(ctx, cudaMemcpyAsync(o.level0_out, l0.p, (size_t)w * h * C * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    // the main stream (and with it the frees of the staging buffers) waits
+    // for the last output band
+    ENB_CUDA(ctx, cudaEventRecord(ev[nin + nout + 1], cs));
+    ENB_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ev[nin + nout + 1], 0));
+    ENB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return ENB_OK;
+}
+
 extern "C" {
 
 int enb_abi_version(void) { return ENBGPU_ABI_VERSION; }
@@ -973,6 +1149,13 @@ enb_status enb_destroy(enb_ctx* ctx)
     prof_resolve(ctx);
     for (cudaEvent_t e : ctx->pool) {
         cudaEventDestroy(e);
+    }
+    for (cudaEvent_t e : ctx->io_events) {
+        cudaEventDestroy(e);
+    }
+    if (ctx->copy_stream) {
+        cudaStreamSynchronize(ctx->copy_stream);
+        cudaStreamDestroy(ctx->copy_stream);
     }
     delete ctx;
     return ENB_OK;
@@ -1485,6 +1668,9 @@ enb_status enb_enblend(enb_ctx* ctx, const enb_image* white, const enb_image* wh
     };
     if (!o.host_buffers) {
         return run(white, white_alpha, black, black_alpha, mask, out, out_alpha, (int32_t*)o.level0_out);
+    }
+    if (!o.plain && alpha_source(white, white_alpha).mode == alpha_source(black, black_alpha).mode) {
+        return enblend_host_banded(ctx, white, white_alpha, black, black_alpha, mask, out, out_alpha, o);
     }
     // Host buffers: the result is formed in place in the device copy of the
     // black image and copied back from there.

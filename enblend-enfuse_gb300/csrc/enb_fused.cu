@@ -186,6 +186,7 @@ struct Out0Args {
     uint64_t seed;
     uint32_t key;                // dither_key(seed)
     int32_t maxv;
+    int ty0;                     // first tile row (16 rows) of the launch
 };
 
 // Level-0 output of the interior quad (X, Y) (tile position qx, qy) from its
@@ -270,7 +271,7 @@ __global__ void __launch_bounds__(256, 3) k_out0(CoarseLevels cl, Out0Args a)
     int32_t (*ss)[ESH][ESW] = reinterpret_cast<int32_t (*)[ESH][ESW]>(&sbuf[0][0][0]);
     griddep_wait();
     griddep_launch();
-    const int X0 = blockIdx.x * ETW, Y0 = blockIdx.y * ETH;
+    const int X0 = blockIdx.x * ETW, Y0 = (blockIdx.y + a.ty0) * ETH;
     const int I0 = X0 >> 1, J0 = Y0 >> 1;
     const int qx = threadIdx.x % 32, qy = threadIdx.x / 32;
     const int i = I0 + qx, j = J0 + qy;
@@ -396,6 +397,7 @@ struct Reduce0Launch {
     int frac;
     int wrap;
     cudaStream_t st;
+    int ty0, nty;
     template <typename TIn, typename T, int C, int S, int AM, bool VEC>
     void operator()() const
     {
@@ -406,7 +408,7 @@ struct Reduce0Launch {
             jobs.j[i] = ReduceJob<Src, T>{Src{(const TIn*)s[k]->p, s[k]->pitch, ap[k], apitch[k], lo[k], hi[k], frac},
                                           (T*)d[k]->p, d[k]->pitch, d[k]->plane, da[k]->p, da[k]->pitch};
         }
-        launch_reduce_jobs<Src, T, C, true>(jobs, n, s[0]->w, s[0]->h, d[0]->w, d[0]->h, wrap, st);
+        launch_reduce_jobs<Src, T, C, true>(jobs, n, s[0]->w, s[0]->h, d[0]->w, d[0]->h, wrap, st, ty0, nty);
     }
 };
 
@@ -470,8 +472,28 @@ static double reduce0_bytes(const PixelView& s, const AlphaSrc& a, const PlanarV
            pbytes(d) + npix_f(d.w, d.h);
 }
 
+// Share of a level's tile rows a banded launch covers (for the byte counts).
+static double row_share(int dh, int ty0, int nty)
+{
+    const int total = reduce_tile_rows(dh);
+    const int n = nty < 0 ? total - ty0 : nty;
+    return total > 0 ? (double)std::max(n, 0) / total : 0.0;
+}
+
+int reduce_tile_rows_of(int dh) { return reduce_tile_rows(dh); }
+
+int reduce_tile_rows_ready(int sh, int dh, int rows_ready)
+{
+    // destination tile row ty reads source rows up to 2 * (16 ty + 15) + 2
+    if (rows_ready >= sh) {
+        return reduce_tile_rows(dh);
+    }
+    const int n = rows_ready >= 2 * RDH + 1 ? (rows_ready - (2 * RDH + 1)) / (2 * RDH) + 1 : 0;
+    return std::min(n, reduce_tile_rows(dh));
+}
+
 static cudaError_t reduce0_launch(int n, const PixelView* const* s, const AlphaSrc* const* a, const PlanarView* const* d,
-                                  const BytePlane* const* da, int frac, int wrap, cudaStream_t st)
+                                  const BytePlane* const* da, int frac, int wrap, cudaStream_t st, int ty0, int nty)
 {
     Reduce0Launch l{};
     double bytes = 0.0;
@@ -491,48 +513,64 @@ static cudaError_t reduce0_launch(int n, const PixelView* const* s, const AlphaS
     l.frac = frac;
     l.wrap = wrap;
     l.st = st;
-    note_launch("reduce0_alpha", bytes);
+    l.ty0 = ty0;
+    l.nty = nty;
+    note_launch("reduce0_alpha", bytes * row_share(d[0]->h, ty0, nty));
     return dispatch_pixels(s[0]->dtype, s[0]->C, s[0]->stride, alpha_mode_code(*a[0]), vec, l);
 }
 
-cudaError_t launch_reduce0_alpha(const PixelView& s, const AlphaSrc& a, int frac, const PlanarView& d,
-                                 const BytePlane& da, int wrap, cudaStream_t st)
+static cudaError_t reduce0_single(const PixelView& s, const AlphaSrc& a, int frac, const PlanarView& d,
+                                  const BytePlane& da, int wrap, cudaStream_t st, int ty0, int nty)
 {
     const PixelView* sv[1] = {&s};
     const AlphaSrc* av[1] = {&a};
     const PlanarView* dv[1] = {&d};
     const BytePlane* dav[1] = {&da};
-    return reduce0_launch(1, sv, av, dv, dav, frac, wrap, st);
+    return reduce0_launch(1, sv, av, dv, dav, frac, wrap, st, ty0, nty);
+}
+
+cudaError_t launch_reduce0_alpha(const PixelView& s, const AlphaSrc& a, int frac, const PlanarView& d,
+                                 const BytePlane& da, int wrap, cudaStream_t st)
+{
+    return reduce0_single(s, a, frac, d, da, wrap, st, 0, -1);
 }
 
 cudaError_t launch_reduce0_alpha2(const PixelView& s0, const AlphaSrc& a0, const PlanarView& d0, const BytePlane& da0,
                                   const PixelView& s1, const AlphaSrc& a1, const PlanarView& d1, const BytePlane& da1,
-                                  int frac, int wrap, cudaStream_t st)
+                                  int frac, int wrap, cudaStream_t st, int ty0, int nty)
 {
     const bool same = s0.w == s1.w && s0.h == s1.h && s0.dtype == s1.dtype && s0.C == s1.C &&
                       s0.stride == s1.stride && a0.mode == a1.mode && a0.lo == a1.lo && a0.hi == a1.hi &&
                       d0.w == d1.w && d0.h == d1.h && d0.dtype == d1.dtype && d0.C == d1.C;
     if (!same) {
-        const cudaError_t e = launch_reduce0_alpha(s0, a0, frac, d0, da0, wrap, st);
-        return e != cudaSuccess ? e : launch_reduce0_alpha(s1, a1, frac, d1, da1, wrap, st);
+        const cudaError_t e = reduce0_single(s0, a0, frac, d0, da0, wrap, st, ty0, nty);
+        return e != cudaSuccess ? e : reduce0_single(s1, a1, frac, d1, da1, wrap, st, ty0, nty);
     }
     const PixelView* sv[2] = {&s0, &s1};
     const AlphaSrc* av[2] = {&a0, &a1};
     const PlanarView* dv[2] = {&d0, &d1};
     const BytePlane* dav[2] = {&da0, &da1};
-    return reduce0_launch(2, sv, av, dv, dav, frac, wrap, st);
+    return reduce0_launch(2, sv, av, dv, dav, frac, wrap, st, ty0, nty);
 }
 
-cudaError_t launch_reduce0_bytes(const BytePlane& s, int frac, const PlanarView& d, int wrap, cudaStream_t st)
+template <typename TD>
+static void reduce0_bytes_launch(const BytePlane& s, int frac, const PlanarView& d, int wrap, cudaStream_t st, int ty0,
+                                 int nty)
 {
-    note_launch("reduce0_mask", npix_f(s.w, s.h) + pbytes(d));
-    ByteSource src{s.p, s.pitch, frac};
+    ReduceJobs<ByteSource, TD> jobs{};
+    jobs.j[0] = ReduceJob<ByteSource, TD>{ByteSource{s.p, s.pitch, frac}, (TD*)d.p, d.pitch, 0, nullptr, 0};
+    jobs.j[1] = jobs.j[0];
+    launch_reduce_jobs<ByteSource, TD, 1, false>(jobs, 1, s.w, s.h, d.w, d.h, wrap, st, ty0, nty);
+}
+
+cudaError_t launch_reduce0_bytes(const BytePlane& s, int frac, const PlanarView& d, int wrap, cudaStream_t st, int ty0,
+                                 int nty)
+{
+    note_launch("reduce0_mask", (npix_f(s.w, s.h) + pbytes(d)) * row_share(d.h, ty0, nty));
     if (d.dtype == ENB_I16) {
-        launch_reduce_tiles<ByteSource, int16_t, 1, false>(src, s.w, s.h, (int16_t*)d.p, d.pitch, 0, d.w, d.h, nullptr,
-                                                           0, wrap, st);
+        reduce0_bytes_launch<int16_t>(s, frac, d, wrap, st, ty0, nty);
     } else {
-        launch_reduce_tiles<ByteSource, int32_t, 1, false>(src, s.w, s.h, (int32_t*)d.p, d.pitch, 0, d.w, d.h, nullptr,
-                                                           0, wrap, st);
+        reduce0_bytes_launch<int32_t>(s, frac, d, wrap, st, ty0, nty);
     }
     return cudaGetLastError();
 }
@@ -611,7 +649,7 @@ cudaError_t launch_up_level(const PlanarView& gw1, const PlanarView& gb1, const 
 }
 
 cudaError_t launch_out0(const PlanarView* gw1, const PlanarView* gb1, const PlanarView* r1, const Out0Host& h,
-                        cudaStream_t st)
+                        cudaStream_t st, int ty0, int nty)
 {
     const PixelView& wv = h.white;
     Out0Args a{};
@@ -653,12 +691,24 @@ cudaError_t launch_out0(const PlanarView* gw1, const PlanarView* gb1, const Plan
         cl = coarse_of(*gw1, *gb1, *r1);
     }
     const double px = npix_f(wv.w, wv.h);
-    note_launch("out0", px * (3.0 * wv.stride * esz_f(wv.dtype) + 1.0 + (h.out_alpha.p ? 1.0 : 0.0)) +
-                            (gw1 ? 3.0 * pbytes(*gw1) : 0.0));
+    {
+        const int rows = (wv.h + ETH - 1) / ETH;
+        const double share = (double)(nty < 0 ? rows - ty0 : nty) / rows;
+        note_launch("out0", share * (px * (3.0 * wv.stride * esz_f(wv.dtype) + 1.0 + (h.out_alpha.p ? 1.0 : 0.0)) +
+                                     (gw1 ? 3.0 * pbytes(*gw1) : 0.0)));
+    }
     const bool vec = vec_ok(wv.p, wv.pitch, wv.dtype, wv.stride) &&
                      vec_ok(h.black.p, h.black.pitch, wv.dtype, wv.stride) && vec_ok(h.out, h.opitch, wv.dtype, wv.stride);
     const int am = alpha_mode_code(h.white_alpha);
-    Out0Launch l{cl, a, grid2d(wv.w, wv.h, ETW, ETH), st};
+    const int rows = (wv.h + ETH - 1) / ETH;
+    if (nty < 0) {
+        nty = rows - ty0;
+    }
+    if (nty <= 0) {
+        return cudaSuccess;
+    }
+    a.ty0 = ty0;
+    Out0Launch l{cl, a, dim3((unsigned)((wv.w + ETW - 1) / ETW), (unsigned)nty), st};
     return dispatch_pixels(wv.dtype, wv.C, wv.stride, am, vec, l);
 }
 

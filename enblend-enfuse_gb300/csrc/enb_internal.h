@@ -182,15 +182,21 @@ cudaError_t launch_reduce0_alpha(const PixelView& src, const AlphaSrc& a, int fr
 // when their formats, alpha sources or geometries differ).
 cudaError_t launch_reduce0_alpha2(const PixelView& s0, const AlphaSrc& a0, const PlanarView& d0, const BytePlane& da0,
                                   const PixelView& s1, const AlphaSrc& a1, const PlanarView& d1, const BytePlane& da1,
-                                  int frac, int wrap, cudaStream_t st);
-cudaError_t launch_reduce0_bytes(const BytePlane& src, int frac, const PlanarView& dst, int wrap, cudaStream_t st);
+                                  int frac, int wrap, cudaStream_t st, int ty0 = 0, int nty = -1);
+cudaError_t launch_reduce0_bytes(const BytePlane& src, int frac, const PlanarView& dst, int wrap, cudaStream_t st,
+                                 int ty0 = 0, int nty = -1);
+// Destination tile rows (16 each) of a reduce into a level of height dh.
+int reduce_tile_rows_of(int dh);
+// A reduced level's tile rows whose source rows [0, rows_ready) are all
+// present (rows_ready >= sh: every tile row).
+int reduce_tile_rows_ready(int sh, int dh, int rows_ready);
 cudaError_t launch_blend_into(const PlanarView& mask, const PlanarView& gw, const PlanarView& gb,
                               const PlanarView& r, int32_t white_value, cudaStream_t st);
 cudaError_t launch_up_level(const PlanarView& gw1, const PlanarView& gb1, const PlanarView& r1,
                             const PlanarView& mask, const PlanarView& gw, const PlanarView& gb,
                             const PlanarView& r, int32_t white_value, int wrap, cudaStream_t st);
 cudaError_t launch_out0(const PlanarView* gw1, const PlanarView* gb1, const PlanarView* r1, const Out0Host& h,
-                        cudaStream_t st);
+                        cudaStream_t st, int ty0 = 0, int nty = -1);
 cudaError_t launch_coarse(const CoarseHost& h, cudaStream_t st);
 
 }  // namespace enb

@@ -81,6 +81,7 @@ struct ReduceJob {
 template <class Src, typename TD>
 struct ReduceJobs {
     ReduceJob<Src, TD> j[2];
+    int ty0;  // first destination tile row of the launch
 };
 
 // Phase 1 for one column item: vertical sums of destination rows r0..r0+7.
@@ -252,15 +253,26 @@ __global__ void __launch_bounds__(RTHREADS, 2) k_reduce(ReduceJobs<Src, TD> jobs
     griddep_wait();
     griddep_launch();
     const ReduceJob<Src, TD> job = blockIdx.z == 0 ? jobs.j[0] : jobs.j[1];
-    reduce_tile<Src, TD, C, ALPHA>(job, blockIdx.x * RDW, blockIdx.y * RDH, sw, sh, dw, dh, wrap, V);
+    reduce_tile<Src, TD, C, ALPHA>(job, blockIdx.x * RDW, (blockIdx.y + jobs.ty0) * RDH, sw, sh, dw, dh, wrap, V);
 }
 
-// One launch over njobs (1 or 2) jobs of the same geometry.
+// Destination tile rows of the reduce (16 rows each).
+inline int reduce_tile_rows(int dh) { return (dh + RDH - 1) / RDH; }
+
+// One launch over njobs (1 or 2) jobs of the same geometry, covering the
+// destination tile rows [ty0, ty0 + nty) (nty < 0: all).
 template <class Src, typename TD, int C, bool ALPHA>
-inline void launch_reduce_jobs(const ReduceJobs<Src, TD>& jobs, int njobs, int sw, int sh, int dw, int dh, int wrap,
-                               cudaStream_t st)
+inline void launch_reduce_jobs(ReduceJobs<Src, TD> jobs, int njobs, int sw, int sh, int dw, int dh, int wrap,
+                               cudaStream_t st, int ty0 = 0, int nty = -1)
 {
-    const dim3 g((unsigned)((dw + RDW - 1) / RDW), (unsigned)((dh + RDH - 1) / RDH), (unsigned)njobs);
+    if (nty < 0) {
+        nty = reduce_tile_rows(dh) - ty0;
+    }
+    if (nty <= 0) {
+        return;
+    }
+    jobs.ty0 = ty0;
+    const dim3 g((unsigned)((dw + RDW - 1) / RDW), (unsigned)nty, (unsigned)njobs);
     (void)launch_pdl(k_reduce<Src, TD, C, ALPHA>, g, dim3(RTHREADS), st, jobs, sw, sh, dw, dh, wrap);
 }
 

@@ -385,3 +385,25 @@ def test_reference_golden_reduce_expand(ctx):
             q.write(1, np.transpose(g[f"expand{k}_src"], (2, 0, 1)))
             ctx.expand(q, 1, q, 0, add=add, wrap=bool(wrap))
             assert np.array_equal(_hwc(q.read(0)), g[f"expand{k}_{key}"]), (k, key)
+
+
+@pytest.mark.parametrize("dt", [np.uint8, np.uint16])
+@pytest.mark.parametrize("planes", [False, True])
+def test_enblend_host_bands(ctx, orc, dt, planes):
+    """Host buffers: inputs copied in 256-row bands while the level-1 reduces
+    run, output copied back in 512-row bands (1100 rows: 5 and 3 bands)."""
+    from enbgpu import synthetic
+    white, black, mask = synthetic.panorama_pair(1100, 300, 200, dt, seed=41)
+    mask[100:700, 210:240] = 90
+    kw = {}
+    if planes:
+        wa, ba = orc.alpha_of(white).copy(), orc.alpha_of(black)
+        wa[300:340, 220:260] = 0
+        white, black = np.ascontiguousarray(white[..., :3]), np.ascontiguousarray(black[..., :3])
+        kw = dict(white_alpha=wa, black_alpha=ba)
+    ref = orc.enblend(white, black, mask, seed=6, want_level0=True, **kw)
+    l0 = np.zeros(black.shape[:2] + (3,), np.int32)
+    out, oa = ctx.enblend(white, black, mask, seed=6, level0=l0, **kw)
+    assert np.array_equal(l0, ref["level0"])
+    assert np.array_equal(out, ref["out"])
+    assert np.array_equal(oa, ref["alpha"])
