@@ -246,7 +246,7 @@ __device__ __forceinline__ void reduce_tile(const ReduceJob<Src, TD>& job, int X
 }
 
 template <class Src, typename TD, int C, bool ALPHA>
-__global__ void __launch_bounds__(RTHREADS, 2) k_reduce(ReduceJobs<Src, TD> jobs, int sw, int sh, int dw, int dh,
+__global__ void __launch_bounds__(RTHREADS, 3) k_reduce(ReduceJobs<Src, TD> jobs, int sw, int sh, int dw, int dh,
                                                         int wrap)
 {
     __shared__ __align__(16) int32_t V[ReduceSmem<C, ALPHA>::NV][RDH][RVP];
