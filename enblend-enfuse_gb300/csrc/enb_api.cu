@@ -211,7 +211,8 @@ int64_t round_up(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
 
 bool planar_ok(const enb_image* im)
 {
-    return im && im->data && im->planar && (im->dtype == ENB_I16 || im->dtype == ENB_I32) && im->width > 0 &&
+    return im && im->data && im->planar && (im->dtype == ENB_I16 || im->dtype == ENB_I32 || im->dtype == ENB_F32) &&
+           im->width > 0 &&
            im->height > 0 && im->channels >= 1 && im->pitch % (int64_t)dtype_size(im->dtype) == 0 &&
            im->plane_pitch % (int64_t)dtype_size(im->dtype) == 0 && im->pitch >= im->width * (int64_t)dtype_size(im->dtype);
 }
@@ -224,8 +225,8 @@ PlanarView planar_view(const enb_image* im)
 
 bool pixels_ok(const enb_image* im)
 {
-    if (!im || !im->data || im->planar || (im->dtype != ENB_U8 && im->dtype != ENB_U16) || im->width <= 0 ||
-        im->height <= 0) {
+    if (!im || !im->data || im->planar || (im->dtype != ENB_U8 && im->dtype != ENB_U16 && im->dtype != ENB_F32) ||
+        im->width <= 0 || im->height <= 0) {
         return false;
     }
     if (im->channels != 1 && im->channels != 3) {
@@ -281,6 +282,8 @@ AlphaSrc alpha_source(const enb_image* img, const enb_image* alpha)
         const uint32_t maxv = img->dtype == ENB_U8 ? 255u : 65535u;
         a.lo = (uint32_t)(maxv / 2.0);  // static_cast of range.second / 2.0
         a.hi = maxv;
+        a.flo = 0.5f;  // float images: range (0, 1), src/common.h:594
+        a.fhi = 1.0f;
     } else {
         a.mode = kAlphaOpaque;
     }
@@ -293,7 +296,8 @@ enb_status pyramid_alloc(enb_ctx* ctx, int levels, int w, int h, int C, int dtyp
 {
     ENB_CHECK(ctx, levels >= 1 && levels <= kMaxLevels, "pyramid: levels outside 1..29");
     ENB_CHECK(ctx, w > 0 && h > 0 && (C == 1 || C == 3), "pyramid: bad size or channel count");
-    ENB_CHECK(ctx, dtype == ENB_I16 || dtype == ENB_I32, "pyramid: dtype must be ENB_I16 or ENB_I32");
+    ENB_CHECK(ctx, dtype == ENB_I16 || dtype == ENB_I32 || dtype == ENB_F32,
+              "pyramid: dtype must be ENB_I16, ENB_I32 or ENB_F32");
     std::unique_ptr<enb_pyramid> p(new enb_pyramid());
     p->levels = levels;
     p->C = C;
@@ -526,9 +530,73 @@ enb_status check_params(enb_ctx* ctx, const enb_enfuse_params* p, int w, int h)
     return ENB_OK;
 }
 
+// Effective width of the built-in exposure weight functions: the user width
+// rescaled to the Gaussian's FWHM (src/exposure_weight.h:56-116).
+double exposure_effective_width(int fn, double width)
+{
+    switch (fn) {
+    case ENB_EXP_LORENTZIAN: return width * kFwhmGaussian / kFwhmLorentzian;
+    case ENB_EXP_HALF_SINE: return width * kFwhmGaussian / kFwhmHalfSine;
+    case ENB_EXP_FULL_SINE: return width * kFwhmGaussian / kFwhmFullSine;
+    case ENB_EXP_BISQUARE: return width * kFwhmGaussian / kFwhmBisquare;
+    default: return width;
+    }
+}
+
+// Scale of float samples: enb_enfuse_params.float_range, 0 = the reference's
+// NumericTraits<float>::max().
+double float_range_of(const enb_enfuse_params* prm)
+{
+    return prm->float_range > 0.0 ? prm->float_range : 3.4028234663852886e38;
+}
+
+enb_status alpha_plane(enb_ctx* ctx, const enb_image* img, const enb_image* alpha, DevBuf& buf, BytePlane& out);
+
+enb_status enfuse_mask_float(enb_ctx* ctx, const enb_enfuse_params* prm, const enb_image* src,
+                             const enb_image* alpha, const FloatPlane& out)
+{
+    ENB_TRY(build_tables(ctx, prm, 1u));  // p log p tables of the entropy
+    FloatWeightParams wp{};
+    wp.use_exposure = prm->w_exposure > 0.0;
+    wp.use_contrast = prm->w_contrast > 0.0;
+    wp.use_saturation = prm->w_saturation > 0.0;
+    wp.use_entropy = prm->w_entropy > 0.0;
+    wp.contrast_window = prm->contrast_window;
+    wp.entropy_window = prm->entropy_window;
+    wp.gray_projector = prm->gray_projector;
+    wp.exp_function = prm->exp_function;
+    if (prm->gray_projector == ENB_GRAY_MIXER) {
+        const double sm = prm->mixer[0] + prm->mixer[1] + prm->mixer[2];
+        for (int i = 0; i < 3; ++i) {
+            wp.mixer[i] = prm->mixer[i] / sm;
+        }
+    }
+    wp.w_exposure = (float)prm->w_exposure;
+    wp.w_contrast = (float)prm->w_contrast;
+    wp.w_saturation = (float)prm->w_saturation;
+    wp.w_entropy = (float)prm->w_entropy;
+    const double range = float_range_of(prm);
+    wp.range = (float)range;
+    wp.opt_hi = (float)prm->exp_optimum;
+    wp.opt_lo = (float)(prm->exp_optimum - (double)wp.opt_hi);
+    const double inv_width = 1.0 / exposure_effective_width(prm->exp_function, prm->exp_width);
+    wp.inv_hi = (float)inv_width;
+    wp.inv_lo = (float)(inv_width - (double)wp.inv_hi);
+    const PixelView pv = pixel_view(src);
+    DevBuf abuf;
+    BytePlane ap;
+    ENB_TRY(alpha_plane(ctx, src, alpha, abuf, ap));
+    ENB_LAUNCH(ctx, launch_f_enfuse_mask(FloatPixelView{(const float*)pv.p, pv.pitch, pv.w, pv.h, pv.C, pv.stride}, ap,
+                                         wp, ctx->tables, out, ctx->stream));
+    return ENB_OK;
+}
+
 enb_status enfuse_mask_impl(enb_ctx* ctx, const enb_enfuse_params* prm, const enb_image* src,
                             const enb_image* alpha, const FloatPlane& out)
 {
+    if (src->dtype == ENB_F32) {
+        return enfuse_mask_float(ctx, prm, src, alpha, out);
+    }
     const uint32_t maxv = src->dtype == ENB_U8 ? 255u : 65535u;
     ENB_TRY(build_tables(ctx, prm, maxv));
     WeightParams wp{};
@@ -553,7 +621,10 @@ enb_status enfuse_mask_impl(enb_ctx* ctx, const enb_enfuse_params* prm, const en
     return ENB_OK;
 }
 
-int fixed_bits_image(int dt) { return dt == ENB_U8 ? ENB_I16 : ENB_I32; }
+// Pyramid types of EnblendNumericTraits (src/numerictraits.h:168-185): u8
+// Int16 9.7 image and mask pyramids; u16 Int32 17.7 image, Int32 9.15 mask;
+// float: FP32 image pyramid (the reference's double), Int32 9.15 mask.
+int fixed_bits_image(int dt) { return dt == ENB_U8 ? ENB_I16 : (dt == ENB_F32 ? ENB_F32 : ENB_I32); }
 int fixed_bits_mask(int dt) { return dt == ENB_U8 ? ENB_I16 : ENB_I32; }
 int mask_frac(int dt) { return dt == ENB_U8 ? 7 : 15; }
 constexpr int kImageFrac = 7;
@@ -1344,16 +1415,22 @@ enb_status enb_to_pyramid(enb_ctx* ctx, const enb_image* src, const enb_image* d
     if (!ctx) {
         return ENB_ERR_INVALID;
     }
-    ENB_CHECK(ctx, planar_ok(dst), "to_pyramid: dst must be a planar I16/I32 level");
+    ENB_CHECK(ctx, planar_ok(dst), "to_pyramid: dst must be a planar I16/I32/F32 level");
     ENB_CHECK(ctx, frac >= 0 && frac <= 24, "to_pyramid: frac_bits outside 0..24");
     ENB_CHECK(ctx, src && src->width == dst->width && src->height == dst->height, "to_pyramid: size mismatch");
+    if (dst->dtype == ENB_F32) {
+        ENB_CHECK(ctx, pixels_ok(src) && src->dtype == ENB_F32 && src->channels == dst->channels,
+                  "to_pyramid: an F32 level takes an interleaved F32 image of its channel count");
+        ENB_LAUNCH(ctx, launch_to_fixed(pixel_view(src), planar_view(dst), frac, ctx->stream));
+        return ENB_OK;
+    }
     if (src->dtype == ENB_F32) {
         ENB_CHECK(ctx, src->channels == 1 && dst->channels == 1 && floats_ok(src, src->width, src->height),
                   "to_pyramid: F32 sources are single-channel planes");
         ENB_LAUNCH(ctx, launch_float_to_fixed(float_plane(src), planar_view(dst), frac, ctx->stream));
         return ENB_OK;
     }
-    ENB_CHECK(ctx, pixels_ok(src), "to_pyramid: src must be interleaved U8/U16");
+    ENB_CHECK(ctx, pixels_ok(src) && src->dtype != ENB_F32, "to_pyramid: src must be interleaved U8/U16");
     ENB_CHECK(ctx, src->channels == dst->channels, "to_pyramid: channel mismatch");
     ENB_LAUNCH(ctx, launch_to_fixed(pixel_view(src), planar_view(dst), frac, ctx->stream));
     return ENB_OK;
@@ -1436,8 +1513,16 @@ enb_status enb_from_pyramid(enb_ctx* ctx, const enb_image* src, const enb_image*
     ENB_CHECK(ctx, planar_ok(src), "from_pyramid: planar source level expected");
     ENB_CHECK(ctx, pixels_ok(dst) && dst->width == src->width && dst->height == src->height &&
                        dst->channels == src->channels,
-              "from_pyramid: dst must be an interleaved U8/U16 image of the level size");
+              "from_pyramid: dst must be an interleaved U8/U16/F32 image of the level size");
     ENB_CHECK(ctx, bytes_ok(alpha, src->width, src->height), "from_pyramid: alpha must be U8 of the level size");
+    ENB_CHECK(ctx, (src->dtype == ENB_F32) == (dst->dtype == ENB_F32),
+              "from_pyramid: F32 levels convert to F32 pixels, fixed point to U8/U16");
+    if (src->dtype == ENB_F32) {
+        const PixelView fv = pixel_view(dst);
+        ENB_LAUNCH(ctx, launch_from_fixed(planar_view(src), byte_plane(alpha), dst->data, fv.pitch, dst->dtype,
+                                          fv.stride, 0, 0, 0, ctx->stream));
+        return ENB_OK;
+    }
     ENB_CHECK(ctx, frac >= 2 && frac <= 24, "from_pyramid: frac_bits must be 2..24");
     ENB_CHECK(ctx, dither == ENB_DITHER_HASH || dither == ENB_DITHER_NEAREST, "from_pyramid: unknown dither mode");
     const PixelView dv = pixel_view(dst);
@@ -1566,7 +1651,7 @@ enb_status enb_enfuse_mask(enb_ctx* ctx, const enb_enfuse_params* prm, const enb
     if (!ctx) {
         return ENB_ERR_INVALID;
     }
-    ENB_CHECK(ctx, pixels_ok(src), "enfuse_mask: src must be interleaved U8/U16 (1 or 3 channels)");
+    ENB_CHECK(ctx, pixels_ok(src), "enfuse_mask: src must be interleaved U8/U16/F32 (1 or 3 channels)");
     ENB_TRY(check_params(ctx, prm, src->width, src->height));
     ENB_CHECK(ctx, floats_ok(mask_out, src->width, src->height), "enfuse_mask: mask_out must be F32 of the image size");
     if (alpha && alpha->data) {
@@ -1589,7 +1674,7 @@ enb_status enb_enfuse(enb_ctx* ctx, const enb_enfuse_params* prm, int K, const e
     }
     ENB_CHECK(ctx, K >= 1 && images, "enfuse: need at least one image");
     for (int k = 0; k < K; ++k) {
-        ENB_CHECK(ctx, pixels_ok(&images[k]), "enfuse: images must be interleaved U8/U16 with 1 or 3 channels");
+        ENB_CHECK(ctx, pixels_ok(&images[k]), "enfuse: images must be interleaved U8/U16/F32 with 1 or 3 channels");
         ENB_CHECK(ctx, same_geometry(&images[k], &images[0]), "enfuse: images differ in size, channels or type");
     }
     ENB_CHECK(ctx, out && pixels_ok(out) && same_geometry(out, &images[0]), "enfuse: out must match the inputs");
@@ -1655,7 +1740,10 @@ enb_status enb_enblend(enb_ctx* ctx, const enb_image* white, const enb_image* wh
         o = *opt;
     }
     ENB_CHECK(ctx, pixels_ok(white) && pixels_ok(black) && same_geometry(white, black),
-              "enblend: white/black must be interleaved U8/U16 images of one geometry");
+              "enblend: white/black must be interleaved U8/U16/F32 images of one geometry");
+    if (black->dtype == ENB_F32) {
+        o.plain = 1;  // the fused level passes are fixed point
+    }
     ENB_CHECK(ctx, out && pixels_ok(out) && same_geometry(out, black), "enblend: out must match the inputs");
     ENB_CHECK(ctx, mask && bytes_ok(mask, black->width, black->height), "enblend: mask must be U8 of the image size");
     ENB_CHECK(ctx, black->width > 1 && black->height > 1, "enblend: image too small");

@@ -22,7 +22,7 @@ struct PlanarView {
     int64_t pitch;
     int64_t plane;
     int w, h, C;
-    int dtype;  // ENB_I16 / ENB_I32
+    int dtype;  // ENB_I16 / ENB_I32 / ENB_F32
 };
 
 // An interleaved pixel image; pitch in elements of the sample type.
@@ -30,7 +30,14 @@ struct PixelView {
     const void* p;
     int64_t pitch;
     int w, h, C, stride;
-    int dtype;  // ENB_U8 / ENB_U16
+    int dtype;  // ENB_U8 / ENB_U16 / ENB_F32
+};
+
+// An interleaved float image (the float-image path); pitch in floats.
+struct FloatPixelView {
+    const float* p;
+    int64_t pitch;
+    int w, h, C, stride;
 };
 
 // An 8-bit plane (alpha, seam mask).
@@ -54,7 +61,8 @@ struct AlphaSrc {
     int mode;
     BytePlane plane;  // kAlphaPlane
     PixelView pix;    // kAlphaChannel3: 4th component thresholded at [lo, hi]
-    uint32_t lo, hi;
+    uint32_t lo, hi;  // integer samples
+    float flo, fhi;   // float samples (pix.dtype == ENB_F32)
 };
 
 // Device-side constant tables of the enfuse weights.
@@ -76,6 +84,20 @@ struct WeightParams {
     double w_saturation;
     float w_sat_hi, w_sat_lo; // w_saturation split into two floats
     uint32_t maxv;
+};
+
+// Weights of float images (src/enfuse.h:962-1212 with float pixels).
+// range stands for NumericTraits<float>::max() in the exposure and entropy
+// weights (FLT_MAX: the reference, 1.0: normalised-float mode).
+struct FloatWeightParams {
+    int use_exposure, use_contrast, use_saturation, use_entropy;
+    int contrast_window, entropy_window;
+    int gray_projector, exp_function;
+    double mixer[3];  // normalised channel-mixer weights
+    float w_exposure, w_contrast, w_saturation, w_entropy;
+    float range;
+    float opt_hi, opt_lo;  // exposure optimum as a sum of two floats
+    float inv_hi, inv_lo;  // 1 / effective width of the weight function, ditto
 };
 
 // Name and algorithmic bytes of the most recent launch on this host thread;
@@ -198,5 +220,18 @@ cudaError_t launch_up_level(const PlanarView& gw1, const PlanarView& gb1, const 
 cudaError_t launch_out0(const PlanarView* gw1, const PlanarView* gb1, const PlanarView* r1, const Out0Host& h,
                         cudaStream_t st, int ty0 = 0, int nty = -1);
 cudaError_t launch_coarse(const CoarseHost& h, cudaStream_t st);
+
+// float-image path (enb_float.cu): FP32 pyramid levels (dtype ENB_F32)
+cudaError_t launch_f_to_pyramid(const FloatPixelView& s, const PlanarView& d, cudaStream_t st);
+cudaError_t launch_f_from_pyramid(const PlanarView& s, const BytePlane& a, float* dst, int64_t dpitch, int dstride,
+                                  cudaStream_t st);
+cudaError_t launch_f_expand(int add, int wrap, const PlanarView& s, const PlanarView& d, cudaStream_t st);
+cudaError_t launch_f_blend(const PlanarView& m, const PlanarView& wt, const PlanarView& b, int32_t wv,
+                           cudaStream_t st);
+cudaError_t launch_f_mask_mul_acc(const PlanarView& lp, const PlanarView& m, int32_t divisor, const PlanarView& r,
+                                  int acc, cudaStream_t st);
+cudaError_t launch_f_copy_level0(const PlanarView& s, float* dst, cudaStream_t st);
+cudaError_t launch_f_enfuse_mask(const FloatPixelView& img, const BytePlane& alpha, const FloatWeightParams& wp,
+                                 const WeightTables& tab, const FloatPlane& out, cudaStream_t st);
 
 }  // namespace enb

@@ -24,7 +24,12 @@ __device__ __forceinline__ int alpha_at(const AlphaSrc& a, int x, int y)
     if (a.mode == kAlphaPlane) {
         return a.plane.p[(int64_t)y * a.plane.pitch + x] != 0;
     }
-    const uint32_t v = load_sample(a.pix.p, a.pix.dtype, (int64_t)y * a.pix.pitch + (int64_t)x * a.pix.stride + 3);
+    const int64_t i = (int64_t)y * a.pix.pitch + (int64_t)x * a.pix.stride + 3;
+    if (a.pix.dtype == ENB_F32) {
+        const float f = reinterpret_cast<const float*>(a.pix.p)[i];
+        return f >= a.flo && f <= a.fhi;
+    }
+    const uint32_t v = load_sample(a.pix.p, a.pix.dtype, i);
     return v >= a.lo && v <= a.hi;
 }
 
@@ -728,6 +733,12 @@ static inline void note(const char* name, double bytes) { last_launch() = Launch
 
 cudaError_t launch_to_fixed(const PixelView& s, const PlanarView& d, int frac, cudaStream_t st)
 {
+    if (s.dtype == ENB_F32 || d.dtype == ENB_F32) {
+        if (s.dtype != d.dtype) {
+            return cudaErrorInvalidValue;
+        }
+        return launch_f_to_pyramid(FloatPixelView{(const float*)s.p, s.pitch, s.w, s.h, s.C, s.stride}, d, st);
+    }
     note("to_fixed", npix(s.w, s.h) * s.C * esz(s.dtype) + planar_bytes(d));
     const dim3 g = row_grid(s.w, s.h);
     if (s.dtype == ENB_U8 && d.dtype == ENB_I16) {
@@ -832,7 +843,13 @@ static cudaError_t reduce_jobs(int wrap, int n, const PlanarView* const* s, cons
                  (sa[i] ? npix(s[i]->w, s[i]->h) + npix(d[i]->w, d[i]->h) : 0.0);
     }
     note(sa[0] ? "reduce_alpha" : "reduce", bytes);
-    if (s[0]->dtype == ENB_I16) {
+    if (s[0]->dtype == ENB_F32) {
+        if (s[0]->C == 1) {
+            reduce_dispatch<float, float, 1>(wrap, n, s, sa, d, da, st);
+        } else {
+            reduce_dispatch<float, float, 3>(wrap, n, s, sa, d, da, st);
+        }
+    } else if (s[0]->dtype == ENB_I16) {
         if (s[0]->C == 1) {
             reduce_dispatch<int16_t, int16_t, 1>(wrap, n, s, sa, d, da, st);
         } else {
@@ -894,6 +911,9 @@ cudaError_t launch_expand(int add, int wrap, const PlanarView& s, const PlanarVi
     if (s.dtype != d.dtype || s.C != d.C) {
         return cudaErrorInvalidValue;
     }
+    if (s.dtype == ENB_F32) {
+        return launch_f_expand(add, wrap, s, d, st);
+    }
     note(add ? "expand_add" : "expand_sub", planar_bytes(s) + 2.0 * planar_bytes(d));
     if (s.dtype == ENB_I16) {
         if (s.C == 1) {
@@ -924,6 +944,9 @@ cudaError_t launch_blend(const PlanarView& m, const PlanarView& wt, const Planar
 {
     if (wt.dtype != b.dtype || wt.C != b.C) {
         return cudaErrorInvalidValue;
+    }
+    if (b.dtype == ENB_F32) {
+        return m.dtype == ENB_I32 ? launch_f_blend(m, wt, b, wv, st) : cudaErrorInvalidValue;
     }
     note("blend", planar_bytes(m) + planar_bytes(wt) + 2.0 * planar_bytes(b));
     const bool m16 = m.dtype == ENB_I16;
@@ -967,6 +990,9 @@ cudaError_t launch_mask_mul_acc(const PlanarView& lp, const PlanarView& m, int32
     if (lp.dtype != r.dtype || lp.C != r.C) {
         return cudaErrorInvalidValue;
     }
+    if (lp.dtype == ENB_F32) {
+        return m.dtype == ENB_I32 ? launch_f_mask_mul_acc(lp, m, divisor, r, acc, st) : cudaErrorInvalidValue;
+    }
     note("mask_mul_acc", planar_bytes(lp) + planar_bytes(m) + (acc ? 2.0 : 1.0) * planar_bytes(r));
     const bool m16 = m.dtype == ENB_I16;
     if (lp.dtype == ENB_I16) {
@@ -988,6 +1014,12 @@ cudaError_t launch_mask_mul_acc(const PlanarView& lp, const PlanarView& m, int32
 cudaError_t launch_from_fixed(const PlanarView& s, const BytePlane& a, void* dst, int64_t dpitch, int ddtype,
                               int dstride, int frac, int dither, uint64_t seed, cudaStream_t st)
 {
+    if (s.dtype == ENB_F32 || ddtype == ENB_F32) {
+        if (s.dtype != ddtype) {
+            return cudaErrorInvalidValue;
+        }
+        return launch_f_from_pyramid(s, a, (float*)dst, dpitch, dstride, st);
+    }
     note("from_fixed", planar_bytes(s) + npix(s.w, s.h) * (1.0 + s.C * esz(ddtype)));
     const dim3 g = row_grid(s.w, s.h);
     if (s.dtype == ENB_I16) {
@@ -1021,6 +1053,8 @@ cudaError_t launch_copy_pixels(const PixelView& s, void* dst, int64_t dpitch, cu
     const dim3 g = row_grid(rowlen, s.h);
     if (s.dtype == ENB_U8) {
         k_copy_pixels<uint8_t><<<g, 256, 0, st>>>((const uint8_t*)s.p, s.pitch, (uint8_t*)dst, dpitch, rowlen, s.h);
+    } else if (s.dtype == ENB_F32) {
+        k_copy_pixels<uint32_t><<<g, 256, 0, st>>>((const uint32_t*)s.p, s.pitch, (uint32_t*)dst, dpitch, rowlen, s.h);
     } else {
         k_copy_pixels<uint16_t><<<g, 256, 0, st>>>((const uint16_t*)s.p, s.pitch, (uint16_t*)dst, dpitch, rowlen, s.h);
     }
@@ -1033,6 +1067,9 @@ cudaError_t launch_alpha_component(const BytePlane& a, void* dst, int64_t dpitch
     const dim3 g = row_grid(a.w, a.h);
     if (ddtype == ENB_U8) {
         k_alpha_component<uint8_t><<<g, 256, 0, st>>>(a.p, a.pitch, (uint8_t*)dst, dpitch, a.w, a.h, (uint8_t)255);
+    } else if (ddtype == ENB_F32) {
+        // AlphaTraits<float>::max() = 1.0 (src/numerictraits.h:247)
+        k_alpha_component<float><<<g, 256, 0, st>>>(a.p, a.pitch, (float*)dst, dpitch, a.w, a.h, 1.0f);
     } else {
         k_alpha_component<uint16_t><<<g, 256, 0, st>>>(a.p, a.pitch, (uint16_t*)dst, dpitch, a.w, a.h, (uint16_t)65535);
     }
@@ -1041,6 +1078,9 @@ cudaError_t launch_alpha_component(const BytePlane& a, void* dst, int64_t dpitch
 
 cudaError_t launch_copy_level0(const PlanarView& s, int32_t* dst, cudaStream_t st)
 {
+    if (s.dtype == ENB_F32) {
+        return launch_f_copy_level0(s, reinterpret_cast<float*>(dst), st);
+    }
     note("copy_level0", planar_bytes(s) + 4.0 * npix(s.w, s.h) * s.C);
     const dim3 g = row_grid(s.w, s.h);
     if (s.dtype == ENB_I16) {

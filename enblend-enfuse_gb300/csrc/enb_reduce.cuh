@@ -39,19 +39,22 @@ constexpr int RVP = 148;                 // padded row of column sums
 __device__ __forceinline__ int rphys(int c) { return c + ((c >> 5) << 2); }
 
 // Planar pyramid level (+ an 8-bit alpha plane when A); NC: read-only load
-// path (the level is not written by the launch).
+// path (the level is not written by the launch).  Samples are delivered in
+// the accumulator type of the reduce (int32 for fixed point, float for the
+// FP32 pyramids of float images).
 template <typename TS, int C, bool A, bool NC = true>
 struct PlanarSource {
     const TS* p;
     int64_t pitch, plane;   // elements
     const uint8_t* a;
     int64_t apitch;
-    __device__ __forceinline__ void load(int gy, int gx, int32_t (&v)[C], int& al) const
+    template <typename AC>
+    __device__ __forceinline__ void load(int gy, int gx, AC (&v)[C], int& al) const
     {
         const int64_t o = (int64_t)gy * pitch + gx;
 #pragma unroll
         for (int c = 0; c < C; ++c) {
-            v[c] = (int32_t)ld_src<NC>(&p[c * plane + o]);
+            v[c] = (AC)ld_src<NC>(&p[c * plane + o]);
         }
         al = A ? (ld_src<NC>(&a[(int64_t)gy * apitch + gx]) != 0) : 1;
     }
@@ -62,7 +65,8 @@ struct ByteSource {
     const uint8_t* p;
     int64_t pitch;
     int frac;
-    __device__ __forceinline__ void load(int gy, int gx, int32_t (&v)[1], int& al) const
+    template <typename AC>
+    __device__ __forceinline__ void load(int gy, int gx, AC (&v)[1], int& al) const
     {
         v[0] = (int32_t)__ldg(&p[(int64_t)gy * pitch + gx]) << frac;
         al = 1;
@@ -88,9 +92,9 @@ struct ReduceJobs {
 // Border items load from clamped (always valid) positions and zero the taps
 // outside the image afterwards, so that no load waits behind a branch and
 // all 19 rows are in flight at once.
-template <class Src, int C, bool ALPHA, bool INTERIOR>
+template <class Src, int C, bool ALPHA, bool INTERIOR, typename AC>
 __device__ __forceinline__ void reduce_column(const Src& src, int gx, int gyb, int sw, int sh, int wrap,
-                                              int32_t (*V)[RDH][RVP], int col, int r0)
+                                              AC (*V)[RDH][RVP], int col, int r0)
 {
     constexpr int NV = C + (ALPHA ? 1 : 0);
     bool colok = true;
@@ -102,7 +106,7 @@ __device__ __forceinline__ void reduce_column(const Src& src, int gx, int gyb, i
             gx = min(max(gx, 0), sw - 1);
         }
     }
-    int32_t x[RGN][NV];
+    AC x[RGN][NV];
 #pragma unroll
     for (int k = 0; k < RGN; ++k) {
         int gy = gyb + k;
@@ -111,7 +115,7 @@ __device__ __forceinline__ void reduce_column(const Src& src, int gx, int gyb, i
             ok = colok && gy >= 0 && gy < sh;
             gy = min(max(gy, 0), sh - 1);
         }
-        int32_t v[C];
+        AC v[C];
         int al = 1;
         src.load(gy, gx, v, al);
         if (ALPHA) {
@@ -119,10 +123,10 @@ __device__ __forceinline__ void reduce_column(const Src& src, int gx, int gyb, i
         }
 #pragma unroll
         for (int ch = 0; ch < C; ++ch) {
-            x[k][ch] = (ALPHA && !al) ? 0 : v[ch];   // without alpha: clamp-to-edge
+            x[k][ch] = (ALPHA && !al) ? (AC)0 : v[ch];   // without alpha: clamp-to-edge
         }
         if (ALPHA) {
-            x[k][NV - 1] = al;
+            x[k][NV - 1] = (AC)al;
         }
     }
     const int pc = rphys(col);
@@ -130,8 +134,22 @@ __device__ __forceinline__ void reduce_column(const Src& src, int gx, int gyb, i
     for (int r = 0; r < RGR; ++r) {
 #pragma unroll
         for (int ch = 0; ch < NV; ++ch) {
-            V[ch][r0 + r][pc] =
-                x[2 * r][ch] + 4 * x[2 * r + 1][ch] + 6 * x[2 * r + 2][ch] + 4 * x[2 * r + 3][ch] + x[2 * r + 4][ch];
+            V[ch][r0 + r][pc] = x[2 * r][ch] + (AC)4 * x[2 * r + 1][ch] + (AC)6 * x[2 * r + 2][ch] +
+                                (AC)4 * x[2 * r + 3][ch] + x[2 * r + 4][ch];
+        }
+    }
+}
+
+__device__ __forceinline__ void store4(float* p, const float (&v)[4], int n)
+{
+    if (n == 4 && ((uintptr_t)p & 15) == 0) {
+        *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    } else {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (q < n) {
+                p[q] = v[q];
+            }
         }
     }
 }
@@ -163,11 +181,23 @@ struct ReduceSmem {
     static constexpr int WORDS = NV * RDH * RVP;
 };
 
+// Normalisation of a tap sum by the opaque weight sum den > 0: truncating
+// integer division for fixed point (pyramid.h:242-250), real division for
+// the float pyramids (SKIPSMImagePixelType double in the reference).
+__device__ __forceinline__ int32_t reduce_norm(int32_t s, int32_t den)
+{
+    return den == 256 ? s / 256 : div_any(s, den);
+}
+__device__ __forceinline__ float reduce_norm(float s, float den) { return __fdiv_rn(s, den); }
+__device__ __forceinline__ int32_t reduce_256(int32_t s) { return s / 256; }
+__device__ __forceinline__ float reduce_256(float s) { return s * 0.00390625f; }
+
 // One 64x16 destination tile at (X0, Y0) of a reduce job (RTHREADS threads;
-// V holds ReduceSmem<C, ALPHA>::WORDS 16-byte aligned words).
-template <class Src, typename TD, int C, bool ALPHA>
+// V holds ReduceSmem<C, ALPHA>::WORDS 16-byte aligned words of the
+// accumulator type AC: int32 for fixed point, float for FP32 levels).
+template <class Src, typename TD, int C, bool ALPHA, typename AC = int32_t>
 __device__ __forceinline__ void reduce_tile(const ReduceJob<Src, TD>& job, int X0, int Y0, int sw, int sh, int dw,
-                                            int dh, int wrap, int32_t (*V)[RDH][RVP])
+                                            int dh, int wrap, AC (*V)[RDH][RVP])
 {
     constexpr int NV = C + (ALPHA ? 1 : 0);
     const int gx0 = 2 * X0 - 2, gy0 = 2 * Y0 - 2;
@@ -178,9 +208,9 @@ __device__ __forceinline__ void reduce_tile(const ReduceJob<Src, TD>& job, int X
         const int col = tid - g * RSW;
         const int gyb = gy0 + 2 * RGR * g;
         if (gx0 >= 0 && gy0 >= 0 && gx0 + RSW <= sw && gy0 + RSH <= sh) {
-            reduce_column<Src, C, ALPHA, true>(job.src, gx0 + col, gyb, sw, sh, wrap, V, col, RGR * g);
+            reduce_column<Src, C, ALPHA, true, AC>(job.src, gx0 + col, gyb, sw, sh, wrap, V, col, RGR * g);
         } else {
-            reduce_column<Src, C, ALPHA, false>(job.src, gx0 + col, gyb, sw, sh, wrap, V, col, RGR * g);
+            reduce_column<Src, C, ALPHA, false, AC>(job.src, gx0 + col, gyb, sw, sh, wrap, V, col, RGR * g);
         }
     }
     __syncthreads();
@@ -191,35 +221,35 @@ __device__ __forceinline__ void reduce_tile(const ReduceJob<Src, TD>& job, int X
         return;
     }
     const int n = min(4, dw - Xb);
-    int32_t s[NV][4];
+    AC s[NV][4];
 #pragma unroll
     for (int ch = 0; ch < NV; ++ch) {
-        const int32_t* row = &V[ch][r][0];
-        const int4 a = *reinterpret_cast<const int4*>(row + rphys(8 * k));
-        const int4 b = *reinterpret_cast<const int4*>(row + rphys(8 * k + 4));
-        const int4 c = *reinterpret_cast<const int4*>(row + rphys(8 * k + 8));
-        const int32_t v[11] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z};
+        const AC* row = &V[ch][r][0];
+        AC v[12];
+        *reinterpret_cast<int4*>(&v[0]) = *reinterpret_cast<const int4*>(row + rphys(8 * k));
+        *reinterpret_cast<int4*>(&v[4]) = *reinterpret_cast<const int4*>(row + rphys(8 * k + 4));
+        *reinterpret_cast<int4*>(&v[8]) = *reinterpret_cast<const int4*>(row + rphys(8 * k + 8));
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            s[ch][q] = v[2 * q] + 4 * v[2 * q + 1] + 6 * v[2 * q + 2] + 4 * v[2 * q + 3] + v[2 * q + 4];
+            s[ch][q] = v[2 * q] + (AC)4 * v[2 * q + 1] + (AC)6 * v[2 * q + 2] + (AC)4 * v[2 * q + 3] + v[2 * q + 4];
         }
     }
     const int64_t o = (int64_t)Y * job.dpitch + Xb;
     if (ALPHA) {
-        int32_t out[C][4];
+        AC out[C][4];
         uint32_t abits = 0;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            const int32_t den = s[NV - 1][q];
+            const AC den = s[NV - 1][q];
 #pragma unroll
             for (int ch = 0; ch < C; ++ch) {
-                out[ch][q] = den <= 0 ? 0 : (den == 256 ? s[ch][q] / 256 : div_any(s[ch][q], den));
+                out[ch][q] = den <= (AC)0 ? (AC)0 : reduce_norm(s[ch][q], den);
             }
-            abits |= (den > 0 ? 255u : 0u) << (8 * q);
+            abits |= (den > (AC)0 ? 255u : 0u) << (8 * q);
         }
 #pragma unroll
         for (int ch = 0; ch < C; ++ch) {
-            store4<TD>(job.dst + ch * job.dplane + o, out[ch], n);
+            store4(job.dst + ch * job.dplane + o, out[ch], n);
         }
         uint8_t* ap = job.da + (int64_t)Y * job.dapitch + Xb;
         if (n == 4 && ((uintptr_t)ap & 3) == 0) {
@@ -235,25 +265,30 @@ __device__ __forceinline__ void reduce_tile(const ReduceJob<Src, TD>& job, int X
     } else {
 #pragma unroll
         for (int ch = 0; ch < C; ++ch) {
-            int32_t out[4];
+            AC out[4];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                out[q] = s[ch][q] / 256;
+                out[q] = reduce_256(s[ch][q]);
             }
-            store4<TD>(job.dst + ch * job.dplane + o, out, n);
+            store4(job.dst + ch * job.dplane + o, out, n);
         }
     }
 }
+
+// Accumulator of a reduce into destination type TD.
+template <typename TD> struct ReduceAcc { typedef int32_t type; };
+template <> struct ReduceAcc<float> { typedef float type; };
 
 template <class Src, typename TD, int C, bool ALPHA>
 __global__ void __launch_bounds__(RTHREADS, 3) k_reduce(ReduceJobs<Src, TD> jobs, int sw, int sh, int dw, int dh,
                                                         int wrap)
 {
-    __shared__ __align__(16) int32_t V[ReduceSmem<C, ALPHA>::NV][RDH][RVP];
+    typedef typename ReduceAcc<TD>::type AC;
+    __shared__ __align__(16) AC V[ReduceSmem<C, ALPHA>::NV][RDH][RVP];
     griddep_wait();
     griddep_launch();
     const ReduceJob<Src, TD> job = blockIdx.z == 0 ? jobs.j[0] : jobs.j[1];
-    reduce_tile<Src, TD, C, ALPHA>(job, blockIdx.x * RDW, (blockIdx.y + jobs.ty0) * RDH, sw, sh, dw, dh, wrap, V);
+    reduce_tile<Src, TD, C, ALPHA, AC>(job, blockIdx.x * RDW, (blockIdx.y + jobs.ty0) * RDH, sw, sh, dw, dh, wrap, V);
 }
 
 // Destination tile rows of the reduce (16 rows each).

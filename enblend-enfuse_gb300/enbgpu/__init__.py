@@ -57,7 +57,7 @@ class EnbEnfuseParams(ctypes.Structure):
                 ("exp_optimum", ctypes.c_double), ("exp_width", ctypes.c_double),
                 ("exp_function", ctypes.c_int32), ("contrast_window", ctypes.c_int32),
                 ("entropy_window", ctypes.c_int32), ("gray_projector", ctypes.c_int32),
-                ("mixer", ctypes.c_double * 3)]
+                ("mixer", ctypes.c_double * 3), ("float_range", ctypes.c_double)]
 
 
 class EnbFuseOptions(ctypes.Structure):
@@ -190,12 +190,25 @@ def plane_image(x) -> EnbImage:
     return EnbImage(ptr, strides[0], 0, w, h, 1, 1, _dtype_code(x), 0)
 
 
+def _pyramid_dtype(img: EnbImage, weight_plane: bool = False) -> int:
+    """EnblendNumericTraits' image pyramid type (src/numerictraits.h:168-185): Int16 for 8-bit samples, Int32
+    for 16-bit samples and float weight planes, FP32 (the reference's double) for float images."""
+    if img.dtype == ENB_U8:
+        return ENB_I16
+    if img.dtype == ENB_F32 and not weight_plane:
+        return ENB_F32
+    return ENB_I32
+
+
 def enfuse_params(exposure_weight: float = 1.0, saturation_weight: float = 0.0, contrast_weight: float = 0.0,
                   entropy_weight: float = 0.0, exposure_optimum: float = 0.5, exposure_width: float = 0.2,
                   exposure_weight_function: str = "gaussian", contrast_window_size: int = 5,
                   entropy_window_size: int = 3, gray_projector: str = "average",
-                  mixer: Sequence[float] = (0.0, 0.0, 0.0)) -> EnbEnfuseParams:
-    """enfuse's weighting options (src/enfuse.cc:117-140, same defaults)."""
+                  mixer: Sequence[float] = (0.0, 0.0, 0.0), float_range: float = 0.0) -> EnbEnfuseParams:
+    """enfuse's weighting options (src/enfuse.cc:117-140, same defaults).
+
+    float_range: float images only; 0 takes the reference's NumericTraits<float>::max() as the sample scale of
+    the exposure and entropy weights, 1.0 is the normalised-float mode for images in [0, 1]."""
     p = EnbEnfuseParams()
     p.w_exposure, p.w_saturation = exposure_weight, saturation_weight
     p.w_contrast, p.w_entropy = contrast_weight, entropy_weight
@@ -204,6 +217,7 @@ def enfuse_params(exposure_weight: float = 1.0, saturation_weight: float = 0.0, 
     p.contrast_window, p.entropy_window = contrast_window_size, entropy_window_size
     p.gray_projector = GRAY_PROJECTORS[gray_projector]
     p.mixer[:] = list(mixer)
+    p.float_range = float_range
     return p
 
 
@@ -226,17 +240,19 @@ class Pyramid:
         self.ctx._check(self.ctx.lib.enb_pyramid_level(self.handle, l, ctypes.byref(img)))
         return img
 
+    def _np_type(self):
+        return {ENB_I16: np.int16, ENB_I32: np.int32, ENB_F32: np.float32}[self.dtype]
+
     def read(self, l: int) -> np.ndarray:
-        """Level l as a (C, H, W) int16/int32 array."""
+        """Level l as a (C, H, W) int16/int32/float32 array."""
         img = self.level_image(l)
-        a = np.empty((img.channels, img.height, img.width), np.int16 if self.dtype == ENB_I16 else np.int32)
+        a = np.empty((img.channels, img.height, img.width), self._np_type())
         self.ctx._check(self.ctx.lib.enb_pyramid_read_level(self.ctx.handle, self.handle, l, a.ctypes.data))
         return a
 
     def write(self, l: int, a: np.ndarray) -> None:
         img = self.level_image(l)
-        t = np.int16 if self.dtype == ENB_I16 else np.int32
-        a = np.ascontiguousarray(a, dtype=t).reshape(img.channels, img.height, img.width)
+        a = np.ascontiguousarray(a, dtype=self._np_type()).reshape(img.channels, img.height, img.width)
         self.ctx._check(self.ctx.lib.enb_pyramid_write_level(self.ctx.handle, self.handle, l, a.ctypes.data))
 
     def free(self) -> None:
@@ -323,9 +339,10 @@ class Context:
     def gaussian_pyramid(self, image, levels: int, alpha=None, wrap: bool = False, frac_bits: int = 7,
                          dtype: Optional[int] = None) -> Pyramid:
         """gaussianPyramid (src/pyramid.h:1468-1636) of a device image."""
-        img = plane_image(image) if image.ndim == 2 and _dtype_code(image) == ENB_F32 else pixel_image(image)
+        weight_plane = image.ndim == 2 and _dtype_code(image) == ENB_F32
+        img = plane_image(image) if weight_plane else pixel_image(image)
         if dtype is None:
-            dtype = ENB_I16 if img.dtype == ENB_U8 else ENB_I32
+            dtype = _pyramid_dtype(img, weight_plane)
         pyr = self.pyramid(levels, img.width, img.height, img.channels, dtype)
         a = ctypes.byref(plane_image(alpha)) if alpha is not None else None
         self._check(self.lib.enb_gaussian_pyramid(self.handle, int(wrap), ctypes.byref(img), a, frac_bits,
@@ -337,7 +354,7 @@ class Context:
         """laplacianPyramid (src/pyramid.h:1647-1747) of a device image."""
         img = pixel_image(image)
         if dtype is None:
-            dtype = ENB_I16 if img.dtype == ENB_U8 else ENB_I32
+            dtype = _pyramid_dtype(img)
         pyr = self.pyramid(levels, img.width, img.height, img.channels, dtype)
         a = ctypes.byref(plane_image(alpha)) if alpha is not None else None
         self._check(self.lib.enb_laplacian_pyramid(self.handle, int(wrap), ctypes.byref(img), a, frac_bits,

@@ -85,7 +85,7 @@ def panorama_pair(h: int, w: int, offset: int, dtype, seed: int, stops: float = 
     rng = np.random.default_rng(seed)
     wu = offset + w
     lr = log_radiance(h, wu, stops, seed)
-    maxv = np.iinfo(dtype).max
+    maxv = 1.0 if np.dtype(dtype) == np.float32 else np.iinfo(dtype).max
     out = []
     for i, x0 in enumerate((0, offset)):
         gain = rng.uniform(0.9, 1.1)

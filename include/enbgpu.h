@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define ENBGPU_ABI_VERSION 2
+#define ENBGPU_ABI_VERSION 3
 
 typedef enum {
     ENB_OK = 0,
@@ -36,7 +36,10 @@ typedef enum {
 typedef enum {
     ENB_U8 = 0,   /* 8-bit unsigned samples */
     ENB_U16 = 1,  /* 16-bit unsigned samples */
-    ENB_F32 = 2,  /* 32-bit float samples (weight masks) */
+    ENB_F32 = 2,  /* 32-bit float: float images (interleaved), weight masks,
+                     and the FP32 pyramid levels of float images, which stand
+                     in for the reference's double pyramids
+                     (src/numerictraits.h:185) */
     ENB_I16 = 3,  /* 16-bit signed fixed point (pyramids of 8-bit images) */
     ENB_I32 = 4   /* 32-bit signed fixed point (pyramids of 16-bit images, masks) */
 } enb_dtype;
@@ -99,6 +102,15 @@ typedef struct {
     int32_t entropy_window; /* --entropy-window-size, odd 3..15, default 3 */
     int32_t gray_projector; /* --gray-projector, enb_gray_projector */
     double mixer[3];        /* channel-mixer weights (unnormalised) */
+    double float_range;     /* float images: the value the reference takes as
+                               NumericTraits<float>::max() in the exposure
+                               (y = gray / max, src/enfuse.h:638) and entropy
+                               (H * max) weights.  0 (default): FLT_MAX, the
+                               reference's behaviour, which makes the exposure
+                               weight constant and the entropy weight huge;
+                               > 0: normalised-float mode, e.g. 1.0 for images
+                               in [0, 1].  Saturation (max 1.0) and contrast
+                               (W * sigma) are the same in both modes. */
 } enb_enfuse_params;
 
 /* Options of the fuse drivers. */
@@ -116,8 +128,9 @@ typedef struct {
                               instead of the fused level passes; same result,
                               for comparisons */
     void* level0_out;      /* optional device buffer (host if host_buffers):
-                              collapsed level 0 before conversion, int32,
-                              interleaved width*height*channels */
+                              collapsed level 0 before conversion, int32
+                              (float for F32 images), interleaved
+                              width*height*channels */
     int32_t coarse_pixels; /* enblend: pyramid levels of at most this many
                               pixels run in one cluster launch; 0: default
                               (none), < 0: every level in its own launches */
@@ -156,7 +169,9 @@ int enb_num_levels(int width, int height, int min_levels, int exact_levels);
 
 /* ---- pyramids (std::vector<PyramidImageType*>*, src/pyramid.h:1471) ----- */
 /* Device-resident pyramid: `levels` planar levels of `channels` planes of
- * dtype ENB_I16 or ENB_I32, level l of size ((w+1)>>1)^l.  Ownership stays
+ * dtype ENB_I16, ENB_I32 or ENB_F32, level l of size ((w+1)>>1)^l.  The
+ * primitives below accept F32 image levels with I32 (9.15) mask levels, the
+ * pyramid types of float images.  Ownership stays
  * with the caller (the reference's `delete` of each level and the vector,
  * src/enfuse.h:1568-1570 -> enb_pyramid_free). */
 enb_status enb_pyramid_create(enb_ctx* ctx, int levels, int width, int height, int channels,
@@ -172,8 +187,10 @@ enb_status enb_pyramid_write_level(enb_ctx* ctx, enb_pyramid* pyr, int level, co
 
 /* ---- primitives (device images) ---------------------------------------- */
 /* copyToPyramidImage / ConvertScalarToPyramidFunctor (src/fixmath.h:116-206,
- * 2019-2147): U8/U16 samples -> `v << frac_bits`; F32 -> fromRealPromote(v *
- * 2^frac_bits).  dst is a planar I16/I32 level. */
+ * 2019-2147): U8/U16 samples -> `v << frac_bits` into a planar I16/I32 level;
+ * an F32 plane (a weight mask) into an I16/I32 level -> fromRealPromote(v *
+ * 2^frac_bits); an interleaved F32 image into an F32 level -> the
+ * logarithmic mapping v >= 0 ? 1 + log1p(v) : 1 / (1 - v) (frac_bits ignored). */
 enb_status enb_to_pyramid(enb_ctx* ctx, const enb_image* src, const enb_image* dst, int frac_bits);
 
 /* reduce (src/pyramid.h:166-573 with alpha, :601-848 without).  src_alpha ==
@@ -198,7 +215,9 @@ enb_status enb_mask_multiply_accumulate(enb_ctx* ctx, const enb_image* lp, const
                                         int32_t divisor, const enb_image* result, int accumulate);
 
 /* copyFromPyramidImageIf (src/fixmath.h:2158-2294, rule :251-277): planar
- * fixed point -> interleaved U8/U16 pixels where alpha != 0. */
+ * fixed point -> interleaved U8/U16 pixels where alpha != 0; an F32 level ->
+ * F32 pixels by v >= 1 ? expm1(v - 1) : 1 - 1/v (src/fixmath.h:320-329;
+ * frac_bits, dither and seed ignored). */
 enb_status enb_from_pyramid(enb_ctx* ctx, const enb_image* src, const enb_image* alpha,
                             const enb_image* dst, int frac_bits, int dither, uint64_t seed);
 
@@ -231,13 +250,15 @@ enb_status enb_blend_pyramids(enb_ctx* ctx, const enb_pyramid* mask_gp, const en
                               enb_pyramid* black_lp, int32_t white_value);
 
 /* ---- enfuse weights ----------------------------------------------------- */
-/* enfuseMask (src/enfuse.h:962-1212): F32 weight plane of an U8/U16 image. */
+/* enfuseMask (src/enfuse.h:962-1212): F32 weight plane of an U8/U16/F32 image. */
 enb_status enb_enfuse_mask(enb_ctx* ctx, const enb_enfuse_params* params, const enb_image* src,
                            const enb_image* alpha, const enb_image* mask_out);
 
 /* ---- drivers ------------------------------------------------------------ */
 /* enfuseMain's weighting, normalisation, pyramids, merge, collapse and
- * output conversion (src/enfuse.h:1217-1617) for K union-sized images.
+ * output conversion (src/enfuse.h:1217-1617) for K union-sized U8, U16 or
+ * F32 images (F32: FP32 pyramids in place of the reference's double ones;
+ * the 4th component of an RGBA F32 image is thresholded at [0.5, 1]).
  * alphas: K alpha planes or NULL (for RGBA images the alpha is then the
  * thresholded 4th component as imported by src/assemble.h:240-253, else fully
  * opaque).  masks_in: K F32 weight planes replacing enfuseMask (--load-masks),
@@ -250,8 +271,9 @@ enb_status enb_enfuse(enb_ctx* ctx, const enb_enfuse_params* params, int K, cons
 /* enblendMain's pyramid section (src/enblend.h:330-510): blend `white` into
  * `black` under the 0/255 seam mask over the whole canvas.  out receives the
  * black image with the blended pixels where the union alpha is set (for RGBA
- * images the 4th component becomes the union alpha, 0 or the type maximum);
- * out may be the black image itself. */
+ * images the 4th component becomes the union alpha, 0 or the type maximum,
+ * 1.0 for F32); out may be the black image itself.  F32 images always take
+ * the per-operation pass structure (the fused passes are fixed point). */
 enb_status enb_enblend(enb_ctx* ctx, const enb_image* white, const enb_image* white_alpha,
                        const enb_image* black, const enb_image* black_alpha, const enb_image* mask,
                        const enb_image* out, const enb_image* out_alpha, const enb_fuse_options* opt);

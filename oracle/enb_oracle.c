@@ -1064,3 +1064,585 @@ int orc_enblend(const void* white, const uint8_t* white_alpha, const void* black
     pyr_free(&bl);
     return rc;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Float images: double pyramids (src/numerictraits.h:185, float row).        */
+/*                                                                            */
+/* The reference builds the image pyramids of float images in double with a   */
+/* logarithmic mapping, reduces and expands them with real divisions, merges  */
+/* them in double and maps level 0 back (src/fixmath.h:165-187, 320-329).     */
+/* The mask pyramids stay Int32 9.15 (the integer operators above).  The      */
+/* weights of float images are evaluated here in double from their            */
+/* definitions; where the reference keeps a running float sum (the sliding   */
+/* window of localStdDevIf, src/enfuse.h:75-219) this restatement computes    */
+/* the exact window statistics instead.                                       */
+/* ------------------------------------------------------------------------- */
+
+/* ConvertScalarToPyramidFunctor, real -> real (src/fixmath.h:165-187).  The
+ * functor's argument is the float sample, so the C++ overload log1p(float)
+ * is the one called: the logarithm is a float, the sum 1.0 + it a double
+ * (this reproduces the reference's double pyramid to the last bit). */
+void orc_real_to_pyramid(const float* src, int64_t npix, int C, int pix_stride, double* dst)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t p = 0; p < npix; ++p) {
+        for (int c = 0; c < C; ++c) {
+            const double v = (double)src[p * pix_stride + c];
+            dst[p * C + c] = v >= 0.0 ? 1.0 + (double)log1pf((float)v) : 1.0 / (1.0 - v);
+        }
+    }
+}
+
+/* SpecializedConvertPyramidToScalarFunctor, real -> real (src/fixmath.h:320-329),
+ * written where alpha != 0 (copyFromPyramidImageIf, src/fixmath.h:2259-2294);
+ * NumericTraits<float>::fromRealPromote is the plain conversion to float. */
+void orc_real_from_pyramid(const double* src, const uint8_t* alpha, int64_t npix, int C, float* dst,
+                           int pix_stride)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t p = 0; p < npix; ++p) {
+        if (!alpha[p]) {
+            continue;
+        }
+        for (int c = 0; c < C; ++c) {
+            const double v = src[p * C + c];
+            dst[p * pix_stride + c] = (float)(v >= 1.0 ? expm1(v - 1.0) : 1.0 - 1.0 / v);
+        }
+    }
+}
+
+/* reduce with alpha over a double pyramid (src/pyramid.h:166-573 with
+ * SKIPSMImagePixelType double): the normalised 5x5 binomial with a real
+ * division; zero where no opaque tap contributes. */
+int orc_reduce_alpha_d(int wrap, const double* src, const uint8_t* alpha, int sw, int sh, int C, double* dst,
+                       uint8_t* dst_alpha)
+{
+    if (sw <= 1 || sh <= 1 || C > 4) {
+        return -1;
+    }
+    const int dw = (sw + 1) >> 1, dh = (sh + 1) >> 1;
+#pragma omp parallel for schedule(static)
+    for (int Y = 0; Y < dh; ++Y) {
+        for (int X = 0; X < dw; ++X) {
+            double num[4] = {0, 0, 0, 0};
+            int den = 0;
+            for (int j = -2; j <= 2; ++j) {
+                const int y = 2 * Y + j;
+                if (y < 0 || y >= sh) {
+                    continue;
+                }
+                for (int i = -2; i <= 2; ++i) {
+                    int x = 2 * X + i;
+                    if (wrap) {
+                        x = imod(x, sw);
+                    } else if (x < 0 || x >= sw) {
+                        continue;
+                    }
+                    const int64_t p = (int64_t)y * sw + x;
+                    if (alpha[p]) {
+                        const int wgt = W5[j + 2] * W5[i + 2];
+                        den += wgt;
+                        for (int c = 0; c < C; ++c) {
+                            num[c] += (double)wgt * src[p * C + c];
+                        }
+                    }
+                }
+            }
+            const int64_t q = (int64_t)Y * dw + X;
+            for (int c = 0; c < C; ++c) {
+                dst[q * C + c] = den > 0 ? num[c] / (double)den : 0.0;
+            }
+            dst_alpha[q] = den > 0 ? 255 : 0;
+        }
+    }
+    return 0;
+}
+
+/* expand over a double pyramid (src/pyramid.h:875-1457): add = 0: dst -= E,
+ * add = 1: dst += E (fromPromote is the identity for double). */
+int orc_expand_d(int add, int wrap, const double* src, int sw, int sh, double* dst, int dw, int dh, int C)
+{
+    if (sw < 1 || sh < 1 || sw != ((dw + 1) >> 1) || sh != ((dh + 1) >> 1) || C > 4) {
+        return -1;
+    }
+#pragma omp parallel for schedule(static)
+    for (int Y = 0; Y < dh; ++Y) {
+        int vi[3], vw[3], vn, vd;
+        expand_vtaps(Y, sh, vi, vw, &vn, &vd);
+        for (int X = 0; X < dw; ++X) {
+            int hi[3], hw[3], hn, hd;
+            expand_htaps(X, sw, dw, wrap, hi, hw, &hn, &hd);
+            const double den = (double)(hd * vd);
+            for (int c = 0; c < C; ++c) {
+                double num = 0.0;
+                for (int a = 0; a < vn; ++a) {
+                    double row = 0.0;
+                    for (int b = 0; b < hn; ++b) {
+                        row += (double)hw[b] * src[((int64_t)vi[a] * sw + hi[b]) * C + c];
+                    }
+                    num += (double)vw[a] * row;
+                }
+                double* d = &dst[((int64_t)Y * dw + X) * C + c];
+                *d = add ? *d + num / den : *d - num / den;
+            }
+        }
+    }
+    return 0;
+}
+
+/* CartesianBlendFunctor on double pixels (src/blend.h:41-76). */
+void orc_blend_d(const int32_t* mask, const double* white, double* black, int64_t npix, int C, int32_t white_value)
+{
+    const double wv = (double)white_value;
+#pragma omp parallel for schedule(static)
+    for (int64_t p = 0; p < npix; ++p) {
+        const double wc = (double)mask[p] / wv;
+        if (wc >= 1.0) {
+            for (int c = 0; c < C; ++c) {
+                black[p * C + c] = white[p * C + c];
+            }
+        } else if (wc > 0.0) {
+            const double bc = 1.0 - wc;
+            for (int c = 0; c < C; ++c) {
+                black[p * C + c] = wc * white[p * C + c] + bc * black[p * C + c];
+            }
+        }
+    }
+}
+
+/* ImageMaskMultiplyFunctor on double pixels (src/enfuse.h:601-620), then the
+ * accumulation into the result pyramid (src/enfuse.h:1576-1588); res = NULL
+ * multiplies in place only. */
+void orc_mask_multiply_d(double* lp, const int32_t* mask, int64_t npix, int C, int32_t divisor, double* res)
+{
+    const double dv = (double)divisor;
+#pragma omp parallel for schedule(static)
+    for (int64_t p = 0; p < npix; ++p) {
+        const double coeff = (double)mask[p] / dv;
+        for (int c = 0; c < C; ++c) {
+            const double v = lp[p * C + c] * coeff;
+            lp[p * C + c] = v;
+            if (res) {
+                res[p * C + c] += v;
+            }
+        }
+    }
+}
+
+typedef struct {
+    int levels;
+    int C;
+    int w[30], h[30];
+    double* lv[30];
+} pyrd_t;
+
+static void pyrd_alloc(pyrd_t* p, int levels, int w, int h, int C)
+{
+    p->levels = levels;
+    p->C = C;
+    for (int l = 0; l < levels; ++l) {
+        p->w[l] = w;
+        p->h[l] = h;
+        p->lv[l] = (double*)calloc((size_t)w * h * C, sizeof(double));
+        w = (w + 1) >> 1;
+        h = (h + 1) >> 1;
+    }
+}
+
+static void pyrd_free(pyrd_t* p)
+{
+    for (int l = 0; l < p->levels; ++l) {
+        free(p->lv[l]);
+    }
+}
+
+/* laplacianPyramid of a float image (src/pyramid.h:1647-1747): log mapping,
+ * Gaussian levels with alpha, then gp[l] -= expand(gp[l+1]). */
+static int laplacian_d(pyrd_t* p, const float* img, int pix_stride, const uint8_t* alpha0, int wrap)
+{
+    orc_real_to_pyramid(img, (int64_t)p->w[0] * p->h[0], p->C, pix_stride, p->lv[0]);
+    const uint8_t* a = alpha0;
+    uint8_t* owned = NULL;
+    int rc = 0;
+    for (int l = 1; l < p->levels && !rc; ++l) {
+        uint8_t* na = (uint8_t*)malloc((size_t)p->w[l] * p->h[l]);
+        rc = orc_reduce_alpha_d(wrap, p->lv[l - 1], a, p->w[l - 1], p->h[l - 1], p->C, p->lv[l], na);
+        free(owned);
+        owned = na;
+        a = na;
+    }
+    free(owned);
+    for (int l = 0; l + 1 < p->levels && !rc; ++l) {
+        rc = orc_expand_d(0, wrap, p->lv[l + 1], p->w[l + 1], p->h[l + 1], p->lv[l], p->w[l], p->h[l], p->C);
+    }
+    return rc;
+}
+
+static int collapse_d(pyrd_t* p, int wrap)
+{
+    for (int l = p->levels - 2; l >= 0; --l) {
+        const int rc = orc_expand_d(1, wrap, p->lv[l + 1], p->w[l + 1], p->h[l + 1], p->lv[l], p->w[l], p->h[l],
+                                    p->C);
+        if (rc) {
+            return rc;
+        }
+    }
+    return 0;
+}
+
+/* MultiGrayscaleAccessor on float RGB (src/mga.h:184-222), stored as float
+ * (fromRealPromote<float>).  NumericTraits<float>::RealPromote is float, so
+ * the average adds the three samples in float before the double division by
+ * 3.0, and the lightness adds min and max in float; luminance
+ * (RGBValue::luminance, 0.3/0.59/0.11 in double) and the mixer (double
+ * weights) are double expressions. */
+static float gray_float(const orc_enfuse_params* prm, float r, float g, float b, double mw0, double mw1, double mw2)
+{
+    const float mx = r > g ? (r > b ? r : b) : (g > b ? g : b);
+    const float mn = r < g ? (r < b ? r : b) : (g < b ? g : b);
+    switch (prm->gray_projector) {
+    case ORC_GRAY_VALUE: return mx;
+    case ORC_GRAY_ANTI_VALUE: return mn;
+    case ORC_GRAY_LIGHTNESS: {
+        const float s = mn + mx;
+        return (float)((double)s / 2.0);
+    }
+    case ORC_GRAY_LUMINANCE: return (float)(0.3 * r + 0.59 * g + 0.11 * b);
+    case ORC_GRAY_MIXER: return (float)(mw0 * (double)r + mw1 * (double)g + mw2 * (double)b);
+    default: {
+        const float s = (r + g) + b;
+        return (float)((double)s / 3.0);
+    }
+    }
+}
+
+static int cmp_f32(const void* a, const void* b)
+{
+    const float x = *(const float*)a, y = *(const float*)b;
+    return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+/* Histogram::entropyOfChannel over raw float keys (src/enfuse.h:346-375);
+ * keys compare as floats (-0 and +0 are one bin). */
+static double entropy_of_f(float* vals, int n)
+{
+    if (n == 0) {
+        return 0.0;
+    }
+    qsort(vals, (size_t)n, sizeof(float), cmp_f32);
+    int bins = 1;
+    for (int i = 1; i < n; ++i) {
+        bins += vals[i] != vals[i - 1];
+    }
+    if (bins <= 1) {
+        return 0.0;
+    }
+    double e = 0.0;
+    int i = 0;
+    while (i < n) {
+        int j = i;
+        while (j < n && vals[j] == vals[i]) {
+            ++j;
+        }
+        const double p = (double)(j - i) / (double)n;
+        e += p * log(p);
+        i = j;
+    }
+    return -e / log((double)bins);
+}
+
+/* enfuseMask for float images (src/enfuse.h:962-1212).  `range` stands for
+ * NumericTraits<float>::max() in the exposure (y = gray / max, :638) and
+ * entropy (H * max) weights: FLT_MAX is the reference's behaviour, 1.0 the
+ * normalised-float mode for images in [0, 1].  Saturation uses max_value 1.0
+ * (:758-761); contrast is W * sigma without a scale (:800-804, 818-823). */
+int orc_enfuse_mask_f(const float* img, int w, int h, int C, int pix_stride, const uint8_t* alpha,
+                      const orc_enfuse_params* prm, double range, float* out)
+{
+    if (C != 1 && C != 3) {
+        return -2;
+    }
+    const int64_t npix = (int64_t)w * h;
+    double mw0 = 0, mw1 = 0, mw2 = 0;
+    if (prm->gray_projector == ORC_GRAY_MIXER) {
+        const double s = prm->mixer[0] + prm->mixer[1] + prm->mixer[2];
+        mw0 = prm->mixer[0] / s;
+        mw1 = prm->mixer[1] / s;
+        mw2 = prm->mixer[2] / s;
+    }
+    float* gray = (float*)malloc(sizeof(float) * (size_t)npix);
+#pragma omp parallel for schedule(static)
+    for (int64_t p = 0; p < npix; ++p) {
+        const float* px = img + p * pix_stride;
+        gray[p] = C == 1 ? px[0] : gray_float(prm, px[0], px[1], px[2], mw0, mw1, mw2);
+    }
+    memset(out, 0, sizeof(float) * (size_t)npix);
+
+    if (prm->w_exposure > 0.0) {
+        const double ew = exposure_effective_width(prm->exp_function, prm->exp_width);
+#pragma omp parallel for schedule(static)
+        for (int64_t p = 0; p < npix; ++p) {
+            if (alpha[p]) {
+                /* toRealPromote(float) / max(): a float division (enfuse.h:638) */
+                const double y = (double)(gray[p] / (float)range);
+                out[p] = (float)(prm->w_exposure * exposure_weight(prm->exp_function, y, prm->exp_optimum, ew));
+            }
+        }
+    }
+
+    if (prm->w_contrast > 0.0) {
+        const int win = prm->contrast_window, b = win / 2;
+        if (win < 2 || w < win || h < win) {
+            free(gray);
+            return -1;
+        }
+#pragma omp parallel for schedule(static)
+        for (int y = b; y < h - b; ++y) {
+            for (int x = b; x < w - b; ++x) {
+                if (!alpha[(int64_t)y * w + x]) {
+                    continue;
+                }
+                double sum = 0.0;
+                int n = 0;
+                for (int yy = y - b; yy <= y + b; ++yy) {
+                    for (int xx = x - b; xx <= x + b; ++xx) {
+                        if (alpha[(int64_t)yy * w + xx]) {
+                            sum += gray[(int64_t)yy * w + xx];
+                            ++n;
+                        }
+                    }
+                }
+                float sd = 0.0f;
+                if (n > 1) {
+                    const double mean = sum / n;
+                    double ss = 0.0;
+                    for (int yy = y - b; yy <= y + b; ++yy) {
+                        for (int xx = x - b; xx <= x + b; ++xx) {
+                            if (alpha[(int64_t)yy * w + xx]) {
+                                const double d = gray[(int64_t)yy * w + xx] - mean;
+                                ss += d * d;
+                            }
+                        }
+                    }
+                    sd = (float)sqrt(ss / (double)(n - 1));
+                }
+                const int64_t p = (int64_t)y * w + x;
+                out[p] = (float)(prm->w_contrast * (double)sd) + out[p];
+            }
+        }
+    }
+
+    if (prm->w_saturation > 0.0 && C == 3) {
+#pragma omp parallel for schedule(static)
+        for (int64_t p = 0; p < npix; ++p) {
+            if (!alpha[p]) {
+                continue;
+            }
+            const float* px = img + p * pix_stride;
+            const float mx = px[0] > px[1] ? (px[0] > px[2] ? px[0] : px[2]) : (px[1] > px[2] ? px[1] : px[2]);
+            const float mn = px[0] < px[1] ? (px[0] < px[2] ? px[0] : px[2]) : (px[1] < px[2] ? px[1] : px[2]);
+            float sw = 0.0f;
+            if (mx != mn) {
+                const double sum = (double)mx + (double)mn;
+                const double diff = (double)mx - (double)mn;
+                const double s = sum <= 1.0 ? diff / sum : diff / (2.0 - sum);
+                sw = (float)(prm->w_saturation * s);
+            }
+            out[p] = sw + out[p];
+        }
+    }
+
+    if (prm->w_entropy > 0.0) {
+        const int win = prm->entropy_window, b = win / 2;
+        if (w < win || h < win) {
+            free(gray);
+            return -1;
+        }
+#pragma omp parallel
+        {
+            float* vals = (float*)malloc(sizeof(float) * (size_t)win * win);
+#pragma omp for schedule(static)
+            for (int y = b; y < h - b; ++y) {
+                for (int x = b; x < w - b; ++x) {
+                    if (!alpha[(int64_t)y * w + x]) {
+                        continue;
+                    }
+                    float mn = FLT_MAX;
+                    for (int c = 0; c < C; ++c) {
+                        int n = 0;
+                        for (int yy = y - b; yy <= y + b; ++yy) {
+                            for (int xx = x - b; xx <= x + b; ++xx) {
+                                const int64_t q = (int64_t)yy * w + xx;
+                                if (alpha[q]) {
+                                    const float v = img[q * pix_stride + c];
+                                    vals[n++] = v == 0.0f ? 0.0f : v;
+                                }
+                            }
+                        }
+                        const float e = (float)(entropy_of_f(vals, n) * range);
+                        mn = e < mn ? e : mn;
+                    }
+                    const int64_t p = (int64_t)y * w + x;
+                    out[p] = (float)(prm->w_entropy * (double)mn) + out[p];
+                }
+            }
+            free(vals);
+        }
+    }
+    free(gray);
+    return 0;
+}
+
+/* enfuseMain for float images (src/enfuse.h:1217-1617): weights (or
+ * masks_in), normalisation, double Laplacian pyramids, Int32 9.15 mask
+ * pyramids with the union alpha, merge, collapse, conversion back.
+ * level0_out: optional (h, w, C) double buffer of the collapsed level 0. */
+int orc_enfuse_f(int K, const float* const* imgs, const uint8_t* const* alphas, int w, int h, int C, int pix_stride,
+                 const orc_enfuse_params* prm, double range, int levels, int wrap, int hard_mask,
+                 const float* const* masks_in, float* out, uint8_t* out_alpha, double* level0_out, float* masks_out)
+{
+    if (K < 1 || (C != 1 && C != 3)) {
+        return -2;
+    }
+    const int64_t npix = (int64_t)w * h;
+    const int mfrac = 15;
+    const int32_t max_mask_pyr = 255 << mfrac;
+    int rc = 0;
+    float** masks = (float**)calloc((size_t)K, sizeof(float*));
+    float* norm = (float*)calloc((size_t)npix, sizeof(float));
+    memset(out_alpha, 0, (size_t)npix);
+    for (int k = 0; k < K && !rc; ++k) {
+        masks[k] = (float*)malloc(sizeof(float) * (size_t)npix);
+        if (masks_in) {
+            memcpy(masks[k], masks_in[k], sizeof(float) * (size_t)npix);
+        } else {
+            rc = orc_enfuse_mask_f(imgs[k], w, h, C, pix_stride, alphas[k], prm, range, masks[k]);
+        }
+        for (int64_t p = 0; p < npix && !rc; ++p) {
+            if (alphas[k][p]) {
+                out_alpha[p] = alphas[k][p];
+            }
+            norm[p] = masks[k][p] + norm[p];
+        }
+    }
+    if (!rc && hard_mask) {
+#pragma omp parallel for schedule(static)
+        for (int64_t p = 0; p < npix; ++p) {
+            float mx = 0.0f;
+            int mi = 0;
+            for (int k = 0; k < K; ++k) {
+                if (masks[k][p] > mx) {
+                    mx = masks[k][p];
+                    mi = k;
+                }
+            }
+            for (int k = 0; k < K; ++k) {
+                masks[k][p] = mx == 0.0f ? 255.0f / (float)K : (k == mi ? 255.0f : 0.0f);
+            }
+        }
+    }
+    levels = levels > 0 ? levels : orc_num_levels(w, h, 1, 0);
+    pyrd_t result;
+    pyrd_alloc(&result, levels, w, h, C);
+    for (int k = 0; k < K && !rc; ++k) {
+        pyrd_t lp;
+        pyr_t mg;
+        pyrd_alloc(&lp, levels, w, h, C);
+        rc = laplacian_d(&lp, imgs[k], pix_stride, alphas[k], wrap);
+        if (!hard_mask) {
+            const float fallback = (float)(255 / K);
+#pragma omp parallel for schedule(static)
+            for (int64_t p = 0; p < npix; ++p) {
+                masks[k][p] = norm[p] > 0.0f ? (255.0f * masks[k][p]) / norm[p] : fallback;
+            }
+        }
+        if (masks_out) {
+            memcpy(masks_out + (size_t)k * npix, masks[k], sizeof(float) * (size_t)npix);
+        }
+        pyr_alloc(&mg, levels, w, h, 1);
+        orc_fixed_from_float(masks[k], npix, mg.lv[0], mfrac, 32);
+        if (!rc) {
+            rc = gaussian_alpha(&mg, out_alpha, wrap, 32);
+        }
+        for (int l = 0; l < levels && !rc; ++l) {
+            orc_mask_multiply_d(lp.lv[l], mg.lv[l], (int64_t)lp.w[l] * lp.h[l], C, max_mask_pyr, result.lv[l]);
+        }
+        pyr_free(&mg);
+        pyrd_free(&lp);
+    }
+    if (!rc) {
+        rc = collapse_d(&result, wrap);
+    }
+    if (!rc) {
+        if (level0_out) {
+            memcpy(level0_out, result.lv[0], sizeof(double) * (size_t)npix * C);
+        }
+        memset(out, 0, sizeof(float) * (size_t)npix * pix_stride);
+        orc_real_from_pyramid(result.lv[0], out_alpha, npix, C, out, pix_stride);
+        if (pix_stride == 4) {
+            for (int64_t p = 0; p < npix; ++p) {
+                out[p * 4 + 3] = out_alpha[p] ? 1.0f : 0.0f;
+            }
+        }
+    }
+    pyrd_free(&result);
+    for (int k = 0; k < K; ++k) {
+        free(masks[k]);
+    }
+    free(masks);
+    free(norm);
+    return rc;
+}
+
+/* enblendMain's pyramid section for float images (src/enblend.h:330-510):
+ * Int32 9.15 mask Gaussian pyramid, double white/black Laplacian pyramids,
+ * blend, collapse, conversion back where the union alpha is set. */
+int orc_enblend_f(const float* white, const uint8_t* white_alpha, const float* black, const uint8_t* black_alpha,
+                  const uint8_t* mask, int w, int h, int C, int pix_stride, int levels, int wrap, float* out,
+                  uint8_t* out_alpha, double* level0_out)
+{
+    if (C > 4) {
+        return -2;
+    }
+    const int64_t npix = (int64_t)w * h;
+    const int mfrac = 15;
+    levels = levels > 0 ? levels : orc_num_levels(w, h, 1, 0);
+    pyr_t mg;
+    pyrd_t wl, bl;
+    pyr_alloc(&mg, levels, w, h, 1);
+    orc_fixed_from_int(mask, ORC_U8, npix, 1, 1, mg.lv[0], mfrac);
+    int rc = gaussian_noalpha(&mg, wrap, 32);
+    pyrd_alloc(&wl, levels, w, h, C);
+    pyrd_alloc(&bl, levels, w, h, C);
+    if (!rc) {
+        rc = laplacian_d(&wl, white, pix_stride, white_alpha, wrap);
+    }
+    if (!rc) {
+        rc = laplacian_d(&bl, black, pix_stride, black_alpha, wrap);
+    }
+    for (int64_t p = 0; p < npix; ++p) {
+        out_alpha[p] = white_alpha[p] ? 255 : black_alpha[p];
+    }
+    if (!rc) {
+        for (int l = 0; l < levels; ++l) {
+            orc_blend_d(mg.lv[l], wl.lv[l], bl.lv[l], (int64_t)bl.w[l] * bl.h[l], C, 255 << mfrac);
+        }
+        rc = collapse_d(&bl, wrap);
+    }
+    if (!rc) {
+        if (level0_out) {
+            memcpy(level0_out, bl.lv[0], sizeof(double) * (size_t)npix * C);
+        }
+        memcpy(out, black, sizeof(float) * (size_t)npix * pix_stride);
+        orc_real_from_pyramid(bl.lv[0], out_alpha, npix, C, out, pix_stride);
+        if (pix_stride == 4) {
+            for (int64_t p = 0; p < npix; ++p) {
+                out[p * 4 + 3] = out_alpha[p] ? 1.0f : 0.0f;
+            }
+        }
+    }
+    pyr_free(&mg);
+    pyrd_free(&wl);
+    pyrd_free(&bl);
+    return rc;
+}

@@ -137,6 +137,43 @@ int orc_enblend(const void* white, const uint8_t* white_alpha, const void* black
                 int C, int pix_stride, int levels, int wrap, void* out, uint8_t* out_alpha,
                 int dither_mode, uint64_t seed, int32_t* level0_out);
 
+/* ---- float images: double pyramids (src/numerictraits.h:185) -------------- */
+
+/* v >= 0 ? 1 + log1p(v) : 1 / (1 - v) (src/fixmath.h:165-187). */
+void orc_real_to_pyramid(const float* src, int64_t npix, int C, int pix_stride, double* dst);
+
+/* v >= 1 ? expm1(v - 1) : 1 - 1/v where alpha != 0 (src/fixmath.h:320-329). */
+void orc_real_from_pyramid(const double* src, const uint8_t* alpha, int64_t npix, int C, float* dst,
+                           int pix_stride);
+
+/* Reduce with alpha of a double level (src/pyramid.h:166-573, real division). */
+int orc_reduce_alpha_d(int wrap, const double* src, const uint8_t* alpha, int sw, int sh, int C, double* dst,
+                       uint8_t* dst_alpha);
+
+/* Expand into a double level; add=0: dst -= E(src), add=1: dst += E(src). */
+int orc_expand_d(int add, int wrap, const double* src, int sw, int sh, double* dst, int dw, int dh, int C);
+
+/* CartesianBlendFunctor on a double level (src/blend.h:41-76). */
+void orc_blend_d(const int32_t* mask, const double* white, double* black, int64_t npix, int C, int32_t white_value);
+
+/* ImageMaskMultiplyFunctor on a double level, accumulated into res when res != NULL. */
+void orc_mask_multiply_d(double* lp, const int32_t* mask, int64_t npix, int C, int32_t divisor, double* res);
+
+/* enfuseMask of a float image; range replaces NumericTraits<float>::max() in
+ * the exposure and entropy weights (FLT_MAX: reference, 1.0: normalised). */
+int orc_enfuse_mask_f(const float* img, int w, int h, int C, int pix_stride, const uint8_t* alpha,
+                      const orc_enfuse_params* p, double range, float* out);
+
+/* enfuse of float images (double pyramids); level0_out: optional double (h, w, C). */
+int orc_enfuse_f(int K, const float* const* imgs, const uint8_t* const* alphas, int w, int h, int C, int pix_stride,
+                 const orc_enfuse_params* p, double range, int levels, int wrap, int hard_mask,
+                 const float* const* masks_in, float* out, uint8_t* out_alpha, double* level0_out, float* masks_out);
+
+/* enblend of float images (double pyramids); level0_out: optional double (h, w, C). */
+int orc_enblend_f(const float* white, const uint8_t* white_alpha, const float* black, const uint8_t* black_alpha,
+                  const uint8_t* mask, int w, int h, int C, int pix_stride, int levels, int wrap, float* out,
+                  uint8_t* out_alpha, double* level0_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -77,6 +77,16 @@ def lib() -> ctypes.CDLL:
         L.orc_enfuse.argtypes = [i, vp, vp, i, i, i, i, i, ctypes.POINTER(OrcParams), i, i, i, vp, vp, vp, i, u64,
                                  vp, vp]
         L.orc_enblend.argtypes = [vp, vp, vp, vp, vp, i, i, i, i, i, i, i, vp, vp, i, u64, vp]
+        L.orc_real_to_pyramid.argtypes = [vp, i64, i, i, vp]
+        L.orc_real_from_pyramid.argtypes = [vp, vp, i64, i, vp, i]
+        L.orc_reduce_alpha_d.argtypes = [i, vp, vp, i, i, i, vp, vp]
+        L.orc_expand_d.argtypes = [i, i, vp, i, i, vp, i, i, i]
+        L.orc_blend_d.argtypes = [vp, vp, vp, i64, i, ctypes.c_int32]
+        L.orc_mask_multiply_d.argtypes = [vp, vp, i64, i, ctypes.c_int32, vp]
+        L.orc_enfuse_mask_f.argtypes = [vp, i, i, i, i, vp, ctypes.POINTER(OrcParams), dbl, vp]
+        L.orc_enfuse_f.argtypes = [i, vp, vp, i, i, i, i, ctypes.POINTER(OrcParams), dbl, i, i, i, vp, vp, vp,
+                                   vp, vp]
+        L.orc_enblend_f.argtypes = [vp, vp, vp, vp, vp, i, i, i, i, i, i, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -119,6 +129,9 @@ def num_levels(w, h, min_levels=1, exact_levels=0) -> int:
 
 def alpha_of(img: np.ndarray) -> np.ndarray:
     """Alpha plane of an image: thresholded 4th component (src/assemble.h:240-253) or opaque."""
+    if img.ndim == 3 and img.shape[2] == 4 and img.dtype == np.float32:
+        a = img[..., 3]
+        return np.where((a >= np.float32(0.5)) & (a <= np.float32(1.0)), 255, 0).astype(np.uint8)
     if img.ndim == 3 and img.shape[2] == 4:
         maxv = 255 if img.dtype == np.uint8 else 65535
         lo = int(maxv / 2.0)
@@ -281,6 +294,134 @@ def enblend(white: np.ndarray, black: np.ndarray, mask: np.ndarray, white_alpha=
                            int(wrap), _p(out), _p(oa), DITHER[dither], seed, _p(l0))
     if rc:
         raise ValueError(f"orc_enblend failed ({rc})")
+    res = {"out": out, "alpha": oa}
+    if want_level0:
+        res["level0"] = l0
+    return res
+
+
+# ---- float images: double pyramids ------------------------------------------
+
+FLT_MAX = float(np.finfo(np.float32).max)
+
+
+def real_to_pyramid(img: np.ndarray) -> np.ndarray:
+    """(H, W, S) float32 image -> (H, W, C) double level 0 (log mapping)."""
+    img, w, h, C, s = _geom(np.asarray(img, np.float32))
+    out = np.empty((h, w, C), np.float64)
+    lib().orc_real_to_pyramid(_p(img), w * h, C, s, _p(out))
+    return out
+
+
+def real_from_pyramid(src: np.ndarray, alpha: np.ndarray, out: Optional[np.ndarray] = None) -> np.ndarray:
+    src = np.ascontiguousarray(src, np.float64)
+    h, w, C = src.shape
+    if out is None:
+        out = np.zeros((h, w, C), np.float32)
+    out = np.ascontiguousarray(out, np.float32)
+    lib().orc_real_from_pyramid(_p(src), _p(np.ascontiguousarray(alpha, np.uint8)), w * h, C, _p(out),
+                                out.shape[2] if out.ndim == 3 else 1)
+    return out
+
+
+def reduce_d(src: np.ndarray, alpha: np.ndarray, wrap: bool = False):
+    src = np.ascontiguousarray(src, np.float64)
+    h, w, C = src.shape
+    dh, dw = (h + 1) >> 1, (w + 1) >> 1
+    dst = np.empty((dh, dw, C), np.float64)
+    da = np.empty((dh, dw), np.uint8)
+    if lib().orc_reduce_alpha_d(int(wrap), _p(src), _p(np.ascontiguousarray(alpha, np.uint8)), w, h, C, _p(dst),
+                                _p(da)):
+        raise ValueError("reduce precondition failed")
+    return dst, da
+
+
+def expand_d(src: np.ndarray, dst: np.ndarray, add: bool, wrap: bool = False) -> np.ndarray:
+    src = np.ascontiguousarray(src, np.float64)
+    out = np.array(dst, np.float64, copy=True, order="C")
+    sh, sw, C = src.shape
+    dh, dw, _ = out.shape
+    if lib().orc_expand_d(int(add), int(wrap), _p(src), sw, sh, _p(out), dw, dh, C):
+        raise ValueError("expand precondition failed")
+    return out
+
+
+def blend_d(mask: np.ndarray, white: np.ndarray, black: np.ndarray, white_value: int) -> np.ndarray:
+    mask = np.ascontiguousarray(mask, np.int32)
+    white = np.ascontiguousarray(white, np.float64)
+    out = np.array(black, np.float64, copy=True, order="C")
+    lib().orc_blend_d(_p(mask), _p(white), _p(out), mask.size, out.shape[2], white_value)
+    return out
+
+
+def mask_multiply_d(lp: np.ndarray, mask: np.ndarray, divisor: int, res: Optional[np.ndarray] = None):
+    """Returns (lp * mask / divisor, res + that) (res None: only the product)."""
+    out = np.array(lp, np.float64, copy=True, order="C")
+    r = None if res is None else np.array(res, np.float64, copy=True, order="C")
+    mask = np.ascontiguousarray(mask, np.int32)
+    lib().orc_mask_multiply_d(_p(out), _p(mask), mask.size, out.shape[2], divisor, _p(r))
+    return out, r
+
+
+def enfuse_mask_f(img: np.ndarray, alpha: Optional[np.ndarray], prm: OrcParams, range_: float = FLT_MAX):
+    img, w, h, C, s = _geom(np.asarray(img, np.float32))
+    if alpha is None:
+        alpha = alpha_of(img)
+    alpha = np.ascontiguousarray(alpha, np.uint8)
+    out = np.zeros((h, w), np.float32)
+    rc = lib().orc_enfuse_mask_f(_p(img), w, h, C, s, _p(alpha), ctypes.byref(prm), range_, _p(out))
+    if rc:
+        raise ValueError(f"orc_enfuse_mask_f failed ({rc})")
+    return out
+
+
+def enfuse_f(images: Sequence[np.ndarray], alphas: Optional[Sequence[np.ndarray]] = None,
+             prm: Optional[OrcParams] = None, range_: float = FLT_MAX, masks=None, levels: int = 0,
+             wrap: bool = False, hard_mask: bool = False, want_level0: bool = False, want_masks: bool = False):
+    """enfuseMain for float32 images (double pyramids).  Returns dict(out, alpha[, level0][, masks])."""
+    imgs = [_geom(np.asarray(x, np.float32))[0] for x in images]
+    _, w, h, C, s = _geom(imgs[0])
+    K = len(imgs)
+    if alphas is None:
+        alphas = [alpha_of(x) for x in imgs]
+    alphas = [np.ascontiguousarray(a, np.uint8) for a in alphas]
+    prm = prm if prm is not None else params()
+    ip = (ctypes.c_void_p * K)(*[x.ctypes.data for x in imgs])
+    ap = (ctypes.c_void_p * K)(*[a.ctypes.data for a in alphas])
+    mp = None
+    if masks is not None:
+        masks = [np.ascontiguousarray(m, np.float32) for m in masks]
+        mp = (ctypes.c_void_p * K)(*[m.ctypes.data for m in masks])
+    out = np.zeros_like(imgs[0])
+    oa = np.zeros((h, w), np.uint8)
+    l0 = np.zeros((h, w, C), np.float64) if want_level0 else None
+    mo = np.zeros((K, h, w), np.float32) if want_masks else None
+    rc = lib().orc_enfuse_f(K, ip, ap, w, h, C, s, ctypes.byref(prm), range_, levels, int(wrap), int(hard_mask), mp,
+                            _p(out), _p(oa), _p(l0), _p(mo))
+    if rc:
+        raise ValueError(f"orc_enfuse_f failed ({rc})")
+    res = {"out": out, "alpha": oa}
+    if want_level0:
+        res["level0"] = l0
+    if want_masks:
+        res["masks"] = mo
+    return res
+
+
+def enblend_f(white: np.ndarray, black: np.ndarray, mask: np.ndarray, white_alpha=None, black_alpha=None,
+              levels: int = 0, wrap: bool = False, want_level0: bool = False):
+    white, w, h, C, s = _geom(np.asarray(white, np.float32))
+    black = _geom(np.asarray(black, np.float32))[0]
+    wa = np.ascontiguousarray(white_alpha if white_alpha is not None else alpha_of(white), np.uint8)
+    ba = np.ascontiguousarray(black_alpha if black_alpha is not None else alpha_of(black), np.uint8)
+    mask = np.ascontiguousarray(mask, np.uint8)
+    out = np.zeros_like(black)
+    oa = np.zeros((h, w), np.uint8)
+    l0 = np.zeros((h, w, C), np.float64) if want_level0 else None
+    rc = lib().orc_enblend_f(_p(white), _p(wa), _p(black), _p(ba), _p(mask), w, h, C, s, levels, int(wrap), _p(out),
+                             _p(oa), _p(l0))
+    if rc:
+        raise ValueError(f"orc_enblend_f failed ({rc})")
     res = {"out": out, "alpha": oa}
     if want_level0:
         res["level0"] = l0

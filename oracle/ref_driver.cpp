@@ -182,9 +182,9 @@ int run_expand(int add, int wrap, const void* src, int sw, int sh, void* dst, in
 // enblendMain's pyramid section (src/enblend.h:384-510) over the whole
 // canvas: mask Gaussian pyramid, white and black Laplacian pyramids with
 // alpha, blend, collapse.  Writes the collapsed level 0 (int32, (h, w, C)).
-template <class T, int C>
+template <class T, int C, class L0>
 int run_enblend(int levels, int wrap, const T* white, const uint8_t* wa, const T* black, const uint8_t* ba,
-                const uint8_t* mask, int w, int h, int32_t* level0)
+                const uint8_t* mask, int w, int h, L0* level0)
 {
     typedef EnblendNumericTraits<typename Pix<T, C>::type> Tr;
     typedef typename Tr::ImageType ImageType;
@@ -229,7 +229,7 @@ int run_enblend(int levels, int wrap, const T* white, const uint8_t* wa, const T
     std::vector<PC> tmp((size_t)w * h * C);
     from_image(l0, tmp.data());
     for (size_t i = 0; i < tmp.size(); ++i) {
-        level0[i] = (int32_t)tmp[i];
+        level0[i] = (L0)tmp[i];
     }
     for (auto* p : *maskGP) delete p;
     for (auto* p : *whiteLP) delete p;
@@ -243,8 +243,8 @@ int run_enblend(int levels, int wrap, const T* white, const uint8_t* wa, const T
 // copyFromPyramidImageIf (src/fixmath.h:2158-2294): the collapsed level 0
 // (int32, (h, w, 3)) to RGB pixels where the alpha plane is nonzero, with the
 // reference's dithering conversion (Mersenne Twister draws).
-template <class T>
-int run_from_pyramid(const int32_t* level0, const uint8_t* alpha, int w, int h, T* out)
+template <class T, class L0>
+int run_from_pyramid(const L0* level0, const uint8_t* alpha, int w, int h, T* out)
 {
     typedef EnblendNumericTraits<vigra::RGBValue<T>> Tr;
     typedef typename Tr::ImagePyramidType ImagePyramidType;
@@ -276,8 +276,8 @@ extern "C" {
 int ref_from_pyramid(int bits, const int32_t* level0, const uint8_t* alpha, int w, int h, void* out)
 {
     try {
-        return bits == 8 ? run_from_pyramid<vigra::UInt8>(level0, alpha, w, h, (vigra::UInt8*)out)
-                         : run_from_pyramid<vigra::UInt16>(level0, alpha, w, h, (vigra::UInt16*)out);
+        return bits == 8 ? run_from_pyramid<vigra::UInt8, int32_t>(level0, alpha, w, h, (vigra::UInt8*)out)
+                         : run_from_pyramid<vigra::UInt16, int32_t>(level0, alpha, w, h, (vigra::UInt16*)out);
     } catch (const std::exception& e) {
         std::cerr << "ref_from_pyramid: " << e.what() << std::endl;
         return 1;
@@ -332,6 +332,57 @@ int ref_enblend(int bits, int levels, int wrap, const void* white, const uint8_t
                                              (const vigra::UInt16*)black, black_alpha, mask, w, h, level0);
     } catch (const std::exception& e) {
         std::cerr << "ref_enblend: " << e.what() << std::endl;
+        return 1;
+    }
+}
+
+// ---- float images: double pyramids (src/numerictraits.h:185) --------------
+// Pyramid levels are (h, w, C) double arrays, pixel images (H, W, 3) float.
+
+// Reduce of one double level (pyramid.h:166-573 with SKIPSMImagePixelType double).
+int ref_reduce_f(int C, int alpha, int wrap, const double* src, const uint8_t* src_alpha, int sw, int sh,
+                 double* dst, uint8_t* dst_alpha)
+{
+    try {
+        return C == 1 ? run_reduce<float, 1>(alpha, wrap, src, src_alpha, sw, sh, dst, dst_alpha)
+                      : run_reduce<float, 3>(alpha, wrap, src, src_alpha, sw, sh, dst, dst_alpha);
+    } catch (const std::exception& e) {
+        std::cerr << "ref_reduce_f: " << e.what() << std::endl;
+        return 1;
+    }
+}
+
+// Expand of one double level into dst (pyramid.h:1102-1457).
+int ref_expand_f(int C, int add, int wrap, const double* src, int sw, int sh, double* dst, int dw, int dh)
+{
+    try {
+        return C == 1 ? run_expand<float, 1>(add, wrap, src, sw, sh, dst, dw, dh)
+                      : run_expand<float, 3>(add, wrap, src, sw, sh, dst, dw, dh);
+    } catch (const std::exception& e) {
+        std::cerr << "ref_expand_f: " << e.what() << std::endl;
+        return 1;
+    }
+}
+
+// The pyramid section of enblendMain on float RGB images: collapsed level 0
+// (double, (h, w, 3)) and the float pixels copyFromPyramidImageIf makes of
+// it where the union alpha is set (out keeps its values elsewhere).
+int ref_enblend_f(int levels, int wrap, const float* white, const uint8_t* white_alpha, const float* black,
+                  const uint8_t* black_alpha, const uint8_t* mask, int w, int h, double* level0, float* out)
+{
+    try {
+        const int rc = run_enblend<float, 3, double>(levels, wrap, white, white_alpha, black, black_alpha, mask, w,
+                                                     h, level0);
+        if (rc) {
+            return rc;
+        }
+        std::vector<uint8_t> ua((size_t)w * h);
+        for (size_t i = 0; i < ua.size(); ++i) {
+            ua[i] = white_alpha[i] ? 255 : black_alpha[i];
+        }
+        return run_from_pyramid<float, double>(level0, ua.data(), w, h, out);
+    } catch (const std::exception& e) {
+        std::cerr << "ref_enblend_f: " << e.what() << std::endl;
         return 1;
     }
 }

@@ -71,6 +71,9 @@ def lib() -> Optional[ctypes.CDLL]:
         L.ref_expand.argtypes = [i, i, i, i, vp, i, i, vp, i, i]
         L.ref_enblend.argtypes = [i, i, i, vp, vp, vp, vp, vp, i, i, vp]
         L.ref_from_pyramid.argtypes = [i, vp, vp, i, i, vp]
+        L.ref_reduce_f.argtypes = [i, i, i, vp, vp, i, i, vp, vp]
+        L.ref_expand_f.argtypes = [i, i, i, vp, i, i, vp, i, i]
+        L.ref_enblend_f.argtypes = [i, i, vp, vp, vp, vp, vp, i, i, vp, vp]
         _lib = L
     return _lib
 
@@ -130,3 +133,43 @@ def from_pyramid(level0: np.ndarray, alpha: np.ndarray, dtype, fill: int = 0) ->
     if lib().ref_from_pyramid(bits, _p(l0), _p(np.ascontiguousarray(alpha, np.uint8)), w, h, _p(out)):
         raise ValueError("reference conversion failed")
     return out
+
+
+# ---- float images: double pyramids ------------------------------------------
+
+def reduce_f(src: np.ndarray, alpha: Optional[np.ndarray], wrap: bool = False):
+    """Reduce of one (H, W, C) double level of a float image's pyramid.
+    Returns (dst, dst_alpha) with alpha, else dst (float64 arrays)."""
+    s = np.ascontiguousarray(src, np.float64)
+    h, w, C = s.shape
+    dh, dw = (h + 1) >> 1, (w + 1) >> 1
+    d = np.zeros((dh, dw, C), np.float64)
+    da = np.zeros((dh, dw), np.uint8)
+    a = np.ascontiguousarray(alpha, np.uint8) if alpha is not None else None
+    if lib().ref_reduce_f(C, int(alpha is not None), int(wrap), _p(s), _p(a), w, h, _p(d), _p(da)):
+        raise ValueError("reference reduce failed")
+    return (d, da) if alpha is not None else d
+
+
+def expand_f(src: np.ndarray, dst: np.ndarray, add: bool, wrap: bool = False) -> np.ndarray:
+    s = np.ascontiguousarray(src, np.float64)
+    d = np.array(dst, np.float64, copy=True, order="C")
+    sh, sw, C = s.shape
+    dh, dw, _ = d.shape
+    if lib().ref_expand_f(C, int(add), int(wrap), _p(s), sw, sh, _p(d), dw, dh):
+        raise ValueError("reference expand failed")
+    return d
+
+
+def enblend_f(white: np.ndarray, white_alpha: np.ndarray, black: np.ndarray, black_alpha: np.ndarray,
+              mask: np.ndarray, levels: int, wrap: bool = False):
+    """enblendMain's pyramid blend of (H, W, 3) float32 images.  Returns
+    (collapsed double level 0, float output: black where the union alpha is 0)."""
+    h, w, _ = white.shape
+    l0 = np.zeros((h, w, 3), np.float64)
+    out = np.array(black, np.float32, copy=True, order="C")
+    args = [np.ascontiguousarray(x) for x in (white.astype(np.float32), white_alpha, black.astype(np.float32),
+                                              black_alpha, mask)]
+    if lib().ref_enblend_f(levels, int(wrap), *[_p(a) for a in args], w, h, _p(l0), _p(out)):
+        raise ValueError("reference enblend failed")
+    return l0, out

@@ -1,4 +1,4 @@
-"""Generate tests/golden/reference_pyramid.npz from the reference's own code.
+"""Generate tests/golden/reference_pyramid.npz and reference_float.npz from the reference's own code.
 
 Runs the reference-code oracle (oracle/reference_build.py: the reference's
 pyramid.h / blend.h / fixmath.h compiled unmodified against the project's
@@ -21,6 +21,48 @@ from oracle import oracle as orc  # noqa: E402
 from oracle import reference_build as ref  # noqa: E402
 
 OUT = Path(__file__).resolve().parent / "reference_pyramid.npz"
+OUT_FLOAT = Path(__file__).resolve().parent / "reference_float.npz"
+
+
+def float_cases() -> None:
+    """Float images: the reference's double pyramids (reduce, expand, enblend)."""
+    rng = np.random.default_rng(20261204)
+    data = {}
+    k = 0
+    for (h, w, off) in [(24, 36, 20), (41, 57, 33)]:
+        for wrap in (False, True):
+            white, black, mask = synthetic.panorama_pair(h, w, off, np.float32, seed=300 + k)
+            mask[: h // 3, off + 2: off + 9] = 128
+            wa, ba = orc.alpha_of(white).copy(), orc.alpha_of(black)
+            wa[3:7, off + 3: off + 11] = 0
+            W, B = np.ascontiguousarray(white[..., :3]), np.ascontiguousarray(black[..., :3])
+            W[0, 0] = -0.25  # negative samples take the rational branch of the mapping
+            levels = orc.num_levels(w, h)
+            l0, out = ref.enblend_f(W, wa, B, ba, mask, levels, wrap)
+            for name, a in (("white", W), ("white_alpha", wa), ("black", B), ("black_alpha", ba),
+                            ("mask", mask), ("level0", l0), ("out", out)):
+                data[f"fenblend{k}_{name}"] = a
+            data[f"fenblend{k}_meta"] = np.array([levels, int(wrap)], np.int32)
+            k += 1
+    data["fenblend_count"] = np.array(k)
+    k = 0
+    for C in (1, 3):
+        for wrap in (False, True):
+            h, w = int(rng.integers(5, 23)), int(rng.integers(5, 23))
+            src = rng.random((h, w, C)) * 2.0 + 0.5
+            alpha = np.where(rng.random((h, w)) < 0.8, 255, 0).astype(np.uint8)
+            d, da = ref.reduce_f(src, alpha, wrap)
+            coarse = rng.random(((h + 1) >> 1, (w + 1) >> 1, C)) - 0.5
+            fine = rng.random((h, w, C)) * 2.0
+            for name, a in (("src", src), ("alpha", alpha), ("dst", d), ("dst_alpha", da), ("coarse", coarse),
+                            ("fine", fine), ("sub", ref.expand_f(coarse, fine, False, wrap)),
+                            ("add", ref.expand_f(coarse, fine, True, wrap))):
+                data[f"fstep{k}_{name}"] = a
+            data[f"fstep{k}_meta"] = np.array([int(wrap)], np.int32)
+            k += 1
+    data["fstep_count"] = np.array(k)
+    np.savez_compressed(OUT_FLOAT, **data)
+    print(f"wrote {OUT_FLOAT} ({OUT_FLOAT.stat().st_size} bytes)")
 
 
 def main() -> None:
@@ -84,6 +126,7 @@ def main() -> None:
         data[f"convert{bits}_out"] = ref.from_pyramid(l0, alpha, dt, fill=7)
     np.savez_compressed(OUT, **data)
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes)")
+    float_cases()
 
 
 if __name__ == "__main__":

@@ -112,3 +112,48 @@ def test_live_enblend(orc, dt, wrap):
         want = ref.enblend_level0(W, wa, B, ba, mask, levels, wrap)
         got = orc.enblend(W, B, mask, white_alpha=wa, black_alpha=ba, wrap=wrap, want_level0=True)["level0"]
         assert np.array_equal(got, want)
+
+
+# ---- float images: the reference's double pyramids ------------------------
+
+GOLDEN_F = np.load(Path(__file__).resolve().parent / "golden" / "reference_float.npz")
+
+
+@pytest.mark.parametrize("k", range(int(GOLDEN_F["fenblend_count"])))
+def test_golden_float_enblend(orc, k):
+    """Float enblend: double level 0 to 1e-13 relative (summation order), output pixels identical."""
+    g = {n: GOLDEN_F[f"fenblend{k}_{n}"]
+         for n in ("white", "white_alpha", "black", "black_alpha", "mask", "level0", "out")}
+    levels, wrap = (int(v) for v in GOLDEN_F[f"fenblend{k}_meta"])
+    res = orc.enblend_f(g["white"], g["black"], g["mask"], white_alpha=g["white_alpha"],
+                        black_alpha=g["black_alpha"], levels=levels, wrap=bool(wrap), want_level0=True)
+    assert np.allclose(res["level0"], g["level0"], rtol=1e-13, atol=1e-13)
+    assert np.array_equal(res["out"], g["out"])
+
+
+@pytest.mark.parametrize("k", range(int(GOLDEN_F["fstep_count"])))
+def test_golden_float_reduce_expand(orc, k):
+    (wrap,) = (bool(v) for v in GOLDEN_F[f"fstep{k}_meta"])
+    d, da = orc.reduce_d(GOLDEN_F[f"fstep{k}_src"], GOLDEN_F[f"fstep{k}_alpha"], wrap)
+    assert np.array_equal(da, GOLDEN_F[f"fstep{k}_dst_alpha"])
+    assert np.allclose(d, GOLDEN_F[f"fstep{k}_dst"], rtol=1e-14, atol=1e-14)
+    coarse, fine = GOLDEN_F[f"fstep{k}_coarse"], GOLDEN_F[f"fstep{k}_fine"]
+    assert np.allclose(orc.expand_d(coarse, fine, False, wrap), GOLDEN_F[f"fstep{k}_sub"], rtol=1e-14, atol=1e-14)
+    assert np.allclose(orc.expand_d(coarse, fine, True, wrap), GOLDEN_F[f"fstep{k}_add"], rtol=1e-14, atol=1e-14)
+
+
+@live
+@pytest.mark.parametrize("wrap", [False, True])
+def test_live_float_enblend(orc, wrap):
+    from enbgpu import synthetic
+    for (h, w, off) in [(60, 90, 50), (31, 45, 24)]:
+        white, black, mask = synthetic.panorama_pair(h, w, off, np.float32, seed=17)
+        mask[: h // 2, off + 1: off + 6] = 200
+        wa, ba = orc.alpha_of(white), orc.alpha_of(black)
+        W, B = np.ascontiguousarray(white[..., :3]), np.ascontiguousarray(black[..., :3])
+        W[1, 1], B[2, 2] = -0.5, 1.75
+        levels = orc.num_levels(W.shape[1], W.shape[0])
+        l0, out = ref.enblend_f(W, wa, B, ba, mask, levels, wrap)
+        got = orc.enblend_f(W, B, mask, white_alpha=wa, black_alpha=ba, wrap=wrap, want_level0=True)
+        assert np.allclose(got["level0"], l0, rtol=1e-13, atol=1e-13)
+        assert np.array_equal(got["out"], out)
