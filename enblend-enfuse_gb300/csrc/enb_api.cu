@@ -50,6 +50,33 @@ struct enb_ctx {
     // host-transfer stream and events of the banded host-buffer path
     cudaStream_t copy_stream = nullptr;
     std::vector<cudaEvent_t> io_events;
+    // batched stacks: plan (workspace, job tables) and graph of the last
+    // batch geometry, staging buffers of host-buffer batches
+    struct BatchCache {
+        std::string key;
+        BatchPlan* plan = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        cudaStream_t gs = nullptr;
+        cudaEvent_t ev[2] = {nullptr, nullptr};
+        void* stage = nullptr;
+        ~BatchCache()
+        {
+            if (exec) {
+                cudaGraphExecDestroy(exec);
+            }
+            batch_plan_destroy(plan);
+            cudaFree(stage);
+            for (cudaEvent_t e : ev) {
+                if (e) {
+                    cudaEventDestroy(e);
+                }
+            }
+            if (gs) {
+                cudaStreamDestroy(gs);
+            }
+        }
+    };
+    std::unique_ptr<BatchCache> batch;
 };
 
 struct enb_pyramid {
@@ -1228,6 +1255,10 @@ enb_status enb_destroy(enb_ctx* ctx)
         cudaStreamSynchronize(ctx->copy_stream);
         cudaStreamDestroy(ctx->copy_stream);
     }
+    if (ctx->batch) {
+        cudaDeviceSynchronize();
+        ctx->batch.reset();
+    }
     delete ctx;
     return ENB_OK;
 }
@@ -1316,6 +1347,7 @@ void enb_default_fuse_options(enb_fuse_options* o)
     memset(o, 0, sizeof *o);
     o->dither = ENB_DITHER_HASH;
     o->seed = 0x5eed;
+    o->graph = 1;
 }
 
 int enb_num_levels(int w, int h, int min_levels, int exact_levels)
@@ -1791,6 +1823,286 @@ enb_status enb_enblend(enb_ctx* ctx, const enb_image* white, const enb_image* wh
         ENB_CUDA(ctx, cudaMemcpyAsync(o.level0_out, l0.p, (size_t)w * h * C * 4, cudaMemcpyDeviceToHost, ctx->stream));
     }
     ENB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return ENB_OK;
+}
+
+// ---- batched stacks ---------------------------------------------------------
+
+static enb_status float_weight_params(enb_ctx* ctx, const enb_enfuse_params* prm, FloatWeightParams& wp)
+{
+    ENB_TRY(build_tables(ctx, prm, 1u));
+    wp = FloatWeightParams{};
+    wp.use_exposure = prm->w_exposure > 0.0;
+    wp.use_contrast = prm->w_contrast > 0.0;
+    wp.use_saturation = prm->w_saturation > 0.0;
+    wp.use_entropy = prm->w_entropy > 0.0;
+    wp.contrast_window = prm->contrast_window;
+    wp.entropy_window = prm->entropy_window;
+    wp.gray_projector = prm->gray_projector;
+    wp.exp_function = prm->exp_function;
+    if (prm->gray_projector == ENB_GRAY_MIXER) {
+        const double sm = prm->mixer[0] + prm->mixer[1] + prm->mixer[2];
+        for (int i = 0; i < 3; ++i) {
+            wp.mixer[i] = prm->mixer[i] / sm;
+        }
+    }
+    wp.w_exposure = (float)prm->w_exposure;
+    wp.w_contrast = (float)prm->w_contrast;
+    wp.w_saturation = (float)prm->w_saturation;
+    wp.w_entropy = (float)prm->w_entropy;
+    const double range = float_range_of(prm);
+    wp.range = (float)range;
+    wp.opt_hi = (float)prm->exp_optimum;
+    wp.opt_lo = (float)(prm->exp_optimum - (double)wp.opt_hi);
+    const double inv_width = 1.0 / exposure_effective_width(prm->exp_function, prm->exp_width);
+    wp.inv_hi = (float)inv_width;
+    wp.inv_lo = (float)(inv_width - (double)wp.inv_hi);
+    return ENB_OK;
+}
+
+enb_status enb_fuse_stacks(enb_ctx* ctx, const enb_enfuse_params* prm, int n, const enb_stack* stacks,
+                           const enb_fuse_options* opt)
+{
+    if (!ctx) {
+        return ENB_ERR_INVALID;
+    }
+    enb_fuse_options o;
+    enb_default_fuse_options(&o);
+    if (opt) {
+        o = *opt;
+    }
+    ENB_CHECK(ctx, n >= 1 && stacks, "fuse_stacks: need at least one stack");
+    int C = -1;
+    for (int i = 0; i < n; ++i) {
+        const enb_stack& st = stacks[i];
+        ENB_CHECK(ctx, st.K >= 1 && st.K <= ENB_BATCH_MAX_K && st.images && st.out,
+                  "fuse_stacks: each stack needs 1..16 images and an output");
+        for (int k = 0; k < st.K; ++k) {
+            ENB_CHECK(ctx, pixels_ok(&st.images[k]) && st.images[k].dtype == ENB_F32,
+                      "fuse_stacks: images must be interleaved F32 with 1 or 3 channels");
+            ENB_CHECK(ctx, same_geometry(&st.images[k], &st.images[0]), "fuse_stacks: a stack's images differ");
+            if (st.alphas && st.alphas[k].data) {
+                ENB_CHECK(ctx, bytes_ok(&st.alphas[k], st.images[0].width, st.images[0].height),
+                          "fuse_stacks: alpha planes must be U8 of the image size");
+            }
+        }
+        ENB_CHECK(ctx, pixels_ok(st.out) && same_geometry(st.out, &st.images[0]),
+                  "fuse_stacks: out must match the stack's images");
+        if (st.out_alpha && st.out_alpha->data) {
+            ENB_CHECK(ctx, bytes_ok(st.out_alpha, st.images[0].width, st.images[0].height),
+                      "fuse_stacks: out_alpha must be U8 of the image size");
+        }
+        ENB_CHECK(ctx, C < 0 || st.images[0].channels == C, "fuse_stacks: all stacks need the same channel count");
+        C = st.images[0].channels;
+        ENB_TRY(check_params(ctx, prm, st.images[0].width, st.images[0].height));
+    }
+    if (o.plain) {
+        // the plain per-stack path: enb_enfuse stack by stack
+        for (int i = 0; i < n; ++i) {
+            enb_fuse_options so = o;
+            so.plain = 0;
+            so.level0_out = nullptr;
+            ENB_TRY(enb_enfuse(ctx, prm, stacks[i].K, stacks[i].images, stacks[i].alphas, nullptr, stacks[i].out,
+                               stacks[i].out_alpha, &so));
+        }
+        return ENB_OK;
+    }
+    FloatWeightParams wp;
+    ENB_TRY(float_weight_params(ctx, prm, wp));
+    const int64_t coarse = o.coarse_pixels == 0 ? 4096 : (o.coarse_pixels < 0 ? 0 : o.coarse_pixels);
+    // cache key: every descriptor, the parameters and the options
+    std::string key;
+    auto put = [&key](const void* p, size_t b) { key.append((const char*)p, b); };
+    put(&n, sizeof n);
+    put(prm, sizeof *prm);
+    put(&coarse, sizeof coarse);
+    put(&o.levels, sizeof o.levels);
+    put(&o.wrap, sizeof o.wrap);
+    put(&o.hard_mask, sizeof o.hard_mask);
+    put(&o.host_buffers, sizeof o.host_buffers);
+    put(&ctx->tables.plogp_fx, sizeof(void*));
+    for (int i = 0; i < n; ++i) {
+        const enb_stack& st = stacks[i];
+        put(&st.K, sizeof st.K);
+        for (int k = 0; k < st.K; ++k) {
+            put(&st.images[k], sizeof(enb_image));
+            const void* ap = st.alphas ? st.alphas[k].data : nullptr;
+            put(&ap, sizeof ap);
+            if (ap) {
+                put(&st.alphas[k].pitch, sizeof(int64_t));
+            }
+        }
+        put(st.out, sizeof(enb_image));
+        const void* oa = st.out_alpha ? st.out_alpha->data : nullptr;
+        put(&oa, sizeof oa);
+        if (oa) {
+            put(&st.out_alpha->pitch, sizeof(int64_t));
+        }
+    }
+    if (!ctx->batch) {
+        ctx->batch.reset(new enb_ctx::BatchCache());
+        ENB_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->batch->gs, cudaStreamNonBlocking));
+        ENB_CUDA(ctx, cudaEventCreateWithFlags(&ctx->batch->ev[0], cudaEventDisableTiming));
+        ENB_CUDA(ctx, cudaEventCreateWithFlags(&ctx->batch->ev[1], cudaEventDisableTiming));
+    }
+    enb_ctx::BatchCache& bc = *ctx->batch;
+    // host buffers: device copies of every image (kept with the plan)
+    std::vector<size_t> in_off, out_off, oa_off;
+    size_t stage_bytes = 0;
+    auto img_bytes = [](const enb_image& im) {
+        const int stride = im.pix_stride > 0 ? im.pix_stride : im.channels;
+        return (size_t)im.width * stride * 4 * (size_t)im.height;
+    };
+    auto up256 = [](size_t v) { return (v + 255) & ~(size_t)255; };
+    if (o.host_buffers) {
+        for (int i = 0; i < n; ++i) {
+            for (int k = 0; k < stacks[i].K; ++k) {
+                in_off.push_back(stage_bytes);
+                stage_bytes += up256(img_bytes(stacks[i].images[k]));
+                in_off.push_back(stage_bytes);  // alpha plane slot
+                if (stacks[i].alphas && stacks[i].alphas[k].data) {
+                    stage_bytes += up256((size_t)stacks[i].images[k].width * stacks[i].images[k].height);
+                }
+            }
+            out_off.push_back(stage_bytes);
+            stage_bytes += up256(img_bytes(*stacks[i].out));
+            oa_off.push_back(stage_bytes);
+            if (stacks[i].out_alpha && stacks[i].out_alpha->data) {
+                stage_bytes += up256((size_t)stacks[i].out->width * stacks[i].out->height);
+            }
+        }
+    }
+    if (bc.key != key || !bc.plan) {
+        if (bc.exec) {
+            cudaGraphExecDestroy(bc.exec);
+            bc.exec = nullptr;
+        }
+        ENB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        ENB_CUDA(ctx, cudaStreamSynchronize(bc.gs));
+        batch_plan_destroy(bc.plan);
+        bc.plan = nullptr;
+        cudaFree(bc.stage);
+        bc.stage = nullptr;
+        bc.key.clear();
+        if (stage_bytes) {
+            ENB_CUDA(ctx, cudaMalloc(&bc.stage, stage_bytes));
+        }
+        std::vector<BatchStackHost> hs((size_t)n);
+        size_t j = 0;
+        for (int i = 0; i < n; ++i) {
+            const enb_stack& st = stacks[i];
+            BatchStackHost& h = hs[(size_t)i];
+            memset(&h, 0, sizeof h);
+            h.K = st.K;
+            h.w = st.images[0].width;
+            h.h = st.images[0].height;
+            h.C = C;
+            for (int k = 0; k < st.K; ++k) {
+                const enb_image& im = st.images[k];
+                const int stride = im.pix_stride > 0 ? im.pix_stride : im.channels;
+                h.istride[k] = stride;
+                const bool has_a = st.alphas && st.alphas[k].data;
+                ENB_CHECK(ctx, has_a || stride != 4, "fuse_stacks: RGBA images need alpha planes");
+                if (o.host_buffers) {
+                    h.img[k] = (const float*)((char*)bc.stage + in_off[j]);
+                    h.ipitch[k] = (int64_t)im.width * stride;
+                    h.alpha[k] = has_a ? (const uint8_t*)((char*)bc.stage + in_off[j + 1]) : nullptr;
+                    h.apitch[k] = im.width;
+                    j += 2;
+                } else {
+                    h.img[k] = (const float*)im.data;
+                    h.ipitch[k] = im.pitch / 4;
+                    h.alpha[k] = has_a ? (const uint8_t*)st.alphas[k].data : nullptr;
+                    h.apitch[k] = has_a ? st.alphas[k].pitch : 0;
+                }
+            }
+            const int ostride = st.out->pix_stride > 0 ? st.out->pix_stride : st.out->channels;
+            h.ostride = ostride;
+            const bool has_oa = st.out_alpha && st.out_alpha->data;
+            if (o.host_buffers) {
+                h.out = (float*)((char*)bc.stage + out_off[(size_t)i]);
+                h.opitch = (int64_t)st.out->width * ostride;
+                h.oalpha = has_oa ? (uint8_t*)((char*)bc.stage + oa_off[(size_t)i]) : nullptr;
+                h.oapitch = st.out->width;
+            } else {
+                h.out = (float*)st.out->data;
+                h.opitch = st.out->pitch / 4;
+                h.oalpha = has_oa ? (uint8_t*)st.out_alpha->data : nullptr;
+                h.oapitch = has_oa ? st.out_alpha->pitch : 0;
+            }
+        }
+        cudaError_t e = batch_plan_create(hs, wp, ctx->tables, o.levels, o.wrap != 0, o.hard_mask != 0, coarse,
+                                          ctx->stream, &bc.plan);
+        if (e != cudaSuccess) {
+            return fail(ctx, e == cudaErrorMemoryAllocation ? ENB_ERR_NOMEM : ENB_ERR_CUDA,
+                        std::string("fuse_stacks: ") + cudaGetErrorString(e));
+        }
+        bc.key = key;
+    }
+    if (o.host_buffers) {
+        size_t j = 0;
+        for (int i = 0; i < n; ++i) {
+            for (int k = 0; k < stacks[i].K; ++k) {
+                const enb_image& im = stacks[i].images[k];
+                const int stride = im.pix_stride > 0 ? im.pix_stride : im.channels;
+                const size_t row = (size_t)im.width * stride * 4;
+                ENB_CUDA(ctx, cudaMemcpy2DAsync((char*)bc.stage + in_off[j], row, im.data, im.pitch, row, im.height,
+                                                cudaMemcpyHostToDevice, ctx->stream));
+                if (stacks[i].alphas && stacks[i].alphas[k].data) {
+                    ENB_CUDA(ctx, cudaMemcpy2DAsync((char*)bc.stage + in_off[j + 1], im.width, stacks[i].alphas[k].data,
+                                                    stacks[i].alphas[k].pitch, im.width, im.height,
+                                                    cudaMemcpyHostToDevice, ctx->stream));
+                }
+                j += 2;
+            }
+        }
+    }
+    const int nsteps = batch_plan_steps(bc.plan);
+    if (o.graph && !ctx->prof) {
+        if (!bc.exec) {
+            cudaGraph_t g = nullptr;
+            ENB_CUDA(ctx, cudaStreamBeginCapture(bc.gs, cudaStreamCaptureModeThreadLocal));
+            cudaError_t e = cudaSuccess;
+            for (int i = 0; i < nsteps && e == cudaSuccess; ++i) {
+                e = batch_plan_launch(bc.plan, i, bc.gs);
+            }
+            const cudaError_t e2 = cudaStreamEndCapture(bc.gs, &g);
+            if (e != cudaSuccess || e2 != cudaSuccess) {
+                if (g) {
+                    cudaGraphDestroy(g);
+                }
+                return cuda_fail(ctx, e != cudaSuccess ? e : e2, "fuse_stacks: graph capture");
+            }
+            e = cudaGraphInstantiate(&bc.exec, g, 0);
+            cudaGraphDestroy(g);
+            ENB_CUDA(ctx, e);
+        }
+        ENB_CUDA(ctx, cudaEventRecord(bc.ev[0], ctx->stream));
+        ENB_CUDA(ctx, cudaStreamWaitEvent(bc.gs, bc.ev[0], 0));
+        ENB_CUDA(ctx, cudaGraphLaunch(bc.exec, bc.gs));
+        ENB_CUDA(ctx, cudaEventRecord(bc.ev[1], bc.gs));
+        ENB_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, bc.ev[1], 0));
+        ctx->launches += (uint64_t)nsteps;
+    } else {
+        for (int i = 0; i < nsteps; ++i) {
+            ENB_LAUNCH(ctx, batch_plan_launch(bc.plan, i, ctx->stream));
+        }
+    }
+    if (o.host_buffers) {
+        for (int i = 0; i < n; ++i) {
+            const enb_image& oi = *stacks[i].out;
+            const int stride = oi.pix_stride > 0 ? oi.pix_stride : oi.channels;
+            const size_t row = (size_t)oi.width * stride * 4;
+            ENB_CUDA(ctx, cudaMemcpy2DAsync(oi.data, oi.pitch, (char*)bc.stage + out_off[(size_t)i], row, row,
+                                            oi.height, cudaMemcpyDeviceToHost, ctx->stream));
+            if (stacks[i].out_alpha && stacks[i].out_alpha->data) {
+                ENB_CUDA(ctx, cudaMemcpy2DAsync(stacks[i].out_alpha->data, stacks[i].out_alpha->pitch,
+                                                (char*)bc.stage + oa_off[(size_t)i], oi.width, oi.width, oi.height,
+                                                cudaMemcpyDeviceToHost, ctx->stream));
+            }
+        }
+        ENB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
     return ENB_OK;
 }
 

@@ -1,0 +1,779 @@
+// enb_batch.cu -- batched fuse of many float exposure stacks of uneven sizes.
+//
+// Every stack is enfuseMain's float path (src/enfuse.h:1217-1617 on float
+// images, FP32 pyramids for the reference's double ones): weights and their
+// normalisation, per exposure a Laplacian image pyramid and an Int32 9.15
+// mask pyramid with the union alpha, the masked merge, the collapse and the
+// conversion back.  The whole batch runs as one short sequence of launches,
+// each covering every stack and exposure at one pyramid level:
+//
+//   weights   one CTA per 16x16 tile of a stack: the K weights of each pixel
+//             (enb_fweights.cuh), their sum, the soft (or hard) masks as
+//             level 0 of the mask pyramids, the union alpha;
+//   down l    one CTA per 64x16 destination tile of level l+1 of one
+//             exposure's image or mask pyramid (reduce with alpha); level 0
+//             of an image is read from the input with the log mapping applied
+//             on the fly, so level 0 is never stored;
+//   coarse    a persistent kernel: each CTA takes stacks from a device work
+//             queue and runs all levels below ~64x64 of that stack (reduce
+//             down, then merge and collapse up) inside the one CTA;
+//   up l      one CTA per 64x16 tile of level l of a stack: the collapsed
+//             result C[l] = sum_k (G_k[l] - E(G_k[l+1])) m_k[l] / D + E(C[l+1])
+//             (the Laplacian, the mask multiply, the accumulation and the
+//             collapse of the reference fused); at level 0 the output pixels
+//             are written instead (v >= 1 ? expm1(v - 1) : 1 - 1/v).
+//
+// Jobs are (stack, kind, tile) entries of host-built tables; a launch's
+// grid is its job count.  The host side (the C ABI in enb_api.cu) captures
+// the launch sequence into a CUDA graph per batch geometry.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "enb_device.cuh"
+#include "enb_fweights.cuh"
+#include "enb_internal.h"
+#include "enb_reduce.cuh"
+
+namespace enb {
+
+// Per-stack geometry and buffers (device table, one entry per stack).
+struct BatchStack {
+    int K, w, h, L, Lc;  // exposures, size, levels, first level of the coarse kernel
+    int istride[kBatchMaxK];
+    const float* img[kBatchMaxK];
+    int64_t ipitch[kBatchMaxK];  // floats
+    const uint8_t* alpha[kBatchMaxK];
+    int64_t apitch[kBatchMaxK];
+    float* out;
+    int64_t opitch;  // floats
+    int ostride;
+    uint8_t* oalpha;  // optional
+    int64_t oapitch;
+    // workspace: levels 0..L-1 at off0 (masks, union alpha), levels 1..L-1
+    // at off1 (image levels, image alphas, collapsed result); pitches in
+    // elements, planes of pitch * height
+    int32_t* m;   // K * s0
+    uint8_t* u;   // s0
+    float* g;     // K * 3 * s1 (C planes used)
+    uint8_t* a;   // K * s1
+    float* r;     // 3 * s1
+    int64_t s0, s1;
+    int64_t off0[kMaxLevels], off1[kMaxLevels];
+    int pitch[kMaxLevels], lw[kMaxLevels], lh[kMaxLevels];
+};
+
+namespace {
+
+__device__ __forceinline__ float* g_level(const BatchStack& s, int k, int l, int C)
+{
+    return s.g + (int64_t)k * C * s.s1 + (int64_t)C * s.off1[l];
+}
+__device__ __forceinline__ uint8_t* a_level(const BatchStack& s, int k, int l)
+{
+    return s.a + (int64_t)k * s.s1 + s.off1[l];
+}
+__device__ __forceinline__ int32_t* m_level(const BatchStack& s, int k, int l)
+{
+    return s.m + (int64_t)k * s.s0 + s.off0[l];
+}
+__device__ __forceinline__ float* r_level(const BatchStack& s, int l, int C)
+{
+    return s.r + (int64_t)C * s.off1[l];
+}
+
+// Level 0 of an exposure's image pyramid read straight from the input: the
+// log mapping (ConvertScalarToPyramidFunctor) applied on load.
+template <int C>
+struct LogPixelSource {
+    const float* p;
+    int64_t pitch;
+    int stride;
+    const uint8_t* a;  // nullptr: opaque
+    int64_t apitch;
+    template <typename AC>
+    __device__ __forceinline__ void load(int gy, int gx, AC (&v)[C], int& al) const
+    {
+        const float* px = p + (int64_t)gy * pitch + (int64_t)gx * stride;
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            v[c] = to_pyramid_value(__ldg(&px[c]));
+        }
+        al = a ? (__ldg(&a[(int64_t)gy * apitch + gx]) != 0) : 1;
+    }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// weights, normalisation, mask level 0, union alpha
+// ---------------------------------------------------------------------------
+
+constexpr int BWT = 16;
+
+template <int CW, int EW>
+__global__ void __launch_bounds__(256) k_batch_weights(const BatchStack* __restrict__ stacks,
+                                                       const int4* __restrict__ jobs, FloatWeightParams wp,
+                                                       WeightTables tab, int hard, int C)
+{
+    extern __shared__ __align__(16) unsigned char bsmem[];
+    const int4 job = jobs[blockIdx.x];
+    const BatchStack& s = stacks[job.x];
+    const int halo = fweight_halo(wp);
+    const FTile t = ftile_carve(bsmem, BWT + 2 * halo, wp.repeat_slots);
+    const int lx = threadIdx.x % BWT, ly = threadIdx.x / BWT;
+    const int x = job.y * BWT + lx, y = job.z * BWT + ly;
+    const bool inside = x < s.w && y < s.h;
+    const int ci = (ly + halo) * t.TW + (lx + halo);
+    const int K = s.K;
+    float wk[kBatchMaxK];
+    uint8_t ua = 0;
+    for (int k = 0; k < K; ++k) {
+        ftile_load(t, wp, s.img[k], s.ipitch[k], s.istride[k], s.w, s.h, C, s.alpha[k], s.apitch[k],
+                   job.y * BWT - halo, job.z * BWT - halo);
+        wk[k] = inside ? f_pixel_weight<CW, EW>(t, wp, tab, ci, x, y, s.w, s.h, C) : 0.0f;
+        ua |= t.a[ci];
+        __syncthreads();  // the next exposure's load overwrites the tile
+    }
+    if (!inside) {
+        return;
+    }
+    // normalisation (src/enfuse.h:1382-1385 sum in exposure order,
+    // :1399-1442 hard mask, :1526-1535 soft mask)
+    const int64_t o = (int64_t)y * s.pitch[0] + x;
+    if (hard) {
+        float mx = 0.0f;
+        int mi = 0;
+        for (int k = 0; k < K; ++k) {
+            if (wk[k] > mx) {
+                mx = wk[k];
+                mi = k;
+            }
+        }
+        const float fallback = __fdiv_rn(255.0f, (float)K);
+        for (int k = 0; k < K; ++k) {
+            const float m = mx == 0.0f ? fallback : (k == mi ? 255.0f : 0.0f);
+            m_level(s, k, 0)[o] = mask_to_fixed<int32_t>(m, 15);
+        }
+    } else {
+        float norm = 0.0f;
+        for (int k = 0; k < K; ++k) {
+            norm = __fadd_rn(wk[k], norm);
+        }
+        const float fallback = (float)(255 / K);
+        for (int k = 0; k < K; ++k) {
+            const float m = norm > 0.0f ? __fdiv_rn(__fmul_rn(255.0f, wk[k]), norm) : fallback;
+            m_level(s, k, 0)[o] = mask_to_fixed<int32_t>(m, 15);
+        }
+    }
+    const uint8_t uv = ua ? 255 : 0;
+    s.u[s.off0[0] + o] = uv;
+    if (s.oalpha) {
+        s.oalpha[(int64_t)y * s.oapitch + x] = uv;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// reduce of one image or mask tile (down sweep)
+// ---------------------------------------------------------------------------
+
+// Job kind k < K: exposure k's image; K <= kind < 2K: exposure kind-K's mask.
+// NC: the source levels are read through the read-only path (they were
+// written by an earlier launch); false inside the coarse kernel, which reads
+// levels it wrote itself.
+template <int C, bool NC>
+__device__ __forceinline__ void batch_reduce_tile(const BatchStack& s, int kind, int l, int X0, int Y0, int wrap,
+                                                  unsigned char* smem)
+{
+    const int sw = s.lw[l], sh = s.lh[l], dw = s.lw[l + 1], dh = s.lh[l + 1];
+    if (kind < s.K) {
+        const int k = kind;
+        float* dst = g_level(s, k, l + 1, C);
+        const int64_t dplane = (int64_t)s.pitch[l + 1] * dh;
+        float(*V)[RDH][RVP] = reinterpret_cast<float(*)[RDH][RVP]>(smem);
+        if (l == 0) {
+            using Src = LogPixelSource<C>;
+            const ReduceJob<Src, float> job{Src{s.img[k], s.ipitch[k], s.istride[k], s.alpha[k], s.apitch[k]}, dst,
+                                            s.pitch[l + 1], dplane, a_level(s, k, l + 1), s.pitch[l + 1]};
+            reduce_tile<Src, float, C, true, float>(job, X0, Y0, sw, sh, dw, dh, wrap, V);
+        } else {
+            using Src = PlanarSource<float, C, true, NC>;
+            const ReduceJob<Src, float> job{
+                Src{g_level(s, k, l, C), s.pitch[l], (int64_t)s.pitch[l] * sh, a_level(s, k, l), s.pitch[l]}, dst,
+                s.pitch[l + 1], dplane, a_level(s, k, l + 1), s.pitch[l + 1]};
+            reduce_tile<Src, float, C, true, float>(job, X0, Y0, sw, sh, dw, dh, wrap, V);
+        }
+    } else {
+        const int k = kind - s.K;
+        using Src = PlanarSource<int32_t, 1, true, NC>;
+        int32_t(*V)[RDH][RVP] = reinterpret_cast<int32_t(*)[RDH][RVP]>(smem);
+        const ReduceJob<Src, int32_t> job{
+            Src{m_level(s, k, l), s.pitch[l], (int64_t)s.pitch[l] * sh, s.u + s.off0[l], s.pitch[l]},
+            m_level(s, k, l + 1), s.pitch[l + 1], (int64_t)s.pitch[l + 1] * dh, s.u + s.off0[l + 1], s.pitch[l + 1]};
+        reduce_tile<Src, int32_t, 1, true, int32_t>(job, X0, Y0, sw, sh, dw, dh, wrap, V);
+    }
+}
+
+constexpr int kBatchReduceSmem = ReduceSmem<3, true>::WORDS * 4;
+
+template <int C>
+__global__ void __launch_bounds__(RTHREADS, 3) k_batch_reduce(const BatchStack* __restrict__ stacks,
+                                                              const int4* __restrict__ jobs, int l, int wrap)
+{
+    __shared__ __align__(16) unsigned char smem[kBatchReduceSmem];
+    const int4 job = jobs[blockIdx.x];
+    batch_reduce_tile<C, true>(stacks[job.x], job.y, l, job.z * RDW, job.w * RDH, wrap, smem);
+}
+
+// ---------------------------------------------------------------------------
+// merge and collapse of one level tile (up sweep)
+// ---------------------------------------------------------------------------
+
+// Expand (src/pyramid.h:875-1457, real division) of the quad (X, Y)..(X+1,
+// Y+1) of destination pixels at source position (i, j) = (X/2, Y/2), from a
+// window staged at source (I0 - 1, J0 - 1); e[q][c] for q = (0,0), (1,0),
+// (0,1), (1,1).
+template <int C>
+__device__ __forceinline__ void expand_quad_f(const float (*ss)[ESH][ESW], int qx, int qy, int i, int j, int sw,
+                                              int sh, int dw, int wrap, float (&e)[4][C])
+{
+    const int X = 2 * i, Y = 2 * j;
+    if (i >= 1 && i + 1 < sw && j >= 1 && j + 1 < sh) {
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            const float* a = &ss[c][qy][qx];
+            const float* b = &ss[c][qy + 1][qx];
+            const float* d = &ss[c][qy + 2][qx];
+            const float hea = a[0] + 6.0f * a[1] + a[2], heb = b[0] + 6.0f * b[1] + b[2],
+                        hec = d[0] + 6.0f * d[1] + d[2];
+            const float hoa = 4.0f * (a[1] + a[2]), hob = 4.0f * (b[1] + b[2]), hoc = 4.0f * (d[1] + d[2]);
+            e[0][c] = (hea + 6.0f * heb + hec) * 0.015625f;
+            e[1][c] = (hoa + 6.0f * hob + hoc) * 0.015625f;
+            e[2][c] = (heb + hec) * 0.0625f;
+            e[3][c] = (hob + hoc) * 0.0625f;
+        }
+        return;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int XX = X + (q & 1), YY = Y + (q >> 1);
+        int vw[3], vden, hw[3], hden;
+        expand_vweights(YY, sh, vw, vden);
+        expand_hweights(XX, sw, dw, wrap, hw, hden);
+        const float den = (float)(hden * vden);
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            float num = 0.0f;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const float* row = &ss[c][qy + a][qx];
+                num += (float)vw[a] * ((float)hw[0] * row[0] + (float)hw[1] * row[1] + (float)hw[2] * row[2]);
+            }
+            e[q][c] = __fdiv_rn(num, den);
+        }
+    }
+}
+
+// Stages the (ESH x ESW) source window at (I0 - 1, J0 - 1) of a planar level
+// (zero outside; x periodic when wrap).  All threads of the CTA call it.
+template <int C>
+__device__ __forceinline__ void stage_window(float (*ss)[ESH][ESW], const float* src, int64_t pitch, int64_t plane,
+                                             int sw, int sh, int I0, int J0, int wrap)
+{
+    for (int k = threadIdx.x; k < ESH * ESW; k += blockDim.x) {
+        const int r = k / ESW, c = k - r * ESW;
+        const int jj = J0 - 1 + r;
+        int ii = I0 - 1 + c;
+        if (wrap) {
+            ii = imod(ii, sw);
+        }
+        const bool in = jj >= 0 && jj < sh && ii >= 0 && ii < sw;
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) {
+            ss[ch][r][c] = in ? src[(int64_t)ch * plane + (int64_t)jj * pitch + ii] : 0.0f;
+        }
+    }
+}
+
+// One 64x16 tile of level l of a stack (256 working threads, 2x2 quads):
+// C[l] = sum_k (G_k[l] - E(G_k[l+1])) m_k[l] / D + E(C[l+1]), written to
+// the result level (l >= 1) or converted into the output pixels (l == 0).
+// At the stack's top level the expand terms are absent.  NC as for the reduce.
+template <int C, bool NC>
+__device__ __forceinline__ void batch_up_tile(const BatchStack& s, int l, int X0, int Y0, int wrap, float inv_d,
+                                              float (*ss)[ESH][ESW])
+{
+    const bool top = l == s.L - 1;
+    const int dw = s.lw[l], dh = s.lh[l];
+    const int sw = top ? 1 : s.lw[l + 1], sh = top ? 1 : s.lh[l + 1];
+    const int I0 = X0 >> 1, J0 = Y0 >> 1;
+    const int tid = threadIdx.x;
+    const int qx = tid % 32, qy = tid / 32;
+    const int i = I0 + qx, j = J0 + qy;
+    const int X = 2 * i, Y = 2 * j;
+    const bool active = tid < 256 && X < dw && Y < dh;
+    const int64_t dp = s.pitch[l];
+    float acc[4][C];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            acc[q][c] = 0.0f;
+        }
+    }
+    const int64_t gplane = (int64_t)dp * dh;
+    for (int k = 0; k < s.K; ++k) {
+        float e[4][C];
+        if (!top) {
+            stage_window<C>(ss, g_level(s, k, l + 1, C), s.pitch[l + 1], (int64_t)s.pitch[l + 1] * sh, sw, sh, I0, J0,
+                            wrap);
+            __syncthreads();
+            if (active) {
+                expand_quad_f<C>(ss, qx, qy, i, j, sw, sh, dw, wrap, e);
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+#pragma unroll
+                for (int c = 0; c < C; ++c) {
+                    e[q][c] = 0.0f;
+                }
+            }
+        }
+        if (active) {
+            const int32_t* mk = m_level(s, k, l);
+            const float* gk = l > 0 ? g_level(s, k, l, C) : nullptr;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int XX = X + (q & 1), YY = Y + (q >> 1);
+                if (XX < dw && YY < dh) {
+                    const float coeff = (float)ld_src<NC>(&mk[(int64_t)YY * dp + XX]) * inv_d;
+                    float g[C];
+                    if (l == 0) {
+                        const float* px = s.img[k] + (int64_t)YY * s.ipitch[k] + (int64_t)XX * s.istride[k];
+#pragma unroll
+                        for (int c = 0; c < C; ++c) {
+                            g[c] = to_pyramid_value(__ldg(&px[c]));
+                        }
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < C; ++c) {
+                            g[c] = gk[(int64_t)c * gplane + (int64_t)YY * dp + XX];
+                        }
+                    }
+#pragma unroll
+                    for (int c = 0; c < C; ++c) {
+                        acc[q][c] += (g[c] - e[q][c]) * coeff;
+                    }
+                }
+            }
+        }
+        if (!top) {
+            __syncthreads();  // the next exposure restages the window
+        }
+    }
+    if (!top) {
+        stage_window<C>(ss, r_level(s, l + 1, C), s.pitch[l + 1], (int64_t)s.pitch[l + 1] * sh, sw, sh, I0, J0, wrap);
+        __syncthreads();
+        if (active) {
+            float e[4][C];
+            expand_quad_f<C>(ss, qx, qy, i, j, sw, sh, dw, wrap, e);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+#pragma unroll
+                for (int c = 0; c < C; ++c) {
+                    acc[q][c] += e[q][c];
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (!active) {
+        return;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int XX = X + (q & 1), YY = Y + (q >> 1);
+        if (XX >= dw || YY >= dh) {
+            continue;
+        }
+        if (l > 0) {
+            float* r = r_level(s, l, C);
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                r[(int64_t)c * gplane + (int64_t)YY * dp + XX] = acc[q][c];
+            }
+        } else {
+            float* o = s.out + (int64_t)YY * s.opitch + (int64_t)XX * s.ostride;
+            const bool on = s.u[(int64_t)YY * dp + XX] != 0;
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                o[c] = on ? from_pyramid_value(acc[q][c]) : 0.0f;
+            }
+            if (s.ostride == 4) {
+                o[3] = on ? 1.0f : 0.0f;  // AlphaTraits<float>::max()
+            }
+        }
+    }
+}
+
+template <int C>
+__global__ void __launch_bounds__(256) k_batch_up(const BatchStack* __restrict__ stacks, const int4* __restrict__ jobs,
+                                                  int l, int wrap, float inv_d)
+{
+    __shared__ float ss[C][ESH][ESW];
+    const int4 job = jobs[blockIdx.x];
+    batch_up_tile<C, true>(stacks[job.x], l, job.y * ETW, job.z * ETH, wrap, inv_d, ss);
+}
+
+// ---------------------------------------------------------------------------
+// coarse levels: one CTA runs a whole stack's coarse end
+// ---------------------------------------------------------------------------
+
+template <int C>
+__global__ void __launch_bounds__(RTHREADS) k_batch_coarse(const BatchStack* __restrict__ stacks,
+                                                           const int* __restrict__ coarse_list, int ncoarse,
+                                                           int* __restrict__ queue, int wrap, float inv_d)
+{
+    __shared__ __align__(16) unsigned char smem[kBatchReduceSmem];
+    __shared__ int item;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            item = atomicAdd(queue, 1);
+        }
+        __syncthreads();
+        const int it = item;
+        __syncthreads();
+        if (it >= ncoarse) {
+            return;
+        }
+        const BatchStack& s = stacks[coarse_list[it]];
+        // down: levels Lc -> L-1 of every image and mask pyramid
+        for (int l = s.Lc; l + 1 < s.L; ++l) {
+            const int tx = (s.lw[l + 1] + RDW - 1) / RDW, ty = (s.lh[l + 1] + RDH - 1) / RDH;
+            for (int kind = 0; kind < 2 * s.K; ++kind) {
+                for (int t = 0; t < tx * ty; ++t) {
+                    batch_reduce_tile<C, false>(s, kind, l, (t % tx) * RDW, (t / tx) * RDH, wrap, smem);
+                    __syncthreads();
+                }
+            }
+        }
+        // up: levels L-1 -> Lc (the fine launches continue from C[Lc])
+        float(*ss)[ESH][ESW] = reinterpret_cast<float(*)[ESH][ESW]>(smem);
+        for (int l = s.L - 1; l >= s.Lc; --l) {
+            const int tx = (s.lw[l] + ETW - 1) / ETW, ty = (s.lh[l] + ETH - 1) / ETH;
+            for (int t = 0; t < tx * ty; ++t) {
+                batch_up_tile<C, false>(s, l, (t % tx) * ETW, (t / tx) * ETH, wrap, inv_d, ss);
+                __syncthreads();
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host: plan of a batch and its launches
+// ---------------------------------------------------------------------------
+
+struct BatchPlan {
+    int C = 3;
+    int nstacks = 0;
+    int wrap = 0, hard = 0;
+    FloatWeightParams wp{};
+    WeightTables tab{};
+    size_t wsmem = 0;
+    void* work = nullptr;         // workspace of all stacks
+    BatchStack* dstacks = nullptr;
+    int4* djobs = nullptr;
+    int* dcoarse = nullptr;       // stacks with a coarse end
+    int* dqueue = nullptr;
+    int ncoarse = 0;
+    struct Step {
+        int kind;  // 0 weights, 1 down, 2 coarse, 3 up
+        int level;
+        int64_t job0, njobs;
+        double bytes;
+    };
+    std::vector<Step> steps;
+    int64_t coarse_pixels = 4096;
+    double pixels = 0.0;  // sum of K * w * h
+};
+
+namespace {
+
+void level_geometry(BatchStack& s, int64_t coarse_pixels)
+{
+    int lw = s.w, lh = s.h;
+    int64_t o0 = 0, o1 = 0;
+    s.Lc = s.L;
+    for (int l = 0; l < s.L; ++l) {
+        s.lw[l] = lw;
+        s.lh[l] = lh;
+        s.pitch[l] = (int)((lw + 31) / 32 * 32);
+        s.off0[l] = o0;
+        s.off1[l] = l >= 1 ? o1 : 0;
+        o0 += (int64_t)s.pitch[l] * lh;
+        if (l >= 1) {
+            o1 += (int64_t)s.pitch[l] * lh;
+            if (s.Lc == s.L && (int64_t)lw * lh <= coarse_pixels) {
+                s.Lc = l;
+            }
+        }
+        lw = (lw + 1) >> 1;
+        lh = (lh + 1) >> 1;
+    }
+    s.s0 = o0;
+    s.s1 = o1 > 0 ? o1 : 1;
+}
+
+}  // namespace
+
+void batch_plan_destroy(BatchPlan* p)
+{
+    if (!p) {
+        return;
+    }
+    cudaFree(p->work);
+    delete p;
+}
+
+cudaError_t batch_plan_create(const std::vector<BatchStackHost>& hs, const FloatWeightParams& wp,
+                              const WeightTables& tab, int levels, int wrap, int hard, int64_t coarse_pixels,
+                              cudaStream_t st, BatchPlan** out)
+{
+    BatchPlan* p = new BatchPlan();
+    p->nstacks = (int)hs.size();
+    p->wrap = wrap;
+    p->hard = hard;
+    p->wp = wp;
+    p->tab = tab;
+    p->C = hs.empty() ? 3 : hs[0].C;
+    p->coarse_pixels = coarse_pixels;
+    std::vector<BatchStack> stacks(hs.size());
+    size_t bytes = 0;
+    auto align = [](size_t v) { return (v + 255) & ~(size_t)255; };
+    std::vector<size_t> base(hs.size());
+    for (size_t i = 0; i < hs.size(); ++i) {
+        BatchStack& s = stacks[i];
+        std::memset(&s, 0, sizeof s);
+        const BatchStackHost& h = hs[i];
+        s.K = h.K;
+        s.w = h.w;
+        s.h = h.h;
+        s.L = enb_num_levels(h.w, h.h, 1, levels);
+        for (int k = 0; k < h.K; ++k) {
+            s.img[k] = h.img[k];
+            s.ipitch[k] = h.ipitch[k];
+            s.istride[k] = h.istride[k];
+            s.alpha[k] = h.alpha[k];
+            s.apitch[k] = h.apitch[k];
+        }
+        s.out = h.out;
+        s.opitch = h.opitch;
+        s.ostride = h.ostride;
+        s.oalpha = h.oalpha;
+        s.oapitch = h.oapitch;
+        level_geometry(s, coarse_pixels);
+        base[i] = bytes;
+        bytes += align((size_t)s.K * s.s0 * 4) + align((size_t)s.s0) + align((size_t)s.K * p->C * s.s1 * 4) +
+                 align((size_t)s.K * s.s1) + align((size_t)p->C * s.s1 * 4);
+        p->pixels += (double)h.K * h.w * h.h;
+    }
+    // job tables
+    std::vector<int4> jobs;
+    auto add_step = [&](int kind, int level, double b) {
+        p->steps.push_back(BatchPlan::Step{kind, level, 0, 0, b});
+        p->steps.back().job0 = (int64_t)jobs.size();
+    };
+    const int halo = fweight_halo(wp);
+    const int TW = BWT + 2 * halo;
+    p->wp.repeat_slots = fweight_slots(wp, TW);
+    p->wsmem = ftile_bytes(TW, p->wp.repeat_slots);
+    double b = 0.0;
+    add_step(0, 0, 0.0);
+    for (int i = 0; i < p->nstacks; ++i) {
+        const BatchStack& s = stacks[i];
+        for (int ty = 0; ty < (s.h + BWT - 1) / BWT; ++ty) {
+            for (int tx = 0; tx < (s.w + BWT - 1) / BWT; ++tx) {
+                jobs.push_back(make_int4(i, tx, ty, 0));
+            }
+        }
+        b += (double)s.K * s.w * s.h * (4.0 * hs[i].istride[0] + 4.0) + (double)s.w * s.h;
+    }
+    p->steps.back().njobs = (int64_t)jobs.size() - p->steps.back().job0;
+    p->steps.back().bytes = b;
+    int maxL = 0;
+    for (const BatchStack& s : stacks) {
+        maxL = std::max(maxL, s.L);
+    }
+    for (int l = 0; l + 1 < maxL; ++l) {
+        add_step(1, l, 0.0);
+        b = 0.0;
+        for (int i = 0; i < p->nstacks; ++i) {
+            const BatchStack& s = stacks[i];
+            if (l + 1 > std::min(s.Lc, s.L - 1)) {
+                continue;
+            }
+            const int tx = (s.lw[l + 1] + RDW - 1) / RDW, ty = (s.lh[l + 1] + RDH - 1) / RDH;
+            for (int kind = 0; kind < 2 * s.K; ++kind) {
+                for (int y = 0; y < ty; ++y) {
+                    for (int x = 0; x < tx; ++x) {
+                        jobs.push_back(make_int4(i, kind, x, y));
+                    }
+                }
+            }
+            const double src = (double)s.lw[l] * s.lh[l], dst = (double)s.lw[l + 1] * s.lh[l + 1];
+            b += s.K * (src * (l == 0 ? 4.0 * hs[i].istride[0] : 4.0 * p->C + 1.0) + dst * (4.0 * p->C + 1.0)) +
+                 s.K * (src * 4.0 + dst * 4.0) + src + dst;
+        }
+        p->steps.back().njobs = (int64_t)jobs.size() - p->steps.back().job0;
+        p->steps.back().bytes = b;
+        if (p->steps.back().njobs == 0) {
+            p->steps.pop_back();
+        }
+    }
+    std::vector<int> coarse;
+    for (int i = 0; i < p->nstacks; ++i) {
+        if (stacks[i].Lc < stacks[i].L) {
+            coarse.push_back(i);
+        }
+    }
+    p->ncoarse = (int)coarse.size();
+    if (p->ncoarse) {
+        add_step(2, 0, 0.0);
+    }
+    for (int l = maxL - 1; l >= 0; --l) {
+        add_step(3, l, 0.0);
+        b = 0.0;
+        for (int i = 0; i < p->nstacks; ++i) {
+            const BatchStack& s = stacks[i];
+            if (l > std::min(s.Lc, s.L) - 1) {
+                continue;
+            }
+            const int tx = (s.lw[l] + ETW - 1) / ETW, ty = (s.lh[l] + ETH - 1) / ETH;
+            for (int y = 0; y < ty; ++y) {
+                for (int x = 0; x < tx; ++x) {
+                    jobs.push_back(make_int4(i, x, y, 0));
+                }
+            }
+            const double px = (double)s.lw[l] * s.lh[l], up = l + 1 < s.L ? (double)s.lw[l + 1] * s.lh[l + 1] : 0.0;
+            b += s.K * (px * ((l == 0 ? 4.0 * hs[i].istride[0] : 4.0 * p->C) + 4.0) + up * 4.0 * p->C) +
+                 up * 4.0 * p->C + px * (l == 0 ? 4.0 * hs[i].ostride + 1.0 : 4.0 * p->C);
+        }
+        p->steps.back().njobs = (int64_t)jobs.size() - p->steps.back().job0;
+        p->steps.back().bytes = b;
+        if (p->steps.back().njobs == 0) {
+            p->steps.pop_back();
+        }
+    }
+    // device memory: workspace, stack table, jobs, coarse list, queue counter
+    const size_t o_st = align(bytes), o_jobs = o_st + align(sizeof(BatchStack) * stacks.size()),
+                 o_coarse = o_jobs + align(sizeof(int4) * std::max<size_t>(jobs.size(), 1)),
+                 o_queue = o_coarse + align(sizeof(int) * std::max<size_t>(coarse.size(), 1)), total = o_queue + 256;
+    cudaError_t e = cudaMalloc(&p->work, total);
+    if (e != cudaSuccess) {
+        delete p;
+        return e;
+    }
+    char* w = (char*)p->work;
+    for (size_t i = 0; i < stacks.size(); ++i) {
+        BatchStack& s = stacks[i];
+        char* q = w + base[i];
+        s.m = (int32_t*)q;
+        q += align((size_t)s.K * s.s0 * 4);
+        s.u = (uint8_t*)q;
+        q += align((size_t)s.s0);
+        s.g = (float*)q;
+        q += align((size_t)s.K * p->C * s.s1 * 4);
+        s.a = (uint8_t*)q;
+        q += align((size_t)s.K * s.s1);
+        s.r = (float*)q;
+    }
+    p->dstacks = (BatchStack*)(w + o_st);
+    p->djobs = (int4*)(w + o_jobs);
+    p->dcoarse = (int*)(w + o_coarse);
+    p->dqueue = (int*)(w + o_queue);
+    e = cudaMemcpyAsync(p->dstacks, stacks.data(), sizeof(BatchStack) * stacks.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !jobs.empty()) {
+        e = cudaMemcpyAsync(p->djobs, jobs.data(), sizeof(int4) * jobs.size(), cudaMemcpyHostToDevice, st);
+    }
+    if (e == cudaSuccess && !coarse.empty()) {
+        e = cudaMemcpyAsync(p->dcoarse, coarse.data(), sizeof(int) * coarse.size(), cudaMemcpyHostToDevice, st);
+    }
+    if (e == cudaSuccess) {
+        e = cudaStreamSynchronize(st);  // the host tables go out of scope
+    }
+    if (e != cudaSuccess) {
+        batch_plan_destroy(p);
+        return e;
+    }
+    *out = p;
+    return cudaSuccess;
+}
+
+int batch_plan_steps(const BatchPlan* p) { return (int)p->steps.size(); }
+double batch_plan_pixels(const BatchPlan* p) { return p->pixels; }
+
+template <int C>
+static cudaError_t launch_step(const BatchPlan* p, const BatchPlan::Step& s, cudaStream_t st)
+{
+    const int4* jobs = p->djobs + s.job0;
+    const float inv_d = (float)(1.0 / (double)(255 << 15));
+    switch (s.kind) {
+    case 0: {
+        note_launch("batch_weights", s.bytes);
+        const int cw = p->wp.use_contrast ? p->wp.contrast_window : 5;
+        const int ew = p->wp.use_entropy ? p->wp.entropy_window : 5;
+        void (*k)(const BatchStack*, const int4*, FloatWeightParams, WeightTables, int, int) = k_batch_weights<0, 0>;
+        if (cw == 5 && ew == 5) {
+            k = k_batch_weights<5, 5>;
+        } else if (cw == 5 && ew == 3) {
+            k = k_batch_weights<5, 3>;
+        } else if (cw == 3 && ew == 3) {
+            k = k_batch_weights<3, 3>;
+        } else if (ew == 5) {
+            k = k_batch_weights<0, 5>;
+        } else if (ew == 3) {
+            k = k_batch_weights<0, 3>;
+        }
+        if (p->wsmem > 48 * 1024) {
+            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->wsmem);
+        }
+        k<<<(unsigned)s.njobs, BWT * BWT, p->wsmem, st>>>(p->dstacks, jobs, p->wp, p->tab, p->hard, C);
+        break;
+    }
+    case 1:
+        note_launch("batch_reduce", s.bytes);
+        k_batch_reduce<C><<<(unsigned)s.njobs, RTHREADS, 0, st>>>(p->dstacks, jobs, s.level, p->wrap);
+        break;
+    case 2: {
+        note_launch("batch_coarse", 0.0);
+        cudaError_t e = cudaMemsetAsync(p->dqueue, 0, sizeof(int), st);
+        if (e != cudaSuccess) {
+            return e;
+        }
+        int sms = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const int grid = std::max(1, std::min(p->ncoarse, 2 * sms));
+        k_batch_coarse<C><<<grid, RTHREADS, 0, st>>>(p->dstacks, p->dcoarse, p->ncoarse, p->dqueue, p->wrap, inv_d);
+        break;
+    }
+    default:
+        note_launch(s.level == 0 ? "batch_up0" : "batch_up", s.bytes);
+        k_batch_up<C><<<(unsigned)s.njobs, 256, 0, st>>>(p->dstacks, jobs, s.level, p->wrap, inv_d);
+        break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t batch_plan_launch(const BatchPlan* p, int i, cudaStream_t st)
+{
+    const BatchPlan::Step& s = p->steps[(size_t)i];
+    return p->C == 1 ? launch_step<1>(p, s, st) : launch_step<3>(p, s, st);
+}
+
+}  // namespace enb

@@ -65,6 +65,20 @@ __device__ __forceinline__ uint32_t frp_unsigned(double v, uint32_t maxv)
     return v > (double)maxv ? maxv : (uint32_t)__double2uint_rz(__dadd_rn(v, 0.5));
 }
 
+// Exact fromRealPromote(m * 2^frac) for 0 <= m * 2^frac < 2^23 in float
+// arithmetic: the product is exact, floor and the fractional part are exact.
+template <typename TD>
+__device__ __forceinline__ TD mask_to_fixed(float m, int frac)
+{
+    const float v = m * (float)(1u << frac);
+    if (v >= 0.0f && v < 8388608.0f) {
+        const float fl = floorf(v);
+        const int r = (int)fl + ((v - fl) >= 0.5f ? 1 : 0);
+        return (TD)r;
+    }
+    return frp_store<TD>(__dmul_rn((double)m, (double)(1u << frac)));
+}
+
 __host__ __device__ __forceinline__ int imod(int a, int m)
 {
     int r = a % m;

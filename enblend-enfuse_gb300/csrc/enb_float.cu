@@ -13,6 +13,7 @@
 #include <stdint.h>
 
 #include "enb_device.cuh"
+#include "enb_fweights.cuh"
 #include "enb_internal.h"
 
 namespace enb {
@@ -27,16 +28,6 @@ inline double npix(int w, int h) { return (double)w * (double)h; }
 // ---------------------------------------------------------------------------
 // Conversions (src/fixmath.h:165-187, 320-329)
 // ---------------------------------------------------------------------------
-
-__device__ __forceinline__ float to_pyramid_value(float v)
-{
-    return v >= 0.0f ? __fadd_rn(1.0f, log1pf(v)) : __fdiv_rn(1.0f, __fsub_rn(1.0f, v));
-}
-
-__device__ __forceinline__ float from_pyramid_value(float v)
-{
-    return v >= 1.0f ? expm1f(__fsub_rn(v, 1.0f)) : __fsub_rn(1.0f, __fdiv_rn(1.0f, v));
-}
 
 template <int C>
 __global__ void __launch_bounds__(256) k_f_to_pyramid(const float* __restrict__ src, int64_t spitch, int stride,
@@ -248,268 +239,28 @@ __global__ void __launch_bounds__(256) k_f_copy_level0(const float* __restrict__
 }
 
 // ---------------------------------------------------------------------------
-// enfuse weights of float images (src/enfuse.h:962-1212)
+// enfuse weights of float images (src/enfuse.h:962-1212), enb_fweights.cuh
 // ---------------------------------------------------------------------------
 
 constexpr int FWT = 16;  // 16x16 weight pixels per CTA
 
-// fl(fl_double(s / 3)) of a float s, the reference's (float)(s / 3.0), in
-// float arithmetic: q1 = fl(s / 3) is the correctly rounded quotient, which
-// is the result unless s / 3 lies within 2^-29 ulp of a float rounding
-// midpoint (where rounding through double could differ).  The remainder
-// s - 3 q1 is exact (fmaf) and locates s / 3 relative to q1; near a midpoint
-// the double expression decides.
-__device__ __forceinline__ float third_of(float s)
-{
-    if (s == 0.0f) {
-        return s;
-    }
-    const float q1 = __fdiv_rn(s, 3.0f);
-    const float rem = __fmaf_rn(-3.0f, q1, s);  // s - 3 q1, exact
-    // s / 3 - q1 = rem / 3; a midpoint sits at +-ulp/2
-    const float ulp = fabsf(__int_as_float(__float_as_int(q1) + 1) - q1);
-    const float d = fabsf(rem) - 1.5f * ulp;  // 3 (|s/3 - q1| - ulp/2), exact or nearly
-    if (fabsf(d) > 1.0e-6f * ulp && (__float_as_int(q1) & 0x7fffff) != 0) {
-        return q1;
-    }
-    return __double2float_rn((double)s / 3.0);
-}
-
-// MultiGrayscaleAccessor on float RGB (src/mga.h:184-222).  The reference's
-// RealPromote of float is float: the average adds the samples in float and
-// divides by 3.0 in double, the lightness adds min and max in float;
-// luminance (0.3/0.59/0.11) and the channel mixer are double expressions.
-__device__ __forceinline__ float gray_of_f(const FloatWeightParams& p, float r, float g, float b)
-{
-    switch (p.gray_projector) {
-    case ENB_GRAY_VALUE: return fmaxf(r, fmaxf(g, b));
-    case ENB_GRAY_ANTI_VALUE: return fminf(r, fminf(g, b));
-    case ENB_GRAY_LIGHTNESS: return 0.5f * __fadd_rn(fminf(r, fminf(g, b)), fmaxf(r, fmaxf(g, b)));
-    case ENB_GRAY_LUMINANCE:
-        return __double2float_rn(__dadd_rn(__dadd_rn(__dmul_rn(0.3, (double)r), __dmul_rn(0.59, (double)g)),
-                                           __dmul_rn(0.11, (double)b)));
-    case ENB_GRAY_MIXER:
-        return __double2float_rn(__dadd_rn(__dadd_rn(__dmul_rn(p.mixer[0], (double)r), __dmul_rn(p.mixer[1], (double)g)),
-                                           __dmul_rn(p.mixer[2], (double)b)));
-    default: return third_of(__fadd_rn(__fadd_rn(r, g), b));
-    }
-}
-
-// The built-in exposure weight functions (src/exposure_weight.h:44-128).
-// The reference forms y = gray / max in float (both operands are float) and
-// z = (y - optimum) / width in double.  Here z is carried as a float-float
-// pair zh + zl (error ~1e-14 relative), so that the functions that vanish at
-// the edge of their support (half-sine, full-sine, bisquare) keep their
-// relative accuracy there; each function is then evaluated in float with a
-// first-order correction for zl.
-__device__ __forceinline__ float exposure_f(const FloatWeightParams& p, float gray)
-{
-    const float y = __fdiv_rn(gray, p.range);
-    // d = y - (opt_hi + opt_lo) as dh + dl: TwoSum(y, -opt_hi), then opt_lo
-    const float s = __fsub_rn(y, p.opt_hi);
-    const float bv = __fsub_rn(s, y);
-    const float e = __fadd_rn(__fsub_rn(y, __fsub_rn(s, bv)), __fsub_rn(-p.opt_hi, bv));
-    const float dl0 = __fsub_rn(e, p.opt_lo);
-    const float dh = __fadd_rn(s, dl0);
-    const float dl = __fsub_rn(dl0, __fsub_rn(dh, s));
-    // z = d * (inv_hi + inv_lo)
-    const float zh = __fmul_rn(dh, p.inv_hi);
-    const float zl = __fadd_rn(__fmaf_rn(dh, p.inv_hi, -zh), __fmaf_rn(dh, p.inv_lo, __fmul_rn(dl, p.inv_hi)));
-    const float az = fabsf(zh);
-    switch (p.exp_function) {
-    case ENB_EXP_LORENTZIAN: return __fdiv_rn(1.0f, __fmaf_rn(0.5f * zh, zh, 1.0f));
-    case ENB_EXP_HALF_SINE: {
-        if (az > 1.57079632679489661923f) {
-            return 0.0f;
-        }
-        float sn, cs;
-        sincosf(zh, &sn, &cs);
-        return fmaxf(__fmaf_rn(-sn, zl, cs), 0.0f);
-    }
-    case ENB_EXP_FULL_SINE: {
-        if (az > 3.14159265358979323846f) {
-            return 0.0f;
-        }
-        // 0.5 + cos(z) / 2 = cos(z / 2)^2, without the cancellation near z = pi
-        float sn, cs;
-        sincosf(0.5f * zh, &sn, &cs);
-        const float c = __fmaf_rn(-sn, 0.5f * zl, cs);
-        return c * c;
-    }
-    case ENB_EXP_BISQUARE: {
-        if (az > 1.0f) {
-            return 0.0f;
-        }
-        // (1 - z^2)(1 + z^2) with 1 - z^2 = (1 - zh)(1 + zh) - 2 zh zl
-        const float one_minus = __fmaf_rn(-2.0f * zh, zl, __fmul_rn(1.0f - zh, 1.0f + zh));
-        const float one_plus = __fmaf_rn(zh, zh, __fmul_rn(2.0f * zh, zl)) + 1.0f;
-        return fmaxf(one_minus, 0.0f) * one_plus;
-    }
-    default: {
-        // exp(-z^2 / 2) with z^2 / 2 = qh + ql
-        const float qh = __fmul_rn(0.5f * zh, zh);
-        const float ql = __fmaf_rn(0.5f * zh, zh, -qh) + zh * zl;
-        return expf(-qh) * (1.0f - ql);
-    }
-    }
-}
-
-// Histogram::entropyOfChannel of n float keys sorted by bit pattern (equal
-// floats are adjacent; -0 was folded into +0), src/enfuse.h:346-375.  The
-// sum of p log p is exact in 2^-56 fixed point (host table; the tables of
-// float images are built with max 1, so scale_logb[b] = 1 / log b); H <= 1.
-__device__ float entropy_f(const uint32_t* v, int n, const WeightTables& tab, int nmax)
-{
-    if (n == 0) {
-        return 0.0f;
-    }
-    int bins = 0;
-    long long acc = 0;
-    const long long* fx = tab.plogp_fx + (int64_t)n * (nmax + 1);
-    int i = 0;
-    while (i < n) {
-        int j = i + 1;
-        while (j < n && v[j] == v[i]) {
-            ++j;
-        }
-        acc += fx[j - i];
-        ++bins;
-        i = j;
-    }
-    if (bins <= 1) {
-        return 0.0f;
-    }
-    const float H = __fmul_rn(-(float)acc * 1.3877787807814457e-17f, tab.scale_logb[bins]);  // 2^-56
-    return fminf(H, 1.0f);
-}
-
+template <int CW, int EW>
 __global__ void __launch_bounds__(256) k_f_enfuse_mask(FloatPixelView img, const uint8_t* __restrict__ alpha,
                                                        int64_t apitch, FloatWeightParams wp, WeightTables tab,
                                                        float* __restrict__ out, int64_t opitch)
 {
     extern __shared__ __align__(16) unsigned char fsmem[];
-    const int halo = max(wp.use_contrast ? wp.contrast_window / 2 : 0, wp.use_entropy ? wp.entropy_window / 2 : 0);
-    const int TW = FWT + 2 * halo;
-    float* s_gray = reinterpret_cast<float*>(fsmem);
-    float* s_raw = s_gray + TW * TW;  // [3][TW*TW]
-    uint8_t* s_a = reinterpret_cast<uint8_t*>(s_raw + 3 * TW * TW);
-
-    const int x0 = blockIdx.x * FWT - halo, y0 = blockIdx.y * FWT - halo;
-    const int w = img.w, h = img.h, C = img.C;
-    for (int k = threadIdx.x; k < TW * TW; k += blockDim.x) {
-        const int r = k / TW, c = k - r * TW;
-        const int gx = x0 + c, gy = y0 + r;
-        float rgb[3] = {0.0f, 0.0f, 0.0f};
-        uint8_t a = 0;
-        if (gx >= 0 && gx < w && gy >= 0 && gy < h) {
-            const float* px = img.p + (int64_t)gy * img.pitch + (int64_t)gx * img.stride;
-            for (int ch = 0; ch < C; ++ch) {
-                rgb[ch] = __ldg(&px[ch]);
-            }
-            a = alpha[(int64_t)gy * apitch + gx] != 0;
-        }
-        s_gray[k] = C == 1 ? rgb[0] : gray_of_f(wp, rgb[0], rgb[1], rgb[2]);
-        s_a[k] = a;
-        for (int ch = 0; ch < 3; ++ch) {
-            s_raw[ch * TW * TW + k] = rgb[ch];
-        }
-    }
-    __syncthreads();
-
+    const int halo = fweight_halo(wp);
+    const FTile t = ftile_carve(fsmem, FWT + 2 * halo, wp.repeat_slots);
+    ftile_load(t, wp, img.p, img.pitch, img.stride, img.w, img.h, img.C, alpha, apitch, blockIdx.x * FWT - halo,
+               blockIdx.y * FWT - halo);
     const int lx = threadIdx.x % FWT, ly = threadIdx.x / FWT;
     const int x = blockIdx.x * FWT + lx, y = blockIdx.y * FWT + ly;
-    if (x >= w || y >= h) {
+    if (x >= img.w || y >= img.h) {
         return;
     }
-    const int ci = (ly + halo) * TW + (lx + halo);
-    float result = 0.0f;
-    if (s_a[ci]) {
-        if (wp.use_exposure) {
-            result = wp.w_exposure * exposure_f(wp, s_gray[ci]);
-        }
-        if (wp.use_contrast) {
-            // sample standard deviation of the opaque window pixels
-            // (localStdDevIf, src/enfuse.h:75-219), two passes around the
-            // float mean; the border strip is not written (0)
-            const int b = wp.contrast_window / 2;
-            float sd = 0.0f;
-            if (x >= b && x < w - b && y >= b && y < h - b) {
-                float sum = 0.0f;
-                int n = 0;
-                for (int dy = -b; dy <= b; ++dy) {
-                    const int row = (ly + halo + dy) * TW + lx + halo;
-                    for (int dx = -b; dx <= b; ++dx) {
-                        if (s_a[row + dx]) {
-                            sum += s_gray[row + dx];
-                            ++n;
-                        }
-                    }
-                }
-                if (n > 1) {
-                    const float mean = __fdiv_rn(sum, (float)n);
-                    float s1 = 0.0f, s2 = 0.0f;
-                    for (int dy = -b; dy <= b; ++dy) {
-                        const int row = (ly + halo + dy) * TW + lx + halo;
-                        for (int dx = -b; dx <= b; ++dx) {
-                            if (s_a[row + dx]) {
-                                const float d = s_gray[row + dx] - mean;
-                                s1 += d;
-                                s2 = fmaf(d, d, s2);
-                            }
-                        }
-                    }
-                    const float var = __fdiv_rn(s2 - __fdiv_rn(s1 * s1, (float)n), (float)(n - 1));
-                    sd = sqrtf(fmaxf(var, 0.0f));
-                }
-            }
-            result = wp.w_contrast * sd + result;
-        }
-        if (wp.use_saturation && C == 3) {
-            // SaturationFunctor with max_value 1.0 (src/enfuse.h:733-780);
-            // 2 - (max + min) is formed as (1 - max) + (1 - min), whose terms
-            // are exact near white
-            const float r = s_raw[ci], g = s_raw[TW * TW + ci], bb = s_raw[2 * TW * TW + ci];
-            const float mx = fmaxf(r, fmaxf(g, bb)), mn = fminf(r, fminf(g, bb));
-            float sw = 0.0f;
-            if (mx != mn) {
-                const float sum = mx + mn, diff = mx - mn;
-                const float den = sum <= 1.0f ? sum : (1.0f - mx) + (1.0f - mn);
-                sw = wp.w_saturation * __fdiv_rn(diff, den);
-            }
-            result = sw + result;
-        }
-        if (wp.use_entropy) {
-            const int b = wp.entropy_window / 2;
-            float emin = 0.0f;
-            if (x >= b && x < w - b && y >= b && y < h - b) {
-                uint32_t vals[kMaxEntropyWindow * kMaxEntropyWindow];
-                const int nmax = wp.entropy_window * wp.entropy_window;
-                emin = 3.402823466e38f;
-                for (int ch = 0; ch < C; ++ch) {
-                    int n = 0;
-                    for (int dy = -b; dy <= b; ++dy) {
-                        const int row = (ly + halo + dy) * TW + lx + halo;
-                        for (int dx = -b; dx <= b; ++dx) {
-                            if (s_a[row + dx]) {
-                                const float f = s_raw[ch * TW * TW + row + dx];
-                                const uint32_t v = __float_as_uint(f == 0.0f ? 0.0f : f);
-                                int q = n++;
-                                while (q > 0 && vals[q - 1] > v) {
-                                    vals[q] = vals[q - 1];
-                                    --q;
-                                }
-                                vals[q] = v;
-                            }
-                        }
-                    }
-                    // fromRealPromote<float>(H * max): the entropy image pixel
-                    emin = fminf(emin, __fmul_rn(entropy_f(vals, n, tab, nmax), wp.range));
-                }
-            }
-            result = __fmul_rn(wp.w_entropy, emin) + result;
-        }
-    }
-    out[(int64_t)y * opitch + x] = result;
+    const int ci = (ly + halo) * t.TW + (lx + halo);
+    out[(int64_t)y * opitch + x] = f_pixel_weight<CW, EW>(t, wp, tab, ci, x, y, img.w, img.h, img.C);
 }
 
 // ---------------------------------------------------------------------------
@@ -604,15 +355,29 @@ cudaError_t launch_f_copy_level0(const PlanarView& s, float* dst, cudaStream_t s
 cudaError_t launch_f_enfuse_mask(const FloatPixelView& img, const BytePlane& alpha, const FloatWeightParams& wp,
                                  const WeightTables& tab, const FloatPlane& out, cudaStream_t st)
 {
-    const int halo = max(wp.use_contrast ? wp.contrast_window / 2 : 0, wp.use_entropy ? wp.entropy_window / 2 : 0);
-    const int TW = FWT + 2 * halo;
-    const size_t smem = (size_t)TW * TW * (4 * sizeof(float) + 1);
+    const int TW = FWT + 2 * fweight_halo(wp);
+    FloatWeightParams p = wp;
+    p.repeat_slots = fweight_slots(wp, TW);
+    const size_t smem = ftile_bytes(TW, p.repeat_slots);
     note_launch("f_enfuse_mask", npix(img.w, img.h) * (img.stride * 4.0 + 1.0 + 4.0));
-    if (smem > 48 * 1024) {
-        cudaFuncSetAttribute(k_f_enfuse_mask, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int cw = p.use_contrast ? p.contrast_window : 5, ew = p.use_entropy ? p.entropy_window : 5;
+    void (*k)(FloatPixelView, const uint8_t*, int64_t, FloatWeightParams, WeightTables, float*, int64_t) =
+        k_f_enfuse_mask<0, 0>;
+    if (cw == 5 && ew == 5) {
+        k = k_f_enfuse_mask<5, 5>;
+    } else if (cw == 5 && ew == 3) {
+        k = k_f_enfuse_mask<5, 3>;
+    } else if (cw == 3 && ew == 3) {
+        k = k_f_enfuse_mask<3, 3>;
+    } else if (ew == 5) {
+        k = k_f_enfuse_mask<0, 5>;
+    } else if (ew == 3) {
+        k = k_f_enfuse_mask<0, 3>;
     }
-    k_f_enfuse_mask<<<grid2d(img.w, img.h, FWT, FWT), FWT * FWT, smem, st>>>(img, alpha.p, alpha.pitch, wp, tab, out.p,
-                                                                             out.pitch);
+    if (smem > 48 * 1024) {
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    }
+    k<<<grid2d(img.w, img.h, FWT, FWT), FWT * FWT, smem, st>>>(img, alpha.p, alpha.pitch, p, tab, out.p, out.pitch);
     return cudaGetLastError();
 }
 

@@ -1,0 +1,380 @@
+// enb_fweights.cuh -- enfuse weights of float images (src/enfuse.h:962-1212
+// with float pixels): the per-pixel functions, a shared-memory tile of one
+// exposure and the weight of one pixel of it.  Used by the per-image weight
+// kernel (enb_float.cu) and by the batched stack fuse (enb_batch.cu).
+#pragma once
+
+#include <stdint.h>
+
+#include "enb_device.cuh"
+#include "enb_entropy.cuh"
+#include "enb_internal.h"
+
+namespace enb {
+
+// The logarithmic mapping of float samples into the pyramid and back
+// (src/fixmath.h:165-187, 320-329).
+__device__ __forceinline__ float to_pyramid_value(float v)
+{
+    return v >= 0.0f ? __fadd_rn(1.0f, log1pf(v)) : __fdiv_rn(1.0f, __fsub_rn(1.0f, v));
+}
+
+__device__ __forceinline__ float from_pyramid_value(float v)
+{
+    return v >= 1.0f ? expm1f(__fsub_rn(v, 1.0f)) : __fsub_rn(1.0f, __fdiv_rn(1.0f, v));
+}
+
+// fl(fl_double(s / 3)) of a float s, the reference's (float)(s / 3.0), in
+// float arithmetic: q1 = fl(s / 3) is the correctly rounded quotient, which
+// is the result unless s / 3 lies within 2^-29 ulp of a float rounding
+// midpoint (where rounding through double could differ).  The remainder
+// s - 3 q1 is exact (fmaf) and locates s / 3 relative to q1; near a midpoint
+// the double expression decides.
+__device__ __forceinline__ float third_of(float s)
+{
+    if (s == 0.0f) {
+        return s;
+    }
+    const float q1 = __fdiv_rn(s, 3.0f);
+    const float rem = __fmaf_rn(-3.0f, q1, s);  // s - 3 q1, exact
+    // s / 3 - q1 = rem / 3; a midpoint sits at +-ulp/2
+    const float ulp = fabsf(__int_as_float(__float_as_int(q1) + 1) - q1);
+    const float d = fabsf(rem) - 1.5f * ulp;  // 3 (|s/3 - q1| - ulp/2), exact or nearly
+    if (fabsf(d) > 1.0e-6f * ulp && (__float_as_int(q1) & 0x7fffff) != 0) {
+        return q1;
+    }
+    return __double2float_rn((double)s / 3.0);
+}
+
+// MultiGrayscaleAccessor on float RGB (src/mga.h:184-222).  The reference's
+// RealPromote of float is float: the average adds the samples in float and
+// divides by 3.0 in double, the lightness adds min and max in float;
+// luminance (0.3/0.59/0.11) and the channel mixer are double expressions.
+__device__ __forceinline__ float gray_of_f(const FloatWeightParams& p, float r, float g, float b)
+{
+    switch (p.gray_projector) {
+    case ENB_GRAY_VALUE: return fmaxf(r, fmaxf(g, b));
+    case ENB_GRAY_ANTI_VALUE: return fminf(r, fminf(g, b));
+    case ENB_GRAY_LIGHTNESS: return 0.5f * __fadd_rn(fminf(r, fminf(g, b)), fmaxf(r, fmaxf(g, b)));
+    case ENB_GRAY_LUMINANCE:
+        return __double2float_rn(__dadd_rn(__dadd_rn(__dmul_rn(0.3, (double)r), __dmul_rn(0.59, (double)g)),
+                                           __dmul_rn(0.11, (double)b)));
+    case ENB_GRAY_MIXER:
+        return __double2float_rn(__dadd_rn(__dadd_rn(__dmul_rn(p.mixer[0], (double)r), __dmul_rn(p.mixer[1], (double)g)),
+                                           __dmul_rn(p.mixer[2], (double)b)));
+    default: return third_of(__fadd_rn(__fadd_rn(r, g), b));
+    }
+}
+
+// The built-in exposure weight functions (src/exposure_weight.h:44-128).
+// The reference forms y = gray / max in float (both operands are float) and
+// z = (y - optimum) / width in double.  Here z is carried as a float-float
+// pair zh + zl (error ~1e-14 relative), so that the functions that vanish at
+// the edge of their support (half-sine, full-sine, bisquare) keep their
+// relative accuracy there; each function is then evaluated in float with a
+// first-order correction for zl.
+__device__ __forceinline__ float exposure_f(const FloatWeightParams& p, float gray)
+{
+    const float y = __fdiv_rn(gray, p.range);
+    // d = y - (opt_hi + opt_lo) as dh + dl: TwoSum(y, -opt_hi), then opt_lo
+    const float s = __fsub_rn(y, p.opt_hi);
+    const float bv = __fsub_rn(s, y);
+    const float e = __fadd_rn(__fsub_rn(y, __fsub_rn(s, bv)), __fsub_rn(-p.opt_hi, bv));
+    const float dl0 = __fsub_rn(e, p.opt_lo);
+    const float dh = __fadd_rn(s, dl0);
+    const float dl = __fsub_rn(dl0, __fsub_rn(dh, s));
+    // z = d * (inv_hi + inv_lo)
+    const float zh = __fmul_rn(dh, p.inv_hi);
+    const float zl = __fadd_rn(__fmaf_rn(dh, p.inv_hi, -zh), __fmaf_rn(dh, p.inv_lo, __fmul_rn(dl, p.inv_hi)));
+    const float az = fabsf(zh);
+    switch (p.exp_function) {
+    case ENB_EXP_LORENTZIAN: return __fdiv_rn(1.0f, __fmaf_rn(0.5f * zh, zh, 1.0f));
+    case ENB_EXP_HALF_SINE: {
+        if (az > 1.57079632679489661923f) {
+            return 0.0f;
+        }
+        float sn, cs;
+        sincosf(zh, &sn, &cs);
+        return fmaxf(__fmaf_rn(-sn, zl, cs), 0.0f);
+    }
+    case ENB_EXP_FULL_SINE: {
+        if (az > 3.14159265358979323846f) {
+            return 0.0f;
+        }
+        // 0.5 + cos(z) / 2 = cos(z / 2)^2, without the cancellation near z = pi
+        float sn, cs;
+        sincosf(0.5f * zh, &sn, &cs);
+        const float c = __fmaf_rn(-sn, 0.5f * zl, cs);
+        return c * c;
+    }
+    case ENB_EXP_BISQUARE: {
+        if (az > 1.0f) {
+            return 0.0f;
+        }
+        // (1 - z^2)(1 + z^2) with 1 - z^2 = (1 - zh)(1 + zh) - 2 zh zl
+        const float one_minus = __fmaf_rn(-2.0f * zh, zl, __fmul_rn(1.0f - zh, 1.0f + zh));
+        const float one_plus = __fmaf_rn(zh, zh, __fmul_rn(2.0f * zh, zl)) + 1.0f;
+        return fmaxf(one_minus, 0.0f) * one_plus;
+    }
+    default: {
+        // exp(-z^2 / 2) with z^2 / 2 = qh + ql
+        const float qh = __fmul_rn(0.5f * zh, zh);
+        const float ql = __fmaf_rn(0.5f * zh, zh, -qh) + zh * zl;
+        return expf(-qh) * (1.0f - ql);
+    }
+    }
+}
+
+// Histogram::entropyOfChannel of n float keys sorted by bit pattern (equal
+// floats are adjacent; -0 was folded into +0), src/enfuse.h:346-375.  The
+// sum of p log p is exact in 2^-56 fixed point (host table; the tables of
+// float images are built with max 1, so scale_logb[b] = 1 / log b); H <= 1.
+__device__ __forceinline__ float entropy_f(const uint32_t* v, int n, const WeightTables& tab, int nmax)
+{
+    if (n == 0) {
+        return 0.0f;
+    }
+    int bins = 0;
+    long long acc = 0;
+    const long long* fx = tab.plogp_fx + (int64_t)n * (nmax + 1);
+    int i = 0;
+    while (i < n) {
+        int j = i + 1;
+        while (j < n && v[j] == v[i]) {
+            ++j;
+        }
+        acc += fx[j - i];
+        ++bins;
+        i = j;
+    }
+    if (bins <= 1) {
+        return 0.0f;
+    }
+    const float H = __fmul_rn(-(float)acc * 1.3877787807814457e-17f, tab.scale_logb[bins]);  // 2^-56
+    return fminf(H, 1.0f);
+}
+
+
+// ---- one exposure's tile in shared memory -----------------------------------
+
+// Histogram key of a float sample: its bit pattern, -0 folded into +0.
+__device__ __forceinline__ uint32_t float_key(float f) { return __float_as_uint(f == 0.0f ? 0.0f : f); }
+
+// Tile of (TW x TW) input pixels around a block of output pixels: gray,
+// the three samples, opaque flags, repeat marks and their hash tables.
+struct FTile {
+    float* gray;     // [TW*TW]
+    float* raw;      // [3][TW*TW]
+    uint32_t* table; // [3][slots]
+    uint8_t* a;      // [TW*TW]
+    uint8_t* meta;   // [TW*TW]
+    uint8_t* flags;  // [3][slots]
+    int TW, slots;
+};
+
+__host__ __device__ inline size_t ftile_bytes(int TW, int slots)
+{
+    return (size_t)TW * TW * (4 * sizeof(float) + 2) + (size_t)slots * 3 * 5;
+}
+
+__device__ __forceinline__ FTile ftile_carve(unsigned char* smem, int TW, int slots)
+{
+    FTile t;
+    t.TW = TW;
+    t.slots = slots;
+    t.gray = reinterpret_cast<float*>(smem);
+    t.raw = t.gray + TW * TW;
+    t.table = reinterpret_cast<uint32_t*>(t.raw + 3 * TW * TW);
+    t.a = reinterpret_cast<uint8_t*>(t.table + 3 * slots);
+    t.meta = t.a + TW * TW;
+    t.flags = t.meta + TW * TW;
+    return t;
+}
+
+// Loads the tile whose top-left input pixel is (x0, y0) (all threads call;
+// ends with the tile complete in shared memory).  alpha == nullptr: opaque.
+__device__ __forceinline__ void ftile_load(const FTile& t, const FloatWeightParams& wp, const float* img, int64_t pitch,
+                                           int stride, int w, int h, int C, const uint8_t* alpha, int64_t apitch,
+                                           int x0, int y0)
+{
+    const int TW = t.TW;
+    for (int k = threadIdx.x; k < TW * TW; k += blockDim.x) {
+        const int r = k / TW, c = k - r * TW;
+        const int gx = x0 + c, gy = y0 + r;
+        float rgb[3] = {0.0f, 0.0f, 0.0f};
+        uint8_t a = 0;
+        if (gx >= 0 && gx < w && gy >= 0 && gy < h) {
+            const float* px = img + (int64_t)gy * pitch + (int64_t)gx * stride;
+            for (int ch = 0; ch < C; ++ch) {
+                rgb[ch] = __ldg(&px[ch]);
+            }
+            a = alpha ? (__ldg(&alpha[(int64_t)gy * apitch + gx]) != 0) : 1;
+        }
+        t.gray[k] = C == 1 ? rgb[0] : gray_of_f(wp, rgb[0], rgb[1], rgb[2]);
+        t.a[k] = a;
+        for (int ch = 0; ch < 3; ++ch) {
+            t.raw[ch * TW * TW + k] = rgb[ch];
+        }
+    }
+    __syncthreads();
+    if (t.slots) {
+        mark_repeats(t.raw, TW * TW, t.a, TW * TW, C, t.table, t.flags, t.slots, t.meta,
+                     [](float f) { return float_key(f); });
+    }
+}
+
+// Sample standard deviation of the opaque window pixels (localStdDevIf,
+// src/enfuse.h:75-219) in two passes around the float mean.  CW > 0: the
+// window size at compile time; CW == 0: b is the runtime half-width.
+template <int CW>
+__device__ __forceinline__ float window_stddev(const FTile& t, int ci, int bdyn)
+{
+    const int b = CW > 0 ? CW / 2 : bdyn;
+    const int TW = t.TW;
+    float sum = 0.0f;
+    int n = 0;
+#pragma unroll
+    for (int dy = -b; dy <= b; ++dy) {
+#pragma unroll
+        for (int dx = -b; dx <= b; ++dx) {
+            const int idx = ci + dy * TW + dx;
+            const bool on = t.a[idx] != 0;
+            sum += on ? t.gray[idx] : 0.0f;
+            n += on ? 1 : 0;
+        }
+    }
+    if (n <= 1) {
+        return 0.0f;
+    }
+    const float mean = __fdiv_rn(sum, (float)n);
+    float s1 = 0.0f, s2 = 0.0f;
+#pragma unroll
+    for (int dy = -b; dy <= b; ++dy) {
+#pragma unroll
+        for (int dx = -b; dx <= b; ++dx) {
+            const int idx = ci + dy * TW + dx;
+            const float d = t.a[idx] ? t.gray[idx] - mean : 0.0f;
+            s1 += d;
+            s2 = fmaf(d, d, s2);
+        }
+    }
+    const float var = __fdiv_rn(s2 - __fdiv_rn(s1 * s1, (float)n), (float)(n - 1));
+    return sqrtf(fmaxf(var, 0.0f));
+}
+
+// H of channel ch of the entropy window at ci (EW: 3 or 5 at compile time,
+// 0: the runtime window wp.entropy_window through an insertion sort).
+template <int EW>
+__device__ __forceinline__ float window_entropy(const FTile& t, const FloatWeightParams& wp, const WeightTables& tab,
+                                                int ci, int ch, int nwin, uint32_t marks)
+{
+    const float* raw = t.raw + ch * t.TW * t.TW;
+    const int nmax = (EW > 0 ? EW * EW : wp.entropy_window * wp.entropy_window);
+    if (EW > 0) {
+        float H;
+        if (!(marks & (1u << ch))) {
+            return entropy_distinct(nwin, tab, nmax);  // all keys distinct
+        }
+        if (entropy_one_repeat<(EW > 0 ? EW : 3)>(raw, t.meta, t.TW, ci, 1u << ch, nwin, tab, nmax,
+                                                  [](float f) { return float_key(f); }, H)) {
+            return H;  // one repeated key (a clipped highlight)
+        }
+        return entropy_window_float<(EW > 0 ? EW : 3)>(raw, t.a, t.TW, ci, tab);
+    }
+    const int b = wp.entropy_window / 2;
+    uint32_t vals[kMaxEntropyWindow * kMaxEntropyWindow];
+    int n = 0;
+    for (int dy = -b; dy <= b; ++dy) {
+        for (int dx = -b; dx <= b; ++dx) {
+            const int idx = ci + dy * t.TW + dx;
+            if (t.a[idx]) {
+                const uint32_t v = float_key(raw[idx]);
+                int q = n++;
+                while (q > 0 && vals[q - 1] > v) {
+                    vals[q] = vals[q - 1];
+                    --q;
+                }
+                vals[q] = v;
+            }
+        }
+    }
+    return entropy_f(vals, n, tab, nmax);
+}
+
+// The enfuseMask weight of the output pixel (x, y) whose tile index is ci:
+// exposure (assigned), + contrast, + saturation, + entropy, float adds in
+// the reference's order (src/enfuse.h:1119-1120, 1133-1134, 1208-1209).
+template <int CW, int EW>
+__device__ __forceinline__ float f_pixel_weight(const FTile& t, const FloatWeightParams& wp, const WeightTables& tab,
+                                                int ci, int x, int y, int w, int h, int C)
+{
+    if (!t.a[ci]) {
+        return 0.0f;
+    }
+    float result = 0.0f;
+    if (wp.use_exposure) {
+        result = wp.w_exposure * exposure_f(wp, t.gray[ci]);
+    }
+    if (wp.use_contrast) {
+        const int b = wp.contrast_window / 2;
+        float sd = 0.0f;  // the border strip is not written (0)
+        if (x >= b && x < w - b && y >= b && y < h - b) {
+            sd = window_stddev<CW>(t, ci, b);
+        }
+        result = wp.w_contrast * sd + result;
+    }
+    if (wp.use_saturation && C == 3) {
+        // SaturationFunctor with max_value 1.0 (src/enfuse.h:733-780);
+        // 2 - (max + min) is formed as (1 - max) + (1 - min), whose terms
+        // are exact near white
+        const int TT = t.TW * t.TW;
+        const float r = t.raw[ci], g = t.raw[TT + ci], bb = t.raw[2 * TT + ci];
+        const float mx = fmaxf(r, fmaxf(g, bb)), mn = fminf(r, fminf(g, bb));
+        float sw = 0.0f;
+        if (mx != mn) {
+            const float sum = mx + mn, diff = mx - mn;
+            const float den = sum <= 1.0f ? sum : (1.0f - mx) + (1.0f - mn);
+            sw = wp.w_saturation * __fdiv_rn(diff, den);
+        }
+        result = sw + result;
+    }
+    if (wp.use_entropy) {
+        const int b = wp.entropy_window / 2;
+        float emin = 0.0f;
+        if (x >= b && x < w - b && y >= b && y < h - b) {
+            int nwin = 0;
+            uint32_t marks = 0xffu;
+            if (EW > 0 && t.slots) {
+                window_marks<(EW > 0 ? EW : 3)>(t.meta, t.TW, ci, nwin, marks);
+            }
+            emin = 3.402823466e38f;
+            for (int ch = 0; ch < C; ++ch) {
+                // fromRealPromote<float>(H * max): the entropy image pixel
+                emin = fminf(emin, __fmul_rn(window_entropy<EW>(t, wp, tab, ci, ch, nwin, marks), wp.range));
+            }
+        }
+        result = __fmul_rn(wp.w_entropy, emin) + result;
+    }
+    return result;
+}
+
+// Halo of the weight windows and the hash slots of the repeat marks.
+__host__ __device__ inline int fweight_halo(const FloatWeightParams& wp)
+{
+    const int hc = wp.use_contrast ? wp.contrast_window / 2 : 0, he = wp.use_entropy ? wp.entropy_window / 2 : 0;
+    return hc > he ? hc : he;
+}
+
+inline int fweight_slots(const FloatWeightParams& wp, int TW)
+{
+    if (!wp.use_entropy || (wp.entropy_window != 3 && wp.entropy_window != 5)) {
+        return 0;
+    }
+    int slots = 64;
+    while (slots < 2 * TW * TW) {
+        slots <<= 1;
+    }
+    return slots;
+}
+
+}  // namespace enb

@@ -7,6 +7,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "enbgpu.h"
 
@@ -98,6 +99,7 @@ struct FloatWeightParams {
     float range;
     float opt_hi, opt_lo;  // exposure optimum as a sum of two floats
     float inv_hi, inv_lo;  // 1 / effective width of the weight function, ditto
+    int repeat_slots;      // hash slots per channel of the repeated-sample marks (0: none)
 };
 
 // Name and algorithmic bytes of the most recent launch on this host thread;
@@ -220,6 +222,30 @@ cudaError_t launch_up_level(const PlanarView& gw1, const PlanarView& gb1, const 
 cudaError_t launch_out0(const PlanarView* gw1, const PlanarView* gb1, const PlanarView* r1, const Out0Host& h,
                         cudaStream_t st, int ty0 = 0, int nty = -1);
 cudaError_t launch_coarse(const CoarseHost& h, cudaStream_t st);
+
+// batched fuse of float stacks (enb_batch.cu)
+constexpr int kBatchMaxK = 16;
+struct BatchStackHost {
+    int K, w, h, C;
+    const float* img[kBatchMaxK];
+    int64_t ipitch[kBatchMaxK];  // floats
+    int istride[kBatchMaxK];
+    const uint8_t* alpha[kBatchMaxK];  // nullptr: opaque
+    int64_t apitch[kBatchMaxK];
+    float* out;
+    int64_t opitch;  // floats
+    int ostride;
+    uint8_t* oalpha;  // nullptr: not written
+    int64_t oapitch;
+};
+struct BatchPlan;
+cudaError_t batch_plan_create(const std::vector<BatchStackHost>& stacks, const FloatWeightParams& wp,
+                              const WeightTables& tab, int levels, int wrap, int hard, int64_t coarse_pixels,
+                              cudaStream_t st, BatchPlan** out);
+void batch_plan_destroy(BatchPlan* p);
+int batch_plan_steps(const BatchPlan* p);
+double batch_plan_pixels(const BatchPlan* p);
+cudaError_t batch_plan_launch(const BatchPlan* p, int step, cudaStream_t st);
 
 // float-image path (enb_float.cu): FP32 pyramid levels (dtype ENB_F32)
 cudaError_t launch_f_to_pyramid(const FloatPixelView& s, const PlanarView& d, cudaStream_t st);

@@ -12,6 +12,7 @@
 
 #include "enb_device.cuh"
 #include "enb_internal.h"
+#include "enb_entropy.cuh"
 #include "enb_reduce.cuh"
 
 namespace enb {
@@ -65,20 +66,6 @@ __global__ void __launch_bounds__(256) k_float_to_fixed(const float* __restrict_
     }
     const double v = __dmul_rn((double)src[(int64_t)y * spitch + x], (double)(1u << frac));
     dst[(int64_t)y * dpitch + x] = frp_store<TD>(v);
-}
-
-// Exact fromRealPromote(m * 2^frac) for 0 <= m * 2^frac < 2^23 in float
-// arithmetic: the product is exact, floor and the fractional part are exact.
-template <typename TD>
-__device__ __forceinline__ TD mask_to_fixed(float m, int frac)
-{
-    const float v = m * (float)(1u << frac);
-    if (v >= 0.0f && v < 8388608.0f) {
-        const float fl = floorf(v);
-        const int r = (int)fl + ((v - fl) >= 0.5f ? 1 : 0);
-        return (TD)r;
-    }
-    return frp_store<TD>(__dmul_rn((double)m, (double)(1u << frac)));
 }
 
 // Soft-mask normalisation fused with the conversion of the mask to fixed
@@ -626,6 +613,14 @@ __global__ void __launch_bounds__(256) k_enfuse_mask(PixelView img, AlphaSrc alp
                 const int nmax = wp.entropy_window * wp.entropy_window;
                 emin = wp.maxv;
                 for (int ch = 0; ch < C; ++ch) {
+                    if (wp.entropy_window == 5 || wp.entropy_window == 3) {
+                        const uint16_t* raw = s_raw + ch * TW * TW;
+                        const uint32_t e = wp.entropy_window == 5
+                                               ? entropy_window_int<5>(raw, s_a, TW, ci, tab, wp.maxv)
+                                               : entropy_window_int<3>(raw, s_a, TW, ci, tab, wp.maxv);
+                        emin = min(emin, e);
+                        continue;
+                    }
                     int n = 0;
                     for (int dy = -b; dy <= b; ++dy) {
                         const int row = (ly + halo + dy) * TW + lx + halo;

@@ -63,7 +63,13 @@ class EnbEnfuseParams(ctypes.Structure):
 class EnbFuseOptions(ctypes.Structure):
     _fields_ = [("levels", ctypes.c_int32), ("wrap", ctypes.c_int32), ("hard_mask", ctypes.c_int32),
                 ("dither", ctypes.c_int32), ("seed", ctypes.c_uint64), ("host_buffers", ctypes.c_int32),
-                ("plain", ctypes.c_int32), ("level0_out", ctypes.c_void_p), ("coarse_pixels", ctypes.c_int32)]
+                ("plain", ctypes.c_int32), ("level0_out", ctypes.c_void_p), ("coarse_pixels", ctypes.c_int32),
+                ("graph", ctypes.c_int32)]
+
+
+class EnbStack(ctypes.Structure):
+    _fields_ = [("K", ctypes.c_int32), ("images", ctypes.POINTER(EnbImage)), ("alphas", ctypes.POINTER(EnbImage)),
+                ("out", ctypes.POINTER(EnbImage)), ("out_alpha", ctypes.POINTER(EnbImage))]
 
 
 _P = ctypes.POINTER
@@ -107,6 +113,8 @@ _SIGNATURES = {
     "enb_enfuse_mask": (ctypes.c_int, [ctypes.c_void_p, _P(EnbEnfuseParams), _IMG, _IMG, _IMG]),
     "enb_enfuse": (ctypes.c_int, [ctypes.c_void_p, _P(EnbEnfuseParams), ctypes.c_int, _IMG, _IMG, _IMG, _IMG,
                                   _IMG, _P(EnbFuseOptions)]),
+    "enb_fuse_stacks": (ctypes.c_int, [ctypes.c_void_p, _P(EnbEnfuseParams), ctypes.c_int, _P(EnbStack),
+                                        _P(EnbFuseOptions)]),
     "enb_enblend": (ctypes.c_int, [ctypes.c_void_p, _IMG, _IMG, _IMG, _IMG, _IMG, _IMG, _IMG,
                                    _P(EnbFuseOptions)]),
 }
@@ -429,6 +437,35 @@ class Context:
                                         ctypes.byref(pixel_image(out)), ctypes.byref(plane_image(out_alpha)),
                                         ctypes.byref(o)))
         return out, out_alpha
+
+    def fuse_stacks(self, stacks, params: Optional[EnbEnfuseParams] = None, outs=None, out_alphas=None,
+                    alphas=None, levels: int = 0, wrap: bool = False, hard_mask: bool = False, plain: bool = False,
+                    graph: bool = True, coarse_pixels: int = 0):
+        """Batched enfuse of independent float stacks (enb_fuse_stacks).  stacks: list of lists of (H, W, S)
+        float32 arrays (numpy: host buffers; torch: device).  Returns the list of outputs (and fills out_alphas
+        when given)."""
+        host = not _is_torch(stacks[0][0])
+        if outs is None:
+            outs = [np.zeros_like(st[0]) if host else st[0].new_zeros(st[0].shape) for st in stacks]
+        keep = []
+        descs = (EnbStack * len(stacks))()
+        for i, st in enumerate(stacks):
+            imgs = (EnbImage * len(st))(*[pixel_image(x) for x in st])
+            al = (EnbImage * len(st))(*[plane_image(a) for a in alphas[i]]) if alphas is not None else None
+            out = pixel_image(outs[i])
+            oa = plane_image(out_alphas[i]) if out_alphas is not None else None
+            keep += [imgs, al, out, oa]
+            descs[i].K = len(st)
+            descs[i].images = ctypes.cast(imgs, ctypes.POINTER(EnbImage))
+            descs[i].alphas = ctypes.cast(al, ctypes.POINTER(EnbImage)) if al is not None else None
+            descs[i].out = ctypes.pointer(out)
+            descs[i].out_alpha = ctypes.pointer(oa) if oa is not None else None
+        p = params if params is not None else enfuse_params()
+        o = self._options(levels, wrap, hard_mask, "hash", 0, host, None, plain, coarse_pixels)
+        o.graph = int(graph)
+        self._check(self.lib.enb_fuse_stacks(self.handle, ctypes.byref(p), len(stacks), descs, ctypes.byref(o)))
+        del keep
+        return outs
 
     def enblend(self, white, black, mask, white_alpha=None, black_alpha=None, out=None, out_alpha=None,
                 levels: int = 0, wrap: bool = False, dither: str = "hash", seed: int = 0x5eed, level0=None,

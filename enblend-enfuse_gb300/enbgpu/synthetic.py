@@ -112,3 +112,85 @@ def enfuse_9x6000x4000_u16(seed: int = 3, h: int = 4000, w: int = 6000):
 
 def enblend_2x4096x3072_u16(seed: int = 2, h: int = 3072, w: int = 4096, offset: int = 2867):
     return panorama_pair(h, w, offset, np.uint16, seed)
+
+
+# ---- device-side generator (torch) for the large batched workload ----------
+
+def _smooth_noise_torch(gen, h: int, w: int, sigma: float, device):
+    import torch
+    import torch.nn.functional as F
+    f = 8
+    hs, ws = max(4, -(-h // f) + 2), max(4, -(-w // f) + 2)
+    n = torch.randn((1, 1, hs, ws), generator=gen, device=device)
+    s = sigma / f
+    r = int(4 * s + 0.5)
+    x = torch.arange(-r, r + 1, device=device, dtype=torch.float32)
+    k = torch.exp(-0.5 * (x / s) ** 2)
+    k = k / k.sum()
+    n = F.pad(n, (r, r, 0, 0), mode="circular")
+    n = F.conv2d(n, k.view(1, 1, 1, -1))
+    n = F.pad(n, (0, 0, r, r), mode="circular")
+    n = F.conv2d(n, k.view(1, 1, -1, 1))
+    up = F.interpolate(n, scale_factor=f, mode="bilinear", align_corners=False)[0, 0, :h, :w]
+    up = up - up.mean()
+    sd = up.std()
+    return up / torch.clamp(sd, min=1e-12)
+
+
+def log_radiance_torch(h: int, w: int, stops: float, seed: int, device="cuda", shapes: int = 40):
+    """(H, W, 3) log2 radiance on the device, built like log_radiance (smooth
+    noise spanning `stops` stops, 40 rectangles and discs with log offsets
+    U(-2, 2), a +-0.25 stop tint per channel) from a torch generator."""
+    import torch
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed)
+    rng = np.random.default_rng(seed)
+    base = _smooth_noise_torch(gen, h, w, 32.0, device)
+    q = torch.quantile(base[:: max(1, h // 256), :: max(1, w // 256)].flatten(),
+                       torch.tensor([0.005, 0.995], device=device))
+    lo, hi = float(q[0]), float(q[1])
+    base = (base - lo) / max(hi - lo, 1e-9) * stops - stops / 2.0 + float(np.log2(0.18))
+    yy = torch.arange(h, device=device, dtype=torch.float32)[:, None]
+    xx = torch.arange(w, device=device, dtype=torch.float32)[None, :]
+    for _ in range(shapes):
+        off = rng.uniform(-2.0, 2.0)
+        cx, cy = rng.uniform(0, w), rng.uniform(0, h)
+        r = rng.uniform(0.02, 0.12) * min(h, w)
+        if rng.random() < 0.5:
+            x0, x1 = int(max(0, cx - r)), int(min(w, cx + r * rng.uniform(0.5, 1.5)))
+            y0, y1 = int(max(0, cy - r)), int(min(h, cy + r * rng.uniform(0.5, 1.5)))
+            base[y0:y1, x0:x1] += off
+        else:
+            base += off * (((xx - cx) ** 2 + (yy - cy) ** 2) <= r * r).float()
+    tint = torch.stack([_smooth_noise_torch(gen, h, w, 64.0, device) * 0.25 for _ in range(3)], dim=-1)
+    return base[..., None] + tint
+
+
+def expose_torch(lograd, ev: float):
+    """clip((2^lograd * 2^ev)^(1/2.2), 0, 1) as float32 on the device."""
+    import torch
+    return torch.clamp(torch.exp2(lograd + ev) ** (1.0 / 2.2), 0.0, 1.0).contiguous()
+
+
+def uneven_stack_specs(n: int = 64, seed: int = 4, lo: int = 512, hi: int = 4096, kmin: int = 3, kmax: int = 7):
+    """The batched workload: n stacks with width and height log-uniform in
+    [lo, hi] and an exposure count uniform in {kmin..kmax}, EVs evenly spaced
+    over +-(count - 1) stops.  Returns [(h, w, evs, seed)]."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(n):
+        w = int(round(np.exp(rng.uniform(np.log(lo), np.log(hi)))))
+        h = int(round(np.exp(rng.uniform(np.log(lo), np.log(hi)))))
+        K = int(rng.integers(kmin, kmax + 1))
+        specs.append((h, w, list(np.linspace(-(K - 1), K - 1, K)), seed * 1000 + i))
+    return specs
+
+
+def uneven_stacks_torch(specs, stops: float = 8.0, device="cuda"):
+    """Device-resident FP32 RGB exposure stacks of the given specs."""
+    out = []
+    for (h, w, evs, s) in specs:
+        lr = log_radiance_torch(h, w, stops, s, device)
+        out.append([expose_torch(lr, ev) for ev in evs])
+        del lr
+    return out

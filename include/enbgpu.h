@@ -133,7 +133,13 @@ typedef struct {
                               width*height*channels */
     int32_t coarse_pixels; /* enblend: pyramid levels of at most this many
                               pixels run in one cluster launch; 0: default
-                              (none), < 0: every level in its own launches */
+                              (none), < 0: every level in its own launches.
+                              enb_fuse_stacks: levels of at most this many
+                              pixels run in the persistent coarse kernel;
+                              0: default (64 x 64), < 0: none */
+    int32_t graph;         /* enb_fuse_stacks: 1 (default) replays a CUDA
+                              graph of the launch sequence, captured once per
+                              batch geometry; 0 launches directly */
 } enb_fuse_options;
 
 typedef struct enb_ctx enb_ctx;
@@ -277,6 +283,30 @@ enb_status enb_enfuse(enb_ctx* ctx, const enb_enfuse_params* params, int K, cons
 enb_status enb_enblend(enb_ctx* ctx, const enb_image* white, const enb_image* white_alpha,
                        const enb_image* black, const enb_image* black_alpha, const enb_image* mask,
                        const enb_image* out, const enb_image* out_alpha, const enb_fuse_options* opt);
+
+/* ---- batched stacks (no counterpart in the reference) ------------------- */
+/* One exposure stack of a batched fuse. */
+#define ENB_BATCH_MAX_K 16
+typedef struct {
+    int32_t K;                  /* exposures, 1..ENB_BATCH_MAX_K */
+    const enb_image* images;    /* K interleaved F32 images of one geometry */
+    const enb_image* alphas;    /* K U8 alpha planes, or NULL (thresholded 4th
+                                   component of RGBA images, else opaque) */
+    const enb_image* out;       /* interleaved F32 result of the geometry */
+    const enb_image* out_alpha; /* U8 union alpha, or NULL */
+} enb_stack;
+
+/* enfuseMain (src/enfuse.h:1217-1617) of n independent float stacks of
+ * arbitrary, different sizes and exposure counts as one batch: every launch
+ * covers all stacks at one pyramid level, the levels of at most
+ * opt->coarse_pixels pixels run in one persistent kernel, and the sequence
+ * is replayed as a CUDA graph.  Each stack's result is that of enb_enfuse on
+ * it (same FP32 arithmetic up to the order of float additions).  masks are
+ * computed (no --load-masks); opt->plain = 1 runs enb_enfuse stack by stack
+ * instead (for comparisons).  The workspace and graph of the last batch
+ * geometry stay cached in the context. */
+enb_status enb_fuse_stacks(enb_ctx* ctx, const enb_enfuse_params* params, int n_stacks, const enb_stack* stacks,
+                           const enb_fuse_options* opt);
 
 #ifdef __cplusplus
 }
