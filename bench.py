@@ -17,6 +17,10 @@ input pixels blended per second (2 x 4096 x 3072 = 25.17 Mpx per step).
   cpu_baseline  the CPU oracle (a port of the reference's algorithm: serial
          pyramids, OpenMP pointwise steps) on a quarter of the rows
 
+  batched_fuse  the batched uneven-stack workload (64 FP32 stacks of
+         uneven sizes and exposure counts): enb_fuse_stacks replayed as one
+         CUDA graph against the plain per-stack path on the same GPU
+
 --impl reference times that CPU implementation alone on the same metric.
 Multi-GPU runs are independent replicas (the path does not shard): each rank
 blends its own copy, value = total Mpx / max-over-ranks time.
@@ -59,6 +63,9 @@ def parse_args():
                     help="run warmup + steps on device inputs only (for ncu launch lists)")
     ap.add_argument("--rows", type=int, default=H,
                     help="with --profile-only: scene height (a smaller case of the same workload for ncu)")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the batched uneven-stack measurement (batched_fuse object)")
+    ap.add_argument("--batched-stacks", type=int, default=64)
     ap.add_argument("--plain", action="store_true",
                     help="with --profile-only: the reference's pass structure instead of the fused passes")
     return ap.parse_args()
@@ -208,6 +215,69 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def batched_fuse(ctx, stream, n_stacks: int, reps: int = 3) -> dict:
+    """The batched uneven-stack workload: n FP32 RGB stacks, width and height
+    log-uniform in [512, 4096], 3..7 exposures, EVs evenly spaced over
+    +-(count - 1) stops, weights exposure 1.0 / saturation 0.2 / contrast 0.5
+    (5x5) / entropy 0.3 (5x5) in normalised-float mode; enb_fuse_stacks (one
+    CUDA graph) against the plain per-stack path (enb_enfuse per stack) on
+    the same GPU, device-resident inputs."""
+    import torch
+    import enbgpu
+    from enbgpu import synthetic
+    specs = synthetic.uneven_stack_specs(n_stacks)
+    stacks = synthetic.uneven_stacks_torch(specs)
+    outs = [st[0].new_zeros(st[0].shape) for st in stacks]
+    units = sum(len(st) * st[0].shape[0] * st[0].shape[1] for st in stacks) / 1e6
+    prm = enbgpu.enfuse_params(saturation_weight=0.2, contrast_weight=0.5, entropy_weight=0.3,
+                               contrast_window_size=5, entropy_window_size=5, float_range=1.0)
+
+    def timed(fn, n):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(n):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / n
+
+    l0 = ctx.launches
+    batched_ms = timed(lambda: ctx.fuse_stacks(stacks, params=prm, outs=outs), reps)
+    launches = (ctx.launches - l0) // (reps + 1)
+    ref = [o.clone() for o in outs]
+    plain_ms = timed(lambda: ctx.fuse_stacks(stacks, params=prm, outs=outs, plain=True), max(1, reps - 1))
+    max_rel = max(float(((o - r).abs() / (r.abs() + 1e-6)).max()) for o, r in zip(outs, ref))
+    ctx.profile(True)
+    ctx.fuse_stacks(stacks, params=prm, outs=outs, graph=False)
+    kb = ctx.profile_report()
+    ctx.profile(False)
+    ctx.profile(True)
+    ctx.fuse_stacks(stacks, params=prm, outs=outs, plain=True)
+    kp = ctx.profile_report()
+    ctx.profile(False)
+    weights_b, weights_p = kb["batch_weights"]["ms"], kp["f_enfuse_mask"]["ms"]
+    return {
+        "workload": f"{n_stacks} FP32 RGB stacks, W,H log-uniform [512,4096], 3..7 exposures, "
+                    "weights exposure 1.0 / saturation 0.2 / contrast 0.5 (5x5) / entropy 0.3 (5x5), "
+                    "normalised-float mode (float_range 1.0)",
+        "units": units, "metric": METRIC,
+        "batched": {"value": units / (batched_ms / 1e3), "ms_per_step": batched_ms, "graph": True,
+                    "launches_per_step": launches},
+        "plain": {"value": units / (plain_ms / 1e3), "ms_per_step": plain_ms,
+                  "what": "enb_enfuse stack by stack (the per-stack path)"},
+        "speedup": plain_ms / batched_ms,
+        "weights_ms": {"batched": weights_b, "plain": weights_p},
+        "excluding_weights_ms": {"batched": batched_ms - weights_b, "plain": plain_ms - weights_p,
+                                 "speedup": (plain_ms - weights_p) / max(batched_ms - weights_b, 1e-9)},
+        "batched_kernels": {k: {"launches": v["launches"], "ms": v["ms"],
+                                "GBps": v["bytes"] / (v["ms"] / 1e3) / 1e9 if v["ms"] > 0 and v["bytes"] else None}
+                            for k, v in kb.items()},
+        "max_rel_diff_vs_plain": max_rel,
+    }
+
+
 def run_ours(args) -> None:
     import torch
     import enbgpu
@@ -345,6 +415,9 @@ def run_ours(args) -> None:
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_oracle_rate(args.seed)
+    if rank == 0 and ws == 1 and not args.no_batched:
+        del dw, db, dm, out, oa
+        line["batched_fuse"] = batched_fuse(ctx, stream, args.batched_stacks)
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()

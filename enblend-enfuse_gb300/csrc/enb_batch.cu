@@ -220,13 +220,30 @@ __device__ __forceinline__ void batch_reduce_tile(const BatchStack& s, int kind,
 
 constexpr int kBatchReduceSmem = ReduceSmem<3, true>::WORDS * 4;
 
+// Image jobs (kind < K) and mask jobs (kind >= K) of a level run as two
+// launches, each with the registers its path needs.
 template <int C>
-__global__ void __launch_bounds__(RTHREADS, 3) k_batch_reduce(const BatchStack* __restrict__ stacks,
+__global__ void __launch_bounds__(RTHREADS, 2) k_batch_reduce(const BatchStack* __restrict__ stacks,
                                                               const int4* __restrict__ jobs, int l, int wrap)
 {
     __shared__ __align__(16) unsigned char smem[kBatchReduceSmem];
     const int4 job = jobs[blockIdx.x];
     batch_reduce_tile<C, true>(stacks[job.x], job.y, l, job.z * RDW, job.w * RDH, wrap, smem);
+}
+
+__global__ void __launch_bounds__(RTHREADS, 3) k_batch_reduce_mask(const BatchStack* __restrict__ stacks,
+                                                                   const int4* __restrict__ jobs, int l, int wrap)
+{
+    __shared__ __align__(16) int32_t V[ReduceSmem<1, true>::NV][RDH][RVP];
+    const int4 job = jobs[blockIdx.x];
+    const BatchStack& s = stacks[job.x];
+    const int k = job.y - s.K;
+    const int sw = s.lw[l], sh = s.lh[l], dw = s.lw[l + 1], dh = s.lh[l + 1];
+    using Src = PlanarSource<int32_t, 1, true, true>;
+    const ReduceJob<Src, int32_t> rj{
+        Src{m_level(s, k, l), s.pitch[l], (int64_t)s.pitch[l] * sh, s.u + s.off0[l], s.pitch[l]}, m_level(s, k, l + 1),
+        s.pitch[l + 1], (int64_t)s.pitch[l + 1] * dh, s.u + s.off0[l + 1], s.pitch[l + 1]};
+    reduce_tile<Src, int32_t, 1, true, int32_t>(rj, job.z * RDW, job.w * RDH, sw, sh, dw, dh, wrap, V);
 }
 
 // ---------------------------------------------------------------------------
@@ -302,12 +319,15 @@ __device__ __forceinline__ void stage_window(float (*ss)[ESH][ESW], const float*
 // One 64x16 tile of level l of a stack (256 working threads, 2x2 quads):
 // C[l] = sum_k (G_k[l] - E(G_k[l+1])) m_k[l] / D + E(C[l+1]), written to
 // the result level (l >= 1) or converted into the output pixels (l == 0).
-// At the stack's top level the expand terms are absent.  NC as for the reduce.
+// At the stack's top level the expand terms are absent.  NC as for the
+// reduce.  The level-(l+1) windows of all K exposures and of C[l+1] are
+// staged together (one barrier); ss holds (K + 1) * C windows.
 template <int C, bool NC>
 __device__ __forceinline__ void batch_up_tile(const BatchStack& s, int l, int X0, int Y0, int wrap, float inv_d,
                                               float (*ss)[ESH][ESW])
 {
     const bool top = l == s.L - 1;
+    const int K = s.K;
     const int dw = s.lw[l], dh = s.lh[l];
     const int sw = top ? 1 : s.lw[l + 1], sh = top ? 1 : s.lh[l + 1];
     const int I0 = X0 >> 1, J0 = Y0 >> 1;
@@ -317,117 +337,83 @@ __device__ __forceinline__ void batch_up_tile(const BatchStack& s, int l, int X0
     const int X = 2 * i, Y = 2 * j;
     const bool active = tid < 256 && X < dw && Y < dh;
     const int64_t dp = s.pitch[l];
-    float acc[4][C];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-#pragma unroll
-        for (int c = 0; c < C; ++c) {
-            acc[q][c] = 0.0f;
-        }
-    }
     const int64_t gplane = (int64_t)dp * dh;
-    for (int k = 0; k < s.K; ++k) {
-        float e[4][C];
-        if (!top) {
-            stage_window<C>(ss, g_level(s, k, l + 1, C), s.pitch[l + 1], (int64_t)s.pitch[l + 1] * sh, sw, sh, I0, J0,
-                            wrap);
-            __syncthreads();
-            if (active) {
-                expand_quad_f<C>(ss, qx, qy, i, j, sw, sh, dw, wrap, e);
-            }
-        } else {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-#pragma unroll
-                for (int c = 0; c < C; ++c) {
-                    e[q][c] = 0.0f;
-                }
-            }
-        }
-        if (active) {
-            const int32_t* mk = m_level(s, k, l);
-            const float* gk = l > 0 ? g_level(s, k, l, C) : nullptr;
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int XX = X + (q & 1), YY = Y + (q >> 1);
-                if (XX < dw && YY < dh) {
-                    const float coeff = (float)ld_src<NC>(&mk[(int64_t)YY * dp + XX]) * inv_d;
-                    float g[C];
-                    if (l == 0) {
-                        const float* px = s.img[k] + (int64_t)YY * s.ipitch[k] + (int64_t)XX * s.istride[k];
-#pragma unroll
-                        for (int c = 0; c < C; ++c) {
-                            g[c] = to_pyramid_value(__ldg(&px[c]));
-                        }
-                    } else {
-#pragma unroll
-                        for (int c = 0; c < C; ++c) {
-                            g[c] = gk[(int64_t)c * gplane + (int64_t)YY * dp + XX];
-                        }
-                    }
-#pragma unroll
-                    for (int c = 0; c < C; ++c) {
-                        acc[q][c] += (g[c] - e[q][c]) * coeff;
-                    }
-                }
-            }
-        }
-        if (!top) {
-            __syncthreads();  // the next exposure restages the window
-        }
-    }
     if (!top) {
-        stage_window<C>(ss, r_level(s, l + 1, C), s.pitch[l + 1], (int64_t)s.pitch[l + 1] * sh, sw, sh, I0, J0, wrap);
-        __syncthreads();
-        if (active) {
-            float e[4][C];
-            expand_quad_f<C>(ss, qx, qy, i, j, sw, sh, dw, wrap, e);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-#pragma unroll
-                for (int c = 0; c < C; ++c) {
-                    acc[q][c] += e[q][c];
-                }
-            }
+        const int64_t sp = s.pitch[l + 1], splane = sp * sh;
+        for (int k = 0; k <= K; ++k) {
+            const float* src = k < K ? g_level(s, k, l + 1, C) : r_level(s, l + 1, C);
+            stage_window<C>(ss + k * C, src, sp, splane, sw, sh, I0, J0, wrap);
         }
-        __syncthreads();
     }
+    __syncthreads();
     if (!active) {
         return;
     }
+    // channel by channel (fewer live registers): the K exposures' terms of
+    // the four quad pixels, then the expand of C[l+1]
+    for (int c = 0; c < C; ++c) {
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll 2
+        for (int k = 0; k < K; ++k) {
+            float g[4], coeff[4];
+            const int32_t* mk = m_level(s, k, l);
+            const float* gk = l > 0 ? g_level(s, k, l, C) + (int64_t)c * gplane : nullptr;
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        const int XX = X + (q & 1), YY = Y + (q >> 1);
-        if (XX >= dw || YY >= dh) {
-            continue;
+            for (int q = 0; q < 4; ++q) {
+                const int XX = min(X + (q & 1), dw - 1), YY = min(Y + (q >> 1), dh - 1);
+                coeff[q] = (float)ld_src<NC>(&mk[(int64_t)YY * dp + XX]) * inv_d;
+                if (l == 0) {
+                    g[q] = to_pyramid_value(
+                        __ldg(&s.img[k][(int64_t)YY * s.ipitch[k] + (int64_t)XX * s.istride[k] + c]));
+                } else {
+                    g[q] = ld_src<NC>(&gk[(int64_t)YY * dp + XX]);
+                }
+            }
+            float e[4][1] = {{0.0f}, {0.0f}, {0.0f}, {0.0f}};
+            if (!top) {
+                expand_quad_f<1>(ss + k * C + c, qx, qy, i, j, sw, sh, dw, wrap, e);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                acc[q] += (g[q] - e[q][0]) * coeff[q];
+            }
         }
-        if (l > 0) {
-            float* r = r_level(s, l, C);
+        if (!top) {
+            float e[4][1];
+            expand_quad_f<1>(ss + K * C + c, qx, qy, i, j, sw, sh, dw, wrap, e);
 #pragma unroll
-            for (int c = 0; c < C; ++c) {
-                r[(int64_t)c * gplane + (int64_t)YY * dp + XX] = acc[q][c];
+            for (int q = 0; q < 4; ++q) {
+                acc[q] += e[q][0];
             }
-        } else {
-            float* o = s.out + (int64_t)YY * s.opitch + (int64_t)XX * s.ostride;
-            const bool on = s.u[(int64_t)YY * dp + XX] != 0;
+        }
 #pragma unroll
-            for (int c = 0; c < C; ++c) {
-                o[c] = on ? from_pyramid_value(acc[q][c]) : 0.0f;
+        for (int q = 0; q < 4; ++q) {
+            const int XX = X + (q & 1), YY = Y + (q >> 1);
+            if (XX >= dw || YY >= dh) {
+                continue;
             }
-            if (s.ostride == 4) {
-                o[3] = on ? 1.0f : 0.0f;  // AlphaTraits<float>::max()
+            if (l > 0) {
+                r_level(s, l, C)[(int64_t)c * gplane + (int64_t)YY * dp + XX] = acc[q];
+            } else {
+                float* o = s.out + (int64_t)YY * s.opitch + (int64_t)XX * s.ostride;
+                const bool on = s.u[(int64_t)YY * dp + XX] != 0;
+                o[c] = on ? from_pyramid_value(acc[q]) : 0.0f;
+                if (c == 0 && s.ostride == 4) {
+                    o[3] = on ? 1.0f : 0.0f;  // AlphaTraits<float>::max()
+                }
             }
         }
     }
 }
 
 template <int C>
-__global__ void __launch_bounds__(256) k_batch_up(const BatchStack* __restrict__ stacks, const int4* __restrict__ jobs,
+__global__ void __launch_bounds__(256, 4) k_batch_up(const BatchStack* __restrict__ stacks, const int4* __restrict__ jobs,
                                                   int l, int wrap, float inv_d)
 {
-    __shared__ float ss[C][ESH][ESW];
+    extern __shared__ __align__(16) float upsmem[];
     const int4 job = jobs[blockIdx.x];
-    batch_up_tile<C, true>(stacks[job.x], l, job.y * ETW, job.z * ETH, wrap, inv_d, ss);
+    batch_up_tile<C, true>(stacks[job.x], l, job.y * ETW, job.z * ETH, wrap, inv_d,
+                           reinterpret_cast<float(*)[ESH][ESW]>(upsmem));
 }
 
 // ---------------------------------------------------------------------------
@@ -439,7 +425,7 @@ __global__ void __launch_bounds__(RTHREADS) k_batch_coarse(const BatchStack* __r
                                                            const int* __restrict__ coarse_list, int ncoarse,
                                                            int* __restrict__ queue, int wrap, float inv_d)
 {
-    __shared__ __align__(16) unsigned char smem[kBatchReduceSmem];
+    extern __shared__ __align__(16) unsigned char smem[];  // max(reduce tile, (K + 1) * C windows)
     __shared__ int item;
     for (;;) {
         if (threadIdx.x == 0) {
@@ -491,8 +477,9 @@ struct BatchPlan {
     int* dcoarse = nullptr;       // stacks with a coarse end
     int* dqueue = nullptr;
     int ncoarse = 0;
+    int maxK = 1;
     struct Step {
-        int kind;  // 0 weights, 1 down, 2 coarse, 3 up
+        int kind;  // 0 weights, 1 image reduce, 4 mask reduce, 2 coarse, 3 up
         int level;
         int64_t job0, njobs;
         double bytes;
@@ -581,6 +568,7 @@ cudaError_t batch_plan_create(const std::vector<BatchStackHost>& hs, const Float
         bytes += align((size_t)s.K * s.s0 * 4) + align((size_t)s.s0) + align((size_t)s.K * p->C * s.s1 * 4) +
                  align((size_t)s.K * s.s1) + align((size_t)p->C * s.s1 * 4);
         p->pixels += (double)h.K * h.w * h.h;
+        p->maxK = std::max(p->maxK, h.K);
     }
     // job tables
     std::vector<int4> jobs;
@@ -618,7 +606,7 @@ cudaError_t batch_plan_create(const std::vector<BatchStackHost>& hs, const Float
                 continue;
             }
             const int tx = (s.lw[l + 1] + RDW - 1) / RDW, ty = (s.lh[l + 1] + RDH - 1) / RDH;
-            for (int kind = 0; kind < 2 * s.K; ++kind) {
+            for (int kind = 0; kind < s.K; ++kind) {
                 for (int y = 0; y < ty; ++y) {
                     for (int x = 0; x < tx; ++x) {
                         jobs.push_back(make_int4(i, kind, x, y));
@@ -626,8 +614,30 @@ cudaError_t batch_plan_create(const std::vector<BatchStackHost>& hs, const Float
                 }
             }
             const double src = (double)s.lw[l] * s.lh[l], dst = (double)s.lw[l + 1] * s.lh[l + 1];
-            b += s.K * (src * (l == 0 ? 4.0 * hs[i].istride[0] : 4.0 * p->C + 1.0) + dst * (4.0 * p->C + 1.0)) +
-                 s.K * (src * 4.0 + dst * 4.0) + src + dst;
+            b += s.K * (src * (l == 0 ? 4.0 * hs[i].istride[0] : 4.0 * p->C + 1.0) + dst * (4.0 * p->C + 1.0));
+        }
+        p->steps.back().njobs = (int64_t)jobs.size() - p->steps.back().job0;
+        p->steps.back().bytes = b;
+        if (p->steps.back().njobs == 0) {
+            p->steps.pop_back();
+        }
+        add_step(4, l, 0.0);
+        b = 0.0;
+        for (int i = 0; i < p->nstacks; ++i) {
+            const BatchStack& s = stacks[i];
+            if (l + 1 > std::min(s.Lc, s.L - 1)) {
+                continue;
+            }
+            const int tx = (s.lw[l + 1] + RDW - 1) / RDW, ty = (s.lh[l + 1] + RDH - 1) / RDH;
+            for (int kind = s.K; kind < 2 * s.K; ++kind) {
+                for (int y = 0; y < ty; ++y) {
+                    for (int x = 0; x < tx; ++x) {
+                        jobs.push_back(make_int4(i, kind, x, y));
+                    }
+                }
+            }
+            const double src = (double)s.lw[l] * s.lh[l], dst = (double)s.lw[l + 1] * s.lh[l + 1];
+            b += s.K * (src * 4.0 + dst * 4.0) + src + dst;
         }
         p->steps.back().njobs = (int64_t)jobs.size() - p->steps.back().job0;
         p->steps.back().bytes = b;
@@ -717,6 +727,9 @@ cudaError_t batch_plan_create(const std::vector<BatchStackHost>& hs, const Float
 int batch_plan_steps(const BatchPlan* p) { return (int)p->steps.size(); }
 double batch_plan_pixels(const BatchPlan* p) { return p->pixels; }
 
+// Shared memory of an up tile: the windows of K exposures and of C[l+1].
+static size_t up_smem_bytes(int K, int C) { return (size_t)(K + 1) * C * ESH * ESW * sizeof(float); }
+
 template <int C>
 static cudaError_t launch_step(const BatchPlan* p, const BatchPlan::Step& s, cudaStream_t st)
 {
@@ -749,6 +762,10 @@ static cudaError_t launch_step(const BatchPlan* p, const BatchPlan::Step& s, cud
         note_launch("batch_reduce", s.bytes);
         k_batch_reduce<C><<<(unsigned)s.njobs, RTHREADS, 0, st>>>(p->dstacks, jobs, s.level, p->wrap);
         break;
+    case 4:
+        note_launch("batch_reduce_mask", s.bytes);
+        k_batch_reduce_mask<<<(unsigned)s.njobs, RTHREADS, 0, st>>>(p->dstacks, jobs, s.level, p->wrap);
+        break;
     case 2: {
         note_launch("batch_coarse", 0.0);
         cudaError_t e = cudaMemsetAsync(p->dqueue, 0, sizeof(int), st);
@@ -759,13 +776,23 @@ static cudaError_t launch_step(const BatchPlan* p, const BatchPlan::Step& s, cud
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         const int grid = std::max(1, std::min(p->ncoarse, 2 * sms));
-        k_batch_coarse<C><<<grid, RTHREADS, 0, st>>>(p->dstacks, p->dcoarse, p->ncoarse, p->dqueue, p->wrap, inv_d);
+        const size_t smem = std::max((size_t)kBatchReduceSmem, up_smem_bytes(p->maxK, C));
+        if (smem > 48 * 1024) {
+            cudaFuncSetAttribute(k_batch_coarse<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        }
+        k_batch_coarse<C><<<grid, RTHREADS, smem, st>>>(p->dstacks, p->dcoarse, p->ncoarse, p->dqueue, p->wrap,
+                                                        inv_d);
         break;
     }
-    default:
+    default: {
         note_launch(s.level == 0 ? "batch_up0" : "batch_up", s.bytes);
-        k_batch_up<C><<<(unsigned)s.njobs, 256, 0, st>>>(p->dstacks, jobs, s.level, p->wrap, inv_d);
+        const size_t smem = up_smem_bytes(p->maxK, C);
+        if (smem > 48 * 1024) {
+            cudaFuncSetAttribute(k_batch_up<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        }
+        k_batch_up<C><<<(unsigned)s.njobs, 256, smem, st>>>(p->dstacks, jobs, s.level, p->wrap, inv_d);
         break;
+    }
     }
     return cudaGetLastError();
 }
