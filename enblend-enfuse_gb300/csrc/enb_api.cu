@@ -2106,4 +2106,162 @@ enb_status enb_fuse_stacks(enb_ctx* ctx, const enb_enfuse_params* prm, int n, co
     return ENB_OK;
 }
 
+// ---- adjoint ----------------------------------------------------------------
+
+enb_status enb_fuse_grad(enb_ctx* ctx, const enb_enfuse_params* prm, int K, const enb_image* images,
+                         const enb_image* logits, const enb_image* target, const enb_image* out,
+                         const enb_image* grad_logits, enb_fuse_grad_result* res, const enb_fuse_options* opt)
+{
+    if (!ctx) {
+        return ENB_ERR_INVALID;
+    }
+    enb_fuse_options o;
+    enb_default_fuse_options(&o);
+    if (opt) {
+        o = *opt;
+    }
+    ENB_CHECK(ctx, K >= 1 && images && target && res, "fuse_grad: images, target and result required");
+    for (int k = 0; k < K; ++k) {
+        ENB_CHECK(ctx, pixels_ok(&images[k]) && images[k].dtype == ENB_F32 && images[k].channels == 3,
+                  "fuse_grad: images must be interleaved F32 RGB");
+        ENB_CHECK(ctx, same_geometry(&images[k], &images[0]), "fuse_grad: images differ in size");
+    }
+    const int w = images[0].width, h = images[0].height;
+    ENB_CHECK(ctx, pixels_ok(target) && target->dtype == ENB_F32 && target->channels == 3 && target->width == w &&
+                       target->height == h,
+              "fuse_grad: target must be an F32 RGB image of the inputs' size");
+    if (out) {
+        ENB_CHECK(ctx, pixels_ok(out) && out->dtype == ENB_F32 && out->width == w && out->height == h,
+                  "fuse_grad: out must be an F32 image of the inputs' size");
+    }
+    for (int k = 0; k < K; ++k) {
+        if (logits) {
+            ENB_CHECK(ctx, floats_ok(&logits[k], w, h), "fuse_grad: logits must be F32 planes of the image size");
+        }
+        if (grad_logits) {
+            ENB_CHECK(ctx, floats_ok(&grad_logits[k], w, h), "fuse_grad: grad_logits must be F32 planes");
+        }
+    }
+    ENB_CHECK(ctx, !o.wrap && !o.hard_mask, "fuse_grad: wrap-around and hard masks are not differentiated");
+    if (prm->w_entropy > 0.0) {
+        return fail(ctx, ENB_ERR_UNSUPPORTED, "fuse_grad: the entropy weight is not differentiated");
+    }
+    ENB_TRY(check_params(ctx, prm, w, h));
+    const int L = enb_num_levels(w, h, 1, o.levels);
+    const int64_t fp = round_up(w, 32), plane = fp * h;
+    DevBuf planes, a255;
+    ENB_CUDA(ctx, planes.alloc((size_t)plane * 4 * K * 6 + 64, ctx->stream));
+    float* wk = (float*)planes.p;
+    float* ak = wk + plane * K;
+    float* mk = ak + plane * K;
+    float* gm = mk + plane * K;
+    float* gw = gm + plane * K;
+    float* ga = gw + plane * K;
+    double* dsc = (double*)(ga + plane * K);
+    const int64_t apitch = round_up(w, 128);
+    ENB_CUDA(ctx, a255.alloc((size_t)(apitch * h), ctx->stream));
+    ENB_CUDA(ctx, cudaMemsetAsync(a255.p, 255, (size_t)(apitch * h), ctx->stream));
+    ENB_CUDA(ctx, cudaMemsetAsync(dsc, 0, 6 * sizeof(double), ctx->stream));
+    const BytePlane alpha{(uint8_t*)a255.p, apitch, w, h};
+    enb_image aimg{};
+    aimg.data = a255.p;
+    aimg.pitch = apitch;
+    aimg.width = w;
+    aimg.height = h;
+    aimg.channels = 1;
+    aimg.pix_stride = 1;
+    aimg.dtype = ENB_U8;
+
+    // forward: weights, logits, masks
+    for (int k = 0; k < K; ++k) {
+        ENB_TRY(enfuse_mask_impl(ctx, prm, &images[k], &aimg, FloatPlane{wk + plane * k, fp, w, h}));
+        if (logits) {
+            ENB_CUDA(ctx, cudaMemcpy2DAsync(ak + plane * k, fp * 4, logits[k].data, logits[k].pitch, (size_t)w * 4, h,
+                                            cudaMemcpyDeviceToDevice, ctx->stream));
+        }
+    }
+    ENB_LAUNCH(ctx, launch_adj_norm(K, wk, logits ? ak : nullptr, mk, fp, plane, w, h, ctx->stream));
+    PyrHolder R(ctx), LP(ctx), M(ctx), GR(ctx), ACC(ctx);
+    ENB_TRY(pyramid_alloc(ctx, L, w, h, 3, ENB_F32, &R.p));
+    ENB_TRY(pyramid_alloc(ctx, L, w, h, 3, ENB_F32, &LP.p));
+    ENB_TRY(pyramid_alloc(ctx, L, w, h, 1, ENB_F32, &M.p));
+    auto build_lp = [&](int k) -> enb_status {
+        ENB_LAUNCH(ctx, launch_to_fixed(pixel_view(&images[k]), level_view(LP.p, 0), 0, ctx->stream));
+        ENB_TRY(gaussian_levels(ctx, 0, LP.p, &alpha));
+        ENB_TRY(laplacian_levels(ctx, 0, LP.p));
+        return ENB_OK;
+    };
+    for (int k = 0; k < K; ++k) {
+        ENB_TRY(build_lp(k));
+        const PlanarView m0 = level_view(M.p, 0);
+        ENB_CUDA(ctx, cudaMemcpy2DAsync(m0.p, m0.pitch * 4, mk + plane * k, fp * 4, (size_t)w * 4, h,
+                                        cudaMemcpyDeviceToDevice, ctx->stream));
+        ENB_TRY(gaussian_levels(ctx, 0, M.p, &alpha));
+        for (int l = 0; l < L; ++l) {
+            ENB_LAUNCH(ctx, launch_adj_merge(level_view(LP.p, l), level_view(M.p, l), level_view(R.p, l), k == 0,
+                                             ctx->stream));
+        }
+    }
+    ENB_TRY(collapse_levels(ctx, 0, R.p));
+    ENB_TRY(pyramid_alloc(ctx, L, w, h, 3, ENB_F32, &GR.p));
+    const PixelView tv = pixel_view(target);
+    float* outp = nullptr;
+    int64_t opitch = 0;
+    int ostride = 3;
+    if (out) {
+        const PixelView ov = pixel_view(out);
+        outp = (float*)out->data;
+        opitch = ov.pitch;
+        ostride = ov.stride;
+        if (ov.stride == 4) {
+            ENB_LAUNCH(ctx, launch_alpha_component(alpha, out->data, ov.pitch, ENB_F32, ctx->stream));
+        }
+    }
+    ENB_LAUNCH(ctx, launch_adj_loss(level_view(R.p, 0), (const float*)target->data, tv.pitch, tv.stride, outp, opitch,
+                                    ostride, level_view(GR.p, 0), dsc, ctx->stream));
+
+    // backward: collapse, merge and mask pyramids per exposure
+    for (int l = 0; l + 1 < L; ++l) {
+        ENB_LAUNCH(ctx, launch_expand_T(level_view(GR.p, l), level_view(GR.p, l + 1), ctx->stream));
+    }
+    ENB_TRY(pyramid_alloc(ctx, L, w, h, 1, ENB_F32, &ACC.p));
+    for (int k = 0; k < K; ++k) {
+        ENB_TRY(build_lp(k));
+        for (int l = L - 1; l >= 0; --l) {
+            const PlanarView nxt = l + 1 < L ? level_view(ACC.p, l + 1) : PlanarView{};
+            ENB_LAUNCH(ctx, launch_adj_mask_level(level_view(GR.p, l), level_view(LP.p, l), l + 1 < L ? &nxt : nullptr,
+                                                  level_view(ACC.p, l), ctx->stream));
+        }
+        const PlanarView a0 = level_view(ACC.p, 0);
+        ENB_CUDA(ctx, cudaMemcpy2DAsync(gm + plane * k, fp * 4, a0.p, a0.pitch * 4, (size_t)w * 4, h,
+                                        cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    ENB_LAUNCH(ctx, launch_adj_norm_bw(K, wk, logits ? ak : nullptr, gm, gw, ga, fp, plane, w, h, ctx->stream));
+    FloatWeightParams wp;
+    ENB_TRY(float_weight_params(ctx, prm, wp));
+    const float inv_width = (float)(1.0 / exposure_effective_width(prm->exp_function, prm->exp_width));
+    for (int k = 0; k < K; ++k) {
+        const PixelView iv = pixel_view(&images[k]);
+        ENB_LAUNCH(ctx, launch_adj_weights_bw(FloatPixelView{(const float*)iv.p, iv.pitch, iv.w, iv.h, 3, iv.stride},
+                                              gw + plane * k, fp, wp, inv_width, (float)prm->exp_width,
+                                              (float)prm->w_exposure, prm->contrast_window, dsc + 1, ctx->stream));
+    }
+    if (grad_logits) {
+        for (int k = 0; k < K; ++k) {
+            ENB_CUDA(ctx, cudaMemcpy2DAsync(grad_logits[k].data, grad_logits[k].pitch, ga + plane * k, fp * 4,
+                                            (size_t)w * 4, h, cudaMemcpyDeviceToDevice, ctx->stream));
+        }
+    }
+    double hs[6];
+    ENB_CUDA(ctx, cudaMemcpyAsync(hs, dsc, sizeof hs, cudaMemcpyDeviceToHost, ctx->stream));
+    ENB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    res->loss = hs[0] / (3.0 * (double)w * (double)h);
+    res->d_exp_optimum = hs[1];
+    res->d_exp_width = hs[2];
+    res->d_w_exposure = hs[3];
+    res->d_w_saturation = hs[4];
+    res->d_w_contrast = hs[5];
+    return ENB_OK;
+}
+
 }  // extern "C"

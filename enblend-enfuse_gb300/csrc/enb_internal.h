@@ -247,6 +247,20 @@ int batch_plan_steps(const BatchPlan* p);
 double batch_plan_pixels(const BatchPlan* p);
 cudaError_t batch_plan_launch(const BatchPlan* p, int step, cudaStream_t st);
 
+// adjoint of the float enfuse (enb_adjoint.cu)
+cudaError_t launch_adj_norm(int K, const float* w, const float* a, float* m, int64_t pitch, int64_t plane, int width,
+                            int height, cudaStream_t st);
+cudaError_t launch_adj_merge(const PlanarView& lp, const PlanarView& m, const PlanarView& r, int first, cudaStream_t st);
+cudaError_t launch_adj_loss(const PlanarView& c0, const float* tgt, int64_t tpitch, int tstride, float* out,
+                            int64_t opitch, int ostride, const PlanarView& g0, double* loss, cudaStream_t st);
+cudaError_t launch_expand_T(const PlanarView& fine, const PlanarView& coarse, cudaStream_t st);
+cudaError_t launch_adj_mask_level(const PlanarView& gr, const PlanarView& lp, const PlanarView* next,
+                                  const PlanarView& acc, cudaStream_t st);
+cudaError_t launch_adj_norm_bw(int K, const float* w, const float* a, const float* gm, float* gw, float* ga,
+                               int64_t pitch, int64_t plane, int width, int height, cudaStream_t st);
+cudaError_t launch_adj_weights_bw(const FloatPixelView& img, const float* gw, int64_t gpitch, const FloatWeightParams& wp,
+                                  float inv_width, float width, float w_exp, int cwin, double* d, cudaStream_t st);
+
 // float-image path (enb_float.cu): FP32 pyramid levels (dtype ENB_F32)
 cudaError_t launch_f_to_pyramid(const FloatPixelView& s, const PlanarView& d, cudaStream_t st);
 cudaError_t launch_f_from_pyramid(const PlanarView& s, const BytePlane& a, float* dst, int64_t dpitch, int dstride,

@@ -67,6 +67,12 @@ class EnbFuseOptions(ctypes.Structure):
                 ("graph", ctypes.c_int32)]
 
 
+class EnbFuseGradResult(ctypes.Structure):
+    _fields_ = [("loss", ctypes.c_double), ("d_exp_optimum", ctypes.c_double), ("d_exp_width", ctypes.c_double),
+                ("d_w_exposure", ctypes.c_double), ("d_w_saturation", ctypes.c_double),
+                ("d_w_contrast", ctypes.c_double)]
+
+
 class EnbStack(ctypes.Structure):
     _fields_ = [("K", ctypes.c_int32), ("images", ctypes.POINTER(EnbImage)), ("alphas", ctypes.POINTER(EnbImage)),
                 ("out", ctypes.POINTER(EnbImage)), ("out_alpha", ctypes.POINTER(EnbImage))]
@@ -113,6 +119,8 @@ _SIGNATURES = {
     "enb_enfuse_mask": (ctypes.c_int, [ctypes.c_void_p, _P(EnbEnfuseParams), _IMG, _IMG, _IMG]),
     "enb_enfuse": (ctypes.c_int, [ctypes.c_void_p, _P(EnbEnfuseParams), ctypes.c_int, _IMG, _IMG, _IMG, _IMG,
                                   _IMG, _P(EnbFuseOptions)]),
+    "enb_fuse_grad": (ctypes.c_int, [ctypes.c_void_p, _P(EnbEnfuseParams), ctypes.c_int, _IMG, _IMG, _IMG, _IMG,
+                                      _IMG, _P(EnbFuseGradResult), _P(EnbFuseOptions)]),
     "enb_fuse_stacks": (ctypes.c_int, [ctypes.c_void_p, _P(EnbEnfuseParams), ctypes.c_int, _P(EnbStack),
                                         _P(EnbFuseOptions)]),
     "enb_enblend": (ctypes.c_int, [ctypes.c_void_p, _IMG, _IMG, _IMG, _IMG, _IMG, _IMG, _IMG,
@@ -466,6 +474,22 @@ class Context:
         self._check(self.lib.enb_fuse_stacks(self.handle, ctypes.byref(p), len(stacks), descs, ctypes.byref(o)))
         del keep
         return outs
+
+    def fuse_grad(self, images, target, params: Optional[EnbEnfuseParams] = None, logits=None, out=None,
+                  grad_logits=None, levels: int = 0) -> dict:
+        """Loss of the float enfuse against `target` and its gradients (enb_fuse_grad).  images: K (H, W, 3)
+        float32 device tensors; logits / grad_logits: K (H, W) float32 device tensors or None."""
+        K = len(images)
+        imgs = (EnbImage * K)(*[pixel_image(x) for x in images])
+        lg = (EnbImage * K)(*[plane_image(a) for a in logits]) if logits is not None else None
+        gl = (EnbImage * K)(*[plane_image(a) for a in grad_logits]) if grad_logits is not None else None
+        p = params if params is not None else enfuse_params(float_range=1.0)
+        o = self._options(levels, False, False, "hash", 0, False, None)
+        r = EnbFuseGradResult()
+        self._check(self.lib.enb_fuse_grad(self.handle, ctypes.byref(p), K, imgs, lg, ctypes.byref(pixel_image(target)),
+                                           ctypes.byref(pixel_image(out)) if out is not None else None, gl,
+                                           ctypes.byref(r), ctypes.byref(o)))
+        return {f: getattr(r, f) for f, _ in EnbFuseGradResult._fields_}
 
     def enblend(self, white, black, mask, white_alpha=None, black_alpha=None, out=None, out_alpha=None,
                 levels: int = 0, wrap: bool = False, dither: str = "hash", seed: int = 0x5eed, level0=None,

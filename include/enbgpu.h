@@ -308,6 +308,31 @@ typedef struct {
 enb_status enb_fuse_stacks(enb_ctx* ctx, const enb_enfuse_params* params, int n_stacks, const enb_stack* stacks,
                            const enb_fuse_options* opt);
 
+/* ---- adjoint (no counterpart in the reference) --------------------------- */
+/* Loss and gradients of the float enfuse against a target image. */
+typedef struct {
+    double loss;            /* mean over pixels and channels of (out - target)^2 */
+    double d_exp_optimum;   /* dL/d exp_optimum */
+    double d_exp_width;     /* dL/d exp_width */
+    double d_w_exposure;    /* dL/d w_exposure */
+    double d_w_saturation;  /* dL/d w_saturation */
+    double d_w_contrast;    /* dL/d w_contrast */
+} enb_fuse_grad_result;
+
+/* The float enfuse of K opaque RGB images (src/enfuse.h:1217-1617 with
+ * continuous soft masks: each weight w_k, from params, is scaled by
+ * exp(logit_k), normalised over the K exposures, and used as a mask without
+ * its 9.15 quantisation), the loss against `target`, and its gradients:
+ * the scalars in `res` and, when grad_logits is given, dL/d logit_k per
+ * pixel.  logits: K F32 planes or NULL (all 0).  out: optional F32 image
+ * receiving the forward result.  Entropy weights, hard masks and wrap-around
+ * are not differentiated (ENB_ERR_UNSUPPORTED).  The backward rebuilds each
+ * exposure's Laplacian pyramid instead of keeping K of them, so the memory
+ * held is one pyramid per kind whatever K.  Device buffers; synchronous. */
+enb_status enb_fuse_grad(enb_ctx* ctx, const enb_enfuse_params* params, int K, const enb_image* images,
+                         const enb_image* logits, const enb_image* target, const enb_image* out,
+                         const enb_image* grad_logits, enb_fuse_grad_result* res, const enb_fuse_options* opt);
+
 #ifdef __cplusplus
 }
 #endif
