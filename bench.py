@@ -17,6 +17,8 @@ input pixels blended per second (2 x 4096 x 3072 = 25.17 Mpx per step).
   cpu_baseline  the CPU oracle (a port of the reference's algorithm: serial
          pyramids, OpenMP pointwise steps) on a quarter of the rows
 
+  adjoint  one step of the differentiable fuse (8 x 2048x2048 FP32):
+         forward, loss and all gradients through enb_fuse_grad
   batched_fuse  the batched uneven-stack workload (64 FP32 stacks of
          uneven sizes and exposure counts): enb_fuse_stacks replayed as one
          CUDA graph against the plain per-stack path on the same GPU
@@ -66,6 +68,7 @@ def parse_args():
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the batched uneven-stack measurement (batched_fuse object)")
     ap.add_argument("--batched-stacks", type=int, default=64)
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-fuse step (adjoint object)")
     ap.add_argument("--plain", action="store_true",
                     help="with --profile-only: the reference's pass structure instead of the fused passes")
     return ap.parse_args()
@@ -278,6 +281,44 @@ def batched_fuse(ctx, stream, n_stacks: int, reps: int = 3) -> dict:
     }
 
 
+def adjoint_step(ctx, stream, reps: int = 3) -> dict:
+    """The differentiable fuse: 8 exposures of 2048x2048 FP32 RGB (EV -3.5..+3.5
+    in 1-stop steps), loss = mean squared difference to the scene's tone-mapped
+    radiance (radiance / (1 + radiance))^(1/2.2); one step = the forward fuse,
+    the loss and all gradients (exposure optimum and width, exposure /
+    saturation / contrast coefficients, a per-exposure logit map) through
+    enb_fuse_grad."""
+    import torch
+    import enbgpu
+    from enbgpu import synthetic
+    h = w = 2048
+    lr = synthetic.log_radiance_torch(h, w, 8.0, seed=5)
+    imgs = [synthetic.expose_torch(lr, ev) for ev in np.arange(-3.5, 3.6, 1.0)]
+    rad = torch.exp2(lr)
+    target = ((rad / (1.0 + rad)) ** (1.0 / 2.2)).float().contiguous()
+    del lr, rad
+    logits = [torch.zeros((h, w), device="cuda") for _ in imgs]
+    grads = [torch.zeros_like(x) for x in logits]
+    prm = enbgpu.enfuse_params(exposure_optimum=0.5, exposure_width=0.2, saturation_weight=0.2, contrast_weight=0.5,
+                               contrast_window_size=5, float_range=1.0)
+    for _ in range(2):
+        r = ctx.fuse_grad(imgs, target, params=prm, logits=logits, grad_logits=grads)
+    torch.cuda.synchronize()
+    t0 = time.time()
+    for _ in range(reps):
+        r = ctx.fuse_grad(imgs, target, params=prm, logits=logits, grad_logits=grads)
+    ms = (time.time() - t0) / reps * 1e3
+    ctx.profile(True)
+    ctx.fuse_grad(imgs, target, params=prm, logits=logits, grad_logits=grads)
+    rep = ctx.profile_report()
+    ctx.profile(False)
+    return {"workload": "8 x 2048x2048 FP32 RGB, EV -3.5..+3.5, weights exposure 1.0 / saturation 0.2 / "
+                        "contrast 0.5 (5x5), per-exposure logit maps", "ms_per_step": ms,
+            "what": "forward + loss + all gradients (enb_fuse_grad, synchronous, host clock)",
+            "loss": r["loss"], "units": 8 * h * w / 1e6,
+            "kernels_ms": {k: round(v["ms"], 3) for k, v in sorted(rep.items(), key=lambda kv: -kv[1]["ms"])}}
+
+
 def run_ours(args) -> None:
     import torch
     import enbgpu
@@ -418,6 +459,8 @@ def run_ours(args) -> None:
     if rank == 0 and ws == 1 and not args.no_batched:
         del dw, db, dm, out, oa
         line["batched_fuse"] = batched_fuse(ctx, stream, args.batched_stacks)
+    if rank == 0 and ws == 1 and not args.no_adjoint:
+        line["adjoint"] = adjoint_step(ctx, stream)
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()

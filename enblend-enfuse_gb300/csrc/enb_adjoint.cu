@@ -269,21 +269,30 @@ __device__ __forceinline__ float exposure_dfdz(int fn, float z)
 }
 
 // Per pixel of exposure k: dL/dw_k times the partial derivatives of w_k,
-// summed into d[0..4] = d/d(optimum, width, W_exp, W_sat, W_con).
-__global__ void __launch_bounds__(256) k_adj_weights_bw(const float* __restrict__ img, int64_t ipitch, int istride,
-                                                        int w, int h, const float* __restrict__ gw, int64_t gpitch,
-                                                        FloatWeightParams wp, float inv_width, float width,
-                                                        float w_exp, int cwin, double* d)
+// summed into d[0..4] = d/d(optimum, width, W_exp, W_sat, W_con).  A 16x16
+// tile of the image (with the contrast window's halo) is staged in shared
+// memory as the forward weight kernel stages it, and sigma is recomputed
+// from it with the forward's arithmetic.
+template <int CW>
+__global__ void __launch_bounds__(256) k_adj_weights_bw(FloatPixelView img, const float* __restrict__ gw,
+                                                        int64_t gpitch, FloatWeightParams wp, float inv_width,
+                                                        float width, float w_exp, double* d)
 {
+    extern __shared__ __align__(16) unsigned char asmem[];
     __shared__ double part[5][8];
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y;
+    const int halo = wp.contrast_window / 2;
+    FloatWeightParams tp = wp;
+    tp.repeat_slots = 0;
+    const FTile t = ftile_carve(asmem, 16 + 2 * halo, 0);
+    ftile_load(t, tp, img.p, img.pitch, img.stride, img.w, img.h, 3, nullptr, 0, blockIdx.x * 16 - halo,
+               blockIdx.y * 16 - halo);
+    const int lx = threadIdx.x % 16, ly = threadIdx.x / 16;
+    const int x = blockIdx.x * 16 + lx, y = blockIdx.y * 16 + ly;
     double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-    if (x < w) {
+    if (x < img.w && y < img.h) {
+        const int ci = (ly + halo) * t.TW + (lx + halo);
         const float g = gw[(int64_t)y * gpitch + x];
-        const float* px = img + (int64_t)y * ipitch + (int64_t)x * istride;
-        const float r = px[0], gg = px[1], b = px[2];
-        const float gray = gray_of_f(wp, r, gg, b);
+        const float gray = t.gray[ci];
         // exposure: z = (y - opt) / width'; dz/dopt = -1/width', dz/dwidth = -z/width
         const float yv = __fdiv_rn(gray, wp.range);
         const float z = (yv - (wp.opt_hi + wp.opt_lo)) * inv_width;
@@ -292,36 +301,19 @@ __global__ void __launch_bounds__(256) k_adj_weights_bw(const float* __restrict_
         s[1] = (double)g * w_exp * df * (-z / width);
         s[2] = (double)g * exposure_f(wp, gray);
         // saturation (max_value 1.0)
+        const int TT = t.TW * t.TW;
+        const float r = t.raw[ci], gg = t.raw[TT + ci], b = t.raw[2 * TT + ci];
         const float mx = fmaxf(r, fmaxf(gg, b)), mn = fminf(r, fminf(gg, b));
         float sat = 0.0f;
         if (mx != mn) {
             const float sum = mx + mn, diff = mx - mn;
-            sat = diff / (sum <= 1.0f ? sum : (1.0f - mx) + (1.0f - mn));
+            sat = __fdiv_rn(diff, sum <= 1.0f ? sum : (1.0f - mx) + (1.0f - mn));
         }
         s[3] = (double)g * sat;
-        // contrast: the sample standard deviation of the window (border strip 0)
-        const int hb = cwin / 2;
+        // contrast: the window's sample standard deviation (border strip 0)
         float sd = 0.0f;
-        if (x >= hb && x < w - hb && y >= hb && y < h - hb) {
-            float sum = 0.0f;
-            const int n = cwin * cwin;
-            for (int dy = -hb; dy <= hb; ++dy) {
-                for (int dx = -hb; dx <= hb; ++dx) {
-                    const float* q = img + (int64_t)(y + dy) * ipitch + (int64_t)(x + dx) * istride;
-                    sum += gray_of_f(wp, q[0], q[1], q[2]);
-                }
-            }
-            const float mean = sum / (float)n;
-            float s1 = 0.0f, s2 = 0.0f;
-            for (int dy = -hb; dy <= hb; ++dy) {
-                for (int dx = -hb; dx <= hb; ++dx) {
-                    const float* q = img + (int64_t)(y + dy) * ipitch + (int64_t)(x + dx) * istride;
-                    const float dd = gray_of_f(wp, q[0], q[1], q[2]) - mean;
-                    s1 += dd;
-                    s2 = fmaf(dd, dd, s2);
-                }
-            }
-            sd = sqrtf(fmaxf((s2 - s1 * s1 / (float)n) / (float)(n - 1), 0.0f));
+        if (x >= halo && x < img.w - halo && y >= halo && y < img.h - halo) {
+            sd = window_stddev<CW>(t, ci, halo);
         }
         s[4] = (double)g * sd;
     }
@@ -337,11 +329,11 @@ __global__ void __launch_bounds__(256) k_adj_weights_bw(const float* __restrict_
     }
     __syncthreads();
     if (threadIdx.x < 5) {
-        double t = 0.0;
+        double tot = 0.0;
         for (int j = 0; j < (int)(blockDim.x >> 5); ++j) {
-            t += part[threadIdx.x][j];
+            tot += part[threadIdx.x][j];
         }
-        atomicAdd(&d[threadIdx.x], t);
+        atomicAdd(&d[threadIdx.x], tot);
     }
 }
 
@@ -404,8 +396,19 @@ cudaError_t launch_adj_weights_bw(const FloatPixelView& img, const float* gw, in
                                   float inv_width, float width, float w_exp, int cwin, double* d, cudaStream_t st)
 {
     note_launch("adj_weights_bw", npix(img.w, img.h) * (img.stride * 4.0 + 4.0));
-    k_adj_weights_bw<<<row_grid(img.w, img.h), 256, 0, st>>>(img.p, img.pitch, img.stride, img.w, img.h, gw, gpitch, wp,
-                                                             inv_width, width, w_exp, cwin, d);
+    FloatWeightParams p = wp;
+    p.contrast_window = cwin;
+    const int TW = 16 + 2 * (cwin / 2);
+    const size_t smem = ftile_bytes(TW, 0);
+    const dim3 g((unsigned)((img.w + 15) / 16), (unsigned)((img.h + 15) / 16));
+    if (cwin == 5) {
+        k_adj_weights_bw<5><<<g, 256, smem, st>>>(img, gw, gpitch, p, inv_width, width, w_exp, d);
+    } else {
+        if (smem > 48 * 1024) {
+            cudaFuncSetAttribute(k_adj_weights_bw<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        }
+        k_adj_weights_bw<0><<<g, 256, smem, st>>>(img, gw, gpitch, p, inv_width, width, w_exp, d);
+    }
     return cudaGetLastError();
 }
 
