@@ -116,7 +116,7 @@ struct LogPixelSource {
 constexpr int BWT = 16;
 
 template <int CW, int EW>
-__global__ void __launch_bounds__(256) k_batch_weights(const BatchStack* __restrict__ stacks,
+__global__ void __launch_bounds__(256, 4) k_batch_weights(const BatchStack* __restrict__ stacks,
                                                        const int4* __restrict__ jobs, FloatWeightParams wp,
                                                        WeightTables tab, int hard, int C)
 {
@@ -414,6 +414,138 @@ __global__ void __launch_bounds__(256, 4) k_batch_up(const BatchStack* __restric
     const int4 job = jobs[blockIdx.x];
     batch_up_tile<C, true>(stacks[job.x], l, job.y * ETW, job.z * ETH, wrap, inv_d,
                            reinterpret_cast<float(*)[ESH][ESW]>(upsmem));
+}
+
+// Level 0 with the exposures' input and mask tiles streamed through shared
+// memory: while exposure k is merged from one buffer, exposure k+1's 64x16
+// input pixels and mask values are copied into the other (cp.async), so the
+// loads of the next exposure are in flight during this one's arithmetic.
+constexpr int kUp0MaxStride = 4;
+
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all_but_one() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Issues the copies of exposure k's input tile and mask tile into buffer b.
+__device__ __forceinline__ void up0_issue(const BatchStack& s, int k, int X0, int Y0, int dw, int dh, float* img_tile,
+                                          int32_t* mask_tile)
+{
+    const int S = s.istride[k];
+    const int nx = min(ETW, dw - X0), ny = min(ETH, dh - Y0);
+    const float* src = s.img[k];
+    for (int e = threadIdx.x; e < ETH * ETW * S; e += blockDim.x) {
+        const int r = e / (ETW * S), c = e - r * (ETW * S);
+        if (r < ny && c < nx * S) {
+            cp_async4(&img_tile[r * ETW * kUp0MaxStride + c], &src[(int64_t)(Y0 + r) * s.ipitch[k] + (int64_t)X0 * S + c]);
+        }
+    }
+    const int32_t* m = m_level(s, k, 0);
+    for (int e = threadIdx.x; e < ETH * ETW; e += blockDim.x) {
+        const int r = e / ETW, c = e - r * ETW;
+        if (r < ny && c < nx) {
+            cp_async4(&mask_tile[r * ETW + c], &m[(int64_t)(Y0 + r) * s.pitch[0] + X0 + c]);
+        }
+    }
+}
+
+template <int C>
+__global__ void __launch_bounds__(256, 3) k_batch_up0(const BatchStack* __restrict__ stacks,
+                                                     const int4* __restrict__ jobs, int wrap, float inv_d)
+{
+    extern __shared__ __align__(16) float up0smem[];
+    const int4 job = jobs[blockIdx.x];
+    const BatchStack& s = stacks[job.x];
+    const int K = s.K;
+    const bool top = s.L == 1;
+    const int X0 = job.y * ETW, Y0 = job.z * ETH;
+    const int dw = s.lw[0], dh = s.lh[0];
+    const int sw = top ? 1 : s.lw[1], sh = top ? 1 : s.lh[1];
+    const int I0 = X0 >> 1, J0 = Y0 >> 1;
+    float(*ss)[ESH][ESW] = reinterpret_cast<float(*)[ESH][ESW]>(up0smem);
+    float* bufs = up0smem + (K + 1) * C * ESH * ESW;
+    float* img_tile[2] = {bufs, bufs + ETH * ETW * kUp0MaxStride};
+    int32_t* mask_tile[2] = {reinterpret_cast<int32_t*>(bufs + 2 * ETH * ETW * kUp0MaxStride),
+                             reinterpret_cast<int32_t*>(bufs + 2 * ETH * ETW * kUp0MaxStride) + ETH * ETW};
+    up0_issue(s, 0, X0, Y0, dw, dh, img_tile[0], mask_tile[0]);
+    cp_async_commit();
+    if (!top) {
+        const int64_t sp = s.pitch[1], splane = sp * sh;
+        for (int k = 0; k <= K; ++k) {
+            const float* src = k < K ? g_level(s, k, 1, C) : r_level(s, 1, C);
+            stage_window<C>(ss + k * C, src, sp, splane, sw, sh, I0, J0, wrap);
+        }
+    }
+    const int tid = threadIdx.x;
+    const int qx = tid % 32, qy = tid / 32;
+    const int i = I0 + qx, j = J0 + qy;
+    const int X = 2 * i, Y = 2 * j;
+    const bool active = X < dw && Y < dh;
+    float acc[4][C];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            acc[q][c] = 0.0f;
+        }
+    }
+    for (int k = 0; k < K; ++k) {
+        if (k + 1 < K) {
+            up0_issue(s, k + 1, X0, Y0, dw, dh, img_tile[(k + 1) & 1], mask_tile[(k + 1) & 1]);
+            cp_async_commit();
+            cp_async_wait_all_but_one();
+        } else {
+            cp_async_wait_all();
+        }
+        __syncthreads();
+        if (active) {
+            const float* it = img_tile[k & 1];
+            const int32_t* mt = mask_tile[k & 1];
+            const int S = s.istride[k];
+            float e[4][C];
+            if (!top) {
+                expand_quad_f<C>(ss + k * C, qx, qy, i, j, sw, sh, dw, wrap, e);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int xx = min(X + (q & 1), dw - 1) - X0, yy = min(Y + (q >> 1), dh - 1) - Y0;
+                const float coeff = (float)mt[yy * ETW + xx] * inv_d;
+#pragma unroll
+                for (int c = 0; c < C; ++c) {
+                    const float g = to_pyramid_value(it[yy * ETW * kUp0MaxStride + xx * S + c]);
+                    acc[q][c] += (g - (top ? 0.0f : e[q][c])) * coeff;
+                }
+            }
+        }
+        __syncthreads();  // the buffer is refilled two exposures on
+    }
+    if (!active) {
+        return;
+    }
+    float e[4][C];
+    if (!top) {
+        expand_quad_f<C>(ss + K * C, qx, qy, i, j, sw, sh, dw, wrap, e);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int XX = X + (q & 1), YY = Y + (q >> 1);
+        if (XX >= dw || YY >= dh) {
+            continue;
+        }
+        float* o = s.out + (int64_t)YY * s.opitch + (int64_t)XX * s.ostride;
+        const bool on = s.u[(int64_t)YY * s.pitch[0] + XX] != 0;
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            o[c] = on ? from_pyramid_value(acc[q][c] + (top ? 0.0f : e[q][c])) : 0.0f;
+        }
+        if (s.ostride == 4) {
+            o[3] = on ? 1.0f : 0.0f;  // AlphaTraits<float>::max()
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -786,6 +918,15 @@ static cudaError_t launch_step(const BatchPlan* p, const BatchPlan::Step& s, cud
     }
     default: {
         note_launch(s.level == 0 ? "batch_up0" : "batch_up", s.bytes);
+        if (s.level == 0) {
+            const size_t smem = up_smem_bytes(p->maxK, C) +
+                                2 * (size_t)ETH * ETW * (kUp0MaxStride * sizeof(float) + sizeof(int32_t));
+            if (smem > 48 * 1024) {
+                cudaFuncSetAttribute(k_batch_up0<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            }
+            k_batch_up0<C><<<(unsigned)s.njobs, 256, smem, st>>>(p->dstacks, jobs, p->wrap, inv_d);
+            break;
+        }
         const size_t smem = up_smem_bytes(p->maxK, C);
         if (smem > 48 * 1024) {
             cudaFuncSetAttribute(k_batch_up<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
