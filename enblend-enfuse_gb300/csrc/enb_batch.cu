@@ -9,11 +9,12 @@
 //
 //   weights   one CTA per 16x16 tile of a stack: the K weights of each pixel
 //             (enb_fweights.cuh), their sum, the soft (or hard) masks as
-//             level 0 of the mask pyramids, the union alpha;
+//             level 0 of the mask pyramids, the union alpha, and level 0 of
+//             the image pyramids;
 //   down l    one CTA per 64x16 destination tile of level l+1 of one
 //             exposure's image or mask pyramid (reduce with alpha); level 0
-//             of an image is read from the input with the log mapping applied
-//             on the fly, so level 0 is never stored;
+//             of each image pyramid (the log mapping) is written by the
+//             weights kernel, which reads the input anyway;
 //   coarse    a persistent kernel: each CTA takes stacks from a device work
 //             queue and runs all levels below ~64x64 of that stack (reduce
 //             down, then merge and collapse up) inside the one CTA;
@@ -62,6 +63,7 @@ struct BatchStack {
     float* g;     // K * 3 * s1 (C planes used)
     uint8_t* a;   // K * s1
     float* r;     // 3 * s1
+    float* g0;    // K * 3 * s0 (level 0 of the image pyramids, written by the weights kernel)
     int64_t s0, s1;
     int64_t off0[kMaxLevels], off1[kMaxLevels];
     int pitch[kMaxLevels], lw[kMaxLevels], lh[kMaxLevels];
@@ -85,23 +87,27 @@ __device__ __forceinline__ float* r_level(const BatchStack& s, int l, int C)
 {
     return s.r + (int64_t)C * s.off1[l];
 }
+// Level 0 of exposure k's image pyramid (planes of pitch[0] * h).
+__device__ __forceinline__ float* g0_level(const BatchStack& s, int k, int C)
+{
+    return s.g0 + (int64_t)k * C * s.s0;
+}
 
-// Level 0 of an exposure's image pyramid read straight from the input: the
-// log mapping (ConvertScalarToPyramidFunctor) applied on load.
+// Level 0 of an exposure's image pyramid (planar floats) with the input's
+// alpha plane, or opaque when there is none.
 template <int C>
-struct LogPixelSource {
+struct Level0Source {
     const float* p;
-    int64_t pitch;
-    int stride;
+    int64_t pitch, plane;
     const uint8_t* a;  // nullptr: opaque
     int64_t apitch;
     template <typename AC>
     __device__ __forceinline__ void load(int gy, int gx, AC (&v)[C], int& al) const
     {
-        const float* px = p + (int64_t)gy * pitch + (int64_t)gx * stride;
+        const int64_t o = (int64_t)gy * pitch + gx;
 #pragma unroll
         for (int c = 0; c < C; ++c) {
-            v[c] = to_pyramid_value(__ldg(&px[c]));
+            v[c] = __ldg(&p[c * plane + o]);
         }
         al = a ? (__ldg(&a[(int64_t)gy * apitch + gx]) != 0) : 1;
     }
@@ -137,6 +143,14 @@ __global__ void __launch_bounds__(256, 4) k_batch_weights(const BatchStack* __re
                    job.y * BWT - halo, job.z * BWT - halo);
         wk[k] = inside ? f_pixel_weight<CW, EW>(t, wp, tab, ci, x, y, s.w, s.h, C) : 0.0f;
         ua |= t.a[ci];
+        if (inside) {
+            // level 0 of the exposure's image pyramid: the log mapping, once
+            float* g0 = g0_level(s, k, C);
+            const int TT = t.TW * t.TW;
+            for (int c = 0; c < C; ++c) {
+                g0[(int64_t)c * s.pitch[0] * s.h + (int64_t)y * s.pitch[0] + x] = to_pyramid_value(t.raw[c * TT + ci]);
+            }
+        }
         __syncthreads();  // the next exposure's load overwrites the tile
     }
     if (!inside) {
@@ -196,9 +210,10 @@ __device__ __forceinline__ void batch_reduce_tile(const BatchStack& s, int kind,
         const int64_t dplane = (int64_t)s.pitch[l + 1] * dh;
         float(*V)[RDH][RVP] = reinterpret_cast<float(*)[RDH][RVP]>(smem);
         if (l == 0) {
-            using Src = LogPixelSource<C>;
-            const ReduceJob<Src, float> job{Src{s.img[k], s.ipitch[k], s.istride[k], s.alpha[k], s.apitch[k]}, dst,
-                                            s.pitch[l + 1], dplane, a_level(s, k, l + 1), s.pitch[l + 1]};
+            using Src = Level0Source<C>;
+            const ReduceJob<Src, float> job{
+                Src{g0_level(s, k, C), s.pitch[0], (int64_t)s.pitch[0] * sh, s.alpha[k], s.apitch[k]}, dst,
+                s.pitch[l + 1], dplane, a_level(s, k, l + 1), s.pitch[l + 1]};
             reduce_tile<Src, float, C, true, float>(job, X0, Y0, sw, sh, dw, dh, wrap, V);
         } else {
             using Src = PlanarSource<float, C, true, NC>;
@@ -301,17 +316,26 @@ template <int C>
 __device__ __forceinline__ void stage_window(float (*ss)[ESH][ESW], const float* src, int64_t pitch, int64_t plane,
                                              int sw, int sh, int I0, int J0, int wrap)
 {
-    for (int k = threadIdx.x; k < ESH * ESW; k += blockDim.x) {
-        const int r = k / ESW, c = k - r * ESW;
+    // element k = r * ESW + c, walked with a stride of blockDim.x
+    int r = (int)threadIdx.x / ESW, c = (int)threadIdx.x - r * ESW;
+    const int dr = (int)blockDim.x / ESW, dc = (int)blockDim.x - dr * ESW;
+    for (; r < ESH;) {
         const int jj = J0 - 1 + r;
         int ii = I0 - 1 + c;
         if (wrap) {
             ii = imod(ii, sw);
         }
         const bool in = jj >= 0 && jj < sh && ii >= 0 && ii < sw;
+        const int64_t o = (int64_t)jj * pitch + ii;
 #pragma unroll
         for (int ch = 0; ch < C; ++ch) {
-            ss[ch][r][c] = in ? src[(int64_t)ch * plane + (int64_t)jj * pitch + ii] : 0.0f;
+            ss[ch][r][c] = in ? src[(int64_t)ch * plane + o] : 0.0f;
+        }
+        c += dc;
+        r += dr;
+        if (c >= ESW) {
+            c -= ESW;
+            ++r;
         }
     }
 }
@@ -363,8 +387,7 @@ __device__ __forceinline__ void batch_up_tile(const BatchStack& s, int l, int X0
                 const int XX = min(X + (q & 1), dw - 1), YY = min(Y + (q >> 1), dh - 1);
                 coeff[q] = (float)ld_src<NC>(&mk[(int64_t)YY * dp + XX]) * inv_d;
                 if (l == 0) {
-                    g[q] = to_pyramid_value(
-                        __ldg(&s.img[k][(int64_t)YY * s.ipitch[k] + (int64_t)XX * s.istride[k] + c]));
+                    g[q] = __ldg(&g0_level(s, k, C)[(int64_t)c * gplane + (int64_t)YY * dp + XX]);
                 } else {
                     g[q] = ld_src<NC>(&gk[(int64_t)YY * dp + XX]);
                 }
@@ -416,12 +439,10 @@ __global__ void __launch_bounds__(256, 4) k_batch_up(const BatchStack* __restric
                            reinterpret_cast<float(*)[ESH][ESW]>(upsmem));
 }
 
-// Level 0 with the exposures' input and mask tiles streamed through shared
+// Level 0 with the exposures' level-0 and mask tiles streamed through shared
 // memory: while exposure k is merged from one buffer, exposure k+1's 64x16
-// input pixels and mask values are copied into the other (cp.async), so the
+// pyramid values and mask values are copied into the other (cp.async), so the
 // loads of the next exposure are in flight during this one's arithmetic.
-constexpr int kUp0MaxStride = 4;
-
 __device__ __forceinline__ void cp_async4(void* smem, const void* gmem)
 {
     const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
@@ -431,24 +452,25 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait_all_but_one() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
-// Issues the copies of exposure k's input tile and mask tile into buffer b.
-__device__ __forceinline__ void up0_issue(const BatchStack& s, int k, int X0, int Y0, int dw, int dh, float* img_tile,
+// Issues the copies of exposure k's level-0 tile (C planes) and mask tile.
+template <int C>
+__device__ __forceinline__ void up0_issue(const BatchStack& s, int k, int X0, int Y0, int dw, int dh, float* g_tile,
                                           int32_t* mask_tile)
 {
-    const int S = s.istride[k];
     const int nx = min(ETW, dw - X0), ny = min(ETH, dh - Y0);
-    const float* src = s.img[k];
-    for (int e = threadIdx.x; e < ETH * ETW * S; e += blockDim.x) {
-        const int r = e / (ETW * S), c = e - r * (ETW * S);
-        if (r < ny && c < nx * S) {
-            cp_async4(&img_tile[r * ETW * kUp0MaxStride + c], &src[(int64_t)(Y0 + r) * s.ipitch[k] + (int64_t)X0 * S + c]);
+    const float* g0 = g0_level(s, k, C);
+    const int64_t plane = (int64_t)s.pitch[0] * dh;
+    for (int e = threadIdx.x; e < C * ETH * ETW; e += blockDim.x) {
+        const int c = e / (ETH * ETW), rc = e - c * (ETH * ETW), r = rc / ETW, x = rc - r * ETW;
+        if (r < ny && x < nx) {
+            cp_async4(&g_tile[e], &g0[c * plane + (int64_t)(Y0 + r) * s.pitch[0] + X0 + x]);
         }
     }
     const int32_t* m = m_level(s, k, 0);
     for (int e = threadIdx.x; e < ETH * ETW; e += blockDim.x) {
-        const int r = e / ETW, c = e - r * ETW;
-        if (r < ny && c < nx) {
-            cp_async4(&mask_tile[r * ETW + c], &m[(int64_t)(Y0 + r) * s.pitch[0] + X0 + c]);
+        const int r = e / ETW, x = e - r * ETW;
+        if (r < ny && x < nx) {
+            cp_async4(&mask_tile[e], &m[(int64_t)(Y0 + r) * s.pitch[0] + X0 + x]);
         }
     }
 }
@@ -468,10 +490,10 @@ __global__ void __launch_bounds__(256, 3) k_batch_up0(const BatchStack* __restri
     const int I0 = X0 >> 1, J0 = Y0 >> 1;
     float(*ss)[ESH][ESW] = reinterpret_cast<float(*)[ESH][ESW]>(up0smem);
     float* bufs = up0smem + (K + 1) * C * ESH * ESW;
-    float* img_tile[2] = {bufs, bufs + ETH * ETW * kUp0MaxStride};
-    int32_t* mask_tile[2] = {reinterpret_cast<int32_t*>(bufs + 2 * ETH * ETW * kUp0MaxStride),
-                             reinterpret_cast<int32_t*>(bufs + 2 * ETH * ETW * kUp0MaxStride) + ETH * ETW};
-    up0_issue(s, 0, X0, Y0, dw, dh, img_tile[0], mask_tile[0]);
+    float* g_tile[2] = {bufs, bufs + C * ETH * ETW};
+    int32_t* mask_tile[2] = {reinterpret_cast<int32_t*>(bufs + 2 * C * ETH * ETW),
+                             reinterpret_cast<int32_t*>(bufs + 2 * C * ETH * ETW) + ETH * ETW};
+    up0_issue<C>(s, 0, X0, Y0, dw, dh, g_tile[0], mask_tile[0]);
     cp_async_commit();
     if (!top) {
         const int64_t sp = s.pitch[1], splane = sp * sh;
@@ -495,7 +517,7 @@ __global__ void __launch_bounds__(256, 3) k_batch_up0(const BatchStack* __restri
     }
     for (int k = 0; k < K; ++k) {
         if (k + 1 < K) {
-            up0_issue(s, k + 1, X0, Y0, dw, dh, img_tile[(k + 1) & 1], mask_tile[(k + 1) & 1]);
+            up0_issue<C>(s, k + 1, X0, Y0, dw, dh, g_tile[(k + 1) & 1], mask_tile[(k + 1) & 1]);
             cp_async_commit();
             cp_async_wait_all_but_one();
         } else {
@@ -503,9 +525,8 @@ __global__ void __launch_bounds__(256, 3) k_batch_up0(const BatchStack* __restri
         }
         __syncthreads();
         if (active) {
-            const float* it = img_tile[k & 1];
+            const float* gt = g_tile[k & 1];
             const int32_t* mt = mask_tile[k & 1];
-            const int S = s.istride[k];
             float e[4][C];
             if (!top) {
                 expand_quad_f<C>(ss + k * C, qx, qy, i, j, sw, sh, dw, wrap, e);
@@ -516,7 +537,7 @@ __global__ void __launch_bounds__(256, 3) k_batch_up0(const BatchStack* __restri
                 const float coeff = (float)mt[yy * ETW + xx] * inv_d;
 #pragma unroll
                 for (int c = 0; c < C; ++c) {
-                    const float g = to_pyramid_value(it[yy * ETW * kUp0MaxStride + xx * S + c]);
+                    const float g = gt[c * ETH * ETW + yy * ETW + xx];
                     acc[q][c] += (g - (top ? 0.0f : e[q][c])) * coeff;
                 }
             }
@@ -698,7 +719,7 @@ cudaError_t batch_plan_create(const std::vector<BatchStackHost>& hs, const Float
         level_geometry(s, coarse_pixels);
         base[i] = bytes;
         bytes += align((size_t)s.K * s.s0 * 4) + align((size_t)s.s0) + align((size_t)s.K * p->C * s.s1 * 4) +
-                 align((size_t)s.K * s.s1) + align((size_t)p->C * s.s1 * 4);
+                 align((size_t)s.K * s.s1) + align((size_t)p->C * s.s1 * 4) + align((size_t)s.K * p->C * s.s0 * 4);
         p->pixels += (double)h.K * h.w * h.h;
         p->maxK = std::max(p->maxK, h.K);
     }
@@ -833,6 +854,8 @@ cudaError_t batch_plan_create(const std::vector<BatchStackHost>& hs, const Float
         s.a = (uint8_t*)q;
         q += align((size_t)s.K * s.s1);
         s.r = (float*)q;
+        q += align((size_t)p->C * s.s1 * 4);
+        s.g0 = (float*)q;
     }
     p->dstacks = (BatchStack*)(w + o_st);
     p->djobs = (int4*)(w + o_jobs);
@@ -919,8 +942,7 @@ static cudaError_t launch_step(const BatchPlan* p, const BatchPlan::Step& s, cud
     default: {
         note_launch(s.level == 0 ? "batch_up0" : "batch_up", s.bytes);
         if (s.level == 0) {
-            const size_t smem = up_smem_bytes(p->maxK, C) +
-                                2 * (size_t)ETH * ETW * (kUp0MaxStride * sizeof(float) + sizeof(int32_t));
+            const size_t smem = up_smem_bytes(p->maxK, C) + 2 * (size_t)ETH * ETW * (C * sizeof(float) + sizeof(int32_t));
             if (smem > 48 * 1024) {
                 cudaFuncSetAttribute(k_batch_up0<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             }

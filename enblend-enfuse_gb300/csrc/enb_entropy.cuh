@@ -155,8 +155,11 @@ namespace enb {
 
 // ---- repeated-sample marks of a float tile ----------------------------------
 //
-// Float samples rarely repeat, and a window whose samples are all distinct
-// has H = log(n) / log(n) computed from n alone.  Every opaque sample of the
+// Float samples rarely repeat except at the clip values 0 and 1.  The
+// samples equal to 0.0 or 1.0 are counted per window (two bins whose sizes
+// are those counts); all other opaque samples go through the repeat marks
+// below, and a window without marks has only singletons besides the two
+// clip bins, so its H follows from three counts.  Every opaque sample of the
 // tile (halo included) goes into a shared-memory hash table per channel; a
 // second insertion of an equal key marks the slot.  meta[p] then carries bit
 // c when sample c of pixel p occurs more than once in the tile, and bit 7
@@ -178,24 +181,29 @@ __device__ __forceinline__ void mark_repeats(const float* raw, int plane, const 
         flags[i] = 0;
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < npx * C; i += blockDim.x) {
-        const int c = i / npx, p = i - c * npx;
+    for (int p = threadIdx.x; p < npx; p += blockDim.x) {
         if (!a[p]) {
             continue;
         }
-        const uint32_t k = key(raw[c * plane + p]);
-        uint32_t* t = table + c * slots;
-        uint32_t h = dup_hash(k, shift);
-        for (int probe = 0; probe < slots; ++probe) {
-            const uint32_t old = atomicCAS(&t[h], kEntropyPad, k);
-            if (old == kEntropyPad) {
-                break;
+        for (int c = 0; c < C; ++c) {
+            const float fv = raw[c * plane + p];
+            if (fv == 0.0f || fv == 1.0f) {
+                continue;  // clip values are counted per window, not hashed
             }
-            if (old == k) {
-                flags[c * slots + h] = 1;
-                break;
+            const uint32_t k = key(fv);
+            uint32_t* t = table + c * slots;
+            uint32_t h = dup_hash(k, shift);
+            for (int probe = 0; probe < slots; ++probe) {
+                const uint32_t old = atomicCAS(&t[h], kEntropyPad, k);
+                if (old == kEntropyPad) {
+                    break;
+                }
+                if (old == k) {
+                    flags[c * slots + h] = 1;
+                    break;
+                }
+                h = (h + 1) & (uint32_t)(slots - 1);
             }
-            h = (h + 1) & (uint32_t)(slots - 1);
         }
     }
     __syncthreads();
@@ -204,7 +212,11 @@ __device__ __forceinline__ void mark_repeats(const float* raw, int plane, const 
         if (a[p]) {
             m = 0x80;
             for (int c = 0; c < C; ++c) {
-                const uint32_t k = key(raw[c * plane + p]);
+                const float fv = raw[c * plane + p];
+                if (fv == 0.0f || fv == 1.0f) {
+                    continue;
+                }
+                const uint32_t k = key(fv);
                 const uint32_t* t = table + c * slots;
                 uint32_t h = dup_hash(k, shift);
                 for (int probe = 0; probe < slots && t[h] != k; ++probe) {
@@ -233,6 +245,55 @@ __device__ __forceinline__ void window_marks(const uint8_t* meta, int TW, int ci
             marks |= m;
         }
     }
+}
+
+// Per-pixel clip counters of a float tile: 5-bit fields, samples equal to 1.0
+// for channels 0..2 at bits 0, 5, 10 and equal to 0.0 at bits 15, 20, 25
+// (opaque pixels only); a window's sum keeps every field below 32.
+__device__ __forceinline__ uint32_t clip_counts(const float* rgb, int C)
+{
+    uint32_t m = 0;
+    for (int c = 0; c < C; ++c) {
+        m |= (rgb[c] == 1.0f ? 1u : 0u) << (5 * c);
+        m |= (rgb[c] == 0.0f ? 1u : 0u) << (15 + 5 * c);
+    }
+    return m;
+}
+
+// Opaque-tap count, OR of the repeat marks and sum of the clip counters of
+// the W x W window at ci.
+template <int W>
+__device__ __forceinline__ void window_counts(const uint8_t* meta, const uint32_t* cnt, int TW, int ci, int& n,
+                                              uint32_t& marks, uint32_t& clips)
+{
+    n = 0;
+    marks = 0;
+    clips = 0;
+#pragma unroll
+    for (int dy = 0; dy < W; ++dy) {
+#pragma unroll
+        for (int dx = 0; dx < W; ++dx) {
+            const int idx = ci + (dy - W / 2) * TW + (dx - W / 2);
+            const uint32_t m = meta[idx];
+            n += (int)(m >> 7);
+            marks |= m;
+            clips += cnt[idx];
+        }
+    }
+}
+
+// H of a window channel without repeat marks: n - m1 - m0 singletons and the
+// bins of the m1 samples equal to 1.0 and the m0 equal to 0.0 (the value the
+// sorting path computes for such a window).
+__device__ __forceinline__ float entropy_clip_bins(int n, int m1, int m0, const WeightTables& tab, int nmax)
+{
+    const int bins = n - m1 - m0 + (m1 > 0 ? 1 : 0) + (m0 > 0 ? 1 : 0);
+    if (n == 0 || bins <= 1) {
+        return 0.0f;
+    }
+    const long long* fx = tab.plogp_fx + (int64_t)n * (nmax + 1);
+    const long long acc = (long long)(n - m1 - m0) * fx[1] + (m1 > 0 ? fx[m1] : 0) + (m0 > 0 ? fx[m0] : 0);
+    return fminf(__fmul_rn(-(float)acc * 1.3877787807814457e-17f, tab.scale_logb[bins]), 1.0f);
 }
 
 // H of n all-distinct keys, the value entropy_window_float computes for them.

@@ -165,6 +165,7 @@ __device__ __forceinline__ uint32_t float_key(float f) { return __float_as_uint(
 struct FTile {
     float* gray;     // [TW*TW]
     float* raw;      // [3][TW*TW]
+    uint32_t* cnt;   // [TW*TW] clip counters (clip_counts)
     uint32_t* table; // [3][slots]
     uint8_t* a;      // [TW*TW]
     uint8_t* meta;   // [TW*TW]
@@ -174,7 +175,7 @@ struct FTile {
 
 __host__ __device__ inline size_t ftile_bytes(int TW, int slots)
 {
-    return (size_t)TW * TW * (4 * sizeof(float) + 2) + (size_t)slots * 3 * 5;
+    return (size_t)TW * TW * (5 * sizeof(float) + 2) + (size_t)slots * 3 * 5;
 }
 
 __device__ __forceinline__ FTile ftile_carve(unsigned char* smem, int TW, int slots)
@@ -184,7 +185,8 @@ __device__ __forceinline__ FTile ftile_carve(unsigned char* smem, int TW, int sl
     t.slots = slots;
     t.gray = reinterpret_cast<float*>(smem);
     t.raw = t.gray + TW * TW;
-    t.table = reinterpret_cast<uint32_t*>(t.raw + 3 * TW * TW);
+    t.cnt = reinterpret_cast<uint32_t*>(t.raw + 3 * TW * TW);
+    t.table = t.cnt + TW * TW;
     t.a = reinterpret_cast<uint8_t*>(t.table + 3 * slots);
     t.meta = t.a + TW * TW;
     t.flags = t.meta + TW * TW;
@@ -198,8 +200,10 @@ __device__ __forceinline__ void ftile_load(const FTile& t, const FloatWeightPara
                                            int x0, int y0)
 {
     const int TW = t.TW;
+    // tile pixel k = r * TW + c, walked with a stride of blockDim.x
+    const int dr = (int)blockDim.x / TW, dc = (int)blockDim.x - dr * TW;
+    int r = (int)threadIdx.x / TW, c = (int)threadIdx.x - r * TW;
     for (int k = threadIdx.x; k < TW * TW; k += blockDim.x) {
-        const int r = k / TW, c = k - r * TW;
         const int gx = x0 + c, gy = y0 + r;
         float rgb[3] = {0.0f, 0.0f, 0.0f};
         uint8_t a = 0;
@@ -212,8 +216,15 @@ __device__ __forceinline__ void ftile_load(const FTile& t, const FloatWeightPara
         }
         t.gray[k] = C == 1 ? rgb[0] : gray_of_f(wp, rgb[0], rgb[1], rgb[2]);
         t.a[k] = a;
+        t.cnt[k] = a ? clip_counts(rgb, C) : 0u;
         for (int ch = 0; ch < 3; ++ch) {
             t.raw[ch * TW * TW + k] = rgb[ch];
+        }
+        c += dc;
+        r += dr;
+        if (c >= TW) {
+            c -= TW;
+            ++r;
         }
     }
     __syncthreads();
@@ -266,18 +277,15 @@ __device__ __forceinline__ float window_stddev(const FTile& t, int ci, int bdyn)
 // 0: the runtime window wp.entropy_window through an insertion sort).
 template <int EW>
 __device__ __forceinline__ float window_entropy(const FTile& t, const FloatWeightParams& wp, const WeightTables& tab,
-                                                int ci, int ch, int nwin, uint32_t marks)
+                                                int ci, int ch, int nwin, uint32_t marks, uint32_t clips)
 {
     const float* raw = t.raw + ch * t.TW * t.TW;
     const int nmax = (EW > 0 ? EW * EW : wp.entropy_window * wp.entropy_window);
     if (EW > 0) {
-        float H;
         if (!(marks & (1u << ch))) {
-            return entropy_distinct(nwin, tab, nmax);  // all keys distinct
-        }
-        if (entropy_one_repeat<(EW > 0 ? EW : 3)>(raw, t.meta, t.TW, ci, 1u << ch, nwin, tab, nmax,
-                                                  [](float f) { return float_key(f); }, H)) {
-            return H;  // one repeated key (a clipped highlight)
+            // no repeated sample besides the clip values: three counts
+            return entropy_clip_bins(nwin, (int)((clips >> (5 * ch)) & 31u), (int)((clips >> (15 + 5 * ch)) & 31u),
+                                     tab, nmax);
         }
         return entropy_window_float<(EW > 0 ? EW : 3)>(raw, t.a, t.TW, ci, tab);
     }
@@ -343,14 +351,14 @@ __device__ __forceinline__ float f_pixel_weight(const FTile& t, const FloatWeigh
         float emin = 0.0f;
         if (x >= b && x < w - b && y >= b && y < h - b) {
             int nwin = 0;
-            uint32_t marks = 0xffu;
+            uint32_t marks = 0xffu, clips = 0;
             if (EW > 0 && t.slots) {
-                window_marks<(EW > 0 ? EW : 3)>(t.meta, t.TW, ci, nwin, marks);
+                window_counts<(EW > 0 ? EW : 3)>(t.meta, t.cnt, t.TW, ci, nwin, marks, clips);
             }
             emin = 3.402823466e38f;
             for (int ch = 0; ch < C; ++ch) {
                 // fromRealPromote<float>(H * max): the entropy image pixel
-                emin = fminf(emin, __fmul_rn(window_entropy<EW>(t, wp, tab, ci, ch, nwin, marks), wp.range));
+                emin = fminf(emin, __fmul_rn(window_entropy<EW>(t, wp, tab, ci, ch, nwin, marks, clips), wp.range));
             }
         }
         result = __fmul_rn(wp.w_entropy, emin) + result;

@@ -159,6 +159,9 @@ def test_enfuse_mask_f32(ctx, orc, float_range, projector):
     lr = synthetic.log_radiance(h, w, 8.0, seed=5)
     img = synthetic.expose(lr, -1.0, np.float32)
     img[10:20, 10:40] = 1.0  # clipped: repeated values in the entropy windows
+    img[30:36, 50:70] = 0.0  # and the dark clip value, with -0 among them
+    img[33, 55:60] = -0.0
+    img[40:44, 80:90, 1] = 0.375  # a repeated value that is no clip value
     alpha = _alpha(rng, h, w, "holes")
     fnames = ["gaussian", "lorentzian", "halfsine", "fullsine", "bisquare"]
     for i, fn in enumerate(fnames):
