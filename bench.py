@@ -69,6 +69,9 @@ def parse_args():
                     help="skip the batched uneven-stack measurement (batched_fuse object)")
     ap.add_argument("--batched-stacks", type=int, default=64)
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-fuse step (adjoint object)")
+    ap.add_argument("--profile-batched", action="store_true",
+                    help="run only a small batched fuse (4 stacks of 5 FP32 1024x768 exposures, every level above 0 "
+                         "in the coarse kernel, no graph): the case of the batched kernels' ncu capture")
     ap.add_argument("--plain", action="store_true",
                     help="with --profile-only: the reference's pass structure instead of the fused passes")
     return ap.parse_args()
@@ -468,8 +471,26 @@ def run_ours(args) -> None:
         torch.distributed.destroy_process_group()
 
 
+def profile_batched() -> None:
+    import torch
+    import enbgpu
+    from enbgpu import synthetic
+    ctx = enbgpu.Context(0)
+    specs = [(768, 1024, list(np.linspace(-4, 4, 5)), 100 + i) for i in range(4)]
+    stacks = synthetic.uneven_stacks_torch(specs)
+    prm = enbgpu.enfuse_params(saturation_weight=0.2, contrast_weight=0.5, entropy_weight=0.3,
+                               contrast_window_size=5, entropy_window_size=5, float_range=1.0)
+    outs = ctx.fuse_stacks(stacks, params=prm, graph=False, coarse_pixels=1 << 30)
+    torch.cuda.synchronize()
+    print("batched profile case ok", float(outs[0].mean()))
+    ctx.close()
+
+
 def main():
     args = parse_args()
+    if args.profile_batched:
+        profile_batched()
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
