@@ -284,8 +284,8 @@ __global__ void __launch_bounds__(256) k_adj_weights_bw(FloatPixelView img, cons
     FloatWeightParams tp = wp;
     tp.repeat_slots = 0;
     const FTile t = ftile_carve(asmem, 16 + 2 * halo, 0);
-    ftile_load(t, tp, img.p, img.pitch, img.stride, img.w, img.h, 3, nullptr, 0, blockIdx.x * 16 - halo,
-               blockIdx.y * 16 - halo);
+    const int opaque = ftile_load(t, tp, img.p, img.pitch, img.stride, img.w, img.h, 3, nullptr, 0,
+                                  blockIdx.x * 16 - halo, blockIdx.y * 16 - halo);
     const int lx = threadIdx.x % 16, ly = threadIdx.x / 16;
     const int x = blockIdx.x * 16 + lx, y = blockIdx.y * 16 + ly;
     double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(256) k_adj_weights_bw(FloatPixelView img, cons
         // contrast: the window's sample standard deviation (border strip 0)
         float sd = 0.0f;
         if (x >= halo && x < img.w - halo && y >= halo && y < img.h - halo) {
-            sd = window_stddev<CW>(t, ci, halo);
+            sd = window_stddev<CW>(t, ci, halo, opaque != 0);
         }
         s[4] = (double)g * sd;
     }

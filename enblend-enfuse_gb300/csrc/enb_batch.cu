@@ -131,17 +131,18 @@ __global__ void __launch_bounds__(256, 4) k_batch_weights(const BatchStack* __re
     const BatchStack& s = stacks[job.x];
     const int halo = fweight_halo(wp);
     const FTile t = ftile_carve(bsmem, BWT + 2 * halo, wp.repeat_slots);
+    float* wk = reinterpret_cast<float*>(bsmem + align16(ftile_bytes(t.TW, t.slots))) + threadIdx.x;  // [K][BWT * BWT]
     const int lx = threadIdx.x % BWT, ly = threadIdx.x / BWT;
     const int x = job.y * BWT + lx, y = job.z * BWT + ly;
     const bool inside = x < s.w && y < s.h;
     const int ci = (ly + halo) * t.TW + (lx + halo);
     const int K = s.K;
-    float wk[kBatchMaxK];
+    const int x0 = job.y * BWT - halo, y0 = job.z * BWT - halo;
     uint8_t ua = 0;
     for (int k = 0; k < K; ++k) {
-        ftile_load(t, wp, s.img[k], s.ipitch[k], s.istride[k], s.w, s.h, C, s.alpha[k], s.apitch[k],
-                   job.y * BWT - halo, job.z * BWT - halo);
-        wk[k] = inside ? f_pixel_weight<CW, EW>(t, wp, tab, ci, x, y, s.w, s.h, C) : 0.0f;
+        const int opaque =
+            ftile_load(t, wp, s.img[k], s.ipitch[k], s.istride[k], s.w, s.h, C, s.alpha[k], s.apitch[k], x0, y0);
+        wk[k * BWT * BWT] = inside ? f_pixel_weight<CW, EW>(t, wp, tab, ci, x, y, s.w, s.h, C, opaque != 0) : 0.0f;
         ua |= t.a[ci];
         if (inside) {
             // level 0 of the exposure's image pyramid: the log mapping, once
@@ -163,8 +164,8 @@ __global__ void __launch_bounds__(256, 4) k_batch_weights(const BatchStack* __re
         float mx = 0.0f;
         int mi = 0;
         for (int k = 0; k < K; ++k) {
-            if (wk[k] > mx) {
-                mx = wk[k];
+            if (wk[k * BWT * BWT] > mx) {
+                mx = wk[k * BWT * BWT];
                 mi = k;
             }
         }
@@ -176,11 +177,11 @@ __global__ void __launch_bounds__(256, 4) k_batch_weights(const BatchStack* __re
     } else {
         float norm = 0.0f;
         for (int k = 0; k < K; ++k) {
-            norm = __fadd_rn(wk[k], norm);
+            norm = __fadd_rn(wk[k * BWT * BWT], norm);
         }
         const float fallback = (float)(255 / K);
         for (int k = 0; k < K; ++k) {
-            const float m = norm > 0.0f ? __fdiv_rn(__fmul_rn(255.0f, wk[k]), norm) : fallback;
+            const float m = norm > 0.0f ? __fdiv_rn(__fmul_rn(255.0f, wk[k * BWT * BWT]), norm) : fallback;
             m_level(s, k, 0)[o] = mask_to_fixed<int32_t>(m, 15);
         }
     }
@@ -732,7 +733,8 @@ cudaError_t batch_plan_create(const std::vector<BatchStackHost>& hs, const Float
     const int halo = fweight_halo(wp);
     const int TW = BWT + 2 * halo;
     p->wp.repeat_slots = fweight_slots(wp, TW);
-    p->wsmem = ftile_bytes(TW, p->wp.repeat_slots);
+    // the tile, then the K weights of each output pixel
+    p->wsmem = align16(ftile_bytes(TW, p->wp.repeat_slots)) + (size_t)p->maxK * BWT * BWT * sizeof(float);
     double b = 0.0;
     add_step(0, 0, 0.0);
     for (int i = 0; i < p->nstacks; ++i) {

@@ -161,24 +161,122 @@ namespace enb {
 // below, and a window without marks has only singletons besides the two
 // clip bins, so its H follows from three counts.  Every opaque sample of the
 // tile (halo included) goes into a shared-memory hash table per channel; a
-// second insertion of an equal key marks the slot.  meta[p] then carries bit
-// c when sample c of pixel p occurs more than once in the tile, and bit 7
-// when p is opaque.  A window with no mark in channel c has all-distinct
-// keys in that channel (marks from matches elsewhere in the tile only send a
-// window down the exact sorting path, they never change a result).
+// second insertion of an equal key flags the slot.  A sample whose slot is
+// flagged occurs more than once in the tile and gets a repeat mark.  A
+// window with no mark in channel c has all-distinct keys in that channel
+// (marks from matches elsewhere in the tile only send a window down the
+// exact sorting path, they never change a result).
+//
+// Per-pixel counters (one 64-bit word per tile pixel, summed over a window):
+//   bits  0..14  samples equal to 1.0, channels 0..2 (5 bits each)
+//   bits 15..29  samples equal to 0.0
+//   bits 30..44  repeat marks
+//   bits 45..49  opaque pixels
+// A 5x5 window's sum keeps every field below 32.
+constexpr int kCntMark = 30, kCntOpaque = 45;
+
+// Histogram key of a float sample: its bit pattern, -0 folded into +0.
+__device__ __forceinline__ uint32_t float_key(float f) { return __float_as_uint(f == 0.0f ? 0.0f : f); }
+
+// Clip-value counters of one opaque pixel (bits 0..29 of its word).
+__device__ __forceinline__ uint32_t clip_counts(const float* rgb, int C)
+{
+    uint32_t m = 0;
+    for (int c = 0; c < C; ++c) {
+        m |= (rgb[c] == 1.0f ? 1u : 0u) << (5 * c);
+        m |= (rgb[c] == 0.0f ? 1u : 0u) << (15 + 5 * c);
+    }
+    return m;
+}
 
 __device__ __forceinline__ uint32_t dup_hash(uint32_t k, int shift) { return (k * 0x9E3779B1u) >> shift; }
 
-// All threads of the block call this.  table: C * slots words, flags: C *
-// slots bytes, slots a power of two >= 2 * npx.
-template <typename KeyOf>
-__device__ __forceinline__ void mark_repeats(const float* raw, int plane, const uint8_t* a, int npx, int C, uint32_t* table,
-                             uint8_t* flags, int slots, uint8_t* meta, KeyOf key)
+// Empties the C hash tables (C * slots key words, C * slots flag bytes;
+// slots a multiple of 64, table and flags 16-byte aligned).
+__device__ __forceinline__ void repeat_tables_clear(uint32_t* table, uint8_t* flags, int C, int slots)
+{
+    uint4* t4 = reinterpret_cast<uint4*>(table);
+    const uint4 pad = make_uint4(kEntropyPad, kEntropyPad, kEntropyPad, kEntropyPad);
+    for (int i = threadIdx.x; i < C * slots / 4; i += blockDim.x) {
+        t4[i] = pad;
+    }
+    uint4* f4 = reinterpret_cast<uint4*>(flags);
+    for (int i = threadIdx.x; i < C * slots / 16; i += blockDim.x) {
+        f4[i] = make_uint4(0u, 0u, 0u, 0u);
+    }
+}
+
+// Marks of a complete tile (all threads call; ends with a barrier).  Pixel
+// p is handled by thread p % blockDim.x.  NP > 0 (npx <= NP * blockDim.x):
+// the keys of a thread probe in lock step, one CAS per pending key a round,
+// so its NP * C insertions are in flight together, and the slot where each
+// key ended up is kept, so that its flag is read without probing again;
+// NP == 0: one key after the other, and a second probe per key to find its
+// slot's flag.  slots: a power of two >= 2 * npx, so every probe sequence
+// meets an empty slot.
+template <int NP>
+__device__ __forceinline__ void mark_repeats(const float* raw, int plane, const uint8_t* a, int npx, int C,
+                                             uint32_t* table, uint8_t* flags, int slots, uint64_t* cnt)
 {
     const int shift = 32 - (31 - __clz(slots));
-    for (int i = threadIdx.x; i < C * slots; i += blockDim.x) {
-        table[i] = kEntropyPad;
-        flags[i] = 0;
+    repeat_tables_clear(table, flags, C, slots);
+    if (NP > 0) {
+        constexpr int N = NP > 0 ? NP : 1;
+        uint32_t kk[N][3], h[N][3];
+        uint32_t pend = 0;  // bit j * 3 + c: key (j, c) still probing
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+            const int p = (int)threadIdx.x + j * (int)blockDim.x;
+            const bool on = p < npx && a[p] != 0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float fv = on && c < C ? raw[c * plane + p] : 0.0f;
+                kk[j][c] = float_key(fv);
+                h[j][c] = (uint32_t)c * (uint32_t)slots + dup_hash(kk[j][c], shift);
+                // clip values are counted per window, not hashed
+                pend |= (on && c < C && fv != 0.0f && fv != 1.0f) ? 1u << (j * 3 + c) : 0u;
+            }
+        }
+        const uint32_t hashed = pend;
+        __syncthreads();
+        for (int round = 0; pend && round < slots; ++round) {
+#pragma unroll
+            for (int j = 0; j < N; ++j) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const uint32_t bit = 1u << (j * 3 + c);
+                    if (pend & bit) {
+                        const uint32_t old = atomicCAS(&table[h[j][c]], kEntropyPad, kk[j][c]);
+                        if (old == kEntropyPad || old == kk[j][c]) {
+                            if (old != kEntropyPad) {
+                                flags[h[j][c]] = 1;
+                            }
+                            pend &= ~bit;
+                        } else {
+                            const uint32_t base = (uint32_t)c * (uint32_t)slots;
+                            h[j][c] = base + ((h[j][c] - base + 1u) & (uint32_t)(slots - 1));
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+            const int p = (int)threadIdx.x + j * (int)blockDim.x;
+            uint64_t m = 0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                if ((hashed >> (j * 3 + c)) & 1u) {
+                    m |= flags[h[j][c]] ? 1ull << (kCntMark + 5 * c) : 0ull;
+                }
+            }
+            if (m) {
+                cnt[p] |= m;
+            }
+        }
+        __syncthreads();
+        return;
     }
     __syncthreads();
     for (int p = threadIdx.x; p < npx; p += blockDim.x) {
@@ -188,9 +286,9 @@ __device__ __forceinline__ void mark_repeats(const float* raw, int plane, const 
         for (int c = 0; c < C; ++c) {
             const float fv = raw[c * plane + p];
             if (fv == 0.0f || fv == 1.0f) {
-                continue;  // clip values are counted per window, not hashed
+                continue;
             }
-            const uint32_t k = key(fv);
+            const uint32_t k = float_key(fv);
             uint32_t* t = table + c * slots;
             uint32_t h = dup_hash(k, shift);
             for (int probe = 0; probe < slots; ++probe) {
@@ -208,77 +306,50 @@ __device__ __forceinline__ void mark_repeats(const float* raw, int plane, const 
     }
     __syncthreads();
     for (int p = threadIdx.x; p < npx; p += blockDim.x) {
-        uint8_t m = 0;
-        if (a[p]) {
-            m = 0x80;
-            for (int c = 0; c < C; ++c) {
-                const float fv = raw[c * plane + p];
-                if (fv == 0.0f || fv == 1.0f) {
-                    continue;
-                }
-                const uint32_t k = key(fv);
-                const uint32_t* t = table + c * slots;
-                uint32_t h = dup_hash(k, shift);
-                for (int probe = 0; probe < slots && t[h] != k; ++probe) {
-                    h = (h + 1) & (uint32_t)(slots - 1);
-                }
-                m |= flags[c * slots + h] ? (uint8_t)(1u << c) : (uint8_t)0;
-            }
+        if (!a[p]) {
+            continue;
         }
-        meta[p] = m;
+        uint64_t m = 0;
+        for (int c = 0; c < C; ++c) {
+            const float fv = raw[c * plane + p];
+            if (fv == 0.0f || fv == 1.0f) {
+                continue;
+            }
+            const uint32_t k = float_key(fv);
+            const uint32_t* t = table + c * slots;
+            uint32_t h = dup_hash(k, shift);
+            for (int probe = 0; probe < slots && t[h] != k; ++probe) {
+                h = (h + 1) & (uint32_t)(slots - 1);
+            }
+            m |= flags[c * slots + h] ? 1ull << (kCntMark + 5 * c) : 0ull;
+        }
+        if (m) {
+            cnt[p] |= m;
+        }
     }
     __syncthreads();
 }
 
-// Opaque-tap count and OR of the repeat marks of the W x W window at ci.
+// Opaque-tap count, repeat marks (bit c: some tap of channel c is marked)
+// and clip counters (bits 0..29) of the W x W window at ci.
 template <int W>
-__device__ __forceinline__ void window_marks(const uint8_t* meta, int TW, int ci, int& n, uint32_t& marks)
+__device__ __forceinline__ void window_counts(const uint64_t* cnt, int TW, int ci, int& n, uint32_t& marks,
+                                              uint32_t& clips)
 {
-    n = 0;
-    marks = 0;
+    uint64_t sum = 0;
 #pragma unroll
     for (int dy = 0; dy < W; ++dy) {
 #pragma unroll
         for (int dx = 0; dx < W; ++dx) {
-            const uint32_t m = meta[ci + (dy - W / 2) * TW + (dx - W / 2)];
-            n += (int)(m >> 7);
-            marks |= m;
+            sum += cnt[ci + (dy - W / 2) * TW + (dx - W / 2)];
         }
     }
-}
-
-// Per-pixel clip counters of a float tile: 5-bit fields, samples equal to 1.0
-// for channels 0..2 at bits 0, 5, 10 and equal to 0.0 at bits 15, 20, 25
-// (opaque pixels only); a window's sum keeps every field below 32.
-__device__ __forceinline__ uint32_t clip_counts(const float* rgb, int C)
-{
-    uint32_t m = 0;
-    for (int c = 0; c < C; ++c) {
-        m |= (rgb[c] == 1.0f ? 1u : 0u) << (5 * c);
-        m |= (rgb[c] == 0.0f ? 1u : 0u) << (15 + 5 * c);
-    }
-    return m;
-}
-
-// Opaque-tap count, OR of the repeat marks and sum of the clip counters of
-// the W x W window at ci.
-template <int W>
-__device__ __forceinline__ void window_counts(const uint8_t* meta, const uint32_t* cnt, int TW, int ci, int& n,
-                                              uint32_t& marks, uint32_t& clips)
-{
-    n = 0;
+    n = (int)((sum >> kCntOpaque) & 31u);
+    clips = (uint32_t)sum & 0x3fffffffu;
     marks = 0;
-    clips = 0;
 #pragma unroll
-    for (int dy = 0; dy < W; ++dy) {
-#pragma unroll
-        for (int dx = 0; dx < W; ++dx) {
-            const int idx = ci + (dy - W / 2) * TW + (dx - W / 2);
-            const uint32_t m = meta[idx];
-            n += (int)(m >> 7);
-            marks |= m;
-            clips += cnt[idx];
-        }
+    for (int c = 0; c < 3; ++c) {
+        marks |= ((sum >> (kCntMark + 5 * c)) & 31u) ? 1u << c : 0u;
     }
 }
 
@@ -294,60 +365,6 @@ __device__ __forceinline__ float entropy_clip_bins(int n, int m1, int m0, const 
     const long long* fx = tab.plogp_fx + (int64_t)n * (nmax + 1);
     const long long acc = (long long)(n - m1 - m0) * fx[1] + (m1 > 0 ? fx[m1] : 0) + (m0 > 0 ? fx[m0] : 0);
     return fminf(__fmul_rn(-(float)acc * 1.3877787807814457e-17f, tab.scale_logb[bins]), 1.0f);
-}
-
-// H of n all-distinct keys, the value entropy_window_float computes for them.
-__device__ __forceinline__ float entropy_distinct(int n, const WeightTables& tab, int nmax)
-{
-    if (n <= 1) {
-        return 0.0f;
-    }
-    const long long acc = (long long)n * tab.plogp_fx[(int64_t)n * (nmax + 1) + 1];
-    const float H = __fmul_rn(-(float)acc * 1.3877787807814457e-17f, tab.scale_logb[n]);
-    return fminf(H, 1.0f);
-}
-
-}  // namespace enb
-
-namespace enb {
-
-// H of a float window channel whose marked taps (bit `bit` of meta) all carry
-// one key: n - m singletons and one bin of m.  Returns false when the marked
-// taps hold more than one key (the caller then sorts the window).
-template <int W, typename KeyOf>
-__device__ __forceinline__ bool entropy_one_repeat(const float* raw, const uint8_t* meta, int TW, int ci,
-                                                   uint32_t bit, int n, const WeightTables& tab, int nmax,
-                                                   KeyOf key, float& H)
-{
-    uint32_t first = kEntropyPad;
-    int m = 0;
-    bool single = true;
-#pragma unroll
-    for (int dy = 0; dy < W; ++dy) {
-#pragma unroll
-        for (int dx = 0; dx < W; ++dx) {
-            const int idx = ci + (dy - W / 2) * TW + (dx - W / 2);
-            const uint32_t mk = meta[idx];
-            if ((mk & 0x80u) && (mk & bit)) {
-                const uint32_t k = key(raw[idx]);
-                single = single && (m == 0 || k == first);
-                first = m == 0 ? k : first;
-                ++m;
-            }
-        }
-    }
-    if (!single) {
-        return false;
-    }
-    const int bins = n - m + 1;
-    if (bins <= 1) {
-        H = 0.0f;
-        return true;
-    }
-    const long long* fx = tab.plogp_fx + (int64_t)n * (nmax + 1);
-    const long long acc = (long long)(n - m) * fx[1] + fx[m];
-    H = fminf(__fmul_rn(-(float)acc * 1.3877787807814457e-17f, tab.scale_logb[bins]), 1.0f);
-    return true;
 }
 
 }  // namespace enb

@@ -252,15 +252,15 @@ __global__ void __launch_bounds__(256) k_f_enfuse_mask(FloatPixelView img, const
     extern __shared__ __align__(16) unsigned char fsmem[];
     const int halo = fweight_halo(wp);
     const FTile t = ftile_carve(fsmem, FWT + 2 * halo, wp.repeat_slots);
-    ftile_load(t, wp, img.p, img.pitch, img.stride, img.w, img.h, img.C, alpha, apitch, blockIdx.x * FWT - halo,
-               blockIdx.y * FWT - halo);
+    const int opaque = ftile_load(t, wp, img.p, img.pitch, img.stride, img.w, img.h, img.C, alpha, apitch,
+                                  blockIdx.x * FWT - halo, blockIdx.y * FWT - halo);
     const int lx = threadIdx.x % FWT, ly = threadIdx.x / FWT;
     const int x = blockIdx.x * FWT + lx, y = blockIdx.y * FWT + ly;
     if (x >= img.w || y >= img.h) {
         return;
     }
     const int ci = (ly + halo) * t.TW + (lx + halo);
-    out[(int64_t)y * opitch + x] = f_pixel_weight<CW, EW>(t, wp, tab, ci, x, y, img.w, img.h, img.C);
+    out[(int64_t)y * opitch + x] = f_pixel_weight<CW, EW>(t, wp, tab, ci, x, y, img.w, img.h, img.C, opaque != 0);
 }
 
 // ---------------------------------------------------------------------------

@@ -157,26 +157,26 @@ __device__ __forceinline__ float entropy_f(const uint32_t* v, int n, const Weigh
 
 // ---- one exposure's tile in shared memory -----------------------------------
 
-// Histogram key of a float sample: its bit pattern, -0 folded into +0.
-__device__ __forceinline__ uint32_t float_key(float f) { return __float_as_uint(f == 0.0f ? 0.0f : f); }
-
 // Tile of (TW x TW) input pixels around a block of output pixels: gray,
-// the three samples, opaque flags, repeat marks and their hash tables.
+// the three samples, the window counters (clip values, repeat marks, opaque
+// flags; enb_entropy.cuh), the repeat hash tables and the opaque flags.
+// TW is even (16 + 2 * halo), which keeps every array 16-byte aligned.
 struct FTile {
     float* gray;     // [TW*TW]
     float* raw;      // [3][TW*TW]
-    uint32_t* cnt;   // [TW*TW] clip counters (clip_counts)
+    uint64_t* cnt;   // [TW*TW]
     uint32_t* table; // [3][slots]
-    uint8_t* a;      // [TW*TW]
-    uint8_t* meta;   // [TW*TW]
     uint8_t* flags;  // [3][slots]
+    uint8_t* a;      // [TW*TW]
     int TW, slots;
 };
 
 __host__ __device__ inline size_t ftile_bytes(int TW, int slots)
 {
-    return (size_t)TW * TW * (5 * sizeof(float) + 2) + (size_t)slots * 3 * 5;
+    return (size_t)TW * TW * (4 * sizeof(float) + sizeof(uint64_t) + 1) + (size_t)slots * 3 * 5;
 }
+
+__host__ __device__ inline size_t align16(size_t n) { return (n + 15) & ~(size_t)15; }
 
 __device__ __forceinline__ FTile ftile_carve(unsigned char* smem, int TW, int slots)
 {
@@ -185,41 +185,65 @@ __device__ __forceinline__ FTile ftile_carve(unsigned char* smem, int TW, int sl
     t.slots = slots;
     t.gray = reinterpret_cast<float*>(smem);
     t.raw = t.gray + TW * TW;
-    t.cnt = reinterpret_cast<uint32_t*>(t.raw + 3 * TW * TW);
-    t.table = t.cnt + TW * TW;
-    t.a = reinterpret_cast<uint8_t*>(t.table + 3 * slots);
-    t.meta = t.a + TW * TW;
-    t.flags = t.meta + TW * TW;
+    t.cnt = reinterpret_cast<uint64_t*>(t.raw + 3 * TW * TW);
+    t.table = reinterpret_cast<uint32_t*>(t.cnt + TW * TW);
+    t.flags = reinterpret_cast<uint8_t*>(t.table + 3 * slots);
+    t.a = t.flags + 3 * slots;
     return t;
 }
 
-// Loads the tile whose top-left input pixel is (x0, y0) (all threads call;
-// ends with the tile complete in shared memory).  alpha == nullptr: opaque.
-__device__ __forceinline__ void ftile_load(const FTile& t, const FloatWeightParams& wp, const float* img, int64_t pitch,
-                                           int stride, int w, int h, int C, const uint8_t* alpha, int64_t apitch,
-                                           int x0, int y0)
+// Writes tile pixel k from its samples and opaque flag.
+__device__ __forceinline__ void ftile_put_px(const FTile& t, const FloatWeightParams& wp, int k, const float (&rgb)[3],
+                                             uint8_t a, int C)
 {
-    const int TW = t.TW;
+    const int TT = t.TW * t.TW;
+    t.gray[k] = C == 1 ? rgb[0] : gray_of_f(wp, rgb[0], rgb[1], rgb[2]);
+    t.a[k] = a;
+    t.cnt[k] = a ? (uint64_t)clip_counts(rgb, C) | (1ull << kCntOpaque) : 0ull;
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+        t.raw[ch * TT + k] = rgb[ch];
+    }
+}
+
+// Samples and opaque flag of input pixel (gx, gy); zero and transparent
+// outside the image.
+__device__ __forceinline__ void ftile_fetch_px(float (&rgb)[3], uint8_t& a, const float* img, int64_t pitch, int stride,
+                                               int w, int h, int C, const uint8_t* alpha, int64_t apitch, int gx, int gy)
+{
+    rgb[0] = rgb[1] = rgb[2] = 0.0f;
+    a = 0;
+    if (gx >= 0 && gx < w && gy >= 0 && gy < h) {
+        const float* px = img + (int64_t)gy * pitch + (int64_t)gx * stride;
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+            if (ch < C) {
+                rgb[ch] = __ldg(&px[ch]);
+            }
+        }
+        a = alpha ? (__ldg(&alpha[(int64_t)gy * apitch + gx]) != 0) : 1;
+    }
+}
+
+// Loads the tile whose top-left input pixel is (x0, y0) (all threads call;
+// ends with the tile and its repeat marks complete in shared memory).
+// alpha == nullptr: opaque.  Returns nonzero when every tile pixel is
+// opaque (and inside the image).
+__device__ __forceinline__ int ftile_load(const FTile& t, const FloatWeightParams& wp, const float* img, int64_t pitch,
+                                          int stride, int w, int h, int C, const uint8_t* alpha, int64_t apitch,
+                                          int x0, int y0)
+{
+    const int TW = t.TW, TT = TW * TW;
     // tile pixel k = r * TW + c, walked with a stride of blockDim.x
     const int dr = (int)blockDim.x / TW, dc = (int)blockDim.x - dr * TW;
     int r = (int)threadIdx.x / TW, c = (int)threadIdx.x - r * TW;
-    for (int k = threadIdx.x; k < TW * TW; k += blockDim.x) {
-        const int gx = x0 + c, gy = y0 + r;
-        float rgb[3] = {0.0f, 0.0f, 0.0f};
-        uint8_t a = 0;
-        if (gx >= 0 && gx < w && gy >= 0 && gy < h) {
-            const float* px = img + (int64_t)gy * pitch + (int64_t)gx * stride;
-            for (int ch = 0; ch < C; ++ch) {
-                rgb[ch] = __ldg(&px[ch]);
-            }
-            a = alpha ? (__ldg(&alpha[(int64_t)gy * apitch + gx]) != 0) : 1;
-        }
-        t.gray[k] = C == 1 ? rgb[0] : gray_of_f(wp, rgb[0], rgb[1], rgb[2]);
-        t.a[k] = a;
-        t.cnt[k] = a ? clip_counts(rgb, C) : 0u;
-        for (int ch = 0; ch < 3; ++ch) {
-            t.raw[ch * TW * TW + k] = rgb[ch];
-        }
+    int mine = 1;
+    for (int k = threadIdx.x; k < TT; k += blockDim.x) {
+        float rgb[3];
+        uint8_t a;
+        ftile_fetch_px(rgb, a, img, pitch, stride, w, h, C, alpha, apitch, x0 + c, y0 + r);
+        ftile_put_px(t, wp, k, rgb, a, C);
+        mine &= a;
         c += dc;
         r += dr;
         if (c >= TW) {
@@ -227,21 +251,49 @@ __device__ __forceinline__ void ftile_load(const FTile& t, const FloatWeightPara
             ++r;
         }
     }
-    __syncthreads();
+    const int opaque = __syncthreads_and(mine);
     if (t.slots) {
-        mark_repeats(t.raw, TW * TW, t.a, TW * TW, C, t.table, t.flags, t.slots, t.meta,
-                     [](float f) { return float_key(f); });
+        if (TT <= 2 * (int)blockDim.x) {
+            mark_repeats<2>(t.raw, TT, t.a, TT, C, t.table, t.flags, t.slots, t.cnt);
+        } else {
+            mark_repeats<0>(t.raw, TT, t.a, TT, C, t.table, t.flags, t.slots, t.cnt);
+        }
     }
+    return opaque;
 }
 
 // Sample standard deviation of the opaque window pixels (localStdDevIf,
 // src/enfuse.h:75-219) in two passes around the float mean.  CW > 0: the
 // window size at compile time; CW == 0: b is the runtime half-width.
+// opaque: every tile pixel is opaque, so no tap is skipped (the same sums).
 template <int CW>
-__device__ __forceinline__ float window_stddev(const FTile& t, int ci, int bdyn)
+__device__ __forceinline__ float window_stddev(const FTile& t, int ci, int bdyn, bool opaque)
 {
-    const int b = CW > 0 ? CW / 2 : bdyn;
     const int TW = t.TW;
+    if (CW > 0 && opaque) {
+        constexpr int B = CW / 2, N = (CW > 0 ? CW * CW : 1);
+        float v[N];
+        float sum = 0.0f;
+#pragma unroll
+        for (int dy = -B; dy <= B; ++dy) {
+#pragma unroll
+            for (int dx = -B; dx <= B; ++dx) {
+                v[(dy + B) * CW + dx + B] = t.gray[ci + dy * TW + dx];
+                sum += v[(dy + B) * CW + dx + B];
+            }
+        }
+        const float mean = __fdiv_rn(sum, (float)N);
+        float s1 = 0.0f, s2 = 0.0f;
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            const float d = v[i] - mean;
+            s1 += d;
+            s2 = fmaf(d, d, s2);
+        }
+        const float var = __fdiv_rn(s2 - __fdiv_rn(s1 * s1, (float)N), (float)(N - 1));
+        return sqrtf(fmaxf(var, 0.0f));
+    }
+    const int b = CW > 0 ? CW / 2 : bdyn;
     float sum = 0.0f;
     int n = 0;
 #pragma unroll
@@ -314,7 +366,7 @@ __device__ __forceinline__ float window_entropy(const FTile& t, const FloatWeigh
 // the reference's order (src/enfuse.h:1119-1120, 1133-1134, 1208-1209).
 template <int CW, int EW>
 __device__ __forceinline__ float f_pixel_weight(const FTile& t, const FloatWeightParams& wp, const WeightTables& tab,
-                                                int ci, int x, int y, int w, int h, int C)
+                                                int ci, int x, int y, int w, int h, int C, bool opaque)
 {
     if (!t.a[ci]) {
         return 0.0f;
@@ -327,7 +379,7 @@ __device__ __forceinline__ float f_pixel_weight(const FTile& t, const FloatWeigh
         const int b = wp.contrast_window / 2;
         float sd = 0.0f;  // the border strip is not written (0)
         if (x >= b && x < w - b && y >= b && y < h - b) {
-            sd = window_stddev<CW>(t, ci, b);
+            sd = window_stddev<CW>(t, ci, b, opaque);
         }
         result = wp.w_contrast * sd + result;
     }
@@ -353,7 +405,7 @@ __device__ __forceinline__ float f_pixel_weight(const FTile& t, const FloatWeigh
             int nwin = 0;
             uint32_t marks = 0xffu, clips = 0;
             if (EW > 0 && t.slots) {
-                window_counts<(EW > 0 ? EW : 3)>(t.meta, t.cnt, t.TW, ci, nwin, marks, clips);
+                window_counts<(EW > 0 ? EW : 3)>(t.cnt, t.TW, ci, nwin, marks, clips);
             }
             emin = 3.402823466e38f;
             for (int ch = 0; ch < C; ++ch) {
