@@ -77,6 +77,9 @@ struct enb_ctx {
         }
     };
     std::unique_ptr<BatchCache> batch;
+    // device error word of the kernels' bounded waits (bit 0: a TMA tile
+    // pipeline wait timed out); read after synchronisations
+    unsigned int* dev_err = nullptr;
 };
 
 struct enb_pyramid {
@@ -92,6 +95,45 @@ struct enb_pyramid {
 };
 
 namespace {
+
+// The context's device error word, allocated (zeroed) on first use; null
+// when it cannot be allocated (the kernels that need it are then not used).
+unsigned int* device_error_word(enb_ctx* ctx)
+{
+    if (!ctx->dev_err) {
+        void* p = nullptr;
+        if (cudaMalloc(&p, sizeof(unsigned int)) != cudaSuccess || cudaMemset(p, 0, sizeof(unsigned int)) != cudaSuccess) {
+            cudaGetLastError();
+            if (p) {
+                cudaFree(p);
+            }
+            return nullptr;
+        }
+        ctx->dev_err = static_cast<unsigned int*>(p);
+    }
+    return ctx->dev_err;
+}
+
+// After a synchronisation of the context's stream: a kernel that gave up a
+// bounded wait fails the call (and the word is cleared).
+enb_status check_device_error(enb_ctx* ctx)
+{
+    if (!ctx->dev_err) {
+        return ENB_OK;
+    }
+    unsigned int v = 0;
+    if (cudaMemcpy(&v, ctx->dev_err, sizeof v, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        ctx->err = "reading the device error word failed";
+        cudaGetLastError();
+        return ENB_ERR_CUDA;
+    }
+    if (v) {
+        cudaMemset(ctx->dev_err, 0, sizeof v);
+        ctx->err = "a kernel's wait for its tile copies timed out (TMA pipeline)";
+        return ENB_ERR_CUDA;
+    }
+    return ENB_OK;
+}
 
 size_t dtype_size(int dt)
 {
@@ -181,9 +223,10 @@ void prof_resolve(enb_ctx* ctx)
 #define ENB_LAUNCH(ctx, call)                                  \
     do {                                                       \
         cudaEvent_t a_ = prof_begin(ctx);                      \
+        last_launch().kernels = 1;                             \
         cudaError_t e_ = (call);                               \
         prof_end((ctx), a_);                                   \
-        (ctx)->launches++;                                     \
+        (ctx)->launches += (uint64_t)last_launch().kernels;    \
         if (e_ != cudaSuccess) {                               \
             return cuda_fail((ctx), e_, #call);                \
         }                                                      \
@@ -924,6 +967,7 @@ enb_status enblend_fused(enb_ctx* ctx, const enb_image* white, const enb_image* 
     h0.dither = o.dither;
     h0.wrap = wrap;
     h0.seed = o.seed;
+    h0.err = device_error_word(ctx);
     PlanarView g0{}, b0{}, r0{};
     if (NL >= 1) {
         g0 = level_view(gw.p, 0);
@@ -1201,7 +1245,7 @@ enb_status enblend_host_banded(enb_ctx* ctx, const enb_image* white, const enb_i
     ENB_CUDA(ctx, cudaEventRecord(ev[nin + nout + 1], cs));
     ENB_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ev[nin + nout + 1], 0));
     ENB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    return ENB_OK;
+    return check_device_error(ctx);
 }
 
 extern "C" {
@@ -1259,6 +1303,10 @@ enb_status enb_destroy(enb_ctx* ctx)
         cudaDeviceSynchronize();
         ctx->batch.reset();
     }
+    if (ctx->dev_err) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(ctx->dev_err);
+    }
     delete ctx;
     return ENB_OK;
 }
@@ -1314,7 +1362,7 @@ enb_status enb_synchronize(enb_ctx* ctx)
         return ENB_ERR_INVALID;
     }
     ENB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    return ENB_OK;
+    return check_device_error(ctx);
 }
 
 const char* enb_last_error(const enb_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }

@@ -29,6 +29,7 @@
 #include "enb_internal.h"
 #include "enb_reduce.cuh"
 #include "enb_tiles.cuh"
+#include "enb_tma.cuh"
 
 namespace enb {
 
@@ -186,14 +187,26 @@ struct Out0Args {
     uint64_t seed;
     uint32_t key;                // dither_key(seed)
     int32_t maxv;
-    int ty0;                     // first tile row (16 rows) of the launch
+    int tx0, ty0;                // first tile column (64 pixels) and row (16 rows) of the launch
+    unsigned int* err;           // device error word (bit 0: a tile wait timed out)
+};
+
+// Coarse taps of an interior tile packed as (Gw, Gb, R) int4 per position
+// and channel (the staging of k_out0).
+struct PackedTaps {
+    const int4 (*s)[ESH][ESW];
+    __device__ __forceinline__ void operator()(int c, int qx, int qy, int kind, int32_t (&ew)[4], int32_t (&eb)[4],
+                                               int32_t (&er)[4]) const
+    {
+        expand_packed(s[c], qx, qy, kind, ew, eb, er);
+    }
 };
 
 // Level-0 output of the interior quad (X, Y) (tile position qx, qy) from its
 // loaded pixels and seam mask and the packed coarse taps of the tile.
-template <typename TIn, typename T, int C, int S, int AM, bool VEC>
-__device__ __forceinline__ void out0_quad(const Out0Args& a, const int4 (*sbuf)[ESH][ESW], int X, int Y, int qx,
-                                          int qy, const TIn (&wp)[4][S], const TIn (&bp)[4][S], const int32_t (&mk)[4])
+template <typename TIn, typename T, int C, int S, int AM, bool VEC, typename Taps>
+__device__ __forceinline__ void out0_quad(const Out0Args& a, const Taps& taps, int X, int Y, int qx, int qy,
+                                          const TIn (&wp)[4][S], const TIn (&bp)[4][S], const int32_t (&mk)[4])
 {
     constexpr int F = 7;
     constexpr int MF = sizeof(TIn) == 1 ? 7 : 15;
@@ -214,7 +227,7 @@ __device__ __forceinline__ void out0_quad(const Out0Args& a, const int4 (*sbuf)[
 #pragma unroll
     for (int c = 0; c < C; ++c) {
         int32_t ew[4], eb[4], er[4];
-        expand_packed(sbuf[c], qx, qy, kind, ew, eb, er);
+        taps(c, qx, qy, kind, ew, eb, er);
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             res[c][q] = merge_sample<T>(kind, mk[q], WV, (int32_t)wp[q][c] << F, ew[q], (int32_t)bp[q][c] << F,
@@ -271,7 +284,7 @@ __global__ void __launch_bounds__(256, 3) k_out0(CoarseLevels cl, Out0Args a)
     int32_t (*ss)[ESH][ESW] = reinterpret_cast<int32_t (*)[ESH][ESW]>(&sbuf[0][0][0]);
     griddep_wait();
     griddep_launch();
-    const int X0 = blockIdx.x * ETW, Y0 = (blockIdx.y + a.ty0) * ETH;
+    const int X0 = (blockIdx.x + a.tx0) * ETW, Y0 = (blockIdx.y + a.ty0) * ETH;
     const int I0 = X0 >> 1, J0 = Y0 >> 1;
     const int qx = threadIdx.x % 32, qy = threadIdx.x / 32;
     const int i = I0 + qx, j = J0 + qy;
@@ -297,7 +310,7 @@ __global__ void __launch_bounds__(256, 3) k_out0(CoarseLevels cl, Out0Args a)
                                (int32_t)__ldg(m0 + a.mpitch) << MF, (int32_t)__ldg(m0 + a.mpitch + 1) << MF};
         stage_coarse4_interior<C, T, true, 256>(sbuf, cl, I0, J0);
         __syncthreads();
-        out0_quad<TIn, T, C, S, AM, VEC>(a, sbuf, X, Y, qx, qy, wp, bp, mk);
+        out0_quad<TIn, T, C, S, AM, VEC>(a, PackedTaps{sbuf}, X, Y, qx, qy, wp, bp, mk);
         return;
     }
 
@@ -374,6 +387,181 @@ __global__ void __launch_bounds__(256, 3) k_out0(CoarseLevels cl, Out0Args a)
         st_px<TIn, S, VEC>(reinterpret_cast<TIn*>(a.out) + (int64_t)YY * a.opitch + (int64_t)XX * S, o[q]);
         if (a.out_alpha) {
             a.out_alpha[(int64_t)YY * a.oapitch + XX] = uni[q] ? 255 : 0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Level 0 on the interior tiles: persistent CTAs fed by a TMA pipeline
+// ---------------------------------------------------------------------------
+//
+// Each CTA walks its share of the interior tiles (blockIdx.x, + gridDim.x,
+// ...) with two shared-memory stages: while the quads of one tile are
+// merged, the TMA unit copies the next tile's image rows, seam-mask rows and
+// coarse neighbourhoods into the other stage, so that the loads of a tile
+// are in flight during the arithmetic of the previous one and no thread
+// spends registers or issue slots on them.  The merge of a quad is
+// out0_quad's, with the coarse taps read from the planar TMA boxes.
+
+// Tensor maps of one launch: the interleaved images as 2-D arrays of w * S
+// samples by h rows, the seam mask, and the 3C coarse planes.
+struct Out0Maps {
+    CUtensorMap white, black, mask;
+    CUtensorMap coarse[9];
+};
+
+// One stage: both images' 16 rows of 64 pixels, the mask rows and, per
+// coarse plane, ESH rows of CBW samples that start XOFF samples left of the
+// tile's first coarse column I0 (a TMA box starts on a 16-byte boundary;
+// the taps used are I0-1 .. I0+32).  Every part is a multiple of 128 bytes.
+template <typename TIn, typename T, int C, int S>
+struct Out0Stage {
+    static constexpr int XOFF = 16 / (int)sizeof(T);
+    static constexpr int CBW = (ESW - 1 + XOFF + XOFF - 1) / XOFF * XOFF;
+    static constexpr int IMG = ETH * ETW * S * (int)sizeof(TIn);
+    static constexpr int MSK = ETH * ETW;
+    static constexpr int PLANE_BYTES = ESH * CBW * (int)sizeof(T);
+    static constexpr int PLANE = (PLANE_BYTES + 127) / 128 * 128;
+    static constexpr int BYTES = 2 * IMG + MSK + 3 * C * PLANE;
+    static constexpr uint32_t TX = (uint32_t)(2 * IMG + MSK + 3 * C * PLANE_BYTES);
+    static_assert(IMG % 128 == 0 && MSK % 128 == 0, "stage parts stay 128-byte aligned");
+};
+
+// Coarse taps of an interior quad from the planar boxes (plane q at p + q *
+// PS samples, rows of CBW samples; column 0 is coarse column I0 - XOFF).
+template <typename T, int C, int CBW, int PS, int XOFF>
+struct PlanarTaps {
+    const T* p;
+    __device__ __forceinline__ void load(int q, int off, int32_t (&v)[3][3]) const
+    {
+        const T* b = p + q * PS + off;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                v[r][c] = (int32_t)b[r * CBW + c];
+            }
+        }
+    }
+    __device__ __forceinline__ void operator()(int c, int qx, int qy, int kind, int32_t (&ew)[4], int32_t (&eb)[4],
+                                               int32_t (&er)[4]) const
+    {
+        const int off = qy * CBW + qx + XOFF - 1;
+        int32_t v[3][3];
+        load(2 * C + c, off, v);
+        expand9<false>(v, er);
+        if (kind != 2) {
+            load(c, off, v);
+            expand9<true>(v, ew);
+        }
+        if (kind != 1) {
+            load(C + c, off, v);
+            expand9<true>(v, eb);
+        }
+    }
+};
+
+// Two horizontally adjacent interleaved pixels from shared memory (S == 4:
+// one 16-byte (u16) or 8-byte (u8) access).
+template <typename TIn, int S>
+__device__ __forceinline__ void lds_pixel_pair(const TIn* p, TIn (&a)[S], TIn (&b)[S])
+{
+    static_assert(S == 4, "RGBA pixels");
+    if (sizeof(TIn) == 2) {
+        const uint4 v = *reinterpret_cast<const uint4*>(p);
+        const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            a[2 * c] = (TIn)(w[c] & 0xffffu);
+            a[2 * c + 1] = (TIn)(w[c] >> 16);
+            b[2 * c] = (TIn)(w[2 + c] & 0xffffu);
+            b[2 * c + 1] = (TIn)(w[2 + c] >> 16);
+        }
+    } else {
+        const uint2 v = *reinterpret_cast<const uint2*>(p);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            a[c] = (TIn)((v.x >> (8 * c)) & 0xffu);
+            b[c] = (TIn)((v.y >> (8 * c)) & 0xffu);
+        }
+    }
+}
+
+// Tiles t = 0 .. nbx * nby - 1 of the rectangle of tile columns bx0.. and
+// rows by0.. (all interior tiles).
+template <typename TIn, typename T, int C, int S, int AM>
+__global__ void __launch_bounds__(256, 3) k_out0_tma(const __grid_constant__ Out0Maps maps, Out0Args a, int bx0,
+                                                     int nbx, int by0, int nby)
+{
+    using St = Out0Stage<TIn, T, C, S>;
+    constexpr int MF = sizeof(TIn) == 1 ? 7 : 15;
+    extern __shared__ __align__(128) unsigned char osm[];
+    __shared__ __align__(8) uint64_t bar[2];
+    const int ntiles = nbx * nby;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_init_fence();
+        tma_prefetch_map(&maps.white);
+        tma_prefetch_map(&maps.black);
+        tma_prefetch_map(&maps.mask);
+    }
+    __syncthreads();
+    griddep_wait();
+    griddep_launch();
+    const int qx = threadIdx.x % 32, qy = threadIdx.x / 32;
+    const auto issue = [&](int t, int s) {
+        const int X0 = (bx0 + t % nbx) * ETW, Y0 = (by0 + t / nbx) * ETH;
+        const int I0 = X0 >> 1, J0 = Y0 >> 1;
+        unsigned char* st = osm + s * St::BYTES;
+        mbar_arrive_expect_tx(&bar[s], St::TX);
+        tma_load_2d(st, &maps.white, X0 * S, Y0, &bar[s]);
+        tma_load_2d(st + St::IMG, &maps.black, X0 * S, Y0, &bar[s]);
+        tma_load_2d(st + 2 * St::IMG, &maps.mask, X0, Y0, &bar[s]);
+#pragma unroll
+        for (int q = 0; q < 3 * C; ++q) {
+            tma_load_2d(st + 2 * St::IMG + St::MSK + q * St::PLANE, &maps.coarse[q], I0 - St::XOFF, J0 - 1, &bar[s]);
+        }
+    };
+    int t = blockIdx.x;
+    if (threadIdx.x == 0 && t < ntiles) {
+        issue(t, 0);
+    }
+    for (int it = 0; t < ntiles; ++it, t += gridDim.x) {
+        const int s = it & 1;
+        const bool next = t + (int)gridDim.x < ntiles;
+        if (threadIdx.x == 0 && next) {
+            // the other stage was last read before the previous barrier
+            fence_proxy_async();
+            issue(t + gridDim.x, s ^ 1);
+        }
+        const bool ok = mbar_wait_bounded(&bar[s], (uint32_t)(it >> 1) & 1u);
+        const int X = (bx0 + t % nbx) * ETW + 2 * qx, Y = (by0 + t / nbx) * ETH + 2 * qy;
+        const unsigned char* st = osm + s * St::BYTES;
+        const TIn* ws = reinterpret_cast<const TIn*>(st) + (2 * qy * ETW + 2 * qx) * S;
+        const TIn* bs = reinterpret_cast<const TIn*>(st + St::IMG) + (2 * qy * ETW + 2 * qx) * S;
+        const uint8_t* ms = st + 2 * St::IMG + 2 * qy * ETW + 2 * qx;
+        TIn wp[4][S], bp[4][S];
+        lds_pixel_pair<TIn, S>(ws, wp[0], wp[1]);
+        lds_pixel_pair<TIn, S>(ws + ETW * S, wp[2], wp[3]);
+        lds_pixel_pair<TIn, S>(bs, bp[0], bp[1]);
+        lds_pixel_pair<TIn, S>(bs + ETW * S, bp[2], bp[3]);
+        const uint32_t m01 = *reinterpret_cast<const uint16_t*>(ms), m23 = *reinterpret_cast<const uint16_t*>(ms + ETW);
+        const int32_t mk[4] = {(int32_t)(m01 & 0xffu) << MF, (int32_t)(m01 >> 8) << MF, (int32_t)(m23 & 0xffu) << MF,
+                               (int32_t)(m23 >> 8) << MF};
+        const PlanarTaps<T, C, St::CBW, St::PLANE / (int)sizeof(T), St::XOFF> taps{
+            reinterpret_cast<const T*>(st + 2 * St::IMG + St::MSK)};
+        out0_quad<TIn, T, C, S, AM, true>(a, taps, X, Y, qx, qy, wp, bp, mk);
+        if (!__syncthreads_and(ok)) {
+            // a stage never completed: report it, let the copies of the next
+            // stage (if any) land, and stop
+            if (threadIdx.x == 0) {
+                atomicOr(a.err, 1u);
+                if (next) {
+                    (void)mbar_wait_bounded(&bar[s ^ 1], (uint32_t)((it + 1) >> 1) & 1u);
+                }
+            }
+            return;
         }
     }
 }
@@ -648,6 +836,99 @@ cudaError_t launch_up_level(const PlanarView& gw1, const PlanarView& gb1, const 
     return cudaGetLastError();
 }
 
+// ---- TMA tensor maps ---------------------------------------------------------
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled of the driver (through the runtime's entry-point
+// query, so that the library needs no link against libcuda); null when the
+// driver has none.
+static EncodeTiledFn encode_tiled()
+{
+    static const EncodeTiledFn fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            return (EncodeTiledFn) nullptr;
+        }
+        return (EncodeTiledFn)f;
+    }();
+    return fn;
+}
+
+// A 2-D map of w x h elements with a row pitch in bytes and a bw x bh box;
+// false when the layout does not meet the TMA rules (16-byte aligned base
+// and pitch, box rows a multiple of 16 bytes).
+static bool map2d(CUtensorMap* m, CUtensorMapDataType dt, int esz, const void* base, int64_t w, int64_t h,
+                  int64_t pitch_bytes, int bw, int bh)
+{
+    const EncodeTiledFn fn = encode_tiled();
+    if (!fn || ((uintptr_t)base & 15) || (pitch_bytes & 15) || pitch_bytes < w * esz || (bw * esz) % 16 ||
+        bw > 256 || bh > 256) {
+        return false;
+    }
+    const cuuint64_t dims[2] = {(cuuint64_t)w, (cuuint64_t)h};
+    const cuuint64_t strides[1] = {(cuuint64_t)pitch_bytes};
+    const cuuint32_t box[2] = {(cuuint32_t)bw, (cuuint32_t)bh};
+    const cuuint32_t estr[2] = {1, 1};
+    return fn(m, dt, 2, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+static int sm_count()
+{
+    static const int n = [] {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        return v > 0 ? v : 1;
+    }();
+    return n;
+}
+
+// The TMA level-0 kernel over the interior rectangle [bx0, bx0 + nbx) x
+// [by0, by0 + nby) of tiles; false when this format or layout has no TMA
+// path (the caller then runs k_out0 there).
+template <typename TIn, typename T, int AM>
+static bool out0_tma_launch(const CoarseLevels& cl, const Out0Args& a, int bx0, int nbx, int by0, int nby,
+                            cudaStream_t st)
+{
+    constexpr int C = 3, S = 4;
+    using St = Out0Stage<TIn, T, C, S>;
+    const CUtensorMapDataType dimg = sizeof(TIn) == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16;
+    const CUtensorMapDataType dpl = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_INT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16;
+    Out0Maps maps;
+    bool ok = map2d(&maps.white, dimg, sizeof(TIn), a.white, (int64_t)a.w * S, a.h, a.wpitch * (int64_t)sizeof(TIn),
+                    ETW * S, ETH) &&
+              map2d(&maps.black, dimg, sizeof(TIn), a.black, (int64_t)a.w * S, a.h, a.bpitch * (int64_t)sizeof(TIn),
+                    ETW * S, ETH) &&
+              map2d(&maps.mask, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, a.mask, a.w, a.h, a.mpitch, ETW, ETH);
+    for (int q = 0; ok && q < 3 * C; ++q) {
+        ok = map2d(&maps.coarse[q], dpl, sizeof(T), cl.p[q], cl.w, cl.h, cl.pitch * (int64_t)sizeof(T), St::CBW, ESH);
+    }
+    if (!ok) {
+        return false;
+    }
+    auto kern = k_out0_tma<TIn, T, C, S, AM>;
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * St::BYTES) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        attr = true;
+    }
+    const int grid = std::min(nbx * nby, 3 * sm_count());
+    return launch_pdl_smem(kern, dim3((unsigned)grid), dim3(256), (size_t)(2 * St::BYTES), st, maps, a, bx0, nbx, by0,
+                           nby) == cudaSuccess;
+}
+
 cudaError_t launch_out0(const PlanarView* gw1, const PlanarView* gb1, const PlanarView* r1, const Out0Host& h,
                         cudaStream_t st, int ty0, int nty)
 {
@@ -681,6 +962,7 @@ cudaError_t launch_out0(const PlanarView* gw1, const PlanarView* gb1, const Plan
     a.seed = h.seed;
     a.key = dither_key(h.seed);
     a.maxv = wv.dtype == ENB_U8 ? 255 : 65535;
+    a.err = h.err;
     // k_out0 compiles these formats in
     const int mf_expect = wv.dtype == ENB_U8 ? 7 : 15;
     if (a.frac != 7 || a.mfrac != mf_expect || a.white_value != (255 << mf_expect) || wv.C > 4) {
@@ -691,8 +973,8 @@ cudaError_t launch_out0(const PlanarView* gw1, const PlanarView* gb1, const Plan
         cl = coarse_of(*gw1, *gb1, *r1);
     }
     const double px = npix_f(wv.w, wv.h);
+    const int rows = (wv.h + ETH - 1) / ETH, cols = (wv.w + ETW - 1) / ETW;
     {
-        const int rows = (wv.h + ETH - 1) / ETH;
         const double share = (double)(nty < 0 ? rows - ty0 : nty) / rows;
         note_launch("out0", share * (px * (3.0 * wv.stride * esz_f(wv.dtype) + 1.0 + (h.out_alpha.p ? 1.0 : 0.0)) +
                                      (gw1 ? 3.0 * pbytes(*gw1) : 0.0)));
@@ -700,16 +982,57 @@ cudaError_t launch_out0(const PlanarView* gw1, const PlanarView* gb1, const Plan
     const bool vec = vec_ok(wv.p, wv.pitch, wv.dtype, wv.stride) &&
                      vec_ok(h.black.p, h.black.pitch, wv.dtype, wv.stride) && vec_ok(h.out, h.opitch, wv.dtype, wv.stride);
     const int am = alpha_mode_code(h.white_alpha);
-    const int rows = (wv.h + ETH - 1) / ETH;
     if (nty < 0) {
         nty = rows - ty0;
     }
     if (nty <= 0) {
         return cudaSuccess;
     }
-    a.ty0 = ty0;
-    Out0Launch l{cl, a, dim3((unsigned)((wv.w + ETW - 1) / ETW), (unsigned)nty), st};
-    return dispatch_pixels(wv.dtype, wv.C, wv.stride, am, vec, l);
+    // k_out0 over the rectangle [tx0, tx0 + ncol) x [ry0, ry0 + nrow) of tiles
+    int kernels = 0;
+    const auto legacy = [&](int tx0, int ncol, int ry0, int nrow) -> cudaError_t {
+        if (ncol <= 0 || nrow <= 0) {
+            return cudaSuccess;
+        }
+        Out0Args b = a;
+        b.tx0 = tx0;
+        b.ty0 = ry0;
+        ++kernels;
+        Out0Launch l{cl, b, dim3((unsigned)ncol, (unsigned)nrow), st};
+        return dispatch_pixels(wv.dtype, wv.C, wv.stride, am, vec, l);
+    };
+    // interior tiles (interior_tile): columns 1 .. bx1, rows 1 .. by1
+    const int bx1 = gw1 ? std::min((wv.w - ETW) / ETW, (cl.w - ESW + 1) / (ETW / 2)) : 0;
+    const int by1 = gw1 ? std::min((wv.h - ETH) / ETH, (cl.h - ESH + 1) / (ETH / 2)) : 0;
+    const int iy0 = std::max(ty0, 1), iy1 = std::min(ty0 + nty - 1, by1);
+    bool tma = false;
+    if (bx1 >= 1 && iy1 >= iy0 && vec && wv.C == 3 && wv.stride == 4 && h.err &&
+        (wv.dtype == ENB_U16 || wv.dtype == ENB_U8)) {
+        const int nbx = bx1, nby = iy1 - iy0 + 1;
+        if (wv.dtype == ENB_U16) {
+            tma = am == 0   ? out0_tma_launch<uint16_t, int32_t, 0>(cl, a, 1, nbx, iy0, nby, st)
+                  : am == 1 ? out0_tma_launch<uint16_t, int32_t, 1>(cl, a, 1, nbx, iy0, nby, st)
+                            : out0_tma_launch<uint16_t, int32_t, 2>(cl, a, 1, nbx, iy0, nby, st);
+        } else {
+            tma = am == 0   ? out0_tma_launch<uint8_t, int16_t, 0>(cl, a, 1, nbx, iy0, nby, st)
+                  : am == 1 ? out0_tma_launch<uint8_t, int16_t, 1>(cl, a, 1, nbx, iy0, nby, st)
+                            : out0_tma_launch<uint8_t, int16_t, 2>(cl, a, 1, nbx, iy0, nby, st);
+        }
+    }
+    cudaError_t e = cudaSuccess;
+    if (tma) {
+        ++kernels;
+        // the border ring of the band around the interior rectangle
+        const cudaError_t r[4] = {legacy(0, 1, ty0, nty), legacy(bx1 + 1, cols - bx1 - 1, ty0, nty),
+                                  legacy(1, bx1, ty0, iy0 - ty0), legacy(1, bx1, iy1 + 1, ty0 + nty - 1 - iy1)};
+        for (cudaError_t x : r) {
+            e = e == cudaSuccess ? x : e;
+        }
+    } else {
+        e = legacy(0, cols, ty0, nty);
+    }
+    last_launch().kernels = kernels;
+    return e;
 }
 
 }  // namespace enb

@@ -107,9 +107,10 @@ struct FloatWeightParams {
 struct LaunchInfo {
     const char* name;
     double bytes;
+    int kernels;  // kernel launches the launcher made (1 unless it says otherwise)
 };
 LaunchInfo& last_launch();
-inline void note_launch(const char* name, double bytes) { last_launch() = LaunchInfo{name, bytes}; }
+inline void note_launch(const char* name, double bytes) { last_launch() = LaunchInfo{name, bytes, 1}; }
 
 // Level-0 pass of the fused enblend (enb_fused.cu).
 struct Out0Host {
@@ -124,6 +125,7 @@ struct Out0Host {
     int32_t* level0;      // collapsed level 0 (interleaved int32) or nullptr
     int frac, dither, wrap;
     uint64_t seed;
+    unsigned int* err;    // device error word of the context (bit 0: a tile wait timed out)
 };
 
 // Coarse end of the fused enblend blend (one launch): slot 0 is the finest
@@ -140,8 +142,8 @@ struct CoarseHost {
 // Default of enb_fuse_options.coarse_pixels == 0: no coarse launch.  With
 // programmatic dependent launch the per-level kernels finish the coarse
 // levels sooner than the cluster launch (measured on the 2x4096x3072 blend:
-// 0.636 ms per call against 0.650-0.665 ms with the cluster launch from
-// 8192 or 32768 pixels down).
+// 0.617 ms per call against 0.635-0.648 ms with the cluster launch from
+// 2048, 8192 or 32768 pixels down).
 constexpr int64_t kCoarsePixels = -1;
 
 // Launch with programmatic stream serialization: the kernel may be scheduled
@@ -155,6 +157,24 @@ inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, c
     cfg.gridDim = grid;
     cfg.blockDim = block;
     cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
+// The same with dynamic shared memory.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl_smem(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                                   Args&&... args)
+{
+    cudaLaunchConfig_t cfg{};
+    cudaLaunchAttribute attr[1];
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;

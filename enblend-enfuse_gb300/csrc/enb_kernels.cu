@@ -717,14 +717,14 @@ static inline dim3 row_grid(int w, int h) { return dim3((unsigned)((w + 255) / 2
 
 LaunchInfo& last_launch()
 {
-    static thread_local LaunchInfo li{"", 0.0};
+    static thread_local LaunchInfo li{"", 0.0, 1};
     return li;
 }
 
 static inline double esz(int dt) { return dt == ENB_U8 ? 1.0 : ((dt == ENB_U16 || dt == ENB_I16) ? 2.0 : 4.0); }
 static inline double npix(int w, int h) { return (double)w * (double)h; }
 static inline double planar_bytes(const PlanarView& v) { return npix(v.w, v.h) * v.C * esz(v.dtype); }
-static inline void note(const char* name, double bytes) { last_launch() = LaunchInfo{name, bytes}; }
+static inline void note(const char* name, double bytes) { last_launch() = LaunchInfo{name, bytes, 1}; }
 
 cudaError_t launch_to_fixed(const PixelView& s, const PlanarView& d, int frac, cudaStream_t st)
 {

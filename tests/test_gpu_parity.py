@@ -329,6 +329,43 @@ def test_enblend_alpha_sources(ctx, orc, plain):
     assert np.array_equal(out.cpu().numpy(), ref["out"])
 
 
+@pytest.mark.parametrize("dt", [np.uint8, np.uint16])
+@pytest.mark.parametrize("wrap", [False, True])
+@pytest.mark.parametrize("planes", [False, True])
+def test_enblend_level0_tma(ctx, orc, dt, wrap, planes):
+    """Canvas rows on 16-byte boundaries (width 640): the interior tiles of
+    level 0 take the TMA pipeline (four more launches for the border ring
+    than on a 641-wide canvas), alpha from the 4th component or from planes,
+    against the oracle; the host-buffer entry point runs it per output band
+    (1100 rows)."""
+    from enbgpu import synthetic
+    h = 1100 if planes else 300
+    white, black, mask = synthetic.panorama_pair(h, 400, 240, dt, seed=43)
+    mask[40:200, 250:300] = 111
+    kw, dkw = {}, {}
+    if planes:
+        wa, ba = orc.alpha_of(white).copy(), orc.alpha_of(black)
+        wa[300:340, 250:290] = 0
+        kw = dict(white_alpha=wa, black_alpha=ba)
+        dkw = dict(white_alpha=_dev(wa), black_alpha=_dev(ba))
+    ref = orc.enblend(white, black, mask, wrap=wrap, seed=8, want_level0=True, **kw)
+    l0 = torch.zeros((h, 640, 3), dtype=torch.int32, device="cuda")
+    n0 = ctx.launches
+    out, oa = ctx.enblend(_dev(white), _dev(black), _dev(mask), wrap=wrap, seed=8, level0=l0, **dkw)
+    n_tma = ctx.launches - n0
+    assert np.array_equal(l0.cpu().numpy(), ref["level0"])
+    assert np.array_equal(out.cpu().numpy(), ref["out"])
+    assert np.array_equal(oa.cpu().numpy(), ref["alpha"])
+    out2, oa2 = ctx.enblend(white, black, mask, wrap=wrap, seed=8, **kw)
+    assert np.array_equal(out2, ref["out"])
+    assert np.array_equal(oa2, ref["alpha"])
+    # the same scene one pixel wider: rows off the 16-byte grid, one level-0 launch
+    w1, b1, m1 = synthetic.panorama_pair(h, 400, 241, dt, seed=43)
+    n0 = ctx.launches
+    ctx.enblend(_dev(w1), _dev(b1), _dev(m1), wrap=wrap, seed=8)
+    assert n_tma == ctx.launches - n0 + 4
+
+
 def test_enblend_in_place(ctx, orc):
     """out may alias the black image (the reference writes into it)."""
     from enbgpu import synthetic
