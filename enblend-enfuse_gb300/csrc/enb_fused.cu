@@ -267,54 +267,23 @@ __device__ __forceinline__ void out0_quad(const Out0Args& a, const Taps& taps, i
     }
 }
 
+// Level-0 output of any tile (X0, Y0) (border tiles, or a single level): the
+// quads' pixels from clamped positions, the coarse planes staged in ss with
+// the border and wrap rules of stage_coarse.  All threads of the CTA call
+// (it contains a barrier); ss must be free on entry.
 template <typename TIn, typename T, int C, int S, int AM, bool VEC>
-__global__ void __launch_bounds__(256, 3) k_out0(CoarseLevels cl, Out0Args a)
+__device__ __forceinline__ void out0_border_tile(const CoarseLevels& cl, const Out0Args& a, int X0, int Y0,
+                                                 int32_t (*ss)[ESH][ESW])
 {
-    // fixed-point formats of the enblend pyramids (the host checks a.frac,
-    // a.mfrac, a.white_value and a.maxv against these): image 9.7 / 17.7,
-    // mask 9.7 (8-bit) / 9.15 (16-bit); one hash per pixel covers the dither
-    // bits of all its samples (F - 1 <= 8, C <= 4)
     constexpr int F = 7;
     constexpr int MF = sizeof(TIn) == 1 ? 7 : 15;
     constexpr int32_t WV = 255 << MF;
     constexpr int32_t MAXV = sizeof(TIn) == 1 ? 255 : 65535;
-    static_assert(C <= 4, "per-pixel dither bits");
-    // packed int4 taps for interior tiles, 3C int32 planes for border tiles
-    __shared__ int4 sbuf[C][ESH][ESW];
-    int32_t (*ss)[ESH][ESW] = reinterpret_cast<int32_t (*)[ESH][ESW]>(&sbuf[0][0][0]);
-    griddep_wait();
-    griddep_launch();
-    const int X0 = (blockIdx.x + a.tx0) * ETW, Y0 = (blockIdx.y + a.ty0) * ETH;
     const int I0 = X0 >> 1, J0 = Y0 >> 1;
     const int qx = threadIdx.x % 32, qy = threadIdx.x / 32;
-    const int i = I0 + qx, j = J0 + qy;
-    const int X = 2 * i, Y = 2 * j;
+    const int X = 2 * (I0 + qx), Y = 2 * (J0 + qy);
     const bool nearest = a.dither == ENB_DITHER_NEAREST;
-
-    if (a.has_coarse && interior_tile(X0, Y0, a.w, a.h, I0, J0, cl.w, cl.h)) {
-        // interior tile: no bounds, packed taps, only the expansions the seam
-        // mask of the quad selects
-        TIn wp[4][S], bp[4][S];
-        const TIn* w0 = reinterpret_cast<const TIn*>(a.white) + (int64_t)Y * a.wpitch + (int64_t)X * S;
-        const TIn* b0 = reinterpret_cast<const TIn*>(a.black) + (int64_t)Y * a.bpitch + (int64_t)X * S;
-        ld_px<TIn, S, VEC>(w0, wp[0]);
-        ld_px<TIn, S, VEC>(w0 + S, wp[1]);
-        ld_px<TIn, S, VEC>(w0 + a.wpitch, wp[2]);
-        ld_px<TIn, S, VEC>(w0 + a.wpitch + S, wp[3]);
-        ld_px<TIn, S, VEC>(b0, bp[0]);
-        ld_px<TIn, S, VEC>(b0 + S, bp[1]);
-        ld_px<TIn, S, VEC>(b0 + a.bpitch, bp[2]);
-        ld_px<TIn, S, VEC>(b0 + a.bpitch + S, bp[3]);
-        const uint8_t* m0 = a.mask + (int64_t)Y * a.mpitch + X;
-        const int32_t mk[4] = {(int32_t)__ldg(m0) << MF, (int32_t)__ldg(m0 + 1) << MF,
-                               (int32_t)__ldg(m0 + a.mpitch) << MF, (int32_t)__ldg(m0 + a.mpitch + 1) << MF};
-        stage_coarse4_interior<C, T, true, 256>(sbuf, cl, I0, J0);
-        __syncthreads();
-        out0_quad<TIn, T, C, S, AM, VEC>(a, PackedTaps{sbuf}, X, Y, qx, qy, wp, bp, mk);
-        return;
-    }
-
-    // border tile (or a single level): the quad's pixels, loaded (from
+    // the quad's pixels, loaded (from
     // clamped positions, unconditionally) before the barrier
     TIn wp[4][S], bp[4][S];
     int32_t mk[4];
@@ -391,6 +360,52 @@ __global__ void __launch_bounds__(256, 3) k_out0(CoarseLevels cl, Out0Args a)
     }
 }
 
+template <typename TIn, typename T, int C, int S, int AM, bool VEC>
+__global__ void __launch_bounds__(256, 3) k_out0(CoarseLevels cl, Out0Args a)
+{
+    // fixed-point formats of the enblend pyramids (the host checks a.frac,
+    // a.mfrac, a.white_value and a.maxv against these): image 9.7 / 17.7,
+    // mask 9.7 (8-bit) / 9.15 (16-bit); one hash per pixel covers the dither
+    // bits of all its samples (F - 1 <= 8, C <= 4)
+    constexpr int MF = sizeof(TIn) == 1 ? 7 : 15;
+    static_assert(C <= 4, "per-pixel dither bits");
+    // packed int4 taps for interior tiles, 3C int32 planes for border tiles
+    __shared__ int4 sbuf[C][ESH][ESW];
+    int32_t (*ss)[ESH][ESW] = reinterpret_cast<int32_t (*)[ESH][ESW]>(&sbuf[0][0][0]);
+    griddep_wait();
+    griddep_launch();
+    const int X0 = (blockIdx.x + a.tx0) * ETW, Y0 = (blockIdx.y + a.ty0) * ETH;
+    const int I0 = X0 >> 1, J0 = Y0 >> 1;
+    const int qx = threadIdx.x % 32, qy = threadIdx.x / 32;
+    const int i = I0 + qx, j = J0 + qy;
+    const int X = 2 * i, Y = 2 * j;
+
+    if (a.has_coarse && interior_tile(X0, Y0, a.w, a.h, I0, J0, cl.w, cl.h)) {
+        // interior tile: no bounds, packed taps, only the expansions the seam
+        // mask of the quad selects
+        TIn wp[4][S], bp[4][S];
+        const TIn* w0 = reinterpret_cast<const TIn*>(a.white) + (int64_t)Y * a.wpitch + (int64_t)X * S;
+        const TIn* b0 = reinterpret_cast<const TIn*>(a.black) + (int64_t)Y * a.bpitch + (int64_t)X * S;
+        ld_px<TIn, S, VEC>(w0, wp[0]);
+        ld_px<TIn, S, VEC>(w0 + S, wp[1]);
+        ld_px<TIn, S, VEC>(w0 + a.wpitch, wp[2]);
+        ld_px<TIn, S, VEC>(w0 + a.wpitch + S, wp[3]);
+        ld_px<TIn, S, VEC>(b0, bp[0]);
+        ld_px<TIn, S, VEC>(b0 + S, bp[1]);
+        ld_px<TIn, S, VEC>(b0 + a.bpitch, bp[2]);
+        ld_px<TIn, S, VEC>(b0 + a.bpitch + S, bp[3]);
+        const uint8_t* m0 = a.mask + (int64_t)Y * a.mpitch + X;
+        const int32_t mk[4] = {(int32_t)__ldg(m0) << MF, (int32_t)__ldg(m0 + 1) << MF,
+                               (int32_t)__ldg(m0 + a.mpitch) << MF, (int32_t)__ldg(m0 + a.mpitch + 1) << MF};
+        stage_coarse4_interior<C, T, true, 256>(sbuf, cl, I0, J0);
+        __syncthreads();
+        out0_quad<TIn, T, C, S, AM, VEC>(a, PackedTaps{sbuf}, X, Y, qx, qy, wp, bp, mk);
+        return;
+    }
+
+    out0_border_tile<TIn, T, C, S, AM, VEC>(cl, a, X0, Y0, ss);
+}
+
 // ---------------------------------------------------------------------------
 // Level 0 on the interior tiles: persistent CTAs fed by a TMA pipeline
 // ---------------------------------------------------------------------------
@@ -404,26 +419,37 @@ __global__ void __launch_bounds__(256, 3) k_out0(CoarseLevels cl, Out0Args a)
 // out0_quad's, with the coarse taps read from the planar TMA boxes.
 
 // Tensor maps of one launch: the interleaved images as 2-D arrays of w * S
-// samples by h rows, the seam mask, and the 3C coarse planes.
+// samples by h rows and the seam mask (used when their rows start on 16-byte
+// boundaries), and the 3C coarse planes (128-byte aligned rows).
 struct Out0Maps {
     CUtensorMap white, black, mask;
     CUtensorMap coarse[9];
 };
 
-// One stage: both images' 16 rows of 64 pixels, the mask rows and, per
-// coarse plane, ESH rows of CBW samples that start XOFF samples left of the
-// tile's first coarse column I0 (a TMA box starts on a 16-byte boundary;
-// the taps used are I0-1 .. I0+32).  Every part is a multiple of 128 bytes.
-template <typename TIn, typename T, int C, int S>
+// How the fine level reaches a stage: OUT0_TMA_ROWS, one 2-D TMA box per
+// image and one for the mask rows; OUT0_CP_ASYNC, each thread copies its own
+// quad's eight pixels with cp.async (any pixel-aligned row pitch) and reads
+// its four mask bytes into registers one tile ahead.
+constexpr int OUT0_TMA_ROWS = 0, OUT0_CP_ASYNC = 1;
+
+// One stage: the fine-level pixels of both images (MODE 0: the tile's 16 rows
+// of 64 pixels; MODE 1: per quad slot q and thread, pixel slots
+// [image][q][thread]), the mask rows (MODE 0) and, per coarse plane, ESH rows
+// of CBW samples that start XOFF samples left of the tile's first coarse
+// column I0 (a TMA box starts on a 16-byte boundary; the taps used are I0-1
+// .. I0+32).  Every part is a multiple of 128 bytes.
+template <typename TIn, typename T, int C, int S, int MODE>
 struct Out0Stage {
     static constexpr int XOFF = 16 / (int)sizeof(T);
     static constexpr int CBW = (ESW - 1 + XOFF + XOFF - 1) / XOFF * XOFF;
-    static constexpr int IMG = ETH * ETW * S * (int)sizeof(TIn);
-    static constexpr int MSK = ETH * ETW;
+    static constexpr int PXB = S * (int)sizeof(TIn);
+    static constexpr int IMG = ETH * ETW * PXB;
+    static constexpr int MSK = MODE == OUT0_TMA_ROWS ? ETH * ETW : 0;
     static constexpr int PLANE_BYTES = ESH * CBW * (int)sizeof(T);
     static constexpr int PLANE = (PLANE_BYTES + 127) / 128 * 128;
     static constexpr int BYTES = 2 * IMG + MSK + 3 * C * PLANE;
-    static constexpr uint32_t TX = (uint32_t)(2 * IMG + MSK + 3 * C * PLANE_BYTES);
+    // bytes the TMA writes per stage
+    static constexpr uint32_t TX = (uint32_t)((MODE == OUT0_TMA_ROWS ? 2 * IMG + MSK : 0) + 3 * C * PLANE_BYTES);
     static_assert(IMG % 128 == 0 && MSK % 128 == 0, "stage parts stay 128-byte aligned");
 };
 
@@ -487,13 +513,68 @@ __device__ __forceinline__ void lds_pixel_pair(const TIn* p, TIn (&a)[S], TIn (&
     }
 }
 
-// Tiles t = 0 .. nbx * nby - 1 of the rectangle of tile columns bx0.. and
-// rows by0.. (all interior tiles).
-template <typename TIn, typename T, int C, int S, int AM>
-__global__ void __launch_bounds__(256, 3) k_out0_tma(const __grid_constant__ Out0Maps maps, Out0Args a, int bx0,
-                                                     int nbx, int by0, int nby)
+// One interleaved RGBA pixel from shared memory (one 8- or 4-byte access).
+template <typename TIn, int S>
+__device__ __forceinline__ void lds_pixel(const TIn* p, TIn (&a)[S])
 {
-    using St = Out0Stage<TIn, T, C, S>;
+    static_assert(S == 4, "RGBA pixels");
+    if (sizeof(TIn) == 2) {
+        const uint2 v = *reinterpret_cast<const uint2*>(p);
+        a[0] = (TIn)(v.x & 0xffffu);
+        a[1] = (TIn)(v.x >> 16);
+        a[2] = (TIn)(v.y & 0xffffu);
+        a[3] = (TIn)(v.y >> 16);
+    } else {
+        const uint32_t v = *reinterpret_cast<const uint32_t*>(p);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            a[c] = (TIn)((v >> (8 * c)) & 0xffu);
+        }
+    }
+}
+
+// The tiles of one level-0 launch over tile rows [ty0, ty0 + nty) and tile
+// columns [0, cols): the interior rectangle of columns bx0 .. bx0 + nbx - 1
+// (bx0 = 1) and rows by0 .. by0 + nby - 1, and the ring around it in the
+// band -- the first column, the columns right of the rectangle, and the band
+// rows above and below it.
+struct Out0Ring {
+    int bx0, nbx, by0, nby;  // interior rectangle
+    int ty0, nty, cols;      // band
+    __host__ __device__ int right() const { return cols - bx0 - nbx; }
+    __host__ __device__ int above() const { return by0 - ty0; }
+    __host__ __device__ int below() const { return ty0 + nty - by0 - nby; }
+    __host__ __device__ int count() const { return nty * (bx0 + right()) + nbx * (above() + below()); }
+    // tile (column, row) of ring tile t
+    __device__ void tile(int t, int& bx, int& by) const
+    {
+        const int nl = nty * bx0, nr = nty * right(), na = nbx * above();
+        if (t < nl) {
+            bx = t % bx0;
+            by = ty0 + t / bx0;
+        } else if ((t -= nl) < nr) {
+            bx = bx0 + nbx + t % right();
+            by = ty0 + t / right();
+        } else if ((t -= nr) < na) {
+            bx = bx0 + t % nbx;
+            by = ty0 + t / nbx;
+        } else {
+            t -= na;
+            bx = bx0 + t % nbx;
+            by = by0 + nby + t / nbx;
+        }
+    }
+};
+
+// The ring tiles go first, through out0_border_tile with their coarse planes
+// staged in stage 1, while the copies of the CTA's first interior tile land
+// in stage 0; then the pipelined interior tiles.
+template <typename TIn, typename T, int C, int S, int AM, int MODE>
+__global__ void __launch_bounds__(256, 3) k_out0_tma(const __grid_constant__ Out0Maps maps, CoarseLevels cl, Out0Args a,
+                                                     Out0Ring ring)
+{
+    const int bx0 = ring.bx0, nbx = ring.nbx, by0 = ring.by0, nby = ring.nby;
+    using St = Out0Stage<TIn, T, C, S, MODE>;
     constexpr int MF = sizeof(TIn) == 1 ? 7 : 15;
     extern __shared__ __align__(128) unsigned char osm[];
     __shared__ __align__(8) uint64_t bar[2];
@@ -502,59 +583,146 @@ __global__ void __launch_bounds__(256, 3) k_out0_tma(const __grid_constant__ Out
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         mbar_init_fence();
-        tma_prefetch_map(&maps.white);
-        tma_prefetch_map(&maps.black);
-        tma_prefetch_map(&maps.mask);
+        if (MODE == OUT0_TMA_ROWS) {
+            tma_prefetch_map(&maps.white);
+            tma_prefetch_map(&maps.black);
+            tma_prefetch_map(&maps.mask);
+        }
     }
     __syncthreads();
     griddep_wait();
     griddep_launch();
     const int qx = threadIdx.x % 32, qy = threadIdx.x / 32;
-    const auto issue = [&](int t, int s) {
-        const int X0 = (bx0 + t % nbx) * ETW, Y0 = (by0 + t / nbx) * ETH;
-        const int I0 = X0 >> 1, J0 = Y0 >> 1;
+    const auto origin = [&](int t, int& X0, int& Y0) {
+        X0 = (bx0 + t % nbx) * ETW;
+        Y0 = (by0 + t / nbx) * ETH;
+    };
+    // the TMA part of a tile's copies (thread 0 arms the stage's barrier,
+    // warp 0 issues)
+    const auto issue_tma = [&](int t, int s) {
+        int X0, Y0;
+        origin(t, X0, Y0);
+        const int I0 = X0 >> 1, J0 = Y0 >> 1, l = threadIdx.x;
         unsigned char* st = osm + s * St::BYTES;
-        mbar_arrive_expect_tx(&bar[s], St::TX);
-        tma_load_2d(st, &maps.white, X0 * S, Y0, &bar[s]);
-        tma_load_2d(st + St::IMG, &maps.black, X0 * S, Y0, &bar[s]);
-        tma_load_2d(st + 2 * St::IMG, &maps.mask, X0, Y0, &bar[s]);
-#pragma unroll
-        for (int q = 0; q < 3 * C; ++q) {
-            tma_load_2d(st + 2 * St::IMG + St::MSK + q * St::PLANE, &maps.coarse[q], I0 - St::XOFF, J0 - 1, &bar[s]);
+        if (l == 0) {
+            mbar_arrive_expect_tx(&bar[s], St::TX);
+            if (MODE == OUT0_TMA_ROWS) {
+                tma_load_2d(st, &maps.white, X0 * S, Y0, &bar[s]);
+                tma_load_2d(st + St::IMG, &maps.black, X0 * S, Y0, &bar[s]);
+                tma_load_2d(st + 2 * St::IMG, &maps.mask, X0, Y0, &bar[s]);
+            }
+        }
+        __syncwarp();
+        if (l < 3 * C) {
+            tma_load_2d(st + 2 * St::IMG + St::MSK + l * St::PLANE, &maps.coarse[l], I0 - St::XOFF, J0 - 1, &bar[s]);
         }
     };
+    // MODE 1: this thread's eight pixels of a tile (one commit group) and
+    // its four mask bytes
+    const auto issue_own = [&](int t, int s) {
+        int X0, Y0;
+        origin(t, X0, Y0);
+        unsigned char* st = osm + s * St::BYTES;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int64_t y = Y0 + 2 * qy + (q >> 1), x = X0 + 2 * qx + (q & 1);
+            const int slot = (q * 256 + (int)threadIdx.x) * St::PXB;
+            cp_async_bytes<St::PXB>(st + slot, reinterpret_cast<const TIn*>(a.white) + y * a.wpitch + x * S);
+            cp_async_bytes<St::PXB>(st + St::IMG + slot, reinterpret_cast<const TIn*>(a.black) + y * a.bpitch + x * S);
+        }
+        cp_async_commit();
+    };
+    const auto mask4 = [&](int t) -> uint32_t {
+        int X0, Y0;
+        origin(t, X0, Y0);
+        const uint8_t* m0 = a.mask + (int64_t)(Y0 + 2 * qy) * a.mpitch + X0 + 2 * qx;
+        return (uint32_t)__ldg(m0) | (uint32_t)__ldg(m0 + 1) << 8 | (uint32_t)__ldg(m0 + a.mpitch) << 16 |
+               (uint32_t)__ldg(m0 + a.mpitch + 1) << 24;
+    };
     int t = blockIdx.x;
-    if (threadIdx.x == 0 && t < ntiles) {
-        issue(t, 0);
+    uint32_t mreg = 0;
+    if (t < ntiles) {
+        if (threadIdx.x < 32) {
+            issue_tma(t, 0);
+        }
+        if (MODE == OUT0_CP_ASYNC) {
+            issue_own(t, 0);
+            mreg = mask4(t);
+        }
+    }
+    {
+        static_assert(St::BYTES >= (int)sizeof(int32_t) * 3 * C * ESH * ESW, "ring staging fits");
+        int32_t (*ss)[ESH][ESW] = reinterpret_cast<int32_t (*)[ESH][ESW]>(osm + St::BYTES);
+        const int nring = ring.count();
+        for (int r = blockIdx.x; r < nring; r += gridDim.x) {
+            int bx, by;
+            ring.tile(r, bx, by);
+            __syncthreads();  // the previous ring tile's readers of ss are done
+            out0_border_tile<TIn, T, C, S, AM, true>(cl, a, bx * ETW, by * ETH, ss);
+        }
+        __syncthreads();  // stage 1 is free for the copies
     }
     for (int it = 0; t < ntiles; ++it, t += gridDim.x) {
         const int s = it & 1;
         const bool next = t + (int)gridDim.x < ntiles;
-        if (threadIdx.x == 0 && next) {
+        uint32_t mnext = 0;
+        if (next) {
             // the other stage was last read before the previous barrier
-            fence_proxy_async();
-            issue(t + gridDim.x, s ^ 1);
+            if (threadIdx.x < 32) {
+                fence_proxy_async();
+                issue_tma(t + gridDim.x, s ^ 1);
+            }
+            if (MODE == OUT0_CP_ASYNC) {
+                issue_own(t + gridDim.x, s ^ 1);
+                mnext = mask4(t + gridDim.x);
+            }
         }
         const bool ok = mbar_wait_bounded(&bar[s], (uint32_t)(it >> 1) & 1u);
-        const int X = (bx0 + t % nbx) * ETW + 2 * qx, Y = (by0 + t / nbx) * ETH + 2 * qy;
+        int X0, Y0;
+        origin(t, X0, Y0);
+        const int X = X0 + 2 * qx, Y = Y0 + 2 * qy;
         const unsigned char* st = osm + s * St::BYTES;
-        const TIn* ws = reinterpret_cast<const TIn*>(st) + (2 * qy * ETW + 2 * qx) * S;
-        const TIn* bs = reinterpret_cast<const TIn*>(st + St::IMG) + (2 * qy * ETW + 2 * qx) * S;
-        const uint8_t* ms = st + 2 * St::IMG + 2 * qy * ETW + 2 * qx;
         TIn wp[4][S], bp[4][S];
-        lds_pixel_pair<TIn, S>(ws, wp[0], wp[1]);
-        lds_pixel_pair<TIn, S>(ws + ETW * S, wp[2], wp[3]);
-        lds_pixel_pair<TIn, S>(bs, bp[0], bp[1]);
-        lds_pixel_pair<TIn, S>(bs + ETW * S, bp[2], bp[3]);
-        const uint32_t m01 = *reinterpret_cast<const uint16_t*>(ms), m23 = *reinterpret_cast<const uint16_t*>(ms + ETW);
-        const int32_t mk[4] = {(int32_t)(m01 & 0xffu) << MF, (int32_t)(m01 >> 8) << MF, (int32_t)(m23 & 0xffu) << MF,
-                               (int32_t)(m23 >> 8) << MF};
+        int32_t mk[4];
+        if (MODE == OUT0_TMA_ROWS) {
+            const TIn* ws = reinterpret_cast<const TIn*>(st) + (2 * qy * ETW + 2 * qx) * S;
+            const TIn* bs = reinterpret_cast<const TIn*>(st + St::IMG) + (2 * qy * ETW + 2 * qx) * S;
+            const uint8_t* ms = st + 2 * St::IMG + 2 * qy * ETW + 2 * qx;
+            lds_pixel_pair<TIn, S>(ws, wp[0], wp[1]);
+            lds_pixel_pair<TIn, S>(ws + ETW * S, wp[2], wp[3]);
+            lds_pixel_pair<TIn, S>(bs, bp[0], bp[1]);
+            lds_pixel_pair<TIn, S>(bs + ETW * S, bp[2], bp[3]);
+            const uint32_t m01 = *reinterpret_cast<const uint16_t*>(ms);
+            const uint32_t m23 = *reinterpret_cast<const uint16_t*>(ms + ETW);
+            mreg = m01 | m23 << 16;
+        } else {
+            // this thread's own copies of this tile are complete
+            if (next) {
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int slot = (q * 256 + (int)threadIdx.x) * St::PXB;
+                lds_pixel<TIn, S>(reinterpret_cast<const TIn*>(st + slot), wp[q]);
+                lds_pixel<TIn, S>(reinterpret_cast<const TIn*>(st + St::IMG + slot), bp[q]);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            mk[q] = (int32_t)((mreg >> (8 * q)) & 0xffu) << MF;
+        }
         const PlanarTaps<T, C, St::CBW, St::PLANE / (int)sizeof(T), St::XOFF> taps{
             reinterpret_cast<const T*>(st + 2 * St::IMG + St::MSK)};
         out0_quad<TIn, T, C, S, AM, true>(a, taps, X, Y, qx, qy, wp, bp, mk);
+        mreg = mnext;
         if (!__syncthreads_and(ok)) {
             // a stage never completed: report it, let the copies of the next
             // stage (if any) land, and stop
+            if (MODE == OUT0_CP_ASYNC) {
+                cp_async_wait<0>();
+            }
             if (threadIdx.x == 0) {
                 atomicOr(a.err, 1u);
                 if (next) {
@@ -895,27 +1063,12 @@ static int sm_count()
 // The TMA level-0 kernel over the interior rectangle [bx0, bx0 + nbx) x
 // [by0, by0 + nby) of tiles; false when this format or layout has no TMA
 // path (the caller then runs k_out0 there).
-template <typename TIn, typename T, int AM>
-static bool out0_tma_launch(const CoarseLevels& cl, const Out0Args& a, int bx0, int nbx, int by0, int nby,
-                            cudaStream_t st)
+template <typename TIn, typename T, int AM, int MODE>
+static bool out0_tma_run(const Out0Maps& maps, const CoarseLevels& cl, const Out0Args& a, const Out0Ring& ring,
+                         cudaStream_t st)
 {
-    constexpr int C = 3, S = 4;
-    using St = Out0Stage<TIn, T, C, S>;
-    const CUtensorMapDataType dimg = sizeof(TIn) == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16;
-    const CUtensorMapDataType dpl = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_INT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16;
-    Out0Maps maps;
-    bool ok = map2d(&maps.white, dimg, sizeof(TIn), a.white, (int64_t)a.w * S, a.h, a.wpitch * (int64_t)sizeof(TIn),
-                    ETW * S, ETH) &&
-              map2d(&maps.black, dimg, sizeof(TIn), a.black, (int64_t)a.w * S, a.h, a.bpitch * (int64_t)sizeof(TIn),
-                    ETW * S, ETH) &&
-              map2d(&maps.mask, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, a.mask, a.w, a.h, a.mpitch, ETW, ETH);
-    for (int q = 0; ok && q < 3 * C; ++q) {
-        ok = map2d(&maps.coarse[q], dpl, sizeof(T), cl.p[q], cl.w, cl.h, cl.pitch * (int64_t)sizeof(T), St::CBW, ESH);
-    }
-    if (!ok) {
-        return false;
-    }
-    auto kern = k_out0_tma<TIn, T, C, S, AM>;
+    using St = Out0Stage<TIn, T, 3, 4, MODE>;
+    auto kern = k_out0_tma<TIn, T, 3, 4, AM, MODE>;
     static bool attr = false;
     if (!attr) {
         if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * St::BYTES) != cudaSuccess) {
@@ -924,9 +1077,37 @@ static bool out0_tma_launch(const CoarseLevels& cl, const Out0Args& a, int bx0, 
         }
         attr = true;
     }
-    const int grid = std::min(nbx * nby, 3 * sm_count());
-    return launch_pdl_smem(kern, dim3((unsigned)grid), dim3(256), (size_t)(2 * St::BYTES), st, maps, a, bx0, nbx, by0,
-                           nby) == cudaSuccess;
+    const int grid = std::min(ring.nbx * ring.nby, 3 * sm_count());
+    return launch_pdl_smem(kern, dim3((unsigned)grid), dim3(256), (size_t)(2 * St::BYTES), st, maps, cl, a, ring) ==
+           cudaSuccess;
+}
+
+// The level-0 kernel with the TMA pipeline over the interior rectangle and
+// the ring of the band; false when the coarse planes do not meet the TMA
+// rules (the caller then runs k_out0).  Images and mask go through 2-D TMA
+// boxes when their rows start on 16-byte boundaries, else through
+// per-thread cp.async copies.
+template <typename TIn, typename T, int AM>
+static bool out0_tma_launch(const CoarseLevels& cl, const Out0Args& a, const Out0Ring& ring, cudaStream_t st)
+{
+    constexpr int C = 3, S = 4;
+    using St0 = Out0Stage<TIn, T, C, S, OUT0_TMA_ROWS>;
+    const CUtensorMapDataType dimg = sizeof(TIn) == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16;
+    const CUtensorMapDataType dpl = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_INT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16;
+    Out0Maps maps;
+    for (int q = 0; q < 3 * C; ++q) {
+        if (!map2d(&maps.coarse[q], dpl, sizeof(T), cl.p[q], cl.w, cl.h, cl.pitch * (int64_t)sizeof(T), St0::CBW,
+                   ESH)) {
+            return false;
+        }
+    }
+    const bool rows = map2d(&maps.white, dimg, sizeof(TIn), a.white, (int64_t)a.w * S, a.h,
+                            a.wpitch * (int64_t)sizeof(TIn), ETW * S, ETH) &&
+                      map2d(&maps.black, dimg, sizeof(TIn), a.black, (int64_t)a.w * S, a.h,
+                            a.bpitch * (int64_t)sizeof(TIn), ETW * S, ETH) &&
+                      map2d(&maps.mask, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, a.mask, a.w, a.h, a.mpitch, ETW, ETH);
+    return rows ? out0_tma_run<TIn, T, AM, OUT0_TMA_ROWS>(maps, cl, a, ring, st)
+                : out0_tma_run<TIn, T, AM, OUT0_CP_ASYNC>(maps, cl, a, ring, st);
 }
 
 cudaError_t launch_out0(const PlanarView* gw1, const PlanarView* gb1, const PlanarView* r1, const Out0Host& h,
@@ -989,15 +1170,10 @@ cudaError_t launch_out0(const PlanarView* gw1, const PlanarView* gb1, const Plan
         return cudaSuccess;
     }
     // k_out0 over the rectangle [tx0, tx0 + ncol) x [ry0, ry0 + nrow) of tiles
-    int kernels = 0;
     const auto legacy = [&](int tx0, int ncol, int ry0, int nrow) -> cudaError_t {
-        if (ncol <= 0 || nrow <= 0) {
-            return cudaSuccess;
-        }
         Out0Args b = a;
         b.tx0 = tx0;
         b.ty0 = ry0;
-        ++kernels;
         Out0Launch l{cl, b, dim3((unsigned)ncol, (unsigned)nrow), st};
         return dispatch_pixels(wv.dtype, wv.C, wv.stride, am, vec, l);
     };
@@ -1008,31 +1184,22 @@ cudaError_t launch_out0(const PlanarView* gw1, const PlanarView* gb1, const Plan
     bool tma = false;
     if (bx1 >= 1 && iy1 >= iy0 && vec && wv.C == 3 && wv.stride == 4 && h.err &&
         (wv.dtype == ENB_U16 || wv.dtype == ENB_U8)) {
-        const int nbx = bx1, nby = iy1 - iy0 + 1;
+        const Out0Ring ring{1, bx1, iy0, iy1 - iy0 + 1, ty0, nty, cols};
         if (wv.dtype == ENB_U16) {
-            tma = am == 0   ? out0_tma_launch<uint16_t, int32_t, 0>(cl, a, 1, nbx, iy0, nby, st)
-                  : am == 1 ? out0_tma_launch<uint16_t, int32_t, 1>(cl, a, 1, nbx, iy0, nby, st)
-                            : out0_tma_launch<uint16_t, int32_t, 2>(cl, a, 1, nbx, iy0, nby, st);
+            tma = am == 0   ? out0_tma_launch<uint16_t, int32_t, 0>(cl, a, ring, st)
+                  : am == 1 ? out0_tma_launch<uint16_t, int32_t, 1>(cl, a, ring, st)
+                            : out0_tma_launch<uint16_t, int32_t, 2>(cl, a, ring, st);
         } else {
-            tma = am == 0   ? out0_tma_launch<uint8_t, int16_t, 0>(cl, a, 1, nbx, iy0, nby, st)
-                  : am == 1 ? out0_tma_launch<uint8_t, int16_t, 1>(cl, a, 1, nbx, iy0, nby, st)
-                            : out0_tma_launch<uint8_t, int16_t, 2>(cl, a, 1, nbx, iy0, nby, st);
+            tma = am == 0   ? out0_tma_launch<uint8_t, int16_t, 0>(cl, a, ring, st)
+                  : am == 1 ? out0_tma_launch<uint8_t, int16_t, 1>(cl, a, ring, st)
+                            : out0_tma_launch<uint8_t, int16_t, 2>(cl, a, ring, st);
         }
     }
-    cudaError_t e = cudaSuccess;
     if (tma) {
-        ++kernels;
-        // the border ring of the band around the interior rectangle
-        const cudaError_t r[4] = {legacy(0, 1, ty0, nty), legacy(bx1 + 1, cols - bx1 - 1, ty0, nty),
-                                  legacy(1, bx1, ty0, iy0 - ty0), legacy(1, bx1, iy1 + 1, ty0 + nty - 1 - iy1)};
-        for (cudaError_t x : r) {
-            e = e == cudaSuccess ? x : e;
-        }
-    } else {
-        e = legacy(0, cols, ty0, nty);
+        last_launch().name = "out0_tma";
+        return cudaSuccess;
     }
-    last_launch().kernels = kernels;
-    return e;
+    return legacy(0, cols, ty0, nty);
 }
 
 }  // namespace enb

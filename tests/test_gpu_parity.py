@@ -332,15 +332,17 @@ def test_enblend_alpha_sources(ctx, orc, plain):
 @pytest.mark.parametrize("dt", [np.uint8, np.uint16])
 @pytest.mark.parametrize("wrap", [False, True])
 @pytest.mark.parametrize("planes", [False, True])
-def test_enblend_level0_tma(ctx, orc, dt, wrap, planes):
-    """Canvas rows on 16-byte boundaries (width 640): the interior tiles of
-    level 0 take the TMA pipeline (four more launches for the border ring
-    than on a 641-wide canvas), alpha from the 4th component or from planes,
-    against the oracle; the host-buffer entry point runs it per output band
-    (1100 rows)."""
+@pytest.mark.parametrize("off", [240, 241])
+def test_enblend_level0_tma(ctx, orc, dt, wrap, planes, off):
+    """RGBA level 0 through the TMA pipeline (profile name out0_tma), on
+    canvases whose rows start on 16-byte boundaries (width 640) and off them
+    (641: every row box starts before its first pixel), alpha from the 4th
+    component or from planes, against the oracle; the host-buffer entry
+    point runs it per output band (1100 rows).  RGB images take the tile
+    kernel (out0)."""
     from enbgpu import synthetic
     h = 1100 if planes else 300
-    white, black, mask = synthetic.panorama_pair(h, 400, 240, dt, seed=43)
+    white, black, mask = synthetic.panorama_pair(h, 400, off, dt, seed=43)
     mask[40:200, 250:300] = 111
     kw, dkw = {}, {}
     if planes:
@@ -349,21 +351,27 @@ def test_enblend_level0_tma(ctx, orc, dt, wrap, planes):
         kw = dict(white_alpha=wa, black_alpha=ba)
         dkw = dict(white_alpha=_dev(wa), black_alpha=_dev(ba))
     ref = orc.enblend(white, black, mask, wrap=wrap, seed=8, want_level0=True, **kw)
-    l0 = torch.zeros((h, 640, 3), dtype=torch.int32, device="cuda")
-    n0 = ctx.launches
+    l0 = torch.zeros((h, 400 + off, 3), dtype=torch.int32, device="cuda")
+    ctx.profile(True)
     out, oa = ctx.enblend(_dev(white), _dev(black), _dev(mask), wrap=wrap, seed=8, level0=l0, **dkw)
-    n_tma = ctx.launches - n0
+    names = set(ctx.profile_report())
+    ctx.profile(False)
+    assert "out0_tma" in names and "out0" not in names
     assert np.array_equal(l0.cpu().numpy(), ref["level0"])
     assert np.array_equal(out.cpu().numpy(), ref["out"])
     assert np.array_equal(oa.cpu().numpy(), ref["alpha"])
     out2, oa2 = ctx.enblend(white, black, mask, wrap=wrap, seed=8, **kw)
     assert np.array_equal(out2, ref["out"])
     assert np.array_equal(oa2, ref["alpha"])
-    # the same scene one pixel wider: rows off the 16-byte grid, one level-0 launch
-    w1, b1, m1 = synthetic.panorama_pair(h, 400, 241, dt, seed=43)
-    n0 = ctx.launches
-    ctx.enblend(_dev(w1), _dev(b1), _dev(m1), wrap=wrap, seed=8)
-    assert n_tma == ctx.launches - n0 + 4
+    if not planes:
+        rgb_w, rgb_b = np.ascontiguousarray(white[..., :3]), np.ascontiguousarray(black[..., :3])
+        ref = orc.enblend(rgb_w, rgb_b, mask, wrap=wrap, seed=8)
+        ctx.profile(True)
+        out, _ = ctx.enblend(_dev(rgb_w), _dev(rgb_b), _dev(mask), wrap=wrap, seed=8)
+        names = set(ctx.profile_report())
+        ctx.profile(False)
+        assert "out0" in names and "out0_tma" not in names
+        assert np.array_equal(out.cpu().numpy(), ref["out"])
 
 
 def test_enblend_in_place(ctx, orc):
