@@ -151,6 +151,9 @@ enb_status enb_create(int device, enb_ctx** ctx);
 enb_status enb_destroy(enb_ctx* ctx);
 /* Queue all later work on `cuda_stream` (a cudaStream_t; NULL = legacy default). */
 enb_status enb_set_stream(enb_ctx* ctx, void* cuda_stream);
+/* Wait for the context's stream.  ENB_ERR_CUDA also when a kernel queued
+ * since the last synchronisation gave up a bounded wait for its tile copies
+ * (the level-0 pipeline of enb_enblend); enb_last_error says which. */
 enb_status enb_synchronize(enb_ctx* ctx);
 /* Message of the last failed call on this context (never NULL). */
 const char* enb_last_error(const enb_ctx* ctx);
