@@ -428,13 +428,14 @@ struct Out0Maps {
 
 // How the fine level reaches a stage: OUT0_TMA_ROWS, one 2-D TMA box per
 // image and one for the mask rows; OUT0_CP_ASYNC, each thread copies its own
-// quad's eight pixels with cp.async (any pixel-aligned row pitch) and reads
-// its four mask bytes into registers one tile ahead.
+// quad's eight pixels with cp.async, a row's pixel pair in one copy where it
+// is aligned to its size (any pixel-aligned row pitch), and reads its four
+// mask bytes into registers one tile ahead.
 constexpr int OUT0_TMA_ROWS = 0, OUT0_CP_ASYNC = 1;
 
 // One stage: the fine-level pixels of both images (MODE 0: the tile's 16 rows
-// of 64 pixels; MODE 1: per quad slot q and thread, pixel slots
-// [image][q][thread]), the mask rows (MODE 0) and, per coarse plane, ESH rows
+// of 64 pixels; MODE 1: pixel-pair slots [image][quad row][thread]), the mask
+// rows (MODE 0) and, per coarse plane, ESH rows
 // of CBW samples that start XOFF samples left of the tile's first coarse
 // column I0 (a TMA box starts on a 16-byte boundary; the taps used are I0-1
 // .. I0+32).  Every part is a multiple of 128 bytes.
@@ -509,26 +510,6 @@ __device__ __forceinline__ void lds_pixel_pair(const TIn* p, TIn (&a)[S], TIn (&
         for (int c = 0; c < 4; ++c) {
             a[c] = (TIn)((v.x >> (8 * c)) & 0xffu);
             b[c] = (TIn)((v.y >> (8 * c)) & 0xffu);
-        }
-    }
-}
-
-// One interleaved RGBA pixel from shared memory (one 8- or 4-byte access).
-template <typename TIn, int S>
-__device__ __forceinline__ void lds_pixel(const TIn* p, TIn (&a)[S])
-{
-    static_assert(S == 4, "RGBA pixels");
-    if (sizeof(TIn) == 2) {
-        const uint2 v = *reinterpret_cast<const uint2*>(p);
-        a[0] = (TIn)(v.x & 0xffffu);
-        a[1] = (TIn)(v.x >> 16);
-        a[2] = (TIn)(v.y & 0xffffu);
-        a[3] = (TIn)(v.y >> 16);
-    } else {
-        const uint32_t v = *reinterpret_cast<const uint32_t*>(p);
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            a[c] = (TIn)((v >> (8 * c)) & 0xffu);
         }
     }
 }
@@ -623,12 +604,22 @@ __global__ void __launch_bounds__(256, 3) k_out0_tma(const __grid_constant__ Out
         int X0, Y0;
         origin(t, X0, Y0);
         unsigned char* st = osm + s * St::BYTES;
+        // the two pixels of a quad row: one copy when the pair is aligned to
+        // its size (on the rows that start on such a boundary), else two
+        const auto pair = [&](unsigned char* dst, const TIn* src) {
+            if (((uintptr_t)src & (2 * St::PXB - 1)) == 0) {
+                cp_async_bytes<2 * St::PXB>(dst, src);
+            } else {
+                cp_async_bytes<St::PXB>(dst, src);
+                cp_async_bytes<St::PXB>(dst + St::PXB, src + S);
+            }
+        };
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int64_t y = Y0 + 2 * qy + (q >> 1), x = X0 + 2 * qx + (q & 1);
-            const int slot = (q * 256 + (int)threadIdx.x) * St::PXB;
-            cp_async_bytes<St::PXB>(st + slot, reinterpret_cast<const TIn*>(a.white) + y * a.wpitch + x * S);
-            cp_async_bytes<St::PXB>(st + St::IMG + slot, reinterpret_cast<const TIn*>(a.black) + y * a.bpitch + x * S);
+        for (int h = 0; h < 2; ++h) {
+            const int64_t y = Y0 + 2 * qy + h, x = X0 + 2 * qx;
+            const int slot = (h * 256 + (int)threadIdx.x) * 2 * St::PXB;
+            pair(st + slot, reinterpret_cast<const TIn*>(a.white) + y * a.wpitch + x * S);
+            pair(st + St::IMG + slot, reinterpret_cast<const TIn*>(a.black) + y * a.bpitch + x * S);
         }
         cp_async_commit();
     };
@@ -703,10 +694,10 @@ __global__ void __launch_bounds__(256, 3) k_out0_tma(const __grid_constant__ Out
                 cp_async_wait<0>();
             }
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int slot = (q * 256 + (int)threadIdx.x) * St::PXB;
-                lds_pixel<TIn, S>(reinterpret_cast<const TIn*>(st + slot), wp[q]);
-                lds_pixel<TIn, S>(reinterpret_cast<const TIn*>(st + St::IMG + slot), bp[q]);
+            for (int h = 0; h < 2; ++h) {
+                const int slot = (h * 256 + (int)threadIdx.x) * 2 * St::PXB;
+                lds_pixel_pair<TIn, S>(reinterpret_cast<const TIn*>(st + slot), wp[2 * h], wp[2 * h + 1]);
+                lds_pixel_pair<TIn, S>(reinterpret_cast<const TIn*>(st + St::IMG + slot), bp[2 * h], bp[2 * h + 1]);
             }
         }
 #pragma unroll

@@ -63,12 +63,12 @@ __device__ __forceinline__ void tma_load_1d(void* dst, const CUtensorMap* map, i
         : "memory");
 }
 
-// Per-thread asynchronous copies of 4 or 8 bytes (naturally aligned) into
-// shared memory, completed per commit group.
+// Per-thread asynchronous copies of 4, 8 or 16 bytes (naturally aligned)
+// into shared memory, completed per commit group.
 template <int N>
 __device__ __forceinline__ void cp_async_bytes(void* dst, const void* src)
 {
-    static_assert(N == 4 || N == 8, "cp.async.ca copies 4, 8 or 16 bytes");
+    static_assert(N == 4 || N == 8 || N == 16, "cp.async.ca copies 4, 8 or 16 bytes");
     asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(smem_addr(dst)), "l"(src), "n"(N) : "memory");
 }
 
