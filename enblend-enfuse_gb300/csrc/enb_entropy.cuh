@@ -206,8 +206,10 @@ __device__ __forceinline__ void repeat_tables_clear(uint32_t* table, uint8_t* fl
     }
 }
 
-// Marks of a complete tile (all threads call; ends with a barrier).  Pixel
-// p is handled by thread p % blockDim.x.  NP > 0 (npx <= NP * blockDim.x):
+// Marks of a complete tile (all threads call after the barrier that
+// completes the tile; the tables were emptied before that barrier by
+// repeat_tables_clear; ends with a barrier).  Pixel p is handled by thread
+// p % blockDim.x.  NP > 0 (npx <= NP * blockDim.x):
 // the keys of a thread probe in lock step, one CAS per pending key a round,
 // so its NP * C insertions are in flight together, and the slot where each
 // key ended up is kept, so that its flag is read without probing again;
@@ -219,7 +221,6 @@ __device__ __forceinline__ void mark_repeats(const float* raw, int plane, const 
                                              uint32_t* table, uint8_t* flags, int slots, uint64_t* cnt)
 {
     const int shift = 32 - (31 - __clz(slots));
-    repeat_tables_clear(table, flags, C, slots);
     if (NP > 0) {
         constexpr int N = NP > 0 ? NP : 1;
         uint32_t kk[N][3], h[N][3];
@@ -238,7 +239,6 @@ __device__ __forceinline__ void mark_repeats(const float* raw, int plane, const 
             }
         }
         const uint32_t hashed = pend;
-        __syncthreads();
         for (int round = 0; pend && round < slots; ++round) {
 #pragma unroll
             for (int j = 0; j < N; ++j) {
@@ -278,7 +278,6 @@ __device__ __forceinline__ void mark_repeats(const float* raw, int plane, const 
         __syncthreads();
         return;
     }
-    __syncthreads();
     for (int p = threadIdx.x; p < npx; p += blockDim.x) {
         if (!a[p]) {
             continue;

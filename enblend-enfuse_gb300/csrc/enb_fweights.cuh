@@ -226,14 +226,19 @@ __device__ __forceinline__ void ftile_fetch_px(float (&rgb)[3], uint8_t& a, cons
 }
 
 // Loads the tile whose top-left input pixel is (x0, y0) (all threads call;
-// ends with the tile and its repeat marks complete in shared memory).
-// alpha == nullptr: opaque.  Returns nonzero when every tile pixel is
-// opaque (and inside the image).
+// ends with the tile and its repeat marks complete in shared memory; the
+// tile and its tables must be out of use since the block's previous
+// barrier).  alpha == nullptr: opaque.  Returns nonzero when every tile
+// pixel is opaque (and inside the image).
 __device__ __forceinline__ int ftile_load(const FTile& t, const FloatWeightParams& wp, const float* img, int64_t pitch,
                                           int stride, int w, int h, int C, const uint8_t* alpha, int64_t apitch,
                                           int x0, int y0)
 {
     const int TW = t.TW, TT = TW * TW;
+    if (t.slots) {
+        // the tables were last read before the block's previous barrier
+        repeat_tables_clear(t.table, t.flags, C, t.slots);
+    }
     // tile pixel k = r * TW + c, walked with a stride of blockDim.x
     const int dr = (int)blockDim.x / TW, dc = (int)blockDim.x - dr * TW;
     int r = (int)threadIdx.x / TW, c = (int)threadIdx.x - r * TW;
