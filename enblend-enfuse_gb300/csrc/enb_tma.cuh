@@ -52,17 +52,6 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
         : "memory");
 }
 
-// 1-D tiled load of the box starting at element x of the tensor map (x *
-// element size a multiple of 16 bytes) into dst, completing on bar.
-__device__ __forceinline__ void tma_load_1d(void* dst, const CUtensorMap* map, int x, uint64_t* bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.1d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2}], [%3];" ::"r"(
-            smem_addr(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(smem_addr(bar))
-        : "memory");
-}
-
 // Per-thread asynchronous copies of 4, 8 or 16 bytes (naturally aligned)
 // into shared memory, completed per commit group.
 template <int N>
