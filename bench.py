@@ -226,8 +226,9 @@ def batched_fuse(ctx, stream, n_stacks: int, reps: int = 3) -> dict:
     log-uniform in [512, 4096], 3..7 exposures, EVs evenly spaced over
     +-(count - 1) stops, weights exposure 1.0 / saturation 0.2 / contrast 0.5
     (5x5) / entropy 0.3 (5x5) in normalised-float mode; enb_fuse_stacks (one
-    CUDA graph) against the plain per-stack path (enb_enfuse per stack) on
-    the same GPU, device-resident inputs."""
+    CUDA graph, level schedule from enb_fuse_stacks_tune) against the plain
+    per-stack path (enb_enfuse per stack) on the same GPU, device-resident
+    inputs."""
     import torch
     import enbgpu
     from enbgpu import synthetic
@@ -249,6 +250,9 @@ def batched_fuse(ctx, stream, n_stacks: int, reps: int = 3) -> dict:
         torch.cuda.synchronize()
         return a.elapsed_time(b) / n
 
+    # the level schedule (coarse threshold) from measured times; the timed
+    # calls below use it (coarse_pixels=0)
+    tune = ctx.tune_stacks(stacks, params=prm, outs=outs, reps=2)
     l0 = ctx.launches
     batched_ms = timed(lambda: ctx.fuse_stacks(stacks, params=prm, outs=outs), reps)
     launches = (ctx.launches - l0) // (reps + 1)
@@ -270,7 +274,8 @@ def batched_fuse(ctx, stream, n_stacks: int, reps: int = 3) -> dict:
                     "normalised-float mode (float_range 1.0)",
         "units": units, "metric": METRIC,
         "batched": {"value": units / (batched_ms / 1e3), "ms_per_step": batched_ms, "graph": True,
-                    "launches_per_step": launches},
+                    "launches_per_step": launches, "coarse_pixels": tune["best"],
+                    "tuned_ms": {str(k): round(v, 3) for k, v in tune["ms"].items()}},
         "plain": {"value": units / (plain_ms / 1e3), "ms_per_step": plain_ms,
                   "what": "enb_enfuse stack by stack (the per-stack path)"},
         "speedup": plain_ms / batched_ms,

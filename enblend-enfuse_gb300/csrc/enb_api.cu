@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <functional>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -80,6 +81,8 @@ struct enb_ctx {
     // device error word of the kernels' bounded waits (bit 0: a TMA tile
     // pipeline wait timed out); read after synchronisations
     unsigned int* dev_err = nullptr;
+    // coarse thresholds chosen by enb_fuse_stacks_tune, per batch geometry
+    std::map<std::string, int32_t> tuned;
 };
 
 struct enb_pyramid {
@@ -1908,6 +1911,28 @@ static enb_status float_weight_params(enb_ctx* ctx, const enb_enfuse_params* prm
     return ENB_OK;
 }
 
+// What the batched fuse's work depends on: the stacks' sizes, exposure
+// counts and channels, the parameters and the options (not the buffers).
+static std::string batch_geometry_key(const enb_enfuse_params* prm, int n, const enb_stack* stacks,
+                                      const enb_fuse_options& o)
+{
+    std::string key;
+    const auto put = [&key](const void* p, size_t b) { key.append((const char*)p, b); };
+    put(&n, sizeof n);
+    put(prm, sizeof *prm);
+    put(&o.levels, sizeof o.levels);
+    put(&o.wrap, sizeof o.wrap);
+    put(&o.hard_mask, sizeof o.hard_mask);
+    for (int i = 0; i < n; ++i) {
+        const enb_image& im = stacks[i].images[0];
+        const int32_t g[4] = {stacks[i].K, im.width, im.height, im.channels};
+        put(g, sizeof g);
+        const int32_t a = stacks[i].alphas ? 1 : 0;
+        put(&a, sizeof a);
+    }
+    return key;
+}
+
 enb_status enb_fuse_stacks(enb_ctx* ctx, const enb_enfuse_params* prm, int n, const enb_stack* stacks,
                            const enb_fuse_options* opt)
 {
@@ -1957,7 +1982,12 @@ enb_status enb_fuse_stacks(enb_ctx* ctx, const enb_enfuse_params* prm, int n, co
     }
     FloatWeightParams wp;
     ENB_TRY(float_weight_params(ctx, prm, wp));
-    const int64_t coarse = o.coarse_pixels == 0 ? 4096 : (o.coarse_pixels < 0 ? 0 : o.coarse_pixels);
+    int32_t cp = o.coarse_pixels;
+    if (cp == 0) {
+        const auto it = ctx->tuned.find(batch_geometry_key(prm, n, stacks, o));
+        cp = it != ctx->tuned.end() ? it->second : 4096;
+    }
+    const int64_t coarse = cp < 0 ? 0 : cp;
     // cache key: every descriptor, the parameters and the options
     std::string key;
     auto put = [&key](const void* p, size_t b) { key.append((const char*)p, b); };
@@ -2155,6 +2185,76 @@ enb_status enb_fuse_stacks(enb_ctx* ctx, const enb_enfuse_params* prm, int n, co
 }
 
 // ---- adjoint ----------------------------------------------------------------
+
+enb_status enb_fuse_stacks_tune(enb_ctx* ctx, const enb_enfuse_params* prm, int n, const enb_stack* stacks,
+                                const enb_fuse_options* opt, const int32_t* candidates, int n_candidates, int reps,
+                                float* times_ms, int32_t* best)
+{
+    if (!ctx) {
+        return ENB_ERR_INVALID;
+    }
+    static const int32_t kDefault[] = {-1, 1024, 4096, 16384, 65536};
+    if (!candidates) {
+        candidates = kDefault;
+        n_candidates = (int)(sizeof kDefault / sizeof kDefault[0]);
+    }
+    ENB_CHECK(ctx, n_candidates >= 1 && reps >= 1, "fuse_stacks_tune: need candidates and reps >= 1");
+    enb_fuse_options o;
+    enb_default_fuse_options(&o);
+    if (opt) {
+        o = *opt;
+    }
+    ENB_CHECK(ctx, !o.plain && !o.host_buffers, "fuse_stacks_tune: tunes the batched device path");
+    for (int c = 0; c < n_candidates; ++c) {
+        ENB_CHECK(ctx, candidates[c] != 0, "fuse_stacks_tune: a candidate of 0 pixels means 'tuned'");
+    }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ENB_CUDA(ctx, cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return cuda_fail(ctx, cudaGetLastError(), "cudaEventCreate");
+    }
+    enb_status st = ENB_OK;
+    float best_ms = 0.0f;
+    int32_t best_cp = candidates[0];
+    for (int c = 0; c < n_candidates && st == ENB_OK; ++c) {
+        enb_fuse_options co = o;
+        co.coarse_pixels = candidates[c];
+        st = enb_fuse_stacks(ctx, prm, n, stacks, &co);  // builds the plan and graph
+        cudaEventRecord(e0, ctx->stream);
+        for (int r = 0; st == ENB_OK && r < reps; ++r) {
+            st = enb_fuse_stacks(ctx, prm, n, stacks, &co);
+        }
+        if (st != ENB_OK) {
+            break;
+        }
+        cudaEventRecord(e1, ctx->stream);
+        if (cudaEventSynchronize(e1) != cudaSuccess) {
+            st = cuda_fail(ctx, cudaGetLastError(), "cudaEventSynchronize");
+            break;
+        }
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        ms /= (float)reps;
+        if (times_ms) {
+            times_ms[c] = ms;
+        }
+        if (c == 0 || ms < best_ms) {
+            best_ms = ms;
+            best_cp = candidates[c];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st != ENB_OK) {
+        return st;
+    }
+    ctx->tuned[batch_geometry_key(prm, n, stacks, o)] = best_cp;
+    if (best) {
+        *best = best_cp;
+    }
+    return check_device_error(ctx);
+}
 
 enb_status enb_fuse_grad(enb_ctx* ctx, const enb_enfuse_params* prm, int K, const enb_image* images,
                          const enb_image* logits, const enb_image* target, const enb_image* out,

@@ -123,6 +123,9 @@ _SIGNATURES = {
                                       _IMG, _P(EnbFuseGradResult), _P(EnbFuseOptions)]),
     "enb_fuse_stacks": (ctypes.c_int, [ctypes.c_void_p, _P(EnbEnfuseParams), ctypes.c_int, _P(EnbStack),
                                         _P(EnbFuseOptions)]),
+    "enb_fuse_stacks_tune": (ctypes.c_int, [ctypes.c_void_p, _P(EnbEnfuseParams), ctypes.c_int, _P(EnbStack),
+                                            _P(EnbFuseOptions), _P(ctypes.c_int32), ctypes.c_int, ctypes.c_int,
+                                            _P(ctypes.c_float), _P(ctypes.c_int32)]),
     "enb_enblend": (ctypes.c_int, [ctypes.c_void_p, _IMG, _IMG, _IMG, _IMG, _IMG, _IMG, _IMG,
                                    _P(EnbFuseOptions)]),
 }
@@ -446,16 +449,7 @@ class Context:
                                         ctypes.byref(o)))
         return out, out_alpha
 
-    def fuse_stacks(self, stacks, params: Optional[EnbEnfuseParams] = None, outs=None, out_alphas=None,
-                    alphas=None, levels: int = 0, wrap: bool = False, hard_mask: bool = False, plain: bool = False,
-                    graph: bool = True, coarse_pixels: int = 0):
-        """Batched enfuse of independent float stacks (enb_fuse_stacks).  stacks: list of lists of (H, W, S)
-        float32 arrays (numpy: host buffers; torch: device).  Returns the list of outputs (and fills out_alphas
-        when given)."""
-        host = not _is_torch(stacks[0][0])
-        if outs is None:
-            outs = [np.zeros_like(st[0]) if host else st[0].new_zeros(st[0].shape) for st in stacks]
-        keep = []
+    def _stack_descs(self, stacks, outs, out_alphas, alphas, keep):
         descs = (EnbStack * len(stacks))()
         for i, st in enumerate(stacks):
             imgs = (EnbImage * len(st))(*[pixel_image(x) for x in st])
@@ -468,6 +462,40 @@ class Context:
             descs[i].alphas = ctypes.cast(al, ctypes.POINTER(EnbImage)) if al is not None else None
             descs[i].out = ctypes.pointer(out)
             descs[i].out_alpha = ctypes.pointer(oa) if oa is not None else None
+        return descs
+
+    def tune_stacks(self, stacks, params: Optional[EnbEnfuseParams] = None, outs=None, alphas=None,
+                    candidates=None, reps: int = 2, levels: int = 0, wrap: bool = False,
+                    hard_mask: bool = False) -> dict:
+        """Autotune the level schedule of the batched fuse on these device stacks (enb_fuse_stacks_tune):
+        {"best": threshold, "ms": {threshold: ms per call}}.  Later fuse_stacks calls on batches of this
+        geometry with coarse_pixels=0 use the chosen threshold."""
+        if outs is None:
+            outs = [st[0].new_zeros(st[0].shape) for st in stacks]
+        keep = []
+        descs = self._stack_descs(stacks, outs, None, alphas, keep)
+        p = params if params is not None else enfuse_params()
+        o = self._options(levels, wrap, hard_mask, "hash", 0, False, None)
+        cands = list(candidates) if candidates is not None else [-1, 1024, 4096, 16384, 65536]
+        carr = (ctypes.c_int32 * len(cands))(*cands)
+        times = (ctypes.c_float * len(cands))()
+        best = ctypes.c_int32()
+        self._check(self.lib.enb_fuse_stacks_tune(self.handle, ctypes.byref(p), len(stacks), descs, ctypes.byref(o),
+                                                  carr, len(cands), reps, times, ctypes.byref(best)))
+        del keep
+        return {"best": int(best.value), "ms": {c: float(t) for c, t in zip(cands, times)}}
+
+    def fuse_stacks(self, stacks, params: Optional[EnbEnfuseParams] = None, outs=None, out_alphas=None,
+                    alphas=None, levels: int = 0, wrap: bool = False, hard_mask: bool = False, plain: bool = False,
+                    graph: bool = True, coarse_pixels: int = 0):
+        """Batched enfuse of independent float stacks (enb_fuse_stacks).  stacks: list of lists of (H, W, S)
+        float32 arrays (numpy: host buffers; torch: device).  Returns the list of outputs (and fills out_alphas
+        when given).  coarse_pixels=0: the threshold tune_stacks chose for this batch geometry, else 64x64."""
+        host = not _is_torch(stacks[0][0])
+        if outs is None:
+            outs = [np.zeros_like(st[0]) if host else st[0].new_zeros(st[0].shape) for st in stacks]
+        keep = []
+        descs = self._stack_descs(stacks, outs, out_alphas, alphas, keep)
         p = params if params is not None else enfuse_params()
         o = self._options(levels, wrap, hard_mask, "hash", 0, host, None, plain, coarse_pixels)
         o.graph = int(graph)

@@ -136,7 +136,8 @@ typedef struct {
                               (none), < 0: every level in its own launches.
                               enb_fuse_stacks: levels of at most this many
                               pixels run in the persistent coarse kernel;
-                              0: default (64 x 64), < 0: none */
+                              0: the threshold enb_fuse_stacks_tune chose for
+                              the batch geometry, else 64 x 64; < 0: none */
     int32_t graph;         /* enb_fuse_stacks: 1 (default) replays a CUDA
                               graph of the launch sequence, captured once per
                               batch geometry; 0 launches directly */
@@ -310,6 +311,22 @@ typedef struct {
  * geometry stay cached in the context. */
 enb_status enb_fuse_stacks(enb_ctx* ctx, const enb_enfuse_params* params, int n_stacks, const enb_stack* stacks,
                            const enb_fuse_options* opt);
+
+/* Autotuner of the batched fuse's level schedule (which levels run in the
+ * persistent coarse kernel, which in per-level launches): runs
+ * enb_fuse_stacks on this batch once per candidate coarse threshold to warm
+ * up and then `reps` times under CUDA events, and keeps the fastest for the
+ * batch's geometry (stack sizes and exposure counts, parameters, options;
+ * not the buffers).  Later enb_fuse_stacks calls on a batch of that
+ * geometry with opt->coarse_pixels == 0 use it.  candidates: n_candidates
+ * thresholds in pixels (< 0: no coarse kernel), or NULL for the built-in
+ * list {-1, 1024, 4096, 16384, 65536}; times_ms (optional) receives the
+ * mean milliseconds per call of each candidate, best the chosen threshold.
+ * The outputs hold the last call's result (every schedule gives the same
+ * bits). */
+enb_status enb_fuse_stacks_tune(enb_ctx* ctx, const enb_enfuse_params* params, int n_stacks, const enb_stack* stacks,
+                                const enb_fuse_options* opt, const int32_t* candidates, int n_candidates, int reps,
+                                float* times_ms, int32_t* best);
 
 /* ---- adjoint (no counterpart in the reference) --------------------------- */
 /* Loss and gradients of the float enfuse against a target image. */

@@ -116,3 +116,25 @@ def test_batch_reference_mode_weights(ctx, orc):
     for i, st in enumerate(stacks):
         ref = orc.enfuse_f(st, prm=orc.params(**kw), range_=orc.FLT_MAX)
         _close(outs[i].cpu().numpy(), ref["out"], 1e-4, 1e-5, f"stack {i}")
+
+
+def test_level_schedule_autotuner(ctx):
+    """enb_fuse_stacks_tune times each candidate coarse threshold, keeps the
+    fastest for the batch geometry, and later default calls on a batch of
+    that geometry (other buffers) use it; every schedule gives the same bits."""
+    stacks = _batch(seed=13)
+    dev = [[_dev(x) for x in st] for st in stacks]
+    p = _params()
+    ref = [o.clone() for o in ctx.fuse_stacks(dev, params=p, coarse_pixels=-1)]
+    cands = [-1, 256, 4096]
+    r = ctx.tune_stacks(dev, params=p, candidates=cands, reps=1)
+    assert r["best"] in cands and set(r["ms"]) == set(cands)
+    assert all(t > 0 for t in r["ms"].values())
+    assert r["ms"][r["best"]] == min(r["ms"].values())
+    # same geometry, new buffers: the tuned schedule, the same result
+    dev2 = [[x.clone() for x in st] for st in dev]
+    outs = ctx.fuse_stacks(dev2, params=p)
+    for a, b in zip(outs, ref):
+        assert torch.equal(a, b)
+    with pytest.raises(Exception):
+        ctx.tune_stacks(dev, params=p, candidates=[0])
