@@ -1042,13 +1042,10 @@ static bool map2d(CUtensorMap* m, CUtensorMapDataType dt, int esz, const void* b
 
 static int sm_count()
 {
-    static const int n = [] {
-        int dev = 0, v = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-        return v > 0 ? v : 1;
-    }();
-    return n;
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 1;
 }
 
 // The TMA level-0 kernel over the interior rectangle [bx0, bx0 + nbx) x
@@ -1060,17 +1057,18 @@ static bool out0_tma_run(const Out0Maps& maps, const CoarseLevels& cl, const Out
 {
     using St = Out0Stage<TIn, T, 3, 4, MODE>;
     auto kern = k_out0_tma<TIn, T, 3, 4, AM, MODE>;
-    static bool attr = false;
-    if (!attr) {
-        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * St::BYTES) != cudaSuccess) {
-            cudaGetLastError();
-            return false;
-        }
-        attr = true;
+    // per call: the attribute belongs to the current device
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * St::BYTES) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
     }
     const int grid = std::min(ring.nbx * ring.nby, 3 * sm_count());
-    return launch_pdl_smem(kern, dim3((unsigned)grid), dim3(256), (size_t)(2 * St::BYTES), st, maps, cl, a, ring) ==
-           cudaSuccess;
+    if (launch_pdl_smem(kern, dim3((unsigned)grid), dim3(256), (size_t)(2 * St::BYTES), st, maps, cl, a, ring) !=
+        cudaSuccess) {
+        cudaGetLastError();  // the caller runs k_out0 instead
+        return false;
+    }
+    return true;
 }
 
 // The level-0 kernel with the TMA pipeline over the interior rectangle and
