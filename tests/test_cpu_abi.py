@@ -65,3 +65,7 @@ def test_create_without_device_fails_cleanly(lib):
 def test_null_context_is_rejected(lib):
     assert lib.enb_synchronize(None) == 1
     assert lib.enb_destroy(None) == 1
+    # the batched fuse, its autotuner and the adjoint reject a null context before any device work
+    assert lib.enb_fuse_stacks(None, None, 0, None, None) == 1
+    assert lib.enb_fuse_stacks_tune(None, None, 0, None, None, None, 0, 1, None, None) == 1
+    assert lib.enb_fuse_grad(None, None, 0, None, None, None, None, None, None, None) == 1
