@@ -190,6 +190,22 @@ def dist_setup():
     return ws, rank, local
 
 
+def max_over_ranks(ms: float, ws: int, device: str = "cuda") -> float:
+    """The job's time: the slowest rank's (all_reduce MAX over the process group)."""
+    if ws <= 1:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(units_per_rank: float, ws: int, steps: int, ms: float) -> float:
+    """Whole-job throughput of ws independent replicas (weak scaling): every
+    rank's units over the slowest rank's time."""
+    return ws * units_per_rank * steps / (ms / 1e3)
+
+
 # --------------------------------------------------------------------------
 # arms
 # --------------------------------------------------------------------------
@@ -378,12 +394,8 @@ def run_ours(args) -> None:
     t1 = time.time()
     sampler.stop()
     launches = ctx.launches - launches0
-    ms = e0.elapsed_time(e1)
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * UNITS * args.steps / (ms / 1e3)
+    ms = max_over_ranks(e0.elapsed_time(e1), ws)
+    value = replica_value(UNITS, ws, args.steps, ms)
 
     # ---- the reference's pass structure on the same GPU, for comparison ----
     plain_steps = max(3, min(args.steps, 20))
@@ -412,12 +424,8 @@ def run_ours(args) -> None:
         ctx.enblend(hw, hb, hm, out=ho, out_alpha=hoa)
     f1.record(stream)
     barrier()
-    e2e_ms = f0.elapsed_time(f1)
-    if ws > 1:
-        t = torch.tensor([e2e_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = ws * UNITS * e2e_steps / (e2e_ms / 1e3)
+    e2e_ms = max_over_ranks(f0.elapsed_time(f1), ws)
+    e2e_value = replica_value(UNITS, ws, e2e_steps, e2e_ms)
     h2d = hw.nbytes + hb.nbytes + hm.nbytes
     d2h = ho.nbytes + hoa.nbytes
 
