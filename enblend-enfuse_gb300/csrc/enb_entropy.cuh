@@ -221,8 +221,8 @@ __device__ __forceinline__ void mark_repeats(const float* raw, int plane, const 
                                              uint32_t* table, uint8_t* flags, int slots, uint64_t* cnt)
 {
     const int shift = 32 - (31 - __clz(slots));
-    if (NP > 0) {
-        constexpr int N = NP > 0 ? NP : 1;
+    if constexpr (NP > 0) {
+        constexpr int N = NP;
         uint32_t kk[N][3], h[N][3];
         uint32_t pend = 0;  // bit j * 3 + c: key (j, c) still probing
 #pragma unroll
@@ -276,57 +276,57 @@ __device__ __forceinline__ void mark_repeats(const float* raw, int plane, const 
             }
         }
         __syncthreads();
-        return;
-    }
-    for (int p = threadIdx.x; p < npx; p += blockDim.x) {
-        if (!a[p]) {
-            continue;
-        }
-        for (int c = 0; c < C; ++c) {
-            const float fv = raw[c * plane + p];
-            if (fv == 0.0f || fv == 1.0f) {
+    } else {
+        for (int p = threadIdx.x; p < npx; p += blockDim.x) {
+            if (!a[p]) {
                 continue;
             }
-            const uint32_t k = float_key(fv);
-            uint32_t* t = table + c * slots;
-            uint32_t h = dup_hash(k, shift);
-            for (int probe = 0; probe < slots; ++probe) {
-                const uint32_t old = atomicCAS(&t[h], kEntropyPad, k);
-                if (old == kEntropyPad) {
-                    break;
+            for (int c = 0; c < C; ++c) {
+                const float fv = raw[c * plane + p];
+                if (fv == 0.0f || fv == 1.0f) {
+                    continue;
                 }
-                if (old == k) {
-                    flags[c * slots + h] = 1;
-                    break;
+                const uint32_t k = float_key(fv);
+                uint32_t* t = table + c * slots;
+                uint32_t h = dup_hash(k, shift);
+                for (int probe = 0; probe < slots; ++probe) {
+                    const uint32_t old = atomicCAS(&t[h], kEntropyPad, k);
+                    if (old == kEntropyPad) {
+                        break;
+                    }
+                    if (old == k) {
+                        flags[c * slots + h] = 1;
+                        break;
+                    }
+                    h = (h + 1) & (uint32_t)(slots - 1);
                 }
-                h = (h + 1) & (uint32_t)(slots - 1);
             }
         }
-    }
-    __syncthreads();
-    for (int p = threadIdx.x; p < npx; p += blockDim.x) {
-        if (!a[p]) {
-            continue;
-        }
-        uint64_t m = 0;
-        for (int c = 0; c < C; ++c) {
-            const float fv = raw[c * plane + p];
-            if (fv == 0.0f || fv == 1.0f) {
+        __syncthreads();
+        for (int p = threadIdx.x; p < npx; p += blockDim.x) {
+            if (!a[p]) {
                 continue;
             }
-            const uint32_t k = float_key(fv);
-            const uint32_t* t = table + c * slots;
-            uint32_t h = dup_hash(k, shift);
-            for (int probe = 0; probe < slots && t[h] != k; ++probe) {
-                h = (h + 1) & (uint32_t)(slots - 1);
+            uint64_t m = 0;
+            for (int c = 0; c < C; ++c) {
+                const float fv = raw[c * plane + p];
+                if (fv == 0.0f || fv == 1.0f) {
+                    continue;
+                }
+                const uint32_t k = float_key(fv);
+                const uint32_t* t = table + c * slots;
+                uint32_t h = dup_hash(k, shift);
+                for (int probe = 0; probe < slots && t[h] != k; ++probe) {
+                    h = (h + 1) & (uint32_t)(slots - 1);
+                }
+                m |= flags[c * slots + h] ? 1ull << (kCntMark + 5 * c) : 0ull;
             }
-            m |= flags[c * slots + h] ? 1ull << (kCntMark + 5 * c) : 0ull;
+            if (m) {
+                cnt[p] |= m;
+            }
         }
-        if (m) {
-            cnt[p] |= m;
-        }
+        __syncthreads();
     }
-    __syncthreads();
 }
 
 // Opaque-tap count, repeat marks (bit c: some tap of channel c is marked)
