@@ -19,7 +19,11 @@
 // or image pixels), then the CTA stages the 34x10 coarse neighbourhoods of the
 // three level-(l+1) pyramids in shared memory.  Tiles inside the image take a
 // path without bounds or border weights, expand only the planes the quad's
-// seam mask selects, and use paired/vector loads and stores.
+// seam mask selects, and use paired/vector loads and stores.  Level 0 of RGBA
+// images runs instead as one persistent launch (k_out0_tma): the border ring
+// through the same tile code, then the interior tiles through a two-stage
+// pipeline fed by TMA (coarse planes; image and mask rows when they start on
+// 16-byte boundaries) or per-thread cp.async (image rows off that grid).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
