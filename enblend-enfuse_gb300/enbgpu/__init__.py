@@ -470,6 +470,8 @@ class Context:
         """Autotune the level schedule of the batched fuse on these device stacks (enb_fuse_stacks_tune):
         {"best": threshold, "ms": {threshold: ms per call}}.  Later fuse_stacks calls on batches of this
         geometry with coarse_pixels=0 use the chosen threshold."""
+        if not all(_is_torch(x) for st in stacks for x in st):
+            raise TypeError("tune_stacks: the stacks must be device tensors (the batched device path is tuned)")
         if outs is None:
             outs = [st[0].new_zeros(st[0].shape) for st in stacks]
         keep = []
@@ -507,6 +509,9 @@ class Context:
                   grad_logits=None, levels: int = 0) -> dict:
         """Loss of the float enfuse against `target` and its gradients (enb_fuse_grad).  images: K (H, W, 3)
         float32 device tensors; logits / grad_logits: K (H, W) float32 device tensors or None."""
+        arrays = list(images) + [target] + [x for x in (out,) if x is not None] + list(logits or []) + list(grad_logits or [])
+        if not all(_is_torch(x) for x in arrays):
+            raise TypeError("fuse_grad: images, target, out, logits and grad_logits must be device tensors")
         K = len(images)
         imgs = (EnbImage * K)(*[pixel_image(x) for x in images])
         lg = (EnbImage * K)(*[plane_image(a) for a in logits]) if logits is not None else None

@@ -69,3 +69,13 @@ def test_null_context_is_rejected(lib):
     assert lib.enb_fuse_stacks(None, None, 0, None, None) == 1
     assert lib.enb_fuse_stacks_tune(None, None, 0, None, None, None, 0, 1, None, None) == 1
     assert lib.enb_fuse_grad(None, None, 0, None, None, None, None, None, None, None) == 1
+
+
+def test_device_only_wrappers_reject_host_arrays():
+    """The autotuner and the adjoint take device tensors only: host arrays are refused before any call."""
+    import enbgpu
+    c = enbgpu.Context.__new__(enbgpu.Context)   # no device needed for the argument check
+    with pytest.raises(TypeError):
+        enbgpu.Context.tune_stacks(c, [[np.zeros((8, 8, 3), np.float32)]])
+    with pytest.raises(TypeError):
+        enbgpu.Context.fuse_grad(c, [np.zeros((8, 8, 3), np.float32)], np.zeros((8, 8, 3), np.float32))
