@@ -79,3 +79,22 @@ def test_device_only_wrappers_reject_host_arrays():
         enbgpu.Context.tune_stacks(c, [[np.zeros((8, 8, 3), np.float32)]])
     with pytest.raises(TypeError):
         enbgpu.Context.fuse_grad(c, [np.zeros((8, 8, 3), np.float32)], np.zeros((8, 8, 3), np.float32))
+
+
+@pytest.mark.parametrize("lang", ["c", "c++"])
+def test_header_is_plain_c(lang, tmp_path):
+    """include/enbgpu.h compiles as C99 and as C++ on its own (a C ABI: no CUDA
+    or C++ types in the signatures)."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+    cc = shutil.which("gcc" if lang == "c" else "g++")
+    if not cc:
+        pytest.skip("no host compiler")
+    inc = Path(__file__).resolve().parents[1] / "include"
+    src = tmp_path / ("t.c" if lang == "c" else "t.cpp")
+    src.write_text('#include "enbgpu.h"\nint main(void) { return enb_abi_version() == ENBGPU_ABI_VERSION ? 0 : 1; }\n')
+    std = ["-std=c99"] if lang == "c" else ["-std=c++11"]
+    r = subprocess.run([cc, *std, "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I", str(inc), str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
