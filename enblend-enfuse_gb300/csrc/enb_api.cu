@@ -83,6 +83,9 @@ struct enb_ctx {
     unsigned int* dev_err = nullptr;
     // coarse thresholds chosen by enb_fuse_stacks_tune, per batch geometry
     std::map<std::string, int32_t> tuned;
+    // enb_debug_overarm_tile_waits: bytes the level-0 pipeline's stage
+    // barriers expect beyond their copies (0 in normal operation)
+    uint32_t tx_extra = 0;
 };
 
 struct enb_pyramid {
@@ -971,6 +974,7 @@ enb_status enblend_fused(enb_ctx* ctx, const enb_image* white, const enb_image* 
     h0.wrap = wrap;
     h0.seed = o.seed;
     h0.err = device_error_word(ctx);
+    h0.tx_extra = ctx->tx_extra;
     PlanarView g0{}, b0{}, r0{};
     if (NL >= 1) {
         g0 = level_view(gw.p, 0);
@@ -1370,6 +1374,16 @@ enb_status enb_synchronize(enb_ctx* ctx)
 
 const char* enb_last_error(const enb_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
 
+enb_status enb_debug_overarm_tile_waits(enb_ctx* ctx, uint32_t extra_bytes)
+{
+    if (!ctx) {
+        return ENB_ERR_INVALID;
+    }
+    ENB_CHECK(ctx, extra_bytes <= 4096, "debug_overarm_tile_waits: at most 4096 extra bytes");
+    ctx->tx_extra = extra_bytes;
+    return ENB_OK;
+}
+
 uint64_t enb_launch_count(const enb_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
 void enb_default_enfuse_params(enb_enfuse_params* p)
@@ -1643,11 +1657,20 @@ enb_status enb_gaussian_pyramid_noalloc(enb_ctx* ctx, int wrap, const enb_image*
     ENB_CHECK(ctx, src && src->width == p->w[0] && src->height == p->h[0], "noalloc: src size differs from level 0");
     ENB_CHECK(ctx, frac >= 0 && frac <= 24, "noalloc: frac_bits outside 0..24");
     const PlanarView l0 = level_view(p, 0);
-    if (src->dtype == ENB_F32) {
+    // Level 0 takes the conversions of enb_to_pyramid, with its checks: an
+    // F32 pyramid the logarithmic mapping of an interleaved F32 image, a
+    // fixed-point pyramid either fromRealPromote(v * 2^frac) of an F32 plane
+    // (one channel) or v << frac of interleaved U8/U16 pixels.
+    const bool f32_plane = p->dtype != ENB_F32 && src->dtype == ENB_F32;
+    if (p->dtype == ENB_F32) {
+        ENB_CHECK(ctx, pixels_ok(src) && src->dtype == ENB_F32 && src->channels == p->C,
+                  "noalloc: an F32 pyramid takes an interleaved F32 image of its channel count");
+    } else if (f32_plane) {
         ENB_CHECK(ctx, src->channels == 1 && p->C == 1 && floats_ok(src, src->width, src->height),
-                  "noalloc: F32 sources are single-channel planes");
+                  "noalloc: F32 sources of a fixed-point pyramid are single-channel planes");
     } else {
-        ENB_CHECK(ctx, pixels_ok(src) && src->channels == p->C, "noalloc: src must be interleaved U8/U16 of the pyramid's channels");
+        ENB_CHECK(ctx, pixels_ok(src) && src->dtype != ENB_F32 && src->channels == p->C,
+                  "noalloc: src must be interleaved U8/U16 of the pyramid's channels");
     }
     if (alpha) {
         ENB_CHECK(ctx, bytes_ok(alpha, src->width, src->height), "noalloc: alpha must be U8 of the image size");
@@ -1674,8 +1697,8 @@ enb_status enb_gaussian_pyramid_noalloc(enb_ctx* ctx, int wrap, const enb_image*
         ENB_TRY(noalloc_scratch(ctx, &s));
         scratch = (uint8_t*)s;
     }
-    cudaError_t e = src->dtype == ENB_F32 ? launch_float_to_fixed(float_plane(src), l0, frac, ctx->stream)
-                                          : launch_to_fixed(pixel_view(src), l0, frac, ctx->stream);
+    cudaError_t e = f32_plane ? launch_float_to_fixed(float_plane(src), l0, frac, ctx->stream)
+                              : launch_to_fixed(pixel_view(src), l0, frac, ctx->stream);
     ctx->launches++;
     if (e != cudaSuccess) {
         return cuda_fail(ctx, e, "noalloc: conversion to fixed point");

@@ -193,6 +193,8 @@ struct Out0Args {
     int32_t maxv;
     int tx0, ty0;                // first tile column (64 pixels) and row (16 rows) of the launch
     unsigned int* err;           // device error word (bit 0: a tile wait timed out)
+    uint32_t tx_extra;           // bytes each stage's barrier expects beyond its
+                                 // copies (0; > 0 only to test the timeout path)
 };
 
 // Coarse taps of an interior tile packed as (Gw, Gb, R) int4 per position
@@ -590,7 +592,7 @@ __global__ void __launch_bounds__(256, 3) k_out0_tma(const __grid_constant__ Out
         const int I0 = X0 >> 1, J0 = Y0 >> 1, l = threadIdx.x;
         unsigned char* st = osm + s * St::BYTES;
         if (l == 0) {
-            mbar_arrive_expect_tx(&bar[s], St::TX);
+            mbar_arrive_expect_tx(&bar[s], St::TX + a.tx_extra);
             if (MODE == OUT0_TMA_ROWS) {
                 tma_load_2d(st, &maps.white, X0 * S, Y0, &bar[s]);
                 tma_load_2d(st + St::IMG, &maps.black, X0 * S, Y0, &bar[s]);
@@ -710,7 +712,12 @@ __global__ void __launch_bounds__(256, 3) k_out0_tma(const __grid_constant__ Out
         }
         const PlanarTaps<T, C, St::CBW, St::PLANE / (int)sizeof(T), St::XOFF> taps{
             reinterpret_cast<const T*>(st + 2 * St::IMG + St::MSK)};
-        out0_quad<TIn, T, C, S, AM, true>(a, taps, X, Y, qx, qy, wp, bp, mk);
+        // a completed phase means every copy of the stage landed; a thread
+        // whose wait ran out writes nothing, so the tiles of a failed launch
+        // keep their previous output
+        if (ok) {
+            out0_quad<TIn, T, C, S, AM, true>(a, taps, X, Y, qx, qy, wp, bp, mk);
+        }
         mreg = mnext;
         if (!__syncthreads_and(ok)) {
             // a stage never completed: report it, let the copies of the next
@@ -1137,6 +1144,7 @@ cudaError_t launch_out0(const PlanarView* gw1, const PlanarView* gb1, const Plan
     a.key = dither_key(h.seed);
     a.maxv = wv.dtype == ENB_U8 ? 255 : 65535;
     a.err = h.err;
+    a.tx_extra = h.tx_extra;
     // k_out0 compiles these formats in
     const int mf_expect = wv.dtype == ENB_U8 ? 7 : 15;
     if (a.frac != 7 || a.mfrac != mf_expect || a.white_value != (255 << mf_expect) || wv.C > 4) {

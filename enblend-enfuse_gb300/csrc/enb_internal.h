@@ -126,6 +126,8 @@ struct Out0Host {
     int frac, dither, wrap;
     uint64_t seed;
     unsigned int* err;    // device error word of the context (bit 0: a tile wait timed out)
+    uint32_t tx_extra;    // bytes the level-0 pipeline's stage barriers expect
+                          // beyond their copies: 0, except to test the timeout
 };
 
 // Coarse end of the fused enblend blend (one launch): slot 0 is the finest

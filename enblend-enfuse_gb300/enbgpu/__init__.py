@@ -87,6 +87,7 @@ _SIGNATURES = {
     "enb_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "enb_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
     "enb_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "enb_debug_overarm_tile_waits": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32]),
     "enb_launch_count": (ctypes.c_uint64, [ctypes.c_void_p]),
     "enb_profile_enable": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "enb_profile_count": (ctypes.c_int, [ctypes.c_void_p]),

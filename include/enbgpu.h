@@ -158,6 +158,16 @@ enb_status enb_set_stream(enb_ctx* ctx, void* cuda_stream);
 enb_status enb_synchronize(enb_ctx* ctx);
 /* Message of the last failed call on this context (never NULL). */
 const char* enb_last_error(const enb_ctx* ctx);
+/* Test hook of the bounded waits (no counterpart in the reference): with
+ * extra_bytes in 1..4096, the level-0 tile pipeline of later enb_enblend
+ * calls on this context arms each stage's barrier for that many bytes more
+ * than its copies deliver, so every wait for a stage runs out (after about
+ * half a second of SM clock), the kernel records the timeout in the
+ * context's error word and returns without writing the waiting tiles, and
+ * the next synchronising call fails with ENB_ERR_CUDA.  Nothing faults and
+ * nothing waits without a limit; the context stays usable.  0 (the default)
+ * restores normal operation. */
+enb_status enb_debug_overarm_tile_waits(enb_ctx* ctx, uint32_t extra_bytes);
 /* Kernels launched on this context since creation (a counter, for profiling). */
 uint64_t enb_launch_count(const enb_ctx* ctx);
 void enb_default_enfuse_params(enb_enfuse_params* p);
@@ -243,10 +253,13 @@ enb_status enb_gaussian_pyramid(enb_ctx* ctx, int wraparound, const enb_image* s
  * fixed-budget embedded pipeline.  The alpha planes of levels 1..L-1 live in
  * a file-scope device array of ENB_NOALLOC_SCRATCH_BYTES (16 MiB, about
  * 48 Mpx at level 0) that every GPU loading the library holds until exit;
- * larger images are rejected with ENB_ERR_INVALID.  The first call on each
- * device looks up that array's device address (make that first call before
- * any stream capture).  All calls share the array: calls that overlap on the
- * GPU (other streams, other threads) race on it. */
+ * larger images are rejected with ENB_ERR_INVALID.  It accepts the same
+ * sources as enb_gaussian_pyramid (level 0 converted as by enb_to_pyramid).
+ * The first call on each device looks up that array's device address (make
+ * that first call before any stream capture) and keeps it for the life of
+ * the process, so a cudaDeviceReset after that first call is not supported.
+ * All calls share the array: calls that overlap on the GPU (other streams,
+ * other threads) race on it. */
 #define ENB_NOALLOC_SCRATCH_BYTES (16u << 20)
 enb_status enb_gaussian_pyramid_noalloc(enb_ctx* ctx, int wraparound, const enb_image* src,
                                         const enb_image* alpha, int frac_bits, enb_pyramid* pyr);

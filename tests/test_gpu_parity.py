@@ -374,6 +374,42 @@ def test_enblend_level0_tma(ctx, orc, dt, wrap, planes, off):
         assert np.array_equal(out.cpu().numpy(), ref["out"])
 
 
+def test_level0_wait_timeout_is_reported(ctx, orc):
+    """The level-0 pipeline's bounded waits: with every stage barrier armed for
+    16 bytes more than its copies deliver (enb_debug_overarm_tile_waits), each
+    CTA's first wait runs out after about half a second, the kernel records it
+    in the context's error word and returns without writing the tiles it was
+    waiting for, and enb_synchronize fails with ENB_ERR_CUDA and the message.
+    Nothing faults and no wait is unbounded; the same context then blends
+    correctly again."""
+    import enbgpu
+    from enbgpu import synthetic
+    white, black, mask = synthetic.panorama_pair(300, 400, 240, np.uint16, seed=43)   # 640 wide: TMA rows
+    ref = orc.enblend(white, black, mask, seed=8)
+    dw, db, dm = _dev(white), _dev(black), _dev(mask)
+    sentinel = 0x1234
+    out = torch.full(black.shape, sentinel, dtype=torch.uint16, device="cuda")
+    ctx._check(ctx.lib.enb_debug_overarm_tile_waits(ctx.handle, 16))
+    try:
+        ctx.enblend(dw, db, dm, out=out, seed=8)
+        with pytest.raises(enbgpu.EnbError) as err:
+            ctx.synchronize()
+        assert err.value.status == enbgpu.ENB_ERR_CUDA
+        assert "timed out" in str(err.value)
+    finally:
+        ctx._check(ctx.lib.enb_debug_overarm_tile_waits(ctx.handle, 0))
+    got = out.cpu().numpy()
+    assert (got[..., :3] == sentinel).any(), "the tiles whose wait ran out must stay unwritten"
+    ctx.synchronize()   # the error word was cleared by the failed synchronisation
+    ctx.profile(True)
+    out2, oa2 = ctx.enblend(dw, db, dm, seed=8)
+    names = set(ctx.profile_report())
+    ctx.profile(False)
+    assert "out0_tma" in names
+    assert np.array_equal(out2.cpu().numpy(), ref["out"])
+    assert np.array_equal(oa2.cpu().numpy(), ref["alpha"])
+
+
 def test_enblend_in_place(ctx, orc):
     """out may alias the black image (the reference writes into it)."""
     from enbgpu import synthetic
