@@ -655,6 +655,79 @@ static int32_t gray_int(const orc_enfuse_params* prm, int32_t r, int32_t g, int3
     }
 }
 
+/* AlternativePercentage / CompactifiedAlternativePercentage
+ * (src/alternativepercentage.h:31-97): is_effective<t> and instantiate<t>
+ * for a sample type whose maximum is `maxv` (the float maximum for float
+ * images).  instantiate converts to the sample type: truncation toward zero
+ * for the integer types, rounding to float for float images. */
+static int cutoff_effective(double v, int pct, double maxv, int compactified)
+{
+    if (compactified) {
+        return v != 0.0 && ((pct && fabs(v) != 100.0) || (!pct && v != maxv));
+    }
+    return v > 0.0 && ((pct && v < 100.0) || (!pct && v < maxv));
+}
+
+static double cutoff_value(double v, int pct, double maxv, int integral, int compactified)
+{
+    double c;
+    if (compactified) {
+        c = pct ? (v >= 0.0 ? v : 100.0 + v) * maxv / 100.0 : (v >= 0.0 ? v : maxv + v);
+    } else {
+        c = pct ? v * maxv / 100.0 : v;
+    }
+    return integral ? trunc(c) : (double)(float)c;
+}
+
+/* The exposure cutoff of one image type: *active, and the lower and upper
+ * limits (src/enfuse.h:655-690).  The upper limit is a compactified
+ * percentage, a negative value counting down from the maximum, as the
+ * option is documented (doc/enfuse-expert-fusion-options.tex:184-185) and as
+ * the reference judges its activity; the reference's functor instantiates it
+ * through the plain base class instead, which converts a negative limit to
+ * the unsigned sample type (undefined behaviour), so the two agree for every
+ * non-negative limit.  -3 for the reference's fatal cases (negative limits,
+ * lower above upper). */
+static int exposure_cutoffs(const orc_enfuse_params* prm, double maxv, int integral, int* active, double* lo,
+                            double* hi)
+{
+    *active = cutoff_effective(prm->exp_cutoff[0], prm->exp_cutoff_pct[0], maxv, 0) ||
+              cutoff_effective(prm->exp_cutoff[1], prm->exp_cutoff_pct[1], maxv, 1);
+    if (!*active) {
+        return 0;
+    }
+    *lo = cutoff_value(prm->exp_cutoff[0], prm->exp_cutoff_pct[0], maxv, integral, 0);
+    *hi = cutoff_value(prm->exp_cutoff[1], prm->exp_cutoff_pct[1], maxv, integral, 1);
+    return (*lo < 0.0 || *hi < 0.0 || *lo > *hi) ? -3 : 0;
+}
+
+/* The entropy cutoff (src/enfuse.h:1145-1192): lower as a plain, upper as a
+ * compactified AlternativePercentage. */
+static int entropy_cutoffs(const orc_enfuse_params* prm, double maxv, int integral, int* active, double* lo,
+                           double* hi)
+{
+    *active = cutoff_effective(prm->ent_cutoff[0], prm->ent_cutoff_pct[0], maxv, 0) ||
+              cutoff_effective(prm->ent_cutoff[1], prm->ent_cutoff_pct[1], maxv, 1);
+    if (!*active) {
+        return 0;
+    }
+    *lo = cutoff_value(prm->ent_cutoff[0], prm->ent_cutoff_pct[0], maxv, integral, 0);
+    *hi = cutoff_value(prm->ent_cutoff[1], prm->ent_cutoff_pct[1], maxv, integral, 1);
+    return (*lo < 0.0 || *hi < 0.0 || *lo > *hi) ? -3 : 0;
+}
+
+/* ClampingFunctor of the entropy cutoff (src/enfuse.h:893-925): per sample
+ * x <= lo -> 0, x >= hi -> max, else x; the third (blue) sample is tested
+ * against the first sample's lower limit, as the reference does. */
+static void clamp_rgb_u32(uint32_t* px, int C, double lo, double hi, uint32_t maxv)
+{
+    const int red_low = (double)px[0] <= lo;
+    for (int c = 0; c < C; ++c) {
+        const int low = (C == 3 && c == 2) ? red_low : ((double)px[c] <= lo);
+        px[c] = low ? 0u : ((double)px[c] >= hi ? maxv : px[c]);
+    }
+}
+
 int orc_local_stddev(const int32_t* gray, const uint8_t* alpha, int w, int h, int window,
                      int32_t* out)
 {
@@ -723,8 +796,19 @@ static double entropy_of(uint32_t* vals, int n)
     return -e / log((double)bins);
 }
 
+static int local_entropy_clamped(const void* img, int dtype, int w, int h, int C, int pix_stride,
+                                 const uint8_t* alpha, int window, int clamp, double lo, double hi, double* out);
+
 int orc_local_entropy(const void* img, int dtype, int w, int h, int C, int pix_stride,
                       const uint8_t* alpha, int window, double* out)
+{
+    return local_entropy_clamped(img, dtype, w, h, C, pix_stride, alpha, window, 0, 0.0, 0.0, out);
+}
+
+/* localEntropyIf (src/enfuse.h:458-566) of the image, its samples first
+ * clamped by the entropy cutoff when `clamp` is set. */
+static int local_entropy_clamped(const void* img, int dtype, int w, int h, int C, int pix_stride,
+                                 const uint8_t* alpha, int window, int clamp, double lo, double hi, double* out)
 {
     if (w < window || h < window || dtype == ORC_F32) {
         return -1;
@@ -746,7 +830,16 @@ int orc_local_entropy(const void* img, int dtype, int w, int h, int C, int pix_s
                         for (int xx = x - b; xx <= x + b; ++xx) {
                             const int64_t p = (int64_t)yy * w + xx;
                             if (alpha[p]) {
-                                vals[n++] = sample_int(img, dtype, p * pix_stride + c);
+                                if (clamp) {
+                                    uint32_t px[3];
+                                    for (int k = 0; k < C; ++k) {
+                                        px[k] = sample_int(img, dtype, p * pix_stride + k);
+                                    }
+                                    clamp_rgb_u32(px, C, lo, hi, (uint32_t)maxv);
+                                    vals[n++] = px[c];
+                                } else {
+                                    vals[n++] = sample_int(img, dtype, p * pix_stride + c);
+                                }
                             }
                         }
                     }
@@ -787,15 +880,45 @@ int orc_enfuse_mask(const void* img, int dtype, int w, int h, int C, int pix_str
     }
     memset(out, 0, sizeof(float) * (size_t)npix);
 
-    /* Exposure (enfuse.h:974-1010, 623-651). */
+    /* Exposure (enfuse.h:974-1010, 623-730), with the cutoff when active. */
     if (prm->w_exposure > 0.0) {
         const double ew = exposure_effective_width(prm->exp_function, prm->exp_width);
+        int cut = 0;
+        double lo = 0.0, hi = 0.0;
+        const int rc = exposure_cutoffs(prm, (double)maxv, 1, &cut, &lo, &hi);
+        if (rc) {
+            free(gray);
+            return rc;
+        }
+        /* the projectors that judge the lower and the upper limit
+         * (enfuse.h:982-986; the caller resolves the reference's fallbacks
+         * between empty projector names) */
+        orc_enfuse_params lp = *prm, up = *prm;
+        lp.gray_projector = prm->exp_cutoff_proj[0];
+        up.gray_projector = prm->exp_cutoff_proj[1];
 #pragma omp parallel for schedule(static)
         for (int64_t p = 0; p < npix; ++p) {
-            if (alpha[p]) {
-                const double y = (double)gray[p] / (double)maxv;
-                out[p] = (float)(prm->w_exposure * exposure_weight(prm->exp_function, y, prm->exp_optimum, ew));
+            if (!alpha[p]) {
+                continue;
             }
+            if (cut) {
+                double lv, uv;
+                if (C == 1) {
+                    lv = uv = (double)gray[p];
+                } else {
+                    const int32_t r = (int32_t)sample_int(img, dtype, p * pix_stride);
+                    const int32_t g = (int32_t)sample_int(img, dtype, p * pix_stride + 1);
+                    const int32_t b = (int32_t)sample_int(img, dtype, p * pix_stride + 2);
+                    lv = (double)gray_int(&lp, r, g, b, maxv, mw0, mw1, mw2);
+                    uv = (double)gray_int(&up, r, g, b, maxv, mw0, mw1, mw2);
+                }
+                if (!(lv >= lo && uv <= hi)) {
+                    out[p] = 0.0f;
+                    continue;
+                }
+            }
+            const double y = (double)gray[p] / (double)maxv;
+            out[p] = (float)(prm->w_exposure * exposure_weight(prm->exp_function, y, prm->exp_optimum, ew));
         }
     }
 
@@ -848,8 +971,15 @@ int orc_enfuse_mask(const void* img, int dtype, int w, int h, int C, int pix_str
 
     /* Entropy (enfuse.h:1139-1211, 832-861). */
     if (prm->w_entropy > 0.0) {
+        int cut = 0;
+        double lo = 0.0, hi = 0.0;
+        int rc = entropy_cutoffs(prm, (double)maxv, 1, &cut, &lo, &hi);
+        if (rc) {
+            free(gray);
+            return rc;
+        }
         double* ent = (double*)calloc((size_t)npix * C, sizeof(double));
-        const int rc = orc_local_entropy(img, dtype, w, h, C, pix_stride, alpha, prm->entropy_window, ent);
+        rc = local_entropy_clamped(img, dtype, w, h, C, pix_stride, alpha, prm->entropy_window, cut, lo, hi, ent);
         if (rc) {
             free(ent);
             free(gray);
@@ -1351,6 +1481,81 @@ static double entropy_of_f(float* vals, int n)
     return -e / log((double)bins);
 }
 
+/* localStdDevIf (src/enfuse.h:75-219) for a float gray image, with the
+ * reference's own rounding: per row, float column sums of the masked window
+ * rows, a float running sum along the row updated by (new column - old
+ * column), and sqrt((sumSqr - sum^2 / n) / (n - 1)) in float.  Rows are
+ * independent (each starts from its own column sums), so the result does not
+ * depend on how rows are shared among threads.  Pixels outside the interior
+ * or without alpha stay 0. */
+static void stddev_sliding_f(const float* gray, const uint8_t* alpha, int w, int h, int win, float* sd)
+{
+    const int b = win / 2;
+#pragma omp parallel
+    {
+        float* csum = (float*)malloc(sizeof(float) * (size_t)(w + 1));
+        float* csq = (float*)malloc(sizeof(float) * (size_t)(w + 1));
+        size_t* cn = (size_t*)malloc(sizeof(size_t) * (size_t)(w + 1));
+#pragma omp for schedule(static)
+        for (int y = b; y < h - b; ++y) {
+            float sum = 0.0f, sumsq = 0.0f;
+            size_t n = 0;
+            for (int i = 0; i <= 2 * b; ++i) {        /* columns 0 .. 2b */
+                float s0 = 0.0f, q0 = 0.0f;
+                size_t n0 = 0;
+                for (int yy = y - b; yy <= y + b; ++yy) {
+                    const int64_t q = (int64_t)yy * w + i;
+                    if (alpha[q]) {
+                        const float v = gray[q];
+                        s0 += v;
+                        q0 += v * v;
+                        ++n0;
+                    }
+                }
+                csum[i] = s0;
+                csq[i] = q0;
+                cn[i] = n0;
+                sum += s0;
+                sumsq += q0;
+                n += n0;
+            }
+            int old = 0, next = win;
+            for (int x = b;; ++x) {
+                const int64_t p = (int64_t)y * w + x;
+                if (alpha[p]) {
+                    sd[p] = n <= 1 ? 0.0f : sqrtf((sumsq - sum * sum / (float)n) / (float)(n - 1));
+                }
+                if (x == w - b - 1) {
+                    break;
+                }
+                const int cx = x + b + 1;
+                float s0 = 0.0f, q0 = 0.0f;
+                size_t n0 = 0;
+                for (int yy = y - b; yy <= y + b; ++yy) {
+                    const int64_t q = (int64_t)yy * w + cx;
+                    if (alpha[q]) {
+                        const float v = gray[q];
+                        s0 += v;
+                        q0 += v * v;
+                        ++n0;
+                    }
+                }
+                csum[next] = s0;
+                csq[next] = q0;
+                cn[next] = n0;
+                sum += s0 - csum[old];
+                sumsq += q0 - csq[old];
+                n += n0 - cn[old];
+                ++old;
+                ++next;
+            }
+        }
+        free(csum);
+        free(csq);
+        free(cn);
+    }
+}
+
 /* enfuseMask for float images (src/enfuse.h:962-1212).  `range` stands for
  * NumericTraits<float>::max() in the exposure (y = gray / max, :638) and
  * entropy (H * max) weights: FLT_MAX is the reference's behaviour, 1.0 the
@@ -1380,9 +1585,29 @@ int orc_enfuse_mask_f(const float* img, int w, int h, int C, int pix_stride, con
 
     if (prm->w_exposure > 0.0) {
         const double ew = exposure_effective_width(prm->exp_function, prm->exp_width);
+        /* the cutoff limits are fractions of the same `range` (enfuse.h:655-690) */
+        int cut = 0;
+        double lo = 0.0, hi = 0.0;
+        const int rc = exposure_cutoffs(prm, range, 0, &cut, &lo, &hi);
+        if (rc) {
+            free(gray);
+            return rc;
+        }
+        orc_enfuse_params lp = *prm, up = *prm;
+        lp.gray_projector = prm->exp_cutoff_proj[0];
+        up.gray_projector = prm->exp_cutoff_proj[1];
 #pragma omp parallel for schedule(static)
         for (int64_t p = 0; p < npix; ++p) {
             if (alpha[p]) {
+                if (cut) {
+                    const float* px = img + p * pix_stride;
+                    const float lv = C == 1 ? gray[p] : gray_float(&lp, px[0], px[1], px[2], mw0, mw1, mw2);
+                    const float uv = C == 1 ? gray[p] : gray_float(&up, px[0], px[1], px[2], mw0, mw1, mw2);
+                    if (!((double)lv >= lo && (double)uv <= hi)) {
+                        out[p] = 0.0f;
+                        continue;
+                    }
+                }
                 /* toRealPromote(float) / max(): a float division (enfuse.h:638) */
                 const double y = (double)(gray[p] / (float)range);
                 out[p] = (float)(prm->w_exposure * exposure_weight(prm->exp_function, y, prm->exp_optimum, ew));
@@ -1390,7 +1615,21 @@ int orc_enfuse_mask_f(const float* img, int w, int h, int C, int pix_stride, con
         }
     }
 
-    if (prm->w_contrast > 0.0) {
+    if (prm->w_contrast > 0.0 && prm->float_sliding_sums) {
+        const int win = prm->contrast_window;
+        if (win < 2 || w < win || h < win) {
+            free(gray);
+            return -1;
+        }
+        float* sd = (float*)calloc((size_t)npix, sizeof(float));
+        stddev_sliding_f(gray, alpha, w, h, win, sd);
+        for (int64_t p = 0; p < npix; ++p) {
+            if (alpha[p]) {
+                out[p] = (float)(prm->w_contrast * (double)sd[p]) + out[p];
+            }
+        }
+        free(sd);
+    } else if (prm->w_contrast > 0.0) {
         const int win = prm->contrast_window, b = win / 2;
         if (win < 2 || w < win || h < win) {
             free(gray);
@@ -1458,6 +1697,13 @@ int orc_enfuse_mask_f(const float* img, int w, int h, int C, int pix_stride, con
             free(gray);
             return -1;
         }
+        int cut = 0;
+        double lo = 0.0, hi = 0.0;
+        const int rc = entropy_cutoffs(prm, range, 0, &cut, &lo, &hi);
+        if (rc) {
+            free(gray);
+            return rc;
+        }
 #pragma omp parallel
         {
             float* vals = (float*)malloc(sizeof(float) * (size_t)win * win);
@@ -1474,7 +1720,14 @@ int orc_enfuse_mask_f(const float* img, int w, int h, int C, int pix_stride, con
                             for (int xx = x - b; xx <= x + b; ++xx) {
                                 const int64_t q = (int64_t)yy * w + xx;
                                 if (alpha[q]) {
-                                    const float v = img[q * pix_stride + c];
+                                    float v = img[q * pix_stride + c];
+                                    if (cut) {
+                                        /* ClampingFunctor (enfuse.h:893-925), the third
+                                         * sample judged low by the first */
+                                        const float* px = img + q * pix_stride;
+                                        const int low = (C == 3 && c == 2) ? ((double)px[0] <= lo) : ((double)v <= lo);
+                                        v = low ? 0.0f : ((double)v >= hi ? (float)range : v);
+                                    }
                                     vals[n++] = v == 0.0f ? 0.0f : v;
                                 }
                             }

@@ -63,6 +63,20 @@ typedef struct {
     int entropy_window;     /* --entropy-window-size, odd >= 3 (enfuse.cc:140) */
     int gray_projector;     /* ORC_GRAY_*          (mga.h:78-87) */
     double mixer[3];        /* channel-mixer weights (mga.h:107-116) */
+    /* --exposure-cutoff (enfuse.cc:1272-1340): lower / upper cutoff values,
+     * each a percentage of the type's maximum or an absolute value, and the
+     * gray projectors (ORC_GRAY_*) that judge them; {0 %, 100 %} is off */
+    double exp_cutoff[2];
+    int exp_cutoff_pct[2];
+    int exp_cutoff_proj[2];
+    /* --entropy-cutoff (enfuse.cc:1213-1270): lower / upper clamp of the
+     * samples before the entropy windows; {0 %, 100 %} is off */
+    double ent_cutoff[2];
+    int ent_cutoff_pct[2];
+    /* float images: 1 forms the contrast windows' sums as the reference does
+     * (float running sums along each row, src/enfuse.h:105-217) instead of
+     * exact double window sums */
+    int float_sliding_sums;
 } orc_enfuse_params;
 
 /* roiBounds level count (src/bounds.h:97-177) for an ROI of w x h. */

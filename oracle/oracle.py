@@ -32,7 +32,11 @@ class OrcParams(ctypes.Structure):
                 ("exp_optimum", ctypes.c_double), ("exp_width", ctypes.c_double),
                 ("exp_function", ctypes.c_int), ("contrast_window", ctypes.c_int),
                 ("entropy_window", ctypes.c_int), ("gray_projector", ctypes.c_int),
-                ("mixer", ctypes.c_double * 3)]
+                ("mixer", ctypes.c_double * 3),
+                ("exp_cutoff", ctypes.c_double * 2), ("exp_cutoff_pct", ctypes.c_int * 2),
+                ("exp_cutoff_proj", ctypes.c_int * 2),
+                ("ent_cutoff", ctypes.c_double * 2), ("ent_cutoff_pct", ctypes.c_int * 2),
+                ("float_sliding_sums", ctypes.c_int)]
 
 
 def build(force: bool = False) -> Path:
@@ -111,7 +115,12 @@ def _geom(img: np.ndarray):
 def params(exposure_weight=1.0, saturation_weight=0.0, contrast_weight=0.0, entropy_weight=0.0,
            exposure_optimum=0.5, exposure_width=0.2, exposure_weight_function="gaussian",
            contrast_window_size=5, entropy_window_size=3, gray_projector="average",
-           mixer=(0.0, 0.0, 0.0)) -> OrcParams:
+           mixer=(0.0, 0.0, 0.0), exposure_cutoff=((0.0, True), (100.0, True)),
+           exposure_cutoff_projectors=("anti-value", "value"), entropy_cutoff=((0.0, True), (100.0, True)),
+           float_sliding_sums=False) -> OrcParams:
+    """enfuse's weighting options.  Cutoffs are (value, is_percentage) pairs, lower then upper, as
+    --exposure-cutoff and --entropy-cutoff give them; float_sliding_sums reproduces the reference's float
+    rounding of the contrast windows of float images."""
     p = OrcParams()
     p.w_exposure, p.w_saturation, p.w_contrast, p.w_entropy = (exposure_weight, saturation_weight,
                                                                contrast_weight, entropy_weight)
@@ -120,6 +129,11 @@ def params(exposure_weight=1.0, saturation_weight=0.0, contrast_weight=0.0, entr
     p.contrast_window, p.entropy_window = contrast_window_size, entropy_window_size
     p.gray_projector = GRAY_PROJECTORS[gray_projector]
     p.mixer[:] = list(mixer)
+    for j in range(2):
+        p.exp_cutoff[j], p.exp_cutoff_pct[j] = exposure_cutoff[j][0], int(exposure_cutoff[j][1])
+        p.exp_cutoff_proj[j] = GRAY_PROJECTORS[exposure_cutoff_projectors[j]]
+        p.ent_cutoff[j], p.ent_cutoff_pct[j] = entropy_cutoff[j][0], int(entropy_cutoff[j][1])
+    p.float_sliding_sums = int(float_sliding_sums)
     return p
 
 
@@ -426,3 +440,35 @@ def enblend_f(white: np.ndarray, black: np.ndarray, mask: np.ndarray, white_alph
     if want_level0:
         res["level0"] = l0
     return res
+
+
+# ---- the reference's option form (oracle.reference_build.enfuse_params keywords) ----------
+
+def params_from_options(opts: dict, **extra) -> OrcParams:
+    """OrcParams of enfuse options given in the keyword form of
+    oracle.reference_build.enfuse_params: gray_projector "" is the default
+    ("average"), "channel-mixer:R:G:B" the mixer with those weights; hard_mask is
+    not a weighting option and is ignored here."""
+    kw = {k: v for k, v in opts.items() if k != "hard_mask"}
+    gp = kw.pop("gray_projector", "") or "average"
+    if gp.startswith("channel-mixer"):
+        kw["mixer"] = tuple(float(v) for v in gp.split(":")[1:4])
+        gp = "channel-mixer"
+    kw["gray_projector"] = gp
+    kw.update(extra)
+    return params(**kw)
+
+
+def convert_with_draw(level0: np.ndarray, alpha: np.ndarray, dtype, draw: int, frac: int = 7) -> np.ndarray:
+    """copyFromPyramidImageIf's dither rule (src/fixmath.h:251-277) when every
+    random draw returns `draw`: q + 1 iff the fraction f >= 3/4, or f lies in
+    [1/4, 3/4) and (draw & (2^(frac-1) - 1)) + 2^(frac-2) <= f; clamped to the
+    type; 0 where alpha is 0."""
+    l0 = np.asarray(level0, np.int64)
+    Q = 1 << (frac - 2)
+    q, f = l0 >> frac, l0 & ((1 << frac) - 1)
+    t = (draw & (2 * Q - 1)) + Q
+    v = np.where(f < Q, q, np.where(f >= 3 * Q, q + 1, np.where(t <= f, q + 1, q)))
+    v = np.clip(v, 0, np.iinfo(dtype).max).astype(dtype)
+    on = np.asarray(alpha) != 0
+    return np.where(on[..., None] if v.ndim == 3 else on, v, np.zeros_like(v))

@@ -1,14 +1,23 @@
 """Build and binding of the reference-code oracle.
 
-TEST INFRASTRUCTURE ONLY.  Compiles the reference's own pyramid, blend and
-fixed-point code (src/pyramid.h, src/blend.h, src/fixmath.h,
-src/numerictraits.h, src/openmp_vigra.h, src/minimizer.cc, src/mersenne.cc),
-unmodified and in place in the reference tree, against the project's
-VIGRA/GSL/LCMS2 shims (oracle/refshim/) into oracle/_ref/libenb_ref.so, with
-ref_driver.cpp as the C entry points.  It pins the C restatement in
-enb_oracle.c (and through it the CUDA path) to the reference's code; the
-committed fixtures under tests/golden/ carry that pin to machines without the
-reference tree.
+TEST INFRASTRUCTURE ONLY.  Compiles the reference's own code, unmodified and
+in place in the reference tree, against the project's VIGRA/GSL/LCMS2 shims
+(oracle/refshim/):
+  * oracle/_ref/libenb_ref.so: the pyramid, blend and fixed-point code
+    (src/pyramid.h, src/blend.h, src/fixmath.h, src/numerictraits.h,
+    src/openmp_vigra.h, src/minimizer.cc, src/mersenne.cc) with
+    ref_driver.cpp as the C entry points;
+  * oracle/_ref/libenb_ref_enfuse.so: enfuse itself (src/enfuse.h with
+    enfuseMask and enfuseMain, src/assemble.h, src/mga.h,
+    src/exposure_weight.h, src/alternativepercentage.cc, src/parameter.cc,
+    src/error_message.cc) with ref_enfuse.cpp as the C entry points.
+They pin the C restatement in enb_oracle.c (and through it the CUDA path) to
+the reference's code; the committed fixtures under tests/golden/ carry that
+pin to machines without the reference tree.
+
+The reference tree is found through the ENB_REFERENCE_SRC environment
+variable (its src/ directory), else as reference/src beside the directory
+that holds this repository.
 """
 from __future__ import annotations
 
@@ -21,12 +30,15 @@ from typing import Optional
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-REF_SRC = Path(os.environ.get("ENB_REFERENCE_SRC", "/root/reference/src"))
+REF_SRC = Path(os.environ.get("ENB_REFERENCE_SRC") or HERE.parents[1] / "reference" / "src")
 OUT_DIR = HERE / "_ref"
 LIB_PATH = OUT_DIR / "libenb_ref.so"
+ENFUSE_LIB_PATH = OUT_DIR / "libenb_ref_enfuse.so"
 SHIM = HERE / "refshim"
 SOURCES = [HERE / "ref_driver.cpp", SHIM / "gsl_shim.cpp"]
 REF_UNITS = ["minimizer.cc", "mersenne.cc"]
+ENFUSE_SOURCES = [HERE / "ref_enfuse.cpp", SHIM / "gsl_shim.cpp"]
+ENFUSE_REF_UNITS = ["minimizer.cc", "mersenne.cc", "alternativepercentage.cc", "parameter.cc", "error_message.cc"]
 
 
 def available() -> bool:
@@ -34,26 +46,33 @@ def available() -> bool:
     return (REF_SRC / "pyramid.h").exists()
 
 
-def _deps():
-    return SOURCES + sorted(SHIM.rglob("*.h")) + sorted(SHIM.rglob("*.hxx"))
+def _deps(sources):
+    return list(sources) + sorted(SHIM.rglob("*.h")) + sorted(SHIM.rglob("*.hxx"))
 
 
-def build_if_available(force: bool = False) -> Optional[Path]:
-    """Compile libenb_ref.so when the reference tree is present; None otherwise."""
-    if not available():
-        return None
-    if not force and LIB_PATH.exists() and all(LIB_PATH.stat().st_mtime >= d.stat().st_mtime for d in _deps()):
-        return LIB_PATH
+def _compile(path: Path, sources, units, force: bool) -> Path:
+    if not force and path.exists() and all(path.stat().st_mtime >= d.stat().st_mtime for d in _deps(sources)):
+        return path
     OUT_DIR.mkdir(exist_ok=True)
-    tmp = LIB_PATH.with_suffix(".so.tmp")
+    tmp = path.with_suffix(".so.tmp")
     cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-fPIC", "-shared", "-DHAVE_CONFIG_H",
-           "-Wno-deprecated-declarations", "-I", str(SHIM), "-I", str(REF_SRC), "-o", str(tmp)]
-    cmd += [str(s) for s in SOURCES] + [str(REF_SRC / u) for u in REF_UNITS]
+           "-Wno-deprecated-declarations", "-I", str(SHIM), "-I", str(REF_SRC),
+           "-I", str(REF_SRC / "layer_selection"), "-o", str(tmp)]
+    cmd += [str(s) for s in sources] + [str(REF_SRC / u) for u in units]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError("reference oracle build failed:\n" + res.stderr[-4000:])
-    os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+    os.replace(tmp, path)
+    return path
+
+
+def build_if_available(force: bool = False) -> Optional[Path]:
+    """Compile libenb_ref.so and libenb_ref_enfuse.so when the reference tree
+    is present; None otherwise."""
+    if not available():
+        return None
+    _compile(ENFUSE_LIB_PATH, ENFUSE_SOURCES, ENFUSE_REF_UNITS, force)
+    return _compile(LIB_PATH, SOURCES, REF_UNITS, force)
 
 
 _lib = None
@@ -173,3 +192,101 @@ def enblend_f(white: np.ndarray, white_alpha: np.ndarray, black: np.ndarray, bla
     if lib().ref_enblend_f(levels, int(wrap), *[_p(a) for a in args], w, h, _p(l0), _p(out)):
         raise ValueError("reference enblend failed")
     return l0, out
+
+
+# ---- enfuse: the reference's enfuseMask and enfuseMain ----------------------
+
+class RefEnfuseParams(ctypes.Structure):
+    """ref_enfuse_params of ref_enfuse.cpp: enfuse's weighting options."""
+    _fields_ = [("w_exposure", ctypes.c_double), ("w_saturation", ctypes.c_double),
+                ("w_contrast", ctypes.c_double), ("w_entropy", ctypes.c_double),
+                ("exp_optimum", ctypes.c_double), ("exp_width", ctypes.c_double),
+                ("exp_function", ctypes.c_int32), ("contrast_window", ctypes.c_int32),
+                ("entropy_window", ctypes.c_int32), ("hard_mask", ctypes.c_int32),
+                ("exp_cutoff", ctypes.c_double * 2), ("exp_cutoff_pct", ctypes.c_int32 * 2),
+                ("ent_cutoff", ctypes.c_double * 2), ("ent_cutoff_pct", ctypes.c_int32 * 2),
+                ("gray_projector", ctypes.c_char * 96), ("exp_cutoff_projector", (ctypes.c_char * 32) * 2)]
+
+
+EXPOSURE_FUNCTIONS = {"gaussian": 0, "lorentzian": 1, "halfsine": 2, "fullsine": 3, "bisquare": 4}
+
+_elib = None
+
+
+def enfuse_lib() -> Optional[ctypes.CDLL]:
+    global _elib
+    if _elib is None:
+        if build_if_available() is None:
+            return None
+        L = ctypes.CDLL(str(ENFUSE_LIB_PATH))
+        vp, i = ctypes.c_void_p, ctypes.c_int
+        L.ref_enfuse_mask.argtypes = [ctypes.POINTER(RefEnfuseParams), i, i, vp, vp, i, i, vp]
+        L.ref_enfuse_main.argtypes = [ctypes.POINTER(RefEnfuseParams), i, i, i, ctypes.POINTER(vp), i, i, i, i,
+                                      ctypes.POINTER(vp), ctypes.c_longlong, vp, vp]
+        _elib = L
+    return _elib
+
+
+def enfuse_params(exposure_weight=1.0, saturation_weight=0.0, contrast_weight=0.0, entropy_weight=0.0,
+                  exposure_optimum=0.5, exposure_width=0.2, exposure_weight_function="gaussian",
+                  contrast_window_size=5, entropy_window_size=3, gray_projector="", hard_mask=False,
+                  exposure_cutoff=((0.0, True), (100.0, True)), exposure_cutoff_projectors=("anti-value", "value"),
+                  entropy_cutoff=((0.0, True), (100.0, True))) -> RefEnfuseParams:
+    """enfuse's options as the reference reads them (src/enfuse.cc:117-160): cutoffs are (value,
+    is_percentage) pairs, lower then upper, as --exposure-cutoff / --entropy-cutoff set them."""
+    p = RefEnfuseParams()
+    p.w_exposure, p.w_saturation, p.w_contrast, p.w_entropy = (exposure_weight, saturation_weight,
+                                                                contrast_weight, entropy_weight)
+    p.exp_optimum, p.exp_width = exposure_optimum, exposure_width
+    p.exp_function = EXPOSURE_FUNCTIONS[exposure_weight_function]
+    p.contrast_window, p.entropy_window = contrast_window_size, entropy_window_size
+    p.hard_mask = int(hard_mask)
+    for j in range(2):
+        p.exp_cutoff[j], p.exp_cutoff_pct[j] = exposure_cutoff[j][0], int(exposure_cutoff[j][1])
+        p.ent_cutoff[j], p.ent_cutoff_pct[j] = entropy_cutoff[j][0], int(entropy_cutoff[j][1])
+        p.exp_cutoff_projector[j].value = exposure_cutoff_projectors[j].encode()
+    p.gray_projector = gray_projector.encode()
+    return p
+
+
+def _depth(a: np.ndarray) -> int:
+    return {np.dtype(np.uint8): 8, np.dtype(np.uint16): 16, np.dtype(np.float32): 32}[a.dtype]
+
+
+def enfuse_mask(img: np.ndarray, alpha: Optional[np.ndarray], prm: RefEnfuseParams) -> np.ndarray:
+    """The reference's enfuseMask (src/enfuse.h:962-1212) of an (H, W, 3) or (H, W) image."""
+    img = np.ascontiguousarray(img)
+    h, w = img.shape[:2]
+    C = img.shape[2] if img.ndim == 3 else 1
+    out = np.zeros((h, w), np.float32)
+    a = np.ascontiguousarray(alpha, np.uint8) if alpha is not None else None
+    if enfuse_lib().ref_enfuse_mask(ctypes.byref(prm), _depth(img), C, _p(img), _p(a), w, h, _p(out)):
+        raise ValueError("reference enfuseMask failed")
+    return out
+
+
+def enfuse_main(images, prm: RefEnfuseParams, levels: int = 0, wrap: bool = False, masks=None,
+                dither: int = -1, save_masks: bool = False):
+    """The reference's enfuseMain (src/enfuse.h:1217-1617) on K union-sized images of one type:
+    (H, W, 3) RGB, (H, W, 4) RGBA (alpha thresholded on import), (H, W) gray.  masks: K (H, W) float32
+    weight planes for --load-masks.  dither: -1 the Mersenne-Twister draws, else every draw returns it.
+    Returns {"out": image (C colour samples), "alpha": 0/1 union alpha, "masks": (K, H, W) saved soft
+    (or hard) masks or None}."""
+    imgs = [np.ascontiguousarray(x) for x in images]
+    K = len(imgs)
+    h, w = imgs[0].shape[:2]
+    S = imgs[0].shape[2] if imgs[0].ndim == 3 else 1
+    C = 3 if S >= 3 else 1
+    out = np.zeros((h, w, C + 1), imgs[0].dtype)
+    ptrs = (ctypes.c_void_p * K)(*[x.ctypes.data for x in imgs])
+    mks = None
+    if masks is not None:
+        ms = [np.ascontiguousarray(m, np.float32) for m in masks]
+        mks = (ctypes.c_void_p * K)(*[m.ctypes.data for m in ms])
+    saved = np.zeros((K, h, w), np.float32) if save_masks else None
+    rc = enfuse_lib().ref_enfuse_main(ctypes.byref(prm), _depth(imgs[0]), S, K, ptrs, w, h, levels, int(wrap),
+                                      mks, dither, _p(out), _p(saved))
+    if rc:
+        raise ValueError(f"reference enfuseMain failed ({rc})")
+    img = out[..., :C] if C == 3 else out[..., 0]
+    return {"out": np.ascontiguousarray(img), "alpha": (out[..., C] != 0).astype(np.uint8), "masks": saved}

@@ -2,9 +2,12 @@
 // The random-number generator is a Mersenne Twister (std::mt19937, the
 // generator gsl_rng_mt19937 names); vectors are plain arrays; the
 // minimisers, used only by the non-identity colour spaces, abort.
+// gsl_shim_set_constant(v >= 0) makes every draw return v (the oracle's
+// reproducible dither runs); v < 0 restores the Mersenne Twister.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
 #include <random>
 
 #include <gsl/gsl_min.h>
@@ -33,7 +36,15 @@ void gsl_rng_set(const gsl_rng* r, unsigned long s)
 {
     const_cast<gsl_rng*>(r)->g.seed((uint32_t)(s == 0 ? 4357 : s));
 }
-unsigned long gsl_rng_get(const gsl_rng* r) { return const_cast<gsl_rng*>(r)->g(); }
+static std::atomic<long long> g_constant_draw{-1};
+
+extern "C" void gsl_shim_set_constant(long long value) { g_constant_draw.store(value); }
+
+unsigned long gsl_rng_get(const gsl_rng* r)
+{
+    const long long c = g_constant_draw.load();
+    return c >= 0 ? (unsigned long)(c & 0xffffffffLL) : (unsigned long)const_cast<gsl_rng*>(r)->g();
+}
 unsigned long gsl_rng_max(const gsl_rng*) { return 0xffffffffUL; }
 unsigned long gsl_rng_min(const gsl_rng*) { return 0; }
 double gsl_rng_uniform(const gsl_rng* r) { return gsl_rng_get(r) / 4294967296.0; }

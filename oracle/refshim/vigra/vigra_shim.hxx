@@ -14,6 +14,7 @@
 //     with PromoteTraits; RGBValue * or / a double yields the real-promoted
 //     RGBValue.
 // It is not VIGRA: only the interfaces the reference headers instantiate.
+// vigra_shim_io.hxx adds what src/enfuse.h, src/assemble.h and src/mga.h use.
 #ifndef ENB_REFSHIM_VIGRA_SHIM_HXX
 #define ENB_REFSHIM_VIGRA_SHIM_HXX
 
@@ -341,6 +342,9 @@ class RGBValue {
     void setRed(V v) { d_[R] = v; }
     void setGreen(V v) { d_[G] = v; }
     void setBlue(V v) { d_[B] = v; }
+    // 0.3 R + 0.59 G + 0.11 B in double, stored as the component type
+    // (rounded and saturated for integer components)
+    V luminance() const { return detail::RequiresExplicitCast<V>::cast(0.3 * red() + 0.59 * green() + 0.11 * blue()); }
     iterator begin() { return d_; }
     iterator end() { return d_ + 3; }
     const_iterator begin() const { return d_; }
@@ -642,6 +646,7 @@ class BasicImage {
     typedef StandardValueAccessor<T> Accessor;
     typedef StandardConstValueAccessor<T> ConstAccessor;
     typedef Size2D size_type;
+    typedef Diff2D difference_type;
 
     BasicImage() : w_(0), h_(0) {}
     BasicImage(int w, int h) : w_(w), h_(h), d_((size_t)w * h) {}
@@ -678,18 +683,6 @@ class BasicImage {
 typedef BasicImage<UInt8> BImage;
 typedef BasicImage<UInt16> UInt16Image;
 typedef BasicImage<RGBValue<UInt16>> UInt16RGBImage;
-
-// Image export (the reference's debug pyramid export; not used by the oracle).
-class ImageExportInfo {
-  public:
-    explicit ImageExportInfo(const char*) {}
-};
-
-template <class SI, class SA>
-inline void exportImage(const triple<SI, SI, SA>&, const ImageExportInfo&)
-{
-    vigra_fail("exportImage: not available in the oracle shim");
-}
 
 // ---- argument object factories --------------------------------------------------------
 template <class T>
@@ -1007,6 +1000,13 @@ struct TinyVector {
 };
 
 template <class T, int N>
+inline TinyVector<T, N> operator/(TinyVector<T, N> v, double d)
+{
+    for (int i = 0; i < N; ++i) v[i] /= d;
+    return v;
+}
+
+template <class T, int N>
 inline std::ostream& operator<<(std::ostream& o, const TinyVector<T, N>& v)
 {
     o << "(";
@@ -1039,6 +1039,26 @@ ENB_SHIM_COLOUR_FUNCTOR(XYZ2LabFunctor)
 ENB_SHIM_COLOUR_FUNCTOR(Lab2XYZFunctor)
 #undef ENB_SHIM_COLOUR_FUNCTOR
 
+// The l-star and pl-star gray projectors (src/mga.h) construct these for
+// every RGB projector; the oracle does not evaluate them.
+#define ENB_SHIM_LAB_FUNCTOR(NAME)                                           \
+    template <class T>                                                        \
+    class NAME {                                                              \
+      public:                                                                 \
+        typedef TinyVector<T, 3> result_type;                                 \
+        NAME() {}                                                             \
+        explicit NAME(double) {}                                              \
+        template <class V>                                                    \
+        result_type operator()(const V&) const                                \
+        {                                                                     \
+            vigra_fail(#NAME ": not available in the oracle shim");           \
+            return result_type();                                             \
+        }                                                                     \
+    };
+ENB_SHIM_LAB_FUNCTOR(RGB2LabFunctor)
+ENB_SHIM_LAB_FUNCTOR(RGBPrime2LabFunctor)
+#undef ENB_SHIM_LAB_FUNCTOR
+
 inline std::string impexListExtensions() { return "tif tiff"; }
 
 // ---- math utilities ------------------------------------------------------------------------
@@ -1057,6 +1077,9 @@ inline T clip_lower(T t)
 inline int roundi(double v) { return v < 0.0 ? (int)(v - 0.5) : (int)(v + 0.5); }
 
 }  // namespace vigra
+
+// Functor expressions, point functors and the in-memory image import/export.
+#include "vigra_shim_io.hxx"
 
 // VIGRA's precondition checks are global macros.
 using vigra::vigra_fail;

@@ -1,13 +1,16 @@
-"""Generate tests/golden/reference_pyramid.npz and reference_float.npz from the reference's own code.
+"""Generate tests/golden/reference_pyramid.npz, reference_float.npz and
+reference_enfuse.npz from the reference's own code.
 
 Runs the reference-code oracle (oracle/reference_build.py: the reference's
-pyramid.h / blend.h / fixmath.h compiled unmodified against the project's
-shims) on small seeded inputs and stores inputs and outputs, so that machines
-without the reference tree can check the C oracle and the CUDA path against
-the reference's results.  Usage: python tests/golden/make_golden.py
+pyramid.h / blend.h / fixmath.h, and enfuse.h's enfuseMask and enfuseMain,
+compiled unmodified against the project's shims) on small seeded inputs and
+stores inputs and outputs, so that machines without the reference tree can
+check the C oracle and the CUDA path against the reference's results.
+Usage: python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
+import json
 import sys
 from pathlib import Path
 
@@ -22,6 +25,151 @@ from oracle import reference_build as ref  # noqa: E402
 
 OUT = Path(__file__).resolve().parent / "reference_pyramid.npz"
 OUT_FLOAT = Path(__file__).resolve().parent / "reference_float.npz"
+OUT_ENFUSE = Path(__file__).resolve().parent / "reference_enfuse.npz"
+
+# enfuseMask cases: weighting options in the keyword form of
+# oracle.reference_build.enfuse_params (cutoffs as (value, is_percentage) pairs)
+MASK_CASES = [
+    dict(exposure_weight=1.0),
+    dict(exposure_weight=1.0, saturation_weight=0.2),
+    dict(exposure_weight=1.0, exposure_optimum=0.35, exposure_width=0.35, exposure_weight_function="lorentzian"),
+    dict(exposure_weight=0.8, exposure_weight_function="halfsine"),
+    dict(exposure_weight=1.0, exposure_weight_function="fullsine", saturation_weight=0.5),
+    dict(exposure_weight=1.0, exposure_weight_function="bisquare"),
+    dict(exposure_weight=0.0, contrast_weight=0.5, contrast_window_size=3),
+    dict(exposure_weight=1.0, contrast_weight=0.5, contrast_window_size=5),
+    dict(exposure_weight=0.0, contrast_weight=1.0, contrast_window_size=7),
+    dict(exposure_weight=0.0, entropy_weight=0.3, entropy_window_size=3),
+    dict(exposure_weight=1.0, entropy_weight=0.3, entropy_window_size=5),
+    dict(exposure_weight=0.0, entropy_weight=1.0, entropy_window_size=7),
+    dict(exposure_weight=1.0, saturation_weight=0.2, contrast_weight=0.5, entropy_weight=0.3, entropy_window_size=5),
+    dict(exposure_weight=1.0, gray_projector="value", contrast_weight=0.3),
+    dict(exposure_weight=1.0, gray_projector="anti-value", contrast_weight=0.3),
+    dict(exposure_weight=1.0, gray_projector="lightness", contrast_weight=0.3),
+    dict(exposure_weight=1.0, gray_projector="luminance", contrast_weight=0.3),
+    dict(exposure_weight=1.0, gray_projector="channel-mixer:0.375:0.5:0.125", contrast_weight=0.3),
+    dict(exposure_weight=1.0, exposure_cutoff=((10.0, True), (90.0, True))),
+    dict(exposure_weight=1.0, exposure_cutoff=((40.0, False), (100.0, True))),
+    dict(exposure_weight=1.0, exposure_cutoff=((0.0, True), (95.0, True)),
+         exposure_cutoff_projectors=("lightness", "luminance")),
+    dict(exposure_weight=1.0, exposure_cutoff=((12.5, True), (87.5, True)),
+         exposure_cutoff_projectors=("average", "average"), saturation_weight=0.2),
+    dict(exposure_weight=0.0, entropy_weight=0.3, entropy_window_size=5, entropy_cutoff=((10.0, True), (90.0, True))),
+    dict(exposure_weight=0.0, entropy_weight=0.3, entropy_window_size=3, entropy_cutoff=((0.0, True), (-10.0, True))),
+    dict(exposure_weight=1.0, entropy_weight=0.3, entropy_window_size=5, entropy_cutoff=((30.0, False), (100.0, True))),
+]
+
+# float images: absolute cutoffs (a percentage of the float maximum is no
+# useful limit for images in [0, 1])
+MASK_CASES_F = [c for c in MASK_CASES if "exposure_cutoff" not in c and "entropy_cutoff" not in c] + [
+    dict(exposure_weight=1.0, exposure_cutoff=((0.2, False), (0.8, False))),
+    dict(exposure_weight=1.0, exposure_cutoff=((0.1, False), (100.0, True)),
+         exposure_cutoff_projectors=("lightness", "luminance")),
+    dict(exposure_weight=0.0, entropy_weight=0.3, entropy_window_size=5, entropy_cutoff=((0.2, False), (0.8, False))),
+]
+
+# enfuseMain cases: (sample type, samples a pixel, K, options, run options)
+MAIN_CASES = [
+    ("u8", 3, 3, dict(exposure_weight=1.0, saturation_weight=0.2), {}),
+    ("u8", 3, 3, dict(exposure_weight=1.0, saturation_weight=0.2, contrast_weight=0.5, entropy_weight=0.3,
+                      entropy_window_size=5), {}),
+    ("u8", 4, 3, dict(exposure_weight=1.0, saturation_weight=0.2, contrast_weight=0.5), {}),
+    ("u8", 1, 3, dict(exposure_weight=1.0, contrast_weight=0.5), {}),
+    ("u8", 3, 3, dict(exposure_weight=1.0, saturation_weight=0.2, hard_mask=True), {}),
+    ("u8", 3, 3, dict(exposure_weight=1.0, saturation_weight=0.2), dict(wrap=True)),
+    ("u8", 3, 4, dict(exposure_weight=0.0, contrast_weight=0.5), {}),
+    ("u8", 3, 3, dict(exposure_weight=1.0, exposure_cutoff=((10.0, True), (90.0, True))), {}),
+    ("u16", 3, 3, dict(exposure_weight=1.0, saturation_weight=0.2), {}),
+    ("u16", 3, 3, dict(exposure_weight=1.0, saturation_weight=0.2, contrast_weight=0.5, entropy_weight=0.3,
+                       entropy_window_size=5), {}),
+    ("u16", 4, 3, dict(exposure_weight=1.0, saturation_weight=0.2, contrast_weight=0.5), {}),
+    ("u16", 1, 3, dict(exposure_weight=1.0, contrast_weight=0.5), {}),
+    ("u16", 3, 3, dict(exposure_weight=1.0, saturation_weight=0.2, hard_mask=True), dict(wrap=True)),
+    ("u16", 3, 3, dict(exposure_weight=1.0), dict(levels=3)),
+    ("u16", 3, 3, dict(exposure_weight=1.0), dict(load=True)),
+    ("u16", 3, 9, dict(exposure_weight=1.0, saturation_weight=0.2, contrast_weight=0.5, entropy_weight=0.3,
+                       entropy_window_size=5), {}),
+    ("f32", 3, 3, dict(exposure_weight=1.0, saturation_weight=0.2), {}),
+    ("f32", 4, 3, dict(exposure_weight=1.0, saturation_weight=0.2, contrast_weight=0.5), {}),
+    ("f32", 3, 3, dict(exposure_weight=1.0, saturation_weight=0.2, hard_mask=True), dict(wrap=True)),
+]
+
+_NP = {"u8": np.uint8, "u16": np.uint16, "f32": np.float32}
+
+
+def main_inputs(dt, S, K, seed, h=37, w=53):
+    """K exposures of the synthetic scene (RGBA: some pixels transparent after
+    the import threshold; gray: the green samples)."""
+    dtype = _NP[dt]
+    imgs = synthetic.exposure_stack(h, w, list(np.linspace(-2.0, 2.0, K)), dtype, 8.0, seed=seed)
+    if S == 4:
+        rng = np.random.default_rng(seed)
+        top = np.iinfo(dtype).max if dtype != np.float32 else 1.0
+        low = top // 3 if dtype != np.float32 else 0.2
+        imgs = [np.concatenate([x, np.full((h, w, 1), top, dtype)], axis=2) for x in imgs]
+        for i, x in enumerate(imgs):
+            x[rng.random((h, w)) < 0.1, 3] = low
+            x[5 + i:12 + i, 7:20, 3] = 0
+    if S == 1:
+        imgs = [np.ascontiguousarray(x[..., 1]) for x in imgs]
+    return imgs
+
+
+def enfuse_cases() -> None:
+    """enfuse: the reference's enfuseMask weights and enfuseMain results."""
+    data = {}
+    rng = np.random.default_rng(20261205)
+    k = 0
+    j = 0
+    for dt in ("u8", "u16", "f32"):
+        for C in (3, 1):
+            img = synthetic.exposure_stack(33, 47, [0.7], _NP[dt], 8.0, seed=11 + j)[0]
+            if C == 1:
+                img = np.ascontiguousarray(img[..., 1])
+            alpha = (rng.random((33, 47)) < 0.85).astype(np.uint8) * 255
+            alpha[4:9, 10:18] = 0
+            data[f"maskimg{j}_image"] = img
+            data[f"maskimg{j}_alpha"] = alpha
+            for opts in (MASK_CASES_F if dt == "f32" else MASK_CASES):
+                if C == 1 and opts.get("gray_projector", "").startswith("channel"):
+                    continue
+                data[f"mask{k}_img"] = np.array(j)
+                data[f"mask{k}_opts"] = np.array(json.dumps(opts))
+                data[f"mask{k}_weight"] = ref.enfuse_mask(img, alpha, ref.enfuse_params(**opts))
+                k += 1
+            j += 1
+    data["mask_count"] = np.array(k)
+    k = 0
+    for dt, S, K, opts, run in MAIN_CASES:
+        imgs = main_inputs(dt, S, K, seed=40 + k)
+        masks = None
+        if run.get("load"):
+            mr = np.random.default_rng(70 + k)
+            masks = [(mr.random(imgs[0].shape[:2]) * 3).astype(np.float32) for _ in range(K)]
+            for m in masks:
+                m[:4, :] = 0.0     # all-zero weights: the integer 255/K fallback
+        levels, wrap = run.get("levels", 0), run.get("wrap", False)
+        prm = ref.enfuse_params(**opts)
+        for i, x in enumerate(imgs):
+            data[f"main{k}_image{i}"] = x
+        if masks is not None:
+            for i, m in enumerate(masks):
+                data[f"main{k}_mask{i}"] = m
+        data[f"main{k}_meta"] = np.array([K, levels, int(wrap), int(masks is not None)], np.int32)
+        data[f"main{k}_opts"] = np.array(json.dumps(opts))
+        draws = (0, 0xFFFFFFFF) if dt != "f32" else (-1,)
+        for j, d in enumerate(draws):
+            r = ref.enfuse_main(imgs, prm, levels=levels, wrap=wrap, masks=masks, dither=d,
+                                save_masks=masks is None)
+            data[f"main{k}_out{j}"] = r["out"]
+            if j == 0:
+                data[f"main{k}_alpha"] = r["alpha"]
+                if r["masks"] is not None:
+                    data[f"main{k}_saved_masks"] = r["masks"]
+        k += 1
+    data["main_count"] = np.array(k)
+    np.savez_compressed(OUT_ENFUSE, **data)
+    print(f"wrote {OUT_ENFUSE} ({OUT_ENFUSE.stat().st_size} bytes)")
 
 
 def float_cases() -> None:
@@ -127,7 +275,13 @@ def main() -> None:
     np.savez_compressed(OUT, **data)
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes)")
     float_cases()
+    enfuse_cases()
 
 
 if __name__ == "__main__":
-    main()
+    if "--enfuse-only" in sys.argv:
+        if ref.lib() is None:
+            raise SystemExit("the reference tree is not available here")
+        enfuse_cases()
+    else:
+        main()

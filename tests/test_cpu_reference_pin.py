@@ -157,3 +157,106 @@ def test_live_float_enblend(orc, wrap):
         got = orc.enblend_f(W, B, mask, white_alpha=wa, black_alpha=ba, wrap=wrap, want_level0=True)
         assert np.allclose(got["level0"], l0, rtol=1e-13, atol=1e-13)
         assert np.array_equal(got["out"], out)
+
+
+# ---- enfuse: the reference's enfuseMask and enfuseMain --------------------------------
+
+import json  # noqa: E402
+
+EGOLDEN = np.load(Path(__file__).resolve().parent / "golden" / "reference_enfuse.npz")
+_DT = {np.dtype(np.uint8): "u8", np.dtype(np.uint16): "u16", np.dtype(np.float32): "f32"}
+
+
+def _mask_case(k):
+    j = int(EGOLDEN[f"mask{k}_img"])
+    return (EGOLDEN[f"maskimg{j}_image"], EGOLDEN[f"maskimg{j}_alpha"], json.loads(str(EGOLDEN[f"mask{k}_opts"])),
+            EGOLDEN[f"mask{k}_weight"])
+
+
+@pytest.mark.parametrize("k", range(int(EGOLDEN["mask_count"])))
+def test_golden_enfuse_mask(orc, k):
+    """enfuseMask (src/enfuse.h:962-1212): exposure functions, gray projectors,
+    saturation, contrast and entropy windows, exposure and entropy cutoffs, on
+    u8/u16/float RGB and gray images with alpha holes.  Integer images: the
+    oracle's weights equal the reference's bit for bit.  Float images: equal
+    too when the oracle forms the contrast windows with the reference's float
+    running sums (NaN where the reference's float variance goes negative)."""
+    img, alpha, opts, want = _mask_case(k)
+    if img.dtype == np.float32:
+        got = orc.enfuse_mask_f(img, alpha, orc.params_from_options(opts, float_sliding_sums=True))
+        assert np.array_equal(got, want, equal_nan=True)
+    else:
+        got = orc.enfuse_mask(img, alpha, orc.params_from_options(opts))
+        assert np.array_equal(got, want)
+
+
+def _main_case(k):
+    K, levels, wrap, load = (int(v) for v in EGOLDEN[f"main{k}_meta"])
+    imgs = [EGOLDEN[f"main{k}_image{i}"] for i in range(K)]
+    masks = [EGOLDEN[f"main{k}_mask{i}"] for i in range(K)] if load else None
+    return imgs, masks, levels, bool(wrap), json.loads(str(EGOLDEN[f"main{k}_opts"]))
+
+
+@pytest.mark.parametrize("k", range(int(EGOLDEN["main_count"])))
+def test_golden_enfuse_main(orc, k):
+    """enfuseMain (src/enfuse.h:1217-1617) end to end: import with the alpha
+    threshold, weights or --load-masks, normalisation (integer 255/K where all
+    weights are 0), hard mask, Laplacian and mask pyramids, merge, collapse and
+    the dithered output.  Integer images: the reference ran with every dither
+    draw returning 0 and with every draw returning 0xffffffff; the oracle's
+    collapsed level 0, converted under the same draws, gives the same pixels
+    both times (which fixes whether each fraction reaches 1/4 and 3/4).  Float
+    images: the output pixels are equal.  The masks the reference saved
+    (--save-masks) equal the oracle's weights (hard mask: the hard masks)."""
+    imgs, masks, levels, wrap, opts = _main_case(k)
+    hard = bool(opts.get("hard_mask", False))
+    if imgs[0].dtype == np.float32:
+        res = orc.enfuse_f(imgs, None, orc.params_from_options(opts, float_sliding_sums=True), masks=masks,
+                           levels=levels, wrap=wrap, hard_mask=hard, want_masks=True)
+        C = 3 if imgs[0].ndim == 3 else 1
+        assert np.array_equal(res["out"][..., :C] if imgs[0].ndim == 3 else res["out"], EGOLDEN[f"main{k}_out0"])
+    else:
+        res = orc.enfuse(imgs, None, orc.params_from_options(opts), masks=masks, levels=levels, wrap=wrap,
+                         hard_mask=hard, want_level0=True, want_masks=True)
+        l0 = res["level0"] if imgs[0].ndim == 3 else res["level0"][..., 0]
+        for j, draw in enumerate((0, 0xFFFFFFFF)):
+            assert np.array_equal(orc.convert_with_draw(l0, res["alpha"], imgs[0].dtype, draw),
+                                  EGOLDEN[f"main{k}_out{j}"]), draw
+    assert np.array_equal((res["alpha"] != 0).astype(np.uint8), EGOLDEN[f"main{k}_alpha"])
+    if f"main{k}_saved_masks" in EGOLDEN:
+        saved = EGOLDEN[f"main{k}_saved_masks"]
+        if hard:
+            assert np.array_equal(res["masks"], saved)
+        else:
+            for i, x in enumerate(imgs):
+                a = orc.alpha_of(x)
+                if x.dtype == np.float32:
+                    w = orc.enfuse_mask_f(x, a, orc.params_from_options(opts, float_sliding_sums=True))
+                else:
+                    w = orc.enfuse_mask(x, a, orc.params_from_options(opts))
+                assert np.array_equal(w, saved[i], equal_nan=True), i
+
+
+@pytest.mark.skipif(not ref.available(), reason="the reference tree is not present")
+@pytest.mark.parametrize("seed", range(4))
+def test_live_enfuse_against_reference(orc, seed):
+    """Random weighting options and images: oracle == reference (enfuseMask
+    and enfuseMain under both constant dither draws)."""
+    from enbgpu import synthetic
+    rng = np.random.default_rng(1000 + seed)
+    dt = [np.uint8, np.uint16][seed % 2]
+    h, w, K = int(rng.integers(20, 45)), int(rng.integers(20, 60)), int(rng.integers(2, 6))
+    opts = dict(exposure_weight=float(rng.choice([0.0, 1.0])), saturation_weight=float(rng.choice([0.0, 0.2])),
+                contrast_weight=float(rng.choice([0.0, 0.5])), entropy_weight=float(rng.choice([0.0, 0.3])),
+                contrast_window_size=int(rng.choice([3, 5])), entropy_window_size=int(rng.choice([3, 5])),
+                exposure_weight_function=str(rng.choice(["gaussian", "lorentzian", "bisquare"])))
+    if sum(opts[k] for k in ("exposure_weight", "saturation_weight", "contrast_weight", "entropy_weight")) == 0:
+        opts["exposure_weight"] = 1.0
+    imgs = synthetic.exposure_stack(h, w, list(np.linspace(-2, 2, K)), dt, 8.0, seed=seed)
+    for x in imgs:
+        assert np.array_equal(orc.enfuse_mask(x, None, orc.params_from_options(opts)),
+                              ref.enfuse_mask(x, orc.alpha_of(x), ref.enfuse_params(**opts)))
+    res = orc.enfuse(imgs, None, orc.params_from_options(opts), want_level0=True)
+    for draw in (0, 0xFFFFFFFF):
+        r = ref.enfuse_main(imgs, ref.enfuse_params(**opts), dither=draw)
+        assert np.array_equal(orc.convert_with_draw(res["level0"], res["alpha"], dt, draw), r["out"])
