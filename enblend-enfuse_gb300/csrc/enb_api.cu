@@ -588,6 +588,10 @@ enb_status check_params(enb_ctx* ctx, const enb_enfuse_params* p, int w, int h)
               "unknown exposure weight function");
     ENB_CHECK(ctx, p->gray_projector >= ENB_GRAY_AVERAGE && p->gray_projector <= ENB_GRAY_MIXER,
               "unknown grayscale projector");
+    ENB_CHECK(ctx,
+              p->exp_cutoff_lower_projector >= ENB_GRAY_AVERAGE && p->exp_cutoff_lower_projector <= ENB_GRAY_MIXER &&
+                  p->exp_cutoff_upper_projector >= ENB_GRAY_AVERAGE && p->exp_cutoff_upper_projector <= ENB_GRAY_MIXER,
+              "unknown grayscale projector of the exposure cutoff");
     if (p->w_contrast > 0.0) {
         ENB_CHECK(ctx, p->contrast_window >= 3 && (p->contrast_window & 1) && p->contrast_window <= kMaxContrastWindow,
                   "contrast window must be odd, 3..31");
@@ -626,6 +630,103 @@ double float_range_of(const enb_enfuse_params* prm)
     return prm->float_range > 0.0 ? prm->float_range : 3.4028234663852886e38;
 }
 
+// AlternativePercentage::is_effective / CompactifiedAlternativePercentage::
+// is_effective (src/alternativepercentage.h:44-52, 76-83) for samples whose
+// maximum is maxv.
+bool cutoff_effective(double v, int pct, double maxv, bool compact)
+{
+    if (compact) {
+        return v != 0.0 && ((pct && fabs(v) != 100.0) || (!pct && v != maxv));
+    }
+    return v > 0.0 && ((pct && v < 100.0) || (!pct && v < maxv));
+}
+
+// instantiate<t> (src/alternativepercentage.h:54-60, 85-95): the limit in
+// sample units, truncated toward zero for integer samples, rounded to float
+// for float samples; the compactified form counts a negative value down
+// from the maximum.
+double cutoff_value(double v, int pct, double maxv, bool integral, bool compact)
+{
+    double c;
+    if (compact) {
+        c = pct ? (v >= 0.0 ? v : 100.0 + v) * maxv / 100.0 : (v >= 0.0 ? v : maxv + v);
+    } else {
+        c = pct ? v * maxv / 100.0 : v;
+    }
+    return integral ? trunc(c) : (double)(float)c;
+}
+
+// The limits of an exposure or entropy cutoff: the lower limit a plain, the
+// upper one a compactified percentage, as both options are documented.  The
+// reference's exposure functor instantiates its upper limit through the
+// plain base class (src/enfuse.h:659-661), which agrees for every
+// non-negative limit; negative limits and a lower limit above the upper one
+// are errors there (exit(1), src/enfuse.h:667-685, 1154-1172) and here.
+enb_status cutoff_limits(enb_ctx* ctx, const char* what, double lower, int lower_pct, double upper, int upper_pct,
+                         double maxv, bool integral, bool& active, double& lo, double& hi)
+{
+    active = cutoff_effective(lower, lower_pct, maxv, false) || cutoff_effective(upper, upper_pct, maxv, true);
+    if (!active) {
+        return ENB_OK;
+    }
+    lo = cutoff_value(lower, lower_pct, maxv, integral, false);
+    hi = cutoff_value(upper, upper_pct, maxv, integral, true);
+    ENB_CHECK(ctx, lo >= 0.0, std::string("negative lower ") + what + " cutoff");
+    ENB_CHECK(ctx, hi >= 0.0, std::string("negative upper ") + what + " cutoff");
+    ENB_CHECK(ctx, lo <= hi, std::string("lower ") + what + " cutoff exceeds upper cutoff");
+    return ENB_OK;
+}
+
+// The cutoffs of integer samples with maximum maxv in WeightParams: limits
+// outside [0, maxv] act as the nearest value outside that range.
+enb_status int_cutoffs(enb_ctx* ctx, const enb_enfuse_params* prm, uint32_t maxv, WeightParams& wp)
+{
+    const auto clampi = [&](double v) { return (int32_t)std::min(std::max(v, -1.0), (double)maxv + 1.0); };
+    bool on = false;
+    double lo = 0.0, hi = 0.0;
+    if (prm->w_exposure > 0.0) {
+        ENB_TRY(cutoff_limits(ctx, "exposure", prm->exp_cutoff_lower, prm->exp_cutoff_lower_pct, prm->exp_cutoff_upper,
+                              prm->exp_cutoff_upper_pct, (double)maxv, true, on, lo, hi));
+        wp.exp_cut = on;
+        wp.cut_proj[0] = prm->exp_cutoff_lower_projector;
+        wp.cut_proj[1] = prm->exp_cutoff_upper_projector;
+        wp.cut_lo = clampi(lo);
+        wp.cut_hi = clampi(hi);
+    }
+    if (prm->w_entropy > 0.0) {
+        ENB_TRY(cutoff_limits(ctx, "entropy", prm->ent_cutoff_lower, prm->ent_cutoff_lower_pct, prm->ent_cutoff_upper,
+                              prm->ent_cutoff_upper_pct, (double)maxv, true, on, lo, hi));
+        wp.ent_cut = on;
+        wp.ent_lo = clampi(lo);
+        wp.ent_hi = clampi(hi);
+    }
+    return ENB_OK;
+}
+
+// The cutoffs of float samples (limits relative to float_range's scale).
+enb_status float_cutoffs(enb_ctx* ctx, const enb_enfuse_params* prm, double range, FloatWeightParams& wp)
+{
+    bool on = false;
+    double lo = 0.0, hi = 0.0;
+    if (prm->w_exposure > 0.0) {
+        ENB_TRY(cutoff_limits(ctx, "exposure", prm->exp_cutoff_lower, prm->exp_cutoff_lower_pct, prm->exp_cutoff_upper,
+                              prm->exp_cutoff_upper_pct, range, false, on, lo, hi));
+        wp.exp_cut = on;
+        wp.cut_proj[0] = prm->exp_cutoff_lower_projector;
+        wp.cut_proj[1] = prm->exp_cutoff_upper_projector;
+        wp.cut_lo = (float)lo;
+        wp.cut_hi = (float)hi;
+    }
+    if (prm->w_entropy > 0.0) {
+        ENB_TRY(cutoff_limits(ctx, "entropy", prm->ent_cutoff_lower, prm->ent_cutoff_lower_pct, prm->ent_cutoff_upper,
+                              prm->ent_cutoff_upper_pct, range, false, on, lo, hi));
+        wp.ent_cut = on;
+        wp.ent_lo = (float)lo;
+        wp.ent_hi = (float)hi;
+    }
+    return ENB_OK;
+}
+
 enb_status alpha_plane(enb_ctx* ctx, const enb_image* img, const enb_image* alpha, DevBuf& buf, BytePlane& out);
 
 enb_status enfuse_mask_float(enb_ctx* ctx, const enb_enfuse_params* prm, const enb_image* src,
@@ -658,6 +759,7 @@ enb_status enfuse_mask_float(enb_ctx* ctx, const enb_enfuse_params* prm, const e
     const double inv_width = 1.0 / exposure_effective_width(prm->exp_function, prm->exp_width);
     wp.inv_hi = (float)inv_width;
     wp.inv_lo = (float)(inv_width - (double)wp.inv_hi);
+    ENB_TRY(float_cutoffs(ctx, prm, range, wp));
     const PixelView pv = pixel_view(src);
     DevBuf abuf;
     BytePlane ap;
@@ -693,6 +795,7 @@ enb_status enfuse_mask_impl(enb_ctx* ctx, const enb_enfuse_params* prm, const en
     wp.w_sat_hi = (float)prm->w_saturation;
     wp.w_sat_lo = (float)(prm->w_saturation - (double)wp.w_sat_hi);
     wp.maxv = maxv;
+    ENB_TRY(int_cutoffs(ctx, prm, maxv, wp));
     ENB_LAUNCH(ctx, launch_enfuse_mask(pixel_view(src), alpha_source(src, alpha), wp, ctx->tables, out, ctx->stream));
     return ENB_OK;
 }
@@ -1402,6 +1505,18 @@ void enb_default_enfuse_params(enb_enfuse_params* p)
     p->contrast_window = 5;
     p->entropy_window = 3;
     p->gray_projector = ENB_GRAY_AVERAGE;
+    // --exposure-cutoff 0%:100%:anti-value:value, --entropy-cutoff 0%:100%
+    // (src/enfuse.cc:124-127, 141-142)
+    p->exp_cutoff_lower = 0.0;
+    p->exp_cutoff_lower_pct = 1;
+    p->exp_cutoff_upper = 100.0;
+    p->exp_cutoff_upper_pct = 1;
+    p->exp_cutoff_lower_projector = ENB_GRAY_ANTI_VALUE;
+    p->exp_cutoff_upper_projector = ENB_GRAY_VALUE;
+    p->ent_cutoff_lower = 0.0;
+    p->ent_cutoff_lower_pct = 1;
+    p->ent_cutoff_upper = 100.0;
+    p->ent_cutoff_upper_pct = 1;
 }
 
 void enb_default_fuse_options(enb_fuse_options* o)
@@ -1931,7 +2046,7 @@ static enb_status float_weight_params(enb_ctx* ctx, const enb_enfuse_params* prm
     const double inv_width = 1.0 / exposure_effective_width(prm->exp_function, prm->exp_width);
     wp.inv_hi = (float)inv_width;
     wp.inv_lo = (float)(inv_width - (double)wp.inv_hi);
-    return ENB_OK;
+    return float_cutoffs(ctx, prm, range, wp);
 }
 
 // What the batched fuse's work depends on: the stacks' sizes, exposure
@@ -2316,6 +2431,15 @@ enb_status enb_fuse_grad(enb_ctx* ctx, const enb_enfuse_params* prm, int K, cons
     ENB_CHECK(ctx, !o.wrap && !o.hard_mask, "fuse_grad: wrap-around and hard masks are not differentiated");
     if (prm->w_entropy > 0.0) {
         return fail(ctx, ENB_ERR_UNSUPPORTED, "fuse_grad: the entropy weight is not differentiated");
+    }
+    {
+        bool cut = false;
+        double lo = 0.0, hi = 0.0;
+        ENB_TRY(cutoff_limits(ctx, "exposure", prm->exp_cutoff_lower, prm->exp_cutoff_lower_pct, prm->exp_cutoff_upper,
+                              prm->exp_cutoff_upper_pct, float_range_of(prm), false, cut, lo, hi));
+        if (cut && prm->w_exposure > 0.0) {
+            return fail(ctx, ENB_ERR_UNSUPPORTED, "fuse_grad: the exposure cutoff is not differentiated");
+        }
     }
     ENB_TRY(check_params(ctx, prm, w, h));
     const int L = enb_num_levels(w, h, 1, o.levels);

@@ -130,8 +130,8 @@ __global__ void __launch_bounds__(256, 4) k_batch_weights(const BatchStack* __re
     const int4 job = jobs[blockIdx.x];
     const BatchStack& s = stacks[job.x];
     const int halo = fweight_halo(wp);
-    const FTile t = ftile_carve(bsmem, BWT + 2 * halo, wp.repeat_slots);
-    float* wk = reinterpret_cast<float*>(bsmem + align16(ftile_bytes(t.TW, t.slots))) + threadIdx.x;  // [K][BWT * BWT]
+    const FTile t = ftile_carve(bsmem, BWT + 2 * halo, wp.repeat_slots, wp.ent_cut);
+    float* wk = reinterpret_cast<float*>(bsmem + align16(ftile_bytes(t.TW, t.slots, wp.ent_cut))) + threadIdx.x;  // [K][BWT * BWT]
     const int lx = threadIdx.x % BWT, ly = threadIdx.x / BWT;
     const int x = job.y * BWT + lx, y = job.z * BWT + ly;
     const bool inside = x < s.w && y < s.h;
@@ -734,7 +734,7 @@ cudaError_t batch_plan_create(const std::vector<BatchStackHost>& hs, const Float
     const int TW = BWT + 2 * halo;
     p->wp.repeat_slots = fweight_slots(wp, TW);
     // the tile, then the K weights of each output pixel
-    p->wsmem = align16(ftile_bytes(TW, p->wp.repeat_slots)) + (size_t)p->maxK * BWT * BWT * sizeof(float);
+    p->wsmem = align16(ftile_bytes(TW, p->wp.repeat_slots, p->wp.ent_cut)) + (size_t)p->maxK * BWT * BWT * sizeof(float);
     double b = 0.0;
     add_step(0, 0, 0.0);
     for (int i = 0; i < p->nstacks; ++i) {

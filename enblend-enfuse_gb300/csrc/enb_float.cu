@@ -251,7 +251,7 @@ __global__ void __launch_bounds__(256) k_f_enfuse_mask(FloatPixelView img, const
 {
     extern __shared__ __align__(16) unsigned char fsmem[];
     const int halo = fweight_halo(wp);
-    const FTile t = ftile_carve(fsmem, FWT + 2 * halo, wp.repeat_slots);
+    const FTile t = ftile_carve(fsmem, FWT + 2 * halo, wp.repeat_slots, wp.ent_cut);
     const int opaque = ftile_load(t, wp, img.p, img.pitch, img.stride, img.w, img.h, img.C, alpha, apitch,
                                   blockIdx.x * FWT - halo, blockIdx.y * FWT - halo);
     const int lx = threadIdx.x % FWT, ly = threadIdx.x / FWT;
@@ -358,7 +358,7 @@ cudaError_t launch_f_enfuse_mask(const FloatPixelView& img, const BytePlane& alp
     const int TW = FWT + 2 * fweight_halo(wp);
     FloatWeightParams p = wp;
     p.repeat_slots = fweight_slots(wp, TW);
-    const size_t smem = ftile_bytes(TW, p.repeat_slots);
+    const size_t smem = ftile_bytes(TW, p.repeat_slots, p.ent_cut);
     note_launch("f_enfuse_mask", npix(img.w, img.h) * (img.stride * 4.0 + 1.0 + 4.0));
     const int cw = p.use_contrast ? p.contrast_window : 5, ew = p.use_entropy ? p.entropy_window : 5;
     void (*k)(FloatPixelView, const uint8_t*, int64_t, FloatWeightParams, WeightTables, float*, int64_t) =

@@ -50,9 +50,9 @@ __device__ __forceinline__ float third_of(float s)
 // RealPromote of float is float: the average adds the samples in float and
 // divides by 3.0 in double, the lightness adds min and max in float;
 // luminance (0.3/0.59/0.11) and the channel mixer are double expressions.
-__device__ __forceinline__ float gray_of_f(const FloatWeightParams& p, float r, float g, float b)
+__device__ __forceinline__ float gray_proj_f(int projector, const FloatWeightParams& p, float r, float g, float b)
 {
-    switch (p.gray_projector) {
+    switch (projector) {
     case ENB_GRAY_VALUE: return fmaxf(r, fmaxf(g, b));
     case ENB_GRAY_ANTI_VALUE: return fminf(r, fminf(g, b));
     case ENB_GRAY_LIGHTNESS: return 0.5f * __fadd_rn(fminf(r, fminf(g, b)), fmaxf(r, fmaxf(g, b)));
@@ -63,6 +63,26 @@ __device__ __forceinline__ float gray_of_f(const FloatWeightParams& p, float r, 
         return __double2float_rn(__dadd_rn(__dadd_rn(__dmul_rn(p.mixer[0], (double)r), __dmul_rn(p.mixer[1], (double)g)),
                                            __dmul_rn(p.mixer[2], (double)b)));
     default: return third_of(__fadd_rn(__fadd_rn(r, g), b));
+    }
+}
+
+__device__ __forceinline__ float gray_of_f(const FloatWeightParams& p, float r, float g, float b)
+{
+    return gray_proj_f(p.gray_projector, p, r, g, b);
+}
+
+// ClampingFunctor of the entropy cutoff (src/enfuse.h:893-925) on float
+// samples: x <= lo -> 0, x >= hi -> range, else x; the third sample is
+// judged low by the first.
+__device__ __forceinline__ void entropy_clamp_f(const FloatWeightParams& p, float (&rgb)[3], int C)
+{
+    const bool red_low = rgb[0] <= p.ent_lo;
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+        if (ch < C) {
+            const bool low = (C == 3 && ch == 2) ? red_low : rgb[ch] <= p.ent_lo;
+            rgb[ch] = low ? 0.0f : (rgb[ch] >= p.ent_hi ? p.range : rgb[ch]);
+        }
     }
 }
 
@@ -157,10 +177,14 @@ __device__ __forceinline__ float entropy_f(const uint32_t* v, int n, const Weigh
 
 // ---- one exposure's tile in shared memory -----------------------------------
 
+__host__ __device__ inline size_t align16_sz(size_t n) { return (n + 15) & ~(size_t)15; }
+
 // Tile of (TW x TW) input pixels around a block of output pixels: gray,
 // the three samples, the window counters (clip values, repeat marks, opaque
 // flags; enb_entropy.cuh), the repeat hash tables and the opaque flags.
 // TW is even (16 + 2 * halo), which keeps every array 16-byte aligned.
+// With the entropy cutoff the entropy windows read their own, clamped
+// copy of the samples (eraw); else eraw is raw.
 struct FTile {
     float* gray;     // [TW*TW]
     float* raw;      // [3][TW*TW]
@@ -168,17 +192,19 @@ struct FTile {
     uint32_t* table; // [3][slots]
     uint8_t* flags;  // [3][slots]
     uint8_t* a;      // [TW*TW]
+    float* eraw;     // [3][TW*TW] (entropy cutoff) or raw
     int TW, slots;
 };
 
-__host__ __device__ inline size_t ftile_bytes(int TW, int slots)
+__host__ __device__ inline size_t ftile_bytes(int TW, int slots, int ent_cut = 0)
 {
-    return (size_t)TW * TW * (4 * sizeof(float) + sizeof(uint64_t) + 1) + (size_t)slots * 3 * 5;
+    return align16_sz((size_t)TW * TW * (4 * sizeof(float) + sizeof(uint64_t) + 1) + (size_t)slots * 3 * 5) +
+           (ent_cut ? (size_t)TW * TW * 3 * sizeof(float) : 0);
 }
 
 __host__ __device__ inline size_t align16(size_t n) { return (n + 15) & ~(size_t)15; }
 
-__device__ __forceinline__ FTile ftile_carve(unsigned char* smem, int TW, int slots)
+__device__ __forceinline__ FTile ftile_carve(unsigned char* smem, int TW, int slots, int ent_cut = 0)
 {
     FTile t;
     t.TW = TW;
@@ -189,6 +215,7 @@ __device__ __forceinline__ FTile ftile_carve(unsigned char* smem, int TW, int sl
     t.table = reinterpret_cast<uint32_t*>(t.cnt + TW * TW);
     t.flags = reinterpret_cast<uint8_t*>(t.table + 3 * slots);
     t.a = t.flags + 3 * slots;
+    t.eraw = ent_cut ? reinterpret_cast<float*>(smem + ftile_bytes(TW, slots, 0)) : t.raw;
     return t;
 }
 
@@ -199,10 +226,20 @@ __device__ __forceinline__ void ftile_put_px(const FTile& t, const FloatWeightPa
     const int TT = t.TW * t.TW;
     t.gray[k] = C == 1 ? rgb[0] : gray_of_f(wp, rgb[0], rgb[1], rgb[2]);
     t.a[k] = a;
-    t.cnt[k] = a ? (uint64_t)clip_counts(rgb, C) | (1ull << kCntOpaque) : 0ull;
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) {
         t.raw[ch * TT + k] = rgb[ch];
+    }
+    if (wp.ent_cut) {
+        float e[3] = {rgb[0], rgb[1], rgb[2]};
+        entropy_clamp_f(wp, e, C);
+        t.cnt[k] = a ? (uint64_t)clip_counts(e, C) | (1ull << kCntOpaque) : 0ull;
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+            t.eraw[ch * TT + k] = e[ch];
+        }
+    } else {
+        t.cnt[k] = a ? (uint64_t)clip_counts(rgb, C) | (1ull << kCntOpaque) : 0ull;
     }
 }
 
@@ -259,9 +296,9 @@ __device__ __forceinline__ int ftile_load(const FTile& t, const FloatWeightParam
     const int opaque = __syncthreads_and(mine);
     if (t.slots) {
         if (TT <= 2 * (int)blockDim.x) {
-            mark_repeats<2>(t.raw, TT, t.a, TT, C, t.table, t.flags, t.slots, t.cnt);
+            mark_repeats<2>(t.eraw, TT, t.a, TT, C, t.table, t.flags, t.slots, t.cnt);
         } else {
-            mark_repeats<0>(t.raw, TT, t.a, TT, C, t.table, t.flags, t.slots, t.cnt);
+            mark_repeats<0>(t.eraw, TT, t.a, TT, C, t.table, t.flags, t.slots, t.cnt);
         }
     }
     return opaque;
@@ -336,7 +373,7 @@ template <int EW>
 __device__ __forceinline__ float window_entropy(const FTile& t, const FloatWeightParams& wp, const WeightTables& tab,
                                                 int ci, int ch, int nwin, uint32_t marks, uint32_t clips)
 {
-    const float* raw = t.raw + ch * t.TW * t.TW;
+    const float* raw = t.eraw + ch * t.TW * t.TW;
     const int nmax = (EW > 0 ? EW * EW : wp.entropy_window * wp.entropy_window);
     if (EW > 0) {
         if (!(marks & (1u << ch))) {
@@ -378,7 +415,18 @@ __device__ __forceinline__ float f_pixel_weight(const FTile& t, const FloatWeigh
     }
     float result = 0.0f;
     if (wp.use_exposure) {
-        result = wp.w_exposure * exposure_f(wp, t.gray[ci]);
+        bool pass = true;
+        if (wp.exp_cut) {
+            float lv = t.gray[ci], uv = lv;
+            if (C == 3) {
+                const int TT = t.TW * t.TW;
+                const float r = t.raw[ci], g = t.raw[TT + ci], bb = t.raw[2 * TT + ci];
+                lv = gray_proj_f(wp.cut_proj[0], wp, r, g, bb);
+                uv = gray_proj_f(wp.cut_proj[1], wp, r, g, bb);
+            }
+            pass = lv >= wp.cut_lo && uv <= wp.cut_hi;
+        }
+        result = pass ? wp.w_exposure * exposure_f(wp, t.gray[ci]) : 0.0f;
     }
     if (wp.use_contrast) {
         const int b = wp.contrast_window / 2;

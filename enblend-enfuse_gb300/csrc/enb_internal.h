@@ -85,6 +85,15 @@ struct WeightParams {
     double w_saturation;
     float w_sat_hi, w_sat_lo; // w_saturation split into two floats
     uint32_t maxv;
+    // exposure cutoff (src/enfuse.h:652-730): exposure weight only where
+    // cut_lo <= lower projection and upper projection <= cut_hi
+    int exp_cut;
+    int cut_proj[2];
+    int32_t cut_lo, cut_hi;
+    // entropy cutoff (src/enfuse.h:1143-1192): samples <= ent_lo -> 0,
+    // >= ent_hi -> maxv before the entropy windows
+    int ent_cut;
+    int32_t ent_lo, ent_hi;
 };
 
 // Weights of float images (src/enfuse.h:962-1212 with float pixels).
@@ -100,6 +109,14 @@ struct FloatWeightParams {
     float opt_hi, opt_lo;  // exposure optimum as a sum of two floats
     float inv_hi, inv_lo;  // 1 / effective width of the weight function, ditto
     int repeat_slots;      // hash slots per channel of the repeated-sample marks (0: none)
+    // exposure cutoff (src/enfuse.h:652-730) and entropy cutoff (src/enfuse.h:
+    // 1143-1192), as in WeightParams with float limits (upper clamp value:
+    // range)
+    int exp_cut;
+    int cut_proj[2];
+    float cut_lo, cut_hi;
+    int ent_cut;
+    float ent_lo, ent_hi;
 };
 
 // Name and algorithmic bytes of the most recent launch on this host thread;

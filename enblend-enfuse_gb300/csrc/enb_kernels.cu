@@ -408,9 +408,9 @@ constexpr int WT = 16;  // 16x16 weight pixels per CTA
 // average = fromRealPromote((r+g+b)/3.0) = (r+g+b+1)/3 and lightness =
 // fromRealPromote((min+max)/2.0) = (min+max+1)/2 exactly for non-negative
 // integers; luminance and the mixer evaluate the reference's double sums.
-__device__ __forceinline__ int32_t gray_of(const WeightParams& wp, uint32_t r, uint32_t g, uint32_t b)
+__device__ __forceinline__ int32_t gray_proj(int projector, const WeightParams& wp, uint32_t r, uint32_t g, uint32_t b)
 {
-    switch (wp.gray_projector) {
+    switch (projector) {
     case ENB_GRAY_VALUE: return (int32_t)max(r, max(g, b));
     case ENB_GRAY_ANTI_VALUE: return (int32_t)min(r, min(g, b));
     case ENB_GRAY_LIGHTNESS: return (int32_t)((min(r, min(g, b)) + max(r, max(g, b)) + 1) >> 1);
@@ -425,6 +425,25 @@ __device__ __forceinline__ int32_t gray_of(const WeightParams& wp, uint32_t r, u
         return (int32_t)frp_unsigned(s, wp.maxv);
     }
     default: return (int32_t)((r + g + b + 1u) / 3u);
+    }
+}
+
+__device__ __forceinline__ int32_t gray_of(const WeightParams& wp, uint32_t r, uint32_t g, uint32_t b)
+{
+    return gray_proj(wp.gray_projector, wp, r, g, b);
+}
+
+// ClampingFunctor of the entropy cutoff (src/enfuse.h:893-925): x <= lo -> 0,
+// x >= hi -> max, else x; the third sample is judged low by the first.
+__device__ __forceinline__ void entropy_clamp(const WeightParams& wp, uint32_t (&rgb)[3], int C)
+{
+    const bool red_low = (int32_t)rgb[0] <= wp.ent_lo;
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+        if (ch < C) {
+            const bool low = (C == 3 && ch == 2) ? red_low : (int32_t)rgb[ch] <= wp.ent_lo;
+            rgb[ch] = low ? 0u : ((int32_t)rgb[ch] >= wp.ent_hi ? wp.maxv : rgb[ch]);
+        }
     }
 }
 
@@ -551,6 +570,11 @@ __global__ void __launch_bounds__(256) k_enfuse_mask(PixelView img, AlphaSrc alp
             }
             g = C == 1 ? (int32_t)rgb[0] : gray_of(wp, rgb[0], rgb[1], rgb[2]);
             a = (uint8_t)alpha_at(alpha, gx, gy);
+            if (wp.ent_cut) {
+                // the tile's samples feed only the entropy windows then; the
+                // saturation reloads its pixel
+                entropy_clamp(wp, rgb, C);
+            }
         }
         s_gray[k] = g;
         s_a[k] = a;
@@ -570,7 +594,20 @@ __global__ void __launch_bounds__(256) k_enfuse_mask(PixelView img, AlphaSrc alp
     if (s_a[ci]) {
         const int32_t g = s_gray[ci];
         if (wp.use_exposure) {
-            result = tab.exposure[g];
+            bool pass = true;
+            if (wp.exp_cut) {
+                int32_t lv = g, uv = g;
+                if (C == 3) {
+                    // the unclamped samples of this pixel
+                    const int64_t base = (int64_t)y * img.pitch + (int64_t)x * img.stride;
+                    const uint32_t r = load_sample(img.p, img.dtype, base), gg = load_sample(img.p, img.dtype, base + 1),
+                                   bb = load_sample(img.p, img.dtype, base + 2);
+                    lv = gray_proj(wp.cut_proj[0], wp, r, gg, bb);
+                    uv = gray_proj(wp.cut_proj[1], wp, r, gg, bb);
+                }
+                pass = lv >= wp.cut_lo && uv <= wp.cut_hi;
+            }
+            result = pass ? tab.exposure[g] : 0.0f;
         }
         if (wp.use_contrast) {
             const int b = wp.contrast_window / 2;
@@ -595,7 +632,13 @@ __global__ void __launch_bounds__(256) k_enfuse_mask(PixelView img, AlphaSrc alp
             result = __fadd_rn(tab.contrast[gc], result);
         }
         if (wp.use_saturation && C == 3) {
-            const uint32_t r = s_raw[ci], gg = s_raw[TW * TW + ci], bb = s_raw[2 * TW * TW + ci];
+            uint32_t r = s_raw[ci], gg = s_raw[TW * TW + ci], bb = s_raw[2 * TW * TW + ci];
+            if (wp.ent_cut) {
+                const int64_t base = (int64_t)y * img.pitch + (int64_t)x * img.stride;
+                r = load_sample(img.p, img.dtype, base);
+                gg = load_sample(img.p, img.dtype, base + 1);
+                bb = load_sample(img.p, img.dtype, base + 2);
+            }
             const uint32_t mx = max(r, max(gg, bb)), mn = min(r, min(gg, bb));
             float sw = 0.0f;
             if (mx != mn) {

@@ -57,7 +57,12 @@ class EnbEnfuseParams(ctypes.Structure):
                 ("exp_optimum", ctypes.c_double), ("exp_width", ctypes.c_double),
                 ("exp_function", ctypes.c_int32), ("contrast_window", ctypes.c_int32),
                 ("entropy_window", ctypes.c_int32), ("gray_projector", ctypes.c_int32),
-                ("mixer", ctypes.c_double * 3), ("float_range", ctypes.c_double)]
+                ("mixer", ctypes.c_double * 3), ("float_range", ctypes.c_double),
+                ("exp_cutoff_lower", ctypes.c_double), ("exp_cutoff_upper", ctypes.c_double),
+                ("exp_cutoff_lower_pct", ctypes.c_int32), ("exp_cutoff_upper_pct", ctypes.c_int32),
+                ("exp_cutoff_lower_projector", ctypes.c_int32), ("exp_cutoff_upper_projector", ctypes.c_int32),
+                ("ent_cutoff_lower", ctypes.c_double), ("ent_cutoff_upper", ctypes.c_double),
+                ("ent_cutoff_lower_pct", ctypes.c_int32), ("ent_cutoff_upper_pct", ctypes.c_int32)]
 
 
 class EnbFuseOptions(ctypes.Structure):
@@ -224,11 +229,15 @@ def enfuse_params(exposure_weight: float = 1.0, saturation_weight: float = 0.0, 
                   entropy_weight: float = 0.0, exposure_optimum: float = 0.5, exposure_width: float = 0.2,
                   exposure_weight_function: str = "gaussian", contrast_window_size: int = 5,
                   entropy_window_size: int = 3, gray_projector: str = "average",
-                  mixer: Sequence[float] = (0.0, 0.0, 0.0), float_range: float = 0.0) -> EnbEnfuseParams:
-    """enfuse's weighting options (src/enfuse.cc:117-140, same defaults).
+                  mixer: Sequence[float] = (0.0, 0.0, 0.0), float_range: float = 0.0,
+                  exposure_cutoff=((0.0, True), (100.0, True)), exposure_cutoff_projectors=("anti-value", "value"),
+                  entropy_cutoff=((0.0, True), (100.0, True))) -> EnbEnfuseParams:
+    """enfuse's weighting options (src/enfuse.cc:117-160, same defaults).
 
     float_range: float images only; 0 takes the reference's NumericTraits<float>::max() as the sample scale of
-    the exposure and entropy weights, 1.0 is the normalised-float mode for images in [0, 1]."""
+    the exposure and entropy weights, 1.0 is the normalised-float mode for images in [0, 1].
+    exposure_cutoff / entropy_cutoff: (lower, upper) limits, each (value, is_percentage), as
+    --exposure-cutoff and --entropy-cutoff give them; exposure_cutoff_projectors judge the two limits."""
     p = EnbEnfuseParams()
     p.w_exposure, p.w_saturation = exposure_weight, saturation_weight
     p.w_contrast, p.w_entropy = contrast_weight, entropy_weight
@@ -238,6 +247,12 @@ def enfuse_params(exposure_weight: float = 1.0, saturation_weight: float = 0.0, 
     p.gray_projector = GRAY_PROJECTORS[gray_projector]
     p.mixer[:] = list(mixer)
     p.float_range = float_range
+    (p.exp_cutoff_lower, p.exp_cutoff_lower_pct), (p.exp_cutoff_upper, p.exp_cutoff_upper_pct) = \
+        [(float(v), int(bool(pct))) for v, pct in exposure_cutoff]
+    p.exp_cutoff_lower_projector = GRAY_PROJECTORS[exposure_cutoff_projectors[0]]
+    p.exp_cutoff_upper_projector = GRAY_PROJECTORS[exposure_cutoff_projectors[1]]
+    (p.ent_cutoff_lower, p.ent_cutoff_lower_pct), (p.ent_cutoff_upper, p.ent_cutoff_upper_pct) = \
+        [(float(v), int(bool(pct))) for v, pct in entropy_cutoff]
     return p
 
 

@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define ENBGPU_ABI_VERSION 3
+#define ENBGPU_ABI_VERSION 4
 
 typedef enum {
     ENB_OK = 0,
@@ -111,6 +111,25 @@ typedef struct {
                                > 0: normalised-float mode, e.g. 1.0 for images
                                in [0, 1].  Saturation (max 1.0) and contrast
                                (W * sigma) are the same in both modes. */
+    /* --exposure-cutoff LOWER[:UPPER[:LOWERPROJ[:UPPERPROJ]]]
+     * (src/enfuse.cc:1272-1340, CutoffExposureFunctor src/enfuse.h:652-730):
+     * a pixel whose lower projection lies below the lower limit, or whose
+     * upper projection lies above the upper limit, gets exposure weight 0.
+     * A limit with its *_pct flag set is a percentage of the sample maximum
+     * (of float_range's scale for float images), else an absolute sample
+     * value; integer limits truncate toward zero; a negative upper limit
+     * counts down from the maximum.  Defaults: 0 % / 100 % (off), projectors
+     * anti-value / value (enb_gray_projector). */
+    double exp_cutoff_lower, exp_cutoff_upper;
+    int32_t exp_cutoff_lower_pct, exp_cutoff_upper_pct;
+    int32_t exp_cutoff_lower_projector, exp_cutoff_upper_projector;
+    /* --entropy-cutoff LOWER[:UPPER] (src/enfuse.cc:1213-1270, src/enfuse.h:
+     * 1143-1192): before the entropy windows, samples at or below the lower
+     * limit become 0 and samples at or above the upper limit the maximum
+     * (the third sample is judged low by the first sample, as the reference
+     * does).  Limits as for the exposure cutoff; defaults 0 % / 100 % (off). */
+    double ent_cutoff_lower, ent_cutoff_upper;
+    int32_t ent_cutoff_lower_pct, ent_cutoff_upper_pct;
 } enb_enfuse_params;
 
 /* Options of the fuse drivers. */
@@ -358,8 +377,8 @@ typedef struct {
  * its 9.15 quantisation), the loss against `target`, and its gradients:
  * the scalars in `res` and, when grad_logits is given, dL/d logit_k per
  * pixel.  logits: K F32 planes or NULL (all 0).  out: optional F32 image
- * receiving the forward result.  Entropy weights, hard masks and wrap-around
- * are not differentiated (ENB_ERR_UNSUPPORTED).  The backward rebuilds each
+ * receiving the forward result.  Entropy weights, the exposure cutoff, hard
+ * masks and wrap-around are not differentiated (ENB_ERR_UNSUPPORTED).  The backward rebuilds each
  * exposure's Laplacian pyramid instead of keeping K of them, so the memory
  * held is one pyramid per kind whatever K.  Device buffers; synchronous. */
 enb_status enb_fuse_grad(enb_ctx* ctx, const enb_enfuse_params* params, int K, const enb_image* images,
