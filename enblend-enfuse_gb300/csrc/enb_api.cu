@@ -1104,12 +1104,150 @@ enb_status enblend_fused(enb_ctx* ctx, const enb_image* white, const enb_image* 
     return ENB_OK;
 }
 
+// enfuseMain's pyramid section for 8/16-bit images as fused level passes
+// (enb_efuse.cu): weights of all exposures per tile with the normalised
+// masks as level 0 of the mask pyramids, K-job reduces, one up pass per
+// level, level 0 straight to the output pixels.  The integers are the
+// per-operation path's (and the reference's).
+enb_status enfuse_fused(enb_ctx* ctx, const enb_enfuse_params* prm, int K, const enb_image* images,
+                        const enb_image* alphas, const enb_image* masks_in, const enb_image* out,
+                        const enb_image* out_alpha, const enb_fuse_options& o, int32_t* level0, int L)
+{
+    const int w = images[0].width, h = images[0].height, C = images[0].channels, dt = images[0].dtype;
+    const size_t ps = dt == ENB_U8 ? 2 : 4;  // Int16 / Int32 pyramids and masks
+    EfuseHost eh{};
+    eh.K = K;
+    eh.L = L;
+    eh.w = w;
+    eh.h = h;
+    eh.C = C;
+    eh.S = pixel_view(&images[0]).stride;
+    eh.dtype = dt;
+    eh.hard = o.hard_mask != 0;
+    eh.wrap = o.wrap != 0;
+    eh.dither = o.dither;
+    eh.seed = o.seed;
+    eh.level0 = level0;
+    const uint32_t maxv = dt == ENB_U8 ? 255u : 65535u;
+    if (!masks_in) {
+        ENB_TRY(build_tables(ctx, prm, maxv));
+        WeightParams& wp = eh.wp;
+        wp.use_exposure = prm->w_exposure > 0.0;
+        wp.use_contrast = prm->w_contrast > 0.0;
+        wp.use_saturation = prm->w_saturation > 0.0;
+        wp.use_entropy = prm->w_entropy > 0.0;
+        wp.contrast_window = prm->contrast_window;
+        wp.entropy_window = prm->entropy_window;
+        wp.gray_projector = prm->gray_projector;
+        if (prm->gray_projector == ENB_GRAY_MIXER) {
+            const double sm = prm->mixer[0] + prm->mixer[1] + prm->mixer[2];
+            for (int i = 0; i < 3; ++i) {
+                wp.mixer[i] = prm->mixer[i] / sm;
+            }
+        }
+        wp.w_saturation = prm->w_saturation;
+        wp.w_sat_hi = (float)prm->w_saturation;
+        wp.w_sat_lo = (float)(prm->w_saturation - (double)wp.w_sat_hi);
+        wp.maxv = maxv;
+        ENB_TRY(int_cutoffs(ctx, prm, maxv, wp));
+        eh.tab = ctx->tables;
+    } else {
+        eh.wp.maxv = maxv;
+    }
+    for (int k = 0; k < K; ++k) {
+        eh.img[k] = pixel_view(&images[k]);
+        eh.alpha[k] = alpha_source(&images[k], alphas ? &alphas[k] : nullptr);
+        if (masks_in) {
+            ENB_CHECK(ctx, floats_ok(&masks_in[k], w, h), "masks_in: F32 planes of the image size expected");
+            eh.masks_in[k] = (const float*)masks_in[k].data;
+            eh.mipitch[k] = masks_in[k].pitch / 4;
+        }
+    }
+    // level geometry and one allocation for every plane
+    int64_t total = 0;
+    int64_t off_m[kMaxLevels] = {}, off_g[kMaxLevels] = {}, off_a[kMaxLevels] = {}, off_u[kMaxLevels] = {},
+            off_r[kMaxLevels] = {};
+    for (int l = 0; l < L; ++l) {
+        eh.lw[l] = l == 0 ? w : (eh.lw[l - 1] + 1) >> 1;
+        eh.lh[l] = l == 0 ? h : (eh.lh[l - 1] + 1) >> 1;
+        eh.pitch[l] = round_up(eh.lw[l], 64);
+        eh.apitch[l] = round_up(eh.lw[l], 128);
+        const int64_t plane = eh.pitch[l] * eh.lh[l] * (int64_t)ps, aplane = eh.apitch[l] * eh.lh[l];
+        off_m[l] = total;
+        total += K * plane;
+        if (l >= 1) {
+            off_g[l] = total;
+            total += K * C * plane;
+            off_a[l] = total;
+            total += round_up(K * aplane, 256);
+            off_u[l] = total;
+            total += round_up(aplane, 256);
+            off_r[l] = total;
+            total += C * plane;
+        }
+    }
+    BytePlane ua;
+    DevBuf ua_buf;
+    if (out_alpha && out_alpha->data) {
+        ENB_CHECK(ctx, bytes_ok(out_alpha, w, h), "out_alpha: must be U8 of the image size");
+        ua = byte_plane(out_alpha);
+    } else {
+        const int64_t pitch = round_up(w, 128);
+        ENB_CUDA(ctx, ua_buf.alloc((size_t)(pitch * h), ctx->stream));
+        ua = BytePlane{(uint8_t*)ua_buf.p, pitch, w, h};
+    }
+    DevBuf mem;
+    ENB_CUDA(ctx, mem.alloc((size_t)total, ctx->stream));
+    uint8_t* base = (uint8_t*)mem.p;
+    for (int l = 0; l < L; ++l) {
+        const int64_t plane = eh.pitch[l] * eh.lh[l] * (int64_t)ps, aplane = eh.apitch[l] * eh.lh[l];
+        for (int k = 0; k < K; ++k) {
+            eh.m[k][l] = base + off_m[l] + k * plane;
+            if (l >= 1) {
+                eh.g[k][l] = base + off_g[l] + (int64_t)k * C * plane;
+                eh.a[k][l] = base + off_a[l] + k * aplane;
+            }
+        }
+        if (l >= 1) {
+            eh.u[l] = base + off_u[l];
+            eh.r[l] = base + off_r[l];
+        }
+    }
+    eh.u[0] = ua.p;
+    eh.upitch0 = ua.pitch;
+    eh.out = out->data;
+    eh.opitch = pixel_view(out).pitch;
+
+    ENB_LAUNCH(ctx, launch_ef_weights(eh, ctx->stream));
+    for (int l = 0; l + 1 < L; ++l) {
+        ENB_LAUNCH(ctx, launch_ef_reduce(eh, l, 0, ctx->stream));
+        ENB_LAUNCH(ctx, launch_ef_reduce(eh, l, 1, ctx->stream));
+    }
+    ENB_LAUNCH(ctx, launch_ef_top(eh, ctx->stream));
+    for (int l = L - 2; l >= 1; --l) {
+        ENB_LAUNCH(ctx, launch_ef_up(eh, l, ctx->stream));
+    }
+    ENB_LAUNCH(ctx, launch_ef_out0(eh, ctx->stream));
+    return ENB_OK;
+}
+
 enb_status enfuse_device(enb_ctx* ctx, const enb_enfuse_params* prm, int K, const enb_image* images,
                          const enb_image* alphas, const enb_image* masks_in, const enb_image* out,
                          const enb_image* out_alpha, const enb_fuse_options& o, int32_t* level0)
 {
     const int w = images[0].width, h = images[0].height, C = images[0].channels, dt = images[0].dtype;
     const int L = enb_num_levels(w, h, 1, o.levels);
+    if (!o.plain && dt != ENB_F32 && K <= kEfuseMaxK && L >= 2 && pixel_view(out).stride == pixel_view(&images[0]).stride) {
+        // one alpha mode for all exposures (the level-1 reduce is compiled per mode)
+        bool uniform = true;
+        const int m0 = alpha_source(&images[0], alphas ? &alphas[0] : nullptr).mode;
+        for (int k = 1; k < K; ++k) {
+            uniform = uniform && alpha_source(&images[k], alphas ? &alphas[k] : nullptr).mode == m0;
+        }
+        if (uniform) {
+            return enfuse_fused(ctx, prm, K, images, alphas, masks_in, out, out_alpha, o, level0, L);
+        }
+    }
     const int pdt = fixed_bits_image(dt), mdt = fixed_bits_mask(dt), mf = mask_frac(dt);
     const int wrap = o.wrap != 0;
     const int64_t fpitch = round_up(w, 32);

@@ -79,6 +79,39 @@ __device__ __forceinline__ TD mask_to_fixed(float m, int frac)
     return frp_store<TD>(__dmul_rn((double)m, (double)(1u << frac)));
 }
 
+// fromRealPromote(lp * fl(m / D)) with D = 255 * 2^F (src/enfuse.h:601-620).
+//
+// For 0 < m < D the exact value t = lp*m/D has denominator 2D after adding
+// 1/2, so its distance to the rounding boundary is either 0 or >= 1/(2D);
+// the double expression differs from t by < 2^-26, which is smaller.  Hence
+// round-half-away(t) is the reference's result unless t is exactly a
+// half-integer, in which case the double expression is evaluated as is.
+template <typename T, int F>
+__device__ __forceinline__ T mask_multiply(int32_t lp, int32_t m)
+{
+    constexpr int32_t D = 255 << F;
+    if (m == 0) {
+        return (T)0;  // lp * 0.0 rounds to 0
+    }
+    if (m == D) {
+        return (T)lp;  // coefficient exactly 1.0
+    }
+    const uint32_t a = lp < 0 ? (uint32_t)(-(int64_t)lp) : (uint32_t)lp;
+    if (m > 0 && m < D && a < (1u << 24)) {
+        const uint64_t N = 2ull * (uint64_t)a * (uint64_t)m + (uint64_t)D;
+        const uint32_t hi = (uint32_t)(N >> (F + 1));
+        const uint32_t lo = (uint32_t)(N & ((1ull << (F + 1)) - 1));
+        const uint32_t q = hi / 255u;
+        const bool tie = lo == 0 && hi == q * 255u;
+        if (!tie) {
+            const int32_t r = lp < 0 ? -(int32_t)q : (int32_t)q;
+            return sizeof(T) == 2 ? (T)min(max(r, -32768), 32767) : (T)r;
+        }
+    }
+    const double coeff = __ddiv_rn((double)m, (double)D);
+    return frp_store<T>(__dmul_rn((double)lp, coeff));
+}
+
 __host__ __device__ __forceinline__ int imod(int a, int m)
 {
     int r = a % m;

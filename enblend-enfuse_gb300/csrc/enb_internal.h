@@ -262,6 +262,41 @@ cudaError_t launch_out0(const PlanarView* gw1, const PlanarView* gb1, const Plan
                         cudaStream_t st, int ty0 = 0, int nty = -1);
 cudaError_t launch_coarse(const CoarseHost& h, cudaStream_t st);
 
+// fused enfuse of K 8/16-bit images (enb_efuse.cu): the level passes of
+// enfuseMain's pyramids (src/enfuse.h:1501-1617) with the weights of all
+// exposures per tile, no level 0 of any image pyramid stored, one up pass
+// per level and level 0 straight to the output pixels.
+constexpr int kEfuseMaxK = 16;
+struct EfuseHost {
+    int K, L, w, h, C, S, dtype;   // exposures, levels, canvas, colour samples, samples a pixel, ENB_U8/U16
+    PixelView img[kEfuseMaxK];
+    AlphaSrc alpha[kEfuseMaxK];
+    const float* masks_in[kEfuseMaxK];  // --load-masks planes or null
+    int64_t mipitch[kEfuseMaxK];        // floats
+    int hard;
+    WeightParams wp;
+    WeightTables tab;
+    int lw[kMaxLevels], lh[kMaxLevels];
+    int64_t pitch[kMaxLevels];     // elements of every image/mask/result plane of level l
+    int64_t apitch[kMaxLevels];    // bytes of the alpha planes of level l
+    void* m[kEfuseMaxK][kMaxLevels];      // mask pyramids M_k[l] (Int16 9.7 / Int32 9.15)
+    void* g[kEfuseMaxK][kMaxLevels];      // image pyramids G_k[l], l >= 1 (C planes)
+    uint8_t* a[kEfuseMaxK][kMaxLevels];   // their alpha, l >= 1
+    uint8_t* u[kMaxLevels];               // union alpha U[l] (U[0]: the output alpha plane)
+    int64_t upitch0;                      // bytes of U[0]
+    void* r[kMaxLevels];                  // result levels R[l], l >= 1 (C planes)
+    void* out;                            // output pixels (the input type, S samples a pixel)
+    int64_t opitch;                       // elements
+    int32_t* level0;                      // collapsed level 0 (interleaved int32) or null
+    int wrap, dither;
+    uint64_t seed;
+};
+cudaError_t launch_ef_weights(const EfuseHost& h, cudaStream_t st);
+cudaError_t launch_ef_reduce(const EfuseHost& h, int l, int masks, cudaStream_t st);
+cudaError_t launch_ef_top(const EfuseHost& h, cudaStream_t st);
+cudaError_t launch_ef_up(const EfuseHost& h, int l, cudaStream_t st);
+cudaError_t launch_ef_out0(const EfuseHost& h, cudaStream_t st);
+
 // batched fuse of float stacks (enb_batch.cu)
 constexpr int kBatchMaxK = 16;
 struct BatchStackHost {

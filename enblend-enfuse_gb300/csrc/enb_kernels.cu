@@ -13,26 +13,10 @@
 #include "enb_device.cuh"
 #include "enb_internal.h"
 #include "enb_entropy.cuh"
+#include "enb_iweights.cuh"
 #include "enb_reduce.cuh"
 
 namespace enb {
-
-__device__ __forceinline__ int alpha_at(const AlphaSrc& a, int x, int y)
-{
-    if (a.mode == kAlphaOpaque) {
-        return 1;
-    }
-    if (a.mode == kAlphaPlane) {
-        return a.plane.p[(int64_t)y * a.plane.pitch + x] != 0;
-    }
-    const int64_t i = (int64_t)y * a.pix.pitch + (int64_t)x * a.pix.stride + 3;
-    if (a.pix.dtype == ENB_F32) {
-        const float f = reinterpret_cast<const float*>(a.pix.p)[i];
-        return f >= a.flo && f <= a.fhi;
-    }
-    const uint32_t v = load_sample(a.pix.p, a.pix.dtype, i);
-    return v >= a.lo && v <= a.hi;
-}
 
 // ---------------------------------------------------------------------------
 // Conversions to fixed point (src/fixmath.h:116-206)
@@ -259,39 +243,6 @@ __global__ void __launch_bounds__(256) k_blend(const TM* __restrict__ mask, int6
     }
 }
 
-// fromRealPromote(lp * fl(m / D)) with D = 255 * 2^F (src/enfuse.h:601-620).
-//
-// For 0 < m < D the exact value t = lp*m/D has denominator 2D after adding
-// 1/2, so its distance to the rounding boundary is either 0 or >= 1/(2D);
-// the double expression differs from t by < 2^-26, which is smaller.  Hence
-// round-half-away(t) is the reference's result unless t is exactly a
-// half-integer, in which case the double expression is evaluated as is.
-template <typename T, int F>
-__device__ __forceinline__ T mask_multiply(int32_t lp, int32_t m)
-{
-    constexpr int32_t D = 255 << F;
-    if (m == 0) {
-        return (T)0;  // lp * 0.0 rounds to 0
-    }
-    if (m == D) {
-        return (T)lp;  // coefficient exactly 1.0
-    }
-    const uint32_t a = lp < 0 ? (uint32_t)(-(int64_t)lp) : (uint32_t)lp;
-    if (m > 0 && m < D && a < (1u << 24)) {
-        const uint64_t N = 2ull * (uint64_t)a * (uint64_t)m + (uint64_t)D;
-        const uint32_t hi = (uint32_t)(N >> (F + 1));
-        const uint32_t lo = (uint32_t)(N & ((1ull << (F + 1)) - 1));
-        const uint32_t q = hi / 255u;
-        const bool tie = lo == 0 && hi == q * 255u;
-        if (!tie) {
-            const int32_t r = lp < 0 ? -(int32_t)q : (int32_t)q;
-            return sizeof(T) == 2 ? (T)min(max(r, -32768), 32767) : (T)r;
-        }
-    }
-    const double coeff = __ddiv_rn((double)m, (double)D);
-    return frp_store<T>(__dmul_rn((double)lp, coeff));
-}
-
 template <typename T, typename TM, int C, int F>
 __global__ void __launch_bounds__(256) k_mask_mul_acc(const T* __restrict__ lp, int64_t lpitch, int64_t lplane,
                                                       const TM* __restrict__ mask, int64_t mpitch,
@@ -402,292 +353,20 @@ __global__ void __launch_bounds__(256) k_copy_level0(const T* __restrict__ src, 
 // enfuse weights (src/enfuse.h:962-1212)
 // ---------------------------------------------------------------------------
 
-constexpr int WT = 16;  // 16x16 weight pixels per CTA
-
-// MultiGrayscaleAccessor::project for integer RGB (src/mga.h:185-222):
-// average = fromRealPromote((r+g+b)/3.0) = (r+g+b+1)/3 and lightness =
-// fromRealPromote((min+max)/2.0) = (min+max+1)/2 exactly for non-negative
-// integers; luminance and the mixer evaluate the reference's double sums.
-__device__ __forceinline__ int32_t gray_proj(int projector, const WeightParams& wp, uint32_t r, uint32_t g, uint32_t b)
-{
-    switch (projector) {
-    case ENB_GRAY_VALUE: return (int32_t)max(r, max(g, b));
-    case ENB_GRAY_ANTI_VALUE: return (int32_t)min(r, min(g, b));
-    case ENB_GRAY_LIGHTNESS: return (int32_t)((min(r, min(g, b)) + max(r, max(g, b)) + 1) >> 1);
-    case ENB_GRAY_LUMINANCE: {
-        const double s = __dadd_rn(__dadd_rn(__dmul_rn(0.3, (double)r), __dmul_rn(0.59, (double)g)),
-                                   __dmul_rn(0.11, (double)b));
-        return (int32_t)frp_unsigned(s, wp.maxv);
-    }
-    case ENB_GRAY_MIXER: {
-        const double s = __dadd_rn(__dadd_rn(__dmul_rn(wp.mixer[0], (double)r), __dmul_rn(wp.mixer[1], (double)g)),
-                                   __dmul_rn(wp.mixer[2], (double)b));
-        return (int32_t)frp_unsigned(s, wp.maxv);
-    }
-    default: return (int32_t)((r + g + b + 1u) / 3u);
-    }
-}
-
-__device__ __forceinline__ int32_t gray_of(const WeightParams& wp, uint32_t r, uint32_t g, uint32_t b)
-{
-    return gray_proj(wp.gray_projector, wp, r, g, b);
-}
-
-// ClampingFunctor of the entropy cutoff (src/enfuse.h:893-925): x <= lo -> 0,
-// x >= hi -> max, else x; the third sample is judged low by the first.
-__device__ __forceinline__ void entropy_clamp(const WeightParams& wp, uint32_t (&rgb)[3], int C)
-{
-    const bool red_low = (int32_t)rgb[0] <= wp.ent_lo;
-#pragma unroll
-    for (int ch = 0; ch < 3; ++ch) {
-        if (ch < C) {
-            const bool low = (C == 3 && ch == 2) ? red_low : (int32_t)rgb[ch] <= wp.ent_lo;
-            rgb[ch] = low ? 0u : ((int32_t)rgb[ch] >= wp.ent_hi ? wp.maxv : rgb[ch]);
-        }
-    }
-}
-
-// fromRealPromote(sqrt((Q - S*S/n) / (n-1))) of the window sums
-// (src/enfuse.h:154-160).  The exact value sqrt((nQ - S^2)/(n(n-1))) is
-// approximated in float (error < 0.01); unless it lies within 0.03 of a
-// rounding boundary that decides the integer, otherwise the reference's
-// double expression is evaluated.
-__device__ __forceinline__ int32_t stddev_round(int64_t S, int64_t Q, int n)
-{
-    if (n <= 1) {
-        return 0;
-    }
-    const int64_t num = (int64_t)n * Q - S * S;
-    const float r = sqrtf(__fdiv_rn((float)num, (float)(n * (n - 1))));
-    const float x = r + 0.5f;
-    const float fl = floorf(x);
-    const float d = x - fl;
-    if (d > 0.03f && d < 0.97f) {
-        return (int32_t)fl;
-    }
-    const double sum = (double)S;
-    const double var = __ddiv_rn(__dadd_rn((double)Q, -__ddiv_rn(__dmul_rn(sum, sum), (double)n)), (double)(n - 1));
-    const double sd = __dsqrt_rn(var);
-    return __double2int_rz(__dadd_rn(sd, 0.5));
-}
-
-// Histogram::entropyOfChannel of n sorted samples (src/enfuse.h:346-375),
-// scaled by the channel maximum and rounded (Histogram::entropyFun).  The
-// sum of p log p is accumulated exactly in 2^-56 fixed point for a float
-// estimate; near a rounding boundary the reference's double sum (bins in
-// ascending key order) is evaluated.
-__device__ int32_t entropy_round(const uint16_t* v, int n, const WeightTables& tab, int nmax, uint32_t maxv)
-{
-    if (n == 0) {
-        return 0;
-    }
-    int bins = 0;
-    long long acc = 0;
-    const long long* fx = tab.plogp_fx + (int64_t)n * (nmax + 1);
-    int i = 0;
-    while (i < n) {
-        int j = i + 1;
-        while (j < n && v[j] == v[i]) {
-            ++j;
-        }
-        acc += fx[j - i];
-        ++bins;
-        i = j;
-    }
-    if (bins <= 1) {
-        return 0;
-    }
-    const float e = -(float)acc * 1.3877787807814457e-17f;  // 2^-56
-    const float val = __fmul_rn(e, tab.scale_logb[bins]);
-    const float x = val + 0.5f;
-    const float fl = floorf(x);
-    const float d = x - fl;
-    if (d > 0.03f && d < 0.97f) {
-        return (int32_t)min((uint32_t)max(fl, 0.0f), maxv);
-    }
-    const double* pl = tab.plogp + (int64_t)n * (nmax + 1);
-    double es = 0.0;
-    i = 0;
-    while (i < n) {
-        int j = i + 1;
-        while (j < n && v[j] == v[i]) {
-            ++j;
-        }
-        es = __dadd_rn(es, pl[j - i]);
-        i = j;
-    }
-    const double H = __ddiv_rn(-es, tab.logb[bins]);
-    return (int32_t)frp_unsigned(__dmul_rn(H, (double)maxv), maxv);
-}
-
-// (float)(w * s) with s = fl(d / S) in double, d < S integers
-// (SaturationFunctor, src/enfuse.h:755-776), via a float-float product;
-// near a float rounding midpoint the double expression is evaluated.
-__device__ __forceinline__ float saturation_weight(const WeightParams& wp, uint32_t d, uint32_t S)
-{
-    const float fd = (float)d, fS = (float)S;
-    const float q1 = __fdiv_rn(fd, fS);
-    const float rem = __fmaf_rn(-q1, fS, fd);       // exact remainder
-    const float q2 = __fdiv_rn(rem, fS);
-    const float p_hi = __fmul_rn(wp.w_sat_hi, q1);
-    const float e1 = __fmaf_rn(wp.w_sat_hi, q1, -p_hi);
-    const float p_lo = __fadd_rn(e1, __fadd_rn(__fmul_rn(wp.w_sat_hi, q2), __fmul_rn(wp.w_sat_lo, q1)));
-    const float s = __fadd_rn(p_hi, p_lo);
-    // residual of the float-float value against its rounding s
-    const float t = __fadd_rn(__fadd_rn(p_hi, -s), p_lo);
-    const float ulp = __int_as_float(__float_as_int(s) + 1) - s;
-    const float dist = fabsf(fabsf(t) - 0.5f * ulp);
-    const bool pow2 = (__float_as_int(s) & 0x7fffff) == 0;  // ulp below s is half as large
-    if (dist > 1.0e-5f * ulp && s > 1.0e-30f && !pow2) {
-        return s;
-    }
-    const double sd = __ddiv_rn((double)d, (double)S);
-    return (float)__dmul_rn(wp.w_saturation, sd);
-}
-
 __global__ void __launch_bounds__(256) k_enfuse_mask(PixelView img, AlphaSrc alpha, WeightParams wp,
                                                      WeightTables tab, float* __restrict__ out, int64_t opitch)
 {
     extern __shared__ unsigned char smem[];
-    const int halo = max(wp.use_contrast ? wp.contrast_window / 2 : 0, wp.use_entropy ? wp.entropy_window / 2 : 0);
-    const int TW = WT + 2 * halo;
-    int32_t* s_gray = reinterpret_cast<int32_t*>(smem);
-    uint16_t* s_raw = reinterpret_cast<uint16_t*>(s_gray + TW * TW);   // [C][TW*TW]
-    uint8_t* s_a = reinterpret_cast<uint8_t*>(s_raw + 3 * TW * TW);
-
-    const int x0 = blockIdx.x * WT - halo, y0 = blockIdx.y * WT - halo;
-    const int w = img.w, h = img.h, C = img.C;
-    for (int k = threadIdx.x; k < TW * TW; k += blockDim.x) {
-        const int r = k / TW, c = k - r * TW;
-        const int gx = x0 + c, gy = y0 + r;
-        int32_t g = 0;
-        uint8_t a = 0;
-        uint32_t rgb[3] = {0, 0, 0};
-        if (gx >= 0 && gx < w && gy >= 0 && gy < h) {
-            const int64_t base = (int64_t)gy * img.pitch + (int64_t)gx * img.stride;
-            for (int ch = 0; ch < C; ++ch) {
-                rgb[ch] = load_sample(img.p, img.dtype, base + ch);
-            }
-            g = C == 1 ? (int32_t)rgb[0] : gray_of(wp, rgb[0], rgb[1], rgb[2]);
-            a = (uint8_t)alpha_at(alpha, gx, gy);
-            if (wp.ent_cut) {
-                // the tile's samples feed only the entropy windows then; the
-                // saturation reloads its pixel
-                entropy_clamp(wp, rgb, C);
-            }
-        }
-        s_gray[k] = g;
-        s_a[k] = a;
-        for (int ch = 0; ch < 3; ++ch) {
-            s_raw[ch * TW * TW + k] = (uint16_t)rgb[ch];
-        }
-    }
+    const int halo = iweight_halo(wp);
+    const ITile t = itile_carve(smem, WT + 2 * halo);
+    itile_load(t, wp, img, alpha, blockIdx.x * WT - halo, blockIdx.y * WT - halo);
     __syncthreads();
-
     const int lx = threadIdx.x % WT, ly = threadIdx.x / WT;
     const int x = blockIdx.x * WT + lx, y = blockIdx.y * WT + ly;
-    if (x >= w || y >= h) {
+    if (x >= img.w || y >= img.h) {
         return;
     }
-    const int ci = (ly + halo) * TW + (lx + halo);
-    float result = 0.0f;
-    if (s_a[ci]) {
-        const int32_t g = s_gray[ci];
-        if (wp.use_exposure) {
-            bool pass = true;
-            if (wp.exp_cut) {
-                int32_t lv = g, uv = g;
-                if (C == 3) {
-                    // the unclamped samples of this pixel
-                    const int64_t base = (int64_t)y * img.pitch + (int64_t)x * img.stride;
-                    const uint32_t r = load_sample(img.p, img.dtype, base), gg = load_sample(img.p, img.dtype, base + 1),
-                                   bb = load_sample(img.p, img.dtype, base + 2);
-                    lv = gray_proj(wp.cut_proj[0], wp, r, gg, bb);
-                    uv = gray_proj(wp.cut_proj[1], wp, r, gg, bb);
-                }
-                pass = lv >= wp.cut_lo && uv <= wp.cut_hi;
-            }
-            result = pass ? tab.exposure[g] : 0.0f;
-        }
-        if (wp.use_contrast) {
-            const int b = wp.contrast_window / 2;
-            uint32_t gc = 0;
-            if (x >= b && x < w - b && y >= b && y < h - b) {
-                int64_t S = 0, Q = 0;
-                int n = 0;
-                for (int dy = -b; dy <= b; ++dy) {
-                    const int row = (ly + halo + dy) * TW + lx + halo;
-                    for (int dx = -b; dx <= b; ++dx) {
-                        if (s_a[row + dx]) {
-                            const int64_t v = s_gray[row + dx];
-                            S += v;
-                            Q += v * v;
-                            ++n;
-                        }
-                    }
-                }
-                // the combine lambda receives the gradient as the pixel's scalar type
-                gc = (uint32_t)stddev_round(S, Q, n) & wp.maxv;
-            }
-            result = __fadd_rn(tab.contrast[gc], result);
-        }
-        if (wp.use_saturation && C == 3) {
-            uint32_t r = s_raw[ci], gg = s_raw[TW * TW + ci], bb = s_raw[2 * TW * TW + ci];
-            if (wp.ent_cut) {
-                const int64_t base = (int64_t)y * img.pitch + (int64_t)x * img.stride;
-                r = load_sample(img.p, img.dtype, base);
-                gg = load_sample(img.p, img.dtype, base + 1);
-                bb = load_sample(img.p, img.dtype, base + 2);
-            }
-            const uint32_t mx = max(r, max(gg, bb)), mn = min(r, min(gg, bb));
-            float sw = 0.0f;
-            if (mx != mn) {
-                const uint32_t sum = mx + mn;
-                const uint32_t S = sum <= wp.maxv ? sum : 2u * wp.maxv - sum;
-                sw = saturation_weight(wp, mx - mn, S);
-            }
-            result = __fadd_rn(sw, result);
-        }
-        if (wp.use_entropy) {
-            const int b = wp.entropy_window / 2;
-            uint32_t emin = 0;
-            if (x >= b && x < w - b && y >= b && y < h - b) {
-                uint16_t vals[kMaxEntropyWindow * kMaxEntropyWindow];
-                const int nmax = wp.entropy_window * wp.entropy_window;
-                emin = wp.maxv;
-                for (int ch = 0; ch < C; ++ch) {
-                    if (wp.entropy_window == 5 || wp.entropy_window == 3) {
-                        const uint16_t* raw = s_raw + ch * TW * TW;
-                        const uint32_t e = wp.entropy_window == 5
-                                               ? entropy_window_int<5>(raw, s_a, TW, ci, tab, wp.maxv)
-                                               : entropy_window_int<3>(raw, s_a, TW, ci, tab, wp.maxv);
-                        emin = min(emin, e);
-                        continue;
-                    }
-                    int n = 0;
-                    for (int dy = -b; dy <= b; ++dy) {
-                        const int row = (ly + halo + dy) * TW + lx + halo;
-                        for (int dx = -b; dx <= b; ++dx) {
-                            if (s_a[row + dx]) {
-                                // insertion into the sorted prefix
-                                const uint16_t v = s_raw[ch * TW * TW + row + dx];
-                                int p = n++;
-                                while (p > 0 && vals[p - 1] > v) {
-                                    vals[p] = vals[p - 1];
-                                    --p;
-                                }
-                                vals[p] = v;
-                            }
-                        }
-                    }
-                    const uint32_t e = (uint32_t)entropy_round(vals, n, tab, nmax, wp.maxv);
-                    emin = min(emin, e);
-                }
-            }
-            result = __fadd_rn(tab.entropy[emin], result);
-        }
-    }
-    out[(int64_t)y * opitch + x] = result;
+    out[(int64_t)y * opitch + x] = i_pixel_weight(t, wp, tab, img, (ly + halo) * t.TW + (lx + halo), x, y);
 }
 
 __global__ void __launch_bounds__(256) k_norm_accumulate(const float* __restrict__ m, int64_t mpitch,

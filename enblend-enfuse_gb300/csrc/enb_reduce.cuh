@@ -311,6 +311,35 @@ inline void launch_reduce_jobs(ReduceJobs<Src, TD> jobs, int njobs, int sw, int 
     (void)launch_pdl(k_reduce<Src, TD, C, ALPHA>, g, dim3(RTHREADS), st, jobs, sw, sh, dw, dh, wrap);
 }
 
+// Up to kReduceMaxJobs jobs of one geometry in one launch (blockIdx.z = job):
+// the K exposures of a fused enfuse level.
+constexpr int kReduceMaxJobs = 16;
+
+template <class Src, typename TD>
+struct ReduceJobsN {
+    ReduceJob<Src, TD> j[kReduceMaxJobs];
+};
+
+template <class Src, typename TD, int C, bool ALPHA>
+__global__ void __launch_bounds__(RTHREADS, 3) k_reduce_n(const __grid_constant__ ReduceJobsN<Src, TD> jobs, int sw,
+                                                          int sh, int dw, int dh, int wrap)
+{
+    typedef typename ReduceAcc<TD>::type AC;
+    __shared__ __align__(16) AC V[ReduceSmem<C, ALPHA>::NV][RDH][RVP];
+    griddep_wait();
+    griddep_launch();
+    reduce_tile<Src, TD, C, ALPHA, AC>(jobs.j[blockIdx.z], blockIdx.x * RDW, blockIdx.y * RDH, sw, sh, dw, dh, wrap,
+                                       V);
+}
+
+template <class Src, typename TD, int C, bool ALPHA>
+inline cudaError_t launch_reduce_n(const ReduceJobsN<Src, TD>& jobs, int njobs, int sw, int sh, int dw, int dh,
+                                   int wrap, cudaStream_t st)
+{
+    const dim3 g((unsigned)((dw + RDW - 1) / RDW), (unsigned)reduce_tile_rows(dh), (unsigned)njobs);
+    return launch_pdl(k_reduce_n<Src, TD, C, ALPHA>, g, dim3(RTHREADS), st, jobs, sw, sh, dw, dh, wrap);
+}
+
 template <class Src, typename TD, int C, bool ALPHA>
 inline void launch_reduce_tiles(const Src& src, int sw, int sh, TD* dst, int64_t dpitch, int64_t dplane, int dw,
                                 int dh, uint8_t* da, int64_t dapitch, int wrap, cudaStream_t st)

@@ -172,6 +172,30 @@ def expose_torch(lograd, ev: float):
     return torch.clamp(torch.exp2(lograd + ev) ** (1.0 / 2.2), 0.0, 1.0).contiguous()
 
 
+def exposure_stack_torch(h: int, w: int, evs, dtype, stops: float, seed: int, noise: float = 0.0, device="cuda"):
+    """Device-resident exposures of one scene (as exposure_stack, from the
+    device generator): clip((radiance * 2^ev)^(1/2.2) + N(0, noise), 0, 1)
+    quantised to uint8 / uint16 (torch tensors of shape (H, W, 3))."""
+    import torch
+    lr = log_radiance_torch(h, w, stops, seed, device)
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed + 7919)
+    maxv = 255.0 if np.dtype(dtype) == np.uint8 else 65535.0
+    out = []
+    for ev in evs:
+        v = torch.exp2(lr + ev) ** (1.0 / 2.2)
+        if noise > 0.0:
+            v = v + noise * torch.randn(v.shape, generator=gen, device=device)
+        q = torch.round(torch.clamp(v, 0.0, 1.0) * maxv).to(torch.int32)
+        if maxv == 255.0:
+            out.append(q.to(torch.uint8).contiguous())
+        else:
+            out.append(q.to(torch.int16).view(torch.uint16).contiguous())
+        del v, q
+    del lr
+    return out
+
+
 def uneven_stack_specs(n: int = 64, seed: int = 4, lo: int = 512, hi: int = 4096, kmin: int = 3, kmax: int = 7):
     """The batched workload: n stacks with width and height log-uniform in
     [lo, hi] and an exposure count uniform in {kmin..kmax}, EVs evenly spaced

