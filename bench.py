@@ -22,6 +22,9 @@ input pixels blended per second (2 x 4096 x 3072 = 25.17 Mpx per step).
   batched_fuse  the batched uneven-stack workload (64 FP32 stacks of
          uneven sizes and exposure counts): enb_fuse_stacks replayed as one
          CUDA graph against the plain per-stack path on the same GPU
+  enfuse_small / enfuse_large  enfuse of 3 x 1024x768 RGB u8 and of
+         9 x 6000x4000 RGB u16 (contrast and entropy 5x5 windows) through the
+         fused integer driver: value, e2e, roofline, kernels, CPU oracle
 
 --impl reference times that CPU implementation alone on the same metric.
 Multi-GPU runs are independent replicas (the path does not shard): each rank
@@ -69,6 +72,8 @@ def parse_args():
                     help="skip the batched uneven-stack measurement (batched_fuse object)")
     ap.add_argument("--batched-stacks", type=int, default=64)
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-fuse step (adjoint object)")
+    ap.add_argument("--no-enfuse", action="store_true",
+                    help="skip the enfuse workloads (enfuse_small: 3x1024x768 u8, enfuse_large: 9x6000x4000 u16)")
     ap.add_argument("--profile-batched", action="store_true",
                     help="run only a small batched fuse (4 stacks of 5 FP32 1024x768 exposures, every level above 0 "
                          "in the coarse kernel, no graph): the case of the batched kernels' ncu capture")
@@ -305,6 +310,119 @@ def batched_fuse(ctx, stream, n_stacks: int, reps: int = 3) -> dict:
     }
 
 
+# The enfuse workloads: 3 x 1024x768 RGB u8 (EV -2, 0, +2; exposure 1.0,
+# saturation 0.2) and 9 x 6000x4000 RGB u16 (EV -4..+4, 12-stop scene, sensor
+# noise N(0, 2^-12) before quantisation; exposure 1.0, saturation 0.2,
+# contrast 0.5 in 5x5 windows, entropy 0.3 in 5x5 windows).
+ENFUSE_WORKLOADS = {
+    "enfuse_3x1024x768_u8": dict(h=768, w=1024, evs=[-2.0, 0.0, 2.0], dtype=np.uint8, stops=8.0, noise=0.0,
+                                 kw=dict(saturation_weight=0.2), seed=1, cpu_rows=768, flush=True),
+    "enfuse_9x6000x4000_u16": dict(h=4000, w=6000, evs=[float(e) for e in range(-4, 5)], dtype=np.uint16,
+                                   stops=12.0, noise=2.0 ** -12,
+                                   kw=dict(saturation_weight=0.2, contrast_weight=0.5, entropy_weight=0.3,
+                                           contrast_window_size=5, entropy_window_size=5),
+                                   seed=3, cpu_rows=96, flush=False),
+}
+
+
+def enfuse_workload(ctx, stream, name: str, steps: int, cpu: bool) -> dict:
+    """One enfuse workload through enb_enfuse (the fused integer driver):
+    device-resident value with per-step CUDA events (the L2 flushed between
+    steps when the inputs fit in it), e2e through the host-buffer entry point
+    with pinned memory, the per-kernel profile with the dominant kernel's
+    roofline, and the CPU oracle on a bounded sample of the rows."""
+    import torch
+    import enbgpu
+    from enbgpu import synthetic
+    sp = ENFUSE_WORKLOADS[name]
+    h, w, K = sp["h"], sp["w"], len(sp["evs"])
+    imgs = synthetic.exposure_stack_torch(h, w, sp["evs"], sp["dtype"], sp["stops"], sp["seed"], sp["noise"])
+    prm = enbgpu.enfuse_params(**sp["kw"])
+    out = torch.empty_like(imgs[0])
+    oa = torch.empty((h, w), dtype=torch.uint8, device="cuda")
+    units = K * h * w / 1e6
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda") if sp["flush"] else None
+
+    def call():
+        ctx.enfuse(imgs, params=prm, out=out, out_alpha=oa)
+
+    for _ in range(3):
+        call()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    l0 = ctx.launches
+    for a, b in ev:
+        if flush is not None:
+            flush.zero_()   # L2 (129 MB) flushed outside the timed interval
+        a.record(stream)
+        call()
+        b.record(stream)
+    torch.cuda.synchronize()
+    launches = (ctx.launches - l0) // steps
+    ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+    # e2e: pinned host buffers, copies inside the call
+    pin = lambda t: t.cpu().pin_memory().numpy()  # noqa: E731
+    himgs = [pin(x) for x in imgs]
+    hout = torch.empty(tuple(out.shape), dtype=out.dtype).pin_memory().numpy()
+    hoa = torch.empty((h, w), dtype=torch.uint8).pin_memory().numpy()
+    for _ in range(2):
+        ctx.enfuse(himgs, params=prm, out=hout, out_alpha=hoa)
+    e2e_steps = max(2, min(steps, 5))
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(e2e_steps):
+        ctx.enfuse(himgs, params=prm, out=hout, out_alpha=hoa)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = f0.elapsed_time(f1) / e2e_steps
+    same = bool(np.array_equal(hout, out.cpu().numpy()))
+    # per-kernel profile
+    ctx.profile(True)
+    for _ in range(2):
+        call()
+    rep = ctx.profile_report()
+    ctx.profile(False)
+    total = sum(v["ms"] for v in rep.values())
+    dom = max(rep, key=lambda k: rep[k]["ms"])
+    d = rep[dom]
+    peaks = measured_peaks()
+    achieved = d["bytes"] / (d["ms"] / 1e3) / 1e9
+    res = {
+        "workload": name.replace("enfuse_", "enfuse ").replace("_", " ") + ", weights " +
+                    ", ".join(f"{k}={v}" for k, v in sorted(dict(exposure_weight=1.0, **sp["kw"]).items())),
+        "units": units, "metric": METRIC, "value": units / (ms / 1e3), "ms_per_step": ms, "steps": steps,
+        "l2": "flushed between steps (256 MB write)" if flush is not None else "inputs larger than L2",
+        "gpu_launches": launches,
+        "e2e": {"value": units / (e2e_ms / 1e3), "unit": METRIC, "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": int(sum(x.nbytes for x in himgs)),
+                "d2h_bytes_per_step": int(hout.nbytes + hoa.nbytes), "same_pixels_as_device_run": same},
+        "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
+                     "algorithmic_bytes_per_launch": d["bytes"] / d["launches"],
+                     "share_of_device_time": d["ms"] / total if total else None},
+        "kernels": {k: {"launches_per_step": v["launches"] / 2, "ms_per_step": v["ms"] / 2,
+                        "GBps": v["bytes"] / (v["ms"] / 1e3) / 1e9 if v["ms"] > 0 else None}
+                    for k, v in sorted(rep.items(), key=lambda kv: -kv[1]["ms"])},
+    }
+    if cpu:
+        from oracle import oracle
+        rows = sp["cpu_rows"]
+        sample = [x[:rows].copy() for x in himgs]
+        orc_prm = oracle.params(**sp["kw"])
+        oracle.enfuse([x[:16].copy() for x in sample], None, orc_prm)  # warm (build, page-in)
+        t = time.perf_counter()
+        oracle.enfuse(sample, None, orc_prm)
+        dt = time.perf_counter() - t
+        res["cpu_baseline"] = {"value": K * w * rows / 1e6 / dt, "unit": METRIC,
+                               "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)), "kind": "port",
+                               "sample": f"{K} x {w}x{rows} (the first {rows} rows of the workload), one run; serial "
+                                         "pyramid passes and OpenMP pointwise passes as in the reference"}
+    del imgs, out, oa, flush
+    torch.cuda.empty_cache()
+    return res
+
+
 def adjoint_step(ctx, stream, reps: int = 3) -> dict:
     """The differentiable fuse: 8 exposures of 2048x2048 FP32 RGB (EV -3.5..+3.5
     in 1-stop steps), loss = mean squared difference to the scene's tone-mapped
@@ -472,8 +590,12 @@ def run_ours(args) -> None:
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_oracle_rate(args.seed)
-    if rank == 0 and ws == 1 and not args.no_batched:
+    if rank == 0 and ws == 1 and not args.no_enfuse:
         del dw, db, dm, out, oa
+        torch.cuda.empty_cache()
+        line["enfuse_small"] = enfuse_workload(ctx, stream, "enfuse_3x1024x768_u8", 20, not args.no_cpu_baseline)
+        line["enfuse_large"] = enfuse_workload(ctx, stream, "enfuse_9x6000x4000_u16", 5, not args.no_cpu_baseline)
+    if rank == 0 and ws == 1 and not args.no_batched:
         line["batched_fuse"] = batched_fuse(ctx, stream, args.batched_stacks)
     if rank == 0 and ws == 1 and not args.no_adjoint:
         line["adjoint"] = adjoint_step(ctx, stream)

@@ -54,7 +54,7 @@ struct EfWeightsArgs {
 };
 
 template <typename TM>
-__global__ void __launch_bounds__(256) k_ef_weights(const __grid_constant__ EfWeightsArgs<TM> a)
+__global__ void __launch_bounds__(256, 3) k_ef_weights(const __grid_constant__ EfWeightsArgs<TM> a)
 {
     extern __shared__ __align__(16) unsigned char esmem[];
     const int halo = iweight_halo(a.wp);
@@ -161,6 +161,48 @@ __device__ __forceinline__ void ef_expand(const int32_t (*s)[ESW], bool interior
     expand_quad(s, qx, qy, X, Y, cw, ch, dw, dh, wrap, e);
 }
 
+// Two horizontally adjacent pixels (the first at an even x) of an
+// interleaved image as 2*S*sizeof(TIn) / UNIT words of UNIT bytes (UNIT: the
+// largest power of two, at most 16, dividing the pair's size; the caller
+// checks that the image's base and row pitch are multiples of it).
+template <int U> struct PairWord;
+template <> struct PairWord<2> { typedef uint16_t type; };
+template <> struct PairWord<4> { typedef uint32_t type; };
+template <> struct PairWord<8> { typedef uint2 type; };
+template <> struct PairWord<16> { typedef uint4 type; };
+
+template <typename TIn, int S>
+struct PixelPair {
+    static constexpr int BYTES = 2 * S * (int)sizeof(TIn);
+    static constexpr int UNIT = (BYTES % 16 == 0) ? 16 : (BYTES % 8 == 0) ? 8 : (BYTES % 4 == 0) ? 4 : 2;
+    static constexpr int NW = BYTES / UNIT;
+    typedef typename PairWord<UNIT>::type W;
+    __device__ __forceinline__ static void load(const TIn* p, TIn (&px)[2][S])
+    {
+        union {
+            W w[NW];
+            TIn s[2 * S];
+        } u;
+#pragma unroll
+        for (int i = 0; i < NW; ++i) {
+            u.w[i] = __ldg(reinterpret_cast<const W*>(p) + i);
+        }
+#pragma unroll
+        for (int i = 0; i < S; ++i) {
+            px[0][i] = u.s[i];
+            px[1][i] = u.s[S + i];
+        }
+    }
+};
+
+// Two adjacent samples of a planar level or mask (x even), as ld2 of the
+// enblend tiles through the read-only path.
+template <typename T>
+__device__ __forceinline__ void ld_pair(const T* p, int32_t& a, int32_t& b)
+{
+    ld2<T, true>(p, a, b);
+}
+
 // ---------------------------------------------------------------------------
 // top level: R = sum_k fromRealPromote(G_k * M_k / D)
 // ---------------------------------------------------------------------------
@@ -204,7 +246,7 @@ __global__ void __launch_bounds__(256) k_ef_top(const __grid_constant__ EfLevelA
 // coarse windows of every channel are staged together (one barrier);
 // ss holds (K + 1) * C windows.
 template <typename T, typename TM, int C, int F>
-__global__ void __launch_bounds__(256) k_ef_up(const __grid_constant__ EfLevelArgs<T, TM> a)
+__global__ void __launch_bounds__(256, 3) k_ef_up(const __grid_constant__ EfLevelArgs<T, TM> a)
 {
     extern __shared__ __align__(16) int32_t ewin[];
     int32_t (*ss)[ESH][ESW] = reinterpret_cast<int32_t (*)[ESH][ESW]>(ewin);
@@ -244,11 +286,35 @@ __global__ void __launch_bounds__(256) k_ef_up(const __grid_constant__ EfLevelAr
         ok[q] = XX < a.dw && YY < a.dh;
         off[q] = (int64_t)min(YY, a.dh - 1) * a.pitch + min(XX, a.dw - 1);
     }
-    for (int k = 0; k < K; ++k) {
-        int32_t m[4];
+    // both pixels of a quad row in one paired load where x + 1 is inside
+    const bool pair = X + 1 < a.dw;
+    // the fine values of exposure k: mask m[4], image g[C][4]
+    const auto fetch = [&](int k, int32_t (&m)[4], int32_t (&g)[C][4]) {
+        if (pair) {
+            ld_pair<TM>(a.m[k] + off[0], m[0], m[1]);
+            ld_pair<TM>(a.m[k] + off[2], m[2], m[3]);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            m[q] = (int32_t)__ldg(&a.m[k][off[q]]);
+            for (int c = 0; c < C; ++c) {
+                ld_pair<T>(a.g[k] + c * a.plane + off[0], g[c][0], g[c][1]);
+                ld_pair<T>(a.g[k] + c * a.plane + off[2], g[c][2], g[c][3]);
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                m[q] = (int32_t)__ldg(&a.m[k][off[q]]);
+#pragma unroll
+                for (int c = 0; c < C; ++c) {
+                    g[c][q] = (int32_t)__ldg(&a.g[k][c * a.plane + off[q]]);
+                }
+            }
+        }
+    };
+    int32_t m[4], g[C][4];
+    fetch(0, m, g);
+    for (int k = 0; k < K; ++k) {
+        int32_t mn[4], gn[C][4];
+        if (k + 1 < K) {
+            fetch(k + 1, mn, gn);  // in flight while exposure k is merged
         }
 #pragma unroll
         for (int c = 0; c < C; ++c) {
@@ -256,9 +322,18 @@ __global__ void __launch_bounds__(256) k_ef_up(const __grid_constant__ EfLevelAr
             ef_expand<true>(ss[k * C + c], interior, qx, qy, X, Y, a.cw, a.ch, a.dw, a.dh, a.wrap, e);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                const int32_t g = (int32_t)__ldg(&a.g[k][c * a.plane + off[q]]);
-                const int32_t lp = (int32_t)cast_store<T>((int64_t)g - e[q]);
+                const int32_t lp = (int32_t)cast_store<T>((int64_t)g[c][q] - e[q]);
                 acc[c][q] += (int32_t)mask_multiply<T, F>(lp, m[q]);
+            }
+        }
+        if (k + 1 < K) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                m[q] = mn[q];
+#pragma unroll
+                for (int c = 0; c < C; ++c) {
+                    g[c][q] = gn[c][q];
+                }
             }
         }
     }
@@ -297,10 +372,11 @@ struct EfOut0Args {
     int dither;
     uint32_t key;
     int32_t maxv;
+    int vec;  // the images' bases and pitches allow the paired pixel loads
 };
 
 template <typename TIn, typename T, typename TM, int C, int S, int F>
-__global__ void __launch_bounds__(256) k_ef_out0(const __grid_constant__ EfOut0Args<TIn, T, TM> a)
+__global__ void __launch_bounds__(256, 3) k_ef_out0(const __grid_constant__ EfOut0Args<TIn, T, TM> a)
 {
     extern __shared__ __align__(16) int32_t ewin[];
     int32_t (*ss)[ESH][ESW] = reinterpret_cast<int32_t (*)[ESH][ESW]>(ewin);
@@ -342,17 +418,46 @@ __global__ void __launch_bounds__(256) k_ef_out0(const __grid_constant__ EfOut0A
         XX[q] = min(XX[q], a.w - 1);
         YY[q] = min(YY[q], a.h - 1);
     }
-    for (int k = 0; k < K; ++k) {
-        int32_t m[4];
-        TIn px[4][S];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            m[q] = (int32_t)__ldg(&a.m0[k][(int64_t)YY[q] * a.mpitch + XX[q]]);
-            const TIn* p = a.img[k] + (int64_t)YY[q] * a.ipitch[k] + (int64_t)XX[q] * S;
+    // both pixels of a quad row in one paired load where x + 1 is inside and
+    // the images are aligned for it
+    const bool pair = a.vec && X + 1 < a.w;
+    const auto fetch = [&](int k, int32_t (&m)[4], TIn (&px)[4][S]) {
+        if (pair) {
+            ld_pair<TM>(a.m0[k] + (int64_t)YY[0] * a.mpitch + X, m[0], m[1]);
+            ld_pair<TM>(a.m0[k] + (int64_t)YY[2] * a.mpitch + X, m[2], m[3]);
+            TIn pp[2][S];
+            PixelPair<TIn, S>::load(a.img[k] + (int64_t)YY[0] * a.ipitch[k] + (int64_t)X * S, pp);
 #pragma unroll
             for (int s = 0; s < S; ++s) {
-                px[q][s] = __ldg(&p[s]);
+                px[0][s] = pp[0][s];
+                px[1][s] = pp[1][s];
             }
+            PixelPair<TIn, S>::load(a.img[k] + (int64_t)YY[2] * a.ipitch[k] + (int64_t)X * S, pp);
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+                px[2][s] = pp[0][s];
+                px[3][s] = pp[1][s];
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                m[q] = (int32_t)__ldg(&a.m0[k][(int64_t)YY[q] * a.mpitch + XX[q]]);
+                const TIn* p = a.img[k] + (int64_t)YY[q] * a.ipitch[k] + (int64_t)XX[q] * S;
+#pragma unroll
+                for (int s = 0; s < S; ++s) {
+                    px[q][s] = __ldg(&p[s]);
+                }
+            }
+        }
+    };
+    int32_t m[4];
+    TIn px[4][S];
+    fetch(0, m, px);
+    for (int k = 0; k < K; ++k) {
+        int32_t mn[4];
+        TIn pn[4][S];
+        if (k + 1 < K) {
+            fetch(k + 1, mn, pn);  // in flight while exposure k is merged
         }
 #pragma unroll
         for (int c = 0; c < C; ++c) {
@@ -363,6 +468,16 @@ __global__ void __launch_bounds__(256) k_ef_out0(const __grid_constant__ EfOut0A
                 // copyToPyramidImage: v << 7 (src/fixmath.h:197-202)
                 const int32_t lp = (int32_t)cast_store<T>(((int64_t)px[q][c] << 7) - e[q]);
                 acc[c][q] += (int32_t)mask_multiply<T, F>(lp, m[q]);
+            }
+        }
+        if (k + 1 < K) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                m[q] = mn[q];
+#pragma unroll
+                for (int s = 0; s < S; ++s) {
+                    px[q][s] = pn[q][s];
+                }
             }
         }
     }
@@ -654,6 +769,11 @@ static cudaError_t ef_out0_t(const EfuseHost& h, cudaStream_t st)
     a.dither = h.dither;
     a.key = dither_key(h.seed);
     a.maxv = sizeof(TIn) == 1 ? 255 : 65535;
+    a.vec = 1;
+    for (int k = 0; k < h.K; ++k) {
+        const size_t unit = (size_t)PixelPair<TIn, S>::UNIT;
+        a.vec &= ((uintptr_t)h.img[k].p % unit) == 0 && ((size_t)h.img[k].pitch * sizeof(TIn)) % unit == 0;
+    }
     const size_t smem = win_smem(h.K, C);
     allow_smem(k_ef_out0<TIn, T, TM, C, S, F>, smem);
     const dim3 g((unsigned)((h.w + ETW - 1) / ETW), (unsigned)((h.h + ETH - 1) / ETH));

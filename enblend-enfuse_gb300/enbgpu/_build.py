@@ -72,6 +72,38 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     return LIB_PATH
 
 
+FRONTEND = ROOT / "frontend"
+FRONTEND_BINS = {"enbgpu-enfuse": ["enfuse_main.cpp", "image_io.cpp"],
+                 "enbgpu-enblend": ["enblend_main.cpp", "image_io.cpp"]}
+
+
+def _cuda_home() -> Path:
+    return Path(_nvcc()).resolve().parent.parent
+
+
+def build_frontends(force: bool = False) -> list:
+    """The enfuse / enblend command-line front ends (C++ host code over the
+    C ABI), linked against libenbgpu.so next to them."""
+    build(force)
+    outs = []
+    cuda = _cuda_home()
+    for name, srcs in FRONTEND_BINS.items():
+        out = PKG_DIR / name
+        deps = [FRONTEND / x for x in srcs] + list(FRONTEND.glob("*.hpp")) + [INCLUDE / "enbgpu.h", LIB_PATH]
+        if force or not out.exists() or any(d.stat().st_mtime > out.stat().st_mtime for d in deps):
+            tmp = out.with_name(out.name + ".tmp")
+            cmd = ["g++", "-std=c++17", "-O2", "-I", str(INCLUDE), "-I", str(cuda / "include"), "-o", str(tmp)]
+            cmd += [str(FRONTEND / x) for x in srcs]
+            cmd += ["-L", str(PKG_DIR), "-lenbgpu", "-L", str(cuda / "lib64"), "-lcudart",
+                    "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + str(cuda / "lib64")]
+            res = subprocess.run(cmd, capture_output=True, text=True)
+            if res.returncode != 0:
+                raise RuntimeError(f"front end {name} failed to build:\n{res.stderr}")
+            os.replace(tmp, out)
+        outs.append(out)
+    return outs
+
+
 if __name__ == "__main__":
     import sys
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

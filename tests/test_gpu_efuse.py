@@ -61,7 +61,9 @@ def test_fused_enfuse_against_oracle(ctx, orc, dt, S, geom):
     l0, out, oa = _run(ctx, imgs, kw, seed=17)
     names = set(ctx.profile_report())
     ctx.profile(False)
-    assert "ef_out0" in names, names
+    # a canvas whose short side is at most 8 pixels has one pyramid level,
+    # which the per-operation passes take
+    assert ("ef_out0" in names) == (orc.num_levels(w, h) >= 2), names
     C = 3 if S != 1 else 1
     assert np.array_equal(l0 if C == 3 else l0[..., 0], ref["level0"] if C == 3 else ref["level0"][..., 0])
     assert np.array_equal(oa, ref["alpha"])
