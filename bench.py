@@ -77,6 +77,9 @@ def parse_args():
     ap.add_argument("--profile-batched", action="store_true",
                     help="run only a small batched fuse (4 stacks of 5 FP32 1024x768 exposures, every level above 0 "
                          "in the coarse kernel, no graph): the case of the batched kernels' ncu capture")
+    ap.add_argument("--profile-enfuse", action="store_true",
+                    help="run only two fused enfuse calls on 9 x 1500x1000 RGB u16 with the 9 x 6000x4000 "
+                         "workload's generator and weights: the case of the fused enfuse kernels' ncu captures")
     ap.add_argument("--plain", action="store_true",
                     help="with --profile-only: the reference's pass structure instead of the fused passes")
     return ap.parse_args()
@@ -475,12 +478,15 @@ def run_ours(args) -> None:
     ctx.set_stream(stream.cuda_stream)
 
     white, black, mask = make_inputs(args.seed, args.rows if args.profile_only else H)
-    dw, db, dm = (torch.from_numpy(x).cuda() for x in (white, black, mask))
-    out = torch.empty_like(db)
+    # device-resident inputs in the layout the host-buffer path stages into:
+    # rows on 128-byte boundaries (the 6963-pixel rows are 55,704 bytes)
+    dw, db, dm = (enbgpu.pitched(x) for x in (white, black, mask))
+    out = torch.empty(black.shape, dtype=torch.uint16, device="cuda")
     oa = torch.empty(mask.shape, dtype=torch.uint8, device="cuda")
 
-    def step(plain=False):
-        ctx.enblend(dw, db, dm, out=out, out_alpha=oa, plain=plain)
+    def step(plain=False, inputs=None):
+        w_, b_, m_ = inputs if inputs is not None else (dw, db, dm)
+        ctx.enblend(w_, b_, m_, out=out, out_alpha=oa, plain=plain)
 
     if args.profile_only:
         for _ in range(args.warmup + args.steps):
@@ -526,6 +532,20 @@ def run_ours(args) -> None:
     p1.record(stream)
     barrier()
     plain_ms = p0.elapsed_time(p1) / plain_steps
+
+    # ---- the same call on dense device rows (55,704-byte pitch, rows not on
+    # 16-byte boundaries: level 0 takes the per-thread copy feed) ----
+    dense = tuple(torch.from_numpy(x).cuda() for x in (white, black, mask))
+    step(inputs=dense)
+    barrier()
+    q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    q0.record(stream)
+    for _ in range(plain_steps):
+        step(inputs=dense)
+    q1.record(stream)
+    barrier()
+    dense_ms = q0.elapsed_time(q1) / plain_steps
+    del dense
 
     # ---- end to end through the host-buffer entry point (pinned memory) ----
     pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
@@ -576,11 +596,15 @@ def run_ours(args) -> None:
         "vs_baseline": None, "dtype": "int32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "levels": enbgpu.num_levels(W + OFFSET, H), "pixel": "RGBA u16",
                    "pyramid": "int32 17.7 fixed point, mask int32 9.15", "parallelism": f"replicas x{ws}",
-                   "l2": "inputs larger than L2 (each image 171 MB)"},
+                   "l2": "inputs larger than L2 (each image 171 MB)",
+                   "device_layout": "rows padded to 128-byte boundaries (enbgpu.pitched), as the host-buffer "
+                                    "path stages them"},
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_ms / e2e_steps},
         "plain_passes": {"value": UNITS / (plain_ms / 1e3), "unit": METRIC, "ms_per_step": plain_ms,
                          "what": "same call with one kernel per reference operation (enb_fuse_options.plain)"},
+        "dense_rows": {"value": UNITS / (dense_ms / 1e3), "unit": METRIC, "ms_per_step": dense_ms,
+                       "what": "same call on unpadded device images (rows not 16-byte aligned)"},
         "gpu_launches": launches,
         "roofline": roofline,
         "kernels": kernels,
@@ -621,10 +645,31 @@ def profile_batched() -> None:
     ctx.close()
 
 
+def profile_enfuse() -> None:
+    """Two fused enfuse calls on 9 x 1500x1000 RGB u16 (EV -4..+4, 12-stop
+    scene, noise 2^-12; exposure 1.0, saturation 0.2, contrast 0.5 and
+    entropy 0.3 in 5x5 windows): 13.5 Mpx*exposures, inputs 81 MB."""
+    import torch
+    import enbgpu
+    from enbgpu import synthetic
+    ctx = enbgpu.Context(0)
+    sp = ENFUSE_WORKLOADS["enfuse_9x6000x4000_u16"]
+    imgs = synthetic.exposure_stack_torch(1000, 1500, sp["evs"], sp["dtype"], sp["stops"], sp["seed"], sp["noise"])
+    prm = enbgpu.enfuse_params(**sp["kw"])
+    for _ in range(2):
+        out, _ = ctx.enfuse(imgs, params=prm)
+    torch.cuda.synchronize()
+    print("enfuse profile case ok", float(out.float().mean()))
+    ctx.close()
+
+
 def main():
     args = parse_args()
     if args.profile_batched:
         profile_batched()
+        return
+    if args.profile_enfuse:
+        profile_enfuse()
         return
     if args.impl == "reference":
         run_reference(args)

@@ -836,10 +836,10 @@ enb_status stage_in(enb_ctx* ctx, const enb_image* host, Staged& s, bool copy)
     const int stride = host->planar ? 1 : (host->pix_stride > 0 ? host->pix_stride : host->channels);
     const int64_t row = (int64_t)host->width * stride * (int64_t)dtype_size(host->dtype);
     // a dense host image keeps its pitch on the device (one contiguous copy)
-    // when that pitch keeps whole pixels at their natural alignment
-    const int64_t px = (int64_t)stride * (int64_t)dtype_size(host->dtype);
-    const int64_t align = stride == 4 ? px : (int64_t)dtype_size(host->dtype);
-    const int64_t pitch = (host->pitch == row && row % align == 0) ? row : round_up(row, 128);
+    // when its rows start on 16-byte boundaries; otherwise the device rows
+    // are 128-byte aligned, so that the level-0 passes can move the staged
+    // images and masks in 2-D TMA boxes
+    const int64_t pitch = (host->pitch == row && row % 16 == 0) ? row : round_up(row, 128);
     ENB_CUDA(ctx, s.buf.alloc((size_t)(pitch * host->height), ctx->stream));
     s.dev.data = s.buf.p;
     s.dev.pitch = pitch;

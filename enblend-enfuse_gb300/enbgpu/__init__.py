@@ -565,11 +565,28 @@ class Context:
         return out, out_alpha
 
 
+def pitched(x, align: int = 128):
+    """A CUDA copy of the image x ((H, W) or (H, W, S), numpy or torch) whose
+    rows start on `align`-byte boundaries, the layout the host-buffer entry
+    points stage into (as cudaMallocPitch would give): the level-0 passes then
+    move whole tiles with 2-D TMA boxes whatever the image width."""
+    import torch
+    t = x if _is_torch(x) else torch.from_numpy(np.ascontiguousarray(x))
+    es = t.element_size()
+    row = t.shape[1] * (t.shape[2] if t.ndim == 3 else 1) * es
+    pitch = (row + align - 1) // align * align
+    buf = torch.empty(t.shape[0] * pitch // es, dtype=t.dtype, device="cuda")
+    strides = (pitch // es,) + tuple(t.stride()[1:])
+    out = buf.as_strided(tuple(t.shape), strides)
+    out.copy_(t)
+    return out
+
+
 def num_levels(width: int, height: int, min_levels: int = 1, exact_levels: int = 0) -> int:
     """roiBounds level count (src/bounds.h:97-177)."""
     return load_library().enb_num_levels(width, height, min_levels, exact_levels)
 
 
 __all__ = ["Context", "Pyramid", "EnbError", "EnbImage", "EnbEnfuseParams", "EnbFuseOptions", "enfuse_params",
-           "num_levels", "load_library", "header_functions", "pixel_image", "plane_image",
+           "num_levels", "pitched", "load_library", "header_functions", "pixel_image", "plane_image",
            "ENB_U8", "ENB_U16", "ENB_F32", "ENB_I16", "ENB_I32"]
