@@ -539,6 +539,7 @@ enb_status build_tables(enb_ctx* ctx, const enb_enfuse_params* prm, uint32_t max
     std::vector<double> plogp(nt, 0.0), logb(nmax + 1, 0.0);
     std::vector<long long> plogp_fx(nt, 0);
     std::vector<float> scale_logb(nmax + 1, 0.0f);
+    std::vector<unsigned long long> scale_fx(nmax + 1, 0ull);
     for (int tot = 1; tot <= nmax; ++tot) {
         for (int c = 1; c <= tot; ++c) {
             const double p = (double)c / (double)tot;
@@ -550,13 +551,14 @@ enb_status build_tables(enb_ctx* ctx, const enb_enfuse_params* prm, uint32_t max
     for (int b = 1; b <= nmax; ++b) {
         logb[b] = log((double)b);
         scale_logb[b] = b >= 2 ? (float)((double)maxv / logb[b]) : 0.0f;
+        scale_fx[b] = b >= 2 ? (unsigned long long)llround(ldexp((double)maxv / logb[b], 40)) : 0ull;
     }
     const size_t sz_f = (size_t)n * 4, sz_pl = (size_t)nt * 8, sz_lb = (size_t)(nmax + 1) * 8,
-                 sz_sl = (size_t)(nmax + 1) * 4;
+                 sz_sl = (size_t)(nmax + 1) * 4, sz_sf = (size_t)(nmax + 1) * 8;
     const size_t o_exp = 0, o_con = round_up((int64_t)(o_exp + sz_f), 256), o_ent = round_up((int64_t)(o_con + sz_f), 256),
                  o_pl = round_up((int64_t)(o_ent + sz_f), 256), o_fx = round_up((int64_t)(o_pl + sz_pl), 256),
                  o_lb = round_up((int64_t)(o_fx + sz_pl), 256), o_sl = round_up((int64_t)(o_lb + sz_lb), 256),
-                 total = round_up((int64_t)(o_sl + sz_sl), 256);
+                 o_sf = round_up((int64_t)(o_sl + sz_sl), 256), total = round_up((int64_t)(o_sf + sz_sf), 256);
     if (ctx->table_mem) {
         cudaFreeAsync(ctx->table_mem, ctx->stream);
         ctx->table_mem = nullptr;
@@ -570,11 +572,12 @@ enb_status build_tables(enb_ctx* ctx, const enb_enfuse_params* prm, uint32_t max
     ENB_CUDA(ctx, cudaMemcpyAsync(b + o_fx, plogp_fx.data(), sz_pl, cudaMemcpyHostToDevice, ctx->stream));
     ENB_CUDA(ctx, cudaMemcpyAsync(b + o_lb, logb.data(), sz_lb, cudaMemcpyHostToDevice, ctx->stream));
     ENB_CUDA(ctx, cudaMemcpyAsync(b + o_sl, scale_logb.data(), sz_sl, cudaMemcpyHostToDevice, ctx->stream));
+    ENB_CUDA(ctx, cudaMemcpyAsync(b + o_sf, scale_fx.data(), sz_sf, cudaMemcpyHostToDevice, ctx->stream));
     // pageable sources: make sure the copies consumed them before the vectors go
     ENB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     ctx->tables = WeightTables{(const float*)(b + o_exp), (const float*)(b + o_con), (const float*)(b + o_ent),
                                (const double*)(b + o_pl), (const long long*)(b + o_fx), (const double*)(b + o_lb),
-                               (const float*)(b + o_sl)};
+                               (const float*)(b + o_sl), (const unsigned long long*)(b + o_sf)};
     ctx->table_key = key;
     return ENB_OK;
 }

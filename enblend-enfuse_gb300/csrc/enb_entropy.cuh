@@ -92,10 +92,30 @@ __device__ __forceinline__ double entropy_sum_double(const uint32_t (&k)[M], int
     return n > 0 ? __dadd_rn(es, pl[run]) : es;
 }
 
-// Integer images: fromRealPromote(H * max) of the window (Histogram::entropyFun).
-// A float estimate from the exact fixed-point sum decides the rounding
-// unless it lies within 0.03 of a boundary; then the reference's double
-// expression is evaluated.
+// fromRealPromote(H * max) with H = -sum p log p / log(bins) from the 2^-56
+// fixed-point sum acc (each term rounded once, so |acc 2^-56 - sum| <=
+// bins 2^-57): the 128-bit product of -acc and max / log(bins) in 2^-40
+// fixed point is H * max in 2^-96 fixed point, whose top 32 fraction bits
+// decide the rounding to within 1e-10.  The reference sums the n <= 225
+// terms in double (error below n 2^-53 log n, times max / log 2 at most
+// n 2^-33 after scaling); where H * max lies within (n + 8) 2^-32 of a
+// half-integer, `near` is set and the caller evaluates the reference's
+// double expression.
+__device__ __forceinline__ uint32_t entropy_fx_round(long long acc, int bins, int n, const WeightTables& tab,
+                                                     uint32_t maxv, bool& near)
+{
+    const unsigned long long A = (unsigned long long)(-acc);  // p log p <= 0
+    const unsigned long long hi = __umul64hi(A, tab.scale_fx[bins]);
+    const uint32_t frac = (uint32_t)hi;
+    const uint32_t dist = frac >= 0x80000000u ? frac - 0x80000000u : 0x80000000u - frac;
+    near = dist <= (uint32_t)(n + 8);
+    const uint32_t m = (uint32_t)(hi >> 32) + (frac >= 0x80000000u ? 1u : 0u);
+    return min(m, maxv);
+}
+
+// Integer images: fromRealPromote(H * max) of the window (Histogram::entropyFun),
+// rounded by entropy_fx_round, with the reference's double expression near
+// a rounding boundary.
 template <int W>
 __device__ __forceinline__ uint32_t entropy_window_int(const uint16_t* raw, const uint8_t* a, int TW, int ci, const WeightTables& tab,
                                        uint32_t maxv)
@@ -113,13 +133,10 @@ __device__ __forceinline__ uint32_t entropy_window_int(const uint16_t* raw, cons
     if (bins <= 1) {
         return 0;
     }
-    const float e = -(float)acc * 1.3877787807814457e-17f;  // 2^-56
-    const float val = __fmul_rn(e, tab.scale_logb[bins]);
-    const float x = val + 0.5f;
-    const float fl = floorf(x);
-    const float d = x - fl;
-    if (d > 0.03f && d < 0.97f) {
-        return min((uint32_t)max(fl, 0.0f), maxv);
+    bool near;
+    const uint32_t r = entropy_fx_round(acc, bins, n, tab, maxv, near);
+    if (!near) {
+        return r;
     }
     const double es = entropy_sum_double<M>(k, n, tab.plogp + (int64_t)n * (M + 1));
     const double H = __ddiv_rn(-es, tab.logb[bins]);

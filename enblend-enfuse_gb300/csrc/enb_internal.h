@@ -75,6 +75,7 @@ struct WeightTables {
     const long long* plogp_fx;// same in 2^-56 fixed point
     const double* logb;       // [n_max+1]: log(b)
     const float* scale_logb;  // [n_max+1]: max / log(b) as float
+    const unsigned long long* scale_fx;  // [n_max+1]: max / log(b) in 2^-40 fixed point
 };
 
 struct WeightParams {

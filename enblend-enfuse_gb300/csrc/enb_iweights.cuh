@@ -76,22 +76,34 @@ __device__ __forceinline__ void entropy_clamp(const WeightParams& wp, uint32_t (
 }
 
 // fromRealPromote(sqrt((Q - S*S/n) / (n-1))) of the window sums
-// (src/enfuse.h:154-160).  The exact value sqrt((nQ - S^2)/(n(n-1))) is
-// approximated in float (error < 0.01); unless it lies within 0.03 of a
-// rounding boundary that decides the integer, otherwise the reference's
-// double expression is evaluated.
+// (src/enfuse.h:154-160).  With num = n Q - S^2 and nn = n (n-1) (exact
+// integers), the rounded deviation is the m with
+//   (2m-1)^2 nn <= 4 num < (2m+1)^2 nn,
+// found from a float estimate (within one of m) and checked in 64-bit
+// integers.  The reference's double expression can round differently only
+// where 4 num lies within its rounding error of a boundary: within tol =
+// 2^-45 num + 2^-48 n Q + 4 of one (a bound on those errors, larger than
+// them by a factor of two or more), and at exact ties, the double expression
+// is evaluated as the reference writes it.
 __device__ __forceinline__ int32_t stddev_round(int64_t S, int64_t Q, int n)
 {
     if (n <= 1) {
         return 0;
     }
     const int64_t num = (int64_t)n * Q - S * S;
-    const float r = sqrtf(__fdiv_rn((float)num, (float)(n * (n - 1))));
-    const float x = r + 0.5f;
-    const float fl = floorf(x);
-    const float d = x - fl;
-    if (d > 0.03f && d < 0.97f) {
-        return (int32_t)fl;
+    const int64_t nn = (int64_t)n * (n - 1);
+    const int64_t num4 = 4 * num;
+    int64_t m = (int64_t)floorf(sqrtf(__fdiv_rn((float)num, (float)nn)) + 0.5f);
+    if (m > 0 && (2 * m - 1) * (2 * m - 1) * nn > num4) {
+        --m;
+    } else if ((2 * m + 1) * (2 * m + 1) * nn <= num4) {
+        ++m;
+    }
+    const int64_t dlo = m > 0 ? num4 - (2 * m - 1) * (2 * m - 1) * nn : INT64_MAX;
+    const int64_t dhi = (2 * m + 1) * (2 * m + 1) * nn - num4;
+    const int64_t tol = (num >> 45) + (((int64_t)n * Q) >> 48) + 4;
+    if (dlo >= tol && dhi >= tol) {
+        return (int32_t)m;
     }
     const double sum = (double)S;
     const double var = __ddiv_rn(__dadd_rn((double)Q, -__ddiv_rn(__dmul_rn(sum, sum), (double)n)), (double)(n - 1));
@@ -101,9 +113,9 @@ __device__ __forceinline__ int32_t stddev_round(int64_t S, int64_t Q, int n)
 
 // Histogram::entropyOfChannel of n sorted samples (src/enfuse.h:346-375),
 // scaled by the channel maximum and rounded (Histogram::entropyFun).  The
-// sum of p log p is accumulated exactly in 2^-56 fixed point for a float
-// estimate; near a rounding boundary the reference's double sum (bins in
-// ascending key order) is evaluated.
+// sum of p log p is accumulated exactly in 2^-56 fixed point and rounded by
+// entropy_fx_round; near a rounding boundary the reference's double sum
+// (bins in ascending key order) is evaluated.
 __device__ __noinline__ static int32_t entropy_round(const uint16_t* v, int n, const WeightTables& tab, int nmax, uint32_t maxv)
 {
     if (n == 0) {
@@ -125,13 +137,10 @@ __device__ __noinline__ static int32_t entropy_round(const uint16_t* v, int n, c
     if (bins <= 1) {
         return 0;
     }
-    const float e = -(float)acc * 1.3877787807814457e-17f;  // 2^-56
-    const float val = __fmul_rn(e, tab.scale_logb[bins]);
-    const float x = val + 0.5f;
-    const float fl = floorf(x);
-    const float d = x - fl;
-    if (d > 0.03f && d < 0.97f) {
-        return (int32_t)min((uint32_t)max(fl, 0.0f), maxv);
+    bool near;
+    const uint32_t r = entropy_fx_round(acc, bins, n, tab, maxv, near);
+    if (!near) {
+        return (int32_t)r;
     }
     const double* pl = tab.plogp + (int64_t)n * (nmax + 1);
     double es = 0.0;

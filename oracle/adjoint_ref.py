@@ -179,8 +179,11 @@ def loss(images, logits, theta, target, **kw) -> torch.Tensor:
 
 
 def central_differences(images, logits, theta, target, coords: Sequence, step: float = 1e-6, **kw):
-    """FP64 central differences of the loss at the given coordinates:
-    ("theta", i) or ("logit", k, y, x)."""
+    """FP64 central differences (L(p + h) - L(p - h)) / 2h of the loss at the
+    given coordinates: ("theta", i) or ("logit", k, y, x).  The difference of
+    the two means of squares is formed per pixel as (a - b)(a + b - 2t) with
+    a, b the two fused images, so that it keeps its precision where one
+    coordinate moves the loss by a few hundred ulps (large images)."""
     out = []
     with torch.no_grad():
         for c in coords:
@@ -192,5 +195,7 @@ def central_differences(images, logits, theta, target, coords: Sequence, step: f
             else:
                 lp[c[1], c[2], c[3]] += step
                 lm[c[1], c[2], c[3]] -= step
-            out.append(float((loss(images, lp, tp, target, **kw) - loss(images, lm, tm, target, **kw)) / (2 * step)))
+            a = fuse(images, lp, tp, **kw)
+            b = fuse(images, lm, tm, **kw)
+            out.append(float(((a - b) * (a + b - 2.0 * target)).mean() / (2 * step)))
     return np.array(out)
