@@ -1027,10 +1027,9 @@ enb_status enblend_fused(enb_ctx* ctx, const enb_image* white, const enb_image* 
         }
         for (int j = 1; j < first; ++j) {
             const BytePlane sa = awc.level(j - 1), da = awc.level(j), sb = abc.level(j - 1), db = abc.level(j);
-            ENB_LAUNCH(ctx, launch_reduce2(wrap, level_view(gw.p, j - 1), &sa, level_view(gw.p, j), &da,
-                                           level_view(gb.p, j - 1), &sb, level_view(gb.p, j), &db, ctx->stream));
-            ENB_LAUNCH(ctx, launch_reduce(wrap, level_view(mg.p, j - 1), nullptr, level_view(mg.p, j), nullptr,
-                                          ctx->stream));
+            ENB_LAUNCH(ctx, launch_reduce_img2_mask(wrap, level_view(gw.p, j - 1), sa, level_view(gw.p, j), da,
+                                                    level_view(gb.p, j - 1), sb, level_view(gb.p, j), db,
+                                                    level_view(mg.p, j - 1), level_view(mg.p, j), ctx->stream));
         }
         int up_from = NL - 2;
         if (first < NL) {

@@ -214,6 +214,12 @@ cudaError_t launch_reduce(int wrap, const PlanarView& src, const BytePlane* src_
 // The same reduce of two levels of equal geometry and type (the white and
 // black pyramids of one level) as one launch; falls back to two launches when
 // the geometries differ.
+// white and black images with alpha and the seam mask without, one level of
+// the enblend down sweep in one launch (integer pyramids)
+cudaError_t launch_reduce_img2_mask(int wrap, const PlanarView& s0, const BytePlane& sa0, const PlanarView& d0,
+                                    const BytePlane& da0, const PlanarView& s1, const BytePlane& sa1,
+                                    const PlanarView& d1, const BytePlane& da1, const PlanarView& ms,
+                                    const PlanarView& md, cudaStream_t st);
 cudaError_t launch_reduce2(int wrap, const PlanarView& s0, const BytePlane* sa0, const PlanarView& d0,
                            const BytePlane* da0, const PlanarView& s1, const BytePlane* sa1, const PlanarView& d1,
                            const BytePlane* da1, cudaStream_t st);

@@ -610,6 +610,59 @@ cudaError_t launch_reduce2(int wrap, const PlanarView& s0, const BytePlane* sa0,
     return reduce_jobs(wrap, 2, sv, sav, dv, dav, st);
 }
 
+template <typename T, typename TM, int C>
+static void reduce_img2_mask_t(int wrap, const PlanarView& s0, const BytePlane& sa0, const PlanarView& d0,
+                               const BytePlane& da0, const PlanarView& s1, const BytePlane& sa1, const PlanarView& d1,
+                               const BytePlane& da1, const PlanarView& ms, const PlanarView& md, cudaStream_t st)
+{
+    using SrcI = PlanarSource<T, C, true>;
+    using SrcM = PlanarSource<TM, 1, false>;
+    ReduceJobs<SrcI, T> img{};
+    img.j[0] = ReduceJob<SrcI, T>{SrcI{(const T*)s0.p, s0.pitch, s0.plane, sa0.p, sa0.pitch}, (T*)d0.p, d0.pitch,
+                                  d0.plane, da0.p, da0.pitch};
+    img.j[1] = ReduceJob<SrcI, T>{SrcI{(const T*)s1.p, s1.pitch, s1.plane, sa1.p, sa1.pitch}, (T*)d1.p, d1.pitch,
+                                  d1.plane, da1.p, da1.pitch};
+    const ReduceJob<SrcM, TM> msk{SrcM{(const TM*)ms.p, ms.pitch, ms.plane, nullptr, 0}, (TM*)md.p, md.pitch, md.plane,
+                                  nullptr, 0};
+    const dim3 g((unsigned)((d0.w + RDW - 1) / RDW), (unsigned)reduce_tile_rows(d0.h), 3u);
+    (void)launch_pdl(k_reduce_img2_mask<SrcI, T, C, SrcM, TM>, g, dim3(RTHREADS), st, img, msk, s0.w, s0.h, d0.w,
+                     d0.h, wrap);
+}
+
+cudaError_t launch_reduce_img2_mask(int wrap, const PlanarView& s0, const BytePlane& sa0, const PlanarView& d0,
+                                    const BytePlane& da0, const PlanarView& s1, const BytePlane& sa1,
+                                    const PlanarView& d1, const BytePlane& da1, const PlanarView& ms,
+                                    const PlanarView& md, cudaStream_t st)
+{
+    const bool same = s0.w == s1.w && s0.h == s1.h && s0.w == ms.w && s0.h == ms.h && d0.w == d1.w && d0.h == d1.h &&
+                      d0.w == md.w && d0.h == md.h && s0.dtype == s1.dtype && s0.dtype == d0.dtype &&
+                      d1.dtype == d0.dtype && s0.C == s1.C && s0.C == d0.C && d1.C == d0.C && ms.C == 1 && md.C == 1 &&
+                      ms.dtype == md.dtype && (s0.dtype == ENB_I16 || s0.dtype == ENB_I32) &&
+                      (ms.dtype == ENB_I16 || ms.dtype == ENB_I32) && (s0.C == 1 || s0.C == 3);
+    if (!same) {
+        return cudaErrorInvalidValue;
+    }
+    note("reduce_level", planar_bytes(s0) + planar_bytes(d0) + planar_bytes(s1) + planar_bytes(d1) +
+                             2.0 * (npix(s0.w, s0.h) + npix(d0.w, d0.h)) + planar_bytes(ms) + planar_bytes(md));
+#define ENB_RIM(T, TM, CC) reduce_img2_mask_t<T, TM, CC>(wrap, s0, sa0, d0, da0, s1, sa1, d1, da1, ms, md, st)
+    const bool m16 = ms.dtype == ENB_I16;
+    if (s0.dtype == ENB_I16) {
+        if (s0.C == 1) {
+            if (m16) ENB_RIM(int16_t, int16_t, 1); else ENB_RIM(int16_t, int32_t, 1);
+        } else {
+            if (m16) ENB_RIM(int16_t, int16_t, 3); else ENB_RIM(int16_t, int32_t, 3);
+        }
+    } else {
+        if (s0.C == 1) {
+            if (m16) ENB_RIM(int32_t, int16_t, 1); else ENB_RIM(int32_t, int32_t, 1);
+        } else {
+            if (m16) ENB_RIM(int32_t, int16_t, 3); else ENB_RIM(int32_t, int32_t, 3);
+        }
+    }
+#undef ENB_RIM
+    return cudaGetLastError();
+}
+
 template <typename T, int C>
 static void expand_dispatch(int add, int wrap, const PlanarView& s, const PlanarView& d, cudaStream_t st)
 {

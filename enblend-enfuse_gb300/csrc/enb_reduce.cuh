@@ -294,6 +294,31 @@ __global__ void __launch_bounds__(RTHREADS, 3) k_reduce(ReduceJobs<Src, TD> jobs
 // Destination tile rows of the reduce (16 rows each).
 inline int reduce_tile_rows(int dh) { return (dh + RDH - 1) / RDH; }
 
+// One level of enblend's down sweep in one launch: the white and black image
+// reduces with alpha (blockIdx.z 0 and 1) and the seam mask's reduce without
+// (blockIdx.z 2), so that the three Gaussian pyramids advance together
+// (src/enblend.h:384-446).
+template <class SrcI, typename TI, int C, class SrcM, typename TM>
+__global__ void __launch_bounds__(RTHREADS, 3) k_reduce_img2_mask(const __grid_constant__ ReduceJobs<SrcI, TI> img,
+                                                                  const __grid_constant__ ReduceJob<SrcM, TM> msk,
+                                                                  int sw, int sh, int dw, int dh, int wrap)
+{
+    typedef typename ReduceAcc<TI>::type ACI;
+    typedef typename ReduceAcc<TM>::type ACM;
+    constexpr size_t BI = sizeof(ACI) * ReduceSmem<C, true>::NV * RDH * RVP;
+    constexpr size_t BM = sizeof(ACM) * ReduceSmem<1, false>::NV * RDH * RVP;
+    __shared__ __align__(16) unsigned char V[BI > BM ? BI : BM];
+    griddep_wait();
+    griddep_launch();
+    if (blockIdx.z < 2) {
+        reduce_tile<SrcI, TI, C, true, ACI>(img.j[blockIdx.z], blockIdx.x * RDW, blockIdx.y * RDH, sw, sh, dw, dh,
+                                            wrap, reinterpret_cast<ACI(*)[RDH][RVP]>(V));
+    } else {
+        reduce_tile<SrcM, TM, 1, false, ACM>(msk, blockIdx.x * RDW, blockIdx.y * RDH, sw, sh, dw, dh, wrap,
+                                             reinterpret_cast<ACM(*)[RDH][RVP]>(V));
+    }
+}
+
 // One launch over njobs (1 or 2) jobs of the same geometry, covering the
 // destination tile rows [ty0, ty0 + nty) (nty < 0: all).
 template <class Src, typename TD, int C, bool ALPHA>
