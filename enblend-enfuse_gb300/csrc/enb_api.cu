@@ -519,10 +519,28 @@ double exposure_fn(int fn, double y, double opt, double width)
 
 enb_status build_tables(enb_ctx* ctx, const enb_enfuse_params* prm, uint32_t maxv)
 {
+    const bool user_table = prm->exposure_table != nullptr && prm->w_exposure > 0.0;
+    if (user_table) {
+        if (maxv == 1u) {
+            return fail(ctx, ENB_ERR_UNSUPPORTED,
+                        "exposure_table: user exposure weight tables apply to 8- and 16-bit images only");
+        }
+        ENB_CHECK(ctx, prm->exposure_table_size == (int32_t)maxv + 1,
+                  "exposure_table: one entry per sample value (256 for 8-bit, 65536 for 16-bit images)");
+    }
+    // a user table enters the cache key through a hash of its contents
+    uint64_t th = 0;
+    if (user_table) {
+        th = 1469598103934665603ull;
+        const unsigned char* tb = reinterpret_cast<const unsigned char*>(prm->exposure_table);
+        for (size_t i = 0; i < (size_t)prm->exposure_table_size * sizeof(double); ++i) {
+            th = (th ^ tb[i]) * 1099511628211ull;
+        }
+    }
     char key[512];
-    snprintf(key, sizeof key, "%u|%.17g|%.17g|%.17g|%.17g|%.17g|%.17g|%d|%d", maxv, prm->w_exposure,
+    snprintf(key, sizeof key, "%u|%.17g|%.17g|%.17g|%.17g|%.17g|%.17g|%d|%d|%d|%llx", maxv, prm->w_exposure,
              prm->w_contrast, prm->w_entropy, prm->w_saturation, prm->exp_optimum, prm->exp_width, prm->exp_function,
-             prm->entropy_window);
+             prm->entropy_window, user_table ? 1 : 0, (unsigned long long)th);
     if (ctx->table_mem && ctx->table_key == key) {
         return ENB_OK;
     }
@@ -532,7 +550,10 @@ enb_status build_tables(enb_ctx* ctx, const enb_enfuse_params* prm, uint32_t max
     std::vector<float> exposure(n), contrast(n), entropy(n);
     for (int g = 0; g < n; ++g) {
         const double y = (double)g / (double)maxv;
-        exposure[g] = (float)(prm->w_exposure * exposure_fn(prm->exp_function, y, prm->exp_optimum, prm->exp_width));
+        // fromRealPromote(weight_ * weight_function_->weight(y)) (src/enfuse.h:638-639)
+        const double f = user_table ? prm->exposure_table[g]
+                                    : exposure_fn(prm->exp_function, y, prm->exp_optimum, prm->exp_width);
+        exposure[g] = (float)(prm->w_exposure * f);
         contrast[g] = (float)(prm->w_contrast * (double)g / (double)maxv);
         entropy[g] = (float)(prm->w_entropy * (double)(float)g);
     }

@@ -53,66 +53,98 @@ struct EfWeightsArgs {
     int64_t upitch;
 };
 
+// Output tile of the weight pass: 32 x 16 pixels, a pair of horizontally
+// adjacent pixels per thread.
+constexpr int EWX = 32, EWY = 16;
+
+// Left and top margins of the weight tile: the windows' halo, the left one
+// rounded up to even so that pair keys are word loads.
+__host__ __device__ inline int ef_halo_x(const WeightParams& wp) { return (iweight_halo(wp) + 1) & ~1; }
+
 template <typename TM>
 __global__ void __launch_bounds__(256, 3) k_ef_weights(const __grid_constant__ EfWeightsArgs<TM> a)
 {
     extern __shared__ __align__(16) unsigned char esmem[];
-    const int halo = iweight_halo(a.wp);
-    const ITile t = itile_carve(esmem, WT + 2 * halo);
-    float* wk = reinterpret_cast<float*>(esmem + ((itile_bytes(t.TW) + 15) & ~(size_t)15)) + threadIdx.x;  // [K][256]
-    const int lx = threadIdx.x % WT, ly = threadIdx.x / WT;
-    const int x = blockIdx.x * WT + lx, y = blockIdx.y * WT + ly;
-    const bool inside = x < a.w && y < a.h;
-    const int ci = (ly + halo) * t.TW + (lx + halo);
+    const int halo = iweight_halo(a.wp), hx = ef_halo_x(a.wp);
+    const int TW = EWX + 2 * hx, TH = EWY + 2 * halo;
+    const ITile t = itile_carve_rect(esmem, TW, TH);
+    long long* fx = reinterpret_cast<long long*>(esmem + ((itile_bytes_rect(TW, TH) + 15) & ~(size_t)15));  // [32]
+    float2* wk = reinterpret_cast<float2*>(fx + 32) + threadIdx.x;  // [K][256]
+    const int px = threadIdx.x % (EWX / 2), py = threadIdx.x / (EWX / 2);
+    const int x = blockIdx.x * EWX + 2 * px, y = blockIdx.y * EWY + py;
+    const bool in0 = x < a.w && y < a.h, in1 = x + 1 < a.w && y < a.h;
+    const int cx = hx + 2 * px, cy = halo + py;
+    const int ci = cy * TW + cx;
     const int K = a.K;
-    uint32_t ua = 0;
+    const bool pair_path = iweight_pair_path(a.wp);
+    if (a.wp.use_entropy && pair_path && (int)threadIdx.x <= a.wp.entropy_window * a.wp.entropy_window) {
+        // the p log p terms of full windows (n = W * W)
+        const int M = a.wp.entropy_window * a.wp.entropy_window;
+        fx[threadIdx.x] = a.tab.plogp_fx[(int64_t)M * (M + 1) + threadIdx.x];
+    }
+    uint32_t ua0 = 0, ua1 = 0;
     for (int k = 0; k < K; ++k) {
         if (a.min[k]) {
             // --load-masks: the loaded weight replaces enfuseMask (src/enfuse.h:1288-1331)
-            wk[k * 256] = inside ? __ldg(&a.min[k][(int64_t)y * a.mipitch[k] + x]) : 0.0f;
-            ua |= inside ? (uint32_t)alpha_at(a.alpha[k], x, y) : 0u;
+            const float* mrow = a.min[k] + (int64_t)y * a.mipitch[k];
+            wk[k * 256] = make_float2(in0 ? __ldg(&mrow[x]) : 0.0f, in1 ? __ldg(&mrow[x + 1]) : 0.0f);
+            ua0 |= in0 ? (uint32_t)alpha_at(a.alpha[k], x, y) : 0u;
+            ua1 |= in1 ? (uint32_t)alpha_at(a.alpha[k], x + 1, y) : 0u;
             continue;
         }
-        itile_load(t, a.wp, a.img[k], a.alpha[k], blockIdx.x * WT - halo, blockIdx.y * WT - halo);
-        __syncthreads();
-        wk[k * 256] = inside ? i_pixel_weight(t, a.wp, a.tab, a.img[k], ci, x, y) : 0.0f;
-        ua |= t.a[ci];
+        // ends with a barrier (which also publishes fx)
+        const int opaque = itile_load_rect(t, a.wp, a.img[k], a.alpha[k], blockIdx.x * EWX - hx, blockIdx.y * EWY - halo);
+        float w0 = 0.0f, w1 = 0.0f;
+        if (opaque && pair_path) {
+            // every window of the tile is whole and opaque: both pixels at once
+            pair_weights(t, a.wp, a.tab, fx, a.img[k].C, cx, cy, w0, w1);
+        } else {
+            w0 = in0 ? i_pixel_weight(t, a.wp, a.tab, a.img[k], ci, x, y) : 0.0f;
+            w1 = in1 ? i_pixel_weight(t, a.wp, a.tab, a.img[k], ci + 1, x + 1, y) : 0.0f;
+        }
+        wk[k * 256] = make_float2(w0, w1);
+        ua0 |= t.a[ci];
+        ua1 |= t.a[ci + 1];
         __syncthreads();  // the next exposure's load overwrites the tile
-    }
-    if (!inside) {
-        return;
     }
     // normalisation (src/enfuse.h:1382-1385 sum in exposure order, 1399-1442
     // hard mask, 1526-1535 soft mask: float 255 * w / sum, integer 255 / K
     // where every weight is 0), then fromRealPromote(m * 2^F) into the mask
     // pyramid's level 0
-    const int64_t o = (int64_t)y * a.mpitch + x;
-    if (a.hard) {
-        float mx = 0.0f;
-        int mi = 0;
-        for (int k = 0; k < K; ++k) {
-            if (wk[k * 256] > mx) {
-                mx = wk[k * 256];
-                mi = k;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        if (!(q == 0 ? in0 : in1)) {
+            continue;
+        }
+        const float* wq = reinterpret_cast<const float*>(wk) + q;
+        const int64_t o = (int64_t)y * a.mpitch + x + q;
+        if (a.hard) {
+            float mx = 0.0f;
+            int mi = 0;
+            for (int k = 0; k < K; ++k) {
+                if (wq[k * 512] > mx) {
+                    mx = wq[k * 512];
+                    mi = k;
+                }
+            }
+            const float fallback = __fdiv_rn(255.0f, (float)K);
+            for (int k = 0; k < K; ++k) {
+                const float m = mx == 0.0f ? fallback : (k == mi ? 255.0f : 0.0f);
+                a.m0[k][o] = mask_to_fixed<TM>(m, a.mfrac);
+            }
+        } else {
+            float norm = 0.0f;
+            for (int k = 0; k < K; ++k) {
+                norm = __fadd_rn(wq[k * 512], norm);
+            }
+            const float fallback = (float)(255 / K);
+            for (int k = 0; k < K; ++k) {
+                const float m = norm > 0.0f ? __fdiv_rn(__fmul_rn(255.0f, wq[k * 512]), norm) : fallback;
+                a.m0[k][o] = mask_to_fixed<TM>(m, a.mfrac);
             }
         }
-        const float fallback = __fdiv_rn(255.0f, (float)K);
-        for (int k = 0; k < K; ++k) {
-            const float m = mx == 0.0f ? fallback : (k == mi ? 255.0f : 0.0f);
-            a.m0[k][o] = mask_to_fixed<TM>(m, a.mfrac);
-        }
-    } else {
-        float norm = 0.0f;
-        for (int k = 0; k < K; ++k) {
-            norm = __fadd_rn(wk[k * 256], norm);
-        }
-        const float fallback = (float)(255 / K);
-        for (int k = 0; k < K; ++k) {
-            const float m = norm > 0.0f ? __fdiv_rn(__fmul_rn(255.0f, wk[k * 256]), norm) : fallback;
-            a.m0[k][o] = mask_to_fixed<TM>(m, a.mfrac);
-        }
+        a.u0[(int64_t)y * a.upitch + x + q] = (q == 0 ? ua0 : ua1) ? 255 : 0;
     }
-    a.u0[(int64_t)y * a.upitch + x] = ua ? 255 : 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -562,10 +594,11 @@ static cudaError_t ef_weights_t(const EfuseHost& h, cudaStream_t st)
     a.mpitch = h.pitch[0];
     a.u0 = h.u[0];
     a.upitch = h.upitch0;
-    const int TW = WT + 2 * iweight_halo(h.wp);
-    const size_t smem = ((itile_bytes(TW) + 15) & ~(size_t)15) + (size_t)h.K * 256 * sizeof(float);
+    const int TW = EWX + 2 * ef_halo_x(h.wp), TH = EWY + 2 * iweight_halo(h.wp);
+    const size_t smem = ((itile_bytes_rect(TW, TH) + 15) & ~(size_t)15) + 32 * sizeof(long long) +
+                        (size_t)h.K * 256 * sizeof(float2);
     allow_smem(k_ef_weights<TM>, smem);
-    const dim3 g((unsigned)((h.w + WT - 1) / WT), (unsigned)((h.h + WT - 1) / WT));
+    const dim3 g((unsigned)((h.w + EWX - 1) / EWX), (unsigned)((h.h + EWY - 1) / EWY));
     return launch_pdl_smem(k_ef_weights<TM>, g, dim3(256), smem, st, a);
 }
 

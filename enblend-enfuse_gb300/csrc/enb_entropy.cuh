@@ -17,12 +17,10 @@ namespace enb {
 
 constexpr uint32_t kEntropyPad = 0xffffffffu;
 
-template <int M>
-__device__ __forceinline__ void sortnet(uint32_t (&k)[M]);
-template <>
-__device__ __forceinline__ void sortnet<9>(uint32_t (&k)[9]) { sortnet9(k); }
-template <>
-__device__ __forceinline__ void sortnet<25>(uint32_t (&k)[25]) { sortnet25(k); }
+template <class CE = CeU32>
+__device__ __forceinline__ void sortnet(uint32_t (&k)[9], CE ce = CE()) { sortnet9(k, ce); }
+template <class CE = CeU32>
+__device__ __forceinline__ void sortnet(uint32_t (&k)[25], CE ce = CE()) { sortnet25(k, ce); }
 
 // Keys of the W x W window centred at smem index ci of a TW-wide tile
 // (transparent taps -> kEntropyPad); returns the number of opaque taps.
@@ -126,7 +124,7 @@ __device__ __forceinline__ uint32_t entropy_window_int(const uint16_t* raw, cons
     if (n == 0) {
         return 0;
     }
-    sortnet<M>(k);
+    sortnet(k);
     long long acc;
     int bins;
     entropy_bins<M>(k, n, tab.plogp_fx + (int64_t)n * (M + 1), acc, bins);
@@ -155,7 +153,7 @@ __device__ __forceinline__ float entropy_window_float(const float* raw, const ui
     if (n == 0) {
         return 0.0f;
     }
-    sortnet<M>(k);
+    sortnet(k);
     long long acc;
     int bins;
     entropy_bins<M>(k, n, tab.plogp_fx + (int64_t)n * (M + 1), acc, bins);

@@ -187,13 +187,18 @@ __device__ __forceinline__ float saturation_weight(const WeightParams& wp, uint3
 // Tile of (TW x TW) input pixels around 16x16 output pixels: gray, the
 // samples (clamped by the entropy cutoff when it is active) and the alpha.
 struct ITile {
-    int32_t* gray;   // [TW*TW]
-    uint16_t* raw;   // [3][TW*TW]
-    uint8_t* a;      // [TW*TW]
-    int TW;
+    int32_t* gray;   // [TT]
+    uint16_t* raw;   // [3][TT]
+    uint8_t* a;      // [TT]
+    int TW;          // row pitch (pixels)
+    int TT;          // plane size: TW * rows
 };
 
 __host__ __device__ inline size_t itile_bytes(int TW) { return (size_t)TW * TW * (sizeof(int32_t) + 3 * sizeof(uint16_t) + 1); }
+__host__ __device__ inline size_t itile_bytes_rect(int TW, int TH)
+{
+    return (size_t)TW * TH * (sizeof(int32_t) + 3 * sizeof(uint16_t) + 1);
+}
 
 __host__ __device__ inline int iweight_halo(const WeightParams& wp)
 {
@@ -206,6 +211,7 @@ __device__ __forceinline__ ITile itile_carve(unsigned char* smem, int TW)
     ITile t;
     t.TW = TW;
     t.gray = reinterpret_cast<int32_t*>(smem);
+    t.TT = TW * TW;
     t.raw = reinterpret_cast<uint16_t*>(t.gray + TW * TW);
     t.a = reinterpret_cast<uint8_t*>(t.raw + 3 * TW * TW);
     return t;
@@ -298,7 +304,7 @@ __device__ __forceinline__ float i_pixel_weight(const ITile& t, const WeightPara
             result = __fadd_rn(tab.contrast[gc], result);
         }
         if (wp.use_saturation && C == 3) {
-            uint32_t r = s_raw[ci], gg = s_raw[TW * TW + ci], bb = s_raw[2 * TW * TW + ci];
+            uint32_t r = s_raw[ci], gg = s_raw[t.TT + ci], bb = s_raw[2 * t.TT + ci];
             if (wp.ent_cut) {
                 const int64_t base = (int64_t)y * img.pitch + (int64_t)x * img.stride;
                 r = load_sample(img.p, img.dtype, base);
@@ -323,7 +329,7 @@ __device__ __forceinline__ float i_pixel_weight(const ITile& t, const WeightPara
                 emin = wp.maxv;
                 for (int ch = 0; ch < C; ++ch) {
                     if (wp.entropy_window == 5 || wp.entropy_window == 3) {
-                        const uint16_t* raw = s_raw + ch * TW * TW;
+                        const uint16_t* raw = s_raw + ch * t.TT;
                         const uint32_t e = wp.entropy_window == 5
                                                ? entropy_window_int<5>(raw, s_a, TW, ci, tab, wp.maxv)
                                                : entropy_window_int<3>(raw, s_a, TW, ci, tab, wp.maxv);
@@ -336,7 +342,7 @@ __device__ __forceinline__ float i_pixel_weight(const ITile& t, const WeightPara
                         for (int dx = -b; dx <= b; ++dx) {
                             if (s_a[row + dx]) {
                                 // insertion into the sorted prefix
-                                const uint16_t v = s_raw[ch * TW * TW + row + dx];
+                                const uint16_t v = s_raw[ch * t.TT + row + dx];
                                 int p = n++;
                                 while (p > 0 && vals[p - 1] > v) {
                                     vals[p] = vals[p - 1];
@@ -356,5 +362,273 @@ __device__ __forceinline__ float i_pixel_weight(const ITile& t, const WeightPara
     return result;
 }
 
+
+// ---- rectangular tiles and pairs of output pixels --------------------------
+
+__device__ __forceinline__ ITile itile_carve_rect(unsigned char* smem, int TW, int TH)
+{
+    ITile t;
+    t.TW = TW;
+    t.TT = TW * TH;
+    t.gray = reinterpret_cast<int32_t*>(smem);
+    t.raw = reinterpret_cast<uint16_t*>(t.gray + t.TT);
+    t.a = reinterpret_cast<uint8_t*>(t.raw + 3 * t.TT);
+    return t;
+}
+
+// Loads the TW x TH tile whose top-left input pixel is (x0, y0) as
+// itile_load does (all threads call); ends with a barrier and returns
+// nonzero when every tile pixel lies in the image and is opaque.
+__device__ __forceinline__ int itile_load_rect(const ITile& t, const WeightParams& wp, const PixelView& img,
+                                               const AlphaSrc& alpha, int x0, int y0)
+{
+    const int TW = t.TW, TT = t.TT;
+    const int w = img.w, h = img.h, C = img.C;
+    int mine = 1;
+    for (int k = threadIdx.x; k < TT; k += blockDim.x) {
+        const int r = k / TW, c = k - r * TW;
+        const int gx = x0 + c, gy = y0 + r;
+        int32_t g = 0;
+        uint8_t a = 0;
+        uint32_t rgb[3] = {0, 0, 0};
+        if (gx >= 0 && gx < w && gy >= 0 && gy < h) {
+            const int64_t base = (int64_t)gy * img.pitch + (int64_t)gx * img.stride;
+            for (int ch = 0; ch < C; ++ch) {
+                rgb[ch] = load_sample(img.p, img.dtype, base + ch);
+            }
+            g = C == 1 ? (int32_t)rgb[0] : gray_of(wp, rgb[0], rgb[1], rgb[2]);
+            a = (uint8_t)alpha_at(alpha, gx, gy);
+            if (wp.ent_cut) {
+                entropy_clamp(wp, rgb, C);
+            }
+        }
+        mine &= a;
+        t.gray[k] = g;
+        t.a[k] = a;
+        for (int ch = 0; ch < 3; ++ch) {
+            t.raw[ch * TT + k] = (uint16_t)rgb[ch];
+        }
+    }
+    return __syncthreads_and(mine);
+}
+
+// Keys of the W x W entropy windows (W = 3 or 5) of two horizontally
+// adjacent pixels, the left one at tile position (cx, cy) with cx even, in
+// a plane of 16-bit samples with an even row pitch TW: key j of a row holds
+// the left pixel's tap in its low half and the right pixel's in its high
+// half, which are the two samples of one word (an aligned word or the
+// middle of two), so a row of five keys takes three word loads.
+template <int W>
+__device__ __forceinline__ void pair_window_keys(const uint16_t* plane, int TW, int cx, int cy, uint32_t (&k)[W * W])
+{
+    constexpr int B = W / 2;
+#pragma unroll
+    for (int dy = 0; dy < W; ++dy) {
+        const uint32_t* row = reinterpret_cast<const uint32_t*>(plane + (cy + dy - B) * TW + cx - 2);
+        const uint32_t w0 = row[0], w1 = row[1], w2 = row[2];  // columns cx-2 .. cx+3
+        const uint32_t m01 = __byte_perm(w0, w1, 0x5432), m12 = __byte_perm(w1, w2, 0x5432);
+        if (W == 5) {
+            k[dy * W + 0] = w0;
+            k[dy * W + 1] = m01;
+            k[dy * W + 2] = w1;
+            k[dy * W + 3] = m12;
+            k[dy * W + 4] = w2;
+        } else {
+            k[dy * W + 0] = m01;
+            k[dy * W + 1] = w1;
+            k[dy * W + W - 1] = m12;
+        }
+    }
+}
+
+// Histogram::entropyOfChannel of M = W * W opaque samples from the bit mask
+// of their sorted order (bit i set: sample i differs from sample i - 1):
+// popc + 1 bins, and each run of set-free bits of length c - 1 a bin of c
+// equal samples.  fx: the 2^-56 fixed-point p log p terms of n = M (in shared
+// memory).  near: the result lies too close to a rounding boundary; the
+// caller then evaluates the reference's double sum.
+template <int M>
+__device__ __forceinline__ uint32_t entropy_from_boundaries(uint32_t bnd, const long long* fx,
+                                                            const WeightTables& tab, uint32_t maxv, bool& near)
+{
+    near = false;
+    const int bins = __popc(bnd) + 1;
+    if (bins <= 1) {
+        return 0u;
+    }
+    long long acc = (long long)bins * fx[1];
+    uint32_t eq = ~bnd & (((1u << M) - 1u) & ~1u);  // sample i equals sample i - 1
+    while (eq) {
+        const int s0 = __ffs(eq) - 1;
+        const int len = __ffs(~(eq >> s0)) - 1;  // a bin of len + 1 equal samples
+        acc += fx[len + 1] - fx[1];
+        eq &= ~(((1u << len) - 1u) << s0);
+    }
+    return entropy_fx_round(acc, bins, M, tab, maxv, near);
+}
+
+// The reference's double expression for one half of the sorted pair keys
+// (the rare rounding-boundary case).
+template <int M>
+__device__ __noinline__ static uint32_t entropy_half_exact(const uint32_t (&k)[M], int half, const WeightTables& tab,
+                                                           uint32_t maxv)
+{
+    uint32_t v[M];
+    int bins = 1;
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+        v[i] = (k[i] >> (16 * half)) & 0xffffu;
+        bins += (i > 0 && v[i] != v[i - 1]) ? 1 : 0;
+    }
+    const double es = entropy_sum_double<M>(v, M, tab.plogp + (int64_t)M * (M + 1));
+    const double H = __ddiv_rn(-es, tab.logb[bins]);
+    return frp_unsigned(__dmul_rn(H, (double)maxv), maxv);
+}
+
+// fromRealPromote(H * max) of the W x W windows of two adjacent pixels in
+// one channel: both windows sorted at once, one per half word (the samples
+// are at most 16 bits wide), then the bins of each from its boundary mask.
+template <int W>
+__device__ __forceinline__ void entropy_pair(const uint16_t* plane, int TW, int cx, int cy, const long long* fx,
+                                             const WeightTables& tab, uint32_t maxv, uint32_t& e0, uint32_t& e1)
+{
+    constexpr int M = W * W;
+    uint32_t k[M];
+    pair_window_keys<W>(plane, TW, cx, cy, k);
+    sortnet(k, CeU16x2());
+    uint32_t b0 = 0, b1 = 0;
+#pragma unroll
+    for (int i = 1; i < M; ++i) {
+        // each half is sorted, so the word difference is the two halves'
+        // differences without a borrow; min(d, 1) per half: 1 where they differ
+        const uint32_t d = k[i] - k[i - 1];
+        uint32_t nz;
+        asm("min.u16x2 %0, %1, %2;" : "=r"(nz) : "r"(d), "r"(0x00010001u));
+        b0 |= (nz & 1u) << i;
+        b1 |= (nz >> 16) << i;
+    }
+    bool near0, near1;
+    e0 = entropy_from_boundaries<M>(b0, fx, tab, maxv, near0);
+    e1 = entropy_from_boundaries<M>(b1, fx, tab, maxv, near1);
+    if (near0) {
+        e0 = entropy_half_exact<M>(k, 0, tab, maxv);
+    }
+    if (near1) {
+        e1 = entropy_half_exact<M>(k, 1, tab, maxv);
+    }
+}
+
+// The rounded window deviations (localStdDevIf) of two adjacent pixels
+// whose CW x CW windows are opaque: column sums of gray and gray^2 over
+// the CW + 1 columns of both windows, each column summed once.
+template <int CW>
+__device__ __forceinline__ void contrast_pair(const int32_t* gray, int TW, int cx, int cy, uint32_t maxv, uint32_t& g0,
+                                              uint32_t& g1)
+{
+    constexpr int B = CW / 2, NC = CW + 1;
+    uint32_t S[NC];
+    uint64_t Q[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+        S[c] = 0u;
+        Q[c] = 0ull;
+    }
+#pragma unroll
+    for (int dy = 0; dy < CW; ++dy) {
+        const int32_t* row = gray + (cy + dy - B) * TW + cx - B;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            const uint32_t v = (uint32_t)row[c];
+            S[c] += v;
+            Q[c] += (uint64_t)v * v;
+        }
+    }
+    uint32_t s0 = 0u;
+    uint64_t q0 = 0ull;
+#pragma unroll
+    for (int c = 0; c < CW; ++c) {
+        s0 += S[c];
+        q0 += Q[c];
+    }
+    const uint32_t s1 = s0 - S[0] + S[CW];
+    const uint64_t q1 = q0 - Q[0] + Q[CW];
+    g0 = (uint32_t)stddev_round((int64_t)s0, (int64_t)q0, CW * CW) & maxv;
+    g1 = (uint32_t)stddev_round((int64_t)s1, (int64_t)q1, CW * CW) & maxv;
+}
+
+// SaturationFunctor of an integer RGB pixel (src/enfuse.h:733-780), as
+// i_pixel_weight evaluates it.
+__device__ __forceinline__ float saturation_of(const WeightParams& wp, uint32_t r, uint32_t g, uint32_t b)
+{
+    const uint32_t mx = max(r, max(g, b)), mn = min(r, min(g, b));
+    if (mx == mn) {
+        return 0.0f;
+    }
+    const uint32_t sum = mx + mn;
+    const uint32_t S = sum <= wp.maxv ? sum : 2u * wp.maxv - sum;
+    return saturation_weight(wp, mx - mn, S);
+}
+
+// Whether the pair path can weight a tile whose pixels are all opaque and
+// inside the image: entropy windows of 3 or 5, contrast windows of 3, 5 or
+// 7, no cutoff (the cutoffs need the unclamped samples of a pixel).
+__host__ __device__ inline bool iweight_pair_path(const WeightParams& wp)
+{
+    return !wp.exp_cut && !wp.ent_cut && (!wp.use_entropy || wp.entropy_window == 3 || wp.entropy_window == 5) &&
+           (!wp.use_contrast || wp.contrast_window == 3 || wp.contrast_window == 5 || wp.contrast_window == 7);
+}
+
+// The weights of the pixel pair at tile position (cx, cy) of a fully opaque
+// tile, in the reference's order of float adds (as i_pixel_weight).
+template <int CW, int EW>
+__device__ __forceinline__ void pair_weights_t(const ITile& t, const WeightParams& wp, const WeightTables& tab,
+                                               const long long* fx, int C, int cx, int cy, float& w0, float& w1)
+{
+    const int ci = cy * t.TW + cx;
+    float r0 = 0.0f, r1 = 0.0f;
+    if (wp.use_exposure) {
+        r0 = tab.exposure[t.gray[ci]];
+        r1 = tab.exposure[t.gray[ci + 1]];
+    }
+    if (CW > 0) {
+        uint32_t g0, g1;
+        contrast_pair<(CW > 0 ? CW : 3)>(t.gray, t.TW, cx, cy, wp.maxv, g0, g1);
+        r0 = __fadd_rn(tab.contrast[g0], r0);
+        r1 = __fadd_rn(tab.contrast[g1], r1);
+    }
+    if (wp.use_saturation && C == 3) {
+        const uint16_t* raw = t.raw;
+        r0 = __fadd_rn(saturation_of(wp, raw[ci], raw[t.TT + ci], raw[2 * t.TT + ci]), r0);
+        r1 = __fadd_rn(saturation_of(wp, raw[ci + 1], raw[t.TT + ci + 1], raw[2 * t.TT + ci + 1]), r1);
+    }
+    if (EW > 0) {
+        uint32_t m0 = wp.maxv, m1 = wp.maxv;
+        for (int ch = 0; ch < C; ++ch) {
+            uint32_t e0, e1;
+            entropy_pair<(EW > 0 ? EW : 3)>(t.raw + ch * t.TT, t.TW, cx, cy, fx, tab, wp.maxv, e0, e1);
+            m0 = min(m0, e0);
+            m1 = min(m1, e1);
+        }
+        r0 = __fadd_rn(tab.entropy[m0], r0);
+        r1 = __fadd_rn(tab.entropy[m1], r1);
+    }
+    w0 = r0;
+    w1 = r1;
+}
+
+__device__ __forceinline__ void pair_weights(const ITile& t, const WeightParams& wp, const WeightTables& tab,
+                                             const long long* fx, int C, int cx, int cy, float& w0, float& w1)
+{
+    const int cw = wp.use_contrast ? wp.contrast_window : 0, ew = wp.use_entropy ? wp.entropy_window : 0;
+#define ENB_PW(CWV, EWV)                                                          \
+    if (cw == CWV && ew == EWV) {                                                 \
+        pair_weights_t<CWV, EWV>(t, wp, tab, fx, C, cx, cy, w0, w1);              \
+        return;                                                                   \
+    }
+    ENB_PW(5, 5) ENB_PW(5, 3) ENB_PW(3, 3) ENB_PW(3, 5) ENB_PW(7, 5) ENB_PW(7, 3)
+    ENB_PW(0, 5) ENB_PW(0, 3) ENB_PW(5, 0) ENB_PW(3, 0) ENB_PW(7, 0) ENB_PW(0, 0)
+#undef ENB_PW
+    w0 = w1 = 0.0f;
+}
 
 }  // namespace enb

@@ -46,21 +46,38 @@ def main():
     print()
     print("namespace enb {")
     print()
-    print("__device__ __forceinline__ void sortnet_ce(uint32_t& a, uint32_t& b)")
-    print("{")
-    print("    const uint32_t lo = min(a, b);")
-    print("    b = max(a, b);")
-    print("    a = lo;")
-    print("}")
+    print("// Compare-exchange of two 32-bit keys (ascending).")
+    print("struct CeU32 {")
+    print("    __device__ __forceinline__ void operator()(uint32_t& a, uint32_t& b) const")
+    print("    {")
+    print("        const uint32_t lo = min(a, b);")
+    print("        b = max(a, b);")
+    print("        a = lo;")
+    print("    }")
+    print("};")
+    print()
+    print("// Compare-exchange of the two 16-bit halves of two words independently")
+    print("// (two windows sorted at once, one per half).")
+    print("struct CeU16x2 {")
+    print("    __device__ __forceinline__ void operator()(uint32_t& a, uint32_t& b) const")
+    print("    {")
+    print("        uint32_t lo, hi;")
+    print('        asm("min.u16x2 %0, %1, %2;" : "=r"(lo) : "r"(a), "r"(b));')
+    print('        asm("max.u16x2 %0, %1, %2;" : "=r"(hi) : "r"(a), "r"(b));')
+    print("        a = lo;")
+    print("        b = hi;")
+    print("    }")
+    print("};")
     for live, n in ((9, 16), (25, 32)):
         pairs = batcher(n, live)
         check(pairs, live)
         print()
         print(f"// Sorts k[0..{live - 1}] ascending ({len(pairs)} comparators).")
-        print(f"__device__ __forceinline__ void sortnet{live}(uint32_t (&k)[{live}])")
+        print("template <class CE = CeU32>")
+        print(f"__device__ __forceinline__ void sortnet{live}(uint32_t (&k)[{live}], CE ce = CE())")
         print("{")
         for a, b in pairs:
-            print(f"    sortnet_ce(k[{a}], k[{b}]);")
+            print(f"    ce(k[{a}], k[{b}]);")
         print("}")
     print()
     print("}  // namespace enb")

@@ -62,7 +62,8 @@ class EnbEnfuseParams(ctypes.Structure):
                 ("exp_cutoff_lower_pct", ctypes.c_int32), ("exp_cutoff_upper_pct", ctypes.c_int32),
                 ("exp_cutoff_lower_projector", ctypes.c_int32), ("exp_cutoff_upper_projector", ctypes.c_int32),
                 ("ent_cutoff_lower", ctypes.c_double), ("ent_cutoff_upper", ctypes.c_double),
-                ("ent_cutoff_lower_pct", ctypes.c_int32), ("ent_cutoff_upper_pct", ctypes.c_int32)]
+                ("ent_cutoff_lower_pct", ctypes.c_int32), ("ent_cutoff_upper_pct", ctypes.c_int32),
+                ("exposure_table", ctypes.c_void_p), ("exposure_table_size", ctypes.c_int32)]
 
 
 class EnbFuseOptions(ctypes.Structure):
@@ -231,13 +232,15 @@ def enfuse_params(exposure_weight: float = 1.0, saturation_weight: float = 0.0, 
                   entropy_window_size: int = 3, gray_projector: str = "average",
                   mixer: Sequence[float] = (0.0, 0.0, 0.0), float_range: float = 0.0,
                   exposure_cutoff=((0.0, True), (100.0, True)), exposure_cutoff_projectors=("anti-value", "value"),
-                  entropy_cutoff=((0.0, True), (100.0, True))) -> EnbEnfuseParams:
+                  entropy_cutoff=((0.0, True), (100.0, True)), exposure_table=None) -> EnbEnfuseParams:
     """enfuse's weighting options (src/enfuse.cc:117-160, same defaults).
 
     float_range: float images only; 0 takes the reference's NumericTraits<float>::max() as the sample scale of
     the exposure and entropy weights, 1.0 is the normalised-float mode for images in [0, 1].
     exposure_cutoff / entropy_cutoff: (lower, upper) limits, each (value, is_percentage), as
-    --exposure-cutoff and --entropy-cutoff give them; exposure_cutoff_projectors judge the two limits."""
+    --exposure-cutoff and --entropy-cutoff give them; exposure_cutoff_projectors judge the two limits.
+    exposure_table: a user-defined exposure weight function tabulated at y = g / max for every sample value g
+    (256 entries for 8-bit, 65536 for 16-bit images; see exposure_table_of); the parameters keep it alive."""
     p = EnbEnfuseParams()
     p.w_exposure, p.w_saturation = exposure_weight, saturation_weight
     p.w_contrast, p.w_entropy = contrast_weight, entropy_weight
@@ -253,7 +256,19 @@ def enfuse_params(exposure_weight: float = 1.0, saturation_weight: float = 0.0, 
     p.exp_cutoff_upper_projector = GRAY_PROJECTORS[exposure_cutoff_projectors[1]]
     (p.ent_cutoff_lower, p.ent_cutoff_lower_pct), (p.ent_cutoff_upper, p.ent_cutoff_upper_pct) = \
         [(float(v), int(bool(pct))) for v, pct in entropy_cutoff]
+    if exposure_table is not None:
+        t = np.ascontiguousarray(exposure_table, dtype=np.float64)
+        p._exposure_table = t  # kept alive with the parameters
+        p.exposure_table, p.exposure_table_size = t.ctypes.data, t.size
     return p
+
+
+def exposure_table_of(weight, bits: int) -> np.ndarray:
+    """weight(y) of a Python callable at y = g / max for g = 0..max (max = 2^bits - 1): the table a
+    user-defined exposure weight function becomes (the same y the reference's ExposureFunctor forms,
+    src/enfuse.h:638)."""
+    maxv = (1 << bits) - 1
+    return np.array([weight(g / maxv) for g in range(maxv + 1)], dtype=np.float64)
 
 
 # --------------------------------------------------------------------------
@@ -588,5 +603,5 @@ def num_levels(width: int, height: int, min_levels: int = 1, exact_levels: int =
 
 
 __all__ = ["Context", "Pyramid", "EnbError", "EnbImage", "EnbEnfuseParams", "EnbFuseOptions", "enfuse_params",
-           "num_levels", "pitched", "load_library", "header_functions", "pixel_image", "plane_image",
+           "num_levels", "pitched", "exposure_table_of", "load_library", "header_functions", "pixel_image", "plane_image",
            "ENB_U8", "ENB_U16", "ENB_F32", "ENB_I16", "ENB_I32"]

@@ -89,12 +89,12 @@ def build_frontends(force: bool = False) -> list:
     cuda = _cuda_home()
     for name, srcs in FRONTEND_BINS.items():
         out = PKG_DIR / name
-        deps = [FRONTEND / x for x in srcs] + list(FRONTEND.glob("*.hpp")) + [INCLUDE / "enbgpu.h", LIB_PATH]
+        deps = [FRONTEND / x for x in srcs] + list(FRONTEND.glob("*.hpp")) + list(INCLUDE.glob("enbgpu*")) + [LIB_PATH]
         if force or not out.exists() or any(d.stat().st_mtime > out.stat().st_mtime for d in deps):
             tmp = out.with_name(out.name + ".tmp")
             cmd = ["g++", "-std=c++17", "-O2", "-I", str(INCLUDE), "-I", str(cuda / "include"), "-o", str(tmp)]
             cmd += [str(FRONTEND / x) for x in srcs]
-            cmd += ["-L", str(PKG_DIR), "-lenbgpu", "-L", str(cuda / "lib64"), "-lcudart",
+            cmd += ["-L", str(PKG_DIR), "-lenbgpu", "-L", str(cuda / "lib64"), "-lcudart", "-ldl",
                     "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + str(cuda / "lib64")]
             res = subprocess.run(cmd, capture_output=True, text=True)
             if res.returncode != 0:

@@ -6,8 +6,10 @@
 // with host buffers and writes the result with its alpha band as the
 // reference's checkpoint does.  Options of the reference that this build does
 // not provide (GPU/OpenCL selection, ICC colour spaces, layer selection,
-// expert parameters, edge-scale contrast, dynamic weight functions) are
-// rejected with a message instead of being ignored.
+// expert parameters, edge-scale contrast, OpenCL weight functions) are
+// rejected with a message instead of being ignored.  User-defined exposure
+// weight functions in shared objects are loaded, checked and tabulated for
+// the images' sample values (exposure_plugin.hpp).
 //
 // --dry-run (this front end's own option) prints the parsed settings as JSON
 // and exits without touching the GPU.
@@ -18,12 +20,14 @@
 #include <cstdio>
 #include <cstring>
 #include <iostream>
+#include <regex>
 #include <sstream>
 #include <string>
 #include <vector>
 
 #include "cli_common.hpp"
 #include "enbgpu.h"
+#include "exposure_plugin.hpp"
 #include "image_io.hpp"
 
 using namespace enbfront;
@@ -42,6 +46,9 @@ struct Settings {
     std::string depth;  // "" = the input's
     int verbose = 0;
     std::vector<std::string> inputs;
+    std::string exp_fn_name = "gaussian";
+    UserWeightFunction user_fn;  // library set: a user-defined exposure weight function
+    std::vector<double> exp_table;
 };
 
 void usage()
@@ -60,7 +67,8 @@ void usage()
         "      --entropy-weight=W           default 0.0\n"
         "      --exposure-optimum=O         default 0.5\n"
         "      --exposure-width=W           default 0.2\n"
-        "      --exposure-weight-function=F gaussian, lorentzian, half-sine, full-sine, bi-square\n"
+        "      --exposure-weight-function=F gaussian, lorentzian, half-sine, full-sine, bi-square,\n"
+        "                                   or SHARED-OBJECT:SYMBOL[:ARGUMENT[:...]]\n"
         "      --exposure-cutoff=L[:U[:LP[:UP]]]   values or percentages, projectors\n"
         "      --contrast-window-size=N     odd, >= 3 (default 5)\n"
         "      --entropy-window-size=N      odd, >= 3 (default 3)\n"
@@ -108,16 +116,46 @@ void mask_templates(const char* arg, std::string& soft, std::string& hard)
     }
 }
 
-int exposure_function(const std::string& name)
+// The built-in exposure weight functions (src/exposure_weight.cc:139-163);
+// -1 for any other name.
+int builtin_exposure_function(const std::string& name)
 {
-    const std::string n = lower(name.substr(0, name.find_first_of(";:/")));
+    const std::string n = lower(name);
     if (n == "gauss" || n == "gaussian") return ENB_EXP_GAUSSIAN;
     if (n == "lorentz" || n == "lorentzian") return ENB_EXP_LORENTZIAN;
     if (n == "halfsine" || n == "half-sine") return ENB_EXP_HALF_SINE;
     if (n == "fullsine" || n == "full-sine") return ENB_EXP_FULL_SINE;
     if (n == "bisquare" || n == "bi-square") return ENB_EXP_BISQUARE;
-    throw UsageError("unknown built-in exposure weight function \"" + name +
-                     "\" (dynamic weight functions are not supported by this front end)");
+    return -1;
+}
+
+// --exposure-weight-function NAME[:SYMBOL[:ARGUMENT...]], split at the path
+// delimiters ",;:" (src/enfuse.cc:1524-1560): a built-in NAME, else the shared
+// object NAME with the weight object SYMBOL and its arguments.
+void exposure_function_option(Settings& s, const std::string& arg)
+{
+    const std::regex delim("[,;:]");  // PATH_OPTION_DELIMITERS_REGEX, src/common.h:47
+    std::vector<std::string> t;
+    for (std::sregex_token_iterator i(arg.begin(), arg.end(), delim, -1), e; i != e; ++i) {
+        t.push_back(i->str());
+    }
+    if (t.empty() || t[0].empty()) {
+        throw UsageError("option \"--exposure-weight-function\" requires an argument");
+    }
+    s.exp_fn_name = t[0];
+    s.user_fn = UserWeightFunction{};
+    const int builtin = builtin_exposure_function(t[0]);
+    if (builtin >= 0) {
+        s.prm.exp_function = builtin;
+        return;
+    }
+    if (t.size() < 2) {
+        // built-in functions take no arguments, so a lone name must be one
+        throw UsageError("unknown built-in exposure weight function \"" + t[0] + "\"");
+    }
+    s.user_fn.library = t[0];
+    s.user_fn.symbol = t[1];
+    s.user_fn.arguments.assign(t.begin() + 2, t.end());
 }
 
 Settings parse(int argc, char** argv)
@@ -201,7 +239,7 @@ Settings parse(int argc, char** argv)
             s.prm.exp_width = v;
             break;
         }
-        case kExpFn: s.prm.exp_function = exposure_function(optarg); break;
+        case kExpFn: exposure_function_option(s, optarg); break;
         case kExpCut: {
             const std::vector<std::string> t = split_numeric(optarg);
             if (t.empty() || t[0].empty()) {
@@ -328,6 +366,15 @@ Settings parse(int argc, char** argv)
     if (s.inputs.empty()) {
         throw UsageError("no input files specified");
     }
+    if (!s.user_fn.library.empty() && s.prm.w_exposure > 0.0) {
+        // loaded and checked once all options are known (src/enfuse.cc:1913-1945)
+        s.user_fn.load(kCommand, s.prm.exp_optimum, s.prm.exp_width);
+        const std::string note = s.user_fn.check();
+        if (!note.empty()) {
+            throw UsageError("unusable exposure weight function \"" + s.exp_fn_name + "\"\n" + kCommand +
+                             ": note: " + note);
+        }
+    }
     return s;
 }
 
@@ -351,7 +398,22 @@ void print_json(const Settings& s)
       << ", \"levels\": " << s.opt.levels << ", \"wrap\": " << s.opt.wrap << ", \"hard_mask\": " << s.opt.hard_mask
       << ", \"save_masks\": " << (s.save_masks ? "true" : "false") << ", \"load_masks\": "
       << (s.load_masks ? "true" : "false") << ", \"soft_template\": \"" << s.soft_template << "\", \"hard_template\": \""
-      << s.hard_template << "\", \"output\": \"" << s.output << "\", \"inputs\": " << s.inputs.size() << "}";
+      << s.hard_template << "\", \"output\": \"" << s.output << "\", \"inputs\": " << s.inputs.size();
+    if (s.user_fn.loaded()) {
+        // the loaded function's library, symbol, arguments and weights at y = 0, 1/4, 1/2, 3/4, 1
+        o << ", \"user_weight\": {\"library\": \"" << s.user_fn.library << "\", \"symbol\": \"" << s.user_fn.symbol
+          << "\", \"arguments\": [";
+        for (size_t i = 0; i < s.user_fn.arguments.size(); ++i) {
+            o << (i ? ", " : "") << "\"" << s.user_fn.arguments[i] << "\"";
+        }
+        o << "], \"samples\": [";
+        o.precision(17);
+        for (int i = 0; i <= 4; ++i) {
+            o << (i ? ", " : "") << s.user_fn.fn->weight(i / 4.0);
+        }
+        o << "]}";
+    }
+    o << "}";
     std::cout << o.str() << std::endl;
 }
 
@@ -380,6 +442,15 @@ int run(Settings& s)
     }
     const int K = (int)imgs.size(), w = first.width, h = first.height;
     const int C = first.samples - first.extra >= 3 ? 3 : 1;
+    if (s.user_fn.loaded()) {
+        if (first.type == SampleType::F32) {
+            throw UsageError("user-defined exposure weight functions are tabulated for 8- and 16-bit images; "
+                             "this build has none for float images");
+        }
+        s.exp_table = s.user_fn.table(first.type == SampleType::U8 ? 255u : 65535u);
+        s.prm.exposure_table = s.exp_table.data();
+        s.prm.exposure_table_size = (int32_t)s.exp_table.size();
+    }
     enb_ctx* ctx = nullptr;
     check(nullptr, enb_create(0, &ctx), "enb_create");
     std::vector<enb_image> di;

@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define ENBGPU_ABI_VERSION 4
+#define ENBGPU_ABI_VERSION 5
 
 typedef enum {
     ENB_OK = 0,
@@ -130,6 +130,17 @@ typedef struct {
      * does).  Limits as for the exposure cutoff; defaults 0 % / 100 % (off). */
     double ent_cutoff_lower, ent_cutoff_upper;
     int32_t ent_cutoff_lower_pct, ent_cutoff_upper_pct;
+    /* User-defined exposure weight function (--exposure-weight-function=
+     * SHARED-OBJECT:SYMBOL[:ARGUMENT...], src/exposure_weight.cc:44-129):
+     * the function's weight(y) tabulated by the caller at y = g / max for
+     * every sample value g = 0..max of the images' type, exposure_table_size
+     * = max + 1 (256 for 8-bit, 65536 for 16-bit images).  It replaces the
+     * built-in exp_function in W_exp * weight(y) (src/enfuse.h:624-651),
+     * also under the exposure cutoff.  NULL (default): exp_function.  Float
+     * images, whose y is no sample index, reject a table
+     * (ENB_ERR_UNSUPPORTED).  The caller keeps the table alive for the call. */
+    const double* exposure_table;
+    int32_t exposure_table_size;
 } enb_enfuse_params;
 
 /* Options of the fuse drivers. */

@@ -918,7 +918,11 @@ int orc_enfuse_mask(const void* img, int dtype, int w, int h, int C, int pix_str
                 }
             }
             const double y = (double)gray[p] / (double)maxv;
-            out[p] = (float)(prm->w_exposure * exposure_weight(prm->exp_function, y, prm->exp_optimum, ew));
+            /* weight_function_->weight(y): the user's function through its
+             * values at the sample values */
+            const double f = prm->exposure_table ? prm->exposure_table[gray[p]]
+                                                 : exposure_weight(prm->exp_function, y, prm->exp_optimum, ew);
+            out[p] = (float)(prm->w_exposure * f);
         }
     }
 

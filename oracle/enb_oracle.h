@@ -77,6 +77,10 @@ typedef struct {
      * (float running sums along each row, src/enfuse.h:105-217) instead of
      * exact double window sums */
     int float_sliding_sums;
+    /* a user-defined exposure weight function (exposure_weight.cc:44-129)
+     * as its values at y = g / max, g = 0..max (integer images); NULL: the
+     * built-in exp_function */
+    const double* exposure_table;
 } orc_enfuse_params;
 
 /* roiBounds level count (src/bounds.h:97-177) for an ROI of w x h. */

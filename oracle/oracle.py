@@ -36,7 +36,7 @@ class OrcParams(ctypes.Structure):
                 ("exp_cutoff", ctypes.c_double * 2), ("exp_cutoff_pct", ctypes.c_int * 2),
                 ("exp_cutoff_proj", ctypes.c_int * 2),
                 ("ent_cutoff", ctypes.c_double * 2), ("ent_cutoff_pct", ctypes.c_int * 2),
-                ("float_sliding_sums", ctypes.c_int)]
+                ("float_sliding_sums", ctypes.c_int), ("exposure_table", ctypes.c_void_p)]
 
 
 def build(force: bool = False) -> Path:
@@ -119,10 +119,11 @@ def params(exposure_weight=1.0, saturation_weight=0.0, contrast_weight=0.0, entr
            contrast_window_size=5, entropy_window_size=3, gray_projector="average",
            mixer=(0.0, 0.0, 0.0), exposure_cutoff=((0.0, True), (100.0, True)),
            exposure_cutoff_projectors=("anti-value", "value"), entropy_cutoff=((0.0, True), (100.0, True)),
-           float_sliding_sums=False) -> OrcParams:
+           float_sliding_sums=False, exposure_table=None) -> OrcParams:
     """enfuse's weighting options.  Cutoffs are (value, is_percentage) pairs, lower then upper, as
     --exposure-cutoff and --entropy-cutoff give them; float_sliding_sums reproduces the reference's float
-    rounding of the contrast windows of float images."""
+    rounding of the contrast windows of float images; exposure_table holds a user-defined exposure weight
+    function's values at y = g / max (integer images)."""
     p = OrcParams()
     p.w_exposure, p.w_saturation, p.w_contrast, p.w_entropy = (exposure_weight, saturation_weight,
                                                                contrast_weight, entropy_weight)
@@ -136,6 +137,10 @@ def params(exposure_weight=1.0, saturation_weight=0.0, contrast_weight=0.0, entr
         p.exp_cutoff_proj[j] = GRAY_PROJECTORS[exposure_cutoff_projectors[j]]
         p.ent_cutoff[j], p.ent_cutoff_pct[j] = entropy_cutoff[j][0], int(entropy_cutoff[j][1])
     p.float_sliding_sums = int(float_sliding_sums)
+    if exposure_table is not None:
+        t = np.ascontiguousarray(exposure_table, dtype=np.float64)
+        p._exposure_table = t
+        p.exposure_table = t.ctypes.data
     return p
 
 

@@ -23,7 +23,7 @@ def test_exports_every_header_symbol(lib):
 
 
 def test_abi_version(lib):
-    assert lib.enb_abi_version() == 4
+    assert lib.enb_abi_version() == 5
 
 
 def test_num_levels_matches_oracle(lib, orc):

@@ -112,3 +112,85 @@ def test_image_files_round_trip(bins, tmp_path, dtype, S):
             for i in range(int.from_bytes(raw[ifd:ifd + 2], "little"))}
     assert {256, 257, 258, 259, 262, 273, 277, 278, 279, 284, 339} <= tags
     assert (338 in tags) == (S in (2, 4))
+
+
+# ---- user-defined exposure weight functions (shared objects) ----------------
+
+REPO = Path(__file__).resolve().parents[1]
+
+
+def build_weight_plugin(tmp: Path) -> Path:
+    """tests/cpp/exposure_weights.cc as a shared object (the interface header
+    include/enbgpu_exposure_weight.hpp)."""
+    so = tmp / "exposure_weights.so"
+    subprocess.run(["g++", "-std=c++17", "-O2", "-shared", "-fPIC", "-I", str(REPO / "include"),
+                    str(REPO / "tests" / "cpp" / "exposure_weights.cc"), "-o", str(so)], check=True)
+    return so
+
+
+@pytest.fixture(scope="module")
+def plugin(tmp_path_factory):
+    return build_weight_plugin(tmp_path_factory.mktemp("plugin"))
+
+
+def test_user_exposure_weight_function_loads(bins, plugin):
+    """SHARED-OBJECT:SYMBOL[:ARGUMENT...]: the object is initialised with the
+    optimum, the width and the arguments (src/exposure_weight.cc:96-129)."""
+    import math
+    r = _run(bins["enbgpu-enfuse"], "--dry-run", "--exposure-optimum=0.4", "--exposure-width=0.3",
+             f"--exposure-weight-function={plugin}:cosine_power:3", "x.tif")
+    u = json.loads(r.stdout)["user_weight"]
+    assert u["symbol"] == "cosine_power" and u["arguments"] == ["3"]
+
+    def cosp(y):
+        z = abs((y - 0.4) / 0.3)
+        return 0.0 if z >= 1.5707963267948966 else math.pow(math.cos(z), 3.0)
+    assert u["samples"] == [cosp(i / 4.0) for i in range(5)]
+    u = json.loads(_run(bins["enbgpu-enfuse"], "--dry-run", f"--exposure-weight-function={plugin};tent",
+                        "x.tif").stdout)["user_weight"]
+    assert u["samples"] == [max(1.0 - abs((i / 4.0 - 0.5) / 0.2) / 4.0, 0.0) for i in range(5)]
+    # not loaded without the exposure weight (src/enfuse.cc:1913)
+    p = json.loads(_run(bins["enbgpu-enfuse"], "--dry-run", "--exposure-weight=0",
+                        f"--exposure-weight-function={plugin}:negative", "x.tif").stdout)
+    assert "user_weight" not in p
+
+
+@pytest.mark.parametrize("spec,msg", [
+    ("negative", "at least one weight is negative"),
+    ("above_one", "at least one weight is larger than one"),
+    ("all_zero", "too many zeros"),
+    ("old_interface", "matches interface version 1, but enbgpu-enfuse requires version 2"),
+    ("cosine_power:abc", "raised exception: exponent is not a number"),
+    ("cosine_power:9", "raised exception: exponent outside (0, 8]"),
+    ("no_such_symbol", "not found in shared object"),
+])
+def test_user_exposure_weight_function_rejected(bins, plugin, spec, msg):
+    """The reference's checks (src/exposure_weight.cc:54-66, 237-264, src/enfuse.cc:1920-1945)."""
+    r = _run(bins["enbgpu-enfuse"], "--dry-run", f"--exposure-weight-function={plugin}:{spec}", "x.tif", check=False)
+    assert r.returncode == 1 and msg in r.stderr, r.stderr
+
+
+def test_user_exposure_weight_missing_library(bins, tmp_path):
+    r = _run(bins["enbgpu-enfuse"], "--dry-run", f"--exposure-weight-function={tmp_path}/none.so:f", "x.tif",
+             check=False)
+    assert r.returncode == 1 and "cannot load" in r.stderr
+
+
+def test_reference_example_plugin_loads(bins, tmp_path):
+    """The reference's own example weight function (doc/examples/enfuse/
+    variable_power.cc), compiled against the reference's exposure_weight_base.h,
+    loads into this front end: the interface classes agree in layout."""
+    from oracle import reference_build as ref
+    if not ref.available():
+        pytest.skip("reference tree not present")
+    import math
+    src = ref.REF_SRC.parent / "doc" / "examples" / "enfuse" / "variable_power.cc"
+    so = tmp_path / "variable_power.so"
+    subprocess.run(["g++", "-std=c++17", "-O2", "-shared", "-fPIC", "-I", str(ref.REF_SRC), str(src), "-o", str(so)],
+                   check=True)
+    u = json.loads(_run(bins["enbgpu-enfuse"], "--dry-run", f"--exposure-weight-function={so}:vpower:3",
+                        "x.tif").stdout)["user_weight"]
+    # max(1 - |(y - opt) / w'|^e, 0), w' = width * FWHM_gauss / (2 / exp(ln 2 / e))
+    wp = 0.2 * 2.3548200450309493820231386529193992755 / (2.0 / math.exp(math.log(2.0) / 3.0))
+    want = [max(1.0 - math.pow(abs((i / 4.0 - 0.5) / wp), 3.0), 0.0) for i in range(5)]
+    assert u["samples"] == pytest.approx(want, rel=1e-14, abs=1e-15)
