@@ -25,6 +25,14 @@
 // where E^T and Rd^T are the transposes of the expand and of the
 // normalised (opaque) reduce, written as gathers with the forward
 // operators' per-position weights and divisors.
+//
+// The image pyramids hold G - 1 rather than the log-mapped G itself
+// (log1p(v) for v >= 0, v / (1 - v) below): reduce and expand are
+// normalised, so every level and every Laplacian but the top one is the
+// same, the collapse yields C - 1 and the top level's Laplacian differs by
+// the same amount for every exposure, which the normalisation's backward
+// cancels.  In FP32 this keeps the fine Laplacians, small differences of
+// values near 1 to 1.7, a few times more accurate.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -94,7 +102,26 @@ __global__ void __launch_bounds__(256) k_adj_merge(const float* __restrict__ lp,
     }
 }
 
-// out = phi(C0); loss += (out - T)^2; gC0 = 2 (out - T) / N * phi'(C0).
+// Level 0 of an image pyramid in the offset form G - 1 (see above) from
+// interleaved float RGB.
+__global__ void __launch_bounds__(256) k_adj_to_pyramid(FloatPixelView img, float* __restrict__ g, int64_t pitch,
+                                                        int64_t plane)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= img.w) {
+        return;
+    }
+    const int y = blockIdx.y;
+    const float* px = img.p + (int64_t)y * img.pitch + (int64_t)x * img.stride;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float v = px[c];
+        g[c * plane + (int64_t)y * pitch + x] = v >= 0.0f ? log1pf(v) : __fdiv_rn(v, 1.0f - v);
+    }
+}
+
+// out = phi(C0) with C0 - 1 given (expm1 above 0, u / (1 + u) below);
+// loss += (out - T)^2; gC0 = 2 (out - T) / N * phi'(C0).
 __global__ void __launch_bounds__(256) k_adj_loss(const float* __restrict__ c0, int64_t pitch, int64_t plane,
                                                   const float* __restrict__ tgt, int64_t tpitch, int tstride,
                                                   float* __restrict__ out, int64_t opitch, int ostride,
@@ -108,11 +135,11 @@ __global__ void __launch_bounds__(256) k_adj_loss(const float* __restrict__ c0, 
         const int64_t o = (int64_t)y * pitch + x;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            const float v = c0[c * plane + o];
-            const float ov = from_pyramid_value(v);
+            const float u = c0[c * plane + o];  // C0 - 1
+            const float ov = u >= 0.0f ? expm1f(u) : __fdiv_rn(u, 1.0f + u);
             const float d = ov - tgt[(int64_t)y * tpitch + (int64_t)x * tstride + c];
             l += (double)d * d;
-            const float dphi = v >= 1.0f ? expf(v - 1.0f) : 1.0f / (v * v);
+            const float dphi = u >= 0.0f ? expf(u) : 1.0f / ((1.0f + u) * (1.0f + u));
             g0[c * plane + o] = 2.0f * d * inv_n * dphi;
             if (out) {
                 out[(int64_t)y * opitch + (int64_t)x * ostride + c] = ov;
@@ -352,6 +379,13 @@ cudaError_t launch_adj_merge(const PlanarView& lp, const PlanarView& m, const Pl
     note_launch("adj_merge", npix(lp.w, lp.h) * (12.0 + 4.0 + (first ? 12.0 : 24.0)));
     k_adj_merge<<<row_grid(lp.w, lp.h), 256, 0, st>>>((const float*)lp.p, (const float*)m.p, (float*)r.p, lp.pitch,
                                                       lp.plane, lp.w, first);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adj_to_pyramid(const FloatPixelView& img, const PlanarView& g, cudaStream_t st)
+{
+    note_launch("adj_to_pyramid", npix(img.w, img.h) * (4.0 * img.stride + 12.0));
+    k_adj_to_pyramid<<<row_grid(img.w, img.h), 256, 0, st>>>(img, (float*)g.p, g.pitch, g.plane);
     return cudaGetLastError();
 }
 

@@ -2642,7 +2642,9 @@ enb_status enb_fuse_grad(enb_ctx* ctx, const enb_enfuse_params* prm, int K, cons
     ENB_TRY(pyramid_alloc(ctx, L, w, h, 3, ENB_F32, &LP.p));
     ENB_TRY(pyramid_alloc(ctx, L, w, h, 1, ENB_F32, &M.p));
     auto build_lp = [&](int k) -> enb_status {
-        ENB_LAUNCH(ctx, launch_to_fixed(pixel_view(&images[k]), level_view(LP.p, 0), 0, ctx->stream));
+        const PixelView iv = pixel_view(&images[k]);
+        ENB_LAUNCH(ctx, launch_adj_to_pyramid(FloatPixelView{(const float*)iv.p, iv.pitch, iv.w, iv.h, 3, iv.stride},
+                                              level_view(LP.p, 0), ctx->stream));
         ENB_TRY(gaussian_levels(ctx, 0, LP.p, &alpha));
         ENB_TRY(laplacian_levels(ctx, 0, LP.p));
         return ENB_OK;

@@ -332,6 +332,8 @@ cudaError_t batch_plan_launch(const BatchPlan* p, int step, cudaStream_t st);
 cudaError_t launch_adj_norm(int K, const float* w, const float* a, float* m, int64_t pitch, int64_t plane, int width,
                             int height, cudaStream_t st);
 cudaError_t launch_adj_merge(const PlanarView& lp, const PlanarView& m, const PlanarView& r, int first, cudaStream_t st);
+// level 0 of an image pyramid in the adjoint's offset form (G - 1)
+cudaError_t launch_adj_to_pyramid(const FloatPixelView& img, const PlanarView& g, cudaStream_t st);
 cudaError_t launch_adj_loss(const PlanarView& c0, const float* tgt, int64_t tpitch, int tstride, float* out,
                             int64_t opitch, int ostride, const PlanarView& g0, double* loss, cudaStream_t st);
 cudaError_t launch_expand_T(const PlanarView& fine, const PlanarView& coarse, cudaStream_t st);
