@@ -353,20 +353,45 @@ __global__ void __launch_bounds__(256) k_copy_level0(const T* __restrict__ src, 
 // enfuse weights (src/enfuse.h:962-1212)
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(256) k_enfuse_mask(PixelView img, AlphaSrc alpha, WeightParams wp,
-                                                     WeightTables tab, float* __restrict__ out, int64_t opitch)
+// 32 x 16 output pixels per CTA, a pair of horizontally adjacent pixels per
+// thread: fully opaque tiles take the pair path (enb_iweights.cuh), the
+// others the per-pixel weight.
+constexpr int EMX = 32, EMY = 16;
+
+__host__ __device__ inline int emask_halo_x(const WeightParams& wp) { return (iweight_halo(wp) + 1) & ~1; }
+
+__global__ void __launch_bounds__(256, 3) k_enfuse_mask(PixelView img, AlphaSrc alpha, WeightParams wp,
+                                                        WeightTables tab, float* __restrict__ out, int64_t opitch)
 {
-    extern __shared__ unsigned char smem[];
-    const int halo = iweight_halo(wp);
-    const ITile t = itile_carve(smem, WT + 2 * halo);
-    itile_load(t, wp, img, alpha, blockIdx.x * WT - halo, blockIdx.y * WT - halo);
-    __syncthreads();
-    const int lx = threadIdx.x % WT, ly = threadIdx.x / WT;
-    const int x = blockIdx.x * WT + lx, y = blockIdx.y * WT + ly;
-    if (x >= img.w || y >= img.h) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int halo = iweight_halo(wp), hx = emask_halo_x(wp);
+    const int TW = EMX + 2 * hx, TH = EMY + 2 * halo;
+    const ITile t = itile_carve_rect(smem, TW, TH);
+    long long* fx = reinterpret_cast<long long*>(smem + ((itile_bytes_rect(TW, TH) + 15) & ~(size_t)15));  // [32]
+    const bool pair_path = iweight_pair_path(wp);
+    if (wp.use_entropy && pair_path && (int)threadIdx.x <= wp.entropy_window * wp.entropy_window) {
+        const int M = wp.entropy_window * wp.entropy_window;
+        fx[threadIdx.x] = tab.plogp_fx[(int64_t)M * (M + 1) + threadIdx.x];
+    }
+    // ends with a barrier (which also publishes fx)
+    const int opaque = itile_load_rect(t, wp, img, alpha, blockIdx.x * EMX - hx, blockIdx.y * EMY - halo);
+    const int px = threadIdx.x % (EMX / 2), py = threadIdx.x / (EMX / 2);
+    const int x = blockIdx.x * EMX + 2 * px, y = blockIdx.y * EMY + py;
+    const int cx = hx + 2 * px, cy = halo + py;
+    if (opaque && pair_path) {
+        float w0, w1;
+        pair_weights(t, wp, tab, fx, img.C, cx, cy, w0, w1);
+        out[(int64_t)y * opitch + x] = w0;
+        out[(int64_t)y * opitch + x + 1] = w1;
         return;
     }
-    out[(int64_t)y * opitch + x] = i_pixel_weight(t, wp, tab, img, (ly + halo) * t.TW + (lx + halo), x, y);
+    const int ci = cy * TW + cx;
+    if (y < img.h && x < img.w) {
+        out[(int64_t)y * opitch + x] = i_pixel_weight(t, wp, tab, img, ci, x, y);
+    }
+    if (y < img.h && x + 1 < img.w) {
+        out[(int64_t)y * opitch + x + 1] = i_pixel_weight(t, wp, tab, img, ci + 1, x + 1, y);
+    }
 }
 
 __global__ void __launch_bounds__(256) k_norm_accumulate(const float* __restrict__ m, int64_t mpitch,
@@ -864,14 +889,13 @@ cudaError_t launch_copy_level0(const PlanarView& s, int32_t* dst, cudaStream_t s
 cudaError_t launch_enfuse_mask(const PixelView& img, const AlphaSrc& alpha, const WeightParams& wp,
                                const WeightTables& tab, const FloatPlane& out, cudaStream_t st)
 {
-    const int halo = max(wp.use_contrast ? wp.contrast_window / 2 : 0, wp.use_entropy ? wp.entropy_window / 2 : 0);
-    const int TW = WT + 2 * halo;
-    const size_t smem = (size_t)TW * TW * (sizeof(int32_t) + 3 * sizeof(uint16_t) + 1);
+    const int TW = EMX + 2 * emask_halo_x(wp), TH = EMY + 2 * iweight_halo(wp);
+    const size_t smem = ((itile_bytes_rect(TW, TH) + 15) & ~(size_t)15) + 32 * sizeof(long long);
     note("enfuse_mask", npix(img.w, img.h) * (img.stride * esz(img.dtype) + (alpha.mode == kAlphaPlane ? 1.0 : 0.0) + 4.0));
     if (smem > 48 * 1024) {
         cudaFuncSetAttribute(k_enfuse_mask, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     }
-    k_enfuse_mask<<<grid2d(img.w, img.h, WT, WT), WT * WT, smem, st>>>(img, alpha, wp, tab, out.p, out.pitch);
+    k_enfuse_mask<<<grid2d(img.w, img.h, EMX, EMY), 256, smem, st>>>(img, alpha, wp, tab, out.p, out.pitch);
     return cudaGetLastError();
 }
 
