@@ -141,35 +141,55 @@ def from_pyramid(v: torch.Tensor) -> torch.Tensor:
     return torch.where(v >= 1.0, torch.expm1(v - 1.0), 1.0 - 1.0 / torch.where(v >= 1.0, torch.ones_like(v), v))
 
 
-def fuse(images: torch.Tensor, logits: torch.Tensor, theta: torch.Tensor, fn: str = "gaussian", cwin: int = 5,
-         range_: float = 1.0, levels: int = 0) -> torch.Tensor:
-    """(H, W, 3) fused image of (K, H, W, 3) float64 images."""
-    K, H, W, _ = images.shape
-    L = levels if levels > 0 else num_levels(W, H)
-    w = weights(images, theta, fn, cwin, range_)
-    wt = w * torch.exp(logits)
-    S = wt.sum(dim=0)
-    m = torch.where(S > 0, wt / torch.where(S > 0, S, torch.ones_like(S)), torch.full_like(wt, 1.0 / K))
+def _operators(H: int, W: int, L: int, dev):
     dims = [(H, W)]
     for _ in range(L - 1):
         dims.append(((dims[-1][0] + 1) >> 1, (dims[-1][1] + 1) >> 1))
-    dev = images.device
     Ah = [reduce_matrix(dims[l][0], dev).to_sparse() for l in range(L - 1)]
     Aw = [reduce_matrix(dims[l][1], dev).to_sparse() for l in range(L - 1)]
     Eh = [expand_matrix(dims[l][0], dims[l + 1][0], dev).to_sparse() for l in range(L - 1)]
     Ew = [expand_matrix(dims[l][1], dims[l + 1][1], dev).to_sparse() for l in range(L - 1)]
+    return Ah, Aw, Eh, Ew
+
+
+def _masks(w: torch.Tensor, logits: torch.Tensor) -> torch.Tensor:
+    K = w.shape[0]
+    wt = w * torch.exp(logits)
+    S = wt.sum(dim=0)
+    return torch.where(S > 0, wt / torch.where(S > 0, S, torch.ones_like(S)), torch.full_like(wt, 1.0 / K))
+
+
+def _forward(images: torch.Tensor, logits: torch.Tensor, theta: torch.Tensor, fn: str = "gaussian", cwin: int = 5,
+             range_: float = 1.0, levels: int = 0, keep: bool = False):
+    """The collapsed level 0 (3, H, W) and, with keep, the weights, masks,
+    Laplacians and operators (for the linearised differences below)."""
+    K, H, W, _ = images.shape
+    L = levels if levels > 0 else num_levels(W, H)
+    w = weights(images, theta, fn, cwin, range_)
+    m = _masks(w, logits)
+    Ah, Aw, Eh, Ew = _operators(H, W, L, images.device)
     G = [to_pyramid(images).permute(0, 3, 1, 2)]  # (K, 3, H, W)
     M = [m[:, None]]
     for l in range(L - 1):
         G.append(separable(Ah[l], G[-1], Aw[l]))
         M.append(separable(Ah[l], M[-1], Aw[l]))
-    R = []
+    R, LPs = [], []
     for l in range(L):
         lp = G[l] - separable(Eh[l], G[l + 1], Ew[l]) if l + 1 < L else G[l]
         R.append((lp * M[l]).sum(dim=0))
+        if keep:
+            LPs.append(lp)
     C = R[L - 1]
     for l in range(L - 2, -1, -1):
         C = R[l] + separable(Eh[l], C, Ew[l])
+    parts = dict(w=w, m=m, LP=LPs, ops=(Ah, Aw, Eh, Ew), L=L) if keep else None
+    return C, parts
+
+
+def fuse(images: torch.Tensor, logits: torch.Tensor, theta: torch.Tensor, fn: str = "gaussian", cwin: int = 5,
+         range_: float = 1.0, levels: int = 0) -> torch.Tensor:
+    """(H, W, 3) fused image of (K, H, W, 3) float64 images."""
+    C, _ = _forward(images, logits, theta, fn, cwin, range_, levels)
     return from_pyramid(C).permute(1, 2, 0)
 
 
@@ -178,24 +198,74 @@ def loss(images, logits, theta, target, **kw) -> torch.Tensor:
     return ((out - target) ** 2).mean()
 
 
+def _phi_difference(p: torch.Tensor, q: torch.Tensor, d: torch.Tensor) -> torch.Tensor:
+    """from_pyramid(p) - from_pyramid(q) with d = p - q given exactly:
+    e^(q-1) expm1(d) above 1, d / (p q) below, the plain difference where the
+    two straddle 1."""
+    hi = (p >= 1.0) & (q >= 1.0)
+    lo = (p < 1.0) & (q < 1.0)
+    one = torch.ones_like(p)
+    return torch.where(hi, torch.exp(q - 1.0) * torch.expm1(d),
+                       torch.where(lo, d / (torch.where(lo, p, one) * torch.where(lo, q, one)),
+                                   from_pyramid(p) - from_pyramid(q)))
+
+
+def _logit_difference(C: torch.Tensor, parts: dict, logits: torch.Tensor, target: torch.Tensor, k: int, y: int,
+                      x: int, step: float) -> float:
+    """(L(a + h) - L(a - h)) / 2h for the logit a_k(y, x).  Only the masks of
+    pixel (y, x) move, and everything between them and the collapsed level 0
+    is linear in the masks: the two mask changes are propagated through the
+    mask pyramids, the merge and the collapse on their own (so that the far
+    field keeps its significant digits instead of vanishing below the ulp of
+    the collapsed values), and the two fused images and the loss difference
+    are formed from them without cancellation."""
+    Ah, Aw, Eh, Ew = parts["ops"]
+    L, LPs = parts["L"], parts["LP"]
+    w = parts["w"][:, y, x]
+    a = logits[:, y, x].clone()
+    m0 = parts["m"][:, y, x]
+    dC = []
+    for sgn in (1.0, -1.0):
+        ak = a.clone()
+        ak[k] = a[k] + sgn * step
+        dm = _masks(w[:, None, None], ak[:, None, None])[:, 0, 0] - m0
+        dM = torch.zeros_like(parts["m"])[:, None]
+        dM[:, 0, y, x] = dm
+        dR = []
+        for l in range(L):
+            dR.append((LPs[l] * dM).sum(dim=0))
+            if l + 1 < L:
+                dM = separable(Ah[l], dM, Aw[l])
+        c = dR[L - 1]
+        for l in range(L - 2, -1, -1):
+            c = dR[l] + separable(Eh[l], c, Ew[l])
+        dC.append(c)
+    p, q = C + dC[0], C + dC[1]
+    dout = _phi_difference(p, q, dC[0] - dC[1])
+    t = target.permute(2, 0, 1)
+    return float((dout * (from_pyramid(p) + from_pyramid(q) - 2.0 * t)).mean() / (2 * step))
+
+
 def central_differences(images, logits, theta, target, coords: Sequence, step: float = 1e-6, **kw):
     """FP64 central differences (L(p + h) - L(p - h)) / 2h of the loss at the
     given coordinates: ("theta", i) or ("logit", k, y, x).  The difference of
     the two means of squares is formed per pixel as (a - b)(a + b - 2t) with
-    a, b the two fused images, so that it keeps its precision where one
-    coordinate moves the loss by a few hundred ulps (large images)."""
+    a, b the two fused images; for a logit coordinate the change of a - b is
+    propagated on its own (_logit_difference), because one pixel's logit
+    moves most pixels of a large image by less than their ulp."""
     out = []
     with torch.no_grad():
+        C = parts = None
         for c in coords:
-            lp, lm = logits.clone(), logits.clone()
+            if c[0] == "logit":
+                if parts is None:
+                    C, parts = _forward(images, logits, theta, keep=True, **kw)
+                out.append(_logit_difference(C, parts, logits, target, c[1], c[2], c[3], step))
+                continue
             tp, tm = theta.clone(), theta.clone()
-            if c[0] == "theta":
-                tp[c[1]] += step
-                tm[c[1]] -= step
-            else:
-                lp[c[1], c[2], c[3]] += step
-                lm[c[1], c[2], c[3]] -= step
-            a = fuse(images, lp, tp, **kw)
-            b = fuse(images, lm, tm, **kw)
+            tp[c[1]] += step
+            tm[c[1]] -= step
+            a = fuse(images, logits, tp, **kw)
+            b = fuse(images, logits, tm, **kw)
             out.append(float(((a - b) * (a + b - 2.0 * target)).mean() / (2 * step)))
     return np.array(out)
