@@ -37,6 +37,9 @@ __device__ __forceinline__ float third_of(float s)
     }
     const float q1 = __fdiv_rn(s, 3.0f);
     const float rem = __fmaf_rn(-3.0f, q1, s);  // s - 3 q1, exact
+    if (rem == 0.0f) {
+        return q1;  // s / 3 is a float: every rounding gives it (white pixels: 3 / 3)
+    }
     // s / 3 - q1 = rem / 3; a midpoint sits at +-ulp/2
     const float ulp = fabsf(__int_as_float(__float_as_int(q1) + 1) - q1);
     const float d = fabsf(rem) - 1.5f * ulp;  // 3 (|s/3 - q1| - ulp/2), exact or nearly
@@ -229,6 +232,9 @@ __device__ __forceinline__ void ftile_put_px(const FTile& t, const FloatWeightPa
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) {
         t.raw[ch * TT + k] = rgb[ch];
+    }
+    if (!wp.use_entropy) {
+        return;  // the window counters and the clamped samples feed only the entropy
     }
     if (wp.ent_cut) {
         float e[3] = {rgb[0], rgb[1], rgb[2]};
