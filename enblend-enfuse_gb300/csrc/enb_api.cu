@@ -2722,4 +2722,55 @@ enb_status enb_fuse_grad(enb_ctx* ctx, const enb_enfuse_params* prm, int K, cons
     return ENB_OK;
 }
 
+// enblend's seam mask by the nearest-feature transform (src/nearest.h:427-553,
+// src/mask.h:1101-1180 for --fine-mask --no-optimize).
+enb_status enb_nft_mask(enb_ctx* ctx, const enb_image* white_alpha, const enb_image* black_alpha,
+                        const enb_image* mask, const enb_fuse_options* opt)
+{
+    if (!ctx) {
+        return ENB_ERR_INVALID;
+    }
+    enb_fuse_options o;
+    enb_default_fuse_options(&o);
+    if (opt) {
+        o = *opt;
+    }
+    ENB_CHECK(ctx, white_alpha && black_alpha && mask, "nft_mask: white_alpha, black_alpha and mask required");
+    const int w = white_alpha->width, h = white_alpha->height;
+    ENB_CHECK(ctx, w >= 1 && h >= 1 && bytes_ok(white_alpha, w, h) && bytes_ok(black_alpha, w, h) && bytes_ok(mask, w, h),
+              "nft_mask: white_alpha, black_alpha and mask must be U8 planes of one size");
+    const int wrap = o.wrap != 0;
+    Staged sw, sb, sm;
+    const enb_image *wi = white_alpha, *bi = black_alpha, *mi = mask;
+    if (o.host_buffers) {
+        ENB_TRY(stage_in(ctx, white_alpha, sw, true));
+        ENB_TRY(stage_in(ctx, black_alpha, sb, true));
+        ENB_TRY(stage_in(ctx, mask, sm, false));
+        wi = &sw.dev;
+        bi = &sb.dev;
+        mi = &sm.dev;
+    }
+    DevBuf scratch, tally;
+    ENB_CUDA(ctx, scratch.alloc(nft_scratch_bytes(w, h, wrap), ctx->stream));
+    ENB_CUDA(ctx, tally.alloc(2 * sizeof(unsigned int), ctx->stream));
+    ENB_CUDA(ctx, cudaMemsetAsync(tally.p, 0, 2 * sizeof(unsigned int), ctx->stream));
+    const BytePlane wp = byte_plane(wi), bp = byte_plane(bi), mp = byte_plane(mi);
+    for (int stage = 0; stage < 3; ++stage) {
+        ENB_LAUNCH(ctx, launch_nft_stage(stage, wp, bp, mp, wrap, scratch.p, (unsigned int*)tally.p, ctx->stream));
+    }
+    unsigned int t[2] = {0u, 0u};
+    ENB_CUDA(ctx, cudaMemcpyAsync(t, tally.p, sizeof t, cudaMemcpyDeviceToHost, ctx->stream));
+    if (o.host_buffers) {
+        ENB_TRY(stage_out(ctx, mask, sm));
+    }
+    ENB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    // quick_tally's overlap check (src/nearest.h:465-470, 531-545): fewer than
+    // 4 (w + h) pixels covered by one image only, in both directions
+    const uint64_t threshold = 4ull * ((uint64_t)w + (uint64_t)h);
+    if (t[0] < threshold && t[1] < threshold) {
+        return fail(ctx, ENB_ERR_INVALID, "nft_mask: excessive image overlap; too high risk of defective seam line");
+    }
+    return ENB_OK;
+}
+
 }  // extern "C"

@@ -328,6 +328,12 @@ int batch_plan_steps(const BatchPlan* p);
 double batch_plan_pixels(const BatchPlan* p);
 cudaError_t batch_plan_launch(const BatchPlan* p, int step, cudaStream_t st);
 
+// nearest-feature seam mask (enb_nft.cu): scratch bytes for a w x h
+// canvas, and the three stages (0 columns and tallies, 1 rows, 2 mask)
+size_t nft_scratch_bytes(int w, int h, int wrap);
+cudaError_t launch_nft_stage(int stage, const BytePlane& white, const BytePlane& black, const BytePlane& mask,
+                             int wrap, void* scratch, unsigned int* tally, cudaStream_t st);
+
 // adjoint of the float enfuse (enb_adjoint.cu)
 cudaError_t launch_adj_norm(int K, const float* w, const float* a, float* m, int64_t pitch, int64_t plane, int width,
                             int height, cudaStream_t st);

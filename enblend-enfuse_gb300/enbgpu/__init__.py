@@ -135,6 +135,7 @@ _SIGNATURES = {
                                             _P(ctypes.c_float), _P(ctypes.c_int32)]),
     "enb_enblend": (ctypes.c_int, [ctypes.c_void_p, _IMG, _IMG, _IMG, _IMG, _IMG, _IMG, _IMG,
                                    _P(EnbFuseOptions)]),
+    "enb_nft_mask": (ctypes.c_int, [ctypes.c_void_p, _IMG, _IMG, _IMG, _P(EnbFuseOptions)]),
 }
 
 
@@ -578,6 +579,19 @@ class Context:
                                          ctypes.byref(pixel_image(out)), ctypes.byref(plane_image(out_alpha)),
                                          ctypes.byref(o)))
         return out, out_alpha
+
+    def nft_mask(self, white_alpha, black_alpha, mask=None, wrap: bool = False):
+        """enblend's seam mask from the nearest-feature transform (enb_nft_mask): 255 where the white image
+        wins.  Alpha planes (H, W) uint8, numpy (host buffers) or torch (device); returns the mask."""
+        host = not _is_torch(white_alpha)
+        if mask is None:
+            shp = white_alpha.shape
+            mask = np.zeros(shp, np.uint8) if host else white_alpha.new_zeros(shp)
+        o = self._options(0, wrap, False, "hash", 0, host, None)
+        self._check(self.lib.enb_nft_mask(self.handle, ctypes.byref(plane_image(white_alpha)),
+                                          ctypes.byref(plane_image(black_alpha)), ctypes.byref(plane_image(mask)),
+                                          ctypes.byref(o)))
+        return mask
 
 
 def pitched(x, align: int = 128):

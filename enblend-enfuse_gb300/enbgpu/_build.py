@@ -20,7 +20,7 @@ INCLUDE = REPO / "include"
 BUILD_DIR = ROOT / "_build"
 LIB_PATH = PKG_DIR / "libenbgpu.so"
 
-SOURCES = ["enb_kernels.cu", "enb_fused.cu", "enb_efuse.cu", "enb_coarse.cu", "enb_float.cu", "enb_batch.cu", "enb_adjoint.cu",
+SOURCES = ["enb_kernels.cu", "enb_fused.cu", "enb_efuse.cu", "enb_nft.cu", "enb_coarse.cu", "enb_float.cu", "enb_batch.cu", "enb_adjoint.cu",
            "enb_api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -4,6 +4,7 @@
 #pragma once
 
 #include <cstdio>
+#include <cstring>
 #include <cstdlib>
 #include <regex>
 #include <stdexcept>
@@ -258,6 +259,36 @@ inline Image with_alpha(const Image& colour, int C, const std::vector<uint8_t>& 
         }
     }
     return o;
+}
+
+// The alpha plane of an image as the library thresholds it (the 4th sample
+// of RGBA pixels between half the type's maximum and the maximum,
+// src/assemble.h:240-253; [0.5, 1] for float), 255 or 0; opaque otherwise.
+inline std::vector<uint8_t> alpha_plane(const Image& img)
+{
+    const size_t npx = (size_t)img.width * img.height;
+    std::vector<uint8_t> a(npx, 255);
+    if (img.samples != 4) {
+        return a;  // the library reads a footprint from the 4th sample of RGBA pixels only
+    }
+    const int ai = 3;
+    for (size_t p = 0; p < npx; ++p) {
+        const size_t i = p * img.samples + ai;
+        bool on;
+        if (img.type == SampleType::U8) {
+            on = img.data[i] >= 127;
+        } else if (img.type == SampleType::U16) {
+            uint16_t v;
+            std::memcpy(&v, &img.data[i * 2], 2);
+            on = v >= 32767;
+        } else {
+            float v;
+            std::memcpy(&v, &img.data[i * 4], 4);
+            on = v >= 0.5f && v <= 1.0f;
+        }
+        a[p] = on ? 255 : 0;
+    }
+    return a;
 }
 
 inline void check(enb_ctx* ctx, enb_status st, const char* what)

@@ -1,15 +1,19 @@
 // enblend_main.cpp -- the enblend command line over the GB300 path.
 //
 // The reference blends its inputs one after another into the accumulated
-// result under seam masks (src/enblend.h:56-560).  Seam generation (nearest
-// feature transform, graph cut, annealing, src/mask.h) is not part of this
-// build, so the masks come from files (--load-masks, src/mask.h:1002-1063):
-// mask i (template "%n" = i + 1, default mask-%n.tif, 8-bit gray, 255 where
-// the new image wins) blends input i + 1 into the result of inputs 0..i.  All
-// images share the union canvas (RGBA with the footprint in the alpha band,
-// or RGB).  The pyramid options (--levels, --wrap, --depth, --output) are the
-// reference's (src/enblend.cc:780-860); the seam-generation, colour-space
-// and GPU options are rejected with a message.
+// result under seam masks (src/enblend.h:56-560).  The masks come from files
+// (--load-masks, src/mask.h:1002-1063: mask i, template "%n" = i + 1,
+// default mask-%n.tif, 8-bit gray, 255 where the new image wins, blends
+// input i + 1 into the result of inputs 0..i), or, with --fine-mask
+// --no-optimize, from the nearest-feature transform of the two footprints on
+// the GPU (enb_nft_mask; the reference's mask for those options,
+// src/mask.h:1101-1180); --save-masks writes them.  The coarse masks and the
+// seam optimisers (vectorised seams, annealing, Dijkstra, graph cut) are not
+// part of this build.  All images share the union canvas (RGBA with the
+// footprint in the alpha band, or RGB).  The pyramid options (--levels,
+// --wrap, --depth, --output) are the reference's (src/enblend.cc:780-860);
+// the other seam-generation, colour-space and GPU options are rejected with
+// a message.
 //
 // --dry-run (this front end's own option) prints the parsed settings as JSON
 // and exits without touching the GPU.
@@ -35,7 +39,8 @@ struct Settings {
     enb_fuse_options opt{};
     std::string output = "a.tif";
     std::string mask_template = "mask-%n.tif";  // src/enblend.cc:140-142
-    bool load_masks = false, dry_run = false;
+    bool load_masks = false, save_masks = false, dry_run = false;
+    bool coarse_mask = true, optimize = true;   // the reference's defaults (src/enblend.cc:133, 136)
     std::string depth;
     int verbose = 0;
     std::vector<std::string> inputs;
@@ -51,6 +56,8 @@ void usage()
         "  -w, --wrap[=MODE]          periodic in x (none, horizontal; vertical and both wrap in x)\n"
         "  -d, --depth=DEPTH          output depth: the input's (8, 16, float)\n"
         "      --load-masks[=TEMPLATE] seam masks (default mask-%n.tif): mask i blends input i+1\n"
+        "      --fine-mask --no-optimize  seams from the nearest-feature transform (on the GPU)\n"
+        "      --save-masks[=TEMPLATE] write the generated seam masks\n"
         "      --dry-run              print the parsed settings and exit\n"
         "  -v, --verbose, -h, --help, -V, --version\n";
 }
@@ -60,7 +67,7 @@ Settings parse(int argc, char** argv)
     Settings s;
     enb_default_fuse_options(&s.opt);
     s.opt.host_buffers = 1;
-    enum { kLoad = 1000, kDry, kUnsupported, kBlendCs, kCompression };
+    enum { kLoad = 1000, kDry, kUnsupported, kBlendCs, kCompression, kSave, kFine, kCoarse, kOpt, kNoOpt };
     static struct option longopts[] = {
         {"load-masks", optional_argument, 0, kLoad},
         {"load-mask", optional_argument, 0, kLoad},
@@ -75,13 +82,13 @@ Settings parse(int argc, char** argv)
         {"blend-colorspace", required_argument, 0, kBlendCs},
         {"blend-color-space", required_argument, 0, kBlendCs},
         {"compression", required_argument, 0, kCompression},
+        {"save-masks", optional_argument, 0, kSave},
+        {"save-mask", optional_argument, 0, kSave},
+        {"fine-mask", no_argument, 0, kFine},
+        {"coarse-mask", optional_argument, 0, kCoarse},
+        {"optimize", no_argument, 0, kOpt},
+        {"no-optimize", no_argument, 0, kNoOpt},
         // seam generation, mask output and GPU selection of the reference
-        {"save-masks", optional_argument, 0, kUnsupported},
-        {"save-mask", optional_argument, 0, kUnsupported},
-        {"fine-mask", no_argument, 0, kUnsupported},
-        {"coarse-mask", optional_argument, 0, kUnsupported},
-        {"optimize", no_argument, 0, kUnsupported},
-        {"no-optimize", no_argument, 0, kUnsupported},
         {"primary-seam-generator", required_argument, 0, kUnsupported},
         {"image-difference", required_argument, 0, kUnsupported},
         {"anneal", required_argument, 0, kUnsupported},
@@ -112,6 +119,16 @@ Settings parse(int argc, char** argv)
                 s.mask_template = optarg;
             }
             break;
+        case kSave:
+            s.save_masks = true;
+            if (optarg && *optarg) {
+                s.mask_template = optarg;
+            }
+            break;
+        case kFine: s.coarse_mask = false; break;
+        case kCoarse: s.coarse_mask = true; break;
+        case kOpt: s.optimize = true; break;
+        case kNoOpt: s.optimize = false; break;
         case 'l': s.opt.levels = levels_arg(optarg); break;
         case 'w': s.opt.wrap = wrap_mode(optarg ? optarg : ""); break;
         case 'd': s.depth = lower(optarg); break;
@@ -147,8 +164,13 @@ Settings parse(int argc, char** argv)
     if (s.inputs.size() < 2) {
         throw UsageError("at least two input images are needed");
     }
-    if (!s.load_masks) {
-        throw UsageError("seam generation is not part of this build: give the seam masks with --load-masks");
+    if (!s.load_masks && (s.coarse_mask || s.optimize)) {
+        throw UsageError("this build generates seams only with --fine-mask --no-optimize (the nearest-feature "
+                         "transform); coarse masks and seam optimisation are not supported: give "
+                         "--fine-mask --no-optimize, or the seam masks with --load-masks");
+    }
+    if (s.load_masks && s.save_masks) {
+        throw UsageError("--load-masks and --save-masks exclude each other");
     }
     return s;
 }
@@ -179,15 +201,33 @@ int run(Settings& s)
     enb_ctx* ctx = nullptr;
     check(nullptr, enb_create(0, &ctx), "enb_create");
     Image result = first;  // the accumulated (black) image, blended into in place
-    std::vector<uint8_t> alpha((size_t)w * h);
+    std::vector<uint8_t> alpha = alpha_plane(first);  // the accumulated union alpha
     for (int i = 1; i < n; ++i) {
         const std::string mf = expand_template(s.mask_template, (unsigned)(n - 1), (unsigned)(i - 1));
-        Image m = read_image(mf);
-        if (m.samples != 1 || m.type != SampleType::U8) {
-            throw UsageError("mask image \"" + mf + "\" must be 8-bit gray without alpha");
-        }
-        if (m.width != w || m.height != h) {
-            throw UsageError("mask in \"" + mf + "\" does not have the canvas size");
+        Image m;
+        if (s.load_masks) {
+            m = read_image(mf);
+            if (m.samples != 1 || m.type != SampleType::U8) {
+                throw UsageError("mask image \"" + mf + "\" must be 8-bit gray without alpha");
+            }
+            if (m.width != w || m.height != h) {
+                throw UsageError("mask in \"" + mf + "\" does not have the canvas size");
+            }
+        } else {
+            // the nearest-feature transform of the new image's footprint
+            // against the accumulated one (src/mask.h:1130-1136)
+            m.width = w;
+            m.height = h;
+            m.samples = 1;
+            m.type = SampleType::U8;
+            m.data.assign((size_t)w * h, 0);
+            std::vector<uint8_t> wa = alpha_plane(imgs[i]);
+            enb_image wd = plane_desc(wa.data(), w, h, w, ENB_U8), bd = plane_desc(alpha.data(), w, h, w, ENB_U8);
+            enb_image md = plane_desc(m.data.data(), w, h, w, ENB_U8);
+            check(ctx, enb_nft_mask(ctx, &wd, &bd, &md, &s.opt), "enb_nft_mask");
+            if (s.save_masks) {
+                write_image(mf, m);
+            }
         }
         enb_image white = pixel_desc(imgs[i]), black = pixel_desc(result);
         enb_image mask = plane_desc(m.data.data(), w, h, w, ENB_U8);
@@ -211,7 +251,8 @@ int main(int argc, char** argv)
         if (s.dry_run) {
             std::cout << "{\"levels\": " << s.opt.levels << ", \"wrap\": " << s.opt.wrap << ", \"mask_template\": \""
                       << s.mask_template << "\", \"output\": \"" << s.output << "\", \"inputs\": " << s.inputs.size()
-                      << "}" << std::endl;
+                      << ", \"seams\": \"" << (s.load_masks ? "loaded" : "nearest-feature")
+                      << "\", \"save_masks\": " << (s.save_masks ? "true" : "false") << "}" << std::endl;
             return 0;
         }
         return run(s);

@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define ENBGPU_ABI_VERSION 5
+#define ENBGPU_ABI_VERSION 6
 
 typedef enum {
     ENB_OK = 0,
@@ -320,6 +320,21 @@ enb_status enb_enfuse_mask(enb_ctx* ctx, const enb_enfuse_params* params, const 
 enb_status enb_enfuse(enb_ctx* ctx, const enb_enfuse_params* params, int K, const enb_image* images,
                       const enb_image* alphas, const enb_image* masks_in, const enb_image* out,
                       const enb_image* out_alpha, const enb_fuse_options* opt);
+
+/* enblend's seam mask from the nearest-feature transform
+ * (nearestFeatureTransform, src/nearest.h:427-553; the mask of --fine-mask
+ * --no-optimize, src/mask.h:1101-1180): mask = 255 where the nearest pixel
+ * covered by the white image only (white_alpha > black_alpha) is nearer than
+ * the nearest pixel covered by the black image only, else 0, with the
+ * reference's Euclidean distance transform in float (the Felzenszwalb-
+ * Huttenlocher transform of its OpenMP build, src/openmp_vigra.h:257-433),
+ * bit-identical.  opt: wrap (the horizontally periodic transform,
+ * src/nearest.h:293-342) and host_buffers; other fields are ignored.  The
+ * call synchronises.  ENB_ERR_INVALID when fewer than 4 (w + h) pixels are
+ * covered by one image only in both directions (the reference's "excessive
+ * image overlap" exit); the mask is then unspecified. */
+enb_status enb_nft_mask(enb_ctx* ctx, const enb_image* white_alpha, const enb_image* black_alpha,
+                        const enb_image* mask, const enb_fuse_options* opt);
 
 /* enblendMain's pyramid section (src/enblend.h:330-510): blend `white` into
  * `black` under the 0/255 seam mask over the whole canvas.  out receives the

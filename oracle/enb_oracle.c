@@ -1903,3 +1903,118 @@ int orc_enblend_f(const float* white, const uint8_t* white_alpha, const float* b
     pyrd_free(&bl);
     return rc;
 }
+
+
+/* ---- nearest-feature seam mask (src/nearest.h, src/openmp_vigra.h) ---------- */
+
+/* The 1-D squared Euclidean transform of Felzenszwalb and Huttenlocher as the
+ * reference writes it (src/openmp_vigra.h:300-351): lower envelope of the
+ * parabolas q^2 + f(q), float arithmetic, with the sample index squared as an
+ * int where the reference squares an int (v[k]) and as a float where it
+ * squares a float (q). */
+static void nft_fh1d(float* d, const float* f, int n, int* v, float* z)
+{
+    int k = 0;
+    v[0] = 0;
+    z[0] = -INFINITY;
+    z[1] = INFINITY;
+    for (int q = 1; q < n; ++q) {
+        const float qf = (float)q;
+        const float sum_q = f[q] + qf * qf;
+        float s = (sum_q - (f[v[k]] + (float)(v[k] * v[k]))) / (float)(2 * (q - v[k]));
+        while (s <= z[k]) {
+            --k;
+            s = (sum_q - (f[v[k]] + (float)(v[k] * v[k]))) / (float)(2 * (q - v[k]));
+        }
+        ++k;
+        v[k] = q;
+        z[k] = s;
+        z[k + 1] = INFINITY;
+    }
+    k = 0;
+    for (int q = 0; q < n; ++q) {
+        while (z[k + 1] < (float)q) {
+            ++k;
+        }
+        d[q] = (float)((q - v[k]) * (q - v[k])) + f[v[k]];
+    }
+}
+
+/* Euclidean distance to the nearest feature (feat != 0) of a w x h image,
+ * columns first, then rows, sqrt in float (src/openmp_vigra.h:355-433). */
+static void nft_distance(const uint8_t* feat, int w, int h, float* dist)
+{
+    const int n = w > h ? w : h;
+    float* inter = (float*)malloc(sizeof(float) * (size_t)w * h);
+    float* f = (float*)malloc(sizeof(float) * (size_t)n);
+    float* d = (float*)malloc(sizeof(float) * (size_t)n);
+    int* v = (int*)malloc(sizeof(int) * (size_t)n);
+    float* z = (float*)malloc(sizeof(float) * (size_t)(n + 1));
+    for (int x = 0; x < w; ++x) {
+        for (int y = 0; y < h; ++y) {
+            f[y] = feat[(size_t)y * w + x] ? 0.0f : FLT_MAX;
+        }
+        nft_fh1d(d, f, h, v, z);
+        for (int y = 0; y < h; ++y) {
+            inter[(size_t)y * w + x] = d[y];
+        }
+    }
+    for (int y = 0; y < h; ++y) {
+        nft_fh1d(d, inter + (size_t)y * w, w, v, z);
+        for (int x = 0; x < w; ++x) {
+            dist[(size_t)y * w + x] = sqrtf(d[x]);
+        }
+    }
+    free(z);
+    free(v);
+    free(d);
+    free(f);
+    free(inter);
+}
+
+int orc_nft_mask(const uint8_t* white, const uint8_t* black, int w, int h, int wrap, uint8_t* mask)
+{
+    const size_t npix = (size_t)w * h;
+    /* saturating_subtract (src/nearest.h:358-372): white - black where white
+     * exceeds black; quick_tally counts such pixels up to the threshold
+     * (src/nearest.h:375-395, 465-470, 531-545) */
+    const unsigned threshold = 2u * 2u * ((unsigned)h + (unsigned)w);
+    unsigned t12 = 0, t21 = 0;
+    for (size_t i = 0; i < npix; ++i) {
+        t12 += (white[i] > black[i] && t12 < threshold) ? 1u : 0u;
+        t21 += (black[i] > white[i] && t21 < threshold) ? 1u : 0u;
+    }
+    if ((t12 > t21 ? t12 : t21) < threshold) {
+        return 2;
+    }
+    /* the periodic transform doubles the image horizontally and keeps the
+     * middle columns: x < w/2 from column w + x, the rest from column x
+     * (quadruple_image / quater_image, src/nearest.h:136-290) */
+    const int W = wrap ? 2 * w : w;
+    uint8_t* f12 = (uint8_t*)malloc((size_t)W * h);
+    uint8_t* f21 = (uint8_t*)malloc((size_t)W * h);
+    float* d12 = (float*)malloc(sizeof(float) * (size_t)W * h);
+    float* d21 = (float*)malloc(sizeof(float) * (size_t)W * h);
+    for (int y = 0; y < h; ++y) {
+        for (int X = 0; X < W; ++X) {
+            const size_t i = (size_t)y * w + (X % w);
+            f12[(size_t)y * W + X] = white[i] > black[i];
+            f21[(size_t)y * W + X] = black[i] > white[i];
+        }
+    }
+    nft_distance(f12, W, h, d12);
+    nft_distance(f21, W, h, d21);
+    const int half = w / 2;
+    for (int y = 0; y < h; ++y) {
+        for (int x = 0; x < w; ++x) {
+            const int X = wrap ? (x < half ? w + x : x) : x;
+            const size_t j = (size_t)y * W + X;
+            mask[(size_t)y * w + x] = d12[j] < d21[j] ? 255 : 0;
+        }
+    }
+    free(d21);
+    free(d12);
+    free(f21);
+    free(f12);
+    return 0;
+}

@@ -192,6 +192,16 @@ int orc_enblend_f(const float* white, const uint8_t* white_alpha, const float* b
                   const uint8_t* mask, int w, int h, int C, int pix_stride, int levels, int wrap, float* out,
                   uint8_t* out_alpha, double* level0_out);
 
+/* Seam mask of enblend's nearest-feature transform (src/nearest.h:427-553,
+ * the fine mask without optimisation, src/mask.h:1101-1180): 255 where the
+ * nearest pixel opaque in white only is nearer than the nearest pixel opaque
+ * in black only (Euclidean distances from the Felzenszwalb-Huttenlocher
+ * transform in float, src/openmp_vigra.h:257-433), else 0; wrap: the
+ * horizontally periodic transform (src/nearest.h:293-342).  Returns 0, or 2
+ * when fewer than 4 (w + h) pixels are opaque in one image only in both
+ * directions (the reference's "excessive image overlap" exit). */
+int orc_nft_mask(const uint8_t* white, const uint8_t* black, int w, int h, int wrap, uint8_t* mask);
+
 #ifdef __cplusplus
 }
 #endif

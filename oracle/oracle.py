@@ -479,3 +479,22 @@ def convert_with_draw(level0: np.ndarray, alpha: np.ndarray, dtype, draw: int, f
     v = np.clip(v, 0, np.iinfo(dtype).max).astype(dtype)
     on = np.asarray(alpha) != 0
     return np.where(on[..., None] if v.ndim == 3 else on, v, np.zeros_like(v))
+
+
+def nft_mask(white_alpha: np.ndarray, black_alpha: np.ndarray, wrap: bool = False) -> np.ndarray:
+    """enblend's nearest-feature seam mask (fine, not optimised) of two alpha
+    planes: 255 where the white image wins.  Raises ValueError on the
+    reference's "excessive image overlap"."""
+    wa = np.ascontiguousarray(white_alpha, np.uint8)
+    ba = np.ascontiguousarray(black_alpha, np.uint8)
+    h, w = wa.shape
+    m = np.zeros((h, w), np.uint8)
+    L = lib()
+    L.orc_nft_mask.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                               ctypes.c_void_p]
+    rc = L.orc_nft_mask(_p(wa), _p(ba), w, h, int(wrap), _p(m))
+    if rc == 2:
+        raise ValueError("excessive image overlap")
+    if rc:
+        raise ValueError(f"orc_nft_mask failed ({rc})")
+    return m

@@ -10,7 +10,11 @@ in place in the reference tree, against the project's VIGRA/GSL/LCMS2 shims
   * oracle/_ref/libenb_ref_enfuse.so: enfuse itself (src/enfuse.h with
     enfuseMask and enfuseMain, src/assemble.h, src/mga.h,
     src/exposure_weight.h, src/alternativepercentage.cc, src/parameter.cc,
-    src/error_message.cc) with ref_enfuse.cpp as the C entry points.
+    src/error_message.cc) with ref_enfuse.cpp as the C entry points;
+  * oracle/_ref/libenb_ref_nft.so: enblend's nearest-feature seam mask
+    (src/nearest.h and the distance transform of src/openmp_vigra.h, built
+    with OPENMP defined as the reference's OpenMP build is) with ref_nft.cpp
+    as the C entry point.
 They pin the C restatement in enb_oracle.c (and through it the CUDA path) to
 the reference's code; the committed fixtures under tests/golden/ carry that
 pin to machines without the reference tree.
@@ -39,6 +43,9 @@ SOURCES = [HERE / "ref_driver.cpp", SHIM / "gsl_shim.cpp"]
 REF_UNITS = ["minimizer.cc", "mersenne.cc"]
 ENFUSE_SOURCES = [HERE / "ref_enfuse.cpp", SHIM / "gsl_shim.cpp"]
 ENFUSE_REF_UNITS = ["minimizer.cc", "mersenne.cc", "alternativepercentage.cc", "parameter.cc", "error_message.cc"]
+NFT_LIB_PATH = OUT_DIR / "libenb_ref_nft.so"
+NFT_SOURCES = [HERE / "ref_nft.cpp"]
+NFT_REF_UNITS = ["parameter.cc", "error_message.cc", "timer.cc", "filenameparse.cc"]
 
 
 def available() -> bool:
@@ -50,12 +57,12 @@ def _deps(sources):
     return list(sources) + sorted(SHIM.rglob("*.h")) + sorted(SHIM.rglob("*.hxx"))
 
 
-def _compile(path: Path, sources, units, force: bool) -> Path:
+def _compile(path: Path, sources, units, force: bool, defines=()) -> Path:
     if not force and path.exists() and all(path.stat().st_mtime >= d.stat().st_mtime for d in _deps(sources)):
         return path
     OUT_DIR.mkdir(exist_ok=True)
     tmp = path.with_suffix(".so.tmp")
-    cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-fPIC", "-shared", "-DHAVE_CONFIG_H",
+    cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-fPIC", "-shared", "-DHAVE_CONFIG_H"] + list(defines) + [
            "-Wno-deprecated-declarations", "-I", str(SHIM), "-I", str(REF_SRC),
            "-I", str(REF_SRC / "layer_selection"), "-o", str(tmp)]
     cmd += [str(s) for s in sources] + [str(REF_SRC / u) for u in units]
@@ -72,6 +79,7 @@ def build_if_available(force: bool = False) -> Optional[Path]:
     if not available():
         return None
     _compile(ENFUSE_LIB_PATH, ENFUSE_SOURCES, ENFUSE_REF_UNITS, force)
+    _compile(NFT_LIB_PATH, NFT_SOURCES, NFT_REF_UNITS, force, ("-DOPENMP",))
     return _compile(LIB_PATH, SOURCES, REF_UNITS, force)
 
 
@@ -290,3 +298,30 @@ def enfuse_main(images, prm: RefEnfuseParams, levels: int = 0, wrap: bool = Fals
         raise ValueError(f"reference enfuseMain failed ({rc})")
     img = out[..., :C] if C == 3 else out[..., 0]
     return {"out": np.ascontiguousarray(img), "alpha": (out[..., C] != 0).astype(np.uint8), "masks": saved}
+
+
+_nlib = None
+
+
+def nft_mask(white_alpha: np.ndarray, black_alpha: np.ndarray, wrap: bool = False) -> Optional[np.ndarray]:
+    """The reference's nearest-feature seam mask of two alpha planes (255
+    where the white image wins); None where the reference exits for
+    excessive overlap."""
+    global _nlib
+    if _nlib is None:
+        if build_if_available() is None:
+            raise RuntimeError("the reference tree is not present")
+        L = ctypes.CDLL(str(NFT_LIB_PATH))
+        vp, i = ctypes.c_void_p, ctypes.c_int
+        L.ref_nft_mask.argtypes = [vp, vp, i, i, i, vp]
+        _nlib = L
+    wa = np.ascontiguousarray(white_alpha, np.uint8)
+    ba = np.ascontiguousarray(black_alpha, np.uint8)
+    h, w = wa.shape
+    m = np.zeros((h, w), np.uint8)
+    rc = _nlib.ref_nft_mask(_p(wa), _p(ba), w, h, int(wrap), _p(m))
+    if rc == 2:
+        return None
+    if rc:
+        raise ValueError(f"ref_nft_mask failed ({rc})")
+    return m

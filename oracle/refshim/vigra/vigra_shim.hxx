@@ -80,6 +80,8 @@ class Diff2D {
     Diff2D& operator-=(const Diff2D& o) { x -= o.x; y -= o.y; return *this; }
     Diff2D operator+(const Diff2D& o) const { return Diff2D(x + o.x, y + o.y); }
     Diff2D operator-(const Diff2D& o) const { return Diff2D(x - o.x, y - o.y); }
+    // VIGRA divides both coordinates (truncating toward zero for ints)
+    Diff2D operator/(int s) const { return Diff2D(x / s, y / s); }
     bool operator==(const Diff2D& o) const { return x == o.x && y == o.y; }
     bool operator!=(const Diff2D& o) const { return !(*this == o); }
     int width() const { return x; }
@@ -674,6 +676,27 @@ class BasicImage {
 
     void resize(int w, int h) { w_ = w; h_ = h; d_.assign((size_t)w * h, T()); }
     void init(const T& v) { std::fill(d_.begin(), d_.end(), v); }
+
+    // scan-order iteration over all pixels (row after row)
+    typedef T* ScanOrderIterator;
+    typedef const T* ConstScanOrderIterator;
+    T* begin() { return d_.data(); }
+    T* end() { return d_.data() + d_.size(); }
+    const T* begin() const { return d_.data(); }
+    const T* end() const { return d_.data() + d_.size(); }
+
+    // a column as a strided iterator
+    struct column_iterator {
+        T* p;
+        int stride;
+        T& operator*() const { return *p; }
+        T* operator->() const { return p; }
+        column_iterator& operator++() { p += stride; return *this; }
+        bool operator!=(const column_iterator& o) const { return p != o.p; }
+        bool operator==(const column_iterator& o) const { return p == o.p; }
+    };
+    column_iterator columnBegin(int x) { return column_iterator{d_.data() + x, w_}; }
+    column_iterator columnEnd(int x) { return column_iterator{d_.data() + x + (size_t)h_ * w_, w_}; }
 
   private:
     int w_, h_;

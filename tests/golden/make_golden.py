@@ -1,5 +1,5 @@
-"""Generate tests/golden/reference_pyramid.npz, reference_float.npz and
-reference_enfuse.npz from the reference's own code.
+"""Generate tests/golden/reference_pyramid.npz, reference_float.npz,
+reference_enfuse.npz and reference_nft.npz from the reference's own code.
 
 Runs the reference-code oracle (oracle/reference_build.py: the reference's
 pyramid.h / blend.h / fixmath.h, and enfuse.h's enfuseMask and enfuseMain,
@@ -26,6 +26,7 @@ from oracle import reference_build as ref  # noqa: E402
 OUT = Path(__file__).resolve().parent / "reference_pyramid.npz"
 OUT_FLOAT = Path(__file__).resolve().parent / "reference_float.npz"
 OUT_ENFUSE = Path(__file__).resolve().parent / "reference_enfuse.npz"
+OUT_NFT = Path(__file__).resolve().parent / "reference_nft.npz"
 
 # enfuseMask cases: weighting options in the keyword form of
 # oracle.reference_build.enfuse_params (cutoffs as (value, is_percentage) pairs)
@@ -213,6 +214,58 @@ def float_cases() -> None:
     print(f"wrote {OUT_FLOAT} ({OUT_FLOAT.stat().st_size} bytes)")
 
 
+def nft_footprints(h: int, w: int, kind: int, rng) -> tuple:
+    """Alpha footprints of an image pair: overlapping strips, discs, noise
+    with holes (kind 0, 1, 2)."""
+    wa = np.zeros((h, w), np.uint8)
+    ba = np.zeros((h, w), np.uint8)
+    if kind == 0:
+        a = int(rng.integers(w // 3, w - 2))
+        b = int(rng.integers(1, a))
+        wa[:, :a] = 255
+        ba[:, b:] = 255
+        wa[int(rng.integers(0, h)), :a // 2] = 0
+    elif kind == 1:
+        yy, xx = np.mgrid[:h, :w]
+        for img in (wa, ba):
+            for _ in range(3):
+                cy, cx, r = rng.integers(0, h), rng.integers(0, w), rng.integers(4, max(5, min(h, w)))
+                img[(yy - cy) ** 2 + (xx - cx) ** 2 < r * r] = 255
+    else:
+        wa[rng.random((h, w)) < 0.55] = 255
+        ba[rng.random((h, w)) < 0.55] = 255
+    return wa, ba
+
+
+def nft_cases() -> None:
+    """enblend's nearest-feature seam masks (src/nearest.h) of seeded
+    footprints, open and periodic, including pairs the reference rejects."""
+    rng = np.random.default_rng(20261204)
+    data = {}
+    k = 0
+    for (h, w) in [(9, 9), (24, 40), (37, 61), (64, 48), (80, 130), (120, 200)]:
+        for kind in (0, 1, 2):
+            for wrap in (False, True):
+                wa, ba = nft_footprints(h, w, kind, rng)
+                m = ref.nft_mask(wa, ba, wrap)
+                data[f"nft{k}_white"] = wa
+                data[f"nft{k}_black"] = ba
+                data[f"nft{k}_wrap"] = np.array(int(wrap))
+                data[f"nft{k}_mask"] = m if m is not None else np.zeros((0, 0), np.uint8)
+                k += 1
+    # nearly complete overlap: rejected
+    wa = np.full((30, 40), 255, np.uint8)
+    ba = wa.copy()
+    ba[0, 0] = 0
+    data[f"nft{k}_white"], data[f"nft{k}_black"], data[f"nft{k}_wrap"] = wa, ba, np.array(0)
+    m = ref.nft_mask(wa, ba, False)
+    data[f"nft{k}_mask"] = m if m is not None else np.zeros((0, 0), np.uint8)
+    k += 1
+    data["nft_count"] = np.array(k)
+    np.savez_compressed(OUT_NFT, **data)
+    print(f"wrote {OUT_NFT} ({OUT_NFT.stat().st_size} bytes)")
+
+
 def main() -> None:
     if ref.lib() is None:
         raise SystemExit("the reference tree is not available here")
@@ -276,9 +329,15 @@ def main() -> None:
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes)")
     float_cases()
     enfuse_cases()
+    nft_cases()
 
 
 if __name__ == "__main__":
+    if "--nft-only" in sys.argv:
+        if ref.lib() is None:
+            raise SystemExit("the reference tree is not available here")
+        nft_cases()
+        raise SystemExit(0)
     if "--enfuse-only" in sys.argv:
         if ref.lib() is None:
             raise SystemExit("the reference tree is not available here")

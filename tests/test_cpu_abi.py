@@ -23,7 +23,7 @@ def test_exports_every_header_symbol(lib):
 
 
 def test_abi_version(lib):
-    assert lib.enb_abi_version() == 5
+    assert lib.enb_abi_version() == 6
 
 
 def test_num_levels_matches_oracle(lib, orc):

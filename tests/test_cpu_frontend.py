@@ -73,11 +73,21 @@ def test_enfuse_rejects_unsupported_options(bins, args, msg):
 def test_enblend_options(bins):
     p = json.loads(_run(bins["enbgpu-enblend"], "--dry-run", "--load-masks=seam-%n.tif", "-l", "7", "-w",
                         "a.tif", "b.tif").stdout)
-    assert p == {"levels": 7, "wrap": 1, "mask_template": "seam-%n.tif", "output": "a.tif", "inputs": 2}
+    assert p == {"levels": 7, "wrap": 1, "mask_template": "seam-%n.tif", "output": "a.tif", "inputs": 2,
+                 "seams": "loaded", "save_masks": False}
+    # the reference's default seams (coarse mask, optimised) are not built
     r = _run(bins["enbgpu-enblend"], "--dry-run", "a.tif", "b.tif", check=False)
-    assert r.returncode == 1 and "--load-masks" in r.stderr
-    r = _run(bins["enbgpu-enblend"], "--dry-run", "--load-masks", "--fine-mask", "a.tif", "b.tif", check=False)
-    assert r.returncode == 1 and "seam" in r.stderr
+    assert r.returncode == 1 and "--fine-mask --no-optimize" in r.stderr and "--load-masks" in r.stderr
+    r = _run(bins["enbgpu-enblend"], "--dry-run", "--fine-mask", "a.tif", "b.tif", check=False)
+    assert r.returncode == 1 and "optimisation" in r.stderr
+    p = json.loads(_run(bins["enbgpu-enblend"], "--dry-run", "--fine-mask", "--no-optimize", "--save-masks=s-%n.npy",
+                        "a.tif", "b.tif", "c.tif").stdout)
+    assert p["seams"] == "nearest-feature" and p["save_masks"] and p["mask_template"] == "s-%n.npy"
+    r = _run(bins["enbgpu-enblend"], "--dry-run", "--load-masks", "--save-masks", "a.tif", "b.tif", check=False)
+    assert r.returncode == 1 and "exclude" in r.stderr
+    r = _run(bins["enbgpu-enblend"], "--dry-run", "--fine-mask", "--no-optimize", "--primary-seam-generator=gc",
+             "a.tif", "b.tif", check=False)
+    assert r.returncode == 1 and "not supported" in r.stderr
 
 
 CONVERT = r"""

@@ -260,3 +260,41 @@ def test_live_enfuse_against_reference(orc, seed):
     for draw in (0, 0xFFFFFFFF):
         r = ref.enfuse_main(imgs, ref.enfuse_params(**opts), dither=draw)
         assert np.array_equal(orc.convert_with_draw(res["level0"], res["alpha"], dt, draw), r["out"])
+
+
+# ---- enblend: the reference's nearest-feature seam mask ------------------------------
+
+NGOLDEN = np.load(Path(__file__).resolve().parent / "golden" / "reference_nft.npz")
+
+
+@pytest.mark.parametrize("k", range(int(NGOLDEN["nft_count"])))
+def test_golden_nft_mask(orc, k):
+    """nearestFeatureTransform (src/nearest.h:427-553) with the
+    Felzenszwalb-Huttenlocher transform of the reference's OpenMP build
+    (src/openmp_vigra.h:257-433): open and periodic, strips, discs, noisy
+    footprints; a pair with too much overlap is rejected as the reference
+    rejects it."""
+    wa, ba, wrap = NGOLDEN[f"nft{k}_white"], NGOLDEN[f"nft{k}_black"], bool(int(NGOLDEN[f"nft{k}_wrap"]))
+    want = NGOLDEN[f"nft{k}_mask"]
+    if want.size == 0:
+        with pytest.raises(ValueError):
+            orc.nft_mask(wa, ba, wrap)
+    else:
+        assert np.array_equal(orc.nft_mask(wa, ba, wrap), want)
+
+
+@pytest.mark.skipif(not ref.available(), reason="the reference tree is not present")
+@pytest.mark.parametrize("seed", range(6))
+def test_live_nft_mask(orc, seed):
+    rng = np.random.default_rng(500 + seed)
+    for _ in range(20):
+        h, w = int(rng.integers(8, 90)), int(rng.integers(8, 140))
+        wa = np.where(rng.random((h, w)) < rng.uniform(0.3, 0.9), 255, 0).astype(np.uint8)
+        ba = np.where(rng.random((h, w)) < rng.uniform(0.3, 0.9), 255, 0).astype(np.uint8)
+        wrap = bool(rng.integers(2))
+        want = ref.nft_mask(wa, ba, wrap)
+        if want is None:
+            with pytest.raises(ValueError):
+                orc.nft_mask(wa, ba, wrap)
+        else:
+            assert np.array_equal(orc.nft_mask(wa, ba, wrap), want)
