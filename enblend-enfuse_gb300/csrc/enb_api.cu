@@ -135,7 +135,8 @@ enb_status check_device_error(enb_ctx* ctx)
     }
     if (v) {
         cudaMemset(ctx->dev_err, 0, sizeof v);
-        ctx->err = "a kernel's wait for its tile copies timed out (TMA pipeline)";
+        ctx->err = (v & 1u) ? "a kernel's wait for its tile copies timed out (TMA pipeline)"
+                            : "a coarse item's wait for its predecessor step timed out (batched fuse)";
         return ENB_ERR_CUDA;
     }
     return ENB_OK;
@@ -2408,7 +2409,11 @@ enb_status enb_fuse_stacks(enb_ctx* ctx, const enb_enfuse_params* prm, int n, co
                 h.oapitch = has_oa ? st.out_alpha->pitch : 0;
             }
         }
-        cudaError_t e = batch_plan_create(hs, wp, ctx->tables, o.levels, o.wrap != 0, o.hard_mask != 0, coarse,
+        unsigned int* err = device_error_word(ctx);
+        if (!err) {
+            return fail(ctx, ENB_ERR_NOMEM, "fuse_stacks: the device error word");
+        }
+        cudaError_t e = batch_plan_create(hs, wp, ctx->tables, o.levels, o.wrap != 0, o.hard_mask != 0, coarse, err,
                                           ctx->stream, &bc.plan);
         if (e != cudaSuccess) {
             return fail(ctx, e == cudaErrorMemoryAllocation ? ENB_ERR_NOMEM : ENB_ERR_CUDA,

@@ -15,9 +15,10 @@
 //             exposure's image or mask pyramid (reduce with alpha); level 0
 //             of each image pyramid (the log mapping) is written by the
 //             weights kernel, which reads the input anyway;
-//   coarse    a persistent kernel: each CTA takes stacks from a device work
-//             queue and runs all levels below ~64x64 of that stack (reduce
-//             down, then merge and collapse up) inside the one CTA;
+//   coarse    a persistent kernel walking a device work queue of (stack,
+//             level, tile) items: every reduce tile of the levels below
+//             ~64x64 of every stack and exposure, then every up tile, each
+//             item waiting (bounded) for the step before it in its stack;
 //   up l      one CTA per 64x16 tile of level l of a stack: the collapsed
 //             result C[l] = sum_k (G_k[l] - E(G_k[l+1])) m_k[l] / D + E(C[l+1])
 //             (the Laplacian, the mask multiply, the accumulation and the
@@ -571,45 +572,91 @@ __global__ void __launch_bounds__(256, 3) k_batch_up0(const BatchStack* __restri
 }
 
 // ---------------------------------------------------------------------------
-// coarse levels: one CTA runs a whole stack's coarse end
+// coarse levels: a persistent kernel walking (stack, level, tile) items
 // ---------------------------------------------------------------------------
+//
+// The coarse end of every stack (its levels of at most coarse_pixels pixels)
+// is a list of items, each one tile of one step: a reduce tile of one
+// exposure's image or mask pyramid (down, level l -> l + 1), or an up tile
+// (Laplacians, masks, merge and collapse of level l).  The items of a step
+// depend on the whole previous step of the same stack (a tile's halo reaches
+// into its neighbours), which a per-(stack, step) counter records: an item
+// waits until the counter of its predecessor step reaches that step's item
+// count, and counts itself in its own step's counter when done.  The host
+// orders the device queue step by step across the stacks (step 0 of every
+// stack, then step 1, ...), so an item's predecessors always come earlier in
+// the queue; the CTAs take items in queue order, so every item an item waits
+// for is held by a running CTA, and no wait depends on a CTA that has not
+// started.  Waits are bounded (about a second); a CTA whose wait runs out
+// sets bit 1 of the context's error word and stops, and the items that
+// depend on its own item then run out too: the launch ends, and the host
+// fails the call.
+
+struct CoarseItem {
+    int stack, up, level, kind, tile;  // up = 0: reduce tile of `kind` (image k < K, mask K + k)
+    int wait_ctr, wait_count;          // predecessor step's counter (-1: none) and its item count
+    int sig_ctr;                       // this step's counter
+};
+
+constexpr long long kCoarseWaitSpins = 1ll << 23;  // x ~128 ns sleeps: about a second
 
 template <int C>
 __global__ void __launch_bounds__(RTHREADS) k_batch_coarse(const BatchStack* __restrict__ stacks,
-                                                           const int* __restrict__ coarse_list, int ncoarse,
-                                                           int* __restrict__ queue, int wrap, float inv_d)
+                                                           const CoarseItem* __restrict__ items, int nitems,
+                                                           int* __restrict__ queue, int* ctrs, unsigned int* err,
+                                                           int wrap, float inv_d)
 {
     extern __shared__ __align__(16) unsigned char smem[];  // max(reduce tile, (K + 1) * C windows)
     __shared__ int item;
+    __shared__ int ready;
     for (;;) {
         if (threadIdx.x == 0) {
-            item = atomicAdd(queue, 1);
+            const int it = atomicAdd(queue, 1);
+            int ok = 1;
+            if (it < nitems) {
+                const int wc = items[it].wait_ctr, need = items[it].wait_count;
+                if (wc >= 0) {
+                    long long spins = 0;
+                    while (atomicAdd(&ctrs[wc], 0) < need) {
+                        if (++spins > kCoarseWaitSpins) {
+                            ok = 0;
+                            break;
+                        }
+                        __nanosleep(128);
+                    }
+                    __threadfence();  // the predecessor step's writes before this item's reads
+                }
+            }
+            item = it;
+            ready = ok;
         }
         __syncthreads();
         const int it = item;
+        const int ok = ready;
         __syncthreads();
-        if (it >= ncoarse) {
+        if (it >= nitems) {
             return;
         }
-        const BatchStack& s = stacks[coarse_list[it]];
-        // down: levels Lc -> L-1 of every image and mask pyramid
-        for (int l = s.Lc; l + 1 < s.L; ++l) {
-            const int tx = (s.lw[l + 1] + RDW - 1) / RDW, ty = (s.lh[l + 1] + RDH - 1) / RDH;
-            for (int kind = 0; kind < 2 * s.K; ++kind) {
-                for (int t = 0; t < tx * ty; ++t) {
-                    batch_reduce_tile<C, false>(s, kind, l, (t % tx) * RDW, (t / tx) * RDH, wrap, smem);
-                    __syncthreads();
-                }
+        if (!ok) {
+            if (threadIdx.x == 0) {
+                atomicOr(err, 2u);
             }
+            return;
         }
-        // up: levels L-1 -> Lc (the fine launches continue from C[Lc])
-        float(*ss)[ESH][ESW] = reinterpret_cast<float(*)[ESH][ESW]>(smem);
-        for (int l = s.L - 1; l >= s.Lc; --l) {
-            const int tx = (s.lw[l] + ETW - 1) / ETW, ty = (s.lh[l] + ETH - 1) / ETH;
-            for (int t = 0; t < tx * ty; ++t) {
-                batch_up_tile<C, false>(s, l, (t % tx) * ETW, (t / tx) * ETH, wrap, inv_d, ss);
-                __syncthreads();
-            }
+        const CoarseItem ci = items[it];
+        const BatchStack& s = stacks[ci.stack];
+        if (!ci.up) {
+            const int tx = (s.lw[ci.level + 1] + RDW - 1) / RDW;
+            batch_reduce_tile<C, false>(s, ci.kind, ci.level, (ci.tile % tx) * RDW, (ci.tile / tx) * RDH, wrap, smem);
+        } else {
+            float(*ss)[ESH][ESW] = reinterpret_cast<float(*)[ESH][ESW]>(smem);
+            const int tx = (s.lw[ci.level] + ETW - 1) / ETW;
+            batch_up_tile<C, false>(s, ci.level, (ci.tile % tx) * ETW, (ci.tile / tx) * ETH, wrap, inv_d, ss);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();  // this item's writes before its count
+            atomicAdd(&ctrs[ci.sig_ctr], 1);
         }
     }
 }
@@ -628,9 +675,10 @@ struct BatchPlan {
     void* work = nullptr;         // workspace of all stacks
     BatchStack* dstacks = nullptr;
     int4* djobs = nullptr;
-    int* dcoarse = nullptr;       // stacks with a coarse end
-    int* dqueue = nullptr;
-    int ncoarse = 0;
+    CoarseItem* ditems = nullptr;  // the coarse items in queue order
+    int* dqueue = nullptr;         // queue position, then one counter per (stack, coarse step)
+    int nitems = 0, nctrs = 0;
+    unsigned int* err = nullptr;   // the context's device error word
     int maxK = 1;
     struct Step {
         int kind;  // 0 weights, 1 image reduce, 4 mask reduce, 2 coarse, 3 up
@@ -683,9 +731,10 @@ void batch_plan_destroy(BatchPlan* p)
 
 cudaError_t batch_plan_create(const std::vector<BatchStackHost>& hs, const FloatWeightParams& wp,
                               const WeightTables& tab, int levels, int wrap, int hard, int64_t coarse_pixels,
-                              cudaStream_t st, BatchPlan** out)
+                              unsigned int* err, cudaStream_t st, BatchPlan** out)
 {
     BatchPlan* p = new BatchPlan();
+    p->err = err;
     p->nstacks = (int)hs.size();
     p->wrap = wrap;
     p->hard = hard;
@@ -800,14 +849,69 @@ cudaError_t batch_plan_create(const std::vector<BatchStackHost>& hs, const Float
             p->steps.pop_back();
         }
     }
-    std::vector<int> coarse;
-    for (int i = 0; i < p->nstacks; ++i) {
-        if (stacks[i].Lc < stacks[i].L) {
-            coarse.push_back(i);
+    // the coarse items: per stack, the down steps (source levels Lc .. L-2,
+    // each all exposures' image and mask tiles) then the up steps (levels
+    // L-1 .. Lc); queued step by step across the stacks
+    std::vector<CoarseItem> items;
+    {
+        struct StackSteps {
+            int stack, base;                       // first counter
+            std::vector<std::vector<CoarseItem>> steps;
+        };
+        std::vector<StackSteps> ss;
+        int nctr = 0;
+        for (int i = 0; i < p->nstacks; ++i) {
+            const BatchStack& s = stacks[i];
+            if (s.Lc >= s.L) {
+                continue;
+            }
+            StackSteps st{i, nctr, {}};
+            for (int l = s.Lc; l + 1 < s.L; ++l) {
+                std::vector<CoarseItem> step;
+                const int t = ((s.lw[l + 1] + RDW - 1) / RDW) * ((s.lh[l + 1] + RDH - 1) / RDH);
+                for (int kind = 0; kind < 2 * s.K; ++kind) {
+                    for (int j = 0; j < t; ++j) {
+                        step.push_back(CoarseItem{i, 0, l, kind, j, -1, 0, 0});
+                    }
+                }
+                st.steps.push_back(step);
+            }
+            for (int l = s.L - 1; l >= s.Lc; --l) {
+                std::vector<CoarseItem> step;
+                const int t = ((s.lw[l] + ETW - 1) / ETW) * ((s.lh[l] + ETH - 1) / ETH);
+                for (int j = 0; j < t; ++j) {
+                    step.push_back(CoarseItem{i, 1, l, 0, j, -1, 0, 0});
+                }
+                st.steps.push_back(step);
+            }
+            for (size_t k = 0; k < st.steps.size(); ++k) {
+                for (CoarseItem& it : st.steps[k]) {
+                    it.sig_ctr = st.base + (int)k;
+                    if (k > 0) {
+                        it.wait_ctr = st.base + (int)k - 1;
+                        it.wait_count = (int)st.steps[k - 1].size();
+                    }
+                }
+            }
+            nctr += (int)st.steps.size();
+            ss.push_back(std::move(st));
         }
+        for (size_t k = 0;; ++k) {
+            bool any = false;
+            for (const StackSteps& st : ss) {
+                if (k < st.steps.size()) {
+                    items.insert(items.end(), st.steps[k].begin(), st.steps[k].end());
+                    any = true;
+                }
+            }
+            if (!any) {
+                break;
+            }
+        }
+        p->nitems = (int)items.size();
+        p->nctrs = nctr;
     }
-    p->ncoarse = (int)coarse.size();
-    if (p->ncoarse) {
+    if (p->nitems) {
         add_step(2, 0, 0.0);
     }
     for (int l = maxL - 1; l >= 0; --l) {
@@ -837,7 +941,8 @@ cudaError_t batch_plan_create(const std::vector<BatchStackHost>& hs, const Float
     // device memory: workspace, stack table, jobs, coarse list, queue counter
     const size_t o_st = align(bytes), o_jobs = o_st + align(sizeof(BatchStack) * stacks.size()),
                  o_coarse = o_jobs + align(sizeof(int4) * std::max<size_t>(jobs.size(), 1)),
-                 o_queue = o_coarse + align(sizeof(int) * std::max<size_t>(coarse.size(), 1)), total = o_queue + 256;
+                 o_queue = o_coarse + align(sizeof(CoarseItem) * std::max<size_t>(items.size(), 1)),
+                 total = o_queue + align(sizeof(int) * (size_t)(1 + p->nctrs));
     cudaError_t e = cudaMalloc(&p->work, total);
     if (e != cudaSuccess) {
         delete p;
@@ -861,14 +966,14 @@ cudaError_t batch_plan_create(const std::vector<BatchStackHost>& hs, const Float
     }
     p->dstacks = (BatchStack*)(w + o_st);
     p->djobs = (int4*)(w + o_jobs);
-    p->dcoarse = (int*)(w + o_coarse);
+    p->ditems = (CoarseItem*)(w + o_coarse);
     p->dqueue = (int*)(w + o_queue);
     e = cudaMemcpyAsync(p->dstacks, stacks.data(), sizeof(BatchStack) * stacks.size(), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess && !jobs.empty()) {
         e = cudaMemcpyAsync(p->djobs, jobs.data(), sizeof(int4) * jobs.size(), cudaMemcpyHostToDevice, st);
     }
-    if (e == cudaSuccess && !coarse.empty()) {
-        e = cudaMemcpyAsync(p->dcoarse, coarse.data(), sizeof(int) * coarse.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !items.empty()) {
+        e = cudaMemcpyAsync(p->ditems, items.data(), sizeof(CoarseItem) * items.size(), cudaMemcpyHostToDevice, st);
     }
     if (e == cudaSuccess) {
         e = cudaStreamSynchronize(st);  // the host tables go out of scope
@@ -925,20 +1030,21 @@ static cudaError_t launch_step(const BatchPlan* p, const BatchPlan::Step& s, cud
         break;
     case 2: {
         note_launch("batch_coarse", 0.0);
-        cudaError_t e = cudaMemsetAsync(p->dqueue, 0, sizeof(int), st);
+        // the queue position and the step counters start at 0 on every run
+        cudaError_t e = cudaMemsetAsync(p->dqueue, 0, sizeof(int) * (size_t)(1 + p->nctrs), st);
         if (e != cudaSuccess) {
             return e;
         }
         int sms = 0, dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const int grid = std::max(1, std::min(p->ncoarse, 2 * sms));
+        const int grid = std::max(1, std::min(p->nitems, 2 * sms));
         const size_t smem = std::max((size_t)kBatchReduceSmem, up_smem_bytes(p->maxK, C));
         if (smem > 48 * 1024) {
             cudaFuncSetAttribute(k_batch_coarse<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         }
-        k_batch_coarse<C><<<grid, RTHREADS, smem, st>>>(p->dstacks, p->dcoarse, p->ncoarse, p->dqueue, p->wrap,
-                                                        inv_d);
+        k_batch_coarse<C><<<grid, RTHREADS, smem, st>>>(p->dstacks, p->ditems, p->nitems, p->dqueue, p->dqueue + 1,
+                                                        p->err, p->wrap, inv_d);
         break;
     }
     default: {

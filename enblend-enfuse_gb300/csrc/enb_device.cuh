@@ -148,15 +148,17 @@ static inline dim3 grid2d(int w, int h, int tw, int th)
 }
 
 // Global load through the read-only path (NC: no thread of the launch writes
-// the data) or a plain, L1-cached load (the data was written earlier in the
-// same launch and is read only after the barrier that follows the write).
+// the data) or a load cached in L2 only (the data was written earlier in the
+// same launch, possibly by another SM, and is read only after the barrier or
+// the release/acquire counter that follows the write; L2 is coherent across
+// SMs, the SMs' L1 caches are not).
 template <bool NC, typename T>
 __device__ __forceinline__ T ld_src(const T* p)
 {
     if (NC) {
         return __ldg(p);
     }
-    return *p;
+    return __ldcg(p);
 }
 
 // Horizontal expand weights on source offsets (-1, 0, +1) of destination

@@ -320,9 +320,10 @@ struct BatchStackHost {
     int64_t oapitch;
 };
 struct BatchPlan;
+// err: the context's device error word (bit 1: a coarse item's wait ran out)
 cudaError_t batch_plan_create(const std::vector<BatchStackHost>& stacks, const FloatWeightParams& wp,
                               const WeightTables& tab, int levels, int wrap, int hard, int64_t coarse_pixels,
-                              cudaStream_t st, BatchPlan** out);
+                              unsigned int* err, cudaStream_t st, BatchPlan** out);
 void batch_plan_destroy(BatchPlan* p);
 int batch_plan_steps(const BatchPlan* p);
 double batch_plan_pixels(const BatchPlan* p);
