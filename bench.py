@@ -426,6 +426,33 @@ def enfuse_workload(ctx, stream, name: str, steps: int, cpu: bool) -> dict:
     return res
 
 
+def seam_mask_step(ctx, stream, white, black, reps: int = 5) -> dict:
+    """enblend's nearest-feature seam mask (enb_nft_mask) of the benchmark
+    pair's footprints on the 6963x3072 canvas, device-resident, CUDA events
+    (the call synchronises, so each rep is timed on its own)."""
+    import torch
+    wa = torch.from_numpy(np.where(white[..., 3] >= 32767, 255, 0).astype(np.uint8)).cuda()
+    ba = torch.from_numpy(np.where(black[..., 3] >= 32767, 255, 0).astype(np.uint8)).cuda()
+    mask = torch.empty_like(wa)
+    ctx.nft_mask(wa, ba, mask=mask)
+    times = []
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ctx.nft_mask(wa, ba, mask=mask)
+        b.record(stream)
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    ctx.profile(True)
+    ctx.nft_mask(wa, ba, mask=mask)
+    rep = ctx.profile_report()
+    ctx.profile(False)
+    h, w = mask.shape
+    return {"workload": f"nearest-feature seam mask of the benchmark pair's footprints, {w}x{h}",
+            "ms_per_call": statistics.median(times), "Mpx_per_s": w * h / 1e6 / (statistics.median(times) / 1e3),
+            "kernels_ms": {k: round(v["ms"], 3) for k, v in rep.items()}}
+
+
 def adjoint_step(ctx, stream, reps: int = 3) -> dict:
     """The differentiable fuse: 8 exposures of 2048x2048 FP32 RGB (EV -3.5..+3.5
     in 1-stop steps), loss = mean squared difference to the scene's tone-mapped
@@ -614,6 +641,8 @@ def run_ours(args) -> None:
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_oracle_rate(args.seed)
+    if rank == 0 and ws == 1:
+        line["seam_mask"] = seam_mask_step(ctx, stream, white, black)
     if rank == 0 and ws == 1 and not args.no_enfuse:
         del dw, db, dm, out, oa
         torch.cuda.empty_cache()

@@ -450,6 +450,11 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem)
     const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
 }
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all_but_one() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
@@ -462,6 +467,23 @@ __device__ __forceinline__ void up0_issue(const BatchStack& s, int k, int X0, in
     const int nx = min(ETW, dw - X0), ny = min(ETH, dh - Y0);
     const float* g0 = g0_level(s, k, C);
     const int64_t plane = (int64_t)s.pitch[0] * dh;
+    if (nx == ETW) {
+        // whole rows: 16-byte copies (rows of the level start on 128-byte
+        // boundaries and a tile on a 256-byte one)
+        constexpr int Q = ETW / 4;  // chunks of a row
+        const int32_t* m = m_level(s, k, 0);
+        for (int e = threadIdx.x; e < (C + 1) * ETH * Q; e += blockDim.x) {
+            const int c = e / (ETH * Q), rc = e - c * (ETH * Q), r = rc / Q, x = (rc - r * Q) * 4;
+            if (r < ny) {
+                if (c < C) {
+                    cp_async16(&g_tile[(c * ETH + r) * ETW + x], &g0[c * plane + (int64_t)(Y0 + r) * s.pitch[0] + X0 + x]);
+                } else {
+                    cp_async16(&mask_tile[r * ETW + x], &m[(int64_t)(Y0 + r) * s.pitch[0] + X0 + x]);
+                }
+            }
+        }
+        return;
+    }
     for (int e = threadIdx.x; e < C * ETH * ETW; e += blockDim.x) {
         const int c = e / (ETH * ETW), rc = e - c * (ETH * ETW), r = rc / ETW, x = rc - r * ETW;
         if (r < ny && x < nx) {
