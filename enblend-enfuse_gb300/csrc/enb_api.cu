@@ -575,12 +575,16 @@ enb_status build_tables(enb_ctx* ctx, const enb_enfuse_params* prm, uint32_t max
         scale_logb[b] = b >= 2 ? (float)((double)maxv / logb[b]) : 0.0f;
         scale_fx[b] = b >= 2 ? (unsigned long long)llround(ldexp((double)maxv / logb[b], 40)) : 0ull;
     }
+    // float images with entropy windows of 3 or 5: the clip-bin entropy table
+    const bool clip_table = maxv == 1u && nmax <= 25;
     const size_t sz_f = (size_t)n * 4, sz_pl = (size_t)nt * 8, sz_lb = (size_t)(nmax + 1) * 8,
-                 sz_sl = (size_t)(nmax + 1) * 4, sz_sf = (size_t)(nmax + 1) * 8;
+                 sz_sl = (size_t)(nmax + 1) * 4, sz_sf = (size_t)(nmax + 1) * 8,
+                 sz_ch = clip_table ? (size_t)(nmax + 1) * (nmax + 1) * (nmax + 1) * 4 : 0;
     const size_t o_exp = 0, o_con = round_up((int64_t)(o_exp + sz_f), 256), o_ent = round_up((int64_t)(o_con + sz_f), 256),
                  o_pl = round_up((int64_t)(o_ent + sz_f), 256), o_fx = round_up((int64_t)(o_pl + sz_pl), 256),
                  o_lb = round_up((int64_t)(o_fx + sz_pl), 256), o_sl = round_up((int64_t)(o_lb + sz_lb), 256),
-                 o_sf = round_up((int64_t)(o_sl + sz_sl), 256), total = round_up((int64_t)(o_sf + sz_sf), 256);
+                 o_sf = round_up((int64_t)(o_sl + sz_sl), 256), o_ch = round_up((int64_t)(o_sf + sz_sf), 256),
+                 total = round_up((int64_t)(o_ch + sz_ch), 256);
     if (ctx->table_mem) {
         cudaFreeAsync(ctx->table_mem, ctx->stream);
         ctx->table_mem = nullptr;
@@ -595,11 +599,16 @@ enb_status build_tables(enb_ctx* ctx, const enb_enfuse_params* prm, uint32_t max
     ENB_CUDA(ctx, cudaMemcpyAsync(b + o_lb, logb.data(), sz_lb, cudaMemcpyHostToDevice, ctx->stream));
     ENB_CUDA(ctx, cudaMemcpyAsync(b + o_sl, scale_logb.data(), sz_sl, cudaMemcpyHostToDevice, ctx->stream));
     ENB_CUDA(ctx, cudaMemcpyAsync(b + o_sf, scale_fx.data(), sz_sf, cudaMemcpyHostToDevice, ctx->stream));
+    WeightTables tab{(const float*)(b + o_exp), (const float*)(b + o_con), (const float*)(b + o_ent),
+                     (const double*)(b + o_pl), (const long long*)(b + o_fx), (const double*)(b + o_lb),
+                     (const float*)(b + o_sl), (const unsigned long long*)(b + o_sf), nullptr};
+    if (clip_table) {
+        ENB_CUDA(ctx, launch_clip_entropy_table(tab, nmax, (float*)(b + o_ch), ctx->stream));
+        tab.clip_h = (const float*)(b + o_ch);
+    }
     // pageable sources: make sure the copies consumed them before the vectors go
     ENB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    ctx->tables = WeightTables{(const float*)(b + o_exp), (const float*)(b + o_con), (const float*)(b + o_ent),
-                               (const double*)(b + o_pl), (const long long*)(b + o_fx), (const double*)(b + o_lb),
-                               (const float*)(b + o_sl), (const unsigned long long*)(b + o_sf)};
+    ctx->tables = tab;
     ctx->table_key = key;
     return ENB_OK;
 }

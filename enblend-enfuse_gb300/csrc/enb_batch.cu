@@ -37,6 +37,7 @@
 #include <vector>
 
 #include "enb_device.cuh"
+#include "enb_fpair.cuh"
 #include "enb_fweights.cuh"
 #include "enb_internal.h"
 #include "enb_reduce.cuh"
@@ -122,6 +123,90 @@ struct Level0Source {
 
 constexpr int BWT = 16;
 
+// Normalisation of the K weights wk[k * ws] of output pixel (x, y) of stack
+// s (src/enfuse.h:1382-1385 sum in exposure order, :1399-1442 hard mask,
+// :1526-1535 soft mask) into level 0 of the mask pyramids, and the union
+// alpha ua.
+__device__ __forceinline__ void batch_normalise(const BatchStack& s, const float* wk, int ws, int x, int y, int hard,
+                                                uint8_t ua)
+{
+    const int K = s.K;
+    const int64_t o = (int64_t)y * s.pitch[0] + x;
+    if (hard) {
+        float mx = 0.0f;
+        int mi = 0;
+        for (int k = 0; k < K; ++k) {
+            if (wk[k * ws] > mx) {
+                mx = wk[k * ws];
+                mi = k;
+            }
+        }
+        const float fallback = __fdiv_rn(255.0f, (float)K);
+        for (int k = 0; k < K; ++k) {
+            const float m = mx == 0.0f ? fallback : (k == mi ? 255.0f : 0.0f);
+            m_level(s, k, 0)[o] = mask_to_fixed<int32_t>(m, 15);
+        }
+    } else {
+        float norm = 0.0f;
+        for (int k = 0; k < K; ++k) {
+            norm = __fadd_rn(wk[k * ws], norm);
+        }
+        const float fallback = (float)(255 / K);
+        for (int k = 0; k < K; ++k) {
+            const float m = norm > 0.0f ? __fdiv_rn(__fmul_rn(255.0f, wk[k * ws]), norm) : fallback;
+            m_level(s, k, 0)[o] = mask_to_fixed<int32_t>(m, 15);
+        }
+    }
+    const uint8_t uv = ua ? 255 : 0;
+    s.u[s.off0[0] + o] = uv;
+    if (s.oalpha) {
+        s.oalpha[(int64_t)y * s.oapitch + x] = uv;
+    }
+}
+
+// batch_normalise with the K weights of output pixel (x, y) in the level-0
+// mask planes as float bits (written by this thread), replaced there by the
+// normalised masks.
+__device__ __forceinline__ void batch_normalise_planes(const BatchStack& s, int x, int y, int hard, uint8_t ua)
+{
+    const int K = s.K;
+    const int64_t o = (int64_t)y * s.pitch[0] + x;
+    if (hard) {
+        float mx = 0.0f;
+        int mi = 0;
+        for (int k = 0; k < K; ++k) {
+            const float wv = __int_as_float(m_level(s, k, 0)[o]);
+            if (wv > mx) {
+                mx = wv;
+                mi = k;
+            }
+        }
+        const float fallback = __fdiv_rn(255.0f, (float)K);
+        for (int k = 0; k < K; ++k) {
+            const float m = mx == 0.0f ? fallback : (k == mi ? 255.0f : 0.0f);
+            m_level(s, k, 0)[o] = mask_to_fixed<int32_t>(m, 15);
+        }
+    } else {
+        float norm = 0.0f;
+        for (int k = 0; k < K; ++k) {
+            norm = __fadd_rn(__int_as_float(m_level(s, k, 0)[o]), norm);
+        }
+        const float fallback = (float)(255 / K);
+        for (int k = 0; k < K; ++k) {
+            int32_t* mp = m_level(s, k, 0) + o;
+            const float m = norm > 0.0f ? __fdiv_rn(__fmul_rn(255.0f, __int_as_float(*mp)), norm) : fallback;
+            *mp = mask_to_fixed<int32_t>(m, 15);
+        }
+    }
+    const uint8_t uv = ua ? 255 : 0;
+    s.u[s.off0[0] + o] = uv;
+    if (s.oalpha) {
+        s.oalpha[(int64_t)y * s.oapitch + x] = uv;
+    }
+}
+
+// Weights of window sizes that the pair kernel does not take: one output
+// pixel per thread on 16x16 tiles (enb_fweights.cuh).
 template <int CW, int EW>
 __global__ void __launch_bounds__(256, 4) k_batch_weights(const BatchStack* __restrict__ stacks,
                                                        const int4* __restrict__ jobs, FloatWeightParams wp,
@@ -155,41 +240,75 @@ __global__ void __launch_bounds__(256, 4) k_batch_weights(const BatchStack* __re
         }
         __syncthreads();  // the next exposure's load overwrites the tile
     }
-    if (!inside) {
-        return;
+    if (inside) {
+        batch_normalise(s, wk, BWT * BWT, x, y, hard, ua);
     }
-    // normalisation (src/enfuse.h:1382-1385 sum in exposure order,
-    // :1399-1442 hard mask, :1526-1535 soft mask)
-    const int64_t o = (int64_t)y * s.pitch[0] + x;
-    if (hard) {
-        float mx = 0.0f;
-        int mi = 0;
-        for (int k = 0; k < K; ++k) {
-            if (wk[k * BWT * BWT] > mx) {
-                mx = wk[k * BWT * BWT];
-                mi = k;
+}
+
+// Weights, normalisation, level 0 of the image pyramids and of the mask
+// pyramids, and the union alpha of a 32x16 tile of a stack, two output
+// pixels per thread (enb_fpair.cuh).  The exposures' tiles come in turn; a
+// pixel's weight waits in its exposure's level-0 mask plane (as float bits)
+// until the normalisation replaces it.
+template <int CW, int EW, int C>
+__global__ void __launch_bounds__(FPT, 4) k_batch_weights_pair(const BatchStack* __restrict__ stacks,
+                                                            const int4* __restrict__ jobs, FloatWeightParams wp,
+                                                            WeightTables tab, int hard)
+{
+    constexpr int HALO = fpair_halo(CW, EW), HX = fpair_halo_x(HALO);
+    constexpr int TW = fpair_tw(CW, EW), TT = TW * fpair_th(CW, EW), NP = (TT + FPT - 1) / FPT;
+    extern __shared__ __align__(16) unsigned char bsmem[];
+    const int4 job = jobs[blockIdx.x];
+    const BatchStack& s = stacks[job.x];
+    const FTileP t = fpair_carve(bsmem, TW, TT, wp.repeat_slots, wp.ent_cut);
+    const int px = threadIdx.x % (FPX / 2), py = threadIdx.x / (FPX / 2);
+    const int x = job.y * FPX + 2 * px, y = job.z * FPY + py;
+    const bool in0 = x < s.w && y < s.h, in1 = x + 1 < s.w && y < s.h;
+    const int cx = HX + 2 * px, cy = HALO + py, ci = cy * TW + cx;
+    const int K = s.K;
+    const int64_t plane = (int64_t)s.pitch[0] * s.h, o = (int64_t)y * s.pitch[0] + x;
+    const int x0 = job.y * FPX - HX, y0 = job.z * FPY - HALO;
+    uint8_t ua0 = 0, ua1 = 0;
+    if (t.slots) {
+        fpair_clear_tables<C>(t);  // published by the load's barrier
+    }
+    for (int k = 0; k < K; ++k) {
+        const int opaque = fpair_load<NP, C, TW, TT>(t, wp, s.img[k], s.ipitch[k], s.istride[k], s.w, s.h, s.alpha[k],
+                                                     s.apitch[k], x0, y0);
+        if (t.slots && k + 1 < K) {
+            fpair_clear_tables<C>(t);  // the marks are in the tile
+        }
+        if (in0) {
+            float w0, w1;
+            fpair_weights<CW, EW, C>(t, wp, tab, cx, cy, x, y, s.w, s.h, opaque != 0, w0, w1);
+            int32_t* m0 = m_level(s, k, 0) + o;
+            float* g0 = g0_level(s, k, C) + o;
+            if (in1) {
+                // x is even and rows start on 128-byte boundaries
+                *reinterpret_cast<int2*>(m0) = make_int2(__float_as_int(w0), __float_as_int(w1));
+#pragma unroll
+                for (int c = 0; c < C; ++c) {
+                    // level 0 of the exposure's image pyramid: the log mapping, once
+                    *reinterpret_cast<float2*>(g0 + c * plane) =
+                        make_float2(to_pyramid_value(t.raw[c * TT + ci]), to_pyramid_value(t.raw[c * TT + ci + 1]));
+                }
+            } else {
+                m0[0] = __float_as_int(w0);
+#pragma unroll
+                for (int c = 0; c < C; ++c) {
+                    g0[c * plane] = to_pyramid_value(t.raw[c * TT + ci]);
+                }
             }
         }
-        const float fallback = __fdiv_rn(255.0f, (float)K);
-        for (int k = 0; k < K; ++k) {
-            const float m = mx == 0.0f ? fallback : (k == mi ? 255.0f : 0.0f);
-            m_level(s, k, 0)[o] = mask_to_fixed<int32_t>(m, 15);
-        }
-    } else {
-        float norm = 0.0f;
-        for (int k = 0; k < K; ++k) {
-            norm = __fadd_rn(wk[k * BWT * BWT], norm);
-        }
-        const float fallback = (float)(255 / K);
-        for (int k = 0; k < K; ++k) {
-            const float m = norm > 0.0f ? __fdiv_rn(__fmul_rn(255.0f, wk[k * BWT * BWT]), norm) : fallback;
-            m_level(s, k, 0)[o] = mask_to_fixed<int32_t>(m, 15);
-        }
+        ua0 |= t.a[ci];
+        ua1 |= t.a[ci + 1];
+        __syncthreads();  // the next exposure's samples overwrite the tile
     }
-    const uint8_t uv = ua ? 255 : 0;
-    s.u[s.off0[0] + o] = uv;
-    if (s.oalpha) {
-        s.oalpha[(int64_t)y * s.oapitch + x] = uv;
+    if (in0) {
+        batch_normalise_planes(s, x, y, hard, ua0);
+    }
+    if (in1) {
+        batch_normalise_planes(s, x + 1, y, hard, ua1);
     }
 }
 
@@ -702,6 +821,7 @@ struct BatchPlan {
     int nitems = 0, nctrs = 0;
     unsigned int* err = nullptr;   // the context's device error word
     int maxK = 1;
+    bool pair_weights = false;  // the weights step runs k_batch_weights_pair
     struct Step {
         int kind;  // 0 weights, 1 image reduce, 4 mask reduce, 2 coarse, 3 up
         int level;
@@ -801,17 +921,27 @@ cudaError_t batch_plan_create(const std::vector<BatchStackHost>& hs, const Float
         p->steps.push_back(BatchPlan::Step{kind, level, 0, 0, b});
         p->steps.back().job0 = (int64_t)jobs.size();
     };
-    const int halo = fweight_halo(wp);
-    const int TW = BWT + 2 * halo;
-    p->wp.repeat_slots = fweight_slots(wp, TW);
     // the tile, then the K weights of each output pixel
-    p->wsmem = align16(ftile_bytes(TW, p->wp.repeat_slots, p->wp.ent_cut)) + (size_t)p->maxK * BWT * BWT * sizeof(float);
+    p->pair_weights = fpair_path(wp);
+    int wtx = BWT, wty = BWT;
+    if (p->pair_weights) {
+        const int cw = wp.use_contrast ? wp.contrast_window : 0, ew = wp.use_entropy ? wp.entropy_window : 0;
+        const int TT = fpair_tw(cw, ew) * fpair_th(cw, ew);
+        p->wp.repeat_slots = fpair_slots(wp, TT);
+        p->wsmem = fpair_tile_bytes(TT, p->wp.repeat_slots, p->wp.ent_cut);
+        wtx = FPX;
+        wty = FPY;
+    } else {
+        const int TW = BWT + 2 * fweight_halo(wp);
+        p->wp.repeat_slots = fweight_slots(wp, TW);
+        p->wsmem = align16(ftile_bytes(TW, p->wp.repeat_slots, p->wp.ent_cut)) + (size_t)p->maxK * BWT * BWT * sizeof(float);
+    }
     double b = 0.0;
     add_step(0, 0, 0.0);
     for (int i = 0; i < p->nstacks; ++i) {
         const BatchStack& s = stacks[i];
-        for (int ty = 0; ty < (s.h + BWT - 1) / BWT; ++ty) {
-            for (int tx = 0; tx < (s.w + BWT - 1) / BWT; ++tx) {
+        for (int ty = 0; ty < (s.h + wty - 1) / wty; ++ty) {
+            for (int tx = 0; tx < (s.w + wtx - 1) / wtx; ++tx) {
                 jobs.push_back(make_int4(i, tx, ty, 0));
             }
         }
@@ -1022,6 +1152,18 @@ static cudaError_t launch_step(const BatchPlan* p, const BatchPlan::Step& s, cud
     switch (s.kind) {
     case 0: {
         note_launch("batch_weights", s.bytes);
+        if (p->pair_weights) {
+            ENB_FPAIR_DISPATCH(p->wp, {
+                auto k = k_batch_weights_pair<CWV, EWV, C>;
+                if (p->wsmem > 48 * 1024) {
+                    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->wsmem);
+                }
+                // as many CTAs per SM as the shared memory holds
+                cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+                k<<<(unsigned)s.njobs, FPT, p->wsmem, st>>>(p->dstacks, jobs, p->wp, p->tab, p->hard);
+            });
+            break;
+        }
         const int cw = p->wp.use_contrast ? p->wp.contrast_window : 5;
         const int ew = p->wp.use_entropy ? p->wp.entropy_window : 5;
         void (*k)(const BatchStack*, const int4*, FloatWeightParams, WeightTables, int, int) = k_batch_weights<0, 0>;

@@ -185,21 +185,25 @@ namespace enb {
 // Per-pixel counters (one 64-bit word per tile pixel, summed over a window):
 //   bits  0..14  samples equal to 1.0, channels 0..2 (5 bits each)
 //   bits 15..29  samples equal to 0.0
-//   bits 30..44  repeat marks
-//   bits 45..49  opaque pixels
-// A 5x5 window's sum keeps every field below 32.
-constexpr int kCntMark = 30, kCntOpaque = 45;
+//   bits 32..46  repeat marks
+//   bits 47..51  opaque pixels
+// A 5x5 window's sum keeps every field below 32, and no field crosses bit
+// 32, so the two 32-bit halves of a sum can be added separately.
+constexpr int kCntMark = 32, kCntOpaque = 47;
 
 // Histogram key of a float sample: its bit pattern, -0 folded into +0.
 __device__ __forceinline__ uint32_t float_key(float f) { return __float_as_uint(f == 0.0f ? 0.0f : f); }
 
 // Clip-value counters of one opaque pixel (bits 0..29 of its word).
-__device__ __forceinline__ uint32_t clip_counts(const float* rgb, int C)
+__device__ __forceinline__ uint32_t clip_counts(const float (&rgb)[3], int C)
 {
     uint32_t m = 0;
-    for (int c = 0; c < C; ++c) {
-        m |= (rgb[c] == 1.0f ? 1u : 0u) << (5 * c);
-        m |= (rgb[c] == 0.0f ? 1u : 0u) << (15 + 5 * c);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        if (c < C) {
+            m |= (rgb[c] == 1.0f ? 1u : 0u) << (5 * c);
+            m |= (rgb[c] == 0.0f ? 1u : 0u) << (15 + 5 * c);
+        }
     }
     return m;
 }

@@ -13,6 +13,7 @@
 #include <stdint.h>
 
 #include "enb_device.cuh"
+#include "enb_fpair.cuh"
 #include "enb_fweights.cuh"
 #include "enb_internal.h"
 
@@ -263,9 +264,60 @@ __global__ void __launch_bounds__(256) k_f_enfuse_mask(FloatPixelView img, const
     out[(int64_t)y * opitch + x] = f_pixel_weight<CW, EW>(t, wp, tab, ci, x, y, img.w, img.h, img.C, opaque != 0);
 }
 
+// The weights of one image, two output pixels per thread on 32x16 tiles
+// (enb_fpair.cuh), for the window sizes of the pair path.
+template <int CW, int EW, int C>
+__global__ void __launch_bounds__(FPT, 4) k_f_enfuse_mask_pair(FloatPixelView img, const uint8_t* __restrict__ alpha,
+                                                                int64_t apitch, FloatWeightParams wp, WeightTables tab,
+                                                                float* __restrict__ out, int64_t opitch)
+{
+    constexpr int HALO = fpair_halo(CW, EW), HX = fpair_halo_x(HALO);
+    constexpr int TW = fpair_tw(CW, EW), TT = TW * fpair_th(CW, EW), NP = (TT + 255) / 256;
+    extern __shared__ __align__(16) unsigned char fsmem[];
+    const FTileP t = fpair_carve(fsmem, TW, TT, wp.repeat_slots, wp.ent_cut);
+    if (t.slots) {
+        fpair_clear_tables<C>(t);  // published by the load's barrier
+    }
+    const int opaque = fpair_load<NP, C, TW, TT>(t, wp, img.p, img.pitch, img.stride, img.w, img.h, alpha, apitch,
+                                                 blockIdx.x * FPX - HX, blockIdx.y * FPY - HALO);
+    const int px = threadIdx.x % (FPX / 2), py = threadIdx.x / (FPX / 2);
+    const int x = blockIdx.x * FPX + 2 * px, y = blockIdx.y * FPY + py;
+    if (x >= img.w || y >= img.h) {
+        return;
+    }
+    float w0, w1;
+    fpair_weights<CW, EW, C>(t, wp, tab, HX + 2 * px, HALO + py, x, y, img.w, img.h, opaque != 0, w0, w1);
+    float* o = out + (int64_t)y * opitch + x;
+    o[0] = w0;
+    if (x + 1 < img.w) {
+        o[1] = w1;
+    }
+}
+
+// H of every window whose only repeated samples are clip values, by
+// entropy_clip_bins (the function that evaluates such windows in the
+// per-pixel weight path), so that the pair path's table lookups agree with
+// it bit for bit.
+__global__ void k_clip_entropy_table(WeightTables tab, int nmax, float* __restrict__ out)
+{
+    const int m = nmax + 1, total = m * m * m;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int n = i / (m * m), m1 = (i / m) % m, m0 = i % m;
+        out[i] = m1 + m0 <= n ? entropy_clip_bins(n, m1, m0, tab, nmax) : 0.0f;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
+
+cudaError_t launch_clip_entropy_table(const WeightTables& tab, int nmax, float* out, cudaStream_t st)
+{
+    const int m = nmax + 1;
+    note_launch("clip_entropy_table", (double)m * m * m * 4.0);
+    k_clip_entropy_table<<<(unsigned)((m * m * m + 255) / 256), 256, 0, st>>>(tab, nmax, out);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_f_to_pyramid(const FloatPixelView& s, const PlanarView& d, cudaStream_t st)
 {
@@ -355,11 +407,29 @@ cudaError_t launch_f_copy_level0(const PlanarView& s, float* dst, cudaStream_t s
 cudaError_t launch_f_enfuse_mask(const FloatPixelView& img, const BytePlane& alpha, const FloatWeightParams& wp,
                                  const WeightTables& tab, const FloatPlane& out, cudaStream_t st)
 {
+    note_launch("f_enfuse_mask", npix(img.w, img.h) * (img.stride * 4.0 + 1.0 + 4.0));
+    if (fpair_path(wp) && (!wp.use_entropy || tab.clip_h)) {
+        const int cw = wp.use_contrast ? wp.contrast_window : 0, ew = wp.use_entropy ? wp.entropy_window : 0;
+        const int TT = fpair_tw(cw, ew) * fpair_th(cw, ew);
+        FloatWeightParams p = wp;
+        p.repeat_slots = fpair_slots(wp, TT);
+        const size_t smem = fpair_tile_bytes(TT, p.repeat_slots, p.ent_cut);
+        const dim3 g = grid2d(img.w, img.h, FPX, FPY);
+        ENB_FPAIR_DISPATCH(p, {
+            auto k = img.C == 1 ? k_f_enfuse_mask_pair<CWV, EWV, 1> : k_f_enfuse_mask_pair<CWV, EWV, 3>;
+            if (smem > 48 * 1024) {
+                cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            }
+            // as many CTAs per SM as the shared memory holds
+            cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+            k<<<g, FPT, smem, st>>>(img, alpha.p, alpha.pitch, p, tab, out.p, out.pitch);
+        });
+        return cudaGetLastError();
+    }
     const int TW = FWT + 2 * fweight_halo(wp);
     FloatWeightParams p = wp;
     p.repeat_slots = fweight_slots(wp, TW);
     const size_t smem = ftile_bytes(TW, p.repeat_slots, p.ent_cut);
-    note_launch("f_enfuse_mask", npix(img.w, img.h) * (img.stride * 4.0 + 1.0 + 4.0));
     const int cw = p.use_contrast ? p.contrast_window : 5, ew = p.use_entropy ? p.entropy_window : 5;
     void (*k)(FloatPixelView, const uint8_t*, int64_t, FloatWeightParams, WeightTables, float*, int64_t) =
         k_f_enfuse_mask<0, 0>;

@@ -76,6 +76,10 @@ struct WeightTables {
     const double* logb;       // [n_max+1]: log(b)
     const float* scale_logb;  // [n_max+1]: max / log(b) as float
     const unsigned long long* scale_fx;  // [n_max+1]: max / log(b) in 2^-40 fixed point
+    // float images, entropy windows of 3 or 5 (n_max = 9 or 25): H of a window
+    // of n opaque taps whose only repeated samples are m1 taps at 1.0 and m0
+    // at 0.0, at [(n * (n_max + 1) + m1) * (n_max + 1) + m0]; else nullptr
+    const float* clip_h;
 };
 
 struct WeightParams {
@@ -361,6 +365,10 @@ cudaError_t launch_f_blend(const PlanarView& m, const PlanarView& wt, const Plan
 cudaError_t launch_f_mask_mul_acc(const PlanarView& lp, const PlanarView& m, int32_t divisor, const PlanarView& r,
                                   int acc, cudaStream_t st);
 cudaError_t launch_f_copy_level0(const PlanarView& s, float* dst, cudaStream_t st);
+// Fills WeightTables.clip_h (tab's other tables on the device) for windows
+// of nmax taps.
+cudaError_t launch_clip_entropy_table(const WeightTables& tab, int nmax, float* out, cudaStream_t st);
+
 cudaError_t launch_f_enfuse_mask(const FloatPixelView& img, const BytePlane& alpha, const FloatWeightParams& wp,
                                  const WeightTables& tab, const FloatPlane& out, cudaStream_t st);
 

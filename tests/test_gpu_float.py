@@ -180,6 +180,58 @@ def test_enfuse_mask_f32(ctx, orc, float_range, projector):
         assert np.all(got[alpha == 0] == 0.0)
 
 
+@pytest.mark.parametrize("h,w", [(5, 5), (17, 33), (61, 97), (130, 257)])
+@pytest.mark.parametrize("windows", [(5, 5), (3, 3), (5, 3), (3, 5), (0, 5), (5, 0), (7, 5)])
+@pytest.mark.parametrize("akind", ["opaque", "holes"])
+def test_enfuse_mask_f32_windows(ctx, orc, h, w, windows, akind):
+    """Contrast windows of 3, 5 and 7 and entropy windows of 3 and 5 (either
+    weight off), odd and even widths, images narrower than a tile, alpha
+    holes, clipped and repeated samples, both cutoffs on the larger sizes."""
+    import enbgpu
+    from enbgpu import synthetic
+    rng = np.random.default_rng(100 + h + w)
+    img = synthetic.expose(synthetic.log_radiance(h, w, 8.0, seed=h), 0.5, np.float32)
+    img[h // 4: h // 2, w // 5: w // 2] = 1.0
+    img[h // 2: h // 2 + 3, : w // 3, 2] = 0.0
+    img[: h // 3, w // 2:, 0] = 0.625
+    alpha = _alpha(rng, h, w, akind)
+    cw, ew = windows
+    if min(h, w) < max(cw, ew):
+        pytest.skip("window larger than the image")
+    kw = dict(exposure_weight=1.0, saturation_weight=0.2, contrast_weight=0.5 if cw else 0.0,
+              entropy_weight=0.3 if ew else 0.0, contrast_window_size=cw or 5, entropy_window_size=ew or 5)
+    if h > 20:
+        kw.update(exposure_cutoff=((2.0, True), (97.0, True)), entropy_cutoff=((5.0, True), (95.0, True)))
+    ref = orc.enfuse_mask_f(img, alpha, orc.params(**kw), 1.0)
+    out = torch.zeros((h, w), dtype=torch.float32, device="cuda")
+    ctx.enfuse_mask(_dev(img), _dev(alpha), out, enbgpu.enfuse_params(float_range=1.0, **kw))
+    got = out.cpu().numpy().astype(np.float64)
+    _close(got, ref.astype(np.float64), WEIGHT_RTOL, 1e-7 * np.abs(ref).max(), f"weights {windows}")
+    assert np.all(got[alpha == 0] == 0.0)
+
+
+@pytest.mark.parametrize("levels", [4, 32, 1024])
+@pytest.mark.parametrize("ew", [3, 5])
+def test_enfuse_mask_f32_repeated_samples(ctx, orc, levels, ew):
+    """Float samples quantised to a few levels: nearly every entropy window
+    holds repeated samples (bins of several taps besides the clip values),
+    in every channel, with alpha holes."""
+    import enbgpu
+    from enbgpu import synthetic
+    rng = np.random.default_rng(levels + ew)
+    h, w = 70, 101
+    img = synthetic.expose(synthetic.log_radiance(h, w, 8.0, seed=9), 0.5, np.float32)
+    img = (np.round(img * levels) / levels).astype(np.float32)
+    alpha = _alpha(rng, h, w, "holes")
+    kw = dict(exposure_weight=1.0, saturation_weight=0.2, contrast_weight=0.5, entropy_weight=0.3,
+              contrast_window_size=5, entropy_window_size=ew)
+    ref = orc.enfuse_mask_f(img, alpha, orc.params(**kw), 1.0)
+    out = torch.zeros((h, w), dtype=torch.float32, device="cuda")
+    ctx.enfuse_mask(_dev(img), _dev(alpha), out, enbgpu.enfuse_params(float_range=1.0, **kw))
+    _close(out.cpu().numpy().astype(np.float64), ref.astype(np.float64), WEIGHT_RTOL, 1e-7 * np.abs(ref).max(),
+           f"weights, {levels} levels")
+
+
 def test_enfuse_mask_f32_entropy_compat(ctx, orc):
     """The reference's float entropy weight (H * FLT_MAX) on its own."""
     import enbgpu
