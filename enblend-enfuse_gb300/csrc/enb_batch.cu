@@ -164,47 +164,6 @@ __device__ __forceinline__ void batch_normalise(const BatchStack& s, const float
     }
 }
 
-// batch_normalise with the K weights of output pixel (x, y) in the level-0
-// mask planes as float bits (written by this thread), replaced there by the
-// normalised masks.
-__device__ __forceinline__ void batch_normalise_planes(const BatchStack& s, int x, int y, int hard, uint8_t ua)
-{
-    const int K = s.K;
-    const int64_t o = (int64_t)y * s.pitch[0] + x;
-    if (hard) {
-        float mx = 0.0f;
-        int mi = 0;
-        for (int k = 0; k < K; ++k) {
-            const float wv = __int_as_float(m_level(s, k, 0)[o]);
-            if (wv > mx) {
-                mx = wv;
-                mi = k;
-            }
-        }
-        const float fallback = __fdiv_rn(255.0f, (float)K);
-        for (int k = 0; k < K; ++k) {
-            const float m = mx == 0.0f ? fallback : (k == mi ? 255.0f : 0.0f);
-            m_level(s, k, 0)[o] = mask_to_fixed<int32_t>(m, 15);
-        }
-    } else {
-        float norm = 0.0f;
-        for (int k = 0; k < K; ++k) {
-            norm = __fadd_rn(__int_as_float(m_level(s, k, 0)[o]), norm);
-        }
-        const float fallback = (float)(255 / K);
-        for (int k = 0; k < K; ++k) {
-            int32_t* mp = m_level(s, k, 0) + o;
-            const float m = norm > 0.0f ? __fdiv_rn(__fmul_rn(255.0f, __int_as_float(*mp)), norm) : fallback;
-            *mp = mask_to_fixed<int32_t>(m, 15);
-        }
-    }
-    const uint8_t uv = ua ? 255 : 0;
-    s.u[s.off0[0] + o] = uv;
-    if (s.oalpha) {
-        s.oalpha[(int64_t)y * s.oapitch + x] = uv;
-    }
-}
-
 // Weights of window sizes that the pair kernel does not take: one output
 // pixel per thread on 16x16 tiles (enb_fweights.cuh).
 template <int CW, int EW>
@@ -302,13 +261,86 @@ __global__ void __launch_bounds__(FPT, 4) k_batch_weights_pair(const BatchStack*
         }
         ua0 |= t.a[ci];
         ua1 |= t.a[ci + 1];
-        __syncthreads();  // the next exposure's samples overwrite the tile
+        __syncthreads();  // the next exposure's load overwrites the tile
     }
+    // the union alpha; k_batch_normalise turns the weights into masks
     if (in0) {
-        batch_normalise_planes(s, x, y, hard, ua0);
+        const uint8_t u0 = ua0 ? 255 : 0, u1 = ua1 ? 255 : 0;
+        s.u[s.off0[0] + o] = u0;
+        if (in1) {
+            s.u[s.off0[0] + o + 1] = u1;
+        }
+        if (s.oalpha) {
+            uint8_t* oa = s.oalpha + (int64_t)y * s.oapitch + x;
+            oa[0] = u0;
+            if (in1) {
+                oa[1] = u1;
+            }
+        }
     }
-    if (in1) {
-        batch_normalise_planes(s, x + 1, y, hard, ua1);
+}
+
+// Normalisation of the weights that k_batch_weights_pair left in the level-0
+// mask planes (float bits) of a 32x16 tile of a stack, two output pixels per
+// thread: src/enfuse.h:1382-1385 (sum in exposure order), :1399-1442 (hard
+// mask), :1526-1535 (soft mask), into Int32 9.15 masks.
+__global__ void __launch_bounds__(256) k_batch_normalise(const BatchStack* __restrict__ stacks,
+                                                         const int4* __restrict__ jobs, int hard)
+{
+    const int4 job = jobs[blockIdx.x];
+    const BatchStack& s = stacks[job.x];
+    const int px = threadIdx.x % (FPX / 2), py = threadIdx.x / (FPX / 2);
+    const int x = job.y * FPX + 2 * px, y = job.z * FPY + py;
+    if (x >= s.w || y >= s.h) {
+        return;
+    }
+    const int K = s.K;
+    const int64_t o = (int64_t)y * s.pitch[0] + x;
+    const bool pair = x + 1 < s.w;
+    const auto wt = [&](int k) {
+        const int32_t* m = m_level(s, k, 0) + o;
+        // x is even and rows start on 128-byte boundaries
+        return pair ? __ldcg(reinterpret_cast<const float2*>(m)) : make_float2(__int_as_float(__ldcg(m)), 0.0f);
+    };
+    const auto put = [&](int k, float m0, float m1) {
+        int32_t* m = m_level(s, k, 0) + o;
+        if (pair) {
+            *reinterpret_cast<int2*>(m) = make_int2(mask_to_fixed<int32_t>(m0, 15), mask_to_fixed<int32_t>(m1, 15));
+        } else {
+            m[0] = mask_to_fixed<int32_t>(m0, 15);
+        }
+    };
+    if (hard) {
+        float mx0 = 0.0f, mx1 = 0.0f;
+        int mi0 = 0, mi1 = 0;
+        for (int k = 0; k < K; ++k) {
+            const float2 w = wt(k);
+            if (w.x > mx0) {
+                mx0 = w.x;
+                mi0 = k;
+            }
+            if (w.y > mx1) {
+                mx1 = w.y;
+                mi1 = k;
+            }
+        }
+        const float fallback = __fdiv_rn(255.0f, (float)K);
+        for (int k = 0; k < K; ++k) {
+            put(k, mx0 == 0.0f ? fallback : (k == mi0 ? 255.0f : 0.0f), mx1 == 0.0f ? fallback : (k == mi1 ? 255.0f : 0.0f));
+        }
+    } else {
+        float n0 = 0.0f, n1 = 0.0f;
+        for (int k = 0; k < K; ++k) {
+            const float2 w = wt(k);
+            n0 = __fadd_rn(w.x, n0);
+            n1 = __fadd_rn(w.y, n1);
+        }
+        const float fallback = (float)(255 / K);
+        for (int k = 0; k < K; ++k) {
+            const float2 w = wt(k);
+            put(k, n0 > 0.0f ? __fdiv_rn(__fmul_rn(255.0f, w.x), n0) : fallback,
+                n1 > 0.0f ? __fdiv_rn(__fmul_rn(255.0f, w.y), n1) : fallback);
+        }
     }
 }
 
@@ -823,7 +855,7 @@ struct BatchPlan {
     int maxK = 1;
     bool pair_weights = false;  // the weights step runs k_batch_weights_pair
     struct Step {
-        int kind;  // 0 weights, 1 image reduce, 4 mask reduce, 2 coarse, 3 up
+        int kind;  // 0 weights, 5 normalisation, 1 image reduce, 4 mask reduce, 2 coarse, 3 up
         int level;
         int64_t job0, njobs;
         double bytes;
@@ -949,6 +981,15 @@ cudaError_t batch_plan_create(const std::vector<BatchStackHost>& hs, const Float
     }
     p->steps.back().njobs = (int64_t)jobs.size() - p->steps.back().job0;
     p->steps.back().bytes = b;
+    if (p->pair_weights) {
+        // the normalisation, over the weights step's tiles
+        const BatchPlan::Step w = p->steps.back();
+        double nb = 0.0;
+        for (const BatchStack& s : stacks) {
+            nb += (double)s.K * s.w * s.h * 12.0;
+        }
+        p->steps.push_back(BatchPlan::Step{5, 0, w.job0, w.njobs, nb});
+    }
     int maxL = 0;
     for (const BatchStack& s : stacks) {
         maxL = std::max(maxL, s.L);
@@ -1184,6 +1225,10 @@ static cudaError_t launch_step(const BatchPlan* p, const BatchPlan::Step& s, cud
         k<<<(unsigned)s.njobs, BWT * BWT, p->wsmem, st>>>(p->dstacks, jobs, p->wp, p->tab, p->hard, C);
         break;
     }
+    case 5:
+        note_launch("batch_normalise", s.bytes);
+        k_batch_normalise<<<(unsigned)s.njobs, 256, 0, st>>>(p->dstacks, jobs, p->hard);
+        break;
     case 1:
         note_launch("batch_reduce", s.bytes);
         k_batch_reduce<C><<<(unsigned)s.njobs, RTHREADS, 0, st>>>(p->dstacks, jobs, s.level, p->wrap);

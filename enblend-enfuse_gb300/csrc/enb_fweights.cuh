@@ -25,26 +25,31 @@ __device__ __forceinline__ float from_pyramid_value(float v)
 }
 
 // fl(fl_double(s / 3)) of a float s, the reference's (float)(s / 3.0), in
-// float arithmetic: q1 = fl(s / 3) is the correctly rounded quotient, which
-// is the result unless s / 3 lies within 2^-29 ulp of a float rounding
-// midpoint (where rounding through double could differ).  The remainder
-// s - 3 q1 is exact (fmaf) and locates s / 3 relative to q1; near a midpoint
-// the double expression decides.
+// float arithmetic.  q = s * fl(1/3) corrected once by its exact remainder
+// (fmaf) approximates s / 3 to within an ulp; the remainder r = s - 3 q of
+// the corrected q (exact) then locates s / 3 = q + r / 3 relative to q.
+// Where |s / 3 - q| lies clearly below half an ulp, q is the correctly
+// rounded quotient and no rounding through double can differ (s / 3 is no
+// float midpoint nor within 2^-29 ulp of one); everywhere else (q off by an
+// ulp, s / 3 near a midpoint, q a power of two) the double expression
+// decides.
 __device__ __forceinline__ float third_of(float s)
 {
     if (s == 0.0f) {
         return s;
     }
-    const float q1 = __fdiv_rn(s, 3.0f);
-    const float rem = __fmaf_rn(-3.0f, q1, s);  // s - 3 q1, exact
+    constexpr float kThird = 0.333333343267440796f;  // fl(1/3)
+    const float q0 = __fmul_rn(s, kThird);
+    const float q = __fmaf_rn(__fmaf_rn(-3.0f, q0, s), kThird, q0);
+    const float rem = __fmaf_rn(-3.0f, q, s);  // s - 3 q, exact
     if (rem == 0.0f) {
-        return q1;  // s / 3 is a float: every rounding gives it (white pixels: 3 / 3)
+        return q;  // s / 3 is a float: every rounding gives it (white pixels: 3 / 3)
     }
-    // s / 3 - q1 = rem / 3; a midpoint sits at +-ulp/2
-    const float ulp = fabsf(__int_as_float(__float_as_int(q1) + 1) - q1);
-    const float d = fabsf(rem) - 1.5f * ulp;  // 3 (|s/3 - q1| - ulp/2), exact or nearly
-    if (fabsf(d) > 1.0e-6f * ulp && (__float_as_int(q1) & 0x7fffff) != 0) {
-        return q1;
+    // s / 3 - q = rem / 3; a midpoint sits at +-ulp/2
+    const float ulp = fabsf(__int_as_float(__float_as_int(q) + 1) - q);
+    const float d = fabsf(rem) - 1.5f * ulp;  // 3 (|s/3 - q| - ulp/2), exact or nearly
+    if (d < -1.0e-6f * ulp && (__float_as_int(q) & 0x7fffff) != 0) {
+        return q;
     }
     return __double2float_rn((double)s / 3.0);
 }
