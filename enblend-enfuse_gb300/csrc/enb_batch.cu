@@ -493,6 +493,39 @@ __device__ __forceinline__ void stage_window(float (*ss)[ESH][ESW], const float*
     }
 }
 
+// stage_window by asynchronous 4-byte copies (zero-filled outside the level;
+// the caller commits and waits): for levels written by an earlier launch.
+template <int C>
+__device__ __forceinline__ void stage_window_async(float (*ss)[ESH][ESW], const float* src, int64_t pitch, int64_t plane,
+                                                   int sw, int sh, int I0, int J0, int wrap)
+{
+    int r = (int)threadIdx.x / ESW, c = (int)threadIdx.x - r * ESW;
+    const int dr = (int)blockDim.x / ESW, dc = (int)blockDim.x - dr * ESW;
+    for (; r < ESH;) {
+        const int jj = J0 - 1 + r;
+        int ii = I0 - 1 + c;
+        if (wrap) {
+            ii = imod(ii, sw);
+        }
+        const bool in = jj >= 0 && jj < sh && ii >= 0 && ii < sw;
+        const float* p = in ? src + (int64_t)jj * pitch + ii : src;  // a valid address where nothing is read
+        const unsigned n = in ? 4u : 0u;
+#pragma unroll
+        for (int ch = 0; ch < C; ++ch) {
+            const unsigned sa = (unsigned)__cvta_generic_to_shared(&ss[ch][r][c]);
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(p + (in ? (int64_t)ch * plane : 0)),
+                         "r"(n)
+                         : "memory");
+        }
+        c += dc;
+        r += dr;
+        if (c >= ESW) {
+            c -= ESW;
+            ++r;
+        }
+    }
+}
+
 // One 64x16 tile of level l of a stack (256 working threads, 2x2 quads):
 // C[l] = sum_k (G_k[l] - E(G_k[l+1])) m_k[l] / D + E(C[l+1]), written to
 // the result level (l >= 1) or converted into the output pixels (l == 0).
@@ -519,7 +552,15 @@ __device__ __forceinline__ void batch_up_tile(const BatchStack& s, int l, int X0
         const int64_t sp = s.pitch[l + 1], splane = sp * sh;
         for (int k = 0; k <= K; ++k) {
             const float* src = k < K ? g_level(s, k, l + 1, C) : r_level(s, l + 1, C);
-            stage_window<C>(ss + k * C, src, sp, splane, sw, sh, I0, J0, wrap);
+            if (NC) {
+                stage_window_async<C>(ss + k * C, src, sp, splane, sw, sh, I0, J0, wrap);
+            } else {
+                stage_window<C>(ss + k * C, src, sp, splane, sw, sh, I0, J0, wrap);
+            }
+        }
+        if (NC) {
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         }
     }
     __syncthreads();
@@ -668,15 +709,16 @@ __global__ void __launch_bounds__(256, 3) k_batch_up0(const BatchStack* __restri
     float* g_tile[2] = {bufs, bufs + C * ETH * ETW};
     int32_t* mask_tile[2] = {reinterpret_cast<int32_t*>(bufs + 2 * C * ETH * ETW),
                              reinterpret_cast<int32_t*>(bufs + 2 * C * ETH * ETW) + ETH * ETW};
-    up0_issue<C>(s, 0, X0, Y0, dw, dh, g_tile[0], mask_tile[0]);
-    cp_async_commit();
+    // the level-1 windows and exposure 0's tiles in one group of copies
     if (!top) {
         const int64_t sp = s.pitch[1], splane = sp * sh;
         for (int k = 0; k <= K; ++k) {
             const float* src = k < K ? g_level(s, k, 1, C) : r_level(s, 1, C);
-            stage_window<C>(ss + k * C, src, sp, splane, sw, sh, I0, J0, wrap);
+            stage_window_async<C>(ss + k * C, src, sp, splane, sw, sh, I0, J0, wrap);
         }
     }
+    up0_issue<C>(s, 0, X0, Y0, dw, dh, g_tile[0], mask_tile[0]);
+    cp_async_commit();
     const int tid = threadIdx.x;
     const int qx = tid % 32, qy = tid / 32;
     const int i = I0 + qx, j = J0 + qy;
