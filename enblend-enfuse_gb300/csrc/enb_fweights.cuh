@@ -96,14 +96,21 @@ __device__ __forceinline__ void entropy_clamp_f(const FloatWeightParams& p, floa
 
 // The built-in exposure weight functions (src/exposure_weight.h:44-128).
 // The reference forms y = gray / max in float (both operands are float) and
-// z = (y - optimum) / width in double.  Here z is carried as a float-float
-// pair zh + zl (error ~1e-14 relative), so that the functions that vanish at
-// the edge of their support (half-sine, full-sine, bisquare) keep their
-// relative accuracy there; each function is then evaluated in float with a
-// first-order correction for zl.
+// z = (y - optimum) / width in double.  The Gaussian and the Lorentzian are
+// evaluated from z in float (relative error of z a few ulps, of the weight at
+// most that times z^2 / 2, where the Gaussian has fallen to exp(-z^2 / 2)).
+// For the functions that vanish at the edge of their support (half-sine,
+// full-sine, bisquare) z is carried as a float-float pair zh + zl (error
+// ~1e-14 relative) so that they keep their relative accuracy there; each is
+// then evaluated in float with a first-order correction for zl.
 __device__ __forceinline__ float exposure_f(const FloatWeightParams& p, float gray)
 {
-    const float y = __fdiv_rn(gray, p.range);
+    const float y = p.range == 1.0f ? gray : __fdiv_rn(gray, p.range);
+    if (p.exp_function == ENB_EXP_GAUSSIAN || p.exp_function == ENB_EXP_LORENTZIAN) {
+        const float z = __fmul_rn(__fsub_rn(y, p.opt_hi), p.inv_hi);
+        const float q = __fmul_rn(__fmul_rn(0.5f, z), z);
+        return p.exp_function == ENB_EXP_GAUSSIAN ? expf(-q) : __fdiv_rn(1.0f, __fadd_rn(1.0f, q));
+    }
     // d = y - (opt_hi + opt_lo) as dh + dl: TwoSum(y, -opt_hi), then opt_lo
     const float s = __fsub_rn(y, p.opt_hi);
     const float bv = __fsub_rn(s, y);
