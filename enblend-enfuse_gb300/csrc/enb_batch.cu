@@ -691,6 +691,15 @@ __device__ __forceinline__ void up0_issue(const BatchStack& s, int k, int X0, in
     }
 }
 
+// Stages of the level-0 merge: an exposure's level-0 tile (C planes), its
+// mask tile and its level-1 window.
+constexpr int kUp0Stages = 3;
+template <int C>
+__host__ __device__ constexpr int up0_stage_floats()
+{
+    return C * ETH * ETW + ETH * ETW + C * ESH * ESW;
+}
+
 template <int C>
 __global__ void __launch_bounds__(256, 3) k_batch_up0(const BatchStack* __restrict__ stacks,
                                                      const int4* __restrict__ jobs, int wrap, float inv_d)
@@ -704,20 +713,31 @@ __global__ void __launch_bounds__(256, 3) k_batch_up0(const BatchStack* __restri
     const int dw = s.lw[0], dh = s.lh[0];
     const int sw = top ? 1 : s.lw[1], sh = top ? 1 : s.lh[1];
     const int I0 = X0 >> 1, J0 = Y0 >> 1;
-    float(*ss)[ESH][ESW] = reinterpret_cast<float(*)[ESH][ESW]>(up0smem);
-    float* bufs = up0smem + (K + 1) * C * ESH * ESW;
-    float* g_tile[2] = {bufs, bufs + C * ETH * ETW};
-    int32_t* mask_tile[2] = {reinterpret_cast<int32_t*>(bufs + 2 * C * ETH * ETW),
-                             reinterpret_cast<int32_t*>(bufs + 2 * C * ETH * ETW) + ETH * ETW};
-    // the level-1 windows and exposure 0's tiles in one group of copies
-    if (!top) {
-        const int64_t sp = s.pitch[1], splane = sp * sh;
-        for (int k = 0; k <= K; ++k) {
-            const float* src = k < K ? g_level(s, k, 1, C) : r_level(s, 1, C);
-            stage_window_async<C>(ss + k * C, src, sp, splane, sw, sh, I0, J0, wrap);
+    const int64_t sp = s.pitch[1], splane = sp * sh;
+    // stage b: [C planes of the level-0 tile][mask tile][C planes of the level-1 window];
+    // after the stages, the window of C[1]
+    const auto g_tile = [&](int b) { return up0smem + b * up0_stage_floats<C>(); };
+    const auto mask_tile = [&](int b) { return reinterpret_cast<int32_t*>(g_tile(b) + C * ETH * ETW); };
+    const auto window = [&](int b) {
+        return reinterpret_cast<float(*)[ESH][ESW]>(g_tile(b) + C * ETH * ETW + ETH * ETW);
+    };
+    float(*rwin)[ESH][ESW] = reinterpret_cast<float(*)[ESH][ESW]>(up0smem + kUp0Stages * up0_stage_floats<C>());
+    const auto issue = [&](int k) {
+        const int b = k % kUp0Stages;
+        if (!top) {
+            stage_window_async<C>(window(b), g_level(s, k, 1, C), sp, splane, sw, sh, I0, J0, wrap);
         }
+        up0_issue<C>(s, k, X0, Y0, dw, dh, g_tile(b), mask_tile(b));
+    };
+    // exposures 0 and 1 (with the window of C[1]) in flight before the first merge
+    if (!top) {
+        stage_window_async<C>(rwin, r_level(s, 1, C), sp, splane, sw, sh, I0, J0, wrap);
     }
-    up0_issue<C>(s, 0, X0, Y0, dw, dh, g_tile[0], mask_tile[0]);
+    issue(0);
+    cp_async_commit();
+    if (K > 1) {
+        issue(1);
+    }
     cp_async_commit();
     const int tid = threadIdx.x;
     const int qx = tid % 32, qy = tid / 32;
@@ -733,20 +753,21 @@ __global__ void __launch_bounds__(256, 3) k_batch_up0(const BatchStack* __restri
         }
     }
     for (int k = 0; k < K; ++k) {
-        if (k + 1 < K) {
-            up0_issue<C>(s, k + 1, X0, Y0, dw, dh, g_tile[(k + 1) & 1], mask_tile[(k + 1) & 1]);
-            cp_async_commit();
-            cp_async_wait_all_but_one();
-        } else {
-            cp_async_wait_all();
+        // the stage of exposure k + 2 was last read while merging exposure
+        // k - 1, before the previous barrier
+        if (k + 2 < K) {
+            issue(k + 2);
         }
+        cp_async_commit();
+        asm volatile("cp.async.wait_group 2;\n" ::: "memory");  // exposure k's group has landed
         __syncthreads();
         if (active) {
-            const float* gt = g_tile[k & 1];
-            const int32_t* mt = mask_tile[k & 1];
+            const int b = k % kUp0Stages;
+            const float* gt = g_tile(b);
+            const int32_t* mt = mask_tile(b);
             float e[4][C];
             if (!top) {
-                expand_quad_f<C>(ss + k * C, qx, qy, i, j, sw, sh, dw, wrap, e);
+                expand_quad_f<C>(window(b), qx, qy, i, j, sw, sh, dw, wrap, e);
             }
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
@@ -759,14 +780,14 @@ __global__ void __launch_bounds__(256, 3) k_batch_up0(const BatchStack* __restri
                 }
             }
         }
-        __syncthreads();  // the buffer is refilled two exposures on
+        __syncthreads();  // this stage is refilled for exposure k + 3
     }
     if (!active) {
         return;
     }
     float e[4][C];
     if (!top) {
-        expand_quad_f<C>(ss + K * C, qx, qy, i, j, sw, sh, dw, wrap, e);
+        expand_quad_f<C>(rwin, qx, qy, i, j, sw, sh, dw, wrap, e);
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -1301,7 +1322,7 @@ static cudaError_t launch_step(const BatchPlan* p, const BatchPlan::Step& s, cud
     default: {
         note_launch(s.level == 0 ? "batch_up0" : "batch_up", s.bytes);
         if (s.level == 0) {
-            const size_t smem = up_smem_bytes(p->maxK, C) + 2 * (size_t)ETH * ETW * (C * sizeof(float) + sizeof(int32_t));
+            const size_t smem = ((size_t)kUp0Stages * up0_stage_floats<C>() + (size_t)C * ESH * ESW) * sizeof(float);
             if (smem > 48 * 1024) {
                 cudaFuncSetAttribute(k_batch_up0<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             }
