@@ -391,7 +391,7 @@ constexpr int kBatchReduceSmem = ReduceSmem<3, true>::WORDS * 4;
 // Image jobs (kind < K) and mask jobs (kind >= K) of a level run as two
 // launches, each with the registers its path needs.
 template <int C>
-__global__ void __launch_bounds__(RTHREADS, 2) k_batch_reduce(const BatchStack* __restrict__ stacks,
+__global__ void __launch_bounds__(RTHREADS, 3) k_batch_reduce(const BatchStack* __restrict__ stacks,
                                                               const int4* __restrict__ jobs, int l, int wrap)
 {
     __shared__ __align__(16) unsigned char smem[kBatchReduceSmem];
