@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(FPT, 4) k_batch_weights_pair(const BatchStack*
     extern __shared__ __align__(16) unsigned char bsmem[];
     const int4 job = jobs[blockIdx.x];
     const BatchStack& s = stacks[job.x];
-    const FTileP t = fpair_carve(bsmem, TW, TT, wp.repeat_slots, wp.ent_cut);
+    const FTileP t0 = fpair_carve(bsmem, TW, TT, wp.repeat_slots, wp.ent_cut);
     const int px = threadIdx.x % (FPX / 2), py = threadIdx.x / (FPX / 2);
     const int x = job.y * FPX + 2 * px, y = job.z * FPY + py;
     const bool in0 = x < s.w && y < s.h, in1 = x + 1 < s.w && y < s.h;
@@ -228,15 +228,14 @@ __global__ void __launch_bounds__(FPT, 4) k_batch_weights_pair(const BatchStack*
     const int64_t plane = (int64_t)s.pitch[0] * s.h, o = (int64_t)y * s.pitch[0] + x;
     const int x0 = job.y * FPX - HX, y0 = job.z * FPY - HALO;
     uint8_t ua0 = 0, ua1 = 0;
-    if (t.slots) {
-        fpair_clear_tables<C>(t);  // published by the load's barrier
+    if (t0.slots) {
+        fpair_clear_tables<C>(fpair_for_exposure(t0, 0));
+        __syncthreads();
     }
     for (int k = 0; k < K; ++k) {
+        const FTileP t = fpair_for_exposure(t0, k);
         const int opaque = fpair_load<NP, C, TW, TT>(t, wp, s.img[k], s.ipitch[k], s.istride[k], s.w, s.h, s.alpha[k],
                                                      s.apitch[k], x0, y0);
-        if (t.slots && k + 1 < K) {
-            fpair_clear_tables<C>(t);  // the marks are in the tile
-        }
         if (in0) {
             float w0, w1;
             fpair_weights<CW, EW, C>(t, wp, tab, cx, cy, x, y, s.w, s.h, opaque != 0, w0, w1);
@@ -261,7 +260,13 @@ __global__ void __launch_bounds__(FPT, 4) k_batch_weights_pair(const BatchStack*
         }
         ua0 |= t.a[ci];
         ua1 |= t.a[ci + 1];
-        __syncthreads();  // the next exposure's load overwrites the tile
+        if (t.slots && k + 1 < K) {
+            // the tables for exposure k + 1 (the load of exposure k has ended
+            // with a barrier; exposure k - 1's row masks were read before
+            // the previous barrier)
+            fpair_clear_tables<C>(fpair_for_exposure(t0, k + 1));
+        }
+        __syncthreads();  // the next exposure's load overwrites the tile; its tables are empty
     }
     // the union alpha; k_batch_normalise turns the weights into masks
     if (in0) {

@@ -276,7 +276,8 @@ __global__ void __launch_bounds__(FPT, 4) k_f_enfuse_mask_pair(FloatPixelView im
     extern __shared__ __align__(16) unsigned char fsmem[];
     const FTileP t = fpair_carve(fsmem, TW, TT, wp.repeat_slots, wp.ent_cut);
     if (t.slots) {
-        fpair_clear_tables<C>(t);  // published by the load's barrier
+        fpair_clear_tables<C>(t);
+        __syncthreads();
     }
     const int opaque = fpair_load<NP, C, TW, TT>(t, wp, img.p, img.pitch, img.stride, img.w, img.h, alpha, apitch,
                                                  blockIdx.x * FPX - HX, blockIdx.y * FPY - HALO);

@@ -49,7 +49,8 @@ struct FTileP {
     float* raw;       // [3][TT]
     float* eraw;      // [3][TT]: the entropy cutoff's clamped samples, else raw
     uint32_t* table;     // [3][slots] repeat hash
-    uint64_t* markrow;   // [3][TH]: bit x of row y: pixel (x, y) has a repeat mark in that channel
+    uint64_t* markrow;   // [3][FPMAXROWS] of the exposure being weighted: bit x of row y: pixel (x, y)
+                         // has a repeat mark in that channel (two such buffers, by exposure parity)
     uint8_t* a;          // [TT] opaque flags
     int TW, TT, slots;
 };
@@ -59,7 +60,7 @@ constexpr int FPMAXROWS = FPY + 6;
 
 __host__ __device__ inline size_t fpair_tile_bytes(int TT, int slots, int ent_cut)
 {
-    return (size_t)TT * (8 + 4 + 12 + (ent_cut ? 12 : 0)) + (size_t)slots * 12 + (size_t)3 * FPMAXROWS * 8 +
+    return (size_t)TT * (8 + 4 + 12 + (ent_cut ? 12 : 0)) + (size_t)slots * 12 + (size_t)2 * 3 * FPMAXROWS * 8 +
            align16_sz((size_t)TT);
 }
 
@@ -97,11 +98,22 @@ __device__ __forceinline__ FTileP fpair_carve(unsigned char* smem, int TW, int T
     t.eraw = ent_cut ? t.raw + 3 * TT : t.raw;
     t.table = reinterpret_cast<uint32_t*>(t.raw + (ent_cut ? 6 : 3) * TT);
     t.markrow = reinterpret_cast<uint64_t*>(t.table + 3 * slots);
-    t.a = reinterpret_cast<uint8_t*>(t.markrow + 3 * FPMAXROWS);
+    t.a = reinterpret_cast<uint8_t*>(t.markrow + 2 * 3 * FPMAXROWS);
     return t;
 }
 
-// Empties the C hash tables of the repeat marks.
+// Tile t with the row-mask buffer of exposure k.
+__device__ __forceinline__ FTileP fpair_for_exposure(FTileP t, int k)
+{
+    t.markrow += (k & 1) * 3 * FPMAXROWS;
+    return t;
+}
+
+// Empties the C hash tables of the repeat marks and the row masks of t
+// (t.markrow: the buffer to be filled next).  The tables are used only while
+// a tile is loaded; the row masks are read while its windows are weighted,
+// so the kernels alternate two row-mask buffers and empty the one that no
+// thread reads.
 template <int C>
 __device__ __forceinline__ void fpair_clear_tables(const FTileP& t)
 {

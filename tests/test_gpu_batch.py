@@ -64,6 +64,25 @@ def test_batch_matches_plain_and_oracle(ctx, orc, hard, wrap):
         _close(got, ref["out"], 1e-4, 1e-5, f"stack {i} vs oracle")
 
 
+@pytest.mark.parametrize("levels", [16, 256])
+def test_batch_repeated_samples_bit_identical(ctx, orc, levels):
+    """Samples quantised to a few levels, so that most entropy windows of
+    every exposure hold repeated samples: the batched fuse equals the
+    per-stack path bit for bit (the same weight arithmetic, whichever
+    exposure of a tile is weighted), and the double oracle within 1e-4."""
+    stacks = [[(np.round(x * levels) / levels).astype(np.float32) for x in st]
+              for st in _batch(seed=41, shapes=[(120, 150, 5), (77, 301, 4), (260, 90, 7)])]
+    dev = [[_dev(x) for x in st] for st in stacks]
+    p = _params()
+    outs = ctx.fuse_stacks(dev, params=p)
+    plain = ctx.fuse_stacks(dev, params=p, plain=True)
+    for i, st in enumerate(stacks):
+        got = outs[i].cpu().numpy()
+        assert np.array_equal(got, plain[i].cpu().numpy()), i
+        ref = orc.enfuse_f(st, prm=orc.params(**KW), range_=1.0)
+        _close(got, ref["out"], 1e-4, 1e-5, f"stack {i} vs oracle")
+
+
 def test_batch_coarse_and_graph_bit_identical(ctx):
     stacks = _batch(seed=11)
     dev = [[_dev(x) for x in st] for st in stacks]
