@@ -490,12 +490,22 @@ __device__ __noinline__ float fpair_entropy_marked(const float* raw, const uint8
             continue;  // in the bin of an earlier marked tap
         }
         const int iy = i / W;
-        const uint32_t k = float_key(raw[(y0 + iy) * TW + x0 + i - iy * W]);
+        // a marked key is never that of 0.0 or -0.0, so the samples' bit
+        // patterns compare as their keys; with n = W * W every tap is opaque
+        const uint32_t k = __float_as_uint(raw[(y0 + iy) * TW + x0 + i - iy * W]);
+        const uint32_t* bits = reinterpret_cast<const uint32_t*>(raw);
         uint32_t same = 0;
+        if (n == M) {
 #pragma unroll
-        for (int j = 0; j < M; ++j) {
-            const int idx = (y0 + j / W) * TW + x0 + j % W;
-            same |= (a[idx] && float_key(raw[idx]) == k) ? 1u << j : 0u;
+            for (int j = 0; j < M; ++j) {
+                same |= bits[(y0 + j / W) * TW + x0 + j % W] == k ? 1u << j : 0u;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < M; ++j) {
+                const int idx = (y0 + j / W) * TW + x0 + j % W;
+                same |= (a[idx] && bits[idx] == k) ? 1u << j : 0u;
+            }
         }
         done |= same;
         const int c = __popc(same);
