@@ -1370,34 +1370,27 @@ bool same_geometry(const enb_image* a, const enb_image* b)
 }
 
 // Device address of g_noalloc_scratch on the context's device, looked up on
-// the first call per device with that device current, then cached.
-constexpr int kMaxNoAllocDevices = 128;
+// every call with that device current (cheap once the module is loaded, and
+// still right after the host application reset the device).
 std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[kMaxNoAllocDevices] = {};
 
 enb_status noalloc_scratch(enb_ctx* ctx, void** out)
 {
-    if (ctx->device < 0 || ctx->device >= kMaxNoAllocDevices) {
-        return fail(ctx, ENB_ERR_INVALID, "noalloc: device ordinal out of range");
-    }
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[ctx->device]) {
-        int cur = -1;
-        ENB_CUDA(ctx, cudaGetDevice(&cur));
-        if (cur != ctx->device) {
-            ENB_CUDA(ctx, cudaSetDevice(ctx->device));
-        }
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (cur != ctx->device) {
-            cudaSetDevice(cur);
-        }
-        if (e != cudaSuccess || !p) {
-            return cuda_fail(ctx, e == cudaSuccess ? cudaErrorInvalidSymbol : e, "cudaGetSymbolAddress(noalloc scratch)");
-        }
-        g_noalloc_ptr[ctx->device] = p;
+    int cur = -1;
+    ENB_CUDA(ctx, cudaGetDevice(&cur));
+    if (cur != ctx->device) {
+        ENB_CUDA(ctx, cudaSetDevice(ctx->device));
     }
-    *out = g_noalloc_ptr[ctx->device];
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (cur != ctx->device) {
+        cudaSetDevice(cur);
+    }
+    if (e != cudaSuccess || !p) {
+        return cuda_fail(ctx, e == cudaSuccess ? cudaErrorInvalidSymbol : e, "cudaGetSymbolAddress(noalloc scratch)");
+    }
+    *out = p;
     return ENB_OK;
 }
 
