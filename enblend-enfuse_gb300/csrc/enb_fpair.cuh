@@ -431,6 +431,20 @@ __device__ __forceinline__ void fpair_contrast(const FTileP& t, int cx, int cy, 
     sd[1] = fpair_sd(s1, q1, OPAQUE ? CW * CW : n1);
 }
 
+// fpair_contrast of windows with transparent taps (tiles at the edge of an
+// alpha mask), out of line.
+template <int CW>
+__device__ __noinline__ float2 fpair_contrast_alpha(const float* gray, const uint8_t* a, int TW, int cx, int cy, float c)
+{
+    FTileP t{};
+    t.gray = const_cast<float*>(gray);
+    t.a = const_cast<uint8_t*>(a);
+    t.TW = TW;
+    float sd[2];
+    fpair_contrast<CW, false>(t, cx, cy, c, sd);
+    return make_float2(sd[0], sd[1]);
+}
+
 // The exposure term of a pixel (as f_pixel_weight): W_exp * f(gray), or 0
 // where the exposure cutoff rejects the pixel.
 __device__ __forceinline__ float f_exposure_term(const FloatWeightParams& wp, float gray, float r, float g, float b,
@@ -583,7 +597,9 @@ __device__ __forceinline__ void fpair_weights(const FTileP& t, const FloatWeight
             if (opaque) {
                 fpair_contrast<CW, true>(t, cx, cy, c, sd);
             } else {
-                fpair_contrast<CW, false>(t, cx, cy, c, sd);
+                const float2 v = fpair_contrast_alpha<CW>(t.gray, t.a, t.TW, cx, cy, c);
+                sd[0] = v.x;
+                sd[1] = v.y;
             }
         }
         // the border strip is not written (0)

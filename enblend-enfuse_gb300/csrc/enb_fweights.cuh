@@ -33,6 +33,9 @@ __device__ __forceinline__ float from_pyramid_value(float v)
 // float midpoint nor within 2^-29 ulp of one); everywhere else (q off by an
 // ulp, s / 3 near a midpoint, q a power of two) the double expression
 // decides.
+// The double expression of third_of's rare cases, out of line.
+static __device__ __noinline__ float third_of_double(float s) { return __double2float_rn((double)s / 3.0); }
+
 __device__ __forceinline__ float third_of(float s)
 {
     if (s == 0.0f) {
@@ -51,25 +54,29 @@ __device__ __forceinline__ float third_of(float s)
     if (d < -1.0e-6f * ulp && (__float_as_int(q) & 0x7fffff) != 0) {
         return q;
     }
-    return __double2float_rn((double)s / 3.0);
+    return third_of_double(s);
 }
 
 // MultiGrayscaleAccessor on float RGB (src/mga.h:184-222).  The reference's
 // RealPromote of float is float: the average adds the samples in float and
 // divides by 3.0 in double, the lightness adds min and max in float;
 // luminance (0.3/0.59/0.11) and the channel mixer are double expressions.
+// m0 r + m1 g + m2 b in double (the luminance and channel-mixer projectors),
+// out of line: the weight kernels' common projectors stay in float.
+static __device__ __noinline__ float gray_mix_double(double m0, double m1, double m2, float r, float g, float b)
+{
+    return __double2float_rn(__dadd_rn(__dadd_rn(__dmul_rn(m0, (double)r), __dmul_rn(m1, (double)g)),
+                                       __dmul_rn(m2, (double)b)));
+}
+
 __device__ __forceinline__ float gray_proj_f(int projector, const FloatWeightParams& p, float r, float g, float b)
 {
     switch (projector) {
     case ENB_GRAY_VALUE: return fmaxf(r, fmaxf(g, b));
     case ENB_GRAY_ANTI_VALUE: return fminf(r, fminf(g, b));
     case ENB_GRAY_LIGHTNESS: return 0.5f * __fadd_rn(fminf(r, fminf(g, b)), fmaxf(r, fmaxf(g, b)));
-    case ENB_GRAY_LUMINANCE:
-        return __double2float_rn(__dadd_rn(__dadd_rn(__dmul_rn(0.3, (double)r), __dmul_rn(0.59, (double)g)),
-                                           __dmul_rn(0.11, (double)b)));
-    case ENB_GRAY_MIXER:
-        return __double2float_rn(__dadd_rn(__dadd_rn(__dmul_rn(p.mixer[0], (double)r), __dmul_rn(p.mixer[1], (double)g)),
-                                           __dmul_rn(p.mixer[2], (double)b)));
+    case ENB_GRAY_LUMINANCE: return gray_mix_double(0.3, 0.59, 0.11, r, g, b);
+    case ENB_GRAY_MIXER: return gray_mix_double(p.mixer[0], p.mixer[1], p.mixer[2], r, g, b);
     default: return third_of(__fadd_rn(__fadd_rn(r, g), b));
     }
 }
@@ -103,26 +110,22 @@ __device__ __forceinline__ void entropy_clamp_f(const FloatWeightParams& p, floa
 // full-sine, bisquare) z is carried as a float-float pair zh + zl (error
 // ~1e-14 relative) so that they keep their relative accuracy there; each is
 // then evaluated in float with a first-order correction for zl.
-__device__ __forceinline__ float exposure_f(const FloatWeightParams& p, float gray)
+// The functions that vanish at the edge of their support, from y = gray /
+// max (out of line: rare, and large with their sines).
+static __device__ __noinline__ float exposure_f_support(int fn, float y, float opt_hi, float opt_lo, float inv_hi, float inv_lo)
 {
-    const float y = p.range == 1.0f ? gray : __fdiv_rn(gray, p.range);
-    if (p.exp_function == ENB_EXP_GAUSSIAN || p.exp_function == ENB_EXP_LORENTZIAN) {
-        const float z = __fmul_rn(__fsub_rn(y, p.opt_hi), p.inv_hi);
-        const float q = __fmul_rn(__fmul_rn(0.5f, z), z);
-        return p.exp_function == ENB_EXP_GAUSSIAN ? expf(-q) : __fdiv_rn(1.0f, __fadd_rn(1.0f, q));
-    }
     // d = y - (opt_hi + opt_lo) as dh + dl: TwoSum(y, -opt_hi), then opt_lo
-    const float s = __fsub_rn(y, p.opt_hi);
+    const float s = __fsub_rn(y, opt_hi);
     const float bv = __fsub_rn(s, y);
-    const float e = __fadd_rn(__fsub_rn(y, __fsub_rn(s, bv)), __fsub_rn(-p.opt_hi, bv));
-    const float dl0 = __fsub_rn(e, p.opt_lo);
+    const float e = __fadd_rn(__fsub_rn(y, __fsub_rn(s, bv)), __fsub_rn(-opt_hi, bv));
+    const float dl0 = __fsub_rn(e, opt_lo);
     const float dh = __fadd_rn(s, dl0);
     const float dl = __fsub_rn(dl0, __fsub_rn(dh, s));
     // z = d * (inv_hi + inv_lo)
-    const float zh = __fmul_rn(dh, p.inv_hi);
-    const float zl = __fadd_rn(__fmaf_rn(dh, p.inv_hi, -zh), __fmaf_rn(dh, p.inv_lo, __fmul_rn(dl, p.inv_hi)));
+    const float zh = __fmul_rn(dh, inv_hi);
+    const float zl = __fadd_rn(__fmaf_rn(dh, inv_hi, -zh), __fmaf_rn(dh, inv_lo, __fmul_rn(dl, inv_hi)));
     const float az = fabsf(zh);
-    switch (p.exp_function) {
+    switch (fn) {
     case ENB_EXP_LORENTZIAN: return __fdiv_rn(1.0f, __fmaf_rn(0.5f * zh, zh, 1.0f));
     case ENB_EXP_HALF_SINE: {
         if (az > 1.57079632679489661923f) {
@@ -158,6 +161,18 @@ __device__ __forceinline__ float exposure_f(const FloatWeightParams& p, float gr
         return expf(-qh) * (1.0f - ql);
     }
     }
+}
+
+
+__device__ __forceinline__ float exposure_f(const FloatWeightParams& p, float gray)
+{
+    const float y = p.range == 1.0f ? gray : __fdiv_rn(gray, p.range);
+    if (p.exp_function == ENB_EXP_GAUSSIAN || p.exp_function == ENB_EXP_LORENTZIAN) {
+        const float z = __fmul_rn(__fsub_rn(y, p.opt_hi), p.inv_hi);
+        const float q = __fmul_rn(__fmul_rn(0.5f, z), z);
+        return p.exp_function == ENB_EXP_GAUSSIAN ? expf(-q) : __fdiv_rn(1.0f, __fadd_rn(1.0f, q));
+    }
+    return exposure_f_support(p.exp_function, y, p.opt_hi, p.opt_lo, p.inv_hi, p.inv_lo);
 }
 
 // Histogram::entropyOfChannel of n float keys sorted by bit pattern (equal
