@@ -374,6 +374,16 @@ __device__ __forceinline__ void fpair_row(const float* row, int cx, float (&v)[2
 }
 
 // Sample deviation from the shifted sums of n taps.
+// fpair_sd of a whole window of N taps, with the reciprocals of N and N - 1
+// as constants (their correctly rounded floats, as __frcp_rn gives them).
+template <int N>
+__device__ __forceinline__ float fpair_sd_full(float s1, float s2)
+{
+    constexpr float rn = (float)(1.0 / N), rn1 = (float)(1.0 / (N - 1));
+    const float var = __fmul_rn(__fsub_rn(s2, __fmul_rn(__fmul_rn(s1, s1), rn)), rn1);
+    return var > 0.0f ? __fsqrt_rn(var) : 0.0f;
+}
+
 __device__ __forceinline__ float fpair_sd(float s1, float s2, int n)
 {
     if (n <= 1) {
@@ -427,8 +437,14 @@ __device__ __forceinline__ void fpair_contrast(const FTileP& t, int cx, int cy, 
         n0 += n[j];
         n1 += n[j + 1];
     }
-    sd[0] = fpair_sd(s0, q0, OPAQUE ? CW * CW : n0);
-    sd[1] = fpair_sd(s1, q1, OPAQUE ? CW * CW : n1);
+    if (OPAQUE) {
+        sd[0] = fpair_sd_full<CW * CW>(s0, q0);
+        sd[1] = fpair_sd_full<CW * CW>(s1, q1);
+    } else {
+        // a window of all CW * CW taps gives the same value as fpair_sd_full
+        sd[0] = n0 == CW * CW ? fpair_sd_full<CW * CW>(s0, q0) : fpair_sd(s0, q0, n0);
+        sd[1] = n1 == CW * CW ? fpair_sd_full<CW * CW>(s1, q1) : fpair_sd(s1, q1, n1);
+    }
 }
 
 // fpair_contrast of windows with transparent taps (tiles at the edge of an
@@ -447,17 +463,22 @@ __device__ __noinline__ float2 fpair_contrast_alpha(const float* gray, const uin
 
 // The exposure term of a pixel (as f_pixel_weight): W_exp * f(gray), or 0
 // where the exposure cutoff rejects the pixel.
+// Whether an RGB pixel passes the exposure cutoff (lower projection >= lo,
+// upper projection <= hi), out of line.
+static __device__ __noinline__ bool exposure_cut_rgb(int p0, int p1, double m0, double m1, double m2, float lo,
+                                                     float hi, float r, float g, float b)
+{
+    return gray_proj_m(p0, m0, m1, m2, r, g, b) >= lo && gray_proj_m(p1, m0, m1, m2, r, g, b) <= hi;
+}
+
 __device__ __forceinline__ float f_exposure_term(const FloatWeightParams& wp, float gray, float r, float g, float b,
                                                  int C)
 {
     bool pass = true;
     if (wp.exp_cut) {
-        float lv = gray, uv = gray;
-        if (C == 3) {
-            lv = gray_proj_f(wp.cut_proj[0], wp, r, g, b);
-            uv = gray_proj_f(wp.cut_proj[1], wp, r, g, b);
-        }
-        pass = lv >= wp.cut_lo && uv <= wp.cut_hi;
+        pass = C == 3 ? exposure_cut_rgb(wp.cut_proj[0], wp.cut_proj[1], wp.mixer[0], wp.mixer[1], wp.mixer[2],
+                                         wp.cut_lo, wp.cut_hi, r, g, b)
+                      : gray >= wp.cut_lo && gray <= wp.cut_hi;
     }
     return pass ? __fmul_rn(wp.w_exposure, exposure_f(wp, gray)) : 0.0f;
 }

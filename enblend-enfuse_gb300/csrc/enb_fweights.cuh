@@ -69,16 +69,22 @@ static __device__ __noinline__ float gray_mix_double(double m0, double m1, doubl
                                        __dmul_rn(m2, (double)b)));
 }
 
-__device__ __forceinline__ float gray_proj_f(int projector, const FloatWeightParams& p, float r, float g, float b)
+// The projector with the channel-mixer weights m0..m2.
+__device__ __forceinline__ float gray_proj_m(int projector, double m0, double m1, double m2, float r, float g, float b)
 {
     switch (projector) {
     case ENB_GRAY_VALUE: return fmaxf(r, fmaxf(g, b));
     case ENB_GRAY_ANTI_VALUE: return fminf(r, fminf(g, b));
     case ENB_GRAY_LIGHTNESS: return 0.5f * __fadd_rn(fminf(r, fminf(g, b)), fmaxf(r, fmaxf(g, b)));
     case ENB_GRAY_LUMINANCE: return gray_mix_double(0.3, 0.59, 0.11, r, g, b);
-    case ENB_GRAY_MIXER: return gray_mix_double(p.mixer[0], p.mixer[1], p.mixer[2], r, g, b);
+    case ENB_GRAY_MIXER: return gray_mix_double(m0, m1, m2, r, g, b);
     default: return third_of(__fadd_rn(__fadd_rn(r, g), b));
     }
+}
+
+__device__ __forceinline__ float gray_proj_f(int projector, const FloatWeightParams& p, float r, float g, float b)
+{
+    return gray_proj_m(projector, p.mixer[0], p.mixer[1], p.mixer[2], r, g, b);
 }
 
 __device__ __forceinline__ float gray_of_f(const FloatWeightParams& p, float r, float g, float b)
