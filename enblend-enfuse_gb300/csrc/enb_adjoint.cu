@@ -315,7 +315,9 @@ __global__ void __launch_bounds__(256) k_adj_weights_bw(FloatPixelView img, cons
                                   blockIdx.x * 16 - halo, blockIdx.y * 16 - halo);
     const int lx = threadIdx.x % 16, ly = threadIdx.x / 16;
     const int x = blockIdx.x * 16 + lx, y = blockIdx.y * 16 + ly;
-    double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    // per pixel and per warp in float (a warp's sum of 32 terms: ~1e-6
+    // relative), per block and across blocks in double
+    float s[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     if (x < img.w && y < img.h) {
         const int ci = (ly + halo) * t.TW + (lx + halo);
         const float g = gw[(int64_t)y * gpitch + x];
@@ -324,9 +326,9 @@ __global__ void __launch_bounds__(256) k_adj_weights_bw(FloatPixelView img, cons
         const float yv = __fdiv_rn(gray, wp.range);
         const float z = (yv - (wp.opt_hi + wp.opt_lo)) * inv_width;
         const float df = exposure_dfdz(wp.exp_function, z);
-        s[0] = (double)g * w_exp * df * (-inv_width);
-        s[1] = (double)g * w_exp * df * (-z / width);
-        s[2] = (double)g * exposure_f(wp, gray);
+        s[0] = g * w_exp * df * (-inv_width);
+        s[1] = g * w_exp * df * (-z / width);
+        s[2] = g * exposure_f(wp, gray);
         // saturation (max_value 1.0)
         const int TT = t.TW * t.TW;
         const float r = t.raw[ci], gg = t.raw[TT + ci], b = t.raw[2 * TT + ci];
@@ -336,13 +338,13 @@ __global__ void __launch_bounds__(256) k_adj_weights_bw(FloatPixelView img, cons
             const float sum = mx + mn, diff = mx - mn;
             sat = __fdiv_rn(diff, sum <= 1.0f ? sum : (1.0f - mx) + (1.0f - mn));
         }
-        s[3] = (double)g * sat;
+        s[3] = g * sat;
         // contrast: the window's sample standard deviation (border strip 0)
         float sd = 0.0f;
         if (x >= halo && x < img.w - halo && y >= halo && y < img.h - halo) {
             sd = window_stddev<CW>(t, ci, halo, opaque != 0);
         }
-        s[4] = (double)g * sd;
+        s[4] = g * sd;
     }
     for (int i = 0; i < 5; ++i) {
         for (int off = 16; off > 0; off >>= 1) {
@@ -351,7 +353,7 @@ __global__ void __launch_bounds__(256) k_adj_weights_bw(FloatPixelView img, cons
     }
     if ((threadIdx.x & 31) == 0) {
         for (int i = 0; i < 5; ++i) {
-            part[i][threadIdx.x >> 5] = s[i];
+            part[i][threadIdx.x >> 5] = (double)s[i];
         }
     }
     __syncthreads();
