@@ -404,7 +404,7 @@ __global__ void __launch_bounds__(RTHREADS, 3) k_batch_reduce(const BatchStack* 
     batch_reduce_tile<C, true>(stacks[job.x], job.y, l, job.z * RDW, job.w * RDH, wrap, smem);
 }
 
-__global__ void __launch_bounds__(RTHREADS, 3) k_batch_reduce_mask(const BatchStack* __restrict__ stacks,
+__global__ void __launch_bounds__(RTHREADS, 4) k_batch_reduce_mask(const BatchStack* __restrict__ stacks,
                                                                    const int4* __restrict__ jobs, int l, int wrap)
 {
     __shared__ __align__(16) int32_t V[ReduceSmem<1, true>::NV][RDH][RVP];
