@@ -658,24 +658,24 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 
 // Issues the copies of exposure k's level-0 tile (C planes) and mask tile.
 template <int C>
-__device__ __forceinline__ void up0_issue(const BatchStack& s, int k, int X0, int Y0, int dw, int dh, float* g_tile,
-                                          int32_t* mask_tile)
+__device__ __forceinline__ void up0_issue(const BatchStack& s, int k, int l, int X0, int Y0, int dw, int dh,
+                                          float* g_tile, int32_t* mask_tile)
 {
     const int nx = min(ETW, dw - X0), ny = min(ETH, dh - Y0);
-    const float* g0 = g0_level(s, k, C);
-    const int64_t plane = (int64_t)s.pitch[0] * dh;
+    const float* g0 = l == 0 ? g0_level(s, k, C) : g_level(s, k, l, C);
+    const int64_t plane = (int64_t)s.pitch[l] * dh, lp = s.pitch[l];
     if (nx == ETW) {
         // whole rows: 16-byte copies (rows of the level start on 128-byte
         // boundaries and a tile on a 256-byte one)
         constexpr int Q = ETW / 4;  // chunks of a row
-        const int32_t* m = m_level(s, k, 0);
+        const int32_t* m = m_level(s, k, l);
         for (int e = threadIdx.x; e < (C + 1) * ETH * Q; e += blockDim.x) {
             const int c = e / (ETH * Q), rc = e - c * (ETH * Q), r = rc / Q, x = (rc - r * Q) * 4;
             if (r < ny) {
                 if (c < C) {
-                    cp_async16(&g_tile[(c * ETH + r) * ETW + x], &g0[c * plane + (int64_t)(Y0 + r) * s.pitch[0] + X0 + x]);
+                    cp_async16(&g_tile[(c * ETH + r) * ETW + x], &g0[c * plane + (int64_t)(Y0 + r) * lp + X0 + x]);
                 } else {
-                    cp_async16(&mask_tile[r * ETW + x], &m[(int64_t)(Y0 + r) * s.pitch[0] + X0 + x]);
+                    cp_async16(&mask_tile[r * ETW + x], &m[(int64_t)(Y0 + r) * lp + X0 + x]);
                 }
             }
         }
@@ -684,14 +684,14 @@ __device__ __forceinline__ void up0_issue(const BatchStack& s, int k, int X0, in
     for (int e = threadIdx.x; e < C * ETH * ETW; e += blockDim.x) {
         const int c = e / (ETH * ETW), rc = e - c * (ETH * ETW), r = rc / ETW, x = rc - r * ETW;
         if (r < ny && x < nx) {
-            cp_async4(&g_tile[e], &g0[c * plane + (int64_t)(Y0 + r) * s.pitch[0] + X0 + x]);
+            cp_async4(&g_tile[e], &g0[c * plane + (int64_t)(Y0 + r) * lp + X0 + x]);
         }
     }
-    const int32_t* m = m_level(s, k, 0);
+    const int32_t* m = m_level(s, k, l);
     for (int e = threadIdx.x; e < ETH * ETW; e += blockDim.x) {
         const int r = e / ETW, x = e - r * ETW;
         if (r < ny && x < nx) {
-            cp_async4(&mask_tile[e], &m[(int64_t)(Y0 + r) * s.pitch[0] + X0 + x]);
+            cp_async4(&mask_tile[e], &m[(int64_t)(Y0 + r) * lp + X0 + x]);
         }
     }
 }
@@ -705,20 +705,26 @@ __host__ __device__ constexpr int up0_stage_floats()
     return C * ETH * ETW + ETH * ETW + C * ESH * ESW;
 }
 
-template <int C>
+// Level l of a stack (one 64x16 tile, 2x2 quads): level 0 converts the
+// result into the output pixels, levels >= 1 write the result level
+// (k_batch_up's computation with the tiles streamed through the stages).
+template <int C, bool L0>
 __global__ void __launch_bounds__(256, 3) k_batch_up0(const BatchStack* __restrict__ stacks,
-                                                     const int4* __restrict__ jobs, int wrap, float inv_d)
+                                                     const int4* __restrict__ jobs, int l, int wrap, float inv_d)
 {
     extern __shared__ __align__(16) float up0smem[];
     const int4 job = jobs[blockIdx.x];
     const BatchStack& s = stacks[job.x];
+    if (L0) {
+        l = 0;
+    }
     const int K = s.K;
-    const bool top = s.L == 1;
+    const bool top = l == s.L - 1;
     const int X0 = job.y * ETW, Y0 = job.z * ETH;
-    const int dw = s.lw[0], dh = s.lh[0];
-    const int sw = top ? 1 : s.lw[1], sh = top ? 1 : s.lh[1];
+    const int dw = s.lw[l], dh = s.lh[l];
+    const int sw = top ? 1 : s.lw[l + 1], sh = top ? 1 : s.lh[l + 1];
     const int I0 = X0 >> 1, J0 = Y0 >> 1;
-    const int64_t sp = s.pitch[1], splane = sp * sh;
+    const int64_t sp = top ? 0 : s.pitch[l + 1], splane = sp * sh;
     // stage b: [C planes of the level-0 tile][mask tile][C planes of the level-1 window];
     // after the stages, the window of C[1]
     const auto g_tile = [&](int b) { return up0smem + b * up0_stage_floats<C>(); };
@@ -730,13 +736,13 @@ __global__ void __launch_bounds__(256, 3) k_batch_up0(const BatchStack* __restri
     const auto issue = [&](int k) {
         const int b = k % kUp0Stages;
         if (!top) {
-            stage_window_async<C>(window(b), g_level(s, k, 1, C), sp, splane, sw, sh, I0, J0, wrap);
+            stage_window_async<C>(window(b), g_level(s, k, l + 1, C), sp, splane, sw, sh, I0, J0, wrap);
         }
-        up0_issue<C>(s, k, X0, Y0, dw, dh, g_tile(b), mask_tile(b));
+        up0_issue<C>(s, k, l, X0, Y0, dw, dh, g_tile(b), mask_tile(b));
     };
     // exposures 0 and 1 (with the window of C[1]) in flight before the first merge
     if (!top) {
-        stage_window_async<C>(rwin, r_level(s, 1, C), sp, splane, sw, sh, I0, J0, wrap);
+        stage_window_async<C>(rwin, r_level(s, l + 1, C), sp, splane, sw, sh, I0, J0, wrap);
     }
     issue(0);
     cp_async_commit();
@@ -798,6 +804,14 @@ __global__ void __launch_bounds__(256, 3) k_batch_up0(const BatchStack* __restri
     for (int q = 0; q < 4; ++q) {
         const int XX = X + (q & 1), YY = Y + (q >> 1);
         if (XX >= dw || YY >= dh) {
+            continue;
+        }
+        if (!L0) {
+            float* r = r_level(s, l, C) + (int64_t)YY * s.pitch[l] + XX;
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                r[(int64_t)c * s.pitch[l] * dh] = acc[q][c] + (top ? 0.0f : e[q][c]);
+            }
             continue;
         }
         float* o = s.out + (int64_t)YY * s.opitch + (int64_t)XX * s.ostride;
@@ -1329,16 +1343,16 @@ static cudaError_t launch_step(const BatchPlan* p, const BatchPlan::Step& s, cud
         if (s.level == 0) {
             const size_t smem = ((size_t)kUp0Stages * up0_stage_floats<C>() + (size_t)C * ESH * ESW) * sizeof(float);
             if (smem > 48 * 1024) {
-                cudaFuncSetAttribute(k_batch_up0<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                cudaFuncSetAttribute(k_batch_up0<C, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             }
-            k_batch_up0<C><<<(unsigned)s.njobs, 256, smem, st>>>(p->dstacks, jobs, p->wrap, inv_d);
+            k_batch_up0<C, true><<<(unsigned)s.njobs, 256, smem, st>>>(p->dstacks, jobs, 0, p->wrap, inv_d);
             break;
         }
-        const size_t smem = up_smem_bytes(p->maxK, C);
+        const size_t smem = ((size_t)kUp0Stages * up0_stage_floats<C>() + (size_t)C * ESH * ESW) * sizeof(float);
         if (smem > 48 * 1024) {
-            cudaFuncSetAttribute(k_batch_up<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaFuncSetAttribute(k_batch_up0<C, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         }
-        k_batch_up<C><<<(unsigned)s.njobs, 256, smem, st>>>(p->dstacks, jobs, s.level, p->wrap, inv_d);
+        k_batch_up0<C, false><<<(unsigned)s.njobs, 256, smem, st>>>(p->dstacks, jobs, s.level, p->wrap, inv_d);
         break;
     }
     }
