@@ -16,7 +16,8 @@
 //   0.0, repeat marks) summed per column; a channel without repeat marks has
 //   only singletons besides the two clip bins, and its H is read from a
 //   table indexed by (n, m1, m0) built by the same function that evaluates
-//   such a window (entropy_clip_bins); marked channels sort their keys.
+//   such a window (entropy_clip_bins); a marked channel counts its bins
+//   exactly from its marked taps (fpair_entropy_marked).
 //
 // Each statistic is summed in one fixed order (columns top to bottom, then
 // the window's columns left to right), whichever tile, kernel or thread
