@@ -584,7 +584,7 @@ __device__ __forceinline__ void batch_up_tile(const BatchStack& s, int l, int X0
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int XX = min(X + (q & 1), dw - 1), YY = min(Y + (q >> 1), dh - 1);
-                coeff[q] = (float)ld_src<NC>(&mk[(int64_t)YY * dp + XX]) * inv_d;
+                coeff[q] = __fmul_rn((float)ld_src<NC>(&mk[(int64_t)YY * dp + XX]), inv_d);
                 if (l == 0) {
                     g[q] = __ldg(&g0_level(s, k, C)[(int64_t)c * gplane + (int64_t)YY * dp + XX]);
                 } else {
@@ -597,7 +597,8 @@ __device__ __forceinline__ void batch_up_tile(const BatchStack& s, int l, int X0
             }
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                acc[q] += (g[q] - e[q][0]) * coeff[q];
+                // rounded like the per-stack merge (k_f_mask_mul_acc)
+                acc[q] = __fadd_rn(acc[q], __fmul_rn(__fsub_rn(g[q], e[q][0]), coeff[q]));
             }
         }
         if (!top) {
@@ -605,7 +606,7 @@ __device__ __forceinline__ void batch_up_tile(const BatchStack& s, int l, int X0
             expand_quad_f<1>(ss + K * C + c, qx, qy, i, j, sw, sh, dw, wrap, e);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                acc[q] += e[q][0];
+                acc[q] = __fadd_rn(acc[q], e[q][0]);
             }
         }
 #pragma unroll
@@ -783,11 +784,12 @@ __global__ void __launch_bounds__(256, 3) k_batch_up0(const BatchStack* __restri
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int xx = min(X + (q & 1), dw - 1) - X0, yy = min(Y + (q >> 1), dh - 1) - Y0;
-                const float coeff = (float)mt[yy * ETW + xx] * inv_d;
+                const float coeff = __fmul_rn((float)mt[yy * ETW + xx], inv_d);
 #pragma unroll
                 for (int c = 0; c < C; ++c) {
                     const float g = gt[c * ETH * ETW + yy * ETW + xx];
-                    acc[q][c] += (g - (top ? 0.0f : e[q][c])) * coeff;
+                    // rounded like the per-stack merge (k_f_mask_mul_acc)
+                    acc[q][c] = __fadd_rn(acc[q][c], __fmul_rn(top ? g : __fsub_rn(g, e[q][c]), coeff));
                 }
             }
         }
@@ -810,7 +812,7 @@ __global__ void __launch_bounds__(256, 3) k_batch_up0(const BatchStack* __restri
             float* r = r_level(s, l, C) + (int64_t)YY * s.pitch[l] + XX;
 #pragma unroll
             for (int c = 0; c < C; ++c) {
-                r[(int64_t)c * s.pitch[l] * dh] = acc[q][c] + (top ? 0.0f : e[q][c]);
+                r[(int64_t)c * s.pitch[l] * dh] = top ? acc[q][c] : __fadd_rn(acc[q][c], e[q][c]);
             }
             continue;
         }
@@ -818,7 +820,7 @@ __global__ void __launch_bounds__(256, 3) k_batch_up0(const BatchStack* __restri
         const bool on = s.u[(int64_t)YY * s.pitch[0] + XX] != 0;
 #pragma unroll
         for (int c = 0; c < C; ++c) {
-            o[c] = on ? from_pyramid_value(acc[q][c] + (top ? 0.0f : e[q][c])) : 0.0f;
+            o[c] = on ? from_pyramid_value(top ? acc[q][c] : __fadd_rn(acc[q][c], e[q][c])) : 0.0f;
         }
         if (s.ostride == 4) {
             o[3] = on ? 1.0f : 0.0f;  // AlphaTraits<float>::max()

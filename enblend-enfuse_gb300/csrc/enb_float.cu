@@ -215,12 +215,14 @@ __global__ void __launch_bounds__(256) k_f_mask_mul_acc(const float* __restrict_
     if (x >= w) {
         return;
     }
-    const float coeff = (float)mask[(int64_t)y * mpitch + x] * inv_divisor;
+    // each product and sum rounded on its own (no fused multiply-add), as
+    // the batched merge rounds them
+    const float coeff = __fmul_rn((float)mask[(int64_t)y * mpitch + x], inv_divisor);
 #pragma unroll
     for (int c = 0; c < C; ++c) {
-        const float v = lp[(int64_t)c * lplane + (int64_t)y * lpitch + x] * coeff;
+        const float v = __fmul_rn(lp[(int64_t)c * lplane + (int64_t)y * lpitch + x], coeff);
         float* r = &res[(int64_t)c * rplane + (int64_t)y * rpitch + x];
-        *r = accumulate ? *r + v : v;
+        *r = accumulate ? __fadd_rn(*r, v) : v;
     }
 }
 

@@ -83,6 +83,22 @@ def test_batch_repeated_samples_bit_identical(ctx, orc, levels):
         _close(got, ref["out"], 1e-4, 1e-5, f"stack {i} vs oracle")
 
 
+def test_batch_gray_stacks_bit_identical(ctx, orc):
+    """One-channel float stacks: the batched fuse equals the per-stack path
+    bit for bit, and the double oracle within 1e-4."""
+    stacks = [[np.ascontiguousarray(x[..., 1]) for x in st]
+              for st in _batch(seed=51, shapes=[(90, 130, 4), (61, 47, 3)])]
+    dev = [[_dev(x) for x in st] for st in stacks]
+    p = _params()
+    outs = ctx.fuse_stacks(dev, params=p)
+    plain = ctx.fuse_stacks(dev, params=p, plain=True)
+    for i, st in enumerate(stacks):
+        got = outs[i].cpu().numpy()
+        assert np.array_equal(got, plain[i].cpu().numpy()), i
+        ref = orc.enfuse_f(st, prm=orc.params(**KW), range_=1.0)
+        _close(got, ref["out"], 1e-4, 1e-5, f"stack {i} vs oracle")
+
+
 def test_batch_coarse_and_graph_bit_identical(ctx):
     stacks = _batch(seed=11)
     dev = [[_dev(x) for x in st] for st in stacks]

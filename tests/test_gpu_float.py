@@ -232,6 +232,27 @@ def test_enfuse_mask_f32_repeated_samples(ctx, orc, levels, ew):
            f"weights, {levels} levels")
 
 
+@pytest.mark.parametrize("shape", [(61, 97), (40, 33, 2)])
+def test_enfuse_mask_f32_gray(ctx, orc, shape):
+    """Gray float images (one channel, alone or with an alpha sample): the
+    weight kernels' one-channel build (no saturation; contrast and entropy of
+    the one channel) against the oracle."""
+    import enbgpu
+    from enbgpu import synthetic
+    h, w = shape[:2]
+    g = synthetic.expose(synthetic.log_radiance(h, w, 8.0, seed=12), 0.5, np.float32)[..., 1]
+    g[h // 3: h // 2, : w // 2] = 1.0
+    g[: h // 4, w // 2:] = np.round(g[: h // 4, w // 2:] * 16) / 16
+    img = g if len(shape) == 2 else np.stack([g, np.ones_like(g)], axis=-1)
+    kw = dict(exposure_weight=1.0, saturation_weight=0.2, contrast_weight=0.5, entropy_weight=0.3,
+              contrast_window_size=5, entropy_window_size=5)
+    ref = orc.enfuse_mask_f(img, None, orc.params(**kw), 1.0)
+    out = torch.zeros((h, w), dtype=torch.float32, device="cuda")
+    ctx.enfuse_mask(_dev(img), None, out, enbgpu.enfuse_params(float_range=1.0, **kw))
+    _close(out.cpu().numpy().astype(np.float64), ref.astype(np.float64), WEIGHT_RTOL, 1e-7 * np.abs(ref).max(),
+           "gray weights")
+
+
 def test_enfuse_mask_f32_entropy_compat(ctx, orc):
     """The reference's float entropy weight (H * FLT_MAX) on its own."""
     import enbgpu
