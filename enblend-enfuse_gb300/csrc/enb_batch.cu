@@ -208,9 +208,11 @@ __global__ void __launch_bounds__(256, 4) k_batch_weights(const BatchStack* __re
 // pyramids, and the union alpha of a 32x16 tile of a stack, two output
 // pixels per thread (enb_fpair.cuh).  The exposures' tiles come in turn; a
 // pixel's weight waits in its exposure's level-0 mask plane (as float bits)
-// until the normalisation replaces it.
+// until the normalisation replaces it.  Five CTAs per SM (48 registers;
+// the 42.6 KB tile of 5x5 windows fits five times): the warps hide the
+// kernel's latencies better than more registers would.
 template <int CW, int EW, int C>
-__global__ void __launch_bounds__(FPT, 4) k_batch_weights_pair(const BatchStack* __restrict__ stacks,
+__global__ void __launch_bounds__(FPT, 5) k_batch_weights_pair(const BatchStack* __restrict__ stacks,
                                                             const int4* __restrict__ jobs, FloatWeightParams wp,
                                                             WeightTables tab, int hard)
 {
