@@ -631,16 +631,6 @@ __device__ __forceinline__ void batch_up_tile(const BatchStack& s, int l, int X0
     }
 }
 
-template <int C>
-__global__ void __launch_bounds__(256, 4) k_batch_up(const BatchStack* __restrict__ stacks, const int4* __restrict__ jobs,
-                                                  int l, int wrap, float inv_d)
-{
-    extern __shared__ __align__(16) float upsmem[];
-    const int4 job = jobs[blockIdx.x];
-    batch_up_tile<C, true>(stacks[job.x], l, job.y * ETW, job.z * ETH, wrap, inv_d,
-                           reinterpret_cast<float(*)[ESH][ESW]>(upsmem));
-}
-
 // Level 0 with the exposures' level-0 and mask tiles streamed through shared
 // memory: while exposure k is merged from one buffer, exposure k+1's 64x16
 // pyramid values and mask values are copied into the other (cp.async), so the
@@ -710,7 +700,7 @@ __host__ __device__ constexpr int up0_stage_floats()
 
 // Level l of a stack (one 64x16 tile, 2x2 quads): level 0 converts the
 // result into the output pixels, levels >= 1 write the result level
-// (k_batch_up's computation with the tiles streamed through the stages).
+// (batch_up_tile's computation with the tiles streamed through the stages).
 template <int C, bool L0>
 __global__ void __launch_bounds__(256, 3) k_batch_up0(const BatchStack* __restrict__ stacks,
                                                      const int4* __restrict__ jobs, int l, int wrap, float inv_d)
