@@ -536,10 +536,11 @@ __device__ __forceinline__ void stage_window_async(float (*ss)[ESH][ESW], const 
 // One 64x16 tile of level l of a stack (256 working threads, 2x2 quads):
 // C[l] = sum_k (G_k[l] - E(G_k[l+1])) m_k[l] / D + E(C[l+1]), written to
 // the result level (l >= 1) or converted into the output pixels (l == 0).
-// At the stack's top level the expand terms are absent.  NC as for the
-// reduce.  The level-(l+1) windows of all K exposures and of C[l+1] are
-// staged together (one barrier); ss holds (K + 1) * C windows.
-template <int C, bool NC>
+// At the stack's top level the expand terms are absent.  The coarse kernel
+// runs it on levels written in the same launch, so the levels >= 1 are read
+// through the coherent path.  The level-(l+1) windows of all K exposures and
+// of C[l+1] are staged together (one barrier); ss holds (K + 1) * C windows.
+template <int C>
 __device__ __forceinline__ void batch_up_tile(const BatchStack& s, int l, int X0, int Y0, int wrap, float inv_d,
                                               float (*ss)[ESH][ESW])
 {
@@ -559,15 +560,7 @@ __device__ __forceinline__ void batch_up_tile(const BatchStack& s, int l, int X0
         const int64_t sp = s.pitch[l + 1], splane = sp * sh;
         for (int k = 0; k <= K; ++k) {
             const float* src = k < K ? g_level(s, k, l + 1, C) : r_level(s, l + 1, C);
-            if (NC) {
-                stage_window_async<C>(ss + k * C, src, sp, splane, sw, sh, I0, J0, wrap);
-            } else {
-                stage_window<C>(ss + k * C, src, sp, splane, sw, sh, I0, J0, wrap);
-            }
-        }
-        if (NC) {
-            asm volatile("cp.async.commit_group;\n" ::: "memory");
-            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+            stage_window<C>(ss + k * C, src, sp, splane, sw, sh, I0, J0, wrap);
         }
     }
     __syncthreads();
@@ -586,11 +579,11 @@ __device__ __forceinline__ void batch_up_tile(const BatchStack& s, int l, int X0
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int XX = min(X + (q & 1), dw - 1), YY = min(Y + (q >> 1), dh - 1);
-                coeff[q] = __fmul_rn((float)ld_src<NC>(&mk[(int64_t)YY * dp + XX]), inv_d);
+                coeff[q] = __fmul_rn((float)ld_src<false>(&mk[(int64_t)YY * dp + XX]), inv_d);
                 if (l == 0) {
                     g[q] = __ldg(&g0_level(s, k, C)[(int64_t)c * gplane + (int64_t)YY * dp + XX]);
                 } else {
-                    g[q] = ld_src<NC>(&gk[(int64_t)YY * dp + XX]);
+                    g[q] = ld_src<false>(&gk[(int64_t)YY * dp + XX]);
                 }
             }
             float e[4][1] = {{0.0f}, {0.0f}, {0.0f}, {0.0f}};
@@ -900,7 +893,7 @@ __global__ void __launch_bounds__(RTHREADS) k_batch_coarse(const BatchStack* __r
         } else {
             float(*ss)[ESH][ESW] = reinterpret_cast<float(*)[ESH][ESW]>(smem);
             const int tx = (s.lw[ci.level] + ETW - 1) / ETW;
-            batch_up_tile<C, false>(s, ci.level, (ci.tile % tx) * ETW, (ci.tile / tx) * ETH, wrap, inv_d, ss);
+            batch_up_tile<C>(s, ci.level, (ci.tile % tx) * ETW, (ci.tile / tx) * ETH, wrap, inv_d, ss);
         }
         __syncthreads();
         if (threadIdx.x == 0) {
