@@ -220,6 +220,16 @@ def replica_value(units_per_rank: float, ws: int, steps: int, ms: float) -> floa
 # arms
 # --------------------------------------------------------------------------
 
+def workload_config(levels: int, ws: int) -> dict:
+    """The `config` of both arms' lines: the enblend workload (the reference
+    arm times a bounded sample of it, named in its cpu_baseline)."""
+    return {"workload": WORKLOAD, "levels": levels, "pixel": "RGBA u16",
+            "pyramid": "int32 17.7 fixed point, mask int32 9.15", "parallelism": f"replicas x{ws}",
+            "l2": "inputs larger than L2 (each image 171 MB)",
+            "device_layout": "rows padded to 128-byte boundaries (enbgpu.pitched), as the host-buffer "
+                             "path stages them"}
+
+
 def run_reference(args) -> None:
     ws, rank, _ = dist_setup()
     if rank != 0:
@@ -239,7 +249,7 @@ def run_reference(args) -> None:
         "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample_rows": CPU_ROWS},
+        "config": workload_config(oracle.num_levels(W + OFFSET, H), ws),
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
                          "sample": f"each step: 2 x 4096x{CPU_ROWS} RGBA u16 (a quarter of the rows)"},
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -666,11 +676,7 @@ def run_ours(args) -> None:
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "levels": enbgpu.num_levels(W + OFFSET, H), "pixel": "RGBA u16",
-                   "pyramid": "int32 17.7 fixed point, mask int32 9.15", "parallelism": f"replicas x{ws}",
-                   "l2": "inputs larger than L2 (each image 171 MB)",
-                   "device_layout": "rows padded to 128-byte boundaries (enbgpu.pitched), as the host-buffer "
-                                    "path stages them"},
+        "config": workload_config(enbgpu.num_levels(W + OFFSET, H), ws),
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_ms / e2e_steps},
         "plain_passes": {"value": UNITS / (plain_ms / 1e3), "unit": METRIC, "ms_per_step": plain_ms,
